@@ -1,0 +1,448 @@
+"""Generate the golden vectors that pin the oracle to the PulseSuite reference.
+
+Run from the repository root in a container that holds the reference source::
+
+    python tests/golden/make_golden.py /path/to/pulsesuite/src
+
+The reference is pure Python but imports ``numba`` and ``pyfftw``, neither of
+which is installed here.  This script writes two tiny stand-in packages into a
+temporary directory: ``numba.jit`` returns the function unchanged (the mode the
+reference's own ``NUMBA_DISABLE_JIT=1`` tox target uses) and
+``pyfftw.interfaces.numpy_fft`` is ``numpy.fft`` (same DFT).  Every output below
+is produced by the reference's own functions on seeded inputs; the inputs and
+outputs are stored as ``.npz`` files next to this script.
+
+Cases
+-----
+kernels_nkN     CalcH (``SBEs._CalcH_fallback``) for every flag combination and
+                dpdt/dCdt/dDdt (``SBEs._dpdt_fallback`` ...), random inputs.
+coulomb_nkN     ``coulomb.CoulombModule`` tables (V0, Chi1D, qe, qh) and
+                ``CalcScreenedArrays`` with and without screening; K0 samples.
+phonon_nkN      ``phonons.InitializePhonons`` tables and ``MBPE``/``MBPH``.
+dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
+                ``OffDiagDephasing2``.
+qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
+                and ``QW2Prop`` (cubic-spline resampling + FFTG).
+solver_step     ``SBEs.SBESolver`` built from params files, several
+                ``QWCalculator`` leapfrog steps on two wires.
+"""
+
+import io
+import os
+import sys
+import tempfile
+import contextlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_NUMBA_STUB = '''
+def jit(*a, **k):
+    if len(a) == 1 and callable(a[0]) and not k:
+        return a[0]
+    return lambda f: f
+njit = jit
+prange = range
+def float64(*a, **k):
+    return None
+class _Cuda:
+    @staticmethod
+    def is_available():
+        return False
+    @staticmethod
+    def jit(*a, **k):
+        if len(a) == 1 and callable(a[0]):
+            return a[0]
+        return lambda f: f
+cuda = _Cuda()
+'''
+
+_PYFFTW_STUB = '''
+import numpy.fft as numpy_fft
+class cache:
+    enable = staticmethod(lambda: None)
+    set_keepalive_time = staticmethod(lambda *a: None)
+'''
+
+
+def _install_stubs(tmp):
+    os.makedirs(os.path.join(tmp, "numba"))
+    os.makedirs(os.path.join(tmp, "pyfftw", "interfaces"))
+    with open(os.path.join(tmp, "numba", "__init__.py"), "w") as f:
+        f.write(_NUMBA_STUB)
+    with open(os.path.join(tmp, "pyfftw", "__init__.py"), "w") as f:
+        f.write("from . import interfaces\n")
+    with open(os.path.join(tmp, "pyfftw", "interfaces", "__init__.py"), "w") as f:
+        f.write(_PYFFTW_STUB)
+
+
+# Material used for the component cases (GaAs-like wire, Appendix values of the
+# synthetic workload): masses in me0, energies in eV.
+MAT = dict(me=0.067, mh=0.45, gap=1.52, epsr=12.9, Delta0=6e-9, HO=100e-3,
+           gam_e=1e12, gam_h=1e12, gam_eh=1e12, Oph=36e-3, Gph=3e-3)
+
+
+def herm_state(rng, n, scale):
+    z = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    q, _ = np.linalg.qr(z)
+    lam = rng.uniform(0.0, scale, n)
+    return (q * lam) @ q.conj().T
+
+
+def cnormal(rng, shape, sigma):
+    return sigma * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2.0)
+
+
+def wire_grid(nk, kabs=3e9):
+    """Half-offset k grid with |k|max = kabs; grid arrays as SBESolver builds them."""
+    from pulsesuite.PSTD3D.typespace import GetKArray, GetSpaceArray
+    from pulsesuite.PSTD3D.usefulsubs import GetArray0Index
+    dnk = (nk - 1) // 2
+    dkr = kabs / (nk - 1 - dnk - 0.5) if nk > 1 else 1.0
+    L = np.pi / dkr
+    nr = 2 * nk + 2
+    kr = np.array([dkr * (-dnk + k - 0.5) for k in range(nk)])
+    r = GetSpaceArray(nr, 2 * L)
+    Qr = GetKArray(nr, 2 * L)
+    Qr = np.roll(Qr, nr // 2)
+    Qr[0] = -Qr[0]
+    NQ0 = GetArray0Index(Qr)
+    kkp = np.zeros((nk, nk), dtype=np.int64)
+    for k in range(nk):
+        for kp in range(nk):
+            kkp[k, kp] = int(np.round((kr[k] - kr[kp]) / dkr)) + NQ0
+    return dict(nk=nk, nr=nr, dkr=dkr, L=L, kr=kr, r=r, Qr=Qr, kkp=kkp, NQ0=NQ0)
+
+
+def derived(g):
+    from scipy.constants import e as e0, hbar, m_e as me0
+    me = MAT["me"] * me0
+    mh = MAT["mh"] * me0
+    gap = MAT["gap"] * e0
+    HO = MAT["HO"] * e0
+    Ee = hbar ** 2 * g["kr"] ** 2 / (2.0 * me)
+    Eh = hbar ** 2 * g["kr"] ** 2 / (2.0 * mh)
+    dcv = np.sqrt((e0 * hbar) ** 2 / (6.0 * me0 * gap) * (me0 / me - 1.0))
+    ae = np.sqrt(me * HO) / hbar
+    ah = np.sqrt(mh * HO) / hbar
+    ehint = np.sqrt(2.0 * ae * ah / (ae ** 2 + ah ** 2))
+    area = np.sqrt(2.0 * np.pi) / np.sqrt(ae ** 2 + ah ** 2) * MAT["Delta0"]
+    return dict(me=me, mh=mh, gap=gap, Ee=Ee, Eh=Eh, dcv=dcv, alphae=ae,
+                alphah=ah, ehint=ehint, area=area)
+
+
+def case_kernels(nk, seed):
+    from pulsesuite.PSTD3D import SBEs
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    C = herm_state(rng, nk, 0.1)
+    D = herm_state(rng, nk, 0.1)
+    P = cnormal(rng, (nk, nk), 1e-3)
+    Meh = cnormal(rng, (nk, nk), 1e-22)
+    Wee = cnormal(rng, (nk, nk), 1e-22)
+    Whh = cnormal(rng, (nk, nk), 1e-22)
+    VC = rng.uniform(0.5e-21, 2e-21, (nk, nk, 3))
+    out = dict(C=C, D=D, P=P, Meh=Meh, Wee=Wee, Whh=Whh, VC=VC, Ee=d["Ee"],
+               Eh=d["Eh"], gap=d["gap"])
+    for exc in (0, 1):
+        for lf in (0, 1):
+            for fp in (0, 1):
+                Heh = np.zeros((nk, nk), complex)
+                Hee = np.zeros((nk, nk), complex)
+                Hhh = np.zeros((nk, nk), complex)
+                SBEs._CalcH_fallback(Meh, Wee, Whh, C, D, P, VC, Heh, Hee, Hhh, nk,
+                                     d["Ee"], d["Eh"], d["gap"], bool(exc), bool(lf),
+                                     bool(fp))
+                tag = f"e{exc}l{lf}f{fp}"
+                out[f"Heh_{tag}"] = Heh
+                out[f"Hee_{tag}"] = Hee
+                out[f"Hhh_{tag}"] = Hhh
+    # RHS with Hamiltonians from the full-flag CalcH and random rates
+    Heh, Hee, Hhh = out["Heh_e1l1f0"], out["Hee_e1l1f0"], out["Hhh_e1l1f0"]
+    GamE = rng.uniform(0.5e12, 2e12, nk)
+    GamH = rng.uniform(0.5e12, 2e12, nk)
+    OffP = cnormal(rng, (nk, nk), 1e-37)
+    out.update(GamE=GamE, GamH=GamH, OffP=OffP)
+    out["dP"] = SBEs._dpdt_fallback(C, D, P, Heh, Hee, Hhh, GamE, GamH, OffP)
+    out["dC"] = SBEs._dCdt_fallback(C, D, P, Heh, Hee, Hhh, GamE, GamH, OffP)
+    out["dD"] = SBEs._dDdt_fallback(C, D, P, Heh, Hee, Hhh, GamE, GamH, OffP)
+    return out
+
+
+def case_coulomb(nk, seed):
+    from pulsesuite.PSTD3D import coulomb
+    from pulsesuite.PSTD3D.usefulsubs import K03
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    cm = coulomb.CoulombModule(g["r"], g["kr"], g["L"], MAT["Delta0"], d["me"], d["mh"],
+                               d["Ee"], d["Eh"], MAT["gam_e"], MAT["gam_h"], d["alphae"],
+                               d["alphah"], MAT["epsr"], g["Qr"], g["kkp"], True)
+    out = dict(kr=g["kr"], r=g["r"], Qr=g["Qr"], kkp=g["kkp"], L=g["L"],
+               Delta0=MAT["Delta0"], me=d["me"], mh=d["mh"], alphae=d["alphae"],
+               alphah=d["alphah"], epsr=MAT["epsr"], Veh0=cm.Veh0, Vee0=cm.Vee0,
+               Vhh0=cm.Vhh0, Chi1De=cm.Chi1De, Chi1Dh=cm.Chi1Dh, qe=cm.qe, qh=cm.qh)
+    for i, (lo, hi) in enumerate(((0.0, 0.02), (0.05, 0.5))):
+        ne = rng.uniform(lo, hi, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+        nh = rng.uniform(lo, hi, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+        out[f"ne{i}"] = ne
+        out[f"nh{i}"] = nh
+        for scr in (0, 1):
+            VC = np.zeros((nk, nk, 3))
+            E1D = np.zeros((nk, nk))
+            cm.CalcScreenedArrays(bool(scr), g["L"], ne, nh, VC, E1D)
+            out[f"VC{i}_s{scr}"] = VC
+            out[f"E1D{i}_s{scr}"] = E1D
+    xs = np.concatenate([np.geomspace(1e-3, 150.0, 200), [1.0, 2.0, 9.0, 18.0, 35.0, 50.0, 99.9]])
+    out["k0_x"] = xs
+    out["k0_jit"] = np.array([coulomb._K03_jit(x) for x in xs])
+    out["k0_cik"] = np.array([K03(x) for x in xs])
+    return out
+
+
+def case_phonon(nk, temp, seed, VC, E1D):
+    from pulsesuite.PSTD3D import phonons
+    from scipy.constants import e as e0, hbar
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    phonons._Temp = temp
+    Oph = MAT["Oph"] * e0 / hbar
+    Gph = MAT["Gph"] * e0 / hbar
+    phonons.InitializePhonons(g["kr"], d["Ee"], d["Eh"], g["L"], MAT["epsr"], Gph, Oph)
+    ne = rng.uniform(0.0, 0.3, nk)
+    nh = rng.uniform(0.0, 0.3, nk)
+    WinE = rng.uniform(0, 1e11, nk)
+    WoutE = rng.uniform(0, 1e11, nk)
+    WinH = rng.uniform(0, 1e11, nk)
+    WoutH = rng.uniform(0, 1e11, nk)
+    out = dict(temp=temp, Oph=Oph, Gph=Gph, ne=ne, nh=nh, VC=VC, E1D=E1D,
+               WinE0=WinE.copy(), WoutE0=WoutE.copy(), WinH0=WinH.copy(),
+               WoutH0=WoutH.copy(), EP=phonons._EP, HP=phonons._HP,
+               Vscale=phonons._Vscale, N0=phonons._NO)
+    phonons.MBPE(ne, VC, E1D, WinE, WoutE)
+    phonons.MBPH(nh, VC, E1D, WinH, WoutH)
+    out.update(WinE=WinE, WoutE=WoutE, WinH=WinH, WoutH=WoutH)
+    fermi = phonons.FermiDistr(d["Ee"] + d["gap"] / 2.0)
+    out["fermi"] = fermi
+    phonons._Temp = 77.0
+    return out
+
+
+def case_dephasing(nk, seed, VC):
+    from pulsesuite.PSTD3D import dephasing
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    dm = dephasing.DephasingModule()
+    dm.InitializeDephasing(g["kr"], d["me"], d["mh"])
+    ne = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    nh = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    P = cnormal(rng, (nk, nk), 1e-3)
+    GamE = np.zeros(nk)
+    GamH = np.zeros(nk)
+    dm.CalcGammaE(g["kr"], ne, nh, VC, GamE)
+    dm.CalcGammaH(g["kr"], ne, nh, VC, GamH)
+    gvec = np.array([1.3e12, 0.9e12, 1.1e12])
+    x = np.zeros((nk, nk), complex)
+    dm.OffDiagDephasing2(ne, nh, P, g["kr"], d["Ee"], d["Eh"], gvec, VC, 0.0, x)
+    De = dephasing.CalcOffDiagDeph_E2(ne, nh, g["kr"], d["Ee"], d["Eh"], gvec[0], gvec[2], VC, nk)
+    Dh = dephasing.CalcOffDiagDeph_H2(ne, nh, g["kr"], d["Ee"], d["Eh"], gvec[1], gvec[2], VC, nk)
+    return dict(kr=g["kr"], me=d["me"], mh=d["mh"], Ee=d["Ee"], Eh=d["Eh"], VC=VC,
+                ne=ne, nh=nh, P=P, g=gvec, GamE=GamE, GamH=GamH, OffP=x, De=De, Dh=Dh,
+                k_p_q=dm._k_p_q, k_m_q=dm._k_m_q, k1p=dm._k1p, k1p_m_q=dm._k1p_m_q,
+                k1=dm._k1, k1_m_q=dm._k1_m_q, xe=dm._xe, xh=dm._xh)
+
+
+def case_qwoptics(nk, seed):
+    from pulsesuite.PSTD3D import qwoptics
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    qw = qwoptics.QWOptics(g["r"], g["L"], d["dcv"], g["kr"], g["Qr"], d["Ee"], d["Eh"],
+                           d["ehint"], d["area"], d["gap"])
+    nr = g["nr"]
+    P = cnormal(rng, (nk, nk), 1e-3)
+    C = herm_state(rng, nk, 0.1)
+    D = herm_state(rng, nk, 0.1)
+    out = dict(kr=g["kr"], r=g["r"], Qr=g["Qr"], kkp=g["kkp"], L=g["L"], dcv=d["dcv"],
+               ehint=d["ehint"], area=d["area"], P=P, C=C, D=D,
+               window=qw._QWWindow, Expikr=qw._Expikr)
+    for w in (1, 2, 3, 4):
+        Px = np.zeros(nr, complex)
+        Py = np.zeros(nr, complex)
+        Pz = np.zeros(nr, complex)
+        qw.QWPolarization3(g["r"], g["kr"], P, d["ehint"], d["area"], g["L"], Px, Py, Pz, 1, w)
+        out[f"Px_w{w}"] = Px
+        out[f"Py_w{w}"] = Py
+        out[f"Pz_w{w}"] = Pz
+    ne = np.abs(np.diag(C)).astype(complex)
+    nh = np.abs(np.diag(D)).astype(complex)
+    re = np.zeros(nr, complex)
+    rh = np.zeros(nr, complex)
+    qw.QWRho5(g["Qr"], g["kr"], g["r"], g["L"], g["kkp"], P, C, D, ne, nh, re, rh, 1, 1)
+    out.update(ne=ne, nh=nh, re=re, rh=rh)
+    # propagation grid covering the wire and beyond, smooth random fields
+    nrr = 3 * nr + 7
+    RR = np.linspace(-1.6 * g["L"], 1.4 * g["L"], nrr)
+    fld = {}
+    for nm in ("Exx", "Eyy", "Ezz", "Vrr"):
+        a = rng.standard_normal(4)
+        fld[nm] = (1e6 * (a[0] * np.cos(RR / g["L"] * 3.1 + a[1]) + a[2] * np.sin(RR / g["L"] * 1.7))
+                   + 1j * 1e5 * a[3] * np.cos(RR / g["L"]))
+    Ex = np.zeros(nr, complex)
+    Ey = np.zeros(nr, complex)
+    Ez = np.zeros(nr, complex)
+    Vr = np.zeros(nr, complex)
+    qw.Prop2QW(RR, fld["Exx"], fld["Eyy"], fld["Ezz"], fld["Vrr"], 0.0, g["r"], Ex, Ey, Ez, Vr, 0.0, 1)
+    out.update(RR=RR, Exx=fld["Exx"], Eyy=fld["Eyy"], Ezz=fld["Ezz"], Vrr=fld["Vrr"],
+               Ex=Ex.copy(), Ey=Ey.copy(), Ez=Ez.copy(), Vr=Vr.copy())
+    for plas in (0, 1):
+        srcs = {}
+        for nm in ("Px", "Py", "Pz", "re", "rh"):
+            srcs[nm] = cnormal(rng, nr, 1.0)
+            out[f"q2p_in_{nm}_{plas}"] = srcs[nm].copy()
+        Pxx = np.zeros(nrr, complex)
+        Pyy = np.zeros(nrr, complex)
+        Pzz = np.zeros(nrr, complex)
+        RhoE = np.zeros(nrr, complex)
+        RhoH = np.zeros(nrr, complex)
+        Exc, Eyc, Ezc, Vrc = Ex.copy(), Ey.copy(), Ez.copy(), Vr.copy()
+        qw.QW2Prop(g["r"], g["Qr"], Exc, Eyc, Ezc, Vrc, srcs["Px"], srcs["Py"], srcs["Pz"],
+                   srcs["re"], srcs["rh"], RR, Pxx, Pyy, Pzz, RhoE, RhoH, 1, 1, False, bool(plas))
+        out.update({f"q2p_Pxx_{plas}": Pxx, f"q2p_Pyy_{plas}": Pyy, f"q2p_Pzz_{plas}": Pzz,
+                    f"q2p_RhoE_{plas}": RhoE, f"q2p_RhoH_{plas}": RhoH})
+    return out
+
+
+QW_PARAMS = """{L}     # L
+6e-9      # Delta0
+1.52      # gap
+0.067     # me
+0.45      # mh
+100e-3    # HO
+1e12      # gam_e
+1e12      # gam_h
+1e12      # gam_eh
+12.9      # epsr
+36e-3     # Oph
+3e-3      # Gph
+0.0       # Edc
+100000    # jmax
+100000    # ntmax
+"""
+
+MB_PARAMS = """1 # Optics
+1 # Excitons
+0 # EHs
+1 # Screened
+1 # Phonon
+0 # DCTrans
+1 # LF
+0 # FreePot
+1 # DiagDph
+1 # OffDiagDph
+0 # Recomb
+0 # PLSpec
+0 # Ignorewire
+0 # Xqwparams
+0 # LorentzDelta
+"""
+
+
+def case_solver(L, nsteps, dt, E0, seed):
+    """Full reference leapfrog steps: SBESolver + QWCalculator on two wires."""
+    from pulsesuite.PSTD3D import SBEs
+    rng = np.random.default_rng(seed)
+    os.makedirs("params", exist_ok=True)
+    with open("params/qw.params", "w") as f:
+        f.write(QW_PARAMS.format(L=repr(L)))
+    with open("params/mb.params", "w") as f:
+        f.write(MB_PARAMS)
+    nrr = 64
+    drr = 2.5 * L / (nrr - 1)
+    rr = np.linspace(-1.25 * L, 1.25 * L, nrr)
+    qrr = np.zeros(nrr)
+    lam = 800e-9
+    s = SBEs.SBESolver(qrr, rr, 0.0, E0, lam, 2, True)
+    nk = s.Nk
+    # a non-trivial starting state so that every term of the step is exercised
+    for w in range(2):
+        for arr in (s.YY1, s.YY2, s.YY3):
+            arr[:, :, w] = cnormal(rng, (nk, nk), 1e-3)
+        for arr in (s.CC1, s.CC2, s.CC3, s.DD1, s.DD2, s.DD3):
+            arr[:, :, w] = herm_state(rng, nk, 0.05)
+    out = dict(L=L, dt=dt, E0=E0, rr=rr, nk=nk, nr=s.Nr, kr=s.kr, r=s.r, Qr=s.Qr,
+               kkp=s.kkp, dcv=s.dcv, ehint=s.ehint, area=s.area, alphae=s.alphae,
+               alphah=s.alphah)
+    init = {}
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        init[nm] = getattr(s, nm).copy()
+        out[f"init_{nm}"] = init[nm]
+    amp = rng.uniform(0.5, 1.5, (nsteps, 3, 2))
+    t = 0.0
+    for n in range(nsteps):
+        flds = []
+        for c in range(3):
+            f = (E0 * amp[n, c, 0] * np.cos(2 * np.pi * rr / (3 * L) + amp[n, c, 1])
+                 + 0j)
+            flds.append(f)
+        Exx, Eyy, Ezz = flds
+        Vrr = np.zeros(nrr, complex)
+        out[f"s{n}_Exx"] = Exx
+        out[f"s{n}_Eyy"] = Eyy
+        out[f"s{n}_Ezz"] = Ezz
+        for w in (1, 2):
+            Pxx = np.zeros(nrr, complex)
+            Pyy = np.zeros(nrr, complex)
+            Pzz = np.zeros(nrr, complex)
+            Rho = np.zeros(nrr, complex)
+            s.QWCalculator(Exx, Eyy, Ezz, Vrr, rr, qrr, dt, w, Pxx, Pyy, Pzz, Rho, [True], [False])
+            out[f"s{n}_w{w}_Pxx"] = Pxx
+            out[f"s{n}_w{w}_Pyy"] = Pyy
+            out[f"s{n}_w{w}_Pzz"] = Pzz
+            out[f"s{n}_w{w}_Rho"] = Rho
+        for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+            out[f"s{n}_{nm}"] = getattr(s, nm).copy()
+        t += dt
+    s.close()
+    return out
+
+
+def main():
+    ref_src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PULSESUITE_SRC")
+    if not ref_src or not os.path.isdir(ref_src):
+        raise SystemExit("usage: make_golden.py /path/to/pulsesuite/src")
+    with tempfile.TemporaryDirectory() as tmp:
+        _install_stubs(tmp)
+        sys.path.insert(0, tmp)
+        sys.path.insert(1, os.path.abspath(ref_src))
+        work = os.path.join(tmp, "run")
+        os.makedirs(work)
+        cwd = os.getcwd()
+        os.chdir(work)
+        sink = io.StringIO()
+        try:
+            with contextlib.redirect_stdout(sink):
+                for nk, seed in ((7, 10), (16, 11), (30, 12)):
+                    np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))
+                for nk, seed in ((8, 20), (16, 21), (30, 22)):
+                    co = case_coulomb(nk, seed)
+                    np.savez_compressed(os.path.join(HERE, f"coulomb_nk{nk}.npz"), **co)
+                    ph = case_phonon(nk, 77.0 if nk != 16 else 300.0, seed + 100, co["VC1_s1"], co["E1D1_s1"])
+                    np.savez_compressed(os.path.join(HERE, f"phonon_nk{nk}.npz"), **ph)
+                    de = case_dephasing(nk, seed + 200, co["VC1_s1"])
+                    np.savez_compressed(os.path.join(HERE, f"dephasing_nk{nk}.npz"), **de)
+                    qo = case_qwoptics(nk, seed + 300)
+                    np.savez_compressed(os.path.join(HERE, f"qwoptics_nk{nk}.npz"), **qo)
+                so = case_solver(14.5e-9, 3, 0.1e-15, 2e7, 40)
+                np.savez_compressed(os.path.join(HERE, "solver_step.npz"), **so)
+        finally:
+            os.chdir(cwd)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
