@@ -1,0 +1,161 @@
+/*
+ * sbe_gb300.h - C ABI of the GB300 quantum-wire SBE / PSTD library (libsbe_gb300.so).
+ *
+ * Conventions
+ *  - Every entry point returns int: 0 = OK, >0 = error (SBE_ERR_*); the message of
+ *    the last error on the calling thread is returned by sbe_last_error().
+ *  - All array arguments are DEVICE pointers (cudaMalloc'd or torch CUDA tensors),
+ *    contiguous, row-major, at least 16-byte aligned.  Complex numbers are
+ *    interleaved (re, im) doubles ("c128").
+ *  - A matrix of one wire is Nk x Nk row-major.  The coherence p is stored
+ *    [kh][ke] and Heh/Meh are stored [ke][kh], as in the reference.
+ *  - Calls are asynchronous on the given stream (a cudaStream_t passed as void*;
+ *    NULL = legacy default stream).  Nothing is copied to or from the host.
+ *  - No call falls back to the CPU: a missing device or a failed launch is an error.
+ *
+ * Reference interfaces replaced (rahulranjansah/pulsesuite, src/pulsesuite/PSTD3D):
+ *  each declaration cites the function it stands in for.
+ */
+#ifndef SBE_GB300_H
+#define SBE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBE_OK 0
+#define SBE_ERR_ARG 1        /* invalid argument (null pointer, size, flag) */
+#define SBE_ERR_UNSUPPORTED 2/* Nk or mode outside what the build supports     */
+#define SBE_ERR_OOM 3        /* device allocation failed                        */
+#define SBE_ERR_CUDA 4       /* a CUDA runtime/driver call failed               */
+#define SBE_ERR_TIMEOUT 5    /* a bounded device-side wait gave up              */
+
+/* Many-body flags (mb.params order, SBEs.py:5004-5022). */
+#define SBE_F_OPTICS     (1 << 0)
+#define SBE_F_EXCITONS   (1 << 1)
+#define SBE_F_EHS        (1 << 2)
+#define SBE_F_SCREENED   (1 << 3)
+#define SBE_F_PHONON     (1 << 4)
+#define SBE_F_DCTRANS    (1 << 5)
+#define SBE_F_LF         (1 << 6)
+#define SBE_F_FREEPOT    (1 << 7)
+#define SBE_F_DIAGDPH    (1 << 8)
+#define SBE_F_OFFDIAGDPH (1 << 9)
+#define SBE_F_RECOMB     (1 << 10)
+
+/* Precision of the RHS contractions. */
+#define SBE_PREC_FP64  0  /* plain FP64 SIMT (drop-in path and on-device reference) */
+#define SBE_PREC_MIXED 1  /* tcgen05 FP16 hi/lo x3, FP32 accumulate, FP64 state    */
+
+/* One wire: grid and material in SI units (qw.params, SBEs.py:4978-5002). */
+typedef struct {
+  int nk;            /* k points (even, >= 4)                                  */
+  int wire_index;    /* w (1-based) for yw(w) and (-1)^w                       */
+  int flags;         /* SBE_F_* bitmask                                        */
+  int pad0;
+  double L;          /* wire length (m); dkr = pi / L, Nr = 2 Nk + 2           */
+  double Delta0;     /* thickness (m)                                          */
+  double gap;        /* band gap (J)                                           */
+  double me, mh;     /* effective masses (kg)                                  */
+  double HO;         /* confinement level spacing (J)                          */
+  double gam_e, gam_h, gam_eh;  /* rates (1/s)                                 */
+  double epsr;       /* background dielectric constant                         */
+  double Oph, Gph;   /* LO phonon frequency and damping (rad/s)                */
+  double temp;       /* lattice temperature (K) (phonons.py:22)                */
+} SbeWireDesc;
+
+typedef struct SbeCtx SbeCtx;
+
+/* ---- library ------------------------------------------------------------- */
+const char* sbe_last_error(void);
+int sbe_version(void);
+/* Physical constants compiled into the library (CODATA 2022: hbar, e, eps0, me0, kB). */
+int sbe_constants(double* out5);
+
+/* ---- context: tables built once on the device in FP64 -------------------- */
+/* Replaces SBESolver.__init__ table set-up (SBEs.py:4623-4972): grid, kkp,
+ * CoulombModule (coulomb.py:1124-1164), InitializePhonons (phonons.py:55),
+ * InitializeDephasing (dephasing.py:472), QWOptics (qwoptics.py:575).        */
+int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out);
+int sbe_ctx_destroy(SbeCtx* ctx);
+/* Per-wire sizes/offsets (elements) of the packed state: out[3*w+0] = Nk,
+ * out[3*w+1] = offset of wire w's Nk*Nk block, out[3*w+2] = offset of its Nr block. */
+int sbe_ctx_layout(const SbeCtx* ctx, long long* out, long long* total_mat, long long* total_r);
+/* Copy one table of wire w into dst (device). which: 0 kr, 1 r, 2 Ee, 3 Eh,
+ * 4 V0 (3*Nk: eh, ee, hh by k1-k2 >= 0), 5 Chi1D (2*Nk by |k1-k2|), 6 qe/qh (2*Nk),
+ * 7 EP (Nk*Nk), 8 HP (Nk*Nk), 9 window (Nr), 10 dephasing maps (6*Nk*Nk int32),
+ * 11 xe/xh (2*Nk), 12 Expikr (c128 Nk*Nr), 13 scalars (16 doubles).          */
+int sbe_ctx_table(const SbeCtx* ctx, int w, int which, void* dst, long long nbytes, void* stream);
+
+/* ---- reference pure functions, one wire, FP64 ---------------------------- */
+/* SBEs.py:1839 dpdt (p[kh][ke]).                                               */
+int sbe_dpdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, const double* GamE, const double* GamH,
+             const double* OffP, double* out, void* stream);
+/* SBEs.py:2210 dCdt.                                                           */
+int sbe_dCdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, double* out, void* stream);
+/* SBEs.py:2502 dDdt.                                                           */
+int sbe_dDdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, double* out, void* stream);
+/* SBEs.py:658 CalcH (VC is Nk*Nk*3 real, [k1][k2][n]; only VC[q][0][n] is read). */
+int sbe_calch(int nk, const double* Meh, const double* Wee, const double* Whh, const double* C,
+              const double* D, const double* P, const double* VC, const double* Ee,
+              const double* Eh, double gap, int excitons, int lf, int freepot, double* Heh,
+              double* Hee, double* Hhh, void* stream);
+
+/* ---- per-wire building blocks of one context (FP64) ---------------------- */
+/* coulomb.py:1195 CalcScreenedArrays for wire w: VC (Nk*Nk*3) and E1D (Nk*Nk). */
+int sbe_screened_arrays(SbeCtx* ctx, int w, const double* ne, const double* nh, double* VC,
+                        double* E1D, void* stream);
+/* dephasing.py:541/584 CalcGammaE/H from VC (Nk*Nk*3).                        */
+int sbe_gamma(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
+              double* GamE, double* GamH, void* stream);
+/* dephasing.py:714 OffDiagDephasing2: x (c128 Nk*Nk); De, Dh ((2Nk+1)*Nk), g = [geh, ge, gh]. */
+int sbe_offdiag(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* P,
+                const double* VC, const double* g3, double* x, double* De, double* Dh,
+                void* stream);
+/* phonons.py:157/223 MBPE/MBPH: Win/Wout accumulated in place.                 */
+int sbe_phonon_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
+                     const double* E1D, double* WinE, double* WoutE, double* WinH,
+                     double* WoutH, void* stream);
+/* qwoptics.py:809 QWPolarization3 and 942 QWRho5 (with x 2 e0 ehint/area), real
+ * space (before FFTG): Px, Py, Pz, re, rh (c128 Nr).  ne/nh c128 Nk.         */
+int sbe_sources(SbeCtx* ctx, int w, const double* P, const double* C, const double* D,
+                const double* ne, const double* nh, double* Px, double* Py, double* Pz,
+                double* re, double* rh, void* stream);
+/* qwoptics.py:667 Prop2QW: spline from the propagation grid RR (n_rr) to the wire
+ * grid, window, real part, FFTG.  fields_in: 4 x c128 n_rr (Exx, Eyy, Ezz, Vrr);
+ * out: 4 x c128 Nr.                                                           */
+int sbe_prop2qw(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* fields_in,
+                double* out, void* stream);
+/* qwoptics.py:717 QW2Prop (real-space sources in): 5 x c128 Nr (Px, Py, Pz, re, rh)
+ * -> 5 x c128 n_rr (Pxx, Pyy, Pzz, RhoE, RhoH).                               */
+int sbe_qw2prop(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* src_in,
+                double* out, int plasmonics, void* stream);
+
+/* ---- the reference time step (leapfrog), all wires of the context -------- */
+/* SBEs.py:5612-5820 _sbe_calculator for every wire of ctx.  State: 9 buffers of
+ * packed Nk*Nk c128 blocks (YY1..3, CC1..3, DD1..3 in that order in state9[]).
+ * Ek: per wire 3 x c128 Nr field in wire k space (FFTG'd Ex, Ey, Ez).
+ * src_out: per wire 5 x c128 Nr real-space sources (Px, Py, Pz, re, rh).     */
+int sbe_leapfrog_step(SbeCtx* ctx, double* const* state9, const double* Ek, double dt,
+                      double* src_out, void* stream);
+
+/* ---- batched RK4 (the GB300 path), all wires ------------------------------- */
+/* One RK4 step of dt for every wire: state P, C, D (packed c128), field in wire
+ * k space at the step start Ek0 and its change per step dEk (both 3 x c128 Nr per
+ * wire; stage fields Ek0 + c dEk).  Relaxation, charge normalisation and the
+ * sources of the new state follow (as in the reference step).  precision:
+ * SBE_PREC_FP64 or SBE_PREC_MIXED.                                             */
+int sbe_rk4_step(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0,
+                 const double* dEk, double dt, int precision, double* src_out, void* stream);
+/* The coherent RHS of every wire at the given state/field (preparation included),
+ * for parity checks.                                                           */
+int sbe_rhs(SbeCtx* ctx, const double* P, const double* C, const double* D, const double* Ek,
+            int precision, double* dP, double* dC, double* dD, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SBE_GB300_H */

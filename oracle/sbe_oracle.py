@@ -884,6 +884,69 @@ class Wire:
                 dCdt(C, D, P, pr["Heh"], pr["Hee"], pr["Hhh"], pr["GamE"], pr["GamH"], z),
                 dDdt(C, D, P, pr["Heh"], pr["Hee"], pr["Hhh"], pr["GamE"], pr["GamH"], z), pr)
 
+    def rk4_step(self, P, C, D, Ek0, dEk, dt, w):
+        """One RK4 step of the batched GPU scheme (no reference counterpart: the
+        reference integrates with leapfrog, SBEs.py:5673-5706).
+
+        The occupation-dependent coefficients (screened VC/E1D, GamE/GamH, the
+        off-diagonal dephasing matrices De/Dh) are evaluated once from the state at
+        the start of the step and held for the four stages; each stage rebuilds
+        Meh (field Ek0 + c dEk, c = 0, 1/2, 1/2, 1), the Hartree-Fock Hamiltonians
+        and the dephasing contraction from its own state.  After the RK4 update the
+        reference's per-step relaxation and charge normalisation are applied
+        (SBEs.py:5677-5702) and the sources of the new state are formed.
+        Returns (P, C, D, Px, Py, Pz, re, rh); re/rh include x 2 e0 ehint/area.
+        """
+        f, c, g, prm = self.flags, self.c, self.g, self.p
+        nk = g["nk"]
+        ne = np.diag(C).copy()
+        nh = np.diag(D).copy()
+        VC, E1D = screened_arrays(self.ct, f["Screened"], g["L"], ne, nh)
+        GamE = np.full(nk, prm["gam_e"])
+        GamH = np.full(nk, prm["gam_h"])
+        if f["DiagDph"]:
+            GamE = gamma_e(g["kr"], ne, nh, VC, self.dt)
+            GamH = gamma_h(g["kr"], ne, nh, VC, self.dt)
+        De = Dh = None
+        if f["OffDiagDph"]:
+            gv = np.array([prm["gam_eh"], prm["gam_e"], prm["gam_h"]])
+            De = offdiag_De(ne, nh, c["Ee"], c["Eh"], gv[0], gv[2], VC)
+            Dh = offdiag_Dh(ne, nh, c["Ee"], c["Eh"], gv[1], gv[2], VC)
+        z = np.zeros((nk, nk), complex)
+
+        def f_rhs(Ps, Cs, Ds, frac):
+            Ek = [Ek0[i] + frac * dEk[i] for i in range(3)]
+            Meh = (calc_meh(Ek[0], Ek[1], Ek[2], w, g["kkp"], c["ehint"], c["dcv"])
+                   if f["Optics"] else z)
+            Heh, Hee, Hhh = calc_h(Meh, z, z, Cs, Ds, Ps, VC, c["Ee"], c["Eh"], prm["gap"],
+                                   f["Excitons"], f["LF"], False)
+            OffP = offdiag_contract(Dh, De, Ps) if De is not None else z
+            return (dpdt(Cs, Ds, Ps, Heh, Hee, Hhh, GamE, GamH, OffP),
+                    dCdt(Cs, Ds, Ps, Heh, Hee, Hhh, GamE, GamH, z),
+                    dDdt(Cs, Ds, Ps, Heh, Hee, Hhh, GamE, GamH, z))
+
+        X = (P, C, D)
+        k1 = f_rhs(*X, 0.0)
+        k2 = f_rhs(*[x + 0.5 * dt * k for x, k in zip(X, k1)], 0.5)
+        k3 = f_rhs(*[x + 0.5 * dt * k for x, k in zip(X, k2)], 0.5)
+        k4 = f_rhs(*[x + dt * k for x, k in zip(X, k3)], 1.0)
+        P, C, D = [x + dt / 6.0 * (a + 2.0 * b + 2.0 * cc + d)
+                   for x, a, b, cc, d in zip(X, k1, k2, k3, k4)]
+        if f["EHs"] or f["Phonon"]:
+            ne3, nh3 = relax(np.diag(C).copy(), np.diag(D).copy(), VC, E1D, self.pt, dt,
+                             f["EHs"], f["Phonon"])
+            C[np.diag_indices(nk)] = ne3
+            D[np.diag_indices(nk)] = nh3
+        ne3 = np.abs(np.diag(C)).astype(complex)
+        nh3 = np.abs(np.diag(D)).astype(complex)
+        total = (np.sum(np.abs(ne3)) + np.sum(np.abs(nh3))) / 2.0
+        ne3 = ne3 * total / (np.sum(np.abs(ne3)) + SMALL)
+        nh3 = nh3 * total / (np.sum(np.abs(nh3)) + SMALL)
+        C[np.diag_indices(nk)] = ne3
+        D[np.diag_indices(nk)] = nh3
+        Px, Py, Pz, re, rh = self.sources(P, C, D, ne3, nh3, w)
+        return P, C, D, Px, Py, Pz, re, rh
+
     def sources(self, p3, C3, D3, ne3, nh3, w):
         """SBEs.py:5720-5753: QWPolarization3 and QWRho5 (x 2 e0 ehint/area)."""
         g, c, f = self.g, self.c, self.flags

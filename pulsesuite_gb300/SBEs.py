@@ -1,0 +1,338 @@
+"""GB300 drop-in for ``pulsesuite.PSTD3D.SBEs`` (the quantum-wire SBE module).
+
+The names, arguments and in-place/return conventions follow the reference
+(src/pulsesuite/PSTD3D/SBEs.py):
+
+* ``dpdt``, ``dCdt``, ``dDdt`` (SBEs.py:1839, 2210, 2502) return new arrays;
+* ``CalcH`` (SBEs.py:658) fills Heh, Hee, Hhh in place;
+* ``SBESolver`` (SBEs.py:4619) with ``QWCalculator`` (SBEs.py:5826), ``chiqw``,
+  ``getqc``, ``QWArea``, ``ShutOffOptics``, ``write_sbes_data`` /
+  ``read_sbes_data`` (SBEs.py:5504-5569);
+* the module-level shims ``InitializeSBE``, ``QWCalculator``, ``chiqw``,
+  ``getqc``, ``QWArea``, ``ShutOffOptics``, ``WriteSBEsData``, ``ReadSBEsData``
+  (SBEs.py:6011-6053).
+
+Arrays may be NumPy (host; results come back as NumPy) or CUDA torch tensors
+(results stay on the device).  All arithmetic runs in libsbe_gb300 on the GPU;
+there is no CPU path.  Text diagnostics the reference appends every step
+(dataQW/info.*.t.dat, EP.*.t.dat, output/PdotE.*.dat) are not written.
+"""
+
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import C0, E0, EPS0, HBAR, KB, ME0, PI, TWOPI
+from .params import read_mb_params, read_qw_params
+from .wires import CDTYPE, WireContext, WireSpec
+
+ii = 1j
+hbar = HBAR
+eV = 1.602176634e-19
+
+
+def _to_dev(x, dtype):
+    if isinstance(x, torch.Tensor):
+        if not x.is_cuda:
+            x = x.cuda()
+        return x.to(dtype).contiguous(), True
+    a = np.ascontiguousarray(np.asarray(x))
+    return torch.from_numpy(a).to("cuda", dtype).contiguous(), False
+
+
+def _ret(t, was_torch):
+    return t if was_torch else t.cpu().numpy()
+
+
+def _rhs_call(which, C, D, p, Heh, Hee, Hhh, GamE=None, GamH=None, Off=None):
+    lib = _lib.load()
+    tC, is_t = _to_dev(C, CDTYPE)
+    tD, _ = _to_dev(D, CDTYPE)
+    tp, _ = _to_dev(p, CDTYPE)
+    th = [_to_dev(h, CDTYPE)[0] for h in (Heh, Hee, Hhh)]
+    nk = tp.shape[0]
+    out = torch.empty_like(tp)
+    s = _lib.stream_handle()
+    if which == 0:
+        ge = _to_dev(GamE, torch.float64)[0]
+        gh = _to_dev(GamH, torch.float64)[0]
+        to = _to_dev(Off, CDTYPE)[0] if Off is not None else None
+        rc = lib.sbe_dpdt(nk, _lib.ptr(tC), _lib.ptr(tD), _lib.ptr(tp), *[_lib.ptr(h) for h in th],
+                          _lib.ptr(ge), _lib.ptr(gh), _lib.ptr(to), _lib.ptr(out), s)
+    elif which == 1:
+        rc = lib.sbe_dCdt(nk, _lib.ptr(tC), _lib.ptr(tD), _lib.ptr(tp), *[_lib.ptr(h) for h in th],
+                          _lib.ptr(out), s)
+    else:
+        rc = lib.sbe_dDdt(nk, _lib.ptr(tC), _lib.ptr(tD), _lib.ptr(tp), *[_lib.ptr(h) for h in th],
+                          _lib.ptr(out), s)
+    _lib.check(rc, ("dpdt", "dCdt", "dDdt")[which])
+    return _ret(out, is_t)
+
+
+def dpdt(C, D, p, Heh, Hee, Hhh, GamE, GamH, OffP):
+    """SBEs.py:1839 dp/dt (p stored [kh][ke])."""
+    return _rhs_call(0, C, D, p, Heh, Hee, Hhh, GamE, GamH, OffP)
+
+
+def dCdt(Cee, Dhh, Phe, Heh, Hee, Hhh, GamE, GamH, OffE):
+    """SBEs.py:2210 dC/dt (GamE, GamH, OffE unused, as in the reference)."""
+    return _rhs_call(1, Cee, Dhh, Phe, Heh, Hee, Hhh)
+
+
+def dDdt(Cee, Dhh, Phe, Heh, Hee, Hhh, GamE, GamH, OffH):
+    """SBEs.py:2502 dD/dt (GamE, GamH, OffH unused, as in the reference)."""
+    return _rhs_call(2, Cee, Dhh, Phe, Heh, Hee, Hhh)
+
+
+def calc_h(Meh, Wee, Whh, C, D, p, VC, Heh, Hee, Hhh, Ee, Eh, gap, excitons, lf, freepot):
+    """SBEs.py:809-1131 CalcH with explicit grid energies and flags; outputs in place."""
+    lib = _lib.load()
+    tM, is_t = _to_dev(Meh, CDTYPE)
+    tW = _to_dev(Wee, CDTYPE)[0]
+    tWh = _to_dev(Whh, CDTYPE)[0]
+    tC = _to_dev(C, CDTYPE)[0]
+    tD = _to_dev(D, CDTYPE)[0]
+    tp = _to_dev(p, CDTYPE)[0]
+    tV = _to_dev(VC, torch.float64)[0]
+    tEe = _to_dev(Ee, torch.float64)[0]
+    tEh = _to_dev(Eh, torch.float64)[0]
+    nk = tp.shape[0]
+    o = [torch.empty_like(tp) for _ in range(3)]
+    _lib.check(lib.sbe_calch(nk, _lib.ptr(tM), _lib.ptr(tW), _lib.ptr(tWh), _lib.ptr(tC),
+                             _lib.ptr(tD), _lib.ptr(tp), _lib.ptr(tV), _lib.ptr(tEe),
+                             _lib.ptr(tEh), float(gap), int(bool(excitons)), int(bool(lf)),
+                             int(bool(freepot)), *[_lib.ptr(x) for x in o],
+                             _lib.stream_handle()), "CalcH")
+    for dst, src in zip((Heh, Hee, Hhh), o):
+        if isinstance(dst, torch.Tensor):
+            dst.copy_(src)
+        else:
+            dst[...] = src.cpu().numpy()
+
+
+def CalcH(Meh, Wee, Whh, C, D, p, VC, Heh, Hee, Hhh):
+    """SBEs.py:658 CalcH with the grid/flags of the initialised solver."""
+    s = _default_solver
+    if s is None:
+        raise RuntimeError("CalcH: call InitializeSBE first")
+    calc_h(Meh, Wee, Whh, C, D, p, VC, Heh, Hee, Hhh, s.Ee, s.Eh, s.gap, s.Excitons, s.LF,
+           s.FreePot)
+
+
+def yw(w):
+    """qwoptics.py:1093: (-1)**floor((w-1)/2)."""
+    return (-1) ** int(np.floor((w - 1) / 2.0))
+
+
+def QWChi1(lam, dky, Ee, Eh, area, geh, dcv):
+    """qwoptics.py:1109-1146: linear susceptibility of the wire (a scalar)."""
+    ww = TWOPI * C0 / lam
+    d1 = Ee + Eh - ii * HBAR * geh - HBAR * ww
+    d2 = Ee + Eh + ii * HBAR * geh + HBAR * ww
+    return 4 * dcv ** 2 / EPS0 / area * dky / TWOPI * np.sum((Ee + Eh) / (d1 * d2))
+
+
+_LEVELS = ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3")
+
+
+class SBESolver:
+    """SBEs.py:4619 SBESolver on the GPU: one device context per wire."""
+
+    def __init__(self, q, rr, r0, Emaxxx, lam, Nw, QW, backend="gb300", params=None, flags=None,
+                 nk=None, temp=77.0):
+        self.Nw = Nw
+        self.QW = QW
+        self.xxx = 1
+        self.jjj = 1
+        self.t = 0.0
+        self.wireoff = True
+        self.small = 1e-200
+        if not QW:
+            return
+        p = params if params is not None else read_qw_params()
+        f = flags if flags is not None else read_mb_params()
+        for k, v in p.items():
+            setattr(self, k, v)
+        self.flags = dict(f)
+        for k, v in f.items():
+            setattr(self, k, v)
+        self.Emax0 = Emaxxx
+        kmax = np.sqrt(1.2 * self.gap * 2.0 * self.me / (HBAR ** 2))
+        self.dkr = TWOPI / (2.0 * self.L)
+        if nk is None:
+            nk = int(np.floor(kmax / self.dkr) * 2 + 1) - 1
+        self.Nk = nk
+        self.Nr = 2 * nk + 2
+        cflags = {k: bool(f.get(k, False)) for k in _lib.FLAG_BITS}
+        self.contexts = []
+        for w in range(1, Nw + 1):
+            spec = WireSpec(nk=nk, L=self.L, Delta0=self.Delta0, gap=self.gap, me=self.me,
+                            mh=self.mh, HO=self.HO, gam_e=self.gam_e, gam_h=self.gam_h,
+                            gam_eh=self.gam_eh, epsr=self.epsr, Oph=self.Oph, Gph=self.Gph,
+                            temp=temp, wire_index=w, flags=cflags)
+            self.contexts.append(WireContext([spec]))
+        c0 = self.contexts[0]
+        self.kr = c0.table(0, "kr").cpu().numpy()
+        self.r = c0.table(0, "r").cpu().numpy()
+        self.Ee = c0.table(0, "Ee").cpu().numpy()
+        self.Eh = c0.table(0, "Eh").cpu().numpy()
+        sc = c0.table(0, "scalars").cpu().numpy()
+        self.dcv, self.alphae, self.alphah, self.ehint, self.area, self.qc = sc[:6]
+        self.dr = (self.r[2] - self.r[1]) * (self.Nr - 1) / float(self.Nr)
+        self.kkp = np.round((self.kr[:, None] - self.kr[None, :]) / self.dkr).astype(np.int64)
+        self.chiw = QWChi1(lam, self.dkr, self.Ee + self.gap, self.Eh, self.area, self.gam_eh,
+                           self.dcv)
+        # initial state (SBEs.py:4829-4849): Fermi diagonals at Ee + gap/2 (both carriers)
+        with np.errstate(over="ignore"):
+            fe = 1.0 / (np.exp((self.Ee + self.gap / 2.0) / KB / temp) + 1.0)
+        dev = torch.device("cuda")
+        self._st = []
+        for w in range(Nw):
+            lv = [torch.zeros((nk, nk), dtype=CDTYPE, device=dev) for _ in range(9)]
+            d = torch.as_tensor(fe, dtype=CDTYPE, device=dev)
+            for i in (3, 4, 5, 6, 7, 8):
+                lv[i].diagonal().copy_(d)
+            self._st.append(lv)
+        self.rr_offset = np.asarray(rr) - r0
+        self._rr_dev = None
+
+    # reference-shaped state views (Nk, Nk, Nw), copied from/to the GPU
+    def _get_level(self, i):
+        return np.stack([self._st[w][i].cpu().numpy() for w in range(self.Nw)], axis=2)
+
+    def _set_level(self, i, arr):
+        arr = np.asarray(arr)
+        for w in range(self.Nw):
+            self._st[w][i].copy_(torch.as_tensor(np.ascontiguousarray(arr[:, :, w]), dtype=CDTYPE))
+
+    def chiqw(self):
+        return self.chiw
+
+    def getqc(self):
+        return self.qc
+
+    def QWArea(self):
+        return self.area
+
+    def ShutOffOptics(self):
+        """SBEs.py:5516: disable optical coupling (rebuilds the wire contexts' flag)."""
+        self.Optics = False
+        self.flags["Optics"] = False
+        for ctx in self.contexts:
+            spec = ctx.specs[0]
+            spec.flags = dict(spec.flags, Optics=False)
+        self.contexts = [WireContext(ctx.specs) for ctx in self.contexts]
+
+    def QWCalculator(self, Exx, Eyy, Ezz, Vrr, rr, q, dt, w, Pxx, Pyy, Pzz, Rho, DoQWP, DoQWDl):
+        """SBEs.py:5826-5985: advance wire w by dt and return its sources in place."""
+        Pxx[:] = 0.0
+        Pyy[:] = 0.0
+        Pzz[:] = 0.0
+        Rho[:] = 0.0
+        if w == 1:
+            if self.jjj == self.jmax:
+                self.jjj = 0
+            self.xxx += 1
+            self.jjj += 1
+            self.t += dt
+        mag = np.max(np.sqrt(np.abs(Exx) ** 2 + np.abs(Eyy) ** 2 + np.abs(Ezz) ** 2))
+        if self.wireoff and mag < 1e-3 * self.Emax0:
+            return
+        self.wireoff = False
+        DoQWP[0] = self.Optics
+        DoQWDl[0] = self.LF
+        ctx = self.contexts[w - 1]
+        RR = torch.as_tensor(np.asarray(rr, dtype=np.float64), device="cuda")
+        f4 = torch.as_tensor(np.stack([np.asarray(a, dtype=complex) for a in (Exx, Eyy, Ezz, Vrr)]),
+                             dtype=CDTYPE, device="cuda").contiguous()
+        Ek = ctx.prop2qw(0, RR, f4)                       # (4, Nr): Ex, Ey, Ez, Vr in wire k space
+        src = torch.empty((5, self.Nr), dtype=CDTYPE, device="cuda")
+        ctx.leapfrog_step(self._st[w - 1], Ek[:3].contiguous(), dt, src)
+        out = ctx.qw2prop(0, RR, src, self.LF).cpu().numpy()
+        Pxx[:] = out[0]
+        Pyy[:] = out[1]
+        Pzz[:] = out[2]
+        Rho[:] = out[4] - out[3]
+        if getattr(self, "ignorewire", False):
+            Pxx[:] = 0.0
+            Pyy[:] = 0.0
+            Pzz[:] = 0.0
+            Rho[:] = 0.0
+
+    def write_sbes_data(self, n):
+        """SBEs.py:5524-5546: dataQW/backup/{CC,DD,YY}{1,2,3}.n.dat, 're im' per line,
+        loop order w, k2, k1."""
+        os.makedirs("dataQW/backup/", exist_ok=True)
+        for key in ("CC1", "CC2", "CC3", "DD1", "DD2", "DD3", "YY1", "YY2", "YY3"):
+            arr = getattr(self, key)
+            with open(f"dataQW/backup/{key}.{n}.dat", "w", encoding="utf-8") as f:
+                for w in range(arr.shape[2]):
+                    for k2 in range(self.Nk):
+                        for k1 in range(self.Nk):
+                            v = arr[k1, k2, w]
+                            f.write(f"{np.real(v)} {np.imag(v)}\n")
+
+    def read_sbes_data(self, Nt):
+        """SBEs.py:5548-5569: inverse of write_sbes_data."""
+        for key in ("CC1", "CC2", "CC3", "DD1", "DD2", "DD3", "YY1", "YY2", "YY3"):
+            arr = np.zeros((self.Nk, self.Nk, self.Nw), dtype=complex)
+            with open(f"dataQW/backup/{key}.{Nt}.dat", "r", encoding="utf-8") as f:
+                for w in range(self.Nw):
+                    for k2 in range(self.Nk):
+                        for k1 in range(self.Nk):
+                            a, b = f.readline().split()
+                            arr[k1, k2, w] = float(a) + 1j * float(b)
+            setattr(self, key, arr)
+
+    def close(self):
+        for c in getattr(self, "contexts", []):
+            c.close()
+
+
+def _level_prop(i):
+    return property(lambda self: self._get_level(i), lambda self, v: self._set_level(i, v))
+
+
+for _i, _n in enumerate(_LEVELS):
+    setattr(SBESolver, _n, _level_prop(_i))
+
+
+_default_solver = None
+
+
+def InitializeSBE(q, rr, r0, Emaxxx, lam, Nw, QW):
+    """SBEs.py:6011: create the default solver from ./params/*.params."""
+    global _default_solver
+    _default_solver = SBESolver(q, rr, r0, Emaxxx, lam, Nw, QW)
+
+
+def QWCalculator(Exx, Eyy, Ezz, Vrr, rr, q, dt, w, Pxx, Pyy, Pzz, Rho, DoQWP, DoQWDl):
+    """SBEs.py:6017: delegate to the default solver."""
+    _default_solver.QWCalculator(Exx, Eyy, Ezz, Vrr, rr, q, dt, w, Pxx, Pyy, Pzz, Rho, DoQWP,
+                                 DoQWDl)
+
+
+def chiqw():
+    return _default_solver.chiqw()
+
+
+def getqc():
+    return _default_solver.getqc()
+
+
+def QWArea():
+    return _default_solver.QWArea()
+
+
+def ShutOffOptics():
+    _default_solver.ShutOffOptics()
+
+
+def WriteSBEsData(n):
+    _default_solver.write_sbes_data(n)
+
+
+def ReadSBEsData(Nt):
+    _default_solver.read_sbes_data(Nt)

@@ -1,0 +1,111 @@
+"""ctypes binding of libsbe_gb300.so (the C ABI declared in include/sbe_gb300.h).
+
+The library is built in-tree by ``pulsesuite_gb300.build``.  There is no CPU
+fallback: if the shared object is missing or no CUDA device is present, every
+entry point raises.
+"""
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsbe_gb300.so")
+
+# flag bits (mb.params order)
+F_OPTICS, F_EXCITONS, F_EHS, F_SCREENED, F_PHONON, F_DCTRANS, F_LF, F_FREEPOT, F_DIAGDPH, \
+    F_OFFDIAGDPH, F_RECOMB = (1 << i for i in range(11))
+FLAG_BITS = dict(Optics=F_OPTICS, Excitons=F_EXCITONS, EHs=F_EHS, Screened=F_SCREENED,
+                 Phonon=F_PHONON, DCTrans=F_DCTRANS, LF=F_LF, FreePot=F_FREEPOT,
+                 DiagDph=F_DIAGDPH, OffDiagDph=F_OFFDIAGDPH, Recomb=F_RECOMB)
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# C-ABI exported symbols (must match include/sbe_gb300.h)
+EXPORTS = (
+    "sbe_last_error", "sbe_version", "sbe_constants", "sbe_ctx_create", "sbe_ctx_destroy",
+    "sbe_ctx_layout", "sbe_ctx_table", "sbe_dpdt", "sbe_dCdt", "sbe_dDdt", "sbe_calch",
+    "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_sources",
+    "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
+)
+
+
+class SbeWireDesc(ctypes.Structure):
+    _fields_ = [("nk", ctypes.c_int), ("wire_index", ctypes.c_int), ("flags", ctypes.c_int),
+                ("pad0", ctypes.c_int), ("L", ctypes.c_double), ("Delta0", ctypes.c_double),
+                ("gap", ctypes.c_double), ("me", ctypes.c_double), ("mh", ctypes.c_double),
+                ("HO", ctypes.c_double), ("gam_e", ctypes.c_double), ("gam_h", ctypes.c_double),
+                ("gam_eh", ctypes.c_double), ("epsr", ctypes.c_double), ("Oph", ctypes.c_double),
+                ("Gph", ctypes.c_double), ("temp", ctypes.c_double)]
+
+
+class SbeError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the shared library (no rebuild); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SbeError(f"{path} is missing: run `python -m pulsesuite_gb300.build` (needs nvcc)")
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    Dbl = ctypes.c_double
+    lib.sbe_last_error.restype = ctypes.c_char_p
+    lib.sbe_version.restype = I
+    sig = {
+        "sbe_constants": [P],
+        "sbe_ctx_create": [P, I, P, P],
+        "sbe_ctx_destroy": [P],
+        "sbe_ctx_layout": [P, P, P, P],
+        "sbe_ctx_table": [P, I, I, P, ctypes.c_longlong, P],
+        "sbe_dpdt": [I, P, P, P, P, P, P, P, P, P, P, P],
+        "sbe_dCdt": [I, P, P, P, P, P, P, P, P],
+        "sbe_dDdt": [I, P, P, P, P, P, P, P, P],
+        "sbe_calch": [I, P, P, P, P, P, P, P, P, P, Dbl, I, I, I, P, P, P, P],
+        "sbe_screened_arrays": [P, I, P, P, P, P, P],
+        "sbe_gamma": [P, I, P, P, P, P, P, P],
+        "sbe_offdiag": [P, I, P, P, P, P, P, P, P, P, P],
+        "sbe_phonon_rates": [P, I, P, P, P, P, P, P, P, P, P],
+        "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
+        "sbe_prop2qw": [P, I, P, I, P, P, P],
+        "sbe_qw2prop": [P, I, P, I, P, P, I, P],
+        "sbe_leapfrog_step": [P, P, P, Dbl, P, P],
+        "sbe_rk4_step": [P, P, P, P, P, P, Dbl, I, P, P],
+        "sbe_rhs": [P, P, P, P, P, I, P, P, P, P],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = I
+    _lib = lib
+    return lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = load().sbe_last_error().decode(errors="replace")
+        raise SbeError(f"{what} failed (code {rc}): {msg}")
+
+
+def ptr(t):
+    """Device pointer of a contiguous torch CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise SbeError("tensor argument must live on the GPU")
+    if not t.is_contiguous():
+        raise SbeError("tensor argument must be contiguous")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)

@@ -1,0 +1,591 @@
+// C ABI of libsbe_gb300: context management and the entry points declared in
+// include/sbe_gb300.h.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "sbe_ctx.cuh"
+
+namespace sbe {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return SBE_OK;
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return SBE_ERR_CUDA;
+}
+
+// Host copy of derived constants: SBEs.py:4794-4823, phonons.py:104-136.
+static WireDev derive(const SbeWireDesc& d, int nk_check_only = 0) {
+  (void)nk_check_only;
+  WireDev W{};
+  W.nk = d.nk;
+  W.nr = 2 * d.nk + 2;
+  W.flags = d.flags;
+  W.w = d.wire_index;
+  W.yw = ((int)std::floor((d.wire_index - 1) / 2.0) % 2 == 0) ? 1 : -1;
+  W.zsign = (d.wire_index % 2 == 0) ? 1 : -1;
+  W.dnk = (d.nk - 1) / 2;
+  W.L = d.L;
+  W.dkr = kTwoPi / (2.0 * d.L);
+  W.Delta0 = d.Delta0;
+  W.gap = d.gap;
+  W.me = d.me;
+  W.mh = d.mh;
+  W.HO = d.HO;
+  W.gam_e = d.gam_e;
+  W.gam_h = d.gam_h;
+  W.gam_eh = d.gam_eh;
+  W.epsr = d.epsr;
+  W.Oph = d.Oph;
+  W.Gph = d.Gph;
+  W.temp = d.temp;
+  W.dcv = std::sqrt((kE0 * kHbar) * (kE0 * kHbar) / (6.0 * kMe0 * d.gap) * (kMe0 / d.me - 1.0));
+  W.alphae = std::sqrt(d.me * d.HO) / kHbar;
+  W.alphah = std::sqrt(d.mh * d.HO) / kHbar;
+  double ae = W.alphae, ah = W.alphah;
+  W.ehint = std::sqrt(2.0 * ae * ah / (ae * ae + ah * ah));
+  W.qc = 2.0 * ae * ah / (ae + ah);
+  W.area = std::sqrt(2.0 * kPi) / std::sqrt(ae * ae + ah * ah) * d.Delta0;
+  W.vscale = kHbar * d.Oph * d.epsr * (1.0 / 8.2 - 1.0 / 10.0);
+  W.n0ph = 1.0 / (std::exp(kHbar * d.Oph / kKb / d.temp) - 1.0);
+  W.nmax = std::min(ae / 2.0, ah / 2.0) / kPi * 0.99;
+  W.pol_scale = 2.0 * W.ehint / W.area / W.L;
+  W.rho_scale = 2.0 * kE0 * W.ehint / W.area;
+  return W;
+}
+
+}  // namespace sbe
+
+using namespace sbe;
+
+extern "C" {
+
+const char* sbe_last_error(void) { return g_err.c_str(); }
+
+int sbe_version(void) { return 1; }
+
+int sbe_constants(double* out5) {
+  if (!out5) return fail(SBE_ERR_ARG, "sbe_constants: null output");
+  out5[0] = kHbar;
+  out5[1] = kE0;
+  out5[2] = kEps0;
+  out5[3] = kMe0;
+  out5[4] = kKb;
+  return SBE_OK;
+}
+
+static const int kUnsupportedFlags = SBE_F_EHS | SBE_F_DCTRANS | SBE_F_RECOMB | SBE_F_FREEPOT;
+
+int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out) {
+  if (!wires || n_wires <= 0 || !out) return fail(SBE_ERR_ARG, "sbe_ctx_create: bad arguments");
+  *out = nullptr;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    return fail(SBE_ERR_CUDA, "sbe_ctx_create: no CUDA device");
+  SbeCtx* c = new SbeCtx();
+  c->nw = n_wires;
+  c->desc.assign(wires, wires + n_wires);
+  long long om = 0, ov = 0, orr = 0, odd = 0, okr = 0;
+  for (int w = 0; w < n_wires; ++w) {
+    const SbeWireDesc& d = wires[w];
+    if (d.nk < 4 || d.nk > 4096 || !(d.L > 0) || !(d.me > 0) || !(d.mh > 0) || !(d.HO > 0) ||
+        !(d.gap > 0) || !(d.Delta0 > 0) || !(d.epsr > 0) || !(d.temp > 0) || d.wire_index < 1) {
+      delete c;
+      return fail(SBE_ERR_ARG, "sbe_ctx_create: invalid wire descriptor " + std::to_string(w));
+    }
+    if (d.flags & kUnsupportedFlags) {
+      delete c;
+      return fail(SBE_ERR_UNSUPPORTED,
+                  "sbe_ctx_create: EHs, DCTrans, Recomb and FreePot are not built (wire " +
+                      std::to_string(w) + ")");
+    }
+    WireDev W = derive(d);
+    W.off_mat = om;
+    W.off_vec = ov;
+    W.off_r = orr;
+    W.off_dd = odd;
+    W.off_kr = okr;
+    W.off_tab = w;
+    om += (long long)W.nk * W.nk;
+    ov += W.nk;
+    orr += W.nr;
+    odd += (long long)(2 * W.nk + 1) * W.nk;
+    okr += (long long)W.nk * W.nr;
+    c->nk_max = std::max(c->nk_max, W.nk);
+    c->nr_max = std::max(c->nr_max, W.nr);
+    if (d.flags & SBE_F_OFFDIAGDPH) c->any_offdiag = 1;
+    c->wires.push_back(W);
+  }
+  c->tot_mat = om;
+  c->tot_vec = ov;
+  c->tot_r = orr;
+  c->tot_dd = odd;
+  c->tot_kr = okr;
+
+  // arena layout
+  struct Part { void** p; size_t bytes; };
+  std::vector<Part> parts;
+  auto add = [&](void** p, size_t bytes) { parts.push_back({p, bytes}); };
+  const size_t D8 = 8, C16 = 16;
+  add((void**)&c->kr, D8 * ov);
+  add((void**)&c->r, D8 * orr);
+  add((void**)&c->Ee, D8 * ov);
+  add((void**)&c->Eh, D8 * ov);
+  add((void**)&c->v0, D8 * 3 * ov);
+  add((void**)&c->chi, D8 * 2 * ov);
+  add((void**)&c->qeh, D8 * 2 * ov);
+  add((void**)&c->iq, 4 * ov);
+  add((void**)&c->EP, D8 * om);
+  add((void**)&c->HP, D8 * om);
+  add((void**)&c->maps, 4 * 6 * om);
+  add((void**)&c->xeh, D8 * 2 * ov);
+  add((void**)&c->window, D8 * orr);
+  add((void**)&c->expikr, C16 * okr);
+  add((void**)&c->wk, C16 * orr);
+  add((void**)&c->vcorr, D8 * 3 * (orr + 2 * n_wires));
+  add((void**)&c->ne, C16 * ov);
+  add((void**)&c->nh, C16 * ov);
+  add((void**)&c->eps, D8 * ov);
+  add((void**)&c->vs, D8 * 3 * ov);
+  add((void**)&c->gamE, D8 * ov);
+  add((void**)&c->gamH, D8 * ov);
+  add((void**)&c->De, D8 * odd);
+  add((void**)&c->Dh, D8 * odd);
+  add((void**)&c->dA, C16 * om);
+  add((void**)&c->dB, C16 * om);
+  add((void**)&c->Heh, C16 * om);
+  add((void**)&c->Hee, C16 * om);
+  add((void**)&c->Hhh, C16 * om);
+  add((void**)&c->tr, C16 * 4 * ov);
+  add((void**)&c->dP, C16 * om);
+  add((void**)&c->dC, C16 * om);
+  add((void**)&c->dD, C16 * om);
+  add((void**)&c->wrate, D8 * 4 * ov);
+  add((void**)&c->G, C16 * 3 * okr);
+  add((void**)&c->kacc, C16 * 3 * om);
+  add((void**)&c->xs, C16 * 3 * om);
+  add((void**)&c->scal, D8 * 16 * n_wires);
+  add((void**)&c->ekst, C16 * 3 * orr);
+  size_t total = 0;
+  for (auto& p : parts) total += (p.bytes + 255) / 256 * 256;
+  if (cudaMalloc(&c->arena, total) != cudaSuccess) {
+    delete c;
+    return fail(SBE_ERR_OOM, "sbe_ctx_create: arena allocation of " + std::to_string(total) +
+                                 " bytes failed");
+  }
+  c->arena_bytes = total;
+  char* base = static_cast<char*>(c->arena);
+  size_t off = 0;
+  for (auto& p : parts) {
+    *p.p = base + off;
+    off += (p.bytes + 255) / 256 * 256;
+  }
+  cudaStream_t s = as_stream(stream);
+  cudaMemsetAsync(c->arena, 0, total, s);
+  if (cudaMalloc(&c->d_wires, sizeof(WireDev) * n_wires) != cudaSuccess) {
+    cudaFree(c->arena);
+    delete c;
+    return fail(SBE_ERR_OOM, "sbe_ctx_create: descriptor allocation failed");
+  }
+  cudaMemcpyAsync(c->d_wires, c->wires.data(), sizeof(WireDev) * n_wires, cudaMemcpyHostToDevice,
+                  s);
+  int rc = build_tables(c, s);
+  if (rc == SBE_OK) rc = cuda_check(cudaStreamSynchronize(s), "sbe_ctx_create: table build");
+  if (rc != SBE_OK) {
+    cudaFree(c->d_wires);
+    cudaFree(c->arena);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return SBE_OK;
+}
+
+int sbe_ctx_destroy(SbeCtx* c) {
+  if (!c) return SBE_OK;
+  int rc = SBE_OK;
+  if (c->d_wires && cudaFree(c->d_wires) != cudaSuccess) rc = SBE_ERR_CUDA;
+  if (c->arena && cudaFree(c->arena) != cudaSuccess) rc = SBE_ERR_CUDA;
+  sbe::mixed_free(c);
+  delete c;
+  if (rc != SBE_OK) set_error("sbe_ctx_destroy: cudaFree failed");
+  return rc;
+}
+
+int sbe_ctx_layout(const SbeCtx* c, long long* out, long long* total_mat, long long* total_r) {
+  if (!c) return fail(SBE_ERR_ARG, "sbe_ctx_layout: null context");
+  for (int w = 0; out && w < c->nw; ++w) {
+    out[3 * w + 0] = c->wires[w].nk;
+    out[3 * w + 1] = c->wires[w].off_mat;
+    out[3 * w + 2] = c->wires[w].off_r;
+  }
+  if (total_mat) *total_mat = c->tot_mat;
+  if (total_r) *total_r = c->tot_r;
+  return SBE_OK;
+}
+
+int sbe_ctx_table(const SbeCtx* c, int w, int which, void* dst, long long nbytes, void* stream) {
+  if (!c || w < 0 || w >= c->nw || !dst) return fail(SBE_ERR_ARG, "sbe_ctx_table: bad arguments");
+  const WireDev& W = c->wires[w];
+  const void* src = nullptr;
+  long long need = 0;
+  long long nk = W.nk, nr = W.nr;
+  switch (which) {
+    case 0: src = c->kr + W.off_vec; need = 8 * nk; break;
+    case 1: src = c->r + W.off_r; need = 8 * nr; break;
+    case 2: src = c->Ee + W.off_vec; need = 8 * nk; break;
+    case 3: src = c->Eh + W.off_vec; need = 8 * nk; break;
+    case 4: src = c->v0 + 3 * W.off_vec; need = 8 * 3 * nk; break;
+    case 5: src = c->chi + 2 * W.off_vec; need = 8 * 2 * nk; break;
+    case 6: src = c->qeh + 2 * W.off_vec; need = 8 * 2 * nk; break;
+    case 7: src = c->EP + W.off_mat; need = 8 * nk * nk; break;
+    case 8: src = c->HP + W.off_mat; need = 8 * nk * nk; break;
+    case 9: src = c->window + W.off_r; need = 8 * nr; break;
+    case 10: src = c->maps + 6 * W.off_mat; need = 4 * 6 * nk * nk; break;
+    case 11: src = c->xeh + 2 * W.off_vec; need = 8 * 2 * nk; break;
+    case 12: src = c->expikr + W.off_kr; need = 16 * nk * nr; break;
+    case 13: {
+      double sc[16] = {W.dcv, W.alphae, W.alphah, W.ehint, W.area, W.qc, W.vscale, W.n0ph,
+                       W.nmax, W.dkr, W.L, 0, 0, 0, 0, 0};
+      if (nbytes < (long long)sizeof(sc)) return fail(SBE_ERR_ARG, "sbe_ctx_table: buffer small");
+      return cuda_check(cudaMemcpyAsync(dst, sc, sizeof(sc), cudaMemcpyHostToDevice,
+                                        as_stream(stream)),
+                        "sbe_ctx_table");
+    }
+    case 14: src = c->wk + W.off_r; need = 16 * nr; break;
+    default: return fail(SBE_ERR_ARG, "sbe_ctx_table: unknown table");
+  }
+  if (nbytes < need) return fail(SBE_ERR_ARG, "sbe_ctx_table: destination too small");
+  return cuda_check(cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToDevice, as_stream(stream)),
+                    "sbe_ctx_table");
+}
+
+// ---- single-wire reference functions ---------------------------------------
+static int rhs_single(int which, int nk, const double* C, const double* D, const double* P,
+                      const double* Heh, const double* Hee, const double* Hhh, const double* GamE,
+                      const double* GamH, const double* OffP, double* out, void* stream) {
+  if (nk < 1 || !C || !D || !P || !Heh || !Hee || !Hhh || !out)
+    return fail(SBE_ERR_ARG, "sbe_rhs single: null pointer or bad nk");
+  const double ih = 1.0 / kHbar;
+  const double2 pos = make_double2(0.0, -ih), neg = make_double2(0.0, ih);
+  auto T = [](const void* A, int oa, const void* B, int ob, double2 al) {
+    Term t;
+    t.A = A; t.B = B; t.opA = oa; t.opB = ob; t.realA = 0; t.alpha = al;
+    return t;
+  };
+  GemmBatch b{};
+  const double2 *c2 = (const double2*)C, *d2 = (const double2*)D, *p2 = (const double2*)P;
+  const double2 *heh = (const double2*)Heh, *hee = (const double2*)Hee, *hhh = (const double2*)Hhh;
+  if (which == 0) {
+    if (!GamE || !GamH) return fail(SBE_ERR_ARG, "sbe_dpdt: null rates");
+    b.t[b.nterms++] = T(hhh, OP_N, p2, OP_N, pos);
+    b.t[b.nterms++] = T(d2, OP_T, heh, OP_T, neg);
+    b.t[b.nterms++] = T(p2, OP_N, hee, OP_T, pos);
+    b.t[b.nterms++] = T(heh, OP_T, c2, OP_N, neg);
+    b.epi = 1;
+    b.Heh = heh;
+    b.P = p2;
+    b.gamE = GamE;
+    b.gamH = GamH;
+    b.offp = (const double2*)OffP;
+  } else if (which == 1) {
+    b.t[b.nterms++] = T(c2, OP_N, hee, OP_T, pos);
+    b.t[b.nterms++] = T(hee, OP_T, c2, OP_N, neg);
+    b.t[b.nterms++] = T(p2, OP_H, heh, OP_T, pos);
+    b.t[b.nterms++] = T(heh, OP_C, p2, OP_N, neg);
+  } else {
+    b.t[b.nterms++] = T(d2, OP_N, hhh, OP_T, pos);
+    b.t[b.nterms++] = T(hhh, OP_T, d2, OP_N, neg);
+    b.t[b.nterms++] = T(p2, OP_C, heh, OP_N, pos);
+    b.t[b.nterms++] = T(heh, OP_H, p2, OP_T, neg);
+  }
+  b.out = (double2*)out;
+  launch_gemm64(nullptr, 1, nk, b, false, nk, as_stream(stream));
+  return cuda_check(cudaGetLastError(), "sbe rhs single");
+}
+
+int sbe_dpdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, const double* GamE, const double* GamH,
+             const double* OffP, double* out, void* stream) {
+  return rhs_single(0, nk, C, D, P, Heh, Hee, Hhh, GamE, GamH, OffP, out, stream);
+}
+
+int sbe_dCdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, double* out, void* stream) {
+  return rhs_single(1, nk, C, D, P, Heh, Hee, Hhh, nullptr, nullptr, nullptr, out, stream);
+}
+
+int sbe_dDdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
+             const double* Hee, const double* Hhh, double* out, void* stream) {
+  return rhs_single(2, nk, C, D, P, Heh, Hee, Hhh, nullptr, nullptr, nullptr, out, stream);
+}
+
+int sbe_calch(int nk, const double* Meh, const double* Wee, const double* Whh, const double* C,
+              const double* D, const double* P, const double* VC, const double* Ee,
+              const double* Eh, double gap, int excitons, int lf, int freepot, double* Heh,
+              double* Hee, double* Hhh, void* stream) {
+  if (nk < 1 || !Meh || !C || !D || !P || !VC || !Ee || !Eh || !Heh || !Hee || !Hhh ||
+      (freepot && (!Wee || !Whh)))
+    return fail(SBE_ERR_ARG, "sbe_calch: null pointer or bad nk");
+  return launch_calch_single(nk, (const double2*)Meh, (const double2*)Wee, (const double2*)Whh,
+                             (const double2*)C, (const double2*)D, (const double2*)P, VC, Ee, Eh,
+                             gap, excitons, lf, freepot, (double2*)Heh, (double2*)Hee,
+                             (double2*)Hhh, as_stream(stream));
+}
+
+// ---- per-wire building blocks ----------------------------------------------
+static int check_w(SbeCtx* c, int w, const char* who) {
+  if (!c || w < 0 || w >= c->nw) return fail(SBE_ERR_ARG, std::string(who) + ": bad context/wire");
+  return SBE_OK;
+}
+
+static void copy_in(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s);
+}
+
+__global__ void k_vs_from_vc(int nk, const double* VC, const double* E1D, double* vs, double* eps) {
+  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nk) return;
+  for (int n = 0; n < 3; ++n) vs[n * nk + d] = VC[((long long)d * nk + 0) * 3 + n];
+  if (E1D) eps[d] = E1D[(long long)d * nk + 0];
+}
+
+static void set_vc(SbeCtx* c, int w, const double* VC, const double* E1D, cudaStream_t s) {
+  const WireDev& W = c->wires[w];
+  k_vs_from_vc<<<(W.nk + 127) / 128, 128, 0, s>>>(W.nk, VC, E1D, c->vs + 3 * W.off_vec,
+                                                  c->eps + W.off_vec);
+}
+
+int sbe_screened_arrays(SbeCtx* c, int w, const double* ne, const double* nh, double* VC,
+                        double* E1D, void* stream) {
+  int rc = check_w(c, w, "sbe_screened_arrays");
+  if (rc) return rc;
+  if (!ne || !nh || !VC || !E1D) return fail(SBE_ERR_ARG, "sbe_screened_arrays: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  launch_screen(c, w, s);
+  launch_expand_vc(c, w, VC, E1D, s);
+  return cuda_check(cudaGetLastError(), "sbe_screened_arrays");
+}
+
+int sbe_gamma(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
+              double* GamE, double* GamH, void* stream) {
+  int rc = check_w(c, w, "sbe_gamma");
+  if (rc) return rc;
+  if (!ne || !nh || !VC || !GamE || !GamH) return fail(SBE_ERR_ARG, "sbe_gamma: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  set_vc(c, w, VC, nullptr, s);
+  launch_gamma(c, w, s);
+  copy_in(GamE, c->gamE + W.off_vec, 8 * W.nk, s);
+  copy_in(GamH, c->gamH + W.off_vec, 8 * W.nk, s);
+  return cuda_check(cudaGetLastError(), "sbe_gamma");
+}
+
+int sbe_offdiag(SbeCtx* c, int w, const double* ne, const double* nh, const double* P,
+                const double* VC, const double* g3, double* x, double* De, double* Dh,
+                void* stream) {
+  int rc = check_w(c, w, "sbe_offdiag");
+  if (rc) return rc;
+  if (!ne || !nh || !P || !VC || !g3 || !x) return fail(SBE_ERR_ARG, "sbe_offdiag: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  double g[3];
+  cudaMemcpyAsync(g, g3, sizeof(g), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  set_vc(c, w, VC, nullptr, s);
+  launch_offdiag_D(c, w, g, false, s);
+  launch_offdiag_AB(c, w, s);
+  copy_in(c->xs + W.off_mat, P, 16 * (size_t)W.nk * W.nk, s);
+  const double2 ihb = make_double2(0.0, kHbar);
+  GemmBatch b{};
+  b.w_only = w;
+  b.t[0] = Term{c->dA, c->xs, OP_N, OP_N, 0, ihb};
+  b.t[1] = Term{c->xs, c->dB, OP_N, OP_T, 0, ihb};
+  b.nterms = 2;
+  b.out = c->dP;
+  b.epi = 0;
+  launch_gemm64(c->d_wires, c->nw, c->nk_max, b, true, 0, s);
+  copy_in(x, c->dP + W.off_mat, 16 * (size_t)W.nk * W.nk, s);
+  size_t ddb = 8 * (size_t)(2 * W.nk + 1) * W.nk;
+  if (De) copy_in(De, c->De + W.off_dd, ddb, s);
+  if (Dh) copy_in(Dh, c->Dh + W.off_dd, ddb, s);
+  return cuda_check(cudaGetLastError(), "sbe_offdiag");
+}
+
+int sbe_phonon_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
+                     const double* E1D, double* WinE, double* WoutE, double* WinH, double* WoutH,
+                     void* stream) {
+  int rc = check_w(c, w, "sbe_phonon_rates");
+  if (rc) return rc;
+  if (!ne || !nh || !VC || !E1D || !WinE || !WoutE || !WinH || !WoutH)
+    return fail(SBE_ERR_ARG, "sbe_phonon_rates: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  set_vc(c, w, VC, E1D, s);
+  launch_phonon_rates_one(c, w, s);
+  // accumulate into the caller's arrays (MBPE/MBPH add to Win/Wout)
+  sbe::add_rates(c->wrate + 4 * W.off_vec, W.nk, WinE, WoutE, WinH, WoutH, s);
+  return cuda_check(cudaGetLastError(), "sbe_phonon_rates");
+}
+
+int sbe_sources(SbeCtx* c, int w, const double* P, const double* C, const double* D,
+                const double* ne, const double* nh, double* Px, double* Py, double* Pz,
+                double* re, double* rh, void* stream) {
+  int rc = check_w(c, w, "sbe_sources");
+  if (rc) return rc;
+  if (!P || !C || !D || !ne || !nh || !Px || !Py || !Pz || !re || !rh)
+    return fail(SBE_ERR_ARG, "sbe_sources: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  size_t mb = 16 * (size_t)W.nk * W.nk;
+  long long n = c->tot_mat;
+  copy_in(c->xs + W.off_mat, P, mb, s);
+  copy_in(c->xs + n + W.off_mat, C, mb, s);
+  copy_in(c->xs + 2 * n + W.off_mat, D, mb, s);
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  double2* src = c->G + 0;  // scratch is the tail of kacc: 5*tot_r <= 3*tot_mat
+  src = c->kacc;
+  launch_sources(c, c->xs, c->xs + n, c->xs + 2 * n, c->ne, c->nh, src, s, w);
+  size_t rb = 16 * (size_t)W.nr;
+  const double2* o = src + 5 * W.off_r;
+  copy_in(Px, o, rb, s);
+  copy_in(Py, o + W.nr, rb, s);
+  copy_in(Pz, o + 2 * W.nr, rb, s);
+  copy_in(re, o + 3 * W.nr, rb, s);
+  copy_in(rh, o + 4 * W.nr, rb, s);
+  return cuda_check(cudaGetLastError(), "sbe_sources");
+}
+
+int sbe_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double* fields_in,
+                double* out, void* stream) {
+  int rc = check_w(c, w, "sbe_prop2qw");
+  if (rc) return rc;
+  if (!RR || n_rr < 2 || !fields_in || !out) return fail(SBE_ERR_ARG, "sbe_prop2qw: bad arguments");
+  return launch_prop2qw(c, w, RR, n_rr, (const double2*)fields_in, (double2*)out,
+                        as_stream(stream));
+}
+
+int sbe_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double* src_in, double* out,
+                int plasmonics, void* stream) {
+  int rc = check_w(c, w, "sbe_qw2prop");
+  if (rc) return rc;
+  if (!RR || n_rr < 2 || !src_in || !out) return fail(SBE_ERR_ARG, "sbe_qw2prop: bad arguments");
+  return launch_qw2prop(c, w, RR, n_rr, (const double2*)src_in, (double2*)out, plasmonics,
+                        as_stream(stream));
+}
+
+// ---- whole-context steps ---------------------------------------------------
+static void prep_frozen(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                        cudaStream_t s) {
+  (void)P;
+  launch_prep_scalar(c, C, D, s);
+  launch_gamma(c, -1, s);
+  if (c->any_offdiag) {
+    launch_offdiag_D(c, -1, nullptr, false, s);
+    launch_offdiag_AB(c, -1, s);
+  }
+}
+
+int sbe_rhs(SbeCtx* c, const double* P, const double* C, const double* D, const double* Ek,
+            int precision, double* dP, double* dC, double* dD, void* stream) {
+  if (!c || !P || !C || !D || !Ek || !dP || !dC || !dD) return fail(SBE_ERR_ARG, "sbe_rhs: null");
+  cudaStream_t s = as_stream(stream);
+  const double2 *p = (const double2*)P, *cc = (const double2*)C, *d = (const double2*)D;
+  prep_frozen(c, p, cc, d, s);
+  launch_calch_ctx(c, p, cc, d, (const double2*)Ek, s);
+  if (precision == SBE_PREC_FP64) {
+    launch_rhs64_ctx(c, p, cc, d, (double2*)dP, (double2*)dC, (double2*)dD, s);
+  } else if (precision == SBE_PREC_MIXED) {
+    int rc = sbe::rhs_mixed(c, p, cc, d, (double2*)dP, (double2*)dC, (double2*)dD, s);
+    if (rc) return rc;
+  } else {
+    return fail(SBE_ERR_ARG, "sbe_rhs: unknown precision");
+  }
+  return cuda_check(cudaGetLastError(), "sbe_rhs");
+}
+
+int sbe_leapfrog_step(SbeCtx* c, double* const* state9, const double* Ek, double dt,
+                      double* src_out, void* stream) {
+  if (!c || !state9 || !Ek || !src_out) return fail(SBE_ERR_ARG, "sbe_leapfrog_step: null");
+  for (int i = 0; i < 9; ++i)
+    if (!state9[i]) return fail(SBE_ERR_ARG, "sbe_leapfrog_step: null state level");
+  cudaStream_t s = as_stream(stream);
+  double2* st[9];
+  for (int i = 0; i < 9; ++i) st[i] = (double2*)state9[i];
+  // SBEs.py:5061-5068: p2 = YY3, C2 = CC3, D2 = DD3 (level 3 is "current")
+  prep_frozen(c, st[2], st[5], st[8], s);
+  launch_calch_ctx(c, st[2], st[5], st[8], (const double2*)Ek, s);
+  launch_rhs64_ctx(c, st[2], st[5], st[8], c->dP, c->dC, c->dD, s);
+  launch_leapfrog(c, st, dt, s);
+  launch_sources(c, st[0], st[3], st[6], c->ne, c->nh, (double2*)src_out, s);
+  launch_leap_shuffle(c, st, s);
+  return cuda_check(cudaGetLastError(), "sbe_leapfrog_step");
+}
+
+int sbe_rk4_step(SbeCtx* c, double* P, double* C, double* D, const double* Ek0, const double* dEk,
+                 double dt, int precision, double* src_out, void* stream) {
+  if (!c || !P || !C || !D || !Ek0 || !src_out) return fail(SBE_ERR_ARG, "sbe_rk4_step: null");
+  if (precision == SBE_PREC_MIXED) {
+    return sbe::rk4_mixed(c, (double2*)P, (double2*)C, (double2*)D, (const double2*)Ek0,
+                         (const double2*)dEk, dt, (double2*)src_out, as_stream(stream));
+  }
+  if (precision != SBE_PREC_FP64) return fail(SBE_ERR_ARG, "sbe_rk4_step: unknown precision");
+  cudaStream_t s = as_stream(stream);
+  double2 *p = (double2*)P, *cc = (double2*)C, *d = (double2*)D;
+  long long n = c->tot_mat;
+  prep_frozen(c, p, cc, d, s);
+  const double frac[4] = {0.0, 0.5, 0.5, 1.0};
+  for (int st = 1; st <= 4; ++st) {
+    const double2 *xp = p, *xc = cc, *xd = d;
+    if (st > 1) {
+      xp = c->xs;
+      xc = c->xs + n;
+      xd = c->xs + 2 * n;
+    }
+    launch_stage_field(c, (const double2*)Ek0, (const double2*)dEk, frac[st - 1], s);
+    launch_calch_ctx(c, xp, xc, xd, c->ekst, s);
+    launch_rhs64_ctx(c, xp, xc, xd, c->dP, c->dC, c->dD, s);
+    launch_rk4_axpy(c, st, dt, p, cc, d, s);
+  }
+  launch_relax_norm(c, cc, d, dt, false, s);
+  launch_sources(c, p, cc, d, c->ne, c->nh, (double2*)src_out, s);
+  return cuda_check(cudaGetLastError(), "sbe_rk4_step");
+}
+
+}  // extern "C"
+
+namespace sbe {
+// rates accumulation helper (MBPE/MBPH add to Win/Wout)
+__global__ void k_add_rates(const double* wr, int nk, double* a, double* b, double* c, double* d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  a[k] += wr[k];
+  b[k] += wr[nk + k];
+  c[k] += wr[2 * nk + k];
+  d[k] += wr[3 * nk + k];
+}
+
+void add_rates(const double* wrate, int nk, double* a, double* b, double* cc, double* d,
+               cudaStream_t s) {
+  k_add_rates<<<(nk + 127) / 128, 128, 0, s>>>(wrate, nk, a, b, cc, d);
+}
+}  // namespace sbe

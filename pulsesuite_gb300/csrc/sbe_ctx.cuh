@@ -1,0 +1,122 @@
+// Host-side context of libsbe_gb300: per-wire descriptors and the device arena.
+#pragma once
+#include "sbe_internal.cuh"
+
+struct SbeCtx {
+  int nw = 0;
+  int nk_max = 0, nr_max = 0;
+  std::vector<SbeWireDesc> desc;
+  std::vector<sbe::WireDev> wires;  // host copy of d_wires
+  sbe::WireDev* d_wires = nullptr;
+  long long tot_mat = 0, tot_vec = 0, tot_r = 0, tot_dd = 0, tot_kr = 0;
+
+  // one arena for everything the context owns
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+
+  // ---- tables (FP64, built once) ----
+  double *kr = nullptr, *r = nullptr, *Ee = nullptr, *Eh = nullptr;  // vec, r, vec, vec
+  double* v0 = nullptr;       // 3*tot_vec: per wire [3][nk] (eh, ee, hh) by k1-k2 >= 0
+  double* chi = nullptr;      // 2*tot_vec: per wire [2][nk] Chi1De/Chi1Dh by |k1-k2|
+  double* qeh = nullptr;      // 2*tot_vec: per wire [2][nk] qe/qh by |k1-k2|
+  int* iq = nullptr;          // tot_vec: round(|ky/dq|) of Vxx2
+  double *EP = nullptr, *HP = nullptr;  // tot_mat
+  int* maps = nullptr;        // 6*tot_mat: k_p_q, k_m_q, k1p, k1p_m_q, k1, k1_m_q
+  double* xeh = nullptr;      // 2*tot_vec
+  double* window = nullptr;   // tot_r
+  double2* expikr = nullptr;  // tot_kr  [nk][nr]
+  double2* wk = nullptr;      // tot_r: FFTG(window)
+  double* vcorr = nullptr;    // 3*(tot_r + 2*nw): Vint correlation scratch
+
+  // ---- per-step workspace ----
+  double2 *ne = nullptr, *nh = nullptr;  // tot_vec
+  double* eps = nullptr;                 // tot_vec
+  double* vs = nullptr;                  // 3*tot_vec screened V by k1-k2
+  double *gamE = nullptr, *gamH = nullptr;
+  double *De = nullptr, *Dh = nullptr;   // tot_dd
+  double2 *dA = nullptr, *dB = nullptr;  // tot_mat dephasing contraction matrices (real values)
+  double2 *Heh = nullptr, *Hee = nullptr, *Hhh = nullptr;  // tot_mat
+  double2* tr = nullptr;                 // 4*tot_vec diagonal traces (C, D) per wire [2][2nk]
+  double2 *dP = nullptr, *dC = nullptr, *dD = nullptr;     // tot_mat
+  double* wrate = nullptr;               // 4*tot_vec Win/Wout e/h
+  double2* G = nullptr;                  // 3*tot_kr source GEMM outputs
+  double2* kacc = nullptr;               // 3*tot_mat RK4 accumulator
+  double2* xs = nullptr;                 // 3*tot_mat RK4 stage state
+  double* scal = nullptr;                // 16*nw per-wire scalars
+  double2* ekst = nullptr;               // 3*tot_r stage field
+
+  int any_offdiag = 0;                   // some wire has OffDiagDph on
+  void* mixed = nullptr;                 // mixed-precision workspace (sbe_tc.cu)
+};
+
+namespace sbe {
+// sbe_tables.cu
+int build_tables(SbeCtx* c, cudaStream_t s);
+// sbe_prep.cu
+void launch_prep_scalar(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s);
+void launch_expand_vc(SbeCtx* c, int w, double* VC, double* E1D, cudaStream_t s);
+void launch_gamma(SbeCtx* c, int w_only, cudaStream_t s);
+void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaStream_t s);
+void launch_offdiag_AB(SbeCtx* c, int w_only, cudaStream_t s);
+void launch_traces(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s);
+void launch_calch_ctx(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                      const double2* Ek, cudaStream_t s);
+int launch_calch_single(int nk, const double2* Meh, const double2* Wee, const double2* Whh,
+                        const double2* C, const double2* D, const double2* P, const double* VC,
+                        const double* Ee, const double* Eh, double gap, int excitons, int lf,
+                        int freepot, double2* Heh, double2* Hee, double2* Hhh, cudaStream_t s);
+// sbe_gemm64.cu
+enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_H = 3 };
+struct Term {
+  const void* A;
+  const void* B;
+  int opA, opB;
+  int realA;        // A is a real (double) matrix
+  double2 alpha;
+};
+struct GemmBatch {
+  int nterms;
+  Term t[6];
+  double2* out;
+  int epi;          // 0 none, 1 dP epilogue
+  // dP epilogue inputs
+  const double2* Heh;
+  const double2* P;
+  const double* gamE;
+  const double* gamH;
+  const double2* offp;  // optional explicit OffP (single-wire API)
+  int w_only = -1;      // >= 0: only this wire of the context
+};
+void launch_gemm64(const WireDev* d_wires, int nw, int nk_max, const GemmBatch& b,
+                   bool batched, int nk_single, cudaStream_t s);
+void launch_sources_gemm64(SbeCtx* c, const GemmBatch& b, cudaStream_t s);
+void launch_rhs64_ctx(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                      double2* dP, double2* dC, double2* dD, cudaStream_t s);
+// sbe_step.cu
+void launch_leapfrog(SbeCtx* c, double2* const* st9, double dt, cudaStream_t s);
+void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_scheme,
+                       cudaStream_t s);
+void launch_sources(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                    const double2* ne, const double2* nh, double2* src, cudaStream_t s,
+                    int w_only = -1);
+void launch_extract_diag(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s);
+void launch_screen(SbeCtx* c, int w_only, cudaStream_t s);
+void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s);
+void launch_leap_shuffle(SbeCtx* c, double2* const* st, cudaStream_t s);
+void add_rates(const double* wrate, int nk, double* a, double* b, double* cc, double* d,
+               cudaStream_t s);
+// sbe_tc.cu (mixed precision)
+void mixed_free(SbeCtx* c);
+int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, double2* dP,
+              double2* dC, double2* dD, cudaStream_t s);
+int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
+              const double2* dEk, double dt, double2* src, cudaStream_t s);
+void launch_rk4_axpy(SbeCtx* c, int stage, double dt, double2* P, double2* C, double2* D,
+                     cudaStream_t s);
+void launch_stage_field(SbeCtx* c, const double2* Ek0, const double2* dEk, double frac,
+                        cudaStream_t s);
+int launch_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
+                   double2* out, cudaStream_t s);
+int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* src,
+                   double2* out, int plasmonics, cudaStream_t s);
+}  // namespace sbe

@@ -1,0 +1,491 @@
+// Per-step preparation of every wire: occupations, screening, diagonal and
+// off-diagonal dephasing, and the Hartree-Fock Hamiltonians (FP64).
+#include "sbe_ctx.cuh"
+
+namespace sbe {
+
+// ---------------------------------------------------------------------------
+// SBEs.py:5200-5204 (ne, nh = diag C, diag D) and coulomb.py:1172-1230
+// (CalcScreenedArrays / Eps1D).  On the reference grid every Coulomb table is a
+// function of k1-k2 only: V0[k1,k2] = v0(k1-k2) for k1 >= k2 and 0 above the
+// diagonal (kkp < 0 is skipped), E1D[k1,k2] = eps(|k1-k2|).  One block per wire
+// forms ne, nh, n1D and the screened vs(d) = v0(d)/eps(d).
+__global__ void k_extract_diag(const WireDev* wires, const double2* C, const double2* D,
+                               double2* ne, double2* nh) {
+  const WireDev W = wires[blockIdx.x];
+  const int nk = W.nk;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    ne[W.off_vec + k] = C[W.off_mat + (long long)k * nk + k];
+    nh[W.off_vec + k] = D[W.off_mat + (long long)k * nk + k];
+  }
+}
+
+void launch_extract_diag(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
+  k_extract_diag<<<c->nw, 256, 0, s>>>(c->d_wires, C, D, c->ne, c->nh);
+}
+
+__global__ void k_screen(const WireDev* wires, int w_only, const double* v0, const double* chi,
+                         const double* qeh, const double2* ne, const double2* nh, double* eps,
+                         double* vs) {
+  const WireDev W = wires[w_only >= 0 ? w_only : blockIdx.x];
+  const int nk = W.nk;
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x)
+    s += ne[W.off_vec + k].x + nh[W.off_vec + k].x;
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  double n1d = red[0] / 2.0 / W.L;
+  n1d = fmin(n1d, W.nmax);
+  const bool screened = (W.flags & SBE_F_SCREENED) != 0;
+  for (int d = threadIdx.x; d < nk; d += blockDim.x) {
+    double e = 1.0;
+    if (screened) {
+      double qe = qeh[2 * W.off_vec + d], qh = qeh[2 * W.off_vec + nk + d];
+      double ce = chi[2 * W.off_vec + d], chh = chi[2 * W.off_vec + nk + d];
+      e = 1.0 - ce * 2 * log(fabs((qe - kPi * n1d) / (qe + n1d))) -
+          chh * 2 * log(fabs((qh - kPi * n1d) / (qh + n1d)));
+    }
+    eps[W.off_vec + d] = e;
+    for (int n = 0; n < 3; ++n)
+      vs[3 * W.off_vec + n * nk + d] = v0[3 * W.off_vec + n * nk + d] / e;
+  }
+}
+
+void launch_screen(SbeCtx* c, int w_only, cudaStream_t s) {
+  k_screen<<<w_only >= 0 ? 1 : c->nw, 256, 0, s>>>(c->d_wires, w_only, c->v0, c->chi, c->qeh,
+                                                   c->ne, c->nh, c->eps, c->vs);
+}
+
+void launch_prep_scalar(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
+  launch_extract_diag(c, C, D, s);
+  launch_screen(c, -1, s);
+}
+
+// Expand to the reference's (Nk, Nk, 3) VC and (Nk, Nk) E1D of wire w.
+__global__ void k_expand_vc(const WireDev* wires, int w, const double* vs, const double* eps,
+                            double* VC, double* E1D) {
+  const WireDev W = wires[w];
+  int k2 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k1 = blockIdx.y;
+  if (k1 >= W.nk || k2 >= W.nk) return;
+  int d = k1 - k2;
+  long long o = (long long)k1 * W.nk + k2;
+  for (int n = 0; n < 3; ++n)
+    VC[3 * o + n] = d >= 0 ? vs[3 * W.off_vec + n * W.nk + d] : 0.0;
+  E1D[o] = eps[W.off_vec + (d >= 0 ? d : -d)];
+}
+
+void launch_expand_vc(SbeCtx* c, int w, double* VC, double* E1D, cudaStream_t s) {
+  int nk = c->wires[w].nk;
+  k_expand_vc<<<dim3((nk + 127) / 128, nk), 128, 0, s>>>(c->d_wires, w, c->vs, c->eps, VC, E1D);
+}
+
+// ---------------------------------------------------------------------------
+// dephasing.py:29-103 (_CalcGammaE_jit/_CalcGammaH_jit) with the index maps of
+// InitializeDephasing and Vxx2 (V[round(|k/dk|), 0]^2, dephasing.py:362-378).
+// One warp per (wire, k), lanes over q.
+__device__ inline double occ_ext(const double2* n, int idx, int nk, bool* ok) {
+  // extended array of the reference: index idx+1 in [1, nk] is valid
+  if (idx < 0 || idx >= nk) { *ok = false; return 0.0; }
+  *ok = true;
+  return n[idx].x;
+}
+
+__global__ void k_gamma(const WireDev* wires, int w_only, const double2* ne, const double2* nh,
+                        const double* vs, const int* iq, const int* maps, const double* xeh,
+                        double* gamE, double* gamH) {
+  int wi = (w_only >= 0) ? w_only : blockIdx.y;
+  const WireDev W = wires[wi];
+  const int nk = W.nk;
+  int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int lane = threadIdx.x & 31;
+  if (k >= nk) return;
+  if (!(W.flags & SBE_F_DIAGDPH)) {
+    if (lane == 0) {
+      gamE[W.off_vec + k] = W.gam_e;
+      gamH[W.off_vec + k] = W.gam_h;
+    }
+    return;
+  }
+  const double2* pe = ne + W.off_vec;
+  const double2* ph = nh + W.off_vec;
+  const long long st = (long long)nk * nk;
+  const int* m = maps + 6 * W.off_mat + (long long)k * nk;
+  const double* v = vs + 3 * W.off_vec;
+  const double* xe = xeh + 2 * W.off_vec;
+  const double* xh = xe + nk;
+  const double pih = kPi / kHbar;
+  double ge = 0.0, gh = 0.0;
+  for (int q = lane; q < nk; q += 32) {
+    int iqq = iq[W.off_vec + q];
+    double veh = v[0 * nk + iqq], vee = v[1 * nk + iqq], vhh = v[2 * nk + iqq];
+    double veh2 = veh * veh, vee2 = vee * vee, vhh2 = vhh * vhh;
+    bool ok, ok1, ok2, ok3;
+    // electrons
+    double a = occ_ext(pe, m[0 * st + q], nk, &ok);
+    if (ok) ge += pih * vee2 * a * (1.0 - a) * fabs(xe[q]);
+    double n1 = occ_ext(ph, m[3 * st + q], nk, &ok1);   // k1p_m_q
+    double n2 = occ_ext(ph, m[2 * st + q], nk, &ok2);   // k1p
+    double n3 = occ_ext(pe, m[1 * st + q], nk, &ok3);   // k_m_q
+    if (ok1 && ok2 && ok3)
+      ge += pih * veh2 * (n1 * (1.0 - n2) * n3 + (1.0 - n1) * n2 * (1.0 - n3)) * fabs(xh[q]);
+    // holes
+    double b = occ_ext(ph, m[0 * st + q], nk, &ok);
+    if (ok) gh += pih * vhh2 * b * (1.0 - b) * fabs(xh[q]);
+    double e1 = occ_ext(pe, m[5 * st + q], nk, &ok1);   // k1_m_q
+    double e2 = occ_ext(pe, m[4 * st + q], nk, &ok2);   // k1
+    double h3 = occ_ext(ph, m[1 * st + q], nk, &ok3);   // k_m_q
+    if (ok1 && ok2 && ok3)
+      gh += pih * veh2 * (e1 * (1.0 - e2) * h3 + (1.0 - e1) * e2 * (1.0 - h3)) * fabs(xe[q]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ge += __shfl_down_sync(0xffffffffu, ge, o);
+    gh += __shfl_down_sync(0xffffffffu, gh, o);
+  }
+  if (lane == 0) {
+    gamE[W.off_vec + k] = ge;
+    gamH[W.off_vec + k] = gh;
+  }
+}
+
+void launch_gamma(SbeCtx* c, int w_only, cudaStream_t s) {
+  int wpb = 8;
+  dim3 g((c->nk_max + wpb - 1) / wpb, w_only >= 0 ? 1 : c->nw);
+  k_gamma<<<g, 32 * wpb, 0, s>>>(c->d_wires, w_only, c->ne, c->nh, c->vs, c->iq, c->maps,
+                                 c->xeh, c->gamE, c->gamH);
+}
+
+// ---------------------------------------------------------------------------
+// dephasing.py:227-317 (_CalcOffDiagDeph_E2_jit / _H2_jit): D[q+Nk][k] for one
+// carrier species "a" (electrons for De, holes for Dh) against itself and the
+// other species "b".  FP64, literal energy differences from the Ee/Eh arrays.
+// g3 = [gam_eh, gam_e, gam_h]: De uses (g0, g2), Dh uses (g1, g2) (quirk kept).
+__global__ void k_offdiag_D64(const WireDev* wires, int w_only, const double2* ne,
+                              const double2* nh, const double* Ee, const double* Eh,
+                              const double* vs, double g0, double g1, double g2, int use_g,
+                              double* De, double* Dh) {
+  int wi = (w_only >= 0) ? w_only : blockIdx.z;
+  const WireDev W = wires[wi];
+  const int nk = W.nk;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int qi = blockIdx.y >> 1;          // 0 .. 2nk
+  int which = blockIdx.y & 1;        // 0 -> De, 1 -> Dh
+  if (qi > 2 * nk || k >= nk) return;
+  int q = qi - nk;
+  double ga = use_g ? (which == 0 ? g0 : g1) : (which == 0 ? W.gam_eh : W.gam_e);
+  double gab = use_g ? g2 : W.gam_h;
+  const double2* na = (which == 0 ? ne : nh) + W.off_vec;
+  const double2* nb = (which == 0 ? nh : ne) + W.off_vec;
+  const double* Ea = (which == 0 ? Ee : Eh) + W.off_vec;
+  const double* Eb = (which == 0 ? Eh : Ee) + W.off_vec;
+  const double* v = vs + 3 * W.off_vec;
+  int aq = q < 0 ? -q : q;
+  double vaa = 0.0, vab = 0.0;
+  if (aq >= 1 && aq < nk) {
+    double x = v[(which == 0 ? 1 : 2) * nk + aq];
+    double y = v[0 * nk + aq];
+    vaa = x * x;
+    vab = y * y;
+  }
+  double acc = 0.0;
+  if (k + q >= 0 && k + q < nk) {
+    double nak = hypot(na[k].x, na[k].y);
+    double bb = kHbar * ga, b2 = kHbar * gab;
+    if (vaa != 0.0) {
+      int plo = max(q + 1, 0), phi = min(q + nk - 1, nk - 1);
+      for (int p = plo; p <= phi; ++p) {
+        double Ed = Ea[k + q] + Ea[p - q] - Ea[p] - Ea[k];
+        double npq = hypot(na[p - q].x, na[p - q].y);
+        double np_ = hypot(na[p].x, na[p].y);
+        double lr = (bb / kPi) / (Ed * Ed + bb * bb);
+        acc += vaa * lr * (npq * (1.0 - np_) * (1.0 - nak) + (1.0 - npq) * np_ * nak);
+      }
+    }
+    if (vab != 0.0) {
+      int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
+      for (int p = plo; p <= phi; ++p) {
+        double Ed = Ea[k + q] + Eb[p + q] - Eb[p] - Ea[k];
+        double npq = hypot(nb[p + q].x, nb[p + q].y);
+        double np_ = hypot(nb[p].x, nb[p].y);
+        double lr = (b2 / kPi) / (Ed * Ed + b2 * b2);
+        acc += vab * lr * (npq * (1.0 - np_) * (1.0 - nak) + (1.0 - npq) * np_ * nak);
+      }
+    }
+  }
+  double* D = (which == 0 ? De : Dh) + W.off_dd;
+  D[(long long)qi * nk + k] = acc * kPi / kHbar;
+}
+
+void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaStream_t s) {
+  (void)fp32;
+  dim3 g((c->nk_max + 127) / 128, 2 * (2 * c->nk_max + 1), w_only >= 0 ? 1 : c->nw);
+  double g0 = 0, g1 = 0, g2 = 0;
+  int use_g = 0;
+  if (g3) { g0 = g3[0]; g1 = g3[1]; g2 = g3[2]; use_g = 1; }
+  k_offdiag_D64<<<g, 128, 0, s>>>(c->d_wires, w_only, c->ne, c->nh, c->Ee, c->Eh, c->vs, g0, g1,
+                                  g2, use_g, c->De, c->Dh);
+}
+
+// dephasing.py:320-356: x = i hbar (A p + p B^T) with A[kh,j] = Dh[j-kh+Nk][kh],
+// B[ke,j] = De[j-ke+Nk][ke] and the j = row entry removed (undel[q=0] = 0).
+__global__ void k_offdiag_AB(const WireDev* wires, int w_only, const double* De,
+                             const double* Dh, double2* A, double2* B) {
+  int wi = (w_only >= 0) ? w_only : blockIdx.z;
+  const WireDev W = wires[wi];
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int row = blockIdx.y;
+  if (row >= W.nk || j >= W.nk) return;
+  int nk = W.nk;
+  long long o = W.off_mat + (long long)row * nk + j;
+  bool on = (w_only >= 0 || (W.flags & SBE_F_OFFDIAGDPH)) && j != row;
+  long long di = W.off_dd + (long long)(j - row + nk) * nk + row;
+  A[o] = make_double2(on ? Dh[di] : 0.0, 0.0);
+  B[o] = make_double2(on ? De[di] : 0.0, 0.0);
+}
+
+void launch_offdiag_AB(SbeCtx* c, int w_only, cudaStream_t s) {
+  dim3 g((c->nk_max + 127) / 128, c->nk_max, w_only >= 0 ? 1 : c->nw);
+  k_offdiag_AB<<<g, 128, 0, s>>>(c->d_wires, w_only, c->De, c->Dh, c->dA, c->dB);
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal traces tr_d(X) = sum_k X[k][k+d], d in (-Nk, Nk), for the direct
+// Coulomb terms of CalcH (SBEs.py:1094-1103).  Layout per wire: [2][2Nk] with
+// entry d + Nk (C first, then D).
+__global__ void k_traces(const WireDev* wires, const double2* C, const double2* D, double2* tr) {
+  const WireDev W = wires[blockIdx.z];
+  int nk = W.nk;
+  int d = blockIdx.x - (nk - 1) + 0;  // blockIdx.x in [0, 2nk-1)
+  int which = blockIdx.y;
+  if ((int)blockIdx.x >= 2 * nk - 1) return;
+  const double2* X = (which == 0 ? C : D) + W.off_mat;
+  int k0 = d >= 0 ? 0 : -d, k1 = d >= 0 ? nk - 1 - d : nk - 1;
+  double sr = 0.0, si = 0.0;
+  for (int k = k0 + threadIdx.x; k <= k1; k += 32) {
+    double2 v = X[(long long)k * nk + k + d];
+    sr += v.x;
+    si += v.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (threadIdx.x == 0) tr[4 * W.off_vec + which * 2 * nk + d + nk] = make_double2(sr, si);
+}
+
+void launch_traces(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
+  k_traces<<<dim3(2 * c->nk_max - 1, 2, c->nw), 32, 0, s>>>(c->d_wires, C, D, c->tr);
+}
+
+// ---------------------------------------------------------------------------
+// SBEs.py:1044-1131 _CalcH_fallback and SBEs.py:5153-5163 _calc_Meh.
+// V[n][q] = VC[|q|][0][n] for 1 <= |q| < Nk (given by vq, stride nk per n).
+struct CalcHArgs {
+  int nk, nr;
+  const double2 *Meh, *Wee, *Whh, *C, *D, *P, *Ek;
+  const double *vq, *Ee, *Eh;
+  const double2* tr;    // [2][2nk] traces (C, D), may be null when !lf
+  double gap, ehint, dcv;
+  int yw, zsign, excitons, lf, freepot, optics;
+  double2 *Heh, *Hee, *Hhh;
+};
+
+__device__ void calch_point(const CalcHArgs& a, int k1, int k2) {
+  const int nk = a.nk;
+  // Meh[ke=k1][kh=k2]
+  double2 heh;
+  if (a.Meh) {
+    heh = a.Meh[(long long)k1 * nk + k2];
+  } else if (a.Ek && a.optics) {
+    int q = k1 - k2;
+    if (q < 0) q += a.nr;
+    double2 ex = a.Ek[q], ey = a.Ek[a.nr + q], ez = a.Ek[2 * a.nr + q];
+    double xcv = a.dcv * ((k2 & 1) ? -1.0 : 1.0);
+    double2 t1 = cscale(ex, -a.ehint * xcv);
+    double2 t2 = cscale(cscale(ey, a.ehint * a.dcv), (double)a.yw);
+    double2 t3 = cscale(cscale(ez, a.ehint * -a.dcv), (double)a.zsign);
+    heh = csub(csub(t1, t2), t3);
+  } else {
+    heh = make_double2(0.0, 0.0);
+  }
+  double2 hee = make_double2(k1 == k2 ? a.Ee[k1] + a.gap : 0.0, 0.0);
+  double2 hhh = make_double2(k1 == k2 ? a.Eh[k1] : 0.0, 0.0);
+  if (a.freepot) {
+    hee = cadd(hee, a.Wee[(long long)k1 * nk + k2]);
+    hhh = cadd(hhh, a.Whh[(long long)k1 * nk + k2]);
+  }
+  if (a.excitons) {
+    int qmin = max(-k1, -k2), qmax = min(nk - 1 - k1, nk - 1 - k2);
+    const double* v0 = a.vq;
+    const double* v1 = a.vq + nk;
+    const double* v2 = a.vq + 2 * nk;
+    for (int q = qmin; q <= qmax; ++q) {
+      if (q == 0) continue;
+      int aq = q < 0 ? -q : q;
+      long long idx = (long long)(k2 + q) * nk + (k1 + q);   // X^T[k1+q][k2+q]
+      double2 pv = a.P[idx];
+      heh.x += v0[aq] * pv.x;
+      heh.y += v0[aq] * pv.y;
+    }
+    if (a.lf) {
+      for (int q = qmin; q <= qmax; ++q) {
+        if (q == 0) continue;
+        int aq = q < 0 ? -q : q;
+        long long idx = (long long)(k2 + q) * nk + (k1 + q);
+        double2 cv = a.C[idx], dv = a.D[idx];
+        hee.x -= v1[aq] * cv.x;
+        hee.y -= v1[aq] * cv.y;
+        hhh.x -= v2[aq] * dv.x;
+        hhh.y -= v2[aq] * dv.y;
+      }
+      int d = k1 - k2;
+      if (d != 0) {
+        int ad = d < 0 ? -d : d;
+        double2 trC = a.tr[d + nk], trCm = a.tr[-d + nk];
+        double2 trD = a.tr[2 * nk + d + nk], trDm = a.tr[2 * nk - d + nk];
+        hee.x += v1[ad] * trC.x - v0[ad] * trDm.x;
+        hee.y += v1[ad] * trC.y - v0[ad] * trDm.y;
+        hhh.x += v2[ad] * trD.x - v0[ad] * trCm.x;
+        hhh.y += v2[ad] * trD.y - v0[ad] * trCm.y;
+      }
+    } else if (k1 == k2) {
+      for (int j = 0; j < nk; ++j) {
+        if (j == k1) continue;
+        int aq = j - k1 < 0 ? k1 - j : j - k1;
+        double2 cv = a.C[(long long)j * nk + j], dv = a.D[(long long)j * nk + j];
+        hee.x -= v1[aq] * cv.x;
+        hee.y -= v1[aq] * cv.y;
+        hhh.x -= v2[aq] * dv.x;
+        hhh.y -= v2[aq] * dv.y;
+      }
+    }
+  }
+  long long o = (long long)k1 * nk + k2;
+  a.Heh[o] = heh;
+  a.Hee[o] = hee;
+  a.Hhh[o] = hhh;
+}
+
+__global__ void k_calch_ctx(const WireDev* wires, const double2* P, const double2* C,
+                            const double2* D, const double2* Ek, const double* vs,
+                            const double* Ee, const double* Eh, const double2* tr, double2* Heh,
+                            double2* Hee, double2* Hhh) {
+  const WireDev W = wires[blockIdx.z];
+  int k1 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k2 = blockIdx.y;
+  if (k1 >= W.nk || k2 >= W.nk) return;
+  CalcHArgs a;
+  a.nk = W.nk;
+  a.nr = W.nr;
+  a.Meh = nullptr;
+  a.Wee = a.Whh = nullptr;
+  a.P = P + W.off_mat;
+  a.C = C + W.off_mat;
+  a.D = D + W.off_mat;
+  a.Ek = Ek ? Ek + 3 * W.off_r : nullptr;
+  a.vq = vs + 3 * W.off_vec;
+  a.Ee = Ee + W.off_vec;
+  a.Eh = Eh + W.off_vec;
+  a.tr = tr + 4 * W.off_vec;
+  a.gap = W.gap;
+  a.ehint = W.ehint;
+  a.dcv = W.dcv;
+  a.yw = W.yw;
+  a.zsign = W.zsign;
+  a.excitons = (W.flags & SBE_F_EXCITONS) != 0;
+  a.lf = (W.flags & SBE_F_LF) != 0;
+  a.freepot = 0;
+  a.optics = (W.flags & SBE_F_OPTICS) != 0;
+  a.Heh = Heh + W.off_mat;
+  a.Hee = Hee + W.off_mat;
+  a.Hhh = Hhh + W.off_mat;
+  calch_point(a, k1, k2);
+}
+
+void launch_calch_ctx(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                      const double2* Ek, cudaStream_t s) {
+  launch_traces(c, C, D, s);
+  dim3 g((c->nk_max + 63) / 64, c->nk_max, c->nw);
+  k_calch_ctx<<<g, 64, 0, s>>>(c->d_wires, P, C, D, Ek, c->vs, c->Ee, c->Eh, c->tr, c->Heh,
+                               c->Hee, c->Hhh);
+}
+
+// Single-wire CalcH on explicit arrays (the reference's pure-function call).
+__global__ void k_vq_from_vc(int nk, const double* VC, double* vq) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nk) return;
+  for (int n = 0; n < 3; ++n) vq[n * nk + q] = VC[((long long)q * nk + 0) * 3 + n];
+}
+
+__global__ void k_traces_single(int nk, const double2* C, const double2* D, double2* tr) {
+  int d = (int)blockIdx.x - (nk - 1);
+  int which = blockIdx.y;
+  const double2* X = which == 0 ? C : D;
+  int k0 = d >= 0 ? 0 : -d, k1 = d >= 0 ? nk - 1 - d : nk - 1;
+  double sr = 0.0, si = 0.0;
+  for (int k = k0 + threadIdx.x; k <= k1; k += 32) {
+    double2 v = X[(long long)k * nk + k + d];
+    sr += v.x;
+    si += v.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (threadIdx.x == 0) tr[which * 2 * nk + d + nk] = make_double2(sr, si);
+}
+
+__global__ void k_calch_single(CalcHArgs a) {
+  int k1 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k2 = blockIdx.y;
+  if (k1 >= a.nk || k2 >= a.nk) return;
+  calch_point(a, k1, k2);
+}
+
+int launch_calch_single(int nk, const double2* Meh, const double2* Wee, const double2* Whh,
+                        const double2* C, const double2* D, const double2* P, const double* VC,
+                        const double* Ee, const double* Eh, double gap, int excitons, int lf,
+                        int freepot, double2* Heh, double2* Hee, double2* Hhh, cudaStream_t s) {
+  double* vq = nullptr;
+  double2* tr = nullptr;
+  if (cudaMallocAsync(&vq, sizeof(double) * 3 * nk, s) != cudaSuccess ||
+      cudaMallocAsync(&tr, sizeof(double2) * 4 * nk, s) != cudaSuccess)
+    return fail(SBE_ERR_OOM, "sbe_calch: scratch allocation failed");
+  k_vq_from_vc<<<(nk + 127) / 128, 128, 0, s>>>(nk, VC, vq);
+  k_traces_single<<<dim3(2 * nk - 1, 2), 32, 0, s>>>(nk, C, D, tr);
+  CalcHArgs a;
+  a.nk = nk;
+  a.nr = 2 * nk + 2;
+  a.Meh = Meh;
+  a.Wee = Wee;
+  a.Whh = Whh;
+  a.C = C;
+  a.D = D;
+  a.P = P;
+  a.Ek = nullptr;
+  a.vq = vq;
+  a.Ee = Ee;
+  a.Eh = Eh;
+  a.tr = tr;
+  a.gap = gap;
+  a.ehint = a.dcv = 0.0;
+  a.yw = a.zsign = 1;
+  a.excitons = excitons;
+  a.lf = lf;
+  a.freepot = freepot;
+  a.optics = 0;
+  a.Heh = Heh;
+  a.Hee = Hee;
+  a.Hhh = Hhh;
+  k_calch_single<<<dim3((nk + 63) / 64, nk), 64, 0, s>>>(a);
+  cudaFreeAsync(vq, s);
+  cudaFreeAsync(tr, s);
+  return cuda_check(cudaGetLastError(), "sbe_calch");
+}
+
+}  // namespace sbe

@@ -1,0 +1,228 @@
+"""Wire descriptors and the device context that owns their tables.
+
+A :class:`WireContext` is a batch of quantum wires (possibly of different Nk)
+whose one-time tables (Coulomb V(q), Chi1D, phonon EP/HP, dephasing index maps,
+e^{ikr}, window) live on the GPU.  State tensors are owned by the caller and are
+packed: wire w's Nk x Nk matrix starts at element ``mat_offset[w]`` of a flat
+complex128 tensor; the per-wire field / source vectors (length Nr = 2 Nk + 2)
+start at ``r_offset[w]``.
+"""
+
+import ctypes
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _lib
+from .constants import E0, HBAR, ME0
+
+CDTYPE = torch.complex128
+
+
+@dataclass
+class WireSpec:
+    """One quantum wire in SI units (qw.params fields, SBEs.py:4978-5002)."""
+    nk: int
+    L: float
+    Delta0: float = 5e-9
+    gap: float = 1.5 * E0
+    me: float = 0.07 * ME0
+    mh: float = 0.45 * ME0
+    HO: float = 100e-3 * E0
+    gam_e: float = 1e12
+    gam_h: float = 1e12
+    gam_eh: float = 1e12
+    epsr: float = 9.1
+    Oph: float = 36e-3 * E0 / HBAR
+    Gph: float = 3e-3 * E0 / HBAR
+    temp: float = 77.0
+    wire_index: int = 1
+    flags: dict = field(default_factory=lambda: dict(
+        Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
+        LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False))
+
+    def flag_bits(self):
+        bits = 0
+        for k, v in self.flags.items():
+            if v:
+                bits |= _lib.FLAG_BITS[k]
+        return bits
+
+    @property
+    def nr(self):
+        return 2 * self.nk + 2
+
+    def to_c(self):
+        return _lib.SbeWireDesc(self.nk, self.wire_index, self.flag_bits(), 0, self.L,
+                                self.Delta0, self.gap, self.me, self.mh, self.HO, self.gam_e,
+                                self.gam_h, self.gam_eh, self.epsr, self.Oph, self.Gph,
+                                self.temp)
+
+
+TABLES = dict(kr=0, r=1, Ee=2, Eh=3, V0=4, Chi1D=5, qeqh=6, EP=7, HP=8, window=9, maps=10,
+              xexh=11, Expikr=12, scalars=13, window_k=14)
+
+
+class WireContext:
+    """Device tables of a batch of wires (sbe_ctx_create)."""
+
+    def __init__(self, specs, device=None):
+        if not torch.cuda.is_available():
+            raise _lib.SbeError("a CUDA device is required (no CPU fallback)")
+        self.lib = _lib.load()
+        self.specs = list(specs)
+        self.device = torch.device(device or "cuda")
+        arr = (_lib.SbeWireDesc * len(self.specs))(*[s.to_c() for s in self.specs])
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.sbe_ctx_create(arr, len(self.specs), _lib.stream_handle(),
+                                               ctypes.byref(h)), "sbe_ctx_create")
+        self.handle = h
+        lay = (ctypes.c_longlong * (3 * len(self.specs)))()
+        tm = ctypes.c_longlong()
+        tr = ctypes.c_longlong()
+        _lib.check(self.lib.sbe_ctx_layout(h, lay, ctypes.byref(tm), ctypes.byref(tr)),
+                   "sbe_ctx_layout")
+        self.nk = [lay[3 * w] for w in range(len(self.specs))]
+        self.mat_offset = [lay[3 * w + 1] for w in range(len(self.specs))]
+        self.r_offset = [lay[3 * w + 2] for w in range(len(self.specs))]
+        self.total_mat = tm.value
+        self.total_r = tr.value
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.sbe_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nw(self):
+        return len(self.specs)
+
+    # ---- packed-state helpers ---------------------------------------------
+    def zeros_state(self):
+        return torch.zeros(self.total_mat, dtype=CDTYPE, device=self.device)
+
+    def zeros_r(self, ncomp):
+        return torch.zeros(ncomp * self.total_r, dtype=CDTYPE, device=self.device)
+
+    def mat(self, flat, w):
+        n = self.nk[w]
+        o = self.mat_offset[w]
+        return flat[o:o + n * n].view(n, n)
+
+    def rvec(self, flat, w, ncomp):
+        """View of wire w's ncomp x Nr block of a packed r-vector tensor."""
+        nr = 2 * self.nk[w] + 2
+        o = ncomp * self.r_offset[w]
+        return flat[o:o + ncomp * nr].view(ncomp, nr)
+
+    def pack(self, mats):
+        return torch.cat([m.reshape(-1) for m in mats]).to(self.device, CDTYPE).contiguous()
+
+    # ---- tables ------------------------------------------------------------
+    def table(self, w, name):
+        which = TABLES[name]
+        nk = self.nk[w]
+        nr = 2 * nk + 2
+        shapes = {0: (nk,), 1: (nr,), 2: (nk,), 3: (nk,), 4: (3, nk), 5: (2, nk), 6: (2, nk),
+                  7: (nk, nk), 8: (nk, nk), 9: (nr,), 11: (2, nk), 13: (16,)}
+        if which == 10:
+            t = torch.empty((6, nk, nk), dtype=torch.int32, device=self.device)
+        elif which == 12:
+            t = torch.empty((nk, nr), dtype=CDTYPE, device=self.device)
+        elif which == 14:
+            t = torch.empty((nr,), dtype=CDTYPE, device=self.device)
+        else:
+            t = torch.empty(shapes[which], dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_ctx_table(self.handle, w, which, _lib.ptr(t),
+                                          t.numel() * t.element_size(), _lib.stream_handle()),
+                   "sbe_ctx_table")
+        return t
+
+    # ---- per-wire reference building blocks ------------------------------
+    def screened_arrays(self, w, ne, nh):
+        nk = self.nk[w]
+        VC = torch.empty((nk, nk, 3), dtype=torch.float64, device=self.device)
+        E1D = torch.empty((nk, nk), dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_screened_arrays(self.handle, w, _lib.ptr(ne), _lib.ptr(nh),
+                                                _lib.ptr(VC), _lib.ptr(E1D),
+                                                _lib.stream_handle()), "sbe_screened_arrays")
+        return VC, E1D
+
+    def gamma(self, w, ne, nh, VC):
+        nk = self.nk[w]
+        ge = torch.empty(nk, dtype=torch.float64, device=self.device)
+        gh = torch.empty(nk, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_gamma(self.handle, w, _lib.ptr(ne), _lib.ptr(nh), _lib.ptr(VC),
+                                      _lib.ptr(ge), _lib.ptr(gh), _lib.stream_handle()),
+                   "sbe_gamma")
+        return ge, gh
+
+    def offdiag(self, w, ne, nh, P, VC, g3):
+        nk = self.nk[w]
+        x = torch.empty((nk, nk), dtype=CDTYPE, device=self.device)
+        De = torch.empty((2 * nk + 1, nk), dtype=torch.float64, device=self.device)
+        Dh = torch.empty_like(De)
+        g = torch.as_tensor(g3, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_offdiag(self.handle, w, _lib.ptr(ne), _lib.ptr(nh), _lib.ptr(P),
+                                        _lib.ptr(VC), _lib.ptr(g), _lib.ptr(x), _lib.ptr(De),
+                                        _lib.ptr(Dh), _lib.stream_handle()), "sbe_offdiag")
+        return x, De, Dh
+
+    def phonon_rates(self, w, ne, nh, VC, E1D, WinE, WoutE, WinH, WoutH):
+        _lib.check(self.lib.sbe_phonon_rates(self.handle, w, _lib.ptr(ne), _lib.ptr(nh),
+                                             _lib.ptr(VC), _lib.ptr(E1D), _lib.ptr(WinE),
+                                             _lib.ptr(WoutE), _lib.ptr(WinH), _lib.ptr(WoutH),
+                                             _lib.stream_handle()), "sbe_phonon_rates")
+
+    def sources(self, w, P, C, D, ne, nh):
+        nr = 2 * self.nk[w] + 2
+        out = [torch.empty(nr, dtype=CDTYPE, device=self.device) for _ in range(5)]
+        _lib.check(self.lib.sbe_sources(self.handle, w, _lib.ptr(P), _lib.ptr(C), _lib.ptr(D),
+                                        _lib.ptr(ne), _lib.ptr(nh), *[_lib.ptr(o) for o in out],
+                                        _lib.stream_handle()), "sbe_sources")
+        return out
+
+    def prop2qw(self, w, RR, fields4):
+        nr = 2 * self.nk[w] + 2
+        out = torch.empty((4, nr), dtype=CDTYPE, device=self.device)
+        _lib.check(self.lib.sbe_prop2qw(self.handle, w, _lib.ptr(RR), RR.numel(),
+                                        _lib.ptr(fields4), _lib.ptr(out), _lib.stream_handle()),
+                   "sbe_prop2qw")
+        return out
+
+    def qw2prop(self, w, RR, src5, plasmonics):
+        out = torch.empty((5, RR.numel()), dtype=CDTYPE, device=self.device)
+        _lib.check(self.lib.sbe_qw2prop(self.handle, w, _lib.ptr(RR), RR.numel(), _lib.ptr(src5),
+                                        _lib.ptr(out), int(bool(plasmonics)),
+                                        _lib.stream_handle()), "sbe_qw2prop")
+        return out
+
+    # ---- whole-batch steps -------------------------------------------------
+    def leapfrog_step(self, state9, Ek, dt, src_out):
+        arr = (ctypes.c_void_p * 9)(*[t.data_ptr() for t in state9])
+        for t in state9:
+            _lib.ptr(t)
+        _lib.check(self.lib.sbe_leapfrog_step(self.handle, arr, _lib.ptr(Ek), float(dt),
+                                              _lib.ptr(src_out), _lib.stream_handle()),
+                   "sbe_leapfrog_step")
+
+    def rk4_step(self, P, C, D, Ek0, dEk, dt, src_out, precision=_lib.PREC_FP64):
+        _lib.check(self.lib.sbe_rk4_step(self.handle, _lib.ptr(P), _lib.ptr(C), _lib.ptr(D),
+                                         _lib.ptr(Ek0), _lib.ptr(dEk), float(dt), int(precision),
+                                         _lib.ptr(src_out), _lib.stream_handle()), "sbe_rk4_step")
+
+    def rhs(self, P, C, D, Ek, precision=_lib.PREC_FP64):
+        dP = torch.empty_like(P)
+        dC = torch.empty_like(C)
+        dD = torch.empty_like(D)
+        _lib.check(self.lib.sbe_rhs(self.handle, _lib.ptr(P), _lib.ptr(C), _lib.ptr(D),
+                                    _lib.ptr(Ek), int(precision), _lib.ptr(dP), _lib.ptr(dC),
+                                    _lib.ptr(dD), _lib.stream_handle()), "sbe_rhs")
+        return dP, dC, dD

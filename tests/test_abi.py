@@ -1,0 +1,48 @@
+"""The C-ABI library loads without a GPU and exports every declared entry point."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    with open(os.path.join(ROOT, "include", "sbe_gb300.h")) as f:
+        src = f.read()
+    return sorted(set(re.findall(r"^\s*(?:const char\*|int)\s+(sbe_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from pulsesuite_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    return _lib.LIB_PATH
+
+
+def test_header_matches_binding_list():
+    from pulsesuite_gb300 import _lib
+    assert _declared() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_all_symbols(lib_path):
+    lib = ctypes.CDLL(lib_path)
+    for name in _declared():
+        assert hasattr(lib, name), name
+
+
+def test_constants_and_errors_without_gpu(lib_path):
+    from pulsesuite_gb300 import _lib
+    from pulsesuite_gb300.constants import E0, EPS0, HBAR, KB, ME0
+    lib = _lib.load(lib_path)
+    out = (ctypes.c_double * 5)()
+    assert lib.sbe_constants(out) == 0
+    assert list(out) == [HBAR, E0, EPS0, ME0, KB]
+    # host-side argument checks return an error code instead of touching the device
+    assert lib.sbe_constants(None) == 1
+    assert b"null" in lib.sbe_last_error()
+    assert lib.sbe_dpdt(0, None, None, None, None, None, None, None, None, None, None, None) == 1
+    assert lib.sbe_ctx_create(None, 0, None, None) == 1

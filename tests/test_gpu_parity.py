@@ -1,0 +1,261 @@
+"""FP64 GPU path vs the reference's golden vectors and the oracle (needs a GPU).
+
+Every call goes through the C ABI of libsbe_gb300 (ctypes, torch device
+buffers).  Tolerances are relative Frobenius errors; the FP64 GPU path sums in a
+different order from NumPy, and the K0 series of the reference loses ~8 digits
+to cancellation near x = 9 (its Chi1D entries there agree to ~1e-9), so
+screening-dependent results use 1e-10.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import sbe_oracle as O  # noqa: E402
+from tests.conftest import golden  # noqa: E402
+
+TIGHT = 1e-12
+SCREEN = 1e-10
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pulsesuite_gb300 import build
+    build.build()
+
+
+def dev(x, dtype=None):
+    t = torch.as_tensor(np.ascontiguousarray(x))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda().contiguous()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+MAT = dict(me=0.067 * O.ME0, mh=0.45 * O.ME0, gap=1.52 * O.E0, HO=100e-3 * O.E0, Delta0=6e-9,
+           gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR,
+           Gph=3e-3 * O.E0 / O.HBAR)
+ALL = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
+           LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
+
+
+def ctx_for(nk, L, nw=1, temp=77.0, flags=None):
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    specs = [WireSpec(nk=nk, L=L, temp=temp, wire_index=w + 1, flags=dict(flags or ALL), **MAT)
+             for w in range(nw)]
+    return WireContext(specs)
+
+
+@pytest.mark.parametrize("nk", [7, 16, 30])
+def test_rhs_functions_vs_golden(nk):
+    from pulsesuite_gb300 import SBEs
+    g = golden(f"kernels_nk{nk}")
+    H = (g["Heh_e1l1f0"], g["Hee_e1l1f0"], g["Hhh_e1l1f0"])
+    dP = SBEs.dpdt(g["C"], g["D"], g["P"], *H, g["GamE"], g["GamH"], g["OffP"])
+    dC = SBEs.dCdt(g["C"], g["D"], g["P"], *H, g["GamE"], g["GamH"], g["OffP"])
+    dD = SBEs.dDdt(g["C"], g["D"], g["P"], *H, g["GamE"], g["GamH"], g["OffP"])
+    assert rel(dP, g["dP"]) < TIGHT
+    assert rel(dC, g["dC"]) < TIGHT
+    assert rel(dD, g["dD"]) < TIGHT
+
+
+@pytest.mark.parametrize("nk", [7, 16, 30])
+def test_calch_vs_golden(nk):
+    from pulsesuite_gb300 import SBEs
+    g = golden(f"kernels_nk{nk}")
+    for exc in (0, 1):
+        for lf in (0, 1):
+            for fp in (0, 1):
+                tag = f"e{exc}l{lf}f{fp}"
+                out = [np.zeros((nk, nk), complex) for _ in range(3)]
+                SBEs.calc_h(g["Meh"], g["Wee"], g["Whh"], g["C"], g["D"], g["P"], g["VC"], *out,
+                            g["Ee"], g["Eh"], float(g["gap"]), exc, lf, fp)
+                for a, n in zip(out, ("Heh", "Hee", "Hhh")):
+                    assert rel(a, g[f"{n}_{tag}"]) < TIGHT, (tag, n)
+
+
+@pytest.mark.parametrize("nk", [8, 16, 30])
+def test_tables_vs_golden(nk):
+    g = golden(f"coulomb_nk{nk}")
+    ph = golden(f"phonon_nk{nk}")
+    de = golden(f"dephasing_nk{nk}")
+    qo = golden(f"qwoptics_nk{nk}")
+    c = ctx_for(nk, float(g["L"]), temp=float(ph["temp"]))
+    assert rel(host(c.table(0, "kr")), g["kr"]) < 1e-15
+    assert rel(host(c.table(0, "r")), g["r"]) == 0.0
+    v0 = host(c.table(0, "V0"))
+    for i, n in enumerate(("Veh0", "Vee0", "Vhh0")):
+        assert rel(v0[i], g[n][:, 0]) < 1e-13, n
+    chi = host(c.table(0, "Chi1D"))
+    assert rel(chi[0], g["Chi1De"][:, 0]) < SCREEN
+    assert rel(chi[1], g["Chi1Dh"][:, 0]) < SCREEN
+    assert rel(host(c.table(0, "EP")), ph["EP"]) < 1e-13
+    assert rel(host(c.table(0, "HP")), ph["HP"]) < 1e-13
+    maps = host(c.table(0, "maps"))
+    for i, n in enumerate(("k_p_q", "k_m_q", "k1p", "k1p_m_q", "k1", "k1_m_q")):
+        assert np.array_equal(maps[i], de[n]), n
+    xx = host(c.table(0, "xexh"))
+    assert rel(xx[0], de["xe"]) < 1e-14 and rel(xx[1], de["xh"]) < 1e-14
+    assert rel(host(c.table(0, "window")), qo["window"]) < 1e-14
+    assert rel(host(c.table(0, "Expikr")), qo["Expikr"]) < 1e-14
+
+
+@pytest.mark.parametrize("nk", [8, 16, 30])
+def test_screening_vs_golden(nk):
+    g = golden(f"coulomb_nk{nk}")
+    for scr in (0, 1):
+        c = ctx_for(nk, float(g["L"]), flags=dict(ALL, Screened=bool(scr)))
+        for i in (0, 1):
+            VC, E1D = c.screened_arrays(0, dev(g[f"ne{i}"]), dev(g[f"nh{i}"]))
+            assert rel(host(VC), g[f"VC{i}_s{scr}"]) < SCREEN
+            assert rel(host(E1D), g[f"E1D{i}_s{scr}"]) < SCREEN
+
+
+@pytest.mark.parametrize("nk", [8, 16, 30])
+def test_dephasing_vs_golden(nk):
+    g = golden(f"dephasing_nk{nk}")
+    cg = golden(f"coulomb_nk{nk}")
+    c = ctx_for(nk, float(cg["L"]))
+    ge, gh = c.gamma(0, dev(g["ne"]), dev(g["nh"]), dev(g["VC"]))
+    assert rel(host(ge), g["GamE"]) < TIGHT
+    assert rel(host(gh), g["GamH"]) < TIGHT
+    x, De, Dh = c.offdiag(0, dev(g["ne"]), dev(g["nh"]), dev(g["P"]), dev(g["VC"]), g["g"])
+    assert rel(host(De), g["De"]) < TIGHT
+    assert rel(host(Dh), g["Dh"]) < TIGHT
+    assert rel(host(x), g["OffP"]) < TIGHT
+
+
+@pytest.mark.parametrize("nk", [8, 16, 30])
+def test_phonon_rates_vs_golden(nk):
+    g = golden(f"phonon_nk{nk}")
+    cg = golden(f"coulomb_nk{nk}")
+    c = ctx_for(nk, float(cg["L"]), temp=float(g["temp"]))
+    w = [dev(g[n]) for n in ("WinE0", "WoutE0", "WinH0", "WoutH0")]
+    c.phonon_rates(0, dev(g["ne"].astype(complex)), dev(g["nh"].astype(complex)), dev(g["VC"]),
+                   dev(g["E1D"]), *w)
+    for t, n in zip(w, ("WinE", "WoutE", "WinH", "WoutH")):
+        assert rel(host(t), g[n]) < TIGHT, n
+
+
+@pytest.mark.parametrize("nk", [8, 16, 30])
+def test_sources_and_resampling_vs_golden(nk):
+    g = golden(f"qwoptics_nk{nk}")
+    c = ctx_for(nk, float(g["L"]), nw=4)
+    rho_scale = 2.0 * O.E0 * float(g["ehint"]) / float(g["area"])
+    for w in (1, 2, 3, 4):
+        Px, Py, Pz, re, rh = c.sources(w - 1, dev(g["P"]), dev(g["C"]), dev(g["D"]),
+                                       dev(g["ne"]), dev(g["nh"]))
+        for a, n in zip((Px, Py, Pz), ("Px", "Py", "Pz")):
+            assert rel(O.fftg(host(a)), g[f"{n}_w{w}"]) < TIGHT, (w, n)
+        assert rel(O.fftg(host(re)) / rho_scale, g["re"]) < TIGHT
+        assert rel(O.fftg(host(rh)) / rho_scale, g["rh"]) < TIGHT
+    RR = dev(g["RR"])
+    f4 = dev(np.stack([g["Exx"], g["Eyy"], g["Ezz"], g["Vrr"]]))
+    Ek = host(c.prop2qw(0, RR, f4))
+    for i, n in enumerate(("Ex", "Ey", "Ez", "Vr")):
+        assert rel(Ek[i], g[n]) < 1e-13, n
+    for pl in (0, 1):
+        src = np.stack([O.ifftg(g[f"q2p_in_{n}_{pl}"]) for n in ("Px", "Py", "Pz", "re", "rh")])
+        out = host(c.qw2prop(0, RR, dev(src), pl))
+        for i, n in enumerate(("Pxx", "Pyy", "Pzz", "RhoE", "RhoH")):
+            assert rel(out[i], g[f"q2p_{n}_{pl}"]) < 1e-13, (pl, n)
+
+
+SOLVER_FLAGS = dict(Optics=1, Excitons=1, EHs=0, Screened=1, Phonon=1, DCTrans=0, LF=1,
+                    FreePot=0, DiagDph=1, OffDiagDph=1, Recomb=0, ignorewire=0)
+
+
+def test_solver_leapfrog_vs_golden():
+    """Three reference QWCalculator steps on two wires (SBESolver drop-in)."""
+    from pulsesuite_gb300 import SBEs
+    g = golden("solver_step")
+    prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
+               mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
+               epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR, Edc=0.0,
+               jmax=100000, ntmax=100000)
+    rr = g["rr"]
+    s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
+                       flags=SOLVER_FLAGS)
+    assert s.Nk == int(g["nk"])
+    assert rel(s.kr, g["kr"]) == 0.0
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        setattr(s, nm, g["init_" + nm])
+    dt = float(g["dt"])
+    for n in range(3):
+        for w in (1, 2):
+            outs = [np.zeros(len(rr), complex) for _ in range(4)]
+            s.QWCalculator(g[f"s{n}_Exx"], g[f"s{n}_Eyy"], g[f"s{n}_Ezz"],
+                           np.zeros(len(rr), complex), rr, None, dt, w, *outs, [False], [False])
+            for a, nm in zip(outs, ("Pxx", "Pyy", "Pzz", "Rho")):
+                assert rel(a, g[f"s{n}_w{w}_{nm}"]) < SCREEN, (n, w, nm)
+        for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+            assert rel(getattr(s, nm), g[f"s{n}_{nm}"]) < SCREEN, (n, nm)
+    s.close()
+
+
+def _seeded_state(rng, nk):
+    z = rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))
+    q, _ = np.linalg.qr(z)
+    C = (q * rng.uniform(0, 0.1, nk)) @ q.conj().T
+    z = rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))
+    q, _ = np.linalg.qr(z)
+    D = (q * rng.uniform(0, 0.1, nk)) @ q.conj().T
+    P = 1e-3 * (rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))) / np.sqrt(2)
+    return P, C, D
+
+
+def _uniform_field_k(wire, E):
+    """Wire-k-space field of a spatially uniform field E along y (Prop2QW of a
+    constant): E * FFTG(window)."""
+    wk = O.fftg(wire.window)
+    z = np.zeros_like(wk)
+    return [z, E * wk, z]
+
+
+@pytest.mark.parametrize("nk", [16, 34])
+def test_batched_rhs_and_rk4_vs_oracle(nk):
+    """Full RHS (preparation included) and one RK4 step, 3 wires, FP64 path."""
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    nw = 3
+    c = ctx_for(nk, L, nw=nw)
+    rng = np.random.default_rng(5)
+    wires = [O.Wire(nk, L, MAT, ALL) for _ in range(nw)]
+    states = [_seeded_state(rng, nk) for _ in range(nw)]
+    fields = [_uniform_field_k(wires[w], 1e7 * (w + 1)) for w in range(nw)]
+    dfields = [_uniform_field_k(wires[w], -3e5 * (w + 1)) for w in range(nw)]
+    P = c.pack([s[0] for s in states])
+    C = c.pack([s[1] for s in states])
+    D = c.pack([s[2] for s in states])
+    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
+    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    dP, dC, dD = c.rhs(P, C, D, Ek)
+    for w in range(nw):
+        rP, rC, rD, _ = wires[w].rhs(*states[w], *fields[w], w + 1)
+        assert rel(host(c.mat(dP, w)), rP) < SCREEN
+        assert rel(host(c.mat(dC, w)), rC) < SCREEN
+        assert rel(host(c.mat(dD, w)), rD) < SCREEN
+    dt = 0.1e-15
+    src = c.zeros_r(5)
+    c.rk4_step(P, C, D, Ek, dEk, dt, src)
+    for w in range(nw):
+        ref = wires[w].rk4_step(*states[w], fields[w], dfields[w], dt, w + 1)
+        assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
+        assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
+        assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
+        s5 = host(c.rvec(src, w, 5))
+        for i in range(5):
+            assert rel(O.fftg(s5[i]), ref[3 + i]) < SCREEN, (w, i)
