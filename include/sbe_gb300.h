@@ -155,6 +155,14 @@ int sbe_rk4_step(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0
 int sbe_rhs(SbeCtx* ctx, const double* P, const double* C, const double* D, const double* Ek,
             int precision, double* dP, double* dC, double* dD, void* stream);
 
+/* ---- diagnostics ------------------------------------------------------------ */
+/* Diagnostic entry, no counterpart in the reference: out[b] = op(A[b]) op(B[b])
+ * for a batch of Nk x Nk matrices through the tcgen05 split-precision engine
+ * (op: 0 N, 1 T, 2 conj, 3 conj-transpose).  complex_mode 0 uses the real parts
+ * only (out imaginary parts are 0).  Nk must be a multiple of 8.               */
+int sbe_tc_selftest(int nk, int nbatch, const double* A, const double* B, int opA, int opB,
+                    int complex_mode, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,7 @@ EXPORTS = (
     "sbe_ctx_layout", "sbe_ctx_table", "sbe_dpdt", "sbe_dCdt", "sbe_dDdt", "sbe_calch",
     "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_sources",
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
+    "sbe_tc_selftest",
 )
 
 
@@ -79,6 +80,7 @@ def load(path=LIB_PATH):
         "sbe_leapfrog_step": [P, P, P, Dbl, P, P],
         "sbe_rk4_step": [P, P, P, P, P, P, Dbl, I, P, P],
         "sbe_rhs": [P, P, P, P, P, I, P, P, P, P],
+        "sbe_tc_selftest": [I, I, P, P, I, I, I, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

@@ -123,7 +123,8 @@ class WireContext:
         return flat[o:o + ncomp * nr].view(ncomp, nr)
 
     def pack(self, mats):
-        return torch.cat([m.reshape(-1) for m in mats]).to(self.device, CDTYPE).contiguous()
+        flat = [torch.as_tensor(m).reshape(-1).to(self.device, CDTYPE) for m in mats]
+        return torch.cat(flat).contiguous()
 
     # ---- tables ------------------------------------------------------------
     def table(self, w, name):

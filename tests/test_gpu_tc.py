@@ -1,0 +1,76 @@
+"""tcgen05 split-precision GEMM engine vs an FP64 product (needs a GPU).
+
+The engine stores each operand as FP16 hi + lo planes after a per-matrix
+power-of-two scaling and accumulates hi*hi + hi*lo + lo*hi in FP32.  Expected
+relative Frobenius error ~1e-7; the bar is 1e-6.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pulsesuite_gb300 import build
+    build.build()
+
+
+def _op(x, op):
+    if op == 1:
+        return x.transpose(-1, -2)
+    if op == 2:
+        return x.conj()
+    if op == 3:
+        return x.conj().transpose(-1, -2)
+    return x
+
+
+def _run(nk, nb, A, B, opA, opB, cplx):
+    from pulsesuite_gb300 import _lib
+    lib = _lib.load()
+    out = torch.empty((nb, nk, nk), dtype=torch.complex128, device="cuda")
+    _lib.check(lib.sbe_tc_selftest(nk, nb, _lib.ptr(A), _lib.ptr(B), opA, opB, int(cplx),
+                                   _lib.ptr(out), _lib.stream_handle()), "sbe_tc_selftest")
+    return out
+
+
+def _rel(a, b):
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
+@pytest.mark.parametrize("nk", [64, 128, 256, 384])
+def test_complex_products_all_ops(nk):
+    g = torch.Generator(device="cpu").manual_seed(nk)
+    nb = 2
+    A = (torch.randn((nb, nk, nk), generator=g, dtype=torch.float64)
+         + 1j * torch.randn((nb, nk, nk), generator=g, dtype=torch.float64)).cuda()
+    B = (torch.randn((nb, nk, nk), generator=g, dtype=torch.float64)
+         + 1j * torch.randn((nb, nk, nk), generator=g, dtype=torch.float64)).cuda()
+    A[1] *= 1e-21   # second batch entry at Hamiltonian scale (J)
+    B[1] *= 3e-3    # and coherence scale
+    for opA in range(4):
+        for opB in range(4):
+            ref = _op(A, opA) @ _op(B, opB)
+            out = _run(nk, nb, A, B, opA, opB, True)
+            for b in range(nb):
+                e = _rel(out[b], ref[b])
+                assert e < TOL, (nk, opA, opB, b, e)
+
+
+@pytest.mark.parametrize("nk", [64, 256])
+def test_real_mode(nk):
+    g = torch.Generator(device="cpu").manual_seed(7 + nk)
+    A = torch.randn((1, nk, nk), generator=g, dtype=torch.float64).to(torch.complex128).cuda()
+    B = torch.randn((1, nk, nk), generator=g, dtype=torch.float64).to(torch.complex128).cuda()
+    out = _run(nk, 1, A, B, 0, 0, False)
+    ref = A.real @ B.real
+    assert _rel(out[0].real, ref[0]) < TOL
+    assert float(out.imag.abs().max()) == 0.0
