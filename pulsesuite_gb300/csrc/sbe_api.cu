@@ -510,12 +510,13 @@ int sbe_rhs(SbeCtx* c, const double* P, const double* C, const double* D, const 
   if (!c || !P || !C || !D || !Ek || !dP || !dC || !dD) return fail(SBE_ERR_ARG, "sbe_rhs: null");
   cudaStream_t s = as_stream(stream);
   const double2 *p = (const double2*)P, *cc = (const double2*)C, *d = (const double2*)D;
-  prep_frozen(c, p, cc, d, s);
-  launch_calch_ctx(c, p, cc, d, (const double2*)Ek, s);
   if (precision == SBE_PREC_FP64) {
+    prep_frozen(c, p, cc, d, s);
+    launch_calch_ctx(c, p, cc, d, (const double2*)Ek, s);
     launch_rhs64_ctx(c, p, cc, d, (double2*)dP, (double2*)dC, (double2*)dD, s);
   } else if (precision == SBE_PREC_MIXED) {
-    int rc = sbe::rhs_mixed(c, p, cc, d, (double2*)dP, (double2*)dC, (double2*)dD, s);
+    int rc = sbe::rhs_mixed(c, p, cc, d, (const double2*)Ek, (double2*)dP, (double2*)dC,
+                            (double2*)dD, s);
     if (rc) return rc;
   } else {
     return fail(SBE_ERR_ARG, "sbe_rhs: unknown precision");

@@ -107,8 +107,13 @@ void add_rates(const double* wrate, int nk, double* a, double* b, double* cc, do
                cudaStream_t s);
 // sbe_tc.cu (mixed precision)
 void mixed_free(SbeCtx* c);
-int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, double2* dP,
-              double2* dC, double2* dD, cudaStream_t s);
+int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, const double2* Ek,
+              double2* dP, double2* dC, double2* dD, cudaStream_t s);
+void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
+                           cudaStream_t s);
+void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int transpose,
+                   const int* e, __half* dst, int mat, int nplanes, int real_only,
+                   cudaStream_t s);
 int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
               const double2* dEk, double dt, double2* src, cudaStream_t s);
 void launch_rk4_axpy(SbeCtx* c, int stage, double dt, double2* P, double2* C, double2* D,

@@ -1,5 +1,6 @@
 // Internal declarations shared by the CUDA translation units of libsbe_gb300.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>

@@ -221,8 +221,126 @@ __global__ void k_offdiag_D64(const WireDev* wires, int w_only, const double2* n
   D[(long long)qi * nk + k] = acc * kPi / kHbar;
 }
 
+// FP32 version of the off-diagonal dephasing sums for the mixed-precision path.
+// On the reference grid (parabolic bands, kr = dkr (j - j0), j0 = dnk + 1/2)
+// the energy differences are exact integer multiples of one constant:
+//   a-a:  E = 2 c_a dkr^2 q (k - p + q)
+//   a-b:  E = dkr^2 q [c_a (2k - 2j0 + q) + c_b (2p - 2j0 + q)]
+// so u = E/(hbar g) is formed without cancellation (the a-b constants are split
+// into an 11-bit head, whose products with the integers |2k + c| < 2^12 are
+// exact in FP32, and a tail).  Lorentz(E, b) = (1/(pi b)) / (1 + u^2).  The a-a
+// kernel depends on k - p only, so it is tabulated per q in shared memory.  One
+// block per (k tile, q, wire x {De, Dh}); the (1 - n_k) / n_k split of the
+// occupation product makes the p-sums two dot products per thread.
+__device__ inline void split12(double v, float* hi, float* lo) {
+  int ex;
+  double m = frexp(v, &ex);                 // v = m 2^ex, 0.5 <= |m| < 1
+  double h = ldexp(rint(ldexp(m, 11)), ex - 11);
+  *hi = (float)h;
+  *lo = (float)(v - h);
+}
+
+__global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const double2* ne,
+                                                     const double2* nh, const double* vs,
+                                                     double* De, double* Dh) {
+  const int wi = blockIdx.z >> 1, which = blockIdx.z & 1;   // 0 De, 1 Dh
+  const WireDev W = wires[wi];
+  const int nk = W.nk;
+  const int qi = blockIdx.y;
+  if (qi > 2 * nk) return;
+  const int q = qi - nk;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ float sh[];
+  float* na = sh;              // |n_a|
+  float* nb = na + nk;         // |n_b|
+  float* Ltab = nb + nk;       // 2nk entries: m - mlo
+  float* Aa = Ltab + 2 * nk;   // per-p weights (a-a)
+  float* Ba = Aa + nk;
+  float* Ab = Ba + nk;         // per-p weights (a-b)
+  float* Bb = Ab + nk;
+  const double2* pa = (which == 0 ? ne : nh) + W.off_vec;
+  const double2* pb = (which == 0 ? nh : ne) + W.off_vec;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    na[i] = (float)hypot(pa[i].x, pa[i].y);
+    nb[i] = (float)hypot(pb[i].x, pb[i].y);
+  }
+  const double ma = which == 0 ? W.me : W.mh, mbm = which == 0 ? W.mh : W.me;
+  const double ca = kHbar * kHbar / (2.0 * ma), cb = kHbar * kHbar / (2.0 * mbm);
+  const double dk2 = W.dkr * W.dkr;
+  const double g_aa = which == 0 ? W.gam_eh : W.gam_e;   // quirk: De uses gam_eh, Dh gam_e
+  const double b_aa = kHbar * g_aa, b_ab = kHbar * W.gam_h;
+  const int aq = q < 0 ? -q : q;
+  const double* v = vs + 3 * W.off_vec;
+  double vaa = 0.0, vab = 0.0;
+  if (aq >= 1 && aq < nk) {
+    double x = v[(which == 0 ? 1 : 2) * nk + aq], y = v[aq];
+    vaa = x * x;
+    vab = y * y;
+  }
+  const int mlo = -nk + 1 + q;
+  const float alpha = (float)(2.0 * ca * dk2 * (double)q / b_aa);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * nk; i += blockDim.x) {
+    float u = alpha * (float)(mlo + i);
+    Ltab[i] = 1.0f / (1.0f + u * u);
+  }
+  for (int p = threadIdx.x; p < nk; p += blockDim.x) {
+    int pm = p - q, pp = p + q;
+    bool okm = pm >= 0 && pm < nk, okp = pp >= 0 && pp < nk;
+    float a_pm = okm ? na[pm] : 0.f, b_pp = okp ? nb[pp] : 0.f;
+    Aa[p] = okm ? a_pm * (1.f - na[p]) : 0.f;
+    Ba[p] = okm ? (1.f - a_pm) * na[p] : 0.f;
+    Ab[p] = okp ? b_pp * (1.f - nb[p]) : 0.f;
+    Bb[p] = okp ? (1.f - b_pp) * nb[p] : 0.f;
+  }
+  __syncthreads();
+  if (k >= nk) return;
+  double acc = 0.0;
+  if (k + q >= 0 && k + q < nk) {
+    const float nak = na[k];
+    if (vaa != 0.0) {
+      int plo = max(q + 1, 0), phi = min(q + nk - 1, nk - 1);
+      float sa = 0.f, sb = 0.f;
+      const int base = k + q - mlo;   // Ltab index of m = k - p + q is base - p
+      for (int p = plo; p <= phi; ++p) {
+        float L = Ltab[base - p];
+        sa = fmaf(L, Aa[p], sa);
+        sb = fmaf(L, Ba[p], sb);
+      }
+      acc += vaa / (kHbar * b_aa) * ((double)(1.f - nak) * sa + (double)nak * sb);
+    }
+    if (vab != 0.0) {
+      int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
+      const int c = -2 * W.dnk - 1 + q;
+      float bah, bal, bbh, bbl;
+      split12(ca * dk2 / b_ab, &bah, &bal);
+      split12(cb * dk2 / b_ab, &bbh, &bbl);
+      const float fk = (float)(2 * k + c);
+      const float ka = bah * fk, kal = bal * fk;   // exact head product + tail
+      const float fq = (float)q;
+      float sa = 0.f, sb = 0.f;
+      for (int p = plo; p <= phi; ++p) {
+        const float fp = (float)(2 * p + c);
+        float s = (ka + bbh * fp) + fmaf(bbl, fp, kal);
+        float u = fq * s;
+        float L = __frcp_rn(fmaf(u, u, 1.0f));
+        sa = fmaf(L, Ab[p], sa);
+        sb = fmaf(L, Bb[p], sb);
+      }
+      acc += vab / (kHbar * b_ab) * ((double)(1.f - nak) * sa + (double)nak * sb);
+    }
+  }
+  double* D = (which == 0 ? De : Dh) + W.off_dd;
+  D[(long long)qi * nk + k] = acc;
+}
+
 void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaStream_t s) {
-  (void)fp32;
+  if (fp32 && w_only < 0 && !g3) {
+    size_t smem = sizeof(float) * 8 * (size_t)c->nk_max;
+    k_offdiag_D32<<<dim3((c->nk_max + 127) / 128, 2 * c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
+        c->d_wires, c->ne, c->nh, c->vs, c->De, c->Dh);
+    return;
+  }
   dim3 g((c->nk_max + 127) / 128, 2 * (2 * c->nk_max + 1), w_only >= 0 ? 1 : c->nw);
   double g0 = 0, g1 = 0, g2 = 0;
   int use_g = 0;

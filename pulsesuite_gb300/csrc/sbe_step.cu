@@ -299,6 +299,7 @@ void launch_sources(SbeCtx* c, const double2* P, const double2* C, const double2
     launch_sources_gemm64(c, b, s);
   }
   int nb = w_only >= 0 ? 1 : c->nw;
+  (void)nb;
   k_src_reduce<<<dim3((c->nr_max + 127) / 128, nb), 128, 0, s>>>(c->d_wires, w_only, c->expikr,
                                                                 c->G, c->tot_kr, c->window, src);
   k_src_final<<<nb, 256, 0, s>>>(c->d_wires, w_only, c->r, ne, nh, src);
@@ -580,4 +581,13 @@ int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* 
   return cuda_check(cudaGetLastError(), "qw2prop");
 }
 
+}  // namespace sbe
+
+namespace sbe {
+void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
+                           cudaStream_t s) {
+  k_src_reduce<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, -1, c->expikr,
+                                                                   c->G, c->tot_kr, c->window, src);
+  k_src_final<<<c->nw, 256, 0, s>>>(c->d_wires, -1, c->r, ne, nh, src);
+}
 }  // namespace sbe

@@ -88,18 +88,468 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
   k_exponents<<<(nbatch + 127) / 128, 128, 0, s>>>(nbatch, mx, e, add, sum);
 }
 
-void mixed_free(SbeCtx* c) { (void)c; }
+// ---------------------------------------------------------------------------
+// Mixed-precision workspace of a context (uniform Nk and flags over its wires).
+//
+// Commutator planes: 14 matrices x 4 planes x Nw x Nk x Nk (FP16):
+//   0 P, 1 P^T, 2 C, 3 C^T, 4 D, 5 D^T            (state, exponent eS)
+//   6 Heh, 7 Heh^T, 8 Hee', 9 Hee'^T, 10 Hhh', 11 Hhh'^T,
+//   12 Hee' + i hbar B, 13 Hhh' + i hbar A         (Hamiltonians, exponent eH)
+// (' = diagonal removed; A, B = off-diagonal dephasing matrices).
+// Exchange: Toeplitz planes T_n (3 x 2 x Nw x Nk x Nk) and sheared state planes
+// S_n (3 x 2 x Nw x 4Nk x Nk).  Sources: E^T planes (4 x Nw x Nr x Nk).
+struct Mixed {
+  int nk = 0, nw = 0, nr = 0;
+  __half *planes = nullptr, *tpl = nullptr, *spl = nullptr, *epl = nullptr;
+  int* ints = nullptr;   // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
+  unsigned* mx = nullptr;
+  double2 *dgE = nullptr, *dgH = nullptr;
+  CUtensorMap mapA, mapB, mapTA, mapSB, mapEB;
+  int* eS() { return ints; }
+  int* eH() { return ints + nw; }
+  int* eT() { return ints + 2 * nw; }
+  int* eE() { return ints + 3 * nw; }
+  int* esc() { return ints + 4 * nw; }
+  int* esx() { return ints + 5 * nw; }
+  int* ess() { return ints + 6 * nw; }
+  int* err() { return ints + 7 * nw; }
+};
 
-int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, double2* dP,
-              double2* dC, double2* dD, cudaStream_t s) {
-  (void)c; (void)P; (void)C; (void)D; (void)dP; (void)dC; (void)dD; (void)s;
-  return fail(SBE_ERR_UNSUPPORTED, "mixed precision path not built");
+enum { M_P = 0, M_PT, M_C, M_CT, M_D, M_DT, M_EH, M_EHT, M_EE, M_EET, M_HH, M_HHT, M_EEX, M_HHX };
+
+void mixed_free(SbeCtx* c) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  if (!m) return;
+  cudaFree(m->planes);
+  cudaFree(m->tpl);
+  cudaFree(m->spl);
+  cudaFree(m->epl);
+  cudaFree(m->ints);
+  cudaFree(m->mx);
+  cudaFree(m->dgE);
+  delete m;
+  c->mixed = nullptr;
+}
+
+// E^T planes: Y[r][k] = Expikr[k][r] (|E| = 1, exponent 13).
+__global__ void k_eplanes(const WireDev* wires, const double2* expikr, __half* dst, int nw) {
+  const WireDev W = wires[blockIdx.z];
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int r = blockIdx.y;
+  if (k >= W.nk || r >= W.nr) return;
+  double2 v = expikr[W.off_kr + (long long)k * W.nr + r];
+  const long long plane = (long long)nw * W.nr * W.nk;
+  long long o = (long long)blockIdx.z * W.nr * W.nk + (long long)r * W.nk + k;
+  double vr = ldexp(v.x, 13), vi = ldexp(v.y, 13);
+  __half rh = __double2half(vr), ih = __double2half(vi);
+  dst[o] = rh;
+  dst[plane + o] = __double2half(vr - (double)__half2float(rh));
+  dst[2 * plane + o] = ih;
+  dst[3 * plane + o] = __double2half(vi - (double)__half2float(ih));
+}
+
+__global__ void k_fill_int(int* p, int n, int v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
+  if (c->mixed) return SBE_OK;
+  const int nk = c->wires[0].nk, nw = c->nw;
+  for (int w = 1; w < nw; ++w)
+    if (c->wires[w].nk != nk || c->wires[w].flags != c->wires[0].flags)
+      return fail(SBE_ERR_UNSUPPORTED,
+                  "mixed path: all wires of a context must share Nk and flags (group by Nk)");
+  if (nk % 8) return fail(SBE_ERR_UNSUPPORTED, "mixed path: Nk must be a multiple of 8");
+  Mixed* m = new Mixed();
+  m->nk = nk;
+  m->nw = nw;
+  m->nr = 2 * nk + 2;
+  const size_t mm = (size_t)nk * nk;
+  bool ok = cudaMalloc(&m->planes, sizeof(__half) * 14 * 4 * nw * mm) == cudaSuccess &&
+            cudaMalloc(&m->tpl, sizeof(__half) * 3 * 2 * nw * mm) == cudaSuccess &&
+            cudaMalloc(&m->spl, sizeof(__half) * 3 * 2 * nw * 4 * mm) == cudaSuccess &&
+            cudaMalloc(&m->epl, sizeof(__half) * 4 * nw * (size_t)m->nr * nk) == cudaSuccess &&
+            cudaMalloc(&m->ints, sizeof(int) * 8 * nw) == cudaSuccess &&
+            cudaMalloc(&m->mx, sizeof(unsigned) * nw) == cudaSuccess &&
+            cudaMalloc(&m->dgE, sizeof(double2) * 2 * nw * nk) == cudaSuccess;
+  if (!ok) {
+    c->mixed = m;
+    mixed_free(c);
+    return fail(SBE_ERR_OOM, "mixed path: workspace allocation failed");
+  }
+  m->dgH = m->dgE + (size_t)nw * nk;
+  cudaMemsetAsync(m->ints, 0, sizeof(int) * 8 * nw, s);
+  TcPlanes pl{m->planes, 14, 4, nw, nk, nk};
+  TcPlanes tp{m->tpl, 3, 2, nw, nk, nk};
+  TcPlanes sp{m->spl, 3, 2, nw, 4 * nk, nk};
+  TcPlanes ep{m->epl, 1, 4, nw, m->nr, nk};
+  int rc = tc_make_maps(pl, pl, &m->mapA, &m->mapB);
+  if (!rc) rc = tc_make_maps(tp, sp, &m->mapTA, &m->mapSB);
+  CUtensorMap dummy;
+  if (!rc) rc = tc_make_maps(tp, ep, &dummy, &m->mapEB);
+  if (rc) {
+    c->mixed = m;
+    mixed_free(c);
+    return rc;
+  }
+  k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(c->d_wires, c->expikr, m->epl, nw);
+  k_fill_int<<<(nw + 127) / 128, 128, 0, s>>>(m->eE(), nw, 13);
+  c->mixed = m;
+  return cuda_check(cudaGetLastError(), "mixed workspace");
+}
+
+// generic per-batch max over several arrays (scaled by fac)
+__global__ void k_absmax_f(const double2* X, long long per_batch, long long bstride, double fac,
+                           unsigned* out) {
+  const int b = blockIdx.y;
+  const double2* x = X + (long long)b * bstride;
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_batch;
+       i += (long long)gridDim.x * blockDim.x) {
+    double2 v = x[i];
+    m = fmaxf(m, (float)(fac * fmax(fabs(v.x), fabs(v.y))));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + b, __float_as_uint(m));
+}
+
+static void absmax_into(const double2* X, long long per, int nw, double fac, unsigned* mx,
+                        cudaStream_t s) {
+  int blocks = (int)std::min<long long>((per + 255) / 256, 128);
+  k_absmax_f<<<dim3(blocks, nw), 256, 0, s>>>(X, per, per, fac, mx);
+}
+
+// Toeplitz exchange planes T_n[t][t'] = vs_n(|t - t'|) (t != t'), real.
+__global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const int* e,
+                                  __half* dst, int nw) {
+  const int b = blockIdx.z / 3, n = blockIdx.z % 3;
+  const WireDev W = wires[b];
+  const int nk = W.nk;
+  int tp = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = blockIdx.y;
+  if (tp >= nk || t >= nk) return;
+  int d = t > tp ? t - tp : tp - t;
+  double v = (d == 0) ? 0.0 : ldexp(vs[3 * W.off_vec + n * nk + d], e[b]);
+  const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
+  __half* base = dst + (long long)n * 2 * plane + (long long)b * mm + (long long)t * nk + tp;
+  __half h = __double2half(v);
+  base[0] = h;
+  base[plane] = __double2half(v - (double)__half2float(h));
+}
+
+__global__ void k_vs_max(const WireDev* wires, const double* vs, unsigned* mx) {
+  const WireDev W = wires[blockIdx.x];
+  float m = 0.f;
+  for (int i = threadIdx.x; i < 3 * W.nk; i += blockDim.x)
+    m = fmaxf(m, (float)fabs(vs[3 * W.off_vec + i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.x, __float_as_uint(m));
+}
+
+// Sheared state planes: row 2 dd + c (dd = d + Nk - 1, c = re / im), column t':
+// S[2dd + c][t'] = component c of X[t' + d][t'] (zero outside the matrix).
+// The exchange sum  H[t][t+d] = sum_t' V(|t - t'|) X[t' + d][t']  is then T S.
+__global__ void k_shear_planes(int nk, int nw, const double2* X, const int* e, __half* dst,
+                               int mat) {
+  const int b = blockIdx.z;
+  const int tp = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = blockIdx.y;   // 0 .. 4nk-1
+  if (tp >= nk) return;
+  const int dd = row >> 1, c = row & 1;
+  const int d = dd - (nk - 1);
+  double v = 0.0;
+  if (dd < 2 * nk - 1 && tp + d >= 0 && tp + d < nk) {
+    double2 x = X[(long long)b * nk * nk + (long long)(tp + d) * nk + tp];
+    v = ldexp(c ? x.y : x.x, e[b]);
+  }
+  const long long rows = 4ll * nk, plane = (long long)nw * rows * nk;
+  __half* base = dst + (long long)mat * 2 * plane + (long long)b * rows * nk + (long long)row * nk + tp;
+  __half h = __double2half(v);
+  base[0] = h;
+  base[plane] = __double2half(v - (double)__half2float(h));
+}
+
+// H = Meh + diagonal energies + direct Coulomb terms (SBEs.py:1044-1131 without
+// the exchange sums, which the exchange GEMM adds).
+__global__ void k_h_init(const WireDev* wires, const double2* Ek, const double* vs,
+                         const double* Ee, const double* Eh, const double2* tr, double2* Heh,
+                         double2* Hee, double2* Hhh) {
+  const WireDev W = wires[blockIdx.z];
+  const int nk = W.nk;
+  int k1 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k2 = blockIdx.y;
+  if (k1 >= nk || k2 >= nk) return;
+  double2 heh = make_double2(0, 0);
+  if (W.flags & SBE_F_OPTICS) {
+    int q = k1 - k2;
+    if (q < 0) q += W.nr;
+    const double2* ek = Ek + 3 * W.off_r;
+    double2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
+    double xcv = W.dcv * ((k2 & 1) ? -1.0 : 1.0);
+    double2 t1 = cscale(ex, -W.ehint * xcv);
+    double2 t2 = cscale(cscale(ey, W.ehint * W.dcv), (double)W.yw);
+    double2 t3 = cscale(cscale(ez, W.ehint * -W.dcv), (double)W.zsign);
+    heh = csub(csub(t1, t2), t3);
+  }
+  double2 hee = make_double2(k1 == k2 ? Ee[W.off_vec + k1] + W.gap : 0.0, 0.0);
+  double2 hhh = make_double2(k1 == k2 ? Eh[W.off_vec + k1] : 0.0, 0.0);
+  const bool exc = (W.flags & SBE_F_EXCITONS) != 0, lf = (W.flags & SBE_F_LF) != 0;
+  int d = k1 - k2;
+  if (exc && lf && d != 0) {
+    const double* v = vs + 3 * W.off_vec;
+    const double2* t = tr + 4 * W.off_vec;
+    int ad = d < 0 ? -d : d;
+    double2 trC = t[d + nk], trCm = t[-d + nk], trD = t[2 * nk + d + nk], trDm = t[2 * nk - d + nk];
+    hee.x += v[nk + ad] * trC.x - v[ad] * trDm.x;
+    hee.y += v[nk + ad] * trC.y - v[ad] * trDm.y;
+    hhh.x += v[2 * nk + ad] * trD.x - v[ad] * trCm.x;
+    hhh.y += v[2 * nk + ad] * trD.y - v[ad] * trCm.y;
+  }
+  long long o = W.off_mat + (long long)k1 * nk + k2;
+  Heh[o] = heh;
+  Hee[o] = hee;
+  Hhh[o] = hhh;
+}
+
+__global__ void k_peel(const WireDev* wires, double2* Hee, double2* Hhh, double2* dgE,
+                       double2* dgH) {
+  const WireDev W = wires[blockIdx.y];
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= W.nk) return;
+  long long o = W.off_mat + (long long)k * W.nk + k;
+  long long v = (long long)blockIdx.y * W.nk + k;
+  dgE[v] = Hee[o];
+  dgH[v] = Hhh[o];
+  Hee[o] = make_double2(0, 0);
+  Hhh[o] = make_double2(0, 0);
+}
+
+// planes with an added i * f * M (M real-valued complex array), used for
+// Hee' + i hbar B and Hhh' + i hbar A.
+__global__ void k_planes_add(const double2* X, const double2* Madd, double f, int nk,
+                             const int* e, __half* dst, int mat, int nw) {
+  const int b = blockIdx.z;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  int r = blockIdx.y;
+  if (c >= nk || r >= nk) return;
+  const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
+  long long o = (long long)r * nk + c;
+  double2 v = X[(long long)b * mm + o];
+  double2 a = Madd[(long long)b * mm + o];
+  v.x -= f * a.y;
+  v.y += f * a.x;
+  double sc = ldexp(1.0, e[b]);
+  double vr = v.x * sc, vi = v.y * sc;
+  __half* base = dst + (long long)mat * 4 * plane + (long long)b * mm + o;
+  __half rh = __double2half(vr), ih = __double2half(vi);
+  base[0] = rh;
+  base[plane] = __double2half(vr - (double)__half2float(rh));
+  base[2 * plane] = ih;
+  base[3 * plane] = __double2half(vi - (double)__half2float(ih));
+}
+
+__global__ void k_add_int(int n, const int* a, const int* b, int* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] + b[i];
+}
+
+static int gemm(Mixed* m, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, int cplx,
+                int nterms, const tc::Term* t, int kskip, const tc::EpiArgs& e, cudaStream_t s) {
+  tc::GemmDesc d{};
+  d.M = M;
+  d.N = N;
+  d.K = K;
+  d.complex_mode = cplx;
+  d.nterms = nterms;
+  for (int i = 0; i < nterms; ++i) d.t[i] = t[i];
+  d.batch = m->nw;
+  d.kskip = kskip;
+  d.nk_shear = m->nk;
+  return tc_gemm_launch(d, A, B, e, s);
+}
+
+static void exponents_from_mx(Mixed* m, int* e, cudaStream_t s) {
+  k_exponents<<<(m->nw + 127) / 128, 128, 0, s>>>(m->nw, m->mx, e, nullptr, nullptr);
+}
+
+// Per-step set-up of the mixed path: the frozen preparation (screening, rates,
+// dephasing matrices with the FP32 Lorentzian sums) and the Toeplitz planes.
+static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  launch_prep_scalar(c, C, D, s);
+  launch_gamma(c, -1, s);
+  if (c->any_offdiag) {
+    launch_offdiag_D(c, -1, nullptr, true, s);
+    launch_offdiag_AB(c, -1, s);
+  } else {
+    cudaMemsetAsync(c->dA, 0, sizeof(double2) * c->tot_mat, s);
+    cudaMemsetAsync(c->dB, 0, sizeof(double2) * c->tot_mat, s);
+  }
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * m->nw, s);
+  k_vs_max<<<m->nw, 256, 0, s>>>(c->d_wires, c->vs, m->mx);
+  exponents_from_mx(m, m->eT(), s);
+  k_toeplitz_planes<<<dim3((m->nk + 127) / 128, m->nk, 3 * m->nw), 128, 0, s>>>(
+      c->d_wires, c->vs, m->eT(), m->tpl, m->nw);
+  return cuda_check(cudaGetLastError(), "mixed prep");
+}
+
+// One stage RHS of every wire at state (P, C, D) and wire-k field Ek.
+static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                       const double2* Ek, double2* dP, double2* dC, double2* dD,
+                       cudaStream_t s) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  const int nk = m->nk, nw = m->nw;
+  const long long mm = (long long)nk * nk;
+  const WireDev& W0 = c->wires[0];
+  // state exponent and planes
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
+  absmax_into(P, mm, nw, 1.0, m->mx, s);
+  absmax_into(C, mm, nw, 1.0, m->mx, s);
+  absmax_into(D, mm, nw, 1.0, m->mx, s);
+  exponents_from_mx(m, m->eS(), s);
+  const double2* st[3] = {P, C, D};
+  for (int i = 0; i < 3; ++i) {
+    launch_planes(st[i], mm, nk, nw, 0, m->eS(), m->planes, 2 * i, 4, 0, s);
+    launch_planes(st[i], mm, nk, nw, 1, m->eS(), m->planes, 2 * i + 1, 4, 0, s);
+  }
+  // Hamiltonians: Meh + diagonal + direct terms, then the exchange GEMMs
+  launch_traces(c, C, D, s);
+  k_h_init<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, Ek, c->vs, c->Ee, c->Eh,
+                                                          c->tr, c->Heh, c->Hee, c->Hhh);
+  int rc = SBE_OK;
+  if (W0.flags & SBE_F_EXCITONS) {
+    k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
+    double2* Hs[3] = {c->Heh, c->Hee, c->Hhh};
+    for (int n = 0; n < 3; ++n) {
+      k_shear_planes<<<dim3((nk + 127) / 128, 4 * nk, nw), 128, 0, s>>>(nk, nw, st[n], m->eS(),
+                                                                        m->spl, n);
+      tc::Term t{n, n, 0, 0, 1};
+      tc::EpiArgs e{};
+      e.kind = tc::EPI_EXCH;
+      e.which = n;
+      e.out = Hs[n];
+      e.out_bstride = mm;
+      e.escale = m->esx();
+      e.nk = nk;
+      e.lf = (W0.flags & SBE_F_LF) ? 1 : 0;
+      e.err = m->err();
+      rc = gemm(m, m->mapTA, m->mapSB, nk, 4 * nk, nk, 0, 1, &t, 1, e, s);
+      if (rc) return rc;
+    }
+  }
+  k_peel<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->Hee, c->Hhh, m->dgE, m->dgH);
+  // Hamiltonian exponent and planes
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
+  absmax_into(c->Heh, mm, nw, 1.0, m->mx, s);
+  absmax_into(c->Hee, mm, nw, 1.0, m->mx, s);
+  absmax_into(c->Hhh, mm, nw, 1.0, m->mx, s);
+  if (c->any_offdiag) {
+    absmax_into(c->dA, mm, nw, 2.0 * kHbar, m->mx, s);
+    absmax_into(c->dB, mm, nw, 2.0 * kHbar, m->mx, s);
+  }
+  exponents_from_mx(m, m->eH(), s);
+  const double2* hs[3] = {c->Heh, c->Hee, c->Hhh};
+  for (int i = 0; i < 3; ++i) {
+    launch_planes(hs[i], mm, nk, nw, 0, m->eH(), m->planes, M_EH + 2 * i, 4, 0, s);
+    launch_planes(hs[i], mm, nk, nw, 1, m->eH(), m->planes, M_EH + 2 * i + 1, 4, 0, s);
+  }
+  dim3 pg((nk + 127) / 128, nk, nw);
+  k_planes_add<<<pg, 128, 0, s>>>(c->Hee, c->dB, kHbar, nk, m->eH(), m->planes, M_EEX, nw);
+  k_planes_add<<<pg, 128, 0, s>>>(c->Hhh, c->dA, kHbar, nk, m->eH(), m->planes, M_HHX, nw);
+  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eH(), m->esc());
+  // commutator GEMMs (term lists follow dpdt/dCdt/dDdt, SBEs.py:1942-2625)
+  const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_DT, M_EH, 0, 0, -1},
+                          {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_CT, 0, 0, -1}};
+  const tc::Term tC[4] = {{M_C, M_EE, 0, 0, 1}, {M_EET, M_CT, 0, 0, -1},
+                          {M_PT, M_EH, 1, 0, 1}, {M_EH, M_PT, 1, 0, -1}};
+  const tc::Term tD[4] = {{M_D, M_HH, 0, 0, 1}, {M_HHT, M_DT, 0, 0, -1},
+                          {M_P, M_EHT, 1, 0, 1}, {M_EHT, M_P, 1, 0, -1}};
+  const tc::Term* tl[3] = {tP, tC, tD};
+  double2* outs[3] = {dP, dC, dD};
+  for (int w = 0; w < 3; ++w) {
+    tc::EpiArgs e{};
+    e.kind = tc::EPI_RHS;
+    e.which = w;
+    e.out = outs[w];
+    e.out_bstride = mm;
+    e.escale = m->esc();
+    e.X = st[w];
+    e.Heh = c->Heh;
+    e.dgE = m->dgE;
+    e.dgH = m->dgH;
+    e.gamE = c->gamE;
+    e.gamH = c->gamH;
+    e.nk = nk;
+    e.err = m->err();
+    rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, 4, tl[w], 0, e, s);
+    if (rc) return rc;
+  }
+  return cuda_check(cudaGetLastError(), "mixed stage");
+}
+
+// Sources of the new state through the engine: G = [P; C; conj(D)] E.
+static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                         double2* src, cudaStream_t s) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  const int nk = m->nk, nw = m->nw;
+  const long long mm = (long long)nk * nk;
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
+  absmax_into(P, mm, nw, 1.0, m->mx, s);
+  absmax_into(C, mm, nw, 1.0, m->mx, s);
+  absmax_into(D, mm, nw, 1.0, m->mx, s);
+  exponents_from_mx(m, m->eS(), s);
+  const double2* st[3] = {P, C, D};
+  for (int i = 0; i < 3; ++i) launch_planes(st[i], mm, nk, nw, 0, m->eS(), m->planes, 2 * i, 4, 0, s);
+  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
+  for (int i = 0; i < 3; ++i) {
+    tc::Term t{2 * i, 0, i == 2 ? 1 : 0, 0, 1};
+    tc::EpiArgs e{};
+    e.kind = tc::EPI_RAW;
+    e.out = c->G + i * c->tot_kr;
+    e.out_bstride = (long long)nk * m->nr;
+    e.escale = m->ess();
+    e.err = m->err();
+    int rc = gemm(m, m->mapA, m->mapEB, nk, m->nr, nk, 1, 1, &t, 0, e, s);
+    if (rc) return rc;
+  }
+  launch_sources_reduce(c, c->ne, c->nh, src, s);
+  return cuda_check(cudaGetLastError(), "mixed sources");
+}
+
+int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, const double2* Ek,
+              double2* dP, double2* dC, double2* dD, cudaStream_t s) {
+  // sbe_rhs has run the FP64 preparation; the mixed call redoes it with the
+  // FP32 dephasing sums so that it measures exactly what the RK4 stages use.
+  int rc = mixed_ensure(c, s);
+  if (rc) return rc;
+  rc = mixed_prep(c, C, D, s);
+  if (rc) return rc;
+  return mixed_stage(c, P, C, D, Ek, dP, dC, dD, s);
 }
 
 int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
               const double2* dEk, double dt, double2* src, cudaStream_t s) {
-  (void)c; (void)P; (void)C; (void)D; (void)Ek0; (void)dEk; (void)dt; (void)src; (void)s;
-  return fail(SBE_ERR_UNSUPPORTED, "mixed precision path not built");
+  int rc = mixed_ensure(c, s);
+  if (rc) return rc;
+  rc = mixed_prep(c, C, D, s);
+  if (rc) return rc;
+  const long long n = c->tot_mat;
+  const double frac[4] = {0.0, 0.5, 0.5, 1.0};
+  for (int st = 1; st <= 4; ++st) {
+    const double2 *xp = P, *xc = C, *xd = D;
+    if (st > 1) {
+      xp = c->xs;
+      xc = c->xs + n;
+      xd = c->xs + 2 * n;
+    }
+    launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
+    rc = mixed_stage(c, xp, xc, xd, c->ekst, c->dP, c->dC, c->dD, s);
+    if (rc) return rc;
+    launch_rk4_axpy(c, st, dt, P, C, D, s);
+  }
+  launch_relax_norm(c, C, D, dt, false, s);
+  return mixed_sources(c, P, C, D, src, s);
 }
 
 }  // namespace sbe

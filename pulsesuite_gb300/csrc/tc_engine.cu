@@ -158,8 +158,8 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
     const long long mb = (long long)b * nk * nk;
     const double ih = 1.0 / 1.0545718176461565e-34;
     const double2* X = e.X + mb;
-    const double* gE = e.dgE + (long long)b * nk;
-    const double* gH = e.dgH + (long long)b * nk;
+    const double2* gE = e.dgE + (long long)b * nk;
+    const double2* gH = e.dgH + (long long)b * nk;
     double2* o = e.out + mb + (long long)m * nk;
 #pragma unroll 4
     for (int j = 0; j < 16; ++j) {
@@ -167,19 +167,20 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
       if (n >= nk) break;
       double gr = re[j] * sc, gi = im[j] * sc;        // G = accumulated products (J)
       double2 x = X[(long long)m * nk + n];
-      double de;
       double2 v;
       if (e.which == 0) {
         // dP[kh=m][ke=n]: (G + (hh[kh] + ee[ke]) P + Heh[ke][kh])/(i hbar) - (gE+gH) P
         double2 h = e.Heh[mb + (long long)n * nk + m];
-        de = gH[m] + gE[n];
-        double ar = gr + de * x.x + h.x, ai = gi + de * x.y + h.y;
+        double2 de = make_double2(gH[m].x + gE[n].x, gH[m].y + gE[n].y);
+        double2 dx = cmuld(de, x);
+        double ar = gr + dx.x + h.x, ai = gi + dx.y + h.y;
         double gam = e.gamE[(long long)b * nk + n] + e.gamH[(long long)b * nk + m];
         v = make_double2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
       } else {
-        const double* g = (e.which == 1) ? gE : gH;
-        de = g[n] - g[m];                              // (e[k2] - e[k1]) X
-        double ar = gr + de * x.x, ai = gi + de * x.y;
+        const double2* g = (e.which == 1) ? gE : gH;
+        double2 de = make_double2(g[n].x - g[m].x, g[n].y - g[m].y);   // (e[k2] - e[k1]) X
+        double2 dx = cmuld(de, x);
+        double ar = gr + dx.x, ai = gi + dx.y;
         v = make_double2(ai * ih, -ar * ih);
       }
       o[n] = v;

@@ -52,8 +52,8 @@ struct EpiArgs {
   // RHS epilogue inputs (per batch strides = nk*nk or nk)
   const double2* X;           // the state matrix whose diagonal terms are added (P, C or D)
   const double2* Heh;         // FP64 Heh (dP only)
-  const double* dgE;          // diagonal energies of Hee (per batch, nk)
-  const double* dgH;          // diagonal energies of Hhh
+  const double2* dgE;         // diagonal of Hee (per batch, nk), peeled off the GEMM operand
+  const double2* dgH;         // diagonal of Hhh
   const double* gamE;
   const double* gamH;
   // exchange epilogue

@@ -1,0 +1,114 @@
+"""Mixed-precision (tcgen05) RHS and RK4 step vs the FP64 GPU path (needs a GPU).
+
+Bars (the benchmark spec's tolerances): RHS relative Frobenius error <= 1e-6;
+observables after a pulse segment <= 1e-5 relative to the FP64 run.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import sbe_oracle as O  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pulsesuite_gb300 import build
+    build.build()
+
+
+MAT = dict(me=0.067 * O.ME0, mh=0.45 * O.ME0, gap=1.52 * O.E0, HO=100e-3 * O.E0, Delta0=6e-9,
+           gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR,
+           Gph=3e-3 * O.E0 / O.HBAR)
+ALL = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
+           LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
+
+
+def make_ctx(nk, nw, temp=300.0, flags=None):
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    specs = [WireSpec(nk=nk, L=L, temp=temp, wire_index=w + 1, flags=dict(flags or ALL), **MAT)
+             for w in range(nw)]
+    return WireContext(specs), L
+
+
+def seeded(rng, nk, pscale=1e-3):
+    def herm(scale):
+        z = rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))
+        q, _ = np.linalg.qr(z)
+        return (q * rng.uniform(0, scale, nk)) @ q.conj().T
+    P = pscale * (rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))) / np.sqrt(2)
+    return P, herm(0.1), herm(0.1)
+
+
+def fields(ctx, amps):
+    out = []
+    for w, a in enumerate(amps):
+        wk = ctx.table(w, "window_k").cpu().numpy()
+        z = np.zeros_like(wk)
+        out.append(np.stack([z, a * wk, z]))
+    return torch.as_tensor(np.concatenate([f.reshape(-1) for f in out])).cuda()
+
+
+def rel(a, b):
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
+@pytest.mark.parametrize("nk", [64, 128, 256])
+def test_mixed_rhs_vs_fp64(nk):
+    from pulsesuite_gb300 import _lib
+    nw = 3
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(nk)
+    st = [seeded(rng, nk) for _ in range(nw)]
+    P = ctx.pack([s[0] for s in st])
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    Ek = fields(ctx, [1e7, 3e7, 5e6])
+    r64 = ctx.rhs(P, C, D, Ek, _lib.PREC_FP64)
+    rmx = ctx.rhs(P, C, D, Ek, _lib.PREC_MIXED)
+    for a, b, n in zip(rmx, r64, ("dP", "dC", "dD")):
+        for w in range(nw):
+            e = rel(ctx.mat(a, w), ctx.mat(b, w))
+            assert e < 1e-6, (nk, n, w, e)
+
+
+@pytest.mark.parametrize("nk", [64, 128])
+def test_mixed_rk4_pulse_vs_fp64(nk):
+    """40 RK4 steps through the rising edge of a pulse, mixed vs FP64."""
+    from pulsesuite_gb300 import _lib
+    nw = 2
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(3)
+    st = [seeded(rng, nk, 1e-4) for _ in range(nw)]
+    states = {}
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        P = ctx.pack([s[0] for s in st])
+        C = ctx.pack([s[1] for s in st])
+        D = ctx.pack([s[2] for s in st])
+        src = ctx.zeros_r(5)
+        dt = 0.1e-15
+        tau = 30e-15
+        w0 = (1.52 * O.E0 + 20e-3 * O.E0) / O.HBAR
+        for n in range(40):
+            t = -2 * tau + n * dt
+            e0 = 2e7 * np.exp(-t * t / tau ** 2) * np.cos(w0 * t)
+            t1 = t + dt
+            e1 = 2e7 * np.exp(-t1 * t1 / tau ** 2) * np.cos(w0 * t1)
+            Ek0 = fields(ctx, [e0, 0.5 * e0])
+            dEk = fields(ctx, [e1 - e0, 0.5 * (e1 - e0)])
+            ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
+        states[prec] = (P, C, D, src)
+    P64, C64, D64, s64 = states[_lib.PREC_FP64]
+    Pm, Cm, Dm, sm = states[_lib.PREC_MIXED]
+    for w in range(nw):
+        ne64 = ctx.mat(C64, w).diagonal()
+        nem = ctx.mat(Cm, w).diagonal()
+        assert rel(nem, ne64) < 1e-5
+        assert rel(ctx.mat(Pm, w), ctx.mat(P64, w)) < 1e-5
+        assert rel(ctx.rvec(sm, w, 5)[:3], ctx.rvec(s64, w, 5)[:3]) < 1e-5
