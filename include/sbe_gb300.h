@@ -155,6 +155,27 @@ int sbe_rk4_step(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0
 int sbe_rhs(SbeCtx* ctx, const double* P, const double* C, const double* D, const double* Ek,
             int precision, double* dP, double* dC, double* dD, void* stream);
 
+/* ---- CUDA graph of one step (no counterpart in the reference) -------------- */
+/* Capture one sbe_rk4_step with the given (fixed) buffers into a CUDA graph on a
+ * private stream and instantiate it; *n_kernels receives the number of kernel
+ * nodes (the launches of one step).  Call once uncaptured first so that the
+ * mixed-precision workspace exists.  Replays read Ek0/dEk and update P, C, D and
+ * src_out in place.                                                             */
+typedef struct SbeGraph SbeGraph;
+int sbe_rk4_graph_create(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0,
+                         const double* dEk, double dt, int precision, double* src_out,
+                         SbeGraph** out, long long* n_kernels);
+int sbe_graph_launch(SbeGraph* g, void* stream);
+int sbe_graph_destroy(SbeGraph* g);
+
+/* ---- kernel timing (no counterpart in the reference) ------------------------ */
+/* enable != 0: record CUDA events around the engine launches of category
+ * 0 commutator GEMMs, 1 exchange GEMMs, 2 source GEMMs, 3 FP32 dephasing sums.
+ * sbe_ctx_profile_read synchronises, returns total ms and launch count of a
+ * category and clears it.                                                      */
+int sbe_ctx_profile(SbeCtx* ctx, int enable);
+int sbe_ctx_profile_read(SbeCtx* ctx, int category, double* total_ms, long long* launches);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Diagnostic entry, no counterpart in the reference: out[b] = op(A[b]) op(B[b])
  * for a batch of Nk x Nk matrices through the tcgen05 split-precision engine

@@ -158,6 +158,30 @@ def k0_truncated(x):
     return math.sqrt(PI / (2.0 * x)) * math.exp(-x)
 
 
+def k0_truncated_vec(x):
+    """Array form of k0_truncated (same operations per element, with the series
+    stopped per element at the first |term| < 1e-15 as the loop above does)."""
+    x = np.asarray(x, dtype=float)
+    out = np.where(x > 100.0, 0.0, 0.0)
+    small = x < 1e-10
+    ser = (x >= 1e-10) & (x < 2.0)
+    asy = (x >= 2.0) & (x <= 100.0)
+    xs = np.where(ser, x, 1.0)
+    x2 = xs * xs
+    res = -np.log(0.5 * xs) - EULER
+    term = np.ones_like(xs)
+    live = np.ones_like(xs, dtype=bool)
+    for k in range(1, 20):
+        term = np.where(live, term * 0.25 * x2 / (k * k), term)
+        res = np.where(live, res + term * (1.0 / k - EULER), res)
+        live = live & ~(np.abs(term) < 1e-15)
+    xa = np.where(asy, x, 1.0)
+    out = np.where(ser, res, out)
+    out = np.where(asy, np.sqrt(PI / (2.0 * xa)) * np.exp(-xa), out)
+    out = np.where(small, 23.0, out)
+    return out
+
+
 def _dfact2(n):
     r = 1.0
     while n > 1:
@@ -252,7 +276,7 @@ def vint(Q, y, a1, a2, Delta0):
     mult = a1 * a2 / PI * (y[1] - y[0]) ** 2
     rr = np.sqrt((yy[:, None] - yy[None, :]) ** 2 + Delta0 ** 2)
     ex = np.exp(-(a1 * yy[:, None]) ** 2 - (a2 * yy[None, :]) ** 2)
-    k0 = np.vectorize(k0_truncated)(dk * rr)
+    k0 = k0_truncated_vec(dk * rr)
     return float(np.sum(ex * mult * k0))
 
 
@@ -268,10 +292,28 @@ def coulomb_tables(g, c, epsr, Delta0, me, mh):
     nq = len(Qr)
     need = np.unique(kkp[(kkp >= 0) & (kkp < nq)])
     tabs = {}
+    fast = len(r) > 130
+    if fast:
+        # large grids: K0t depends on |i - j| only (up to the rounding of y_i - y_j),
+        # so it is evaluated once per distance and gathered; the double sum itself
+        # is kept as written
+        ny = len(r)
+        n1, n2 = ny // 4, 3 * ny // 4
+        yy = r[n1:n2 + 1]
+        idx = np.abs(np.arange(len(yy))[:, None] - np.arange(len(yy))[None, :])
+        rdist = np.sqrt((yy - yy[0]) ** 2 + Delta0 ** 2)
     for name, (a1, a2) in (("eh", (ae, ah)), ("ee", (ae, ae)), ("hh", (ah, ah))):
         t = np.zeros(nq)
+        if fast:
+            ex = np.exp(-(a1 * yy[:, None]) ** 2 - (a2 * yy[None, :]) ** 2)
+            mult = a1 * a2 / PI * (r[1] - r[0]) ** 2
+            kmin = (a1 + a2) / 4.0
         for j in need:
-            t[j] = pref * vint(Qr[j], r, a1, a2, Delta0)
+            if fast:
+                kd = k0_truncated_vec(max(abs(Qr[j]), kmin) * rdist)
+                t[j] = pref * float(np.sum(ex * mult * kd[idx]))
+            else:
+                t[j] = pref * vint(Qr[j], r, a1, a2, Delta0)
         tabs[name] = t
     valid = (kkp >= 0) & (kkp < nq)
     idx = np.where(valid, kkp, 0)

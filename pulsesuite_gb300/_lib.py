@@ -27,7 +27,8 @@ EXPORTS = (
     "sbe_ctx_layout", "sbe_ctx_table", "sbe_dpdt", "sbe_dCdt", "sbe_dDdt", "sbe_calch",
     "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_sources",
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
-    "sbe_tc_selftest",
+    "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
+    "sbe_ctx_profile", "sbe_ctx_profile_read",
 )
 
 
@@ -81,6 +82,11 @@ def load(path=LIB_PATH):
         "sbe_rk4_step": [P, P, P, P, P, P, Dbl, I, P, P],
         "sbe_rhs": [P, P, P, P, P, I, P, P, P, P],
         "sbe_tc_selftest": [I, I, P, P, I, I, I, P, P],
+        "sbe_rk4_graph_create": [P, P, P, P, P, P, Dbl, I, P, P, P],
+        "sbe_graph_launch": [P, P],
+        "sbe_graph_destroy": [P],
+        "sbe_ctx_profile": [P, I],
+        "sbe_ctx_profile_read": [P, I, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

@@ -213,6 +213,12 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
 int sbe_ctx_destroy(SbeCtx* c) {
   if (!c) return SBE_OK;
   int rc = SBE_OK;
+  for (auto& v : c->prof_ev)
+    for (auto& pr : v) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->d_wires && cudaFree(c->d_wires) != cudaSuccess) rc = SBE_ERR_CUDA;
   if (c->arena && cudaFree(c->arena) != cudaSuccess) rc = SBE_ERR_CUDA;
   sbe::mixed_free(c);
@@ -570,6 +576,93 @@ int sbe_rk4_step(SbeCtx* c, double* P, double* C, double* D, const double* Ek0, 
   launch_relax_norm(c, cc, d, dt, false, s);
   launch_sources(c, p, cc, d, c->ne, c->nh, (double2*)src_out, s);
   return cuda_check(cudaGetLastError(), "sbe_rk4_step");
+}
+
+// ---- CUDA graph of one step -------------------------------------------------
+struct SbeGraph {
+  cudaGraphExec_t exec = nullptr;
+};
+
+int sbe_rk4_graph_create(SbeCtx* c, double* P, double* C, double* D, const double* Ek0,
+                         const double* dEk, double dt, int precision, double* src_out,
+                         SbeGraph** out, long long* n_kernels) {
+  if (!c || !out) return fail(SBE_ERR_ARG, "sbe_rk4_graph_create: null");
+  *out = nullptr;
+  if (c->prof) return fail(SBE_ERR_ARG, "sbe_rk4_graph_create: disable profiling first");
+  cudaStream_t cs;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(SBE_ERR_CUDA, "sbe_rk4_graph_create: stream");
+  int rc = SBE_OK;
+  if (precision == SBE_PREC_MIXED) rc = sbe::mixed_prepare(c, cs);
+  if (rc == SBE_OK) rc = cuda_check(cudaStreamSynchronize(cs), "graph warm-up");
+  cudaGraph_t g = nullptr;
+  if (rc == SBE_OK) {
+    rc = cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (rc == SBE_OK) {
+      int rc2 = sbe_rk4_step(c, P, C, D, Ek0, dEk, dt, precision, src_out, (void*)cs);
+      rc = cuda_check(cudaStreamEndCapture(cs, &g), "end capture");
+      if (rc2) rc = rc2;
+    }
+  }
+  SbeGraph* sg = nullptr;
+  if (rc == SBE_OK) {
+    size_t n = 0;
+    cudaGraphGetNodes(g, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(g, nodes.data(), &n);
+    long long kc = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kc;
+    }
+    if (n_kernels) *n_kernels = kc;
+    sg = new SbeGraph();
+    rc = cuda_check(cudaGraphInstantiate(&sg->exec, g, 0), "graph instantiate");
+    if (rc) {
+      delete sg;
+      sg = nullptr;
+    }
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  *out = sg;
+  return rc;
+}
+
+int sbe_graph_launch(SbeGraph* g, void* stream) {
+  if (!g || !g->exec) return fail(SBE_ERR_ARG, "sbe_graph_launch: null graph");
+  return cuda_check(cudaGraphLaunch(g->exec, as_stream(stream)), "sbe_graph_launch");
+}
+
+int sbe_graph_destroy(SbeGraph* g) {
+  if (!g) return SBE_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  delete g;
+  return SBE_OK;
+}
+
+// ---- kernel timing ----------------------------------------------------------
+int sbe_ctx_profile(SbeCtx* c, int enable) {
+  if (!c) return fail(SBE_ERR_ARG, "sbe_ctx_profile: null");
+  c->prof = enable ? 1 : 0;
+  return SBE_OK;
+}
+
+int sbe_ctx_profile_read(SbeCtx* c, int category, double* total_ms, long long* launches) {
+  if (!c || category < 0 || category > 3) return fail(SBE_ERR_ARG, "sbe_ctx_profile_read");
+  double tot = 0.0;
+  for (auto& pr : c->prof_ev[category]) {
+    float ms = 0.f;
+    cudaEventSynchronize(pr.second);
+    cudaEventElapsedTime(&ms, pr.first, pr.second);
+    tot += ms;
+    c->ev_pool.push_back(pr.first);
+    c->ev_pool.push_back(pr.second);
+  }
+  if (total_ms) *total_ms = tot;
+  if (launches) *launches = (long long)c->prof_ev[category].size();
+  c->prof_ev[category].clear();
+  return SBE_OK;
 }
 
 }  // extern "C"

@@ -47,7 +47,47 @@ struct SbeCtx {
 
   int any_offdiag = 0;                   // some wire has OffDiagDph on
   void* mixed = nullptr;                 // mixed-precision workspace (sbe_tc.cu)
+
+  // kernel timing (sbe_ctx_profile): event pairs per category, and a pool
+  int prof = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[4];
+  std::vector<cudaEvent_t> ev_pool;
 };
+
+namespace sbe {
+// Records a pair of events around the launches in its scope when profiling is on.
+struct ProfScope {
+  SbeCtx* c;
+  int cat;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  static cudaEvent_t take(SbeCtx* c) {
+    cudaEvent_t e;
+    if (!c->ev_pool.empty()) {
+      e = c->ev_pool.back();
+      c->ev_pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
+  ProfScope(SbeCtx* c_, int cat_, cudaStream_t s_) : c(c_), cat(cat_), s(s_) {
+    if (c->prof) {
+      a = take(c);
+      b = take(c);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEventRecord(b, s);
+      c->prof_ev[cat].push_back({a, b});
+    }
+  }
+};
+int mixed_prepare(SbeCtx* c, cudaStream_t s);
+int tc_gemm_init();
+}  // namespace sbe
 
 namespace sbe {
 // sbe_tables.cu

@@ -380,7 +380,10 @@ static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_
   launch_prep_scalar(c, C, D, s);
   launch_gamma(c, -1, s);
   if (c->any_offdiag) {
-    launch_offdiag_D(c, -1, nullptr, true, s);
+    {
+      ProfScope ps(c, 3, s);
+      launch_offdiag_D(c, -1, nullptr, true, s);
+    }
     launch_offdiag_AB(c, -1, s);
   } else {
     cudaMemsetAsync(c->dA, 0, sizeof(double2) * c->tot_mat, s);
@@ -434,6 +437,7 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
       e.nk = nk;
       e.lf = (W0.flags & SBE_F_LF) ? 1 : 0;
       e.err = m->err();
+      ProfScope ps(c, 1, s);
       rc = gemm(m, m->mapTA, m->mapSB, nk, 4 * nk, nk, 0, 1, &t, 1, e, s);
       if (rc) return rc;
     }
@@ -482,6 +486,7 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
     e.gamH = c->gamH;
     e.nk = nk;
     e.err = m->err();
+    ProfScope ps(c, 0, s);
     rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, 4, tl[w], 0, e, s);
     if (rc) return rc;
   }
@@ -510,11 +515,18 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     e.out_bstride = (long long)nk * m->nr;
     e.escale = m->ess();
     e.err = m->err();
+    ProfScope ps(c, 2, s);
     int rc = gemm(m, m->mapA, m->mapEB, nk, m->nr, nk, 1, 1, &t, 0, e, s);
     if (rc) return rc;
   }
   launch_sources_reduce(c, c->ne, c->nh, src, s);
   return cuda_check(cudaGetLastError(), "mixed sources");
+}
+
+int mixed_prepare(SbeCtx* c, cudaStream_t s) {
+  int rc = mixed_ensure(c, s);
+  if (rc) return rc;
+  return tc_gemm_init();
 }
 
 int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, const double2* Ek,

@@ -406,16 +406,24 @@ int tc_make_maps(const TcPlanes& a, const TcPlanes& b, CUtensorMap* ma, CUtensor
   return make_map(b, tc::BN, mb);
 }
 
-int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorMap& mb,
-                   const tc::EpiArgs& e, cudaStream_t s) {
+static const int kTcSmem = 192 * 1024 + 1024 + 256;
+
+int tc_gemm_init() {
   static bool attr = false;
-  const int smem = 192 * 1024 + 1024 + 256;
   if (!attr) {
-    if (cudaFuncSetAttribute(tc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(tc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTcSmem) != cudaSuccess)
       return fail(SBE_ERR_CUDA, "tc_gemm: cannot raise the shared-memory limit");
     attr = true;
   }
+  return SBE_OK;
+}
+
+int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorMap& mb,
+                   const tc::EpiArgs& e, cudaStream_t s) {
+  const int smem = kTcSmem;
+  int rc = tc_gemm_init();
+  if (rc) return rc;
   dim3 grid((d.N + tc::BN - 1) / tc::BN, (d.M + tc::BM - 1) / tc::BM, d.batch);
   tc::k_tc_gemm<<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
   return cuda_check(cudaGetLastError(), "tc_gemm launch");

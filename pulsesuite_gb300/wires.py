@@ -59,6 +59,39 @@ class WireSpec:
                                 self.temp)
 
 
+class RK4Graph:
+    """One captured RK4 step (sbe_rk4_graph_create); launch() replays it on the
+    current stream.  ``kernels`` is the number of kernel launches per step."""
+
+    def __init__(self, ctx, P, C, D, Ek0, dEk, dt, src_out, precision):
+        self.ctx = ctx
+        self._keep = (P, C, D, Ek0, dEk, src_out)
+        h = ctypes.c_void_p()
+        n = ctypes.c_longlong()
+        _lib.check(ctx.lib.sbe_rk4_graph_create(ctx.handle, _lib.ptr(P), _lib.ptr(C),
+                                                _lib.ptr(D), _lib.ptr(Ek0), _lib.ptr(dEk),
+                                                float(dt), int(precision), _lib.ptr(src_out),
+                                                ctypes.byref(h), ctypes.byref(n)),
+                   "sbe_rk4_graph_create")
+        self.handle = h
+        self.kernels = n.value
+
+    def launch(self):
+        _lib.check(self.ctx.lib.sbe_graph_launch(self.handle, _lib.stream_handle()),
+                   "sbe_graph_launch")
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            self.ctx.lib.sbe_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 TABLES = dict(kr=0, r=1, Ee=2, Eh=3, V0=4, Chi1D=5, qeqh=6, EP=7, HP=8, window=9, maps=10,
               xexh=11, Expikr=12, scalars=13, window_k=14)
 
@@ -218,6 +251,22 @@ class WireContext:
         _lib.check(self.lib.sbe_rk4_step(self.handle, _lib.ptr(P), _lib.ptr(C), _lib.ptr(D),
                                          _lib.ptr(Ek0), _lib.ptr(dEk), float(dt), int(precision),
                                          _lib.ptr(src_out), _lib.stream_handle()), "sbe_rk4_step")
+
+    def rk4_graph(self, P, C, D, Ek0, dEk, dt, src_out, precision=_lib.PREC_FP64):
+        """Capture one rk4_step on these buffers into a CUDA graph (RK4Graph)."""
+        return RK4Graph(self, P, C, D, Ek0, dEk, dt, src_out, precision)
+
+    def profile(self, enable=True):
+        _lib.check(self.lib.sbe_ctx_profile(self.handle, int(bool(enable))), "sbe_ctx_profile")
+
+    def profile_read(self, category):
+        """(total ms, launches) of a timed category since the last read:
+        0 commutator GEMMs, 1 exchange GEMMs, 2 source GEMMs, 3 FP32 dephasing."""
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        _lib.check(self.lib.sbe_ctx_profile_read(self.handle, int(category), ctypes.byref(ms),
+                                                 ctypes.byref(n)), "sbe_ctx_profile_read")
+        return ms.value, n.value
 
     def rhs(self, P, C, D, Ek, precision=_lib.PREC_FP64):
         dP = torch.empty_like(P)

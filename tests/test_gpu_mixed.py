@@ -78,6 +78,35 @@ def test_mixed_rhs_vs_fp64(nk):
             assert e < 1e-6, (nk, n, w, e)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_graph_replay_matches_direct_step(prec):
+    """A captured RK4 step replays to the same state as the direct call."""
+    nk, nw = 64, 2
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(11)
+    st = [seeded(rng, nk) for _ in range(nw)]
+    Ek0 = fields(ctx, [1e7, 2e7])
+    dEk = fields(ctx, [1e5, -1e5])
+    outs = []
+    for use_graph in (False, True):
+        P = ctx.pack([s[0] for s in st])
+        C = ctx.pack([s[1] for s in st])
+        D = ctx.pack([s[2] for s in st])
+        src = ctx.zeros_r(5)
+        if use_graph:
+            ctx.rk4_step(P.clone(), C.clone(), D.clone(), Ek0, dEk, 1e-16, src.clone(), prec)
+            g = ctx.rk4_graph(P, C, D, Ek0, dEk, 1e-16, src, prec)
+            assert g.kernels > 10
+            g.launch()
+            g.close()
+        else:
+            ctx.rk4_step(P, C, D, Ek0, dEk, 1e-16, src, prec)
+        torch.cuda.synchronize()
+        outs.append((P, C, D, src))
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
+
+
 @pytest.mark.parametrize("nk", [64, 128])
 def test_mixed_rk4_pulse_vs_fp64(nk):
     """40 RK4 steps through the rising edge of a pulse, mixed vs FP64."""
