@@ -319,11 +319,12 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
       const float ka = bah * fk, kal = bal * fk;   // exact head product + tail
       const float fq = (float)q;
       float sa = 0.f, sb = 0.f;
-      for (int p = plo; p <= phi; ++p) {
-        const float fp = (float)(2 * p + c);
+      float fp = (float)(2 * plo + c);   // exact small integers, stepped by 2
+      for (int p = plo; p <= phi; ++p, fp += 2.0f) {
         float s = (ka + bbh * fp) + fmaf(bbl, fp, kal);
         float u = fq * s;
-        float L = __frcp_rn(fmaf(u, u, 1.0f));
+        float L;   // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L) : "f"(fmaf(u, u, 1.0f)));
         sa = fmaf(L, Ab[p], sa);
         sb = fmaf(L, Bb[p], sb);
       }

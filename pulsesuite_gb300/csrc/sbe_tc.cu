@@ -101,6 +101,7 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 struct Mixed {
   int nk = 0, nw = 0, nr = 0;
   __half *planes = nullptr, *tpl = nullptr, *spl = nullptr, *epl = nullptr;
+  float* xsh = nullptr;  // exchange sums in the sheared layout: 3 x Nw x Nk x 4Nk
   int* ints = nullptr;   // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
   unsigned* mx = nullptr;
   double2 *dgE = nullptr, *dgH = nullptr;
@@ -124,6 +125,7 @@ void mixed_free(SbeCtx* c) {
   cudaFree(m->tpl);
   cudaFree(m->spl);
   cudaFree(m->epl);
+  cudaFree(m->xsh);
   cudaFree(m->ints);
   cudaFree(m->mx);
   cudaFree(m->dgE);
@@ -170,6 +172,7 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
             cudaMalloc(&m->tpl, sizeof(__half) * 3 * 2 * nw * mm) == cudaSuccess &&
             cudaMalloc(&m->spl, sizeof(__half) * 3 * 2 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->epl, sizeof(__half) * 4 * nw * (size_t)m->nr * nk) == cudaSuccess &&
+            cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->ints, sizeof(int) * 8 * nw) == cudaSuccess &&
             cudaMalloc(&m->mx, sizeof(unsigned) * nw) == cudaSuccess &&
             cudaMalloc(&m->dgE, sizeof(double2) * 2 * nw * nk) == cudaSuccess;
@@ -270,16 +273,22 @@ __global__ void k_shear_planes(int nk, int nw, const double2* X, const int* e, _
   base[plane] = __double2half(v - (double)__half2float(h));
 }
 
-// H = Meh + diagonal energies + direct Coulomb terms (SBEs.py:1044-1131 without
-// the exchange sums, which the exchange GEMM adds).
-__global__ void k_h_init(const WireDev* wires, const double2* Ek, const double* vs,
-                         const double* Ee, const double* Eh, const double2* tr, double2* Heh,
-                         double2* Hee, double2* Hhh) {
+// H = Meh + diagonal energies + direct Coulomb terms + exchange sums
+// (SBEs.py:1044-1131).  The exchange sums come from the sheared FP32 GEMM output
+// xsh[n][b][k1][2 dd + c], dd = k2 - k1 + Nk - 1, which is read along rows
+// (coalesced in k2).  The diagonal of Hee / Hhh is split off into dgE / dgH
+// (the GEMM operands carry H' = H - diag); the max |component| of the
+// operands goes to mx[b].
+__global__ void k_h_build(const WireDev* wires, const double2* Ek, const double* vs,
+                          const double* Ee, const double* Eh, const double2* tr, const float* xsh,
+                          int have_x, double2* Heh, double2* Hee, double2* Hhh, double2* dgE,
+                          double2* dgH, unsigned* mx) {
   const WireDev W = wires[blockIdx.z];
   const int nk = W.nk;
-  int k1 = blockIdx.x * blockDim.x + threadIdx.x;
-  int k2 = blockIdx.y;
-  if (k1 >= nk || k2 >= nk) return;
+  const int k2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k1 = blockIdx.y;
+  float hmax = 0.f;
+  if (k1 < nk && k2 < nk) {
   double2 heh = make_double2(0, 0);
   if (W.flags & SBE_F_OPTICS) {
     int q = k1 - k2;
@@ -306,23 +315,38 @@ __global__ void k_h_init(const WireDev* wires, const double2* Ek, const double* 
     hhh.x += v[2 * nk + ad] * trD.x - v[ad] * trCm.x;
     hhh.y += v[2 * nk + ad] * trD.y - v[ad] * trCm.y;
   }
+  if (have_x) {
+    const long long ms = (long long)nk * 4 * nk;
+    const long long rowo = ((long long)blockIdx.z * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
+    const long long plane = (long long)gridDim.z * ms;
+    float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
+    heh.x += xe.x;
+    heh.y += xe.y;
+    if (lf || d == 0) {
+      float2 xc = *reinterpret_cast<const float2*>(xsh + plane + rowo);
+      float2 xd = *reinterpret_cast<const float2*>(xsh + 2 * plane + rowo);
+      hee.x -= xc.x;
+      hee.y -= xc.y;
+      hhh.x -= xd.x;
+      hhh.y -= xd.y;
+    }
+  }
   long long o = W.off_mat + (long long)k1 * nk + k2;
   Heh[o] = heh;
+  if (d == 0) {
+    long long vo = (long long)blockIdx.z * nk + k1;
+    dgE[vo] = hee;
+    dgH[vo] = hhh;
+    hee = make_double2(0, 0);
+    hhh = make_double2(0, 0);
+  }
   Hee[o] = hee;
   Hhh[o] = hhh;
-}
-
-__global__ void k_peel(const WireDev* wires, double2* Hee, double2* Hhh, double2* dgE,
-                       double2* dgH) {
-  const WireDev W = wires[blockIdx.y];
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= W.nk) return;
-  long long o = W.off_mat + (long long)k * W.nk + k;
-  long long v = (long long)blockIdx.y * W.nk + k;
-  dgE[v] = Hee[o];
-  dgH[v] = Hhh[o];
-  Hee[o] = make_double2(0, 0);
-  Hhh[o] = make_double2(0, 0);
+  hmax = (float)fmax(fmax(fmax(fabs(heh.x), fabs(heh.y)), fmax(fabs(hee.x), fabs(hee.y))),
+                     fmax(fabs(hhh.x), fabs(hhh.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) hmax = fmaxf(hmax, __shfl_down_sync(0xffffffffu, hmax, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(hmax));
 }
 
 // planes with an added i * f * M (M real-valued complex array), used for
@@ -347,6 +371,39 @@ __global__ void k_planes_add(const double2* X, const double2* Madd, double f, in
   base[plane] = __double2half(vr - (double)__half2float(rh));
   base[2 * plane] = ih;
   base[3 * plane] = __double2half(vi - (double)__half2float(ih));
+}
+
+// dC (dD) from W = C Hee'^T + P^H Heh^T (V = D Hhh'^T + conj(P) Heh): for
+// Hermitian C, Hee (D, Hhh) the four terms of dCdt (dDdt) are W - W^H, so
+//   dX[i][j] = (W[i][j] - conj(W[j][i]) + (g[j] - g[i]) X[i][j]) / (i hbar)
+// with g the peeled diagonal.  The result is exactly anti-Hermitian, which
+// keeps C and D Hermitian.  Tiles (bi, bj) and (bj, bi) meet in shared memory.
+__global__ void k_antiherm(int nk, const double2* W, long long wb, const double2* X,
+                           const double2* g, double2* out) {
+  __shared__ double2 t[32][33];
+  const int b = blockIdx.z;
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const double2* w = W + (long long)b * wb;
+  const long long mb = (long long)b * nk * nk;
+  // t[jj][ii] = W[j0 + jj][i0 + ii]   (the transposed tile)
+  for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
+    int r = j0 + jj, cc = i0 + threadIdx.x;
+    t[jj][threadIdx.x] = (r < nk && cc < nk) ? w[(long long)r * nk + cc] : make_double2(0, 0);
+  }
+  __syncthreads();
+  const double ih = 1.0 / kHbar;
+  for (int ii = threadIdx.y; ii < 32; ii += blockDim.y) {
+    int i = i0 + ii, j = j0 + threadIdx.x;
+    if (i >= nk || j >= nk) continue;
+    double2 a = w[(long long)i * nk + j];
+    double2 bT = t[threadIdx.x][ii];                 // W[j][i]
+    double2 x = X[mb + (long long)i * nk + j];
+    double2 gi = g[(long long)b * nk + i], gj = g[(long long)b * nk + j];
+    double2 de = make_double2(gj.x - gi.x, gj.y - gi.y);
+    double2 dx = make_double2(de.x * x.x - de.y * x.y, de.x * x.y + de.y * x.x);
+    double re = a.x - bT.x + dx.x, im = a.y + bT.y + dx.y;
+    out[mb + (long long)i * nk + j] = make_double2(im * ih, -re * ih);
+  }
 }
 
 __global__ void k_add_int(int n, const int* a, const int* b, int* out) {
@@ -416,38 +473,32 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
     launch_planes(st[i], mm, nk, nw, 0, m->eS(), m->planes, 2 * i, 4, 0, s);
     launch_planes(st[i], mm, nk, nw, 1, m->eS(), m->planes, 2 * i + 1, 4, 0, s);
   }
-  // Hamiltonians: Meh + diagonal + direct terms, then the exchange GEMMs
+  // exchange sums (sheared GEMMs, FP32 output), then the Hamiltonians: Meh +
+  // diagonal + direct + exchange, diagonal peeled, maximum for the H exponent
   launch_traces(c, C, D, s);
-  k_h_init<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, Ek, c->vs, c->Ee, c->Eh,
-                                                          c->tr, c->Heh, c->Hee, c->Hhh);
   int rc = SBE_OK;
-  if (W0.flags & SBE_F_EXCITONS) {
+  const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
+  if (have_x) {
     k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
-    double2* Hs[3] = {c->Heh, c->Hee, c->Hhh};
     for (int n = 0; n < 3; ++n) {
       k_shear_planes<<<dim3((nk + 127) / 128, 4 * nk, nw), 128, 0, s>>>(nk, nw, st[n], m->eS(),
                                                                         m->spl, n);
       tc::Term t{n, n, 0, 0, 1};
       tc::EpiArgs e{};
-      e.kind = tc::EPI_EXCH;
-      e.which = n;
-      e.out = Hs[n];
-      e.out_bstride = mm;
+      e.kind = tc::EPI_F32;
+      e.outf = m->xsh + (long long)n * nw * 4 * mm;
+      e.out_bstride = 4 * mm;
       e.escale = m->esx();
-      e.nk = nk;
-      e.lf = (W0.flags & SBE_F_LF) ? 1 : 0;
       e.err = m->err();
       ProfScope ps(c, 1, s);
       rc = gemm(m, m->mapTA, m->mapSB, nk, 4 * nk, nk, 0, 1, &t, 1, e, s);
       if (rc) return rc;
     }
   }
-  k_peel<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->Hee, c->Hhh, m->dgE, m->dgH);
-  // Hamiltonian exponent and planes
   cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
-  absmax_into(c->Heh, mm, nw, 1.0, m->mx, s);
-  absmax_into(c->Hee, mm, nw, 1.0, m->mx, s);
-  absmax_into(c->Hhh, mm, nw, 1.0, m->mx, s);
+  k_h_build<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, Ek, c->vs, c->Ee, c->Eh,
+                                                           c->tr, m->xsh, have_x, c->Heh, c->Hee,
+                                                           c->Hhh, m->dgE, m->dgH, m->mx);
   if (c->any_offdiag) {
     absmax_into(c->dA, mm, nw, 2.0 * kHbar, m->mx, s);
     absmax_into(c->dB, mm, nw, 2.0 * kHbar, m->mx, s);
@@ -456,26 +507,27 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   const double2* hs[3] = {c->Heh, c->Hee, c->Hhh};
   for (int i = 0; i < 3; ++i) {
     launch_planes(hs[i], mm, nk, nw, 0, m->eH(), m->planes, M_EH + 2 * i, 4, 0, s);
-    launch_planes(hs[i], mm, nk, nw, 1, m->eH(), m->planes, M_EH + 2 * i + 1, 4, 0, s);
+    if (i == 0)   // Hee'^T and Hhh'^T are not needed in the W - W^H form
+      launch_planes(hs[i], mm, nk, nw, 1, m->eH(), m->planes, M_EH + 2 * i + 1, 4, 0, s);
   }
   dim3 pg((nk + 127) / 128, nk, nw);
   k_planes_add<<<pg, 128, 0, s>>>(c->Hee, c->dB, kHbar, nk, m->eH(), m->planes, M_EEX, nw);
   k_planes_add<<<pg, 128, 0, s>>>(c->Hhh, c->dA, kHbar, nk, m->eH(), m->planes, M_HHX, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eH(), m->esc());
-  // commutator GEMMs (term lists follow dpdt/dCdt/dDdt, SBEs.py:1942-2625)
+  // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
+  // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
   const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_DT, M_EH, 0, 0, -1},
                           {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_CT, 0, 0, -1}};
-  const tc::Term tC[4] = {{M_C, M_EE, 0, 0, 1}, {M_EET, M_CT, 0, 0, -1},
-                          {M_PT, M_EH, 1, 0, 1}, {M_EH, M_PT, 1, 0, -1}};
-  const tc::Term tD[4] = {{M_D, M_HH, 0, 0, 1}, {M_HHT, M_DT, 0, 0, -1},
-                          {M_P, M_EHT, 1, 0, 1}, {M_EHT, M_P, 1, 0, -1}};
+  const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
+  const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
   const tc::Term* tl[3] = {tP, tC, tD};
-  double2* outs[3] = {dP, dC, dD};
+  const int nt[3] = {4, 2, 2};
+  double2* Wbuf[3] = {dP, c->G, c->G + c->tot_kr};
   for (int w = 0; w < 3; ++w) {
     tc::EpiArgs e{};
-    e.kind = tc::EPI_RHS;
+    e.kind = (w == 0) ? tc::EPI_RHS : tc::EPI_RAW;
     e.which = w;
-    e.out = outs[w];
+    e.out = Wbuf[w];
     e.out_bstride = mm;
     e.escale = m->esc();
     e.X = st[w];
@@ -487,9 +539,12 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
     e.nk = nk;
     e.err = m->err();
     ProfScope ps(c, 0, s);
-    rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, 4, tl[w], 0, e, s);
+    rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, nt[w], tl[w], 0, e, s);
     if (rc) return rc;
   }
+  dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, c->G, mm, C, m->dgE, dC);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, c->G + c->tot_kr, mm, D, m->dgH, dD);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 

@@ -143,6 +143,20 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
                                const float* re, const float* im) {
   if (m >= d.M) return;
   const double sc = ldexp(1.0, -e.escale[b]);
+  if (e.kind == EPI_F32) {
+    float* o = e.outf + (long long)b * e.out_bstride + (long long)m * d.N + n0;
+    const float scf = (float)sc;
+    if (n0 + 16 <= d.N) {
+      float4* o4 = reinterpret_cast<float4*>(o);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        o4[j] = make_float4(re[4 * j] * scf, re[4 * j + 1] * scf, re[4 * j + 2] * scf,
+                            re[4 * j + 3] * scf);
+    } else {
+      for (int j = 0; j < 16 && n0 + j < d.N; ++j) o[j] = re[j] * scf;
+    }
+    return;
+  }
   if (e.kind == EPI_RAW) {
     double2* o = e.out + (long long)b * e.out_bstride + (long long)m * d.N;
 #pragma unroll

@@ -41,12 +41,14 @@ enum Epi : int {
   EPI_RAW = 0,      // out[b][m][n] = (re, im) * 2^-(ea[b]+eb[b])      (self-test)
   EPI_RHS = 1,      // stage RHS of P, C or D (see sbe_tc.cu)
   EPI_EXCH = 2,     // exchange Hamiltonian assembly (see sbe_tc.cu)
+  EPI_F32 = 3,      // outf[b][m][n] = acc * 2^-escale[b] as FP32 (real mode)
 };
 
 struct EpiArgs {
   int kind;
   int which;                  // RHS: 0 dP, 1 dC, 2 dD;  EXCH: 0 eh, 1 ee, 2 hh
   double2* out;               // FP64 complex output (per batch stride out_bstride)
+  float* outf;                // FP32 output (EPI_F32, per batch stride out_bstride)
   long long out_bstride;
   const int* escale;          // per batch exponent of the product scale (e_A + e_B)
   // RHS epilogue inputs (per batch strides = nk*nk or nk)
