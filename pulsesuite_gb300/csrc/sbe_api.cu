@@ -175,6 +175,9 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   add((void**)&c->xs, C16 * 3 * om);
   add((void**)&c->scal, D8 * 16 * n_wires);
   add((void**)&c->ekst, C16 * 3 * orr);
+  add((void**)&c->occf, 4 * 2 * ov);
+  add((void**)&c->dconst, 4 * 16 * (size_t)n_wires);
+  add((void**)&c->dpre, 4 * 4 * ov);
   size_t total = 0;
   for (auto& p : parts) total += (p.bytes + 255) / 256 * 256;
   if (cudaMalloc(&c->arena, total) != cudaSuccess) {

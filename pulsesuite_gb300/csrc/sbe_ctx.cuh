@@ -44,6 +44,9 @@ struct SbeCtx {
   double2* xs = nullptr;                 // 3*tot_mat RK4 stage state
   double* scal = nullptr;                // 16*nw per-wire scalars
   double2* ekst = nullptr;               // 3*tot_r stage field
+  float* occf = nullptr;                 // 2*tot_vec |ne|, |nh| in FP32
+  float* dconst = nullptr;               // 16*nw FP32 dephasing constants
+  float* dpre = nullptr;                 // 4*tot_vec FP32 dephasing prefactors per |q|
 
   int any_offdiag = 0;                   // some wire has OffDiagDph on
   void* mixed = nullptr;                 // mixed-precision workspace (sbe_tc.cu)

@@ -240,11 +240,19 @@ __device__ inline void split12(double v, float* hi, float* lo) {
   *lo = (float)(v - h);
 }
 
-__global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const double2* ne,
-                                                     const double2* nh, const double* vs,
+__global__ void k_occf(const WireDev* wires, const double2* ne, const double2* nh, float* occf) {
+  const WireDev& W = wires[blockIdx.y];
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= W.nk) return;
+  occf[2 * W.off_vec + k] = (float)hypot(ne[W.off_vec + k].x, ne[W.off_vec + k].y);
+  occf[2 * W.off_vec + W.nk + k] = (float)hypot(nh[W.off_vec + k].x, nh[W.off_vec + k].y);
+}
+
+__global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const float* occf,
+                                                     const float* dconst, const float* dpre,
                                                      double* De, double* Dh) {
   const int wi = blockIdx.z >> 1, which = blockIdx.z & 1;   // 0 De, 1 Dh
-  const WireDev W = wires[wi];
+  const WireDev& W = wires[wi];
   const int nk = W.nk;
   const int qi = blockIdx.y;
   if (qi > 2 * nk) return;
@@ -258,27 +266,22 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
   float* Ba = Aa + nk;
   float* Ab = Ba + nk;         // per-p weights (a-b)
   float* Bb = Ab + nk;
-  const double2* pa = (which == 0 ? ne : nh) + W.off_vec;
-  const double2* pb = (which == 0 ? nh : ne) + W.off_vec;
+  // |n_e|, |n_h| as FP32 (formed once per step by k_occf)
+  const float* pa = occf + 2 * W.off_vec + (which == 0 ? 0 : nk);
+  const float* pb = occf + 2 * W.off_vec + (which == 0 ? nk : 0);
   for (int i = threadIdx.x; i < nk; i += blockDim.x) {
-    na[i] = (float)hypot(pa[i].x, pa[i].y);
-    nb[i] = (float)hypot(pb[i].x, pb[i].y);
+    na[i] = pa[i];
+    nb[i] = pb[i];
   }
-  const double ma = which == 0 ? W.me : W.mh, mbm = which == 0 ? W.mh : W.me;
-  const double ca = kHbar * kHbar / (2.0 * ma), cb = kHbar * kHbar / (2.0 * mbm);
-  const double dk2 = W.dkr * W.dkr;
-  const double g_aa = which == 0 ? W.gam_eh : W.gam_e;   // quirk: De uses gam_eh, Dh gam_e
-  const double b_aa = kHbar * g_aa, b_ab = kHbar * W.gam_h;
+  // per-(wire, species) constants and per-q prefactors (k_deph_consts)
+  const float* cw = dconst + (long long)(2 * wi + which) * 8;
+  const float alpha = cw[0] * (float)q;
+  const float bah = cw[1], bal = cw[2], bbh = cw[3], bbl = cw[4];
+  const float* pq = dpre + 2 * (2 * W.off_vec + (long long)which * nk) + 0;
   const int aq = q < 0 ? -q : q;
-  const double* v = vs + 3 * W.off_vec;
-  double vaa = 0.0, vab = 0.0;
-  if (aq >= 1 && aq < nk) {
-    double x = v[(which == 0 ? 1 : 2) * nk + aq], y = v[aq];
-    vaa = x * x;
-    vab = y * y;
-  }
+  const float vaa = (aq >= 1 && aq < nk) ? pq[2 * aq] : 0.f;
+  const float vab = (aq >= 1 && aq < nk) ? pq[2 * aq + 1] : 0.f;
   const int mlo = -nk + 1 + q;
-  const float alpha = (float)(2.0 * ca * dk2 * (double)q / b_aa);
   __syncthreads();
   for (int i = threadIdx.x; i < 2 * nk; i += blockDim.x) {
     float u = alpha * (float)(mlo + i);
@@ -295,10 +298,10 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
   }
   __syncthreads();
   if (k >= nk) return;
-  double acc = 0.0;
+  float acc = 0.f;
   if (k + q >= 0 && k + q < nk) {
     const float nak = na[k];
-    if (vaa != 0.0) {
+    if (vaa != 0.f) {
       int plo = max(q + 1, 0), phi = min(q + nk - 1, nk - 1);
       float sa = 0.f, sb = 0.f;
       const int base = k + q - mlo;   // Ltab index of m = k - p + q is base - p
@@ -307,14 +310,11 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
         sa = fmaf(L, Aa[p], sa);
         sb = fmaf(L, Ba[p], sb);
       }
-      acc += vaa / (kHbar * b_aa) * ((double)(1.f - nak) * sa + (double)nak * sb);
+      acc += vaa * ((1.f - nak) * sa + nak * sb);
     }
-    if (vab != 0.0) {
+    if (vab != 0.f) {
       int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
       const int c = -2 * W.dnk - 1 + q;
-      float bah, bal, bbh, bbl;
-      split12(ca * dk2 / b_ab, &bah, &bal);
-      split12(cb * dk2 / b_ab, &bbh, &bbl);
       const float fk = (float)(2 * k + c);
       const float ka = bah * fk, kal = bal * fk;   // exact head product + tail
       const float fq = (float)q;
@@ -328,18 +328,50 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
         sa = fmaf(L, Ab[p], sa);
         sb = fmaf(L, Bb[p], sb);
       }
-      acc += vab / (kHbar * b_ab) * ((double)(1.f - nak) * sa + (double)nak * sb);
+      acc += vab * ((1.f - nak) * sa + nak * sb);
     }
   }
   double* D = (which == 0 ? De : Dh) + W.off_dd;
-  D[(long long)qi * nk + k] = acc;
+  D[(long long)qi * nk + k] = (double)acc;
+}
+
+// Constants of k_offdiag_D32 (FP64, once per step): per (wire, species)
+// [2 c_a dkr^2 / b_aa, head/tail of c_a dkr^2 / b_ab, head/tail of c_b dkr^2 / b_ab]
+// and per |q| the prefactors V_aa(q)^2 / (hbar b_aa) and V_ab(q)^2 / (hbar b_ab)
+// (D = (pi/hbar) V^2 Lorentz = V^2 / (hbar b) / (1 + u^2)).
+__global__ void k_deph_consts(const WireDev* wires, const double* vs, float* dconst, float* dpre) {
+  const int wi = blockIdx.y >> 1, which = blockIdx.y & 1;
+  const WireDev& W = wires[wi];
+  const int nk = W.nk;
+  const double ma = which == 0 ? W.me : W.mh, mbm = which == 0 ? W.mh : W.me;
+  const double ca = kHbar * kHbar / (2.0 * ma), cb = kHbar * kHbar / (2.0 * mbm);
+  const double dk2 = W.dkr * W.dkr;
+  const double g_aa = which == 0 ? W.gam_eh : W.gam_e;   // quirk: De uses gam_eh, Dh gam_e
+  const double b_aa = kHbar * g_aa, b_ab = kHbar * W.gam_h;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    float* cw = dconst + (long long)(2 * wi + which) * 8;
+    cw[0] = (float)(2.0 * ca * dk2 / b_aa);
+    split12(ca * dk2 / b_ab, &cw[1], &cw[2]);
+    split12(cb * dk2 / b_ab, &cw[3], &cw[4]);
+  }
+  const double* v = vs + 3 * W.off_vec;
+  float* pq = dpre + 2 * (2 * W.off_vec + (long long)which * nk);
+  for (int aq = blockIdx.x * blockDim.x + threadIdx.x; aq < nk; aq += gridDim.x * blockDim.x) {
+    double x = v[(which == 0 ? 1 : 2) * nk + aq], y = v[aq];
+    pq[2 * aq] = (float)(x * x / (kHbar * b_aa));
+    pq[2 * aq + 1] = (float)(y * y / (kHbar * b_ab));
+  }
 }
 
 void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaStream_t s) {
   if (fp32 && w_only < 0 && !g3) {
     size_t smem = sizeof(float) * 8 * (size_t)c->nk_max;
+    k_occf<<<dim3((c->nk_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, c->ne, c->nh,
+                                                                 c->occf);
+    k_deph_consts<<<dim3((c->nk_max + 127) / 128, 2 * c->nw), 128, 0, s>>>(c->d_wires, c->vs,
+                                                                          c->dconst, c->dpre);
     k_offdiag_D32<<<dim3((c->nk_max + 127) / 128, 2 * c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
-        c->d_wires, c->ne, c->nh, c->vs, c->De, c->Dh);
+        c->d_wires, c->occf, c->dconst, c->dpre, c->De, c->Dh);
     return;
   }
   dim3 g((c->nk_max + 127) / 128, 2 * (2 * c->nk_max + 1), w_only >= 0 ? 1 : c->nw);

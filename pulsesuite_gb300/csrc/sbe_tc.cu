@@ -58,16 +58,16 @@ __global__ void k_planes(const double2* X, long long bstride, int nk, int transp
     if (r >= nk || c >= nk) continue;
     double2 v = transpose ? tile[threadIdx.x][i] : tile[i][threadIdx.x];
     long long o = (long long)r * nk + c;
-    double vr = v.x * sc, vi = v.y * sc;
-    __half rh = __double2half(vr);
-    __half rl = __double2half(vr - (double)__half2float(rh));
+    // scale in FP64 (exact), round once to FP32 (24 bits >= the 22 the planes
+    // keep) and split in FP32: the FP64 pipe is the scarce one on GB300
+    const float vr = (float)(v.x * sc), vi = (float)(v.y * sc);
+    const __half rh = __float2half_rn(vr);
     base[o] = rh;
-    base[plane + o] = rl;
+    base[plane + o] = __float2half_rn(vr - __half2float(rh));
     if (!real_only) {
-      __half ih = __double2half(vi);
-      __half il = __double2half(vi - (double)__half2float(ih));
+      const __half ih = __float2half_rn(vi);
       base[2 * plane + o] = ih;
-      base[3 * plane + o] = il;
+      base[3 * plane + o] = __float2half_rn(vi - __half2float(ih));
     }
   }
 }
@@ -261,16 +261,17 @@ __global__ void k_shear_planes(int nk, int nw, const double2* X, const int* e, _
   if (tp >= nk) return;
   const int dd = row >> 1, c = row & 1;
   const int d = dd - (nk - 1);
-  double v = 0.0;
+  float v = 0.f;
   if (dd < 2 * nk - 1 && tp + d >= 0 && tp + d < nk) {
-    double2 x = X[(long long)b * nk * nk + (long long)(tp + d) * nk + tp];
-    v = ldexp(c ? x.y : x.x, e[b]);
+    const double* x = reinterpret_cast<const double*>(
+        X + (long long)b * nk * nk + (long long)(tp + d) * nk + tp);
+    v = (float)(x[c] * ldexp(1.0, e[b]));
   }
   const long long rows = 4ll * nk, plane = (long long)nw * rows * nk;
   __half* base = dst + (long long)mat * 2 * plane + (long long)b * rows * nk + (long long)row * nk + tp;
-  __half h = __double2half(v);
+  const __half h = __float2half_rn(v);
   base[0] = h;
-  base[plane] = __double2half(v - (double)__half2float(h));
+  base[plane] = __float2half_rn(v - __half2float(h));
 }
 
 // H = Meh + diagonal energies + direct Coulomb terms + exchange sums
@@ -283,67 +284,71 @@ __global__ void k_h_build(const WireDev* wires, const double2* Ek, const double*
                           const double* Ee, const double* Eh, const double2* tr, const float* xsh,
                           int have_x, double2* Heh, double2* Hee, double2* Hhh, double2* dgE,
                           double2* dgH, unsigned* mx) {
-  const WireDev W = wires[blockIdx.z];
+  const WireDev& W = wires[blockIdx.z];
   const int nk = W.nk;
   const int k2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int k1 = blockIdx.y;
   float hmax = 0.f;
   if (k1 < nk && k2 < nk) {
-  double2 heh = make_double2(0, 0);
-  if (W.flags & SBE_F_OPTICS) {
-    int q = k1 - k2;
-    if (q < 0) q += W.nr;
-    const double2* ek = Ek + 3 * W.off_r;
-    double2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
-    double xcv = W.dcv * ((k2 & 1) ? -1.0 : 1.0);
-    double2 t1 = cscale(ex, -W.ehint * xcv);
-    double2 t2 = cscale(cscale(ey, W.ehint * W.dcv), (double)W.yw);
-    double2 t3 = cscale(cscale(ez, W.ehint * -W.dcv), (double)W.zsign);
-    heh = csub(csub(t1, t2), t3);
-  }
-  double2 hee = make_double2(k1 == k2 ? Ee[W.off_vec + k1] + W.gap : 0.0, 0.0);
-  double2 hhh = make_double2(k1 == k2 ? Eh[W.off_vec + k1] : 0.0, 0.0);
-  const bool exc = (W.flags & SBE_F_EXCITONS) != 0, lf = (W.flags & SBE_F_LF) != 0;
-  int d = k1 - k2;
-  if (exc && lf && d != 0) {
-    const double* v = vs + 3 * W.off_vec;
-    const double2* t = tr + 4 * W.off_vec;
-    int ad = d < 0 ? -d : d;
-    double2 trC = t[d + nk], trCm = t[-d + nk], trD = t[2 * nk + d + nk], trDm = t[2 * nk - d + nk];
-    hee.x += v[nk + ad] * trC.x - v[ad] * trDm.x;
-    hee.y += v[nk + ad] * trC.y - v[ad] * trDm.y;
-    hhh.x += v[2 * nk + ad] * trD.x - v[ad] * trCm.x;
-    hhh.y += v[2 * nk + ad] * trD.y - v[ad] * trCm.y;
-  }
-  if (have_x) {
-    const long long ms = (long long)nk * 4 * nk;
-    const long long rowo = ((long long)blockIdx.z * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
-    const long long plane = (long long)gridDim.z * ms;
-    float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
-    heh.x += xe.x;
-    heh.y += xe.y;
-    if (lf || d == 0) {
-      float2 xc = *reinterpret_cast<const float2*>(xsh + plane + rowo);
-      float2 xd = *reinterpret_cast<const float2*>(xsh + 2 * plane + rowo);
+    // off-diagonal elements in FP32 (they only feed the FP16 hi/lo operands and
+    // the driving term of dP); the diagonal (gap + kinetic energy) in FP64
+    float2 heh = make_float2(0.f, 0.f), hee = heh, hhh = heh;
+    if (W.flags & SBE_F_OPTICS) {
+      int q = k1 - k2;
+      if (q < 0) q += W.nr;
+      const double2* ek = Ek + 3 * W.off_r;
+      double2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
+      const float ed = (float)(W.ehint * W.dcv);
+      const float sx = (k2 & 1) ? ed : -ed;               // -ehint Xcv
+      const float sy = -ed * (float)W.yw, sz = ed * (float)W.zsign;
+      heh.x = sx * (float)ex.x + sy * (float)ey.x + sz * (float)ez.x;
+      heh.y = sx * (float)ex.y + sy * (float)ey.y + sz * (float)ez.y;
+    }
+    const bool exc = (W.flags & SBE_F_EXCITONS) != 0, lf = (W.flags & SBE_F_LF) != 0;
+    const int d = k1 - k2;
+    if (exc && lf && d != 0) {
+      const double* v = vs + 3 * W.off_vec;
+      const double2* t = tr + 4 * W.off_vec;
+      const int ad = d < 0 ? -d : d;
+      const float v0 = (float)v[ad], v1 = (float)v[nk + ad], v2 = (float)v[2 * nk + ad];
+      double2 trC = t[d + nk], trCm = t[-d + nk], trD = t[2 * nk + d + nk],
+              trDm = t[2 * nk - d + nk];
+      hee.x = v1 * (float)trC.x - v0 * (float)trDm.x;
+      hee.y = v1 * (float)trC.y - v0 * (float)trDm.y;
+      hhh.x = v2 * (float)trD.x - v0 * (float)trCm.x;
+      hhh.y = v2 * (float)trD.y - v0 * (float)trCm.y;
+    }
+    float2 xc = make_float2(0.f, 0.f), xd = xc;
+    if (have_x) {
+      const long long ms = (long long)nk * 4 * nk;
+      const long long rowo = ((long long)blockIdx.z * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
+      const long long plane = (long long)gridDim.z * ms;
+      float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
+      heh.x += xe.x;
+      heh.y += xe.y;
+      if (lf || d == 0) {
+        xc = *reinterpret_cast<const float2*>(xsh + plane + rowo);
+        xd = *reinterpret_cast<const float2*>(xsh + 2 * plane + rowo);
+      }
+    }
+    const long long o = W.off_mat + (long long)k1 * nk + k2;
+    Heh[o] = make_double2(heh.x, heh.y);
+    if (d == 0) {
+      const long long vo = (long long)blockIdx.z * nk + k1;
+      dgE[vo] = make_double2(Ee[W.off_vec + k1] + W.gap - (double)xc.x, -(double)xc.y);
+      dgH[vo] = make_double2(Eh[W.off_vec + k1] - (double)xd.x, -(double)xd.y);
+      hee = make_float2(0.f, 0.f);
+      hhh = hee;
+    } else {
       hee.x -= xc.x;
       hee.y -= xc.y;
       hhh.x -= xd.x;
       hhh.y -= xd.y;
     }
-  }
-  long long o = W.off_mat + (long long)k1 * nk + k2;
-  Heh[o] = heh;
-  if (d == 0) {
-    long long vo = (long long)blockIdx.z * nk + k1;
-    dgE[vo] = hee;
-    dgH[vo] = hhh;
-    hee = make_double2(0, 0);
-    hhh = make_double2(0, 0);
-  }
-  Hee[o] = hee;
-  Hhh[o] = hhh;
-  hmax = (float)fmax(fmax(fmax(fabs(heh.x), fabs(heh.y)), fmax(fabs(hee.x), fabs(hee.y))),
-                     fmax(fabs(hhh.x), fabs(hhh.y)));
+    Hee[o] = make_double2(hee.x, hee.y);
+    Hhh[o] = make_double2(hhh.x, hhh.y);
+    hmax = fmaxf(fmaxf(fmaxf(fabsf(heh.x), fabsf(heh.y)), fmaxf(fabsf(hee.x), fabsf(hee.y))),
+                 fmaxf(fabsf(hhh.x), fabsf(hhh.y)));
   }
   for (int o = 16; o > 0; o >>= 1) hmax = fmaxf(hmax, __shfl_down_sync(0xffffffffu, hmax, o));
   if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(hmax));
@@ -361,16 +366,14 @@ __global__ void k_planes_add(const double2* X, const double2* Madd, double f, in
   long long o = (long long)r * nk + c;
   double2 v = X[(long long)b * mm + o];
   double2 a = Madd[(long long)b * mm + o];
-  v.x -= f * a.y;
-  v.y += f * a.x;
-  double sc = ldexp(1.0, e[b]);
-  double vr = v.x * sc, vi = v.y * sc;
+  const double sc = ldexp(1.0, e[b]);
+  const float vr = (float)((v.x - f * a.y) * sc), vi = (float)((v.y + f * a.x) * sc);
   __half* base = dst + (long long)mat * 4 * plane + (long long)b * mm + o;
-  __half rh = __double2half(vr), ih = __double2half(vi);
+  const __half rh = __float2half_rn(vr), ih = __float2half_rn(vi);
   base[0] = rh;
-  base[plane] = __double2half(vr - (double)__half2float(rh));
+  base[plane] = __float2half_rn(vr - __half2float(rh));
   base[2 * plane] = ih;
-  base[3 * plane] = __double2half(vi - (double)__half2float(ih));
+  base[3 * plane] = __float2half_rn(vi - __half2float(ih));
 }
 
 // dC (dD) from W = C Hee'^T + P^H Heh^T (V = D Hhh'^T + conj(P) Heh): for
