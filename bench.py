@@ -43,6 +43,9 @@ C0 = 299792458.0
 WORKLOADS = {
     "multiwire": dict(nw=32, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
                       dt=0.05e-15, spacing=100e-9),
+    # the same wires, fewer of them: the case the kernel-level profiles are taken on
+    "profile": dict(nw=8, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
+                    dt=0.05e-15, spacing=100e-9),
 }
 
 MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta0=6e-9,
