@@ -134,6 +134,21 @@ int sbe_prop2qw(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* fi
 int sbe_qw2prop(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* src_in,
                 double* out, int plasmonics, void* stream);
 
+/* ---- Prop2QW without allocation (no counterpart in the reference) ------------
+ * Same arguments and results as sbe_prop2qw, for callers that must not allocate
+ * device memory (a host code whose pool owns all device memory, or a loop that
+ * must not take the allocator's lock): the scratch is one static device array
+ * per device, so nothing is allocated or freed.  Limits: n_rr <=
+ * SBE_NOALLOC_MAX_GRID, wire Nr <= SBE_NOALLOC_MAX_NR; larger calls return an
+ * error before any launch.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress); make it before any stream capture.  Calls that overlap
+ * in time on one device (other streams, threads or contexts) race on the shared
+ * scratch; calls on one stream are ordered.                                    */
+#define SBE_NOALLOC_MAX_GRID 8192
+#define SBE_NOALLOC_MAX_NR 2050
+int sbe_prop2qw_noalloc(SbeCtx* ctx, int w, const double* RR, int n_rr,
+                        const double* fields_in, double* out, void* stream);
+
 /* ---- the reference time step (leapfrog), all wires of the context -------- */
 /* SBEs.py:5612-5820 _sbe_calculator for every wire of ctx.  State: 9 buffers of
  * packed Nk*Nk c128 blocks (YY1..3, CC1..3, DD1..3 in that order in state9[]).

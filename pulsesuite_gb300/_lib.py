@@ -28,7 +28,7 @@ EXPORTS = (
     "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_sources",
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
     "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
-    "sbe_ctx_profile", "sbe_ctx_profile_read",
+    "sbe_ctx_profile", "sbe_ctx_profile_read", "sbe_prop2qw_noalloc",
 )
 
 
@@ -77,6 +77,7 @@ def load(path=LIB_PATH):
         "sbe_phonon_rates": [P, I, P, P, P, P, P, P, P, P, P],
         "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
         "sbe_prop2qw": [P, I, P, I, P, P, P],
+        "sbe_prop2qw_noalloc": [P, I, P, I, P, P, P],
         "sbe_qw2prop": [P, I, P, I, P, P, I, P],
         "sbe_leapfrog_step": [P, P, P, Dbl, P, P],
         "sbe_rk4_step": [P, P, P, P, P, P, Dbl, I, P, P],

@@ -165,6 +165,8 @@ void launch_stage_field(SbeCtx* c, const double2* Ek0, const double2* dEk, doubl
                         cudaStream_t s);
 int launch_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
                    double2* out, cudaStream_t s);
+int launch_prop2qw_scratch(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
+                           double2* out, double2* coef, double2* tmp, cudaStream_t s);
 int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* src,
                    double2* out, int plasmonics, cudaStream_t s);
 }  // namespace sbe

@@ -516,6 +516,19 @@ int launch_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double2* 
   return cuda_check(cudaGetLastError(), "prop2qw");
 }
 
+// The same three launches as launch_prop2qw on scratch the caller provides:
+// coef holds 12 n_rr and tmp 4 Nr complex values.  Allocates nothing.
+int launch_prop2qw_scratch(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
+                           double2* out, double2* coef, double2* tmp, cudaStream_t s) {
+  const WireDev& W = c->wires[w];
+  k_spline_coef<<<1, 32, 0, s>>>(n_rr, RR, fin, 4, coef);
+  k_spline_eval<<<dim3((W.nr + 127) / 128, 4), 128, 0, s>>>(n_rr, RR, fin, coef, W.nr,
+                                                           c->r + W.off_r, 4,
+                                                           c->window + W.off_r, 1, tmp);
+  k_fftg<<<dim3(W.nr, 4), 128, 0, s>>>(W.nr, 4, tmp, out);
+  return cuda_check(cudaGetLastError(), "prop2qw (caller scratch)");
+}
+
 // qwoptics.py:760-805 charge renormalisation (Plasmonics).  mode 0: on the wire
 // grid (re, rh -> |.| scaled to total); mode 1: on the propagation grid.
 __global__ void k_plasmonics(int n, const double* grid, double2* a, double2* b, double* total_io,
