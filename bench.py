@@ -1,17 +1,21 @@
-"""Benchmark: batched mixed-precision SBE wire-steps/s on GB300.
+"""Benchmark: batched mixed-precision SBE + PSTD wire-steps/s on GB300.
 
-Workload (default, "multiwire"): 32 identical GaAs-like quantum wires, Nk = 512
-k points each (|k| <= 3e9 1/m, Nr = 1026), T = 300 K, Coulomb Hartree-Fock +
-screening + LO-phonon relaxation + diagonal and off-diagonal dephasing, driven by
-a Gaussian pulse E0 = 5e7 V/m, tau = 50 fs, hbar w0 = Eg + 20 meV, polarised
-along the wires and retarded by the wire position (wires 100 nm apart), RK4 with
-dt = 0.05 fs.  One step advances every wire by dt (4 RHS evaluations,
-relaxation, charge normalisation and the polarisation/charge sources).
+Workload (default, "multiwire"): 32 identical GaAs-like quantum wires spaced
+100 nm apart along a 1-D PSTD grid of Nx = 16384 cells of 10 nm (background
+epsr = 12.9, absorbing layers of 128 cells), Nk = 512 k points per wire
+(|k| <= 3e9 1/m, Nr = 1026), T = 300 K, Coulomb Hartree-Fock + screening +
+LO-phonon relaxation + diagonal and off-diagonal dephasing.  The field is a
+Gaussian pulse E0 = 5e7 V/m, tau = 50 fs, hbar w0 = Eg + 20 meV, launched by a
+current sheet 2.5 um left of the array and already in flight at step 0 (its peak
+at the array centre).  One step = one coupled step: field sampled onto every
+wire, H update, RK4 step of every wire (dt = 0.05 fs: 4 RHS evaluations,
+relaxation, charge normalisation, sources), sources deposited on the grid,
+polarisation current, E update, longitudinal Ex.
 
 value     : wire-steps/s of the mixed path (tcgen05 FP16 hi/lo x3, FP32 accumulate,
-            FP64 state) through WireContext.rk4_step with device-resident inputs.
-e2e       : the same through the same call with the step's field copied from
-            pinned host memory and the sources read back every step.
+            FP64 state) through CoupledLine.step with device-resident state.
+e2e       : the same call with the grid field (Ex, Ey, Ez) copied in from pinned
+            host memory and the grid sources (Px, Py, Pz, Rho) read back every step.
 fp64_gpu  : the plain FP64 GPU path on the same state (the metric's denominator).
 roofline  : commutator GEMM launches (the dominant kernel), CUDA events around
             each launch inside the timed region.
@@ -42,10 +46,12 @@ C0 = 299792458.0
 
 WORKLOADS = {
     "multiwire": dict(nw=32, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
-                      dt=0.05e-15, spacing=100e-9),
+                      dt=0.05e-15, spacing=100e-9, nx=16384, dx=10e-9, n_abc=128,
+                      abc=0.05, x_src=-2.5e-6),
     # the same wires, fewer of them: the case the kernel-level profiles are taken on
     "profile": dict(nw=8, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
-                    dt=0.05e-15, spacing=100e-9),
+                    dt=0.05e-15, spacing=100e-9, nx=16384, dx=10e-9, n_abc=128,
+                    abc=0.05, x_src=-2.5e-6),
 }
 
 MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta0=6e-9,
@@ -54,6 +60,9 @@ MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta
 FLAGS = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
              LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel err"
+# dram__bytes_read.sum + dram__bytes_write.sum of one 2-term commutator launch,
+# 8 wires x Nk = 512 (ncu), per wire
+TRAFFIC_PER_WIRE = (67.17e6 + 4.10e6) / 8
 
 
 def wire_L(nk, kmax):
@@ -65,10 +74,25 @@ def pulse(t, wl):
     return wl["E0"] * np.exp(-t * t / wl["tau"] ** 2) * np.cos(w0 * t)
 
 
-def wire_delays(wl):
-    n = np.sqrt(MAT["epsr"])
-    x = (np.arange(wl["nw"]) - (wl["nw"] - 1) / 2.0) * wl["spacing"]
-    return x * n / C0
+def wire_positions(wl):
+    return (np.arange(wl["nw"]) - (wl["nw"] - 1) / 2.0) * wl["spacing"]
+
+
+def w0_of(wl):
+    return (MAT["gap"] + wl["det"] * E0C) / HBAR
+
+
+def incident_state(wl, x, x_src, t, dt):
+    """Grid fields of the pulse a current sheet at x_src has emitted since t = -inf:
+    Ey(x, t) = E_inc(t - |x - x_src| / v), Hz(x, t - dt/2) = sign(x - x_src) Ey / eta."""
+    v = C0 / np.sqrt(MAT["epsr"])
+    eta = np.sqrt(1.25663706127e-06 / (8.8541878188e-12 * MAT["epsr"]))
+    d = np.abs(x - x_src)
+    E = np.zeros((2, len(x)), complex)
+    H = np.zeros((2, len(x)), complex)
+    E[0] = pulse(t - d / v, wl)
+    H[0] = np.sign(x - x_src) * pulse(t - dt / 2 - d / v, wl) / eta
+    return E, H
 
 
 def env():
@@ -130,10 +154,12 @@ def reference_arm(args, wl):
 
 
 def config_of(wl, impl):
-    return {"workload": f"{wl['nw']} wires x Nk={wl['nk']} GaAs-like quantum wires, local "
-                        f"retarded pulse E0={wl['E0']:.0e} V/m tau={wl['tau']*1e15:.0f} fs, "
-                        f"T={wl['temp']:.0f} K, RK4 dt={wl['dt']*1e15:.2f} fs",
-            "wires": wl["nw"], "nk": wl["nk"], "nr": 2 * wl["nk"] + 2,
+    return {"workload": f"{wl['nw']} wires x Nk={wl['nk']} GaAs-like quantum wires every "
+                        f"{wl['spacing']*1e9:.0f} nm on a 1-D PSTD grid Nx={wl['nx']} "
+                        f"dx={wl['dx']*1e9:.0f} nm, pulse E0={wl['E0']:.0e} V/m "
+                        f"tau={wl['tau']*1e15:.0f} fs, T={wl['temp']:.0f} K, "
+                        f"RK4 dt={wl['dt']*1e15:.2f} fs",
+            "wires": wl["nw"], "nk": wl["nk"], "nr": 2 * wl["nk"] + 2, "nx": wl["nx"],
             "flags": "Optics Excitons Screened Phonon LF DiagDph OffDiagDph",
             "integrator": "RK4 (coefficients frozen per step) + reference relaxation/normalisation",
             "l2": "inputs larger than L2 (FP64 state 403 MB, FP16 operand planes 1.9 GB per stage)",
@@ -208,6 +234,7 @@ def gpu_arm(args, wl):
     torch.cuda.set_device(local)
     ge.build()
     from pulsesuite_gb300 import _lib
+    from pulsesuite_gb300.pstd import CoupledLine, Pstd1D, SheetSource
     from pulsesuite_gb300.wires import WireContext, WireSpec
 
     nw, nk = wl["nw"], wl["nk"]
@@ -216,48 +243,39 @@ def gpu_arm(args, wl):
              for w in range(nw)]
     ctx = WireContext(specs)
     prec = _lib.PREC_MIXED if args.precision == "mixed" else _lib.PREC_FP64
-    nr = 2 * nk + 2
-    wk = torch.stack([ctx.table(w, "window_k") for w in range(nw)])     # (nw, nr)
-    delays = torch.as_tensor(wire_delays(wl), device="cuda")
-
-    def field_k(t):
-        """(nw, 3, nr) wire-k field of the retarded uniform pulse (along y)."""
-        amp = torch.as_tensor(pulse(t - wire_delays(wl), wl), device="cuda")
-        f = torch.zeros((nw, 3, nr), dtype=torch.complex128, device="cuda")
-        f[:, 1, :] = amp[:, None] * wk
-        return f
+    nx, dx, dt = wl["nx"], wl["dx"], wl["dt"]
+    grid = Pstd1D(nx, dx, MAT["epsr"], n_abc=wl["n_abc"], abc_strength=wl["abc"])
+    x = grid.x.cpu().numpy()
+    i_src = int(np.argmin(np.abs(x - wl["x_src"])))
+    x_src = float(x[i_src])
+    v = C0 / np.sqrt(MAT["epsr"])
+    t_start = (0.0 - x_src) / v                 # pulse peak at the array centre at step 0
+    line = CoupledLine(ctx, grid, wire_positions(wl),
+                       source=SheetSource(index=i_src, E0=wl["E0"], tau=wl["tau"],
+                                          w0=w0_of(wl), tpeak=0.0),
+                       t0=t_start, longitudinal=True)
+    E0h, H0h = incident_state(wl, x, x_src, t_start, dt)
 
     fe = 1.0 / (np.exp((ctx.table(0, "Ee").cpu().numpy() + MAT["gap"] / 2.0) / 1.380649e-23
                        / wl["temp"]) + 1.0)
 
-    def fresh_state():
+    def fresh():
         d = np.diag(fe).astype(complex)
+        P = ctx.zeros_state()
         C = ctx.pack([d] * nw)
         D = ctx.pack([d] * nw)
-        P = ctx.zeros_state()
-        return P, C, D
+        E = torch.as_tensor(E0h).cuda().contiguous()
+        H = torch.as_tensor(H0h).cuda().contiguous()
+        Ex = torch.zeros(nx, dtype=torch.complex128, device="cuda")
+        return P, C, D, E, H, Ex
 
-    P, C, D = fresh_state()
-    src = ctx.zeros_r(5)
-    dt = wl["dt"]
-    t = -2 * wl["tau"]
-    Ek0 = torch.zeros(3 * ctx.total_r, dtype=torch.complex128, device="cuda")
-    dEk = torch.zeros_like(Ek0)
-
-    def set_field(t):
-        f0 = field_k(t)
-        f1 = field_k(t + dt)
-        Ek0.copy_(f0.reshape(-1))
-        dEk.copy_((f1 - f0).reshape(-1))
-
-    # warm-up
+    st = fresh()
+    line.reset()
     for _ in range(args.warmup):
-        set_field(t)
-        ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
-        t += dt
+        line.step(*st, dt, prec)
     torch.cuda.synchronize()
 
-    # timed region: device-resident inputs, engine launches timed with events
+    # timed region: device-resident state, engine launches timed with events
     ctx.profile(True)
     for cat in range(4):
         ctx.profile_read(cat)
@@ -270,9 +288,7 @@ def gpu_arm(args, wl):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
     for _ in range(args.steps):
-        set_field(t)
-        ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
-        t += dt
+        line.step(*st, dt, prec)
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -286,10 +302,9 @@ def gpu_arm(args, wl):
     ctx.profile(False)
     value = world * nw * args.steps / (ms / 1e3)
 
-    # CUDA graph of the same step (launch count, replay time)
-    graph = ctx.rk4_graph(P, C, D, Ek0, dEk, dt, src, prec)
+    # CUDA graph of the same coupled step (launch count, replay time)
+    graph = line.graph(*st, dt, prec)
     n_kernels = graph.kernels
-    set_field(t)
     graph.launch()
     torch.cuda.synchronize()
     g0 = torch.cuda.Event(enable_timing=True)
@@ -302,49 +317,60 @@ def gpu_arm(args, wl):
     graph_ms = g0.elapsed_time(g1) / args.steps
     graph.close()
 
-    # end to end: field from pinned host memory in, sources back to pinned host
-    h_src = torch.empty(5 * ctx.total_r, dtype=torch.complex128).pin_memory()
-    host_fields = []
-    tt_ = t
-    for _ in range(args.steps):
-        f0 = field_k(tt_)
-        f1 = field_k(tt_ + dt)
-        host_fields.append((f0.reshape(-1).cpu().pin_memory(),
-                            (f1 - f0).reshape(-1).cpu().pin_memory()))
-        tt_ += dt
+    # PSTD field step alone (H and E updates of the 16384-cell grid)
+    Et, Ht = st[3].clone(), st[4].clone()
+    Jt = torch.zeros_like(Et)
+    for _ in range(3):
+        grid.step(Et, Ht, Jt, dt)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for _ in range(100):
+        grid.step(Et, Ht, Jt, dt)
+    p1.record()
+    torch.cuda.synchronize()
+    pstd_ms = p0.elapsed_time(p1) / 100
+
+    # end to end: grid field (Ex, Ey, Ez) in from pinned host memory, grid sources
+    # (Px, Py, Pz, Rho) back to pinned host memory, every step
+    h_in = [torch.cat([st[5][None], st[3]]).cpu().pin_memory() for _ in range(args.steps)]
+    h_out = torch.empty((4, nx), dtype=torch.complex128).pin_memory()
+    Pg, rho = line.view("Pg"), line.view("rho")
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
     for i in range(args.steps):
-        Ek0.copy_(host_fields[i][0], non_blocking=True)
-        dEk.copy_(host_fields[i][1], non_blocking=True)
-        ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
-        h_src.copy_(src, non_blocking=True)
+        st[5].copy_(h_in[i][0], non_blocking=True)
+        st[3].copy_(h_in[i][1:], non_blocking=True)
+        line.step(*st, dt, prec)
+        h_out[:3].copy_(Pg, non_blocking=True)
+        h_out[3].copy_(rho, non_blocking=True)
     e1.record()
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     e2e_val = world * nw * args.steps / (e2e_ms / 1e3)
 
     # RHS error of the mixed path against the FP64 path at the current state
-    Ek_now = field_k(t).reshape(-1).contiguous()
+    P, C, D = st[0], st[1], st[2]
+    Ek_now = line.view("Ek").clone()
     r64 = ctx.rhs(P, C, D, Ek_now, _lib.PREC_FP64)
     rmx = ctx.rhs(P, C, D, Ek_now, _lib.PREC_MIXED)
     rhs_err = max(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) for a, b in zip(rmx, r64))
+    field_peak = float(Ek_now.abs().max())
 
     # plain FP64 GPU path on the same state (a few steps: it is slow by design)
     fp64_ms = fp64_val = None
     n64 = max(1, args.fp64_steps)
     if not args.no_fp64:
-        P2, C2, D2 = P.clone(), C.clone(), D.clone()
-        set_field(t)
-        ctx.rk4_step(P2, C2, D2, Ek0, dEk, dt, src, _lib.PREC_FP64)
+        st64 = tuple(t.clone() for t in st)
+        line.step(*st64, dt, _lib.PREC_FP64)
         torch.cuda.synchronize()
         f0e = torch.cuda.Event(enable_timing=True)
         f1e = torch.cuda.Event(enable_timing=True)
         f0e.record()
         for _ in range(n64):
-            ctx.rk4_step(P2, C2, D2, Ek0, dEk, dt, src, _lib.PREC_FP64)
+            line.step(*st64, dt, _lib.PREC_FP64)
         f1e.record()
         torch.cuda.synchronize()
         fp64_ms = f0e.elapsed_time(f1e) / n64
@@ -358,8 +384,12 @@ def gpu_arm(args, wl):
     peaks, pk_kind = measured_peaks()
     comm_ms, comm_n = prof[0]
     per_launch_s = comm_ms / max(comm_n, 1) / 1e3
-    useful = 32.0 * nk ** 3 * nw          # 4 complex terms x 8 flop x Nk^3 per wire
-    executed = 96.0 * nk ** 3 * nw        # 12 FP16 MMA-GEMMs per term
+    # algorithmic work of a1-a3 (dP, dC, dD as 12 complex Nk^3 products, 96 Nk^3 flop per
+    # wire per RHS evaluation) over the 3 commutator launches of an evaluation
+    useful = 32.0 * nk ** 3 * nw
+    # executed: 8 complex products per evaluation (W - W^H form) x 4 real products x 3
+    # hi/lo terms x 2 Nk^3 = 192 Nk^3 per evaluation, 64 Nk^3 per launch
+    executed = 64.0 * nk ** 3 * nw
     achieved = useful / per_launch_s / 1e12
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     roof = {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)", "achieved": achieved,
@@ -368,11 +398,16 @@ def gpu_arm(args, wl):
             "executed_tflops": executed / per_launch_s / 1e12,
             "executed_frac": executed / per_launch_s / 1e12 / peak,
             "avg_launch_ms": per_launch_s * 1e3, "launches": comm_n,
-            "traffic": None,
-            "flops_model": "useful 32*Nk^3 per wire per launch (4 complex Nk^3 products); "
-                           "executed 96*Nk^3 (4 real products x 3 hi/lo terms per complex term)"}
+            "traffic": TRAFFIC_PER_WIRE * nw,
+            "traffic_note": "dram read+write bytes of one 2-term commutator launch from an "
+                            "ncu capture of the 8-wire case, scaled by wires",
+            "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
+                           "12 complex Nk^3 products) over its 3 commutator launches = 32*Nk^3 "
+                           "per launch; executed 64*Nk^3 per launch (8 complex products per "
+                           "evaluation x 4 real products x 3 hi/lo terms)"}
     other = {name: {"ms_per_step": prof[c][0] / args.steps, "launches": prof[c][1]}
              for c, name in ((1, "exchange_gemm"), (2, "source_gemm"), (3, "dephasing_fp32"))}
+    other["pstd_field_step"] = {"ms_per_step": pstd_ms, "launches": 6}
 
     cpu = None
     if not args.no_cpu:
@@ -382,25 +417,26 @@ def gpu_arm(args, wl):
                "sample": f"one RK4 wire-step of one wire (Nk={nk}) of this workload, NumPy FP64 "
                          "restatement (BLAS matmuls multi-threaded, O(Nk^3) sums single-threaded)"}
 
-    line = {"metric": METRIC, "value": value, "unit": "wire-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
-            "data": "synthetic", "config": config_of(wl, args.precision),
-            "clocks": clk,
-            "e2e": {"value": e2e_val, "unit": "wire-steps/s",
-                    "h2d_bytes_per_step": int(2 * 3 * ctx.total_r * 16),
-                    "d2h_bytes_per_step": int(5 * ctx.total_r * 16)},
-            "gpu_launches": int(n_kernels * args.steps),
-            "gpu_launches_per_step": int(n_kernels),
-            "graph_replay_ms_per_step": graph_ms,
-            "roofline": roof, "other_kernels": other,
-            "fp64_gpu": {"value": fp64_val, "unit": "wire-steps/s", "ms_per_step": fp64_ms,
-                         "steps": n64},
-            "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
-            "rhs_rel_err_vs_fp64": rhs_err,
-            "cpu_baseline": cpu}
-    print(json.dumps(line), flush=True)
+    line_out = {"metric": METRIC, "value": value, "unit": "wire-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
+                "data": "synthetic", "config": config_of(wl, args.precision),
+                "clocks": clk,
+                "e2e": {"value": e2e_val, "unit": "wire-steps/s",
+                        "h2d_bytes_per_step": int(3 * nx * 16),
+                        "d2h_bytes_per_step": int(4 * nx * 16)},
+                "gpu_launches": int(n_kernels * args.steps),
+                "gpu_launches_per_step": int(n_kernels),
+                "graph_replay_ms_per_step": graph_ms,
+                "roofline": roof, "other_kernels": other,
+                "fp64_gpu": {"value": fp64_val, "unit": "wire-steps/s", "ms_per_step": fp64_ms,
+                             "steps": n64},
+                "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
+                "rhs_rel_err_vs_fp64": rhs_err,
+                "wire_field_peak_k": field_peak,
+                "cpu_baseline": cpu}
+    print(json.dumps(line_out), flush=True)
     if dist:
         dist.destroy_process_group()
 

@@ -183,6 +183,79 @@ int sbe_rk4_graph_create(SbeCtx* ctx, double* P, double* C, double* D, const dou
 int sbe_graph_launch(SbeGraph* g, void* stream);
 int sbe_graph_destroy(SbeGraph* g);
 
+/* ---- 1-D PSTD field grid --------------------------------------------------------
+ * The reference has no 1-D Maxwell stepper; these entries assemble its pieces:
+ * dfdx1D = IFFT(i q FFT f) (PSTD3D/usefulsubs.py:163-185), the grids
+ * GetSpaceArray / GetKArray (PSTD3D/typespace.py:815-849, positions;
+ * libpulsesuite/helpers.py:838-863, wavenumbers in FFT order), the longitudinal
+ * field of ElongfromRho (PSTD3D/rhoPJ.py:703-880, x component) and the mask
+ * multiply of ApplyABC (usefulsubs.py:584-609).  Propagation along x (the wire
+ * axis); transverse fields E = (Ey, Ez) and H = (Hz, Hy), each 2 x c128 nx;
+ * longitudinal Ex (c128 nx).  Leapfrog: H^{n+1/2} = H^{n-1/2} - dt/mu0 curl E^n,
+ * E^{n+1} = mask (E^n + dt/eps (curl H^{n+1/2} - J^{n+1/2})), J = (Jy, Jz).      */
+typedef struct {
+  int nx;              /* grid points: power of two in [256, 65536]            */
+  int n_abc;           /* absorbing cells at each end (0: periodic grid)       */
+  int pad0, pad1;
+  double dx;           /* cell size (m)                                        */
+  double epsr;         /* background relative permittivity                     */
+  double abc_strength; /* mask = exp(-abc_strength s^2), s = depth in layer    */
+} SbePstdDesc;
+typedef struct SbePstd SbePstd;
+int sbe_pstd_create(const SbePstdDesc* desc, void* stream, SbePstd** out);
+int sbe_pstd_destroy(SbePstd* p);
+/* device copies of the positions x and wavenumbers q (nx doubles each; NULL skips) */
+int sbe_pstd_grid(SbePstd* p, double* x, double* q, void* stream);
+/* dfdx1D (usefulsubs.py:163-185) of nf = 1 or 2 fields (nf x c128 nx) into df   */
+int sbe_pstd_deriv(SbePstd* p, const double* f, int nf, double* df, void* stream);
+int sbe_pstd_update_h(SbePstd* p, const double* E, double* H, double dt, void* stream);
+int sbe_pstd_update_e(SbePstd* p, double* E, const double* H, const double* J, double dt,
+                      void* stream);
+/* update_h then update_e; J may be NULL.  dt must satisfy c dt pi/(sqrt(epsr) dx) <= 2. */
+int sbe_pstd_step(SbePstd* p, double* E, double* H, const double* J, double dt, void* stream);
+/* Ex from the charge density rho and the polarisation Px (rhoPJ.py:836-866, x only) */
+int sbe_pstd_elong(SbePstd* p, const double* rho, const double* Px, double* Ex, void* stream);
+
+/* ---- wires on the PSTD grid (coupled step) --------------------------------------
+ * Field -> wire: Prop2QW (qwoptics.py:667-715) with the grid spline evaluated at
+ * x_w + r; wire -> field: QW2Prop (qwoptics.py:717-805, no plasmonic
+ * renormalisation) of the real-space sources at x - x_w, summed over wires, and
+ * Rho = RhoH - RhoE (SBEs.py:5917).  The soft source is a current sheet at one
+ * cell launching E_inc(t) = E0 exp(-((t - tpeak)/tau)^2) cos(w0 (t - tpeak)).  */
+typedef struct {
+  int src_index;       /* grid cell of the soft source, -1: none               */
+  int longitudinal;    /* 1: Ex = longitudinal field of the wires' Rho and Px  */
+  int pad0, pad1;
+  double E0, tau, w0, tpeak;
+  double t0;           /* time of step 0                                       */
+} SbeCoupleDesc;
+typedef struct SbeCouple SbeCouple;
+/* wire_x: HOST array of the nw wire centre positions (m) on the grid.          */
+int sbe_couple_create(SbeCtx* ctx, SbePstd* p, const double* wire_x, const SbeCoupleDesc* desc,
+                      void* stream, SbeCouple** out);
+int sbe_couple_destroy(SbeCouple* cp);
+/* Device pointers of the coupling buffers: Ek (per wire 3 x c128 Nr, wire k
+ * space), src (per wire 5 x c128 Nr real-space sources), Pg (3 x c128 nx), rho
+ * (c128 nx), J (2 x c128 nx).  NULL arguments are skipped.                     */
+int sbe_couple_buffers(SbeCouple* cp, double** Ek, double** src, double** Pg, double** rho,
+                       double** J);
+int sbe_couple_set_step(SbeCouple* cp, long long n, void* stream);
+/* Start a new run: step counter 0, previous grid polarisation P^n = 0 (the first
+ * current is P^1 / dt, so start the wires from P = 0), Pg, rho and J cleared.  */
+int sbe_couple_reset(SbeCouple* cp, void* stream);
+/* Sample Ex and E = (Ey, Ez) onto every wire (fills Ek).                       */
+int sbe_couple_sample(SbeCouple* cp, const double* Ex, const double* E, void* stream);
+/* Deposit the wire sources in src onto the grid (fills Pg and rho).            */
+int sbe_couple_deposit(SbeCouple* cp, void* stream);
+/* One coupled step t_n -> t_{n+1}: sample E^n, H update, RK4 step of every wire
+ * (precision SBE_PREC_FP64 or SBE_PREC_MIXED), deposit, J, E update, Ex.       */
+int sbe_couple_step(SbeCouple* cp, double* P, double* C, double* D, double* E, double* H,
+                    double* Ex, double dt, int precision, void* stream);
+/* CUDA graph of one sbe_couple_step on these buffers (replay with sbe_graph_launch). */
+int sbe_couple_graph_create(SbeCouple* cp, double* P, double* C, double* D, double* E, double* H,
+                            double* Ex, double dt, int precision, SbeGraph** out,
+                            long long* n_kernels);
+
 /* ---- kernel timing (no counterpart in the reference) ------------------------ */
 /* enable != 0: record CUDA events around the engine launches of category
  * 0 commutator GEMMs, 1 exchange GEMMs, 2 source GEMMs, 3 FP32 dephasing sums.

@@ -1,0 +1,212 @@
+"""CPU FP64 restatement of the 1-D PSTD field step and of its coupling to the wires.
+
+TEST INFRASTRUCTURE ONLY.  Imported by ``tests/`` and by ``bench.py``'s CPU
+baseline; nothing in ``pulsesuite_gb300`` imports or calls it.
+
+The reference has no 1-D Maxwell stepper (rahulranjansah/pulsesuite,
+``src/pulsesuite/...``); the step below assembles its pieces, each cited:
+
+* grids: positions ``GetSpaceArray`` (PSTD3D/typespace.py:815-849, numpy linspace),
+  wavenumbers in FFT order ``GetKArray`` (libpulsesuite/helpers.py:838-863);
+* spectral derivative ``dfdx1D`` = IFFT(i q FFT f) (PSTD3D/usefulsubs.py:163-185);
+* longitudinal field ``ElongfromRho`` (PSTD3D/rhoPJ.py:703-880), x component:
+  small = (q[1] - q[0]) / 1e4 (:779), rho_term = -i rho / (eps (q^2 + small)),
+  P_term = -(q Px) / (eps (q^2 + small)), Ex = IFFT((rho_term + P_term) q) (:836-866);
+* absorbing mask multiply as in ``ApplyABC`` (usefulsubs.py:584-609), with the
+  mask exp(-strength s^2) over n_abc cells at each end (s = depth fraction);
+* leapfrog for propagation along x: d_t Hz = -(1/mu0) d_x Ey, d_t Hy = (1/mu0) d_x Ez,
+  d_t Ey = -(1/eps)(d_x Hz + Jy), d_t Ez = (1/eps)(d_x Hy - Jz);
+* field -> wire: ``Prop2QW`` (PSTD3D/qwoptics.py:667-715) with the grid spline
+  evaluated at x_w + r; wire -> field: ``QW2Prop`` (qwoptics.py:717-805) of the
+  real-space sources at x - x_w, summed over wires; Rho = RhoH - RhoE (SBEs.py:5917).
+"""
+
+import numpy as np
+
+from . import sbe_oracle as O
+
+MU0 = 1.25663706127e-06   # scipy.constants.mu_0 (CODATA 2022)
+EPS0 = O.EPS0
+C0 = 299792458.0
+
+
+def pstd_grid(nx, dx):
+    """Positions (typespace.py:815-849) and FFT-order wavenumbers (helpers.py:838-863)."""
+    x = O.space_array(nx, (nx - 1) * dx)
+    dq = 2.0 * np.pi / (nx * dx)
+    i = np.arange(nx)
+    q = np.where(i <= nx // 2, i, i - nx).astype(float) * dq
+    return x, q
+
+
+def abc_mask(nx, n_abc, strength):
+    j = np.arange(nx)
+    d = np.minimum(j, nx - 1 - j)
+    m = np.ones(nx)
+    if n_abc > 0:
+        inl = d < n_abc
+        s = (n_abc - d[inl]) / n_abc
+        m[inl] = np.exp(-strength * s * s)
+    return m
+
+
+def deriv(f, q):
+    """usefulsubs.py:163-185 dfdx1D."""
+    return np.fft.ifft(np.fft.fft(np.asarray(f, complex)) * (1j * q))
+
+
+def elong(rho, px, q, epsr):
+    """rhoPJ.py:836-866 restricted to the x component."""
+    small = (q[1] - q[0]) / 1e4
+    inv_eps = 1.0 / (EPS0 * epsr)
+    rk = np.fft.fft(np.asarray(rho, complex))
+    pk = np.fft.fft(np.asarray(px, complex))
+    qs = q * q + small
+    rho_term = -1j * rk * inv_eps / qs
+    p_term = -(q * pk) * inv_eps / qs
+    return np.fft.ifft((rho_term + p_term) * q)
+
+
+def stable(dt, dx, epsr):
+    return C0 / np.sqrt(epsr) * dt * np.pi / dx <= 2.0
+
+
+class Pstd1D:
+    """Field state E = (Ey, Ez), H = (Hz, Hy) on the grid (2 x nx complex each)."""
+
+    def __init__(self, nx, dx, epsr, n_abc=0, strength=0.0):
+        self.nx, self.dx, self.epsr = nx, dx, epsr
+        self.x, self.q = pstd_grid(nx, dx)
+        self.mask = abc_mask(nx, n_abc, strength)
+        self.masked = n_abc > 0
+
+    def update_h(self, E, H, dt):
+        a = dt / MU0
+        H = H.copy()
+        H[0] = H[0] + (-a) * deriv(E[0], self.q)
+        H[1] = H[1] + a * deriv(E[1], self.q)
+        if self.masked:
+            H = H * self.mask
+        return H
+
+    def update_e(self, E, H, J, dt):
+        ie = dt / (EPS0 * self.epsr)
+        E = E.copy()
+        E[0] = E[0] + (-ie) * deriv(H[0], self.q)
+        E[1] = E[1] + ie * deriv(H[1], self.q)
+        if J is not None:
+            E[0] = E[0] + (-ie) * J[0]
+            E[1] = E[1] + (-ie) * J[1]
+        if self.masked:
+            E = E * self.mask
+        return E
+
+    def step(self, E, H, J, dt):
+        H = self.update_h(E, H, dt)
+        return self.update_e(E, H, J, dt), H
+
+    def energy(self, E, H_prev, H_next):
+        """Discrete invariant of the leapfrog (no mask, no current):
+        eps |E^n|^2 + mu0 Re(H^{n-1/2} . conj(H^{n+1/2})), summed over the grid."""
+        e = EPS0 * self.epsr * np.sum(np.abs(E) ** 2)
+        h = MU0 * np.sum(np.real(H_prev * np.conj(H_next)))
+        return e + h
+
+
+def rescale_vec(x0, b, c, d, z0, x1):
+    """Vectorised spliner.py:153-189 evaluation with precomputed coefficients
+    (locate = binary search, spliner.py:1137-1167; 0 outside [x0[0], x0[-1]])."""
+    x1 = np.asarray(x1, float)
+    out = np.zeros(len(x1), complex)
+    n = len(x0)
+    ok = (x1 >= x0[0]) & (x1 <= x0[n - 1])
+    u = x1[ok]
+    j = np.searchsorted(x0, u, side="right") - 1
+    j = np.clip(j, 0, n - 1)
+    dx = u - x0[j]
+    z0 = np.asarray(z0, complex)
+    out[ok] = z0[j] + dx * (b[j] + dx * (c[j] + dx * d[j]))
+    return out
+
+
+class CoupledLine:
+    """Wires on the 1-D grid (one oracle ``Wire`` per wire, its 1-based index and
+    centre position) with a soft-source current sheet at cell ``src_index``."""
+
+    def __init__(self, pstd, wires, windex, wx, src_index=-1, E0=0.0, tau=1.0, w0=0.0,
+                 tpeak=0.0, t0=0.0, longitudinal=True):
+        self.p = pstd
+        self.wires = wires
+        self.windex = list(windex)
+        self.wx = np.asarray(wx, float)
+        self.src_index, self.E0, self.tau, self.w0, self.tpeak, self.t0 = (
+            src_index, E0, tau, w0, tpeak, t0)
+        self.longitudinal = longitudinal
+        self.eta = np.sqrt(MU0 / (EPS0 * pstd.epsr))
+        nx = pstd.nx
+        self.Pold = np.zeros((3, nx), complex)
+        self.n = 0
+
+    def sample(self, Ex, E):
+        """Grid fields at time t_n on every wire: [Ex_k, Ey_k, Ez_k] per wire."""
+        x = self.p.x
+        coefs = [O.spline_coeffs(x, f) for f in (Ex, E[0], E[1])]
+        out = []
+        for wi, xw in zip(self.wires, self.wx):
+            u = xw + wi.g["r"]
+            ek = []
+            for f, (b, c, d) in zip((Ex, E[0], E[1]), coefs):
+                v = rescale_vec(x, b, c, d, f, u) * wi.window
+                ek.append(O.fftg(np.real(v).astype(complex)))
+            out.append(ek)
+        return out
+
+    def deposit(self, srcs):
+        """srcs: per wire real-space (Px, Py, Pz, re, rh).  Returns (Pg (3, nx), rho)."""
+        x = self.p.x
+        nx = self.p.nx
+        Pg = np.zeros((3, nx), complex)
+        rho = np.zeros(nx, complex)
+        for wi, xw, s in zip(self.wires, self.wx, srcs):
+            r = wi.g["r"]
+            u = x - xw
+            vals = []
+            for comp in s:
+                b, c, d = O.spline_coeffs(r, comp)
+                vals.append(rescale_vec(r, b, c, d, comp, u))
+            for k in range(3):
+                Pg[k] = Pg[k] + vals[k]
+            rho = rho + (vals[4] - vals[3])
+        return Pg, rho
+
+    def current(self, Pg, dt):
+        J = np.zeros((2, self.p.nx), complex)
+        J[0] = (Pg[1] - self.Pold[1]) / dt
+        J[1] = (Pg[2] - self.Pold[2]) / dt
+        if self.src_index >= 0:
+            th = self.t0 + (self.n + 0.5) * dt
+            a = (th - self.tpeak) / self.tau
+            einc = np.exp(-a * a) * np.cos(self.w0 * (th - self.tpeak))
+            jamp = -2.0 * self.E0 / (self.eta * self.p.dx)
+            J[0, self.src_index] += jamp * einc
+        self.Pold = Pg.copy()
+        return J
+
+    def step(self, states, E, H, Ex, dt):
+        """states: per wire [P, C, D] (updated in place).  Returns (E, H, Ex, srcs)."""
+        eks = self.sample(Ex, E)
+        H = self.p.update_h(E, H, dt)
+        srcs = []
+        z = [np.zeros_like(eks[0][0])] * 3
+        for i, (wi, st) in enumerate(zip(self.wires, states)):
+            P, C, D, Px, Py, Pz, re, rh = wi.rk4_step(st[0], st[1], st[2], eks[i], z, dt,
+                                                     self.windex[i])
+            st[0], st[1], st[2] = P, C, D
+            srcs.append([O.ifftg(a) for a in (Px, Py, Pz, re, rh)])
+        Pg, rho = self.deposit(srcs)
+        J = self.current(Pg, dt)
+        E = self.p.update_e(E, H, J, dt)
+        if self.longitudinal:
+            Ex = elong(rho, Pg[0], self.p.q, self.p.epsr)
+        self.n += 1
+        return E, H, Ex, srcs

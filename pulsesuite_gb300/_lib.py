@@ -29,6 +29,11 @@ EXPORTS = (
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
     "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
     "sbe_ctx_profile", "sbe_ctx_profile_read", "sbe_prop2qw_noalloc",
+    "sbe_pstd_create", "sbe_pstd_destroy", "sbe_pstd_grid", "sbe_pstd_deriv", "sbe_pstd_update_h",
+    "sbe_pstd_update_e", "sbe_pstd_step", "sbe_pstd_elong", "sbe_couple_create",
+    "sbe_couple_destroy", "sbe_couple_buffers", "sbe_couple_set_step", "sbe_couple_reset",
+    "sbe_couple_sample",
+    "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
 )
 
 
@@ -39,6 +44,19 @@ class SbeWireDesc(ctypes.Structure):
                 ("HO", ctypes.c_double), ("gam_e", ctypes.c_double), ("gam_h", ctypes.c_double),
                 ("gam_eh", ctypes.c_double), ("epsr", ctypes.c_double), ("Oph", ctypes.c_double),
                 ("Gph", ctypes.c_double), ("temp", ctypes.c_double)]
+
+
+class SbePstdDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("n_abc", ctypes.c_int), ("pad0", ctypes.c_int),
+                ("pad1", ctypes.c_int), ("dx", ctypes.c_double), ("epsr", ctypes.c_double),
+                ("abc_strength", ctypes.c_double)]
+
+
+class SbeCoupleDesc(ctypes.Structure):
+    _fields_ = [("src_index", ctypes.c_int), ("longitudinal", ctypes.c_int),
+                ("pad0", ctypes.c_int), ("pad1", ctypes.c_int), ("E0", ctypes.c_double),
+                ("tau", ctypes.c_double), ("w0", ctypes.c_double), ("tpeak", ctypes.c_double),
+                ("t0", ctypes.c_double)]
 
 
 class SbeError(RuntimeError):
@@ -88,6 +106,23 @@ def load(path=LIB_PATH):
         "sbe_graph_destroy": [P],
         "sbe_ctx_profile": [P, I],
         "sbe_ctx_profile_read": [P, I, P, P],
+        "sbe_pstd_create": [P, P, P],
+        "sbe_pstd_destroy": [P],
+        "sbe_pstd_grid": [P, P, P, P],
+        "sbe_pstd_deriv": [P, P, I, P, P],
+        "sbe_pstd_update_h": [P, P, P, Dbl, P],
+        "sbe_pstd_update_e": [P, P, P, P, Dbl, P],
+        "sbe_pstd_step": [P, P, P, P, Dbl, P],
+        "sbe_pstd_elong": [P, P, P, P, P],
+        "sbe_couple_create": [P, P, P, P, P, P],
+        "sbe_couple_destroy": [P],
+        "sbe_couple_buffers": [P, P, P, P, P, P],
+        "sbe_couple_set_step": [P, ctypes.c_longlong, P],
+        "sbe_couple_reset": [P, P],
+        "sbe_couple_sample": [P, P, P, P],
+        "sbe_couple_deposit": [P, P],
+        "sbe_couple_step": [P, P, P, P, P, P, P, Dbl, I, P],
+        "sbe_couple_graph_create": [P, P, P, P, P, P, P, Dbl, I, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

@@ -586,23 +586,26 @@ struct SbeGraph {
   cudaGraphExec_t exec = nullptr;
 };
 
-int sbe_rk4_graph_create(SbeCtx* c, double* P, double* C, double* D, const double* Ek0,
-                         const double* dEk, double dt, int precision, double* src_out,
-                         SbeGraph** out, long long* n_kernels) {
-  if (!c || !out) return fail(SBE_ERR_ARG, "sbe_rk4_graph_create: null");
+}  // extern "C"
+
+namespace sbe {
+// Runs body once on a private non-blocking stream under capture and instantiates
+// the graph.  The mixed workspace is prepared (allocated) before the capture.
+int capture_graph(SbeCtx* c, int precision, const std::function<int(cudaStream_t)>& body,
+                  SbeGraph** out, long long* n_kernels) {
   *out = nullptr;
-  if (c->prof) return fail(SBE_ERR_ARG, "sbe_rk4_graph_create: disable profiling first");
+  if (c->prof) return fail(SBE_ERR_ARG, "graph capture: disable profiling first");
   cudaStream_t cs;
   if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
-    return fail(SBE_ERR_CUDA, "sbe_rk4_graph_create: stream");
+    return fail(SBE_ERR_CUDA, "graph capture: stream");
   int rc = SBE_OK;
-  if (precision == SBE_PREC_MIXED) rc = sbe::mixed_prepare(c, cs);
+  if (precision == SBE_PREC_MIXED) rc = mixed_prepare(c, cs);
   if (rc == SBE_OK) rc = cuda_check(cudaStreamSynchronize(cs), "graph warm-up");
   cudaGraph_t g = nullptr;
   if (rc == SBE_OK) {
     rc = cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
     if (rc == SBE_OK) {
-      int rc2 = sbe_rk4_step(c, P, C, D, Ek0, dEk, dt, precision, src_out, (void*)cs);
+      int rc2 = body(cs);
       rc = cuda_check(cudaStreamEndCapture(cs, &g), "end capture");
       if (rc2) rc = rc2;
     }
@@ -630,6 +633,21 @@ int sbe_rk4_graph_create(SbeCtx* c, double* P, double* C, double* D, const doubl
   cudaStreamDestroy(cs);
   *out = sg;
   return rc;
+}
+}  // namespace sbe
+
+extern "C" {
+
+int sbe_rk4_graph_create(SbeCtx* c, double* P, double* C, double* D, const double* Ek0,
+                         const double* dEk, double dt, int precision, double* src_out,
+                         SbeGraph** out, long long* n_kernels) {
+  if (!c || !out) return fail(SBE_ERR_ARG, "sbe_rk4_graph_create: null");
+  return sbe::capture_graph(
+      c, precision,
+      [&](cudaStream_t cs) {
+        return sbe_rk4_step(c, P, C, D, Ek0, dEk, dt, precision, src_out, (void*)cs);
+      },
+      out, n_kernels);
 }
 
 int sbe_graph_launch(SbeGraph* g, void* stream) {

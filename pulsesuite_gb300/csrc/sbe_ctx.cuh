@@ -1,5 +1,7 @@
 // Host-side context of libsbe_gb300: per-wire descriptors and the device arena.
 #pragma once
+#include <functional>
+
 #include "sbe_internal.cuh"
 
 struct SbeCtx {
@@ -167,6 +169,8 @@ int launch_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double2* 
                    double2* out, cudaStream_t s);
 int launch_prop2qw_scratch(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
                            double2* out, double2* coef, double2* tmp, cudaStream_t s);
+int capture_graph(SbeCtx* c, int precision, const std::function<int(cudaStream_t)>& body,
+                  SbeGraph** out, long long* n_kernels);
 int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* src,
                    double2* out, int plasmonics, cudaStream_t s);
 }  // namespace sbe

@@ -25,6 +25,10 @@ qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
                 and ``QW2Prop`` (cubic-spline resampling + FFTG).
 solver_step     ``SBEs.SBESolver`` built from params files, several
                 ``QWCalculator`` leapfrog steps on two wires.
+pstd            Pieces of the field step: ``usefulsubs.dfdx1D`` on FFT-order
+                wavenumbers (``libpulsesuite.helpers.GetKArray``), the grids of
+                ``typespace`` and ``helpers``, and ``rhoPJ.ElongfromRho`` on an
+                (Nx, 1, 1) grid.
 """
 
 import io
@@ -411,6 +415,28 @@ def case_solver(L, nsteps, dt, E0, seed):
     return out
 
 
+def case_pstd(nx, dx, seed):
+    from pulsesuite.PSTD3D import rhoPJ, typespace, usefulsubs
+    from pulsesuite.libpulsesuite import helpers
+    rng = np.random.default_rng(seed)
+    q = helpers.GetKArray(nx, nx * dx)
+    x_h = helpers.GetSpaceArray(nx, (nx - 1) * dx)
+    x_t = typespace.GetSpaceArray(nx, (nx - 1) * dx)
+    f = cnormal(rng, (nx,), 1.0)
+    df = usefulsubs.dfdx1D(f.copy(), q)
+    sp = typespace.ss(1, nx, 1, 1, dx, 1.0, 1.0, 12.9)
+    qx = typespace.GetKxArray(sp)
+    epsr_used = typespace.GetEpsr(sp)
+    rho = cnormal(rng, (nx, 1, 1), 1.0)
+    px = cnormal(rng, (nx, 1, 1), 1e-9)
+    outs = [np.zeros((nx, 1, 1), complex) for _ in range(10)]
+    z = np.zeros((nx, 1, 1), complex)
+    rhoPJ.ElongfromRho(sp, rho.copy(), px.copy(), z.copy(), z.copy(), *outs)
+    return dict(nx=nx, dx=dx, q=q, x_helpers=x_h, x_typespace=x_t, f=f, df=df, qx_space=qx,
+                epsr_space=epsr_used, rho=rho[:, 0, 0], px=px[:, 0, 0],
+                Exl_PRho=outs[0][:, 0, 0], Exl_P=outs[3][:, 0, 0], Exl_Rho=outs[6][:, 0, 0])
+
+
 def main():
     ref_src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PULSESUITE_SRC")
     if not ref_src or not os.path.isdir(ref_src):
@@ -437,6 +463,7 @@ def main():
                     np.savez_compressed(os.path.join(HERE, f"dephasing_nk{nk}.npz"), **de)
                     qo = case_qwoptics(nk, seed + 300)
                     np.savez_compressed(os.path.join(HERE, f"qwoptics_nk{nk}.npz"), **qo)
+                np.savez_compressed(os.path.join(HERE, "pstd.npz"), **case_pstd(256, 10e-9, 50))
                 so = case_solver(14.5e-9, 3, 0.1e-15, 2e7, 40)
                 np.savez_compressed(os.path.join(HERE, "solver_step.npz"), **so)
         finally:
