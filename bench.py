@@ -300,6 +300,7 @@ def gpu_arm(args, wl):
         dist.barrier()
     prof = {cat: ctx.profile_read(cat) for cat in range(4)}
     ctx.profile(False)
+    ctx.check()
     value = world * nw * args.steps / (ms / 1e3)
 
     # CUDA graph of the same coupled step (launch count, replay time)

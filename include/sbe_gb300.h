@@ -264,6 +264,11 @@ int sbe_couple_graph_create(SbeCouple* cp, double* P, double* C, double* D, doub
 int sbe_ctx_profile(SbeCtx* ctx, int enable);
 int sbe_ctx_profile_read(SbeCtx* ctx, int category, double* total_ms, long long* launches);
 
+/* ---- device-side error flags (no counterpart in the reference) ------------- */
+/* Waits for the stream, then reports whether a bounded wait of the tensor-core
+ * engine gave up since the last check (SBE_ERR_TIMEOUT; the flags are cleared). */
+int sbe_ctx_check(SbeCtx* ctx, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Diagnostic entry, no counterpart in the reference: out[b] = op(A[b]) op(B[b])
  * for a batch of Nk x Nk matrices through the tcgen05 split-precision engine
@@ -271,6 +276,12 @@ int sbe_ctx_profile_read(SbeCtx* ctx, int category, double* total_ms, long long*
  * only (out imaginary parts are 0).  Nk must be a multiple of 8.               */
 int sbe_tc_selftest(int nk, int nbatch, const double* A, const double* B, int opA, int opB,
                     int complex_mode, double* out, void* stream);
+/* Diagnostic entry, no counterpart in the reference: the integer-pipe FP64 ->
+ * FP32 (round to nearest even; results below 2^-126 flush to zero) and exact
+ * FP32 -> FP64 conversions the mixed path uses: f_out[i] = fp32(d_in[i]),
+ * d_out[i] = fp64(f_in[i]).                                                    */
+int sbe_convert_selftest(const double* d_in, const float* f_in, long long n, float* f_out,
+                         double* d_out, void* stream);
 
 #ifdef __cplusplus
 }

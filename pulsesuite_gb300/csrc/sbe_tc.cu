@@ -1,26 +1,36 @@
 // Mixed-precision (tcgen05) path of the SBE right-hand side: FP16 hi/lo plane
-// conversion, per-wire power-of-two scaling and the self-test entry point.
+// conversion, per-wire power-of-two scaling, the stage pipeline and the
+// self-test entry point.
+//
+// GB300 executes FP64 arithmetic and the double <-> float conversions at a
+// small fraction of its FP32 rate, so the per-element code of this file uses
+// FP32 arithmetic and the integer-pipe conversions of fp_bits.cuh.  FP64
+// arithmetic is kept where the result needs it: the RK4 accumulation of the
+// state and the peeled diagonal energies (formed once per row).
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
+#include "fp_bits.cuh"
 #include "sbe_ctx.cuh"
 #include "tc_gemm.cuh"
 
 namespace sbe {
 
 // ---------------------------------------------------------------------------
-// max(|re|, |im|) of each batch entry of a packed complex array (float bits,
-// atomicMax on the unsigned pattern of a non-negative float).
+// max(|re|, |im|) of each batch entry of a packed complex array (integer compare
+// of the magnitudes' bit patterns; atomicMax on the pattern of the FP32 value).
 __global__ void k_absmax(const double2* X, long long per_batch, long long bstride, unsigned* out) {
   const int b = blockIdx.y;
   const double2* x = X + (long long)b * bstride;
-  float m = 0.f;
+  unsigned long long m = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_batch;
        i += (long long)gridDim.x * blockDim.x) {
-    double2 v = x[i];
-    m = fmaxf(m, (float)fmax(fabs(v.x), fabs(v.y)));
+    const double2 v = x[i];
+    m = max(m, max(absbits(v.x), absbits(v.y)));
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out + b, __float_as_uint(m));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + b, bits_to_fmax(m));
 }
 
 // e[b] = 14 - ceil(log2(max)): scaled magnitudes stay <= 2^14 (FP16 max 65504).
@@ -31,6 +41,20 @@ __global__ void k_exponents(int nb, const unsigned* mx, int* e, const int* add, 
   int v = (m > 0.f) ? 14 - (int)ceilf(log2f(m)) : 0;
   e[b] = v;
   if (sum) sum[b] = v + (add ? add[b] : 0);
+}
+
+// e[b] from the larger of two maxima (same rule as k_exponents)
+__global__ void k_exponents2(int nb, const unsigned* mx1, const unsigned* mx2, int* e) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  float m = fmaxf(__uint_as_float(mx1[b]), __uint_as_float(mx2[b])) * 1.0001f;
+  e[b] = (m > 0.f) ? 14 - (int)ceilf(log2f(m)) : 0;
+}
+
+__device__ __forceinline__ void put_hilo(__half* base, long long plane, float v) {
+  const __half h = __float2half_rn(v);
+  base[0] = h;
+  base[plane] = __float2half_rn(v - __half2float(h));
 }
 
 // FP16 hi/lo planes of a batch of Nk x Nk complex matrices, scaled by 2^e[b];
@@ -50,7 +74,7 @@ __global__ void k_planes(const double2* X, long long bstride, int nk, int transp
     tile[i][threadIdx.x] = (r < nk && c < nk) ? x[(long long)r * nk + c] : make_double2(0, 0);
   }
   __syncthreads();
-  const double sc = ldexp(1.0, e[b]);
+  const int eb = e[b];
   const long long plane = (long long)nbatch * nk * nk;
   __half* base = dst + ((long long)mat * nplanes) * plane + (long long)b * nk * nk;
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
@@ -58,17 +82,9 @@ __global__ void k_planes(const double2* X, long long bstride, int nk, int transp
     if (r >= nk || c >= nk) continue;
     double2 v = transpose ? tile[threadIdx.x][i] : tile[i][threadIdx.x];
     long long o = (long long)r * nk + c;
-    // scale in FP64 (exact), round once to FP32 (24 bits >= the 22 the planes
-    // keep) and split in FP32: the FP64 pipe is the scarce one on GB300
-    const float vr = (float)(v.x * sc), vi = (float)(v.y * sc);
-    const __half rh = __float2half_rn(vr);
-    base[o] = rh;
-    base[plane + o] = __float2half_rn(vr - __half2float(rh));
-    if (!real_only) {
-      const __half ih = __float2half_rn(vi);
-      base[2 * plane + o] = ih;
-      base[3 * plane + o] = __float2half_rn(vi - __half2float(ih));
-    }
+    // exact scaling and one rounding to FP32 (24 bits >= the 22 the planes keep)
+    put_hilo(base + o, plane, f64_to_f32(v.x, eb));
+    if (!real_only) put_hilo(base + 2 * plane + o, plane, f64_to_f32(v.y, eb));
   }
 }
 
@@ -78,6 +94,51 @@ void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int 
   dim3 blk(32, 8), grid((nk + 31) / 32, (nk + 31) / 32, nbatch);
   k_planes<<<grid, blk, 0, s>>>(X, bstride, nk, transpose, e, dst, mat, nplanes, nbatch,
                                 real_only);
+}
+
+// Both layouts of a batch of Nk x Nk complex matrices from one read: planes of X
+// into matrix slot matN and of X^T into slot matT (matT < 0: none), same scale.
+template <typename T>
+__device__ __forceinline__ float2 scaled2(T v, int e);
+template <>
+__device__ __forceinline__ float2 scaled2<double2>(double2 v, int e) {
+  return f64_to_f32(v, e);
+}
+template <>
+__device__ __forceinline__ float2 scaled2<float2>(float2 v, int e) {
+  return make_float2(f32_ldexp(v.x, e), f32_ldexp(v.y, e));
+}
+
+template <typename T>
+__global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int matN, int matT,
+                            int nbatch) {
+  __shared__ T tile[32][33];
+  const int b = blockIdx.z;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const T* x = X + (long long)b * nk * nk;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    T z;
+    z.x = 0;
+    z.y = 0;
+    tile[i][threadIdx.x] = (r < nk && c < nk) ? x[(long long)r * nk + c] : z;
+  }
+  __syncthreads();
+  const int eb = e[b];
+  const long long plane = (long long)nbatch * nk * nk;
+  __half* bn = dst + (long long)matN * 4 * plane + (long long)b * nk * nk;
+  __half* bt = dst + (long long)(matT < 0 ? 0 : matT) * 4 * plane + (long long)b * nk * nk;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    for (int pass = 0; pass < (matT < 0 ? 1 : 2); ++pass) {
+      // pass 0: row r0 + i of X;  pass 1: row c0 + i of X^T (= column c0 + i of X)
+      const int r = (pass ? c0 : r0) + i, c = (pass ? r0 : c0) + threadIdx.x;
+      if (r >= nk || c >= nk) continue;
+      const float2 v = scaled2<T>(pass ? tile[threadIdx.x][i] : tile[i][threadIdx.x], eb);
+      __half* base = (pass ? bt : bn) + (long long)r * nk + c;
+      put_hilo(base, plane, v.x);
+      put_hilo(base + 2 * plane, plane, v.y);
+    }
+  }
 }
 
 void launch_exponents(const double2* X, long long per_batch, long long bstride, int nbatch,
@@ -91,20 +152,32 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 // ---------------------------------------------------------------------------
 // Mixed-precision workspace of a context (uniform Nk and flags over its wires).
 //
-// Commutator planes: 14 matrices x 4 planes x Nw x Nk x Nk (FP16):
-//   0 P, 1 P^T, 2 C, 3 C^T, 4 D, 5 D^T            (state, exponent eS)
-//   6 Heh, 7 Heh^T, 8 Hee', 9 Hee'^T, 10 Hhh', 11 Hhh'^T,
-//   12 Hee' + i hbar B, 13 Hhh' + i hbar A         (Hamiltonians, exponent eH)
-// (' = diagonal removed; A, B = off-diagonal dephasing matrices).
+// Commutator planes: 14 matrix slots x 4 planes x Nw x Nk x Nk (FP16):
+//   0 P, 1 P^T, 2 C, 4 D                            (state, exponent eS)
+//   6 Heh, 7 Heh^T, 8 Hee', 10 Hhh',
+//   12 Hee' + i hbar B, 13 Hhh' + i hbar A          (Hamiltonians, exponent eH)
+// (' = diagonal removed; A, B = off-diagonal dephasing matrices; C^T = conj C and
+// D^T = conj D are taken by conjugating the C and D operands).
 // Exchange: Toeplitz planes T_n (3 x 2 x Nw x Nk x Nk) and sheared state planes
 // S_n (3 x 2 x Nw x 4Nk x Nk).  Sources: E^T planes (4 x Nw x Nr x Nk).
+// Stage values in FP32: kf (dP, dC, dD), accf (RK4 sums), Hf (Heh, Hee', Hhh'),
+// Wf (W, V of the W - W^H form, in the G buffer).
 struct Mixed {
   int nk = 0, nw = 0, nr = 0;
   __half *planes = nullptr, *tpl = nullptr, *spl = nullptr, *epl = nullptr;
-  float* xsh = nullptr;  // exchange sums in the sheared layout: 3 x Nw x Nk x 4Nk
-  int* ints = nullptr;   // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
-  unsigned* mx = nullptr;
-  double2 *dgE = nullptr, *dgH = nullptr;
+  float* xsh = nullptr;    // exchange sums in the sheared layout: 3 x Nw x Nk x 4Nk
+  int* ints = nullptr;     // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
+  unsigned* mx = nullptr;  // [0, nw): Hamiltonian maximum; [nw, 2nw): state; [2nw, 3nw): hbar A/B
+  float2* kf = nullptr;    // 3 x tot_mat stage derivatives
+  float2* accf = nullptr;  // 3 x tot_mat RK4 sums k1 + 2 k2 + 2 k3
+  float2* hf = nullptr;    // 3 x tot_mat Heh, Hee', Hhh'
+  float* habf = nullptr;   // 2 x tot_mat hbar A, hbar B
+  float2* ekf = nullptr;   // 3 x tot_r stage field
+  float* vsf = nullptr;    // 3 x nw x nk screened V by |k1 - k2|
+  float2* trf = nullptr;   // 4 x nw x nk traces [2][2nk]
+  float* gamf = nullptr;   // 2 x nw x nk GamE, GamH
+  float2* dgf = nullptr;   // 4 x nw x nk: hi and lo parts of the peeled Hee, Hhh diagonals
+  double2 *dgE = nullptr, *dgH = nullptr;  // the peeled diagonals in FP64
   CUtensorMap mapA, mapB, mapTA, mapSB, mapEB;
   int* eS() { return ints; }
   int* eH() { return ints + nw; }
@@ -114,6 +187,9 @@ struct Mixed {
   int* esx() { return ints + 5 * nw; }
   int* ess() { return ints + 6 * nw; }
   int* err() { return ints + 7 * nw; }
+  unsigned* mxH() { return mx; }
+  unsigned* mxS() { return mx + nw; }
+  unsigned* mxAB() { return mx + 2 * nw; }
 };
 
 enum { M_P = 0, M_PT, M_C, M_CT, M_D, M_DT, M_EH, M_EHT, M_EE, M_EET, M_HH, M_HHT, M_EEX, M_HHX };
@@ -128,6 +204,7 @@ void mixed_free(SbeCtx* c) {
   cudaFree(m->xsh);
   cudaFree(m->ints);
   cudaFree(m->mx);
+  cudaFree(m->kf);
   cudaFree(m->dgE);
   delete m;
   c->mixed = nullptr;
@@ -142,12 +219,8 @@ __global__ void k_eplanes(const WireDev* wires, const double2* expikr, __half* d
   double2 v = expikr[W.off_kr + (long long)k * W.nr + r];
   const long long plane = (long long)nw * W.nr * W.nk;
   long long o = (long long)blockIdx.z * W.nr * W.nk + (long long)r * W.nk + k;
-  double vr = ldexp(v.x, 13), vi = ldexp(v.y, 13);
-  __half rh = __double2half(vr), ih = __double2half(vi);
-  dst[o] = rh;
-  dst[plane + o] = __double2half(vr - (double)__half2float(rh));
-  dst[2 * plane + o] = ih;
-  dst[3 * plane + o] = __double2half(vi - (double)__half2float(ih));
+  put_hilo(dst + o, plane, f64_to_f32(v.x, 13));
+  put_hilo(dst + 2 * plane + o, plane, f64_to_f32(v.y, 13));
 }
 
 __global__ void k_fill_int(int* p, int n, int v) {
@@ -167,22 +240,38 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   m->nk = nk;
   m->nw = nw;
   m->nr = 2 * nk + 2;
-  const size_t mm = (size_t)nk * nk;
+  const size_t mm = (size_t)nk * nk, tm = (size_t)nw * mm, tr = (size_t)nw * m->nr;
+  // one block for the FP32 stage buffers
+  const size_t fbytes = sizeof(float2) * (3 * tm + 3 * tm + 3 * tm + 3 * tr + 4 * (size_t)nw * nk +
+                                          4 * (size_t)nw * nk) +
+                        sizeof(float) * (2 * tm + 3 * (size_t)nw * nk + 2 * (size_t)nw * nk);
+  void* fblock = nullptr;
   bool ok = cudaMalloc(&m->planes, sizeof(__half) * 14 * 4 * nw * mm) == cudaSuccess &&
             cudaMalloc(&m->tpl, sizeof(__half) * 3 * 2 * nw * mm) == cudaSuccess &&
             cudaMalloc(&m->spl, sizeof(__half) * 3 * 2 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->epl, sizeof(__half) * 4 * nw * (size_t)m->nr * nk) == cudaSuccess &&
             cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->ints, sizeof(int) * 8 * nw) == cudaSuccess &&
-            cudaMalloc(&m->mx, sizeof(unsigned) * nw) == cudaSuccess &&
+            cudaMalloc(&m->mx, sizeof(unsigned) * 3 * nw) == cudaSuccess &&
+            cudaMalloc(&fblock, fbytes) == cudaSuccess &&
             cudaMalloc(&m->dgE, sizeof(double2) * 2 * nw * nk) == cudaSuccess;
+  m->kf = static_cast<float2*>(fblock);
   if (!ok) {
     c->mixed = m;
     mixed_free(c);
     return fail(SBE_ERR_OOM, "mixed path: workspace allocation failed");
   }
+  m->accf = m->kf + 3 * tm;
+  m->hf = m->accf + 3 * tm;
+  m->ekf = m->hf + 3 * tm;
+  m->trf = m->ekf + 3 * tr;
+  m->dgf = m->trf + 4 * (size_t)nw * nk;
+  m->habf = reinterpret_cast<float*>(m->dgf + 4 * (size_t)nw * nk);
+  m->vsf = m->habf + 2 * tm;
+  m->gamf = m->vsf + 3 * (size_t)nw * nk;
   m->dgH = m->dgE + (size_t)nw * nk;
   cudaMemsetAsync(m->ints, 0, sizeof(int) * 8 * nw, s);
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 3 * nw, s);
   TcPlanes pl{m->planes, 14, 4, nw, nk, nk};
   TcPlanes tp{m->tpl, 3, 2, nw, nk, nk};
   TcPlanes sp{m->spl, 3, 2, nw, 4 * nk, nk};
@@ -202,30 +291,18 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   return cuda_check(cudaGetLastError(), "mixed workspace");
 }
 
-// generic per-batch max over several arrays (scaled by fac)
-__global__ void k_absmax_f(const double2* X, long long per_batch, long long bstride, double fac,
-                           unsigned* out) {
-  const int b = blockIdx.y;
-  const double2* x = X + (long long)b * bstride;
-  float m = 0.f;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_batch;
-       i += (long long)gridDim.x * blockDim.x) {
-    double2 v = x[i];
-    m = fmaxf(m, (float)(fac * fmax(fabs(v.x), fabs(v.y))));
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out + b, __float_as_uint(m));
-}
-
-static void absmax_into(const double2* X, long long per, int nw, double fac, unsigned* mx,
-                        cudaStream_t s) {
+static void absmax_into(const double2* X, long long per, int nw, unsigned* mx, cudaStream_t s) {
   int blocks = (int)std::min<long long>((per + 255) / 256, 128);
-  k_absmax_f<<<dim3(blocks, nw), 256, 0, s>>>(X, per, per, fac, mx);
+  k_absmax<<<dim3(blocks, nw), 256, 0, s>>>(X, per, per, mx);
 }
 
-// Toeplitz exchange planes T_n[t][t'] = vs_n(|t - t'|) (t != t'), real.
+// ---------------------------------------------------------------------------
+// Per-step tables of the mixed path (coefficients frozen over the step).
+
+// Toeplitz exchange planes T_n[t][t'] = vs_n(|t - t'|) (t != t'), real; and the
+// FP32 copy of vs for the direct terms.
 __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const int* e,
-                                  __half* dst, int nw) {
+                                  __half* dst, int nw, float* vsf) {
   const int b = blockIdx.z / 3, n = blockIdx.z % 3;
   const WireDev W = wires[b];
   const int nk = W.nk;
@@ -233,97 +310,166 @@ __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const 
   int t = blockIdx.y;
   if (tp >= nk || t >= nk) return;
   int d = t > tp ? t - tp : tp - t;
-  double v = (d == 0) ? 0.0 : ldexp(vs[3 * W.off_vec + n * nk + d], e[b]);
+  const double vd = vs[3 * W.off_vec + n * nk + d];
+  if (t == 0) vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(vd);
+  const float v = (d == 0) ? 0.f : f64_to_f32(vd, e[b]);
   const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
-  __half* base = dst + (long long)n * 2 * plane + (long long)b * mm + (long long)t * nk + tp;
-  __half h = __double2half(v);
-  base[0] = h;
-  base[plane] = __double2half(v - (double)__half2float(h));
+  put_hilo(dst + (long long)n * 2 * plane + (long long)b * mm + (long long)t * nk + tp, plane, v);
 }
 
 __global__ void k_vs_max(const WireDev* wires, const double* vs, unsigned* mx) {
   const WireDev W = wires[blockIdx.x];
-  float m = 0.f;
-  for (int i = threadIdx.x; i < 3 * W.nk; i += blockDim.x)
-    m = fmaxf(m, (float)fabs(vs[3 * W.off_vec + i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.x, __float_as_uint(m));
+  unsigned long long m = 0;
+  for (int i = threadIdx.x; i < 3 * W.nk; i += blockDim.x) m = max(m, absbits(vs[3 * W.off_vec + i]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.x, bits_to_fmax(m));
 }
+
+// hbar A and hbar B in FP32 (dephasing.py:714-743 contraction matrices A[k][j] =
+// Dh[j - k][k], B[k][j] = De[j - k][k], j != k) and max(2 hbar |A|, 2 hbar |B|).
+__global__ void k_hab(const WireDev* wires, const double* De, const double* Dh, float* habf,
+                      long long tot_mat, unsigned* mx) {
+  const WireDev W = wires[blockIdx.z];
+  const int nk = W.nk;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
+  float m = 0.f;
+  if (j < nk && row < nk) {
+    const bool on = (W.flags & SBE_F_OFFDIAGDPH) && j != row;
+    const long long di = W.off_dd + (long long)(j - row + nk) * nk + row;
+    const float ha = on ? (float)kHbar * f64_to_f32(Dh[di]) : 0.f;
+    const float hb = on ? (float)kHbar * f64_to_f32(De[di]) : 0.f;
+    const long long o = W.off_mat + (long long)row * nk + j;
+    habf[o] = ha;
+    habf[tot_mat + o] = hb;
+    m = 2.f * fmaxf(fabsf(ha), fabsf(hb));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(m));
+}
+
+__global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH, float* gamf,
+                        int nw) {
+  const WireDev W = wires[blockIdx.y];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= W.nk) return;
+  gamf[(long long)blockIdx.y * W.nk + k] = f64_to_f32(gE[W.off_vec + k]);
+  gamf[((long long)nw + blockIdx.y) * W.nk + k] = f64_to_f32(gH[W.off_vec + k]);
+}
+
+// ---------------------------------------------------------------------------
+// Per-stage kernels.
 
 // Sheared state planes: row 2 dd + c (dd = d + Nk - 1, c = re / im), column t':
 // S[2dd + c][t'] = component c of X[t' + d][t'] (zero outside the matrix).
 // The exchange sum  H[t][t+d] = sum_t' V(|t - t'|) X[t' + d][t']  is then T S.
-__global__ void k_shear_planes(int nk, int nw, const double2* X, const int* e, __half* dst,
-                               int mat) {
-  const int b = blockIdx.z;
-  const int tp = blockIdx.x * blockDim.x + threadIdx.x;
-  const int row = blockIdx.y;   // 0 .. 4nk-1
-  if (tp >= nk) return;
-  const int dd = row >> 1, c = row & 1;
-  const int d = dd - (nk - 1);
-  float v = 0.f;
-  if (dd < 2 * nk - 1 && tp + d >= 0 && tp + d < nk) {
-    const double* x = reinterpret_cast<const double*>(
-        X + (long long)b * nk * nk + (long long)(tp + d) * nk + tp);
-    v = (float)(x[c] * ldexp(1.0, e[b]));
+// A block writes dd in [dd0, dd0 + 32) x t' in [t0, t0 + 32); the source elements
+// lie in rows t0 + dd0 - (Nk - 1) ... + 62 of columns t0 ... t0 + 31, which are
+// read row by row (coalesced) into shared memory and then read along diagonals
+// (row stride 32 double2: diagonal reads are free of bank conflicts).
+// blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire.
+__global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* X1,
+                              const double2* X2, const int* e, __half* dst) {
+  __shared__ double2 tile[63][32];
+  const int n = blockIdx.z / nw, b = blockIdx.z % nw;
+  const double2* X = (n == 0 ? X0 : n == 1 ? X1 : X2) + (long long)b * nk * nk;
+  const int t0 = blockIdx.x * 32, dd0 = blockIdx.y * 32;
+  const int rbase = t0 + dd0 - (nk - 1);
+  const int tx = threadIdx.x;
+  for (int rr = threadIdx.y; rr < 63; rr += blockDim.y) {
+    const int r = rbase + rr, c = t0 + tx;
+    tile[rr][tx] = (r >= 0 && r < nk && c < nk) ? X[(long long)r * nk + c] : make_double2(0, 0);
   }
+  __syncthreads();
+  const int eb = e[b];
   const long long rows = 4ll * nk, plane = (long long)nw * rows * nk;
-  __half* base = dst + (long long)mat * 2 * plane + (long long)b * rows * nk + (long long)row * nk + tp;
-  const __half h = __float2half_rn(v);
-  base[0] = h;
-  base[plane] = __float2half_rn(v - __half2float(h));
+  __half* base = dst + (long long)n * 2 * plane + (long long)b * rows * nk;
+  const int tp = t0 + tx;
+  if (tp >= nk) return;
+  for (int ddl = threadIdx.y; ddl < 32; ddl += blockDim.y) {
+    const int dd = dd0 + ddl;
+    if (dd >= 2 * nk) break;
+    const double2 v = tile[tx + ddl][tx];
+    put_hilo(base + (long long)(2 * dd) * nk + tp, plane, f64_to_f32(v.x, eb));
+    put_hilo(base + (long long)(2 * dd + 1) * nk + tp, plane, f64_to_f32(v.y, eb));
+  }
+}
+
+// Diagonal traces tr_d(X) = sum_k X[k][k+d] of C and D (SBEs.py:1094-1103) in
+// FP32, layout per wire [2][2Nk] with entry d + Nk; and the stage field in FP32.
+__global__ void k_traces_f(const WireDev* wires, const double2* C, const double2* D, float2* trf) {
+  const WireDev W = wires[blockIdx.z];
+  const int nk = W.nk;
+  const int d = (int)blockIdx.x - (nk - 1);
+  if ((int)blockIdx.x >= 2 * nk - 1) return;
+  const double2* X = (blockIdx.y == 0 ? C : D) + W.off_mat;
+  const int k0 = d >= 0 ? 0 : -d, k1 = d >= 0 ? nk - 1 - d : nk - 1;
+  float sr = 0.f, si = 0.f;
+  for (int k = k0 + threadIdx.x; k <= k1; k += 32) {
+    const float2 v = f64_to_f32(X[(long long)k * nk + k + d]);
+    sr += v.x;
+    si += v.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (threadIdx.x == 0)
+    trf[(long long)blockIdx.z * 4 * nk + blockIdx.y * 2 * nk + d + nk] = make_float2(sr, si);
+}
+
+__global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) ekf[i] = f64_to_f32(ek[i]);
 }
 
 // H = Meh + diagonal energies + direct Coulomb terms + exchange sums
-// (SBEs.py:1044-1131).  The exchange sums come from the sheared FP32 GEMM output
-// xsh[n][b][k1][2 dd + c], dd = k2 - k1 + Nk - 1, which is read along rows
-// (coalesced in k2).  The diagonal of Hee / Hhh is split off into dgE / dgH
-// (the GEMM operands carry H' = H - diag); the max |component| of the
-// operands goes to mx[b].
-__global__ void k_h_build(const WireDev* wires, const double2* Ek, const double* vs,
-                          const double* Ee, const double* Eh, const double2* tr, const float* xsh,
-                          int have_x, double2* Heh, double2* Hee, double2* Hhh, double2* dgE,
-                          double2* dgH, unsigned* mx) {
+// (SBEs.py:1044-1131) in FP32: Heh, Hee' and Hhh' (diagonal removed) into hf.
+// The exchange sums come from the sheared FP32 GEMM output xsh[n][b][k1][2 dd + c],
+// dd = k2 - k1 + Nk - 1, read along rows (coalesced in k2).  The diagonal of
+// Hee / Hhh (gap + kinetic energy) is formed in FP64 into dgE / dgH and split into
+// FP32 hi / lo parts (dgf).  The block maximum of the operands goes to mx[b].
+__global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* vsf,
+                          const double* Ee, const double* Eh, const float2* trf, const float* xsh,
+                          int have_x, float2* hf, long long tot_mat, double2* dgE, double2* dgH,
+                          float2* dgf, unsigned* mx) {
   const WireDev& W = wires[blockIdx.z];
-  const int nk = W.nk;
+  const int nk = W.nk, b = blockIdx.z, nw = gridDim.z;
   const int k2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int k1 = blockIdx.y;
   float hmax = 0.f;
   if (k1 < nk && k2 < nk) {
-    // off-diagonal elements in FP32 (they only feed the FP16 hi/lo operands and
-    // the driving term of dP); the diagonal (gap + kinetic energy) in FP64
     float2 heh = make_float2(0.f, 0.f), hee = heh, hhh = heh;
     if (W.flags & SBE_F_OPTICS) {
       int q = k1 - k2;
       if (q < 0) q += W.nr;
-      const double2* ek = Ek + 3 * W.off_r;
-      double2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
+      const float2* ek = ekf + 3 * W.off_r;
+      const float2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
       const float ed = (float)(W.ehint * W.dcv);
       const float sx = (k2 & 1) ? ed : -ed;               // -ehint Xcv
       const float sy = -ed * (float)W.yw, sz = ed * (float)W.zsign;
-      heh.x = sx * (float)ex.x + sy * (float)ey.x + sz * (float)ez.x;
-      heh.y = sx * (float)ex.y + sy * (float)ey.y + sz * (float)ez.y;
+      heh.x = sx * ex.x + sy * ey.x + sz * ez.x;
+      heh.y = sx * ex.y + sy * ey.y + sz * ez.y;
     }
     const bool exc = (W.flags & SBE_F_EXCITONS) != 0, lf = (W.flags & SBE_F_LF) != 0;
     const int d = k1 - k2;
     if (exc && lf && d != 0) {
-      const double* v = vs + 3 * W.off_vec;
-      const double2* t = tr + 4 * W.off_vec;
+      const float* v = vsf + (long long)b * 3 * nk;
+      const float2* t = trf + (long long)b * 4 * nk;
       const int ad = d < 0 ? -d : d;
-      const float v0 = (float)v[ad], v1 = (float)v[nk + ad], v2 = (float)v[2 * nk + ad];
-      double2 trC = t[d + nk], trCm = t[-d + nk], trD = t[2 * nk + d + nk],
-              trDm = t[2 * nk - d + nk];
-      hee.x = v1 * (float)trC.x - v0 * (float)trDm.x;
-      hee.y = v1 * (float)trC.y - v0 * (float)trDm.y;
-      hhh.x = v2 * (float)trD.x - v0 * (float)trCm.x;
-      hhh.y = v2 * (float)trD.y - v0 * (float)trCm.y;
+      const float v0 = v[ad], v1 = v[nk + ad], v2 = v[2 * nk + ad];
+      const float2 trC = t[d + nk], trCm = t[-d + nk], trD = t[2 * nk + d + nk],
+                   trDm = t[2 * nk - d + nk];
+      hee.x = v1 * trC.x - v0 * trDm.x;
+      hee.y = v1 * trC.y - v0 * trDm.y;
+      hhh.x = v2 * trD.x - v0 * trCm.x;
+      hhh.y = v2 * trD.y - v0 * trCm.y;
     }
     float2 xc = make_float2(0.f, 0.f), xd = xc;
     if (have_x) {
       const long long ms = (long long)nk * 4 * nk;
-      const long long rowo = ((long long)blockIdx.z * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
-      const long long plane = (long long)gridDim.z * ms;
-      float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
+      const long long rowo = ((long long)b * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
+      const long long plane = (long long)nw * ms;
+      const float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
       heh.x += xe.x;
       heh.y += xe.y;
       if (lf || d == 0) {
@@ -332,11 +478,19 @@ __global__ void k_h_build(const WireDev* wires, const double2* Ek, const double*
       }
     }
     const long long o = W.off_mat + (long long)k1 * nk + k2;
-    Heh[o] = make_double2(heh.x, heh.y);
+    hf[o] = heh;
     if (d == 0) {
-      const long long vo = (long long)blockIdx.z * nk + k1;
-      dgE[vo] = make_double2(Ee[W.off_vec + k1] + W.gap - (double)xc.x, -(double)xc.y);
-      dgH[vo] = make_double2(Eh[W.off_vec + k1] - (double)xd.x, -(double)xd.y);
+      // FP64 only on the diagonal (one element per row)
+      const long long vo = (long long)b * nk + k1;
+      const double2 ge = make_double2(Ee[W.off_vec + k1] + W.gap - (double)xc.x, -(double)xc.y);
+      const double2 gh = make_double2(Eh[W.off_vec + k1] - (double)xd.x, -(double)xd.y);
+      dgE[vo] = ge;
+      dgH[vo] = gh;
+      const float2 geh = make_float2((float)ge.x, (float)ge.y), ghh = make_float2((float)gh.x, (float)gh.y);
+      dgf[vo] = geh;
+      dgf[(long long)nw * nk + vo] = make_float2((float)(ge.x - (double)geh.x), (float)(ge.y - (double)geh.y));
+      dgf[2ll * nw * nk + vo] = ghh;
+      dgf[3ll * nw * nk + vo] = make_float2((float)(gh.x - (double)ghh.x), (float)(gh.y - (double)ghh.y));
       hee = make_float2(0.f, 0.f);
       hhh = hee;
     } else {
@@ -345,68 +499,132 @@ __global__ void k_h_build(const WireDev* wires, const double2* Ek, const double*
       hhh.x -= xd.x;
       hhh.y -= xd.y;
     }
-    Hee[o] = make_double2(hee.x, hee.y);
-    Hhh[o] = make_double2(hhh.x, hhh.y);
+    hf[tot_mat + o] = hee;
+    hf[2 * tot_mat + o] = hhh;
     hmax = fmaxf(fmaxf(fmaxf(fabsf(heh.x), fabsf(heh.y)), fmaxf(fabsf(hee.x), fabsf(hee.y))),
                  fmaxf(fabsf(hhh.x), fabsf(hhh.y)));
   }
+  __shared__ float red[4];
   for (int o = 16; o > 0; o >>= 1) hmax = fmaxf(hmax, __shfl_down_sync(0xffffffffu, hmax, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(hmax));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = hmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) hmax = fmaxf(hmax, red[w]);
+    atomicMax(mx + b, __float_as_uint(hmax));
+  }
 }
 
-// planes with an added i * f * M (M real-valued complex array), used for
-// Hee' + i hbar B and Hhh' + i hbar A.
-__global__ void k_planes_add(const double2* X, const double2* Madd, double f, int nk,
-                             const int* e, __half* dst, int mat, int nw) {
+// Planes of Hee', Hhh' (slots M_EE, M_HH) and of Hee' + i hbar B, Hhh' + i hbar A
+// (slots M_EEX, M_HHX) from the FP32 values.
+__global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA, const float* hB,
+                          int nk, const int* e, __half* dst, int nw) {
   const int b = blockIdx.z;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  int r = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
   if (c >= nk || r >= nk) return;
   const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
-  long long o = (long long)r * nk + c;
-  double2 v = X[(long long)b * mm + o];
-  double2 a = Madd[(long long)b * mm + o];
-  const double sc = ldexp(1.0, e[b]);
-  const float vr = (float)((v.x - f * a.y) * sc), vi = (float)((v.y + f * a.x) * sc);
-  __half* base = dst + (long long)mat * 4 * plane + (long long)b * mm + o;
-  const __half rh = __float2half_rn(vr), ih = __float2half_rn(vi);
-  base[0] = rh;
-  base[plane] = __float2half_rn(vr - __half2float(rh));
-  base[2 * plane] = ih;
-  base[3 * plane] = __float2half_rn(vi - __half2float(ih));
+  const long long o = (long long)b * mm + (long long)r * nk + c;
+  const int eb = e[b];
+  const float2 a = hee[o], h = hhh[o];
+  const float bb = hB[o], aa = hA[o];
+  const float v[4][2] = {{a.x, a.y}, {h.x, h.y}, {a.x, a.y + bb}, {h.x, h.y + aa}};
+  const int slot[4] = {M_EE, M_HH, M_EEX, M_HHX};
+  for (int i = 0; i < 4; ++i) {
+    __half* base = dst + (long long)slot[i] * 4 * plane + o;
+    put_hilo(base, plane, f32_ldexp(v[i][0], eb));
+    put_hilo(base + 2 * plane, plane, f32_ldexp(v[i][1], eb));
+  }
 }
 
 // dC (dD) from W = C Hee'^T + P^H Heh^T (V = D Hhh'^T + conj(P) Heh): for
 // Hermitian C, Hee (D, Hhh) the four terms of dCdt (dDdt) are W - W^H, so
 //   dX[i][j] = (W[i][j] - conj(W[j][i]) + (g[j] - g[i]) X[i][j]) / (i hbar)
 // with g the peeled diagonal.  The result is exactly anti-Hermitian, which
-// keeps C and D Hermitian.  Tiles (bi, bj) and (bj, bi) meet in shared memory.
-__global__ void k_antiherm(int nk, const double2* W, long long wb, const double2* X,
-                           const double2* g, double2* out) {
-  __shared__ double2 t[32][33];
+// keeps C and D Hermitian.  A block owns the tile pair (bi, bj), (bj, bi) with
+// bi <= bj and reads each W element once.  W holds FP32 accumulator values; the
+// diagonal difference g[j] - g[i] comes from the hi / lo FP32 parts of g (the hi
+// parts of two close energies differ exactly).
+__global__ void k_antiherm(int nk, const float2* W, const double2* X, const float2* ghi,
+                           const float2* glo, float2* out) {
+  __shared__ float2 ta[32][33], tb[32][33];
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bi > bj) return;
   const int b = blockIdx.z;
-  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
-  const double2* w = W + (long long)b * wb;
+  const int i0 = bi * 32, j0 = bj * 32;
   const long long mb = (long long)b * nk * nk;
-  // t[jj][ii] = W[j0 + jj][i0 + ii]   (the transposed tile)
-  for (int jj = threadIdx.y; jj < 32; jj += blockDim.y) {
-    int r = j0 + jj, cc = i0 + threadIdx.x;
-    t[jj][threadIdx.x] = (r < nk && cc < nk) ? w[(long long)r * nk + cc] : make_double2(0, 0);
+  const float2* w = W + mb;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int ia = i0 + r, ja = j0 + threadIdx.x;
+    ta[r][threadIdx.x] = (ia < nk && ja < nk) ? w[(long long)ia * nk + ja] : make_float2(0, 0);
+    const int ib = j0 + r, jb = i0 + threadIdx.x;
+    tb[r][threadIdx.x] = (ib < nk && jb < nk) ? w[(long long)ib * nk + jb] : make_float2(0, 0);
   }
   __syncthreads();
-  const double ih = 1.0 / kHbar;
-  for (int ii = threadIdx.y; ii < 32; ii += blockDim.y) {
-    int i = i0 + ii, j = j0 + threadIdx.x;
-    if (i >= nk || j >= nk) continue;
-    double2 a = w[(long long)i * nk + j];
-    double2 bT = t[threadIdx.x][ii];                 // W[j][i]
-    double2 x = X[mb + (long long)i * nk + j];
-    double2 gi = g[(long long)b * nk + i], gj = g[(long long)b * nk + j];
-    double2 de = make_double2(gj.x - gi.x, gj.y - gi.y);
-    double2 dx = make_double2(de.x * x.x - de.y * x.y, de.x * x.y + de.y * x.x);
-    double re = a.x - bT.x + dx.x, im = a.y + bT.y + dx.y;
-    out[mb + (long long)i * nk + j] = make_double2(im * ih, -re * ih);
+  const float ih = (float)(1.0 / kHbar);
+  const float2* gh = ghi + (long long)b * nk;
+  const float2* gl = glo + (long long)b * nk;
+  for (int pass = 0; pass < (bi == bj ? 1 : 2); ++pass) {
+    const int ri0 = pass ? j0 : i0, cj0 = pass ? i0 : j0;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+      const int i = ri0 + r, j = cj0 + threadIdx.x;
+      if (i >= nk || j >= nk) continue;
+      const float2 a = pass ? tb[r][threadIdx.x] : ta[r][threadIdx.x];      // W[i][j]
+      const float2 bt = pass ? ta[threadIdx.x][r] : tb[threadIdx.x][r];     // W[j][i]
+      const float2 x = f64_to_f32(X[mb + (long long)i * nk + j]);
+      const float dr = (gh[j].x - gh[i].x) + (gl[j].x - gl[i].x);
+      const float di = (gh[j].y - gh[i].y) + (gl[j].y - gl[i].y);
+      const float re = (a.x - bt.x) + (dr * x.x - di * x.y);
+      const float im = (a.y + bt.y) + (dr * x.y + di * x.x);
+      out[mb + (long long)i * nk + j] = make_float2(im * ih, -re * ih);
+    }
   }
+}
+
+// RK4 stage update of the mixed path: the stage derivative k and the sums
+// k1 + 2 k2 + 2 k3 are FP32 (they carry the RHS's FP32-accumulated precision);
+// the state is FP64 and only the additions to it are FP64.  Stages 1-3 also
+// measure the next stage state's maximum per wire into mx[b].
+// grid (blocks per wire, wires).
+__global__ void k_rk4_mixed(long long per, int stage, float dt, double2* X, float2* acc,
+                            double2* xs, const float2* k, unsigned* mx) {
+  const int b = blockIdx.y;
+  const long long o = (long long)b * per;
+  unsigned long long m = 0;
+  const float f = (stage == 1 || stage == 2) ? 0.5f * dt : dt;
+  for (long long i = o + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < o + per;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 kv = k[i];
+    const double2 x = X[i];
+    if (stage < 4) {
+      if (stage == 1) {
+        acc[i] = kv;
+      } else {
+        const float2 a = acc[i];
+        acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
+      }
+      const double2 v = make_double2(x.x + f32_to_f64(f * kv.x), x.y + f32_to_f64(f * kv.y));
+      xs[i] = v;
+      m = max(m, max(absbits(v.x), absbits(v.y)));
+    } else {
+      const float2 a = acc[i];
+      const float s = dt / 6.f;
+      X[i] = make_double2(x.x + f32_to_f64(s * (a.x + kv.x)), x.y + f32_to_f64(s * (a.y + kv.y)));
+    }
+  }
+  if (stage < 4) {
+    __shared__ unsigned long long red[8];
+    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, red[w]);
+      atomicMax(mx + b, bits_to_fmax(m));
+    }
+  }
+}
+
+__global__ void k_f32_to_f64(long long n, const float2* a, double2* out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = f32_to_f64(a[i]);
 }
 
 __global__ void k_add_int(int n, const int* a, const int* b, int* out) {
@@ -429,63 +647,68 @@ static int gemm(Mixed* m, const CUtensorMap& A, const CUtensorMap& B, int M, int
   return tc_gemm_launch(d, A, B, e, s);
 }
 
-static void exponents_from_mx(Mixed* m, int* e, cudaStream_t s) {
-  k_exponents<<<(m->nw + 127) / 128, 128, 0, s>>>(m->nw, m->mx, e, nullptr, nullptr);
+static void exponents_from(Mixed* m, const unsigned* mx, int* e, cudaStream_t s) {
+  k_exponents<<<(m->nw + 127) / 128, 128, 0, s>>>(m->nw, mx, e, nullptr, nullptr);
 }
 
 // Per-step set-up of the mixed path: the frozen preparation (screening, rates,
-// dephasing matrices with the FP32 Lorentzian sums) and the Toeplitz planes.
+// dephasing matrices with the FP32 Lorentzian sums) and its FP32 tables.
 static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
+  const int nk = m->nk, nw = m->nw;
   launch_prep_scalar(c, C, D, s);
   launch_gamma(c, -1, s);
+  cudaMemsetAsync(m->mxAB(), 0, sizeof(unsigned) * nw, s);
   if (c->any_offdiag) {
-    {
-      ProfScope ps(c, 3, s);
-      launch_offdiag_D(c, -1, nullptr, true, s);
-    }
-    launch_offdiag_AB(c, -1, s);
-  } else {
-    cudaMemsetAsync(c->dA, 0, sizeof(double2) * c->tot_mat, s);
-    cudaMemsetAsync(c->dB, 0, sizeof(double2) * c->tot_mat, s);
+    ProfScope ps(c, 3, s);
+    launch_offdiag_D(c, -1, nullptr, true, s);
   }
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * m->nw, s);
-  k_vs_max<<<m->nw, 256, 0, s>>>(c->d_wires, c->vs, m->mx);
-  exponents_from_mx(m, m->eT(), s);
-  k_toeplitz_planes<<<dim3((m->nk + 127) / 128, m->nk, 3 * m->nw), 128, 0, s>>>(
-      c->d_wires, c->vs, m->eT(), m->tpl, m->nw);
+  k_hab<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, c->De, c->Dh, m->habf,
+                                                       c->tot_mat, m->mxAB());
+  k_gam_f<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->gamE, c->gamH, m->gamf, nw);
+  cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
+  k_vs_max<<<nw, 256, 0, s>>>(c->d_wires, c->vs, m->mxH());
+  exponents_from(m, m->mxH(), m->eT(), s);
+  k_toeplitz_planes<<<dim3((nk + 127) / 128, nk, 3 * nw), 128, 0, s>>>(c->d_wires, c->vs, m->eT(),
+                                                                       m->tpl, nw, m->vsf);
   return cuda_check(cudaGetLastError(), "mixed prep");
 }
 
-// One stage RHS of every wire at state (P, C, D) and wire-k field Ek.
+// One stage RHS of every wire at state (P, C, D) and wire-k field Ek (FP64);
+// the derivatives go to m->kf (FP32).  When state_max_ready is set, mxS already
+// holds the per-wire maximum of the state (written by the previous stage's
+// update); otherwise it is measured here.
 static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const double2* D,
-                       const double2* Ek, double2* dP, double2* dC, double2* dD,
-                       cudaStream_t s) {
+                       const double2* Ek, int state_max_ready, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
-  const long long mm = (long long)nk * nk;
+  const long long mm = (long long)nk * nk, tm = c->tot_mat;
   const WireDev& W0 = c->wires[0];
-  // state exponent and planes
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
-  absmax_into(P, mm, nw, 1.0, m->mx, s);
-  absmax_into(C, mm, nw, 1.0, m->mx, s);
-  absmax_into(D, mm, nw, 1.0, m->mx, s);
-  exponents_from_mx(m, m->eS(), s);
-  const double2* st[3] = {P, C, D};
-  for (int i = 0; i < 3; ++i) {
-    launch_planes(st[i], mm, nk, nw, 0, m->eS(), m->planes, 2 * i, 4, 0, s);
-    launch_planes(st[i], mm, nk, nw, 1, m->eS(), m->planes, 2 * i + 1, 4, 0, s);
+  // state exponent and planes: P and P^T from one read; C and D need only their
+  // own layout (C^T = conj C and D^T = conj D for the Hermitian C and D)
+  if (!state_max_ready) {
+    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+    absmax_into(P, mm, nw, m->mxS(), s);
+    absmax_into(C, mm, nw, m->mxS(), s);
+    absmax_into(D, mm, nw, m->mxS(), s);
   }
-  // exchange sums (sheared GEMMs, FP32 output), then the Hamiltonians: Meh +
-  // diagonal + direct + exchange, diagonal peeled, maximum for the H exponent
-  launch_traces(c, C, D, s);
+  exponents_from(m, m->mxS(), m->eS(), s);
+  const double2* st[3] = {P, C, D};
+  const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eS(), m->planes, M_P, M_PT, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eS(), m->planes, M_C, -1, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eS(), m->planes, M_D, -1, nw);
+  // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
+  // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
+  k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
+  k_traces_f<<<dim3(2 * nk - 1, 2, nw), 32, 0, s>>>(c->d_wires, C, D, m->trf);
   int rc = SBE_OK;
   const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
   if (have_x) {
     k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
+    k_shear_tiles<<<dim3((nk + 31) / 32, (2 * nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
+        nk, nw, P, C, D, m->eS(), m->spl);
     for (int n = 0; n < 3; ++n) {
-      k_shear_planes<<<dim3((nk + 127) / 128, 4 * nk, nw), 128, 0, s>>>(nk, nw, st[n], m->eS(),
-                                                                        m->spl, n);
       tc::Term t{n, n, 0, 0, 1};
       tc::EpiArgs e{};
       e.kind = tc::EPI_F32;
@@ -498,56 +721,48 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
       if (rc) return rc;
     }
   }
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
-  k_h_build<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, Ek, c->vs, c->Ee, c->Eh,
-                                                           c->tr, m->xsh, have_x, c->Heh, c->Hee,
-                                                           c->Hhh, m->dgE, m->dgH, m->mx);
-  if (c->any_offdiag) {
-    absmax_into(c->dA, mm, nw, 2.0 * kHbar, m->mx, s);
-    absmax_into(c->dB, mm, nw, 2.0 * kHbar, m->mx, s);
-  }
-  exponents_from_mx(m, m->eH(), s);
-  const double2* hs[3] = {c->Heh, c->Hee, c->Hhh};
-  for (int i = 0; i < 3; ++i) {
-    launch_planes(hs[i], mm, nk, nw, 0, m->eH(), m->planes, M_EH + 2 * i, 4, 0, s);
-    if (i == 0)   // Hee'^T and Hhh'^T are not needed in the W - W^H form
-      launch_planes(hs[i], mm, nk, nw, 1, m->eH(), m->planes, M_EH + 2 * i + 1, 4, 0, s);
-  }
-  dim3 pg((nk + 127) / 128, nk, nw);
-  k_planes_add<<<pg, 128, 0, s>>>(c->Hee, c->dB, kHbar, nk, m->eH(), m->planes, M_EEX, nw);
-  k_planes_add<<<pg, 128, 0, s>>>(c->Hhh, c->dA, kHbar, nk, m->eH(), m->planes, M_HHX, nw);
+  cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
+  k_h_build<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
+      c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, m->xsh, have_x, m->hf, tm, m->dgE, m->dgH,
+      m->dgf, m->mxH());
+  // H exponent: max over the operands and the step's 2 hbar |A|, |B|
+  k_exponents2<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH());
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->planes, M_EH, M_EHT, nw);
+  k_hplanes<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
+      m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->planes, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eH(), m->esc());
   // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
   // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
-  const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_DT, M_EH, 0, 0, -1},
-                          {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_CT, 0, 0, -1}};
+  const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_D, M_EH, 1, 0, -1},
+                          {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_C, 0, 1, -1}};
   const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
   const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
   const tc::Term* tl[3] = {tP, tC, tD};
   const int nt[3] = {4, 2, 2};
-  double2* Wbuf[3] = {dP, c->G, c->G + c->tot_kr};
+  float2* wf = reinterpret_cast<float2*>(c->G);
+  float2* out[3] = {m->kf, wf, wf + tm};
   for (int w = 0; w < 3; ++w) {
     tc::EpiArgs e{};
-    e.kind = (w == 0) ? tc::EPI_RHS : tc::EPI_RAW;
+    e.kind = (w == 0) ? tc::EPI_RHSF : tc::EPI_RAWF;
     e.which = w;
-    e.out = Wbuf[w];
+    e.outf2 = out[w];
     e.out_bstride = mm;
     e.escale = m->esc();
     e.X = st[w];
-    e.Heh = c->Heh;
-    e.dgE = m->dgE;
-    e.dgH = m->dgH;
-    e.gamE = c->gamE;
-    e.gamH = c->gamH;
+    e.hehf = m->hf;
+    e.dgf = m->dgf;
+    e.gamf = m->gamf;
     e.nk = nk;
+    e.nw = nw;
     e.err = m->err();
     ProfScope ps(c, 0, s);
     rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, nt[w], tl[w], 0, e, s);
     if (rc) return rc;
   }
-  dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, c->G, mm, C, m->dgE, dC);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, c->G + c->tot_kr, mm, D, m->dgH, dD);
+  const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
+  const long long vn = (long long)nw * nk;
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, C, m->dgf, m->dgf + vn, m->kf + tm);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + tm, D, m->dgf + 2 * vn, m->dgf + 3 * vn, m->kf + 2 * tm);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 
@@ -557,13 +772,15 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   const long long mm = (long long)nk * nk;
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * nw, s);
-  absmax_into(P, mm, nw, 1.0, m->mx, s);
-  absmax_into(C, mm, nw, 1.0, m->mx, s);
-  absmax_into(D, mm, nw, 1.0, m->mx, s);
-  exponents_from_mx(m, m->eS(), s);
+  cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+  absmax_into(P, mm, nw, m->mxS(), s);
+  absmax_into(C, mm, nw, m->mxS(), s);
+  absmax_into(D, mm, nw, m->mxS(), s);
+  exponents_from(m, m->mxS(), m->eS(), s);
   const double2* st[3] = {P, C, D};
-  for (int i = 0; i < 3; ++i) launch_planes(st[i], mm, nk, nw, 0, m->eS(), m->planes, 2 * i, 4, 0, s);
+  const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
+  for (int i = 0; i < 3; ++i)
+    k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->planes, 2 * i, -1, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
   for (int i = 0; i < 3; ++i) {
     tc::Term t{2 * i, 0, i == 2 ? 1 : 0, 0, 1};
@@ -595,7 +812,15 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
   if (rc) return rc;
   rc = mixed_prep(c, C, D, s);
   if (rc) return rc;
-  return mixed_stage(c, P, C, D, Ek, dP, dC, dD, s);
+  rc = mixed_stage(c, P, C, D, Ek, 0, s);
+  if (rc) return rc;
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  const long long n = c->tot_mat;
+  const int g = (int)((n + 255) / 256);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf, dP);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf + n, dC);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf + 2 * n, dD);
+  return cuda_check(cudaGetLastError(), "rhs_mixed");
 }
 
 int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
@@ -604,7 +829,10 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   if (rc) return rc;
   rc = mixed_prep(c, C, D, s);
   if (rc) return rc;
+  Mixed* m = static_cast<Mixed*>(c->mixed);
   const long long n = c->tot_mat;
+  const long long per = (long long)m->nk * m->nk;
+  const int bpw = (int)std::min<long long>((per + 255) / 256, 64);
   const double frac[4] = {0.0, 0.5, 0.5, 1.0};
   for (int st = 1; st <= 4; ++st) {
     const double2 *xp = P, *xc = C, *xd = D;
@@ -614,9 +842,14 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
       xd = c->xs + 2 * n;
     }
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
-    rc = mixed_stage(c, xp, xc, xd, c->ekst, c->dP, c->dC, c->dD, s);
+    rc = mixed_stage(c, xp, xc, xd, c->ekst, st > 1, s);
     if (rc) return rc;
-    launch_rk4_axpy(c, st, dt, P, C, D, s);
+    // RK4 update; stages 1-3 also measure the next stage state's maximum
+    if (st < 4) cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
+    double2* X[3] = {P, C, D};
+    for (int i = 0; i < 3; ++i)
+      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(per, st, (float)dt, X[i], m->accf + i * n,
+                                                  c->xs + i * n, m->kf + i * n, m->mxS());
   }
   launch_relax_norm(c, C, D, dt, false, s);
   return mixed_sources(c, P, C, D, src, s);
@@ -625,6 +858,48 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
 }  // namespace sbe
 
 using namespace sbe;
+
+__global__ void k_convert_selftest(const double* din, const float* fin, long long n, float* fout,
+                                   double* dout) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fout[i] = f64_to_f32(din[i]);
+  dout[i] = f32_to_f64(fin[i]);
+}
+
+// Diagnostic entry (no counterpart in the reference): the integer-pipe
+// conversions of the mixed path, f_out = fp32(d_in) and d_out = fp64(f_in).
+extern "C" int sbe_convert_selftest(const double* d_in, const float* f_in, long long n,
+                                    float* f_out, double* d_out, void* stream) {
+  if (!d_in || !f_in || !f_out || !d_out || n < 0)
+    return fail(SBE_ERR_ARG, "sbe_convert_selftest: bad arguments");
+  if (n == 0) return SBE_OK;
+  k_convert_selftest<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(d_in, f_in, n,
+                                                                               f_out, d_out);
+  return cuda_check(cudaGetLastError(), "sbe_convert_selftest");
+}
+
+// Device-side error flags of the engine (bounded waits that gave up), read and
+// cleared after the stream has drained.
+extern "C" int sbe_ctx_check(SbeCtx* c, void* stream) {
+  if (!c) return fail(SBE_ERR_ARG, "sbe_ctx_check: null context");
+  int rc = cuda_check(cudaStreamSynchronize(as_stream(stream)), "sbe_ctx_check");
+  if (rc) return rc;
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  if (!m) return SBE_OK;
+  std::vector<int> h(m->nw);
+  rc = cuda_check(cudaMemcpy(h.data(), m->err(), sizeof(int) * m->nw, cudaMemcpyDeviceToHost),
+                  "sbe_ctx_check: read flags");
+  if (rc) return rc;
+  int any = 0;
+  for (int v : h) any |= v;
+  if (any) {
+    cudaMemset(m->err(), 0, sizeof(int) * m->nw);
+    return fail(SBE_ERR_TIMEOUT, "a tensor-core pipeline wait timed out (results of the "
+                                 "affected calls are invalid)");
+  }
+  return SBE_OK;
+}
 
 extern "C" int sbe_tc_selftest(int nk, int nbatch, const double* A, const double* B, int opA,
                                int opB, int complex_mode, double* out, void* stream) {

@@ -2,6 +2,7 @@
 #include <cudaTypedefs.h>
 
 #include "sbe_ctx.cuh"
+#include "fp_bits.cuh"
 #include "tc_gemm.cuh"
 
 namespace sbe {
@@ -158,11 +159,53 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
     return;
   }
   if (e.kind == EPI_RAW) {
+    // exact widening and power-of-two scaling on the integer pipe
     double2* o = e.out + (long long)b * e.out_bstride + (long long)m * d.N;
+    const int es = -e.escale[b];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       int n = n0 + j;
-      if (n < d.N) o[n] = make_double2(re[j] * sc, d.complex_mode ? im[j] * sc : 0.0);
+      if (n < d.N)
+        o[n] = make_double2(f32_to_f64_scaled(re[j], es),
+                            d.complex_mode ? f32_to_f64_scaled(im[j], es) : 0.0);
+    }
+    return;
+  }
+  if (e.kind == EPI_RAWF) {
+    float2* o = e.outf2 + (long long)b * e.out_bstride + (long long)m * d.N;
+    const int es = -e.escale[b];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      int n = n0 + j;
+      if (n < d.N) o[n] = make_float2(f32_ldexp(re[j], es), f32_ldexp(im[j], es));
+    }
+    return;
+  }
+  if (e.kind == EPI_RHSF) {
+    // dP[kh=m][ke=n] = (G + (hh[kh] + ee[ke]) P + Heh[ke][kh])/(i hbar) - (gE+gH) P in
+    // FP32 (the peeled diagonal energies add, so no cancellation), from the FP64
+    // stage state P converted on the integer pipe.
+    const int nk = e.nk, nw = e.nw;
+    const long long mb = (long long)b * nk * nk, vb = (long long)b * nk, vn = (long long)nw * nk;
+    const float ih = (float)(1.0 / 1.0545718176461565e-34);
+    const int es = -e.escale[b];
+    const double2* X = e.X + mb + (long long)m * nk;
+    const float2 gh = e.dgf[2 * vn + vb + m], gl = e.dgf[3 * vn + vb + m];
+    const float gamH = e.gamf[vn + vb + m];
+    float2* o = e.outf2 + mb + (long long)m * nk;
+#pragma unroll 4
+    for (int j = 0; j < 16; ++j) {
+      const int n = n0 + j;
+      if (n >= nk) break;
+      const float gr = f32_ldexp(re[j], es), gi = f32_ldexp(im[j], es);
+      const float2 x = f64_to_f32(X[n]);
+      const float2 h = e.hehf[mb + (long long)n * nk + m];
+      const float2 eh = e.dgf[vb + n], el = e.dgf[vn + vb + n];
+      const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
+      const float ar = gr + (der * x.x - dei * x.y) + h.x;
+      const float ai = gi + (der * x.y + dei * x.x) + h.y;
+      const float gam = e.gamf[vb + n] + gamH;
+      o[n] = make_float2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
     }
     return;
   }

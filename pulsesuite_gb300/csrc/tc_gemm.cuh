@@ -42,6 +42,8 @@ enum Epi : int {
   EPI_RHS = 1,      // stage RHS of P, C or D (see sbe_tc.cu)
   EPI_EXCH = 2,     // exchange Hamiltonian assembly (see sbe_tc.cu)
   EPI_F32 = 3,      // outf[b][m][n] = acc * 2^-escale[b] as FP32 (real mode)
+  EPI_RHSF = 4,     // stage RHS of P in FP32 (see sbe_tc.cu)
+  EPI_RAWF = 5,     // outf2[b][m][n] = (re, im) * 2^-escale[b] as FP32 complex
 };
 
 struct EpiArgs {
@@ -70,6 +72,12 @@ struct EpiArgs {
   const int* yw;              // per batch yw(w)
   const int* zsign;           // per batch (-1)^w
   int* err;                   // error flag (bounded waits)
+  // FP32 outputs and inputs of EPI_RHSF / EPI_RAWF
+  float2* outf2;
+  const float2* hehf;         // Heh in FP32 [ke][kh] per batch
+  const float2* dgf;          // peeled diagonals: [4][nw][nk] Hee hi, Hee lo, Hhh hi, Hhh lo
+  const float* gamf;          // [2][nw][nk] GamE, GamH
+  int nw;
 };
 
 struct GemmDesc {

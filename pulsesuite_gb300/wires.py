@@ -256,6 +256,10 @@ class WireContext:
         """Capture one rk4_step on these buffers into a CUDA graph (RK4Graph)."""
         return RK4Graph(self, P, C, D, Ek0, dEk, dt, src_out, precision)
 
+    def check(self):
+        """Wait for the current stream and raise if a device-side bounded wait gave up."""
+        _lib.check(self.lib.sbe_ctx_check(self.handle, _lib.stream_handle()), "sbe_ctx_check")
+
     def profile(self, enable=True):
         _lib.check(self.lib.sbe_ctx_profile(self.handle, int(bool(enable))), "sbe_ctx_profile")
 

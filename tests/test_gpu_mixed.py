@@ -72,6 +72,7 @@ def test_mixed_rhs_vs_fp64(nk):
     Ek = fields(ctx, [1e7, 3e7, 5e6])
     r64 = ctx.rhs(P, C, D, Ek, _lib.PREC_FP64)
     rmx = ctx.rhs(P, C, D, Ek, _lib.PREC_MIXED)
+    ctx.check()
     for a, b, n in zip(rmx, r64, ("dP", "dC", "dD")):
         for w in range(nw):
             e = rel(ctx.mat(a, w), ctx.mat(b, w))
@@ -133,6 +134,7 @@ def test_mixed_rk4_pulse_vs_fp64(nk):
             dEk = fields(ctx, [e1 - e0, 0.5 * (e1 - e0)])
             ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
         states[prec] = (P, C, D, src)
+    ctx.check()
     P64, C64, D64, s64 = states[_lib.PREC_FP64]
     Pm, Cm, Dm, sm = states[_lib.PREC_MIXED]
     for w in range(nw):

@@ -80,3 +80,34 @@ def test_real_mode(nk):
     ref = A.real @ B.real
     assert _rel(out[0].real, ref[0]) < tol(nk)
     assert float(out.imag.abs().max()) == 0.0
+
+
+def test_integer_pipe_conversions_match_hardware():
+    """fp32(x) and fp64(f) of the mixed path's integer-pipe helpers vs the GPU's own
+    conversions, bit for bit (FP32 subnormal results are flushed to zero by design)."""
+    import numpy as np
+    from pulsesuite_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(0)
+    n = 1 << 16
+    mant = rng.uniform(1.0, 2.0, n)
+    expo = rng.integers(-140, 130, n)
+    d = mant * np.exp2(expo.astype(float)) * rng.choice([-1.0, 1.0], n)
+    # ties: FP32 values plus exactly half an FP32 ulp
+    f = rng.uniform(1, 2, 1024).astype(np.float32).astype(np.float64)
+    d[:1024] = f + np.exp2(np.floor(np.log2(f)) - 24)
+    d[1024:1030] = [0.0, -0.0, np.inf, -np.inf, 3.4028234663852886e38, 1.1754943508222875e-38]
+    fin = (rng.standard_normal(n) * np.exp2(rng.integers(-149, 127, n).astype(float))).astype(np.float32)
+    fin[:6] = [0.0, -0.0, np.inf, 1e-45, -3e-39, 3.4e38]
+    dd = torch.as_tensor(d).cuda()
+    ff = torch.as_tensor(fin).cuda()
+    fo = torch.empty(n, dtype=torch.float32, device="cuda")
+    do = torch.empty(n, dtype=torch.float64, device="cuda")
+    _lib.check(lib.sbe_convert_selftest(_lib.ptr(dd), _lib.ptr(ff), n, _lib.ptr(fo), _lib.ptr(do),
+                                        _lib.stream_handle()), "sbe_convert_selftest")
+    torch.cuda.synchronize()
+    hw_f = dd.float()
+    normal = (hw_f.abs() >= 1.1754943508222875e-38) | (hw_f == 0) | torch.isinf(hw_f)
+    assert torch.equal(fo[normal].view(torch.int32), hw_f[normal].view(torch.int32))
+    assert torch.all(fo[~normal] == 0)
+    assert torch.equal(do.view(torch.int64), ff.double().view(torch.int64))
