@@ -19,6 +19,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fp_bits.cuh"
 #include "pstd.cuh"
 
 namespace {
@@ -44,7 +45,9 @@ struct SbeCouple {
   double2 *g_y = nullptr, *g_c1 = nullptr, *g_c2 = nullptr, *g_coef = nullptr;
   double2 *w_c1 = nullptr, *w_c2 = nullptr, *w_coef = nullptr;
   double2* twr = nullptr;     // tot_r: exp(-2 pi i m / Nr) per wire
+  float2* twrf = nullptr;     // the same in FP32
   double2* wv = nullptr;      // 3 tot_r: sampled fields on the wire grids (real parts)
+  float* wvf = nullptr;       // the same in FP32
   double2 *Ek = nullptr, *dEk = nullptr, *src = nullptr;  // 3, 3, 5 x tot_r
   double2 *Pg = nullptr, *Pold = nullptr, *rho = nullptr, *J = nullptr;  // 3, 3, 1, 2 x nx
   long long* step = nullptr;  // device step counter
@@ -241,7 +244,7 @@ __device__ __forceinline__ double2 spl_eval(const double2* y, const double2* b, 
 // Grid fields -> wire grids: spline at x_w + r_j, window, real part.
 __global__ void k_couple_eval(const WireDev* wires, int nx, const double* xg, const double2* gy,
                               const double2* gcoef, const double* wx, const double* r,
-                              const double* window, double2* wv) {
+                              const double* window, double2* wv, float* wvf) {
   const int w = blockIdx.y;
   const WireDev W = wires[w];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,8 +258,52 @@ __global__ void k_couple_eval(const WireDev* wires, int nx, const double* xg, co
     for (int f = 0; f < 3; ++f)
       v[f] = spl_eval(gy + (long long)f * nx, gcoef + 3LL * f * nx, nx, i, dx).x;
   }
-  for (int f = 0; f < 3; ++f)
-    wv[3 * W.off_r + (long long)f * W.nr + j] = make_double2(v[f] * win, 0.0);
+  for (int f = 0; f < 3; ++f) {
+    const double a = v[f] * win;
+    wv[3 * W.off_r + (long long)f * W.nr + j] = make_double2(a, 0.0);
+    wvf[3 * W.off_r + (long long)f * W.nr + j] = f64_to_f32(a);
+  }
+}
+
+// FFTG as k_couple_fftg in FP32 with compensated (Kahan) sums, for the
+// mixed-precision step (its field operands are FP32 values).
+__global__ void __launch_bounds__(256) k_couple_fftg_f(const WireDev* wires, const float2* twr,
+                                                       const float* wv, double2* Ek) {
+  const int w = blockIdx.y;
+  const WireDev W = wires[w];
+  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= W.nr) return;
+  const int nr = W.nr;
+  const float2* tw = twr + W.off_r;
+  const float* v0 = wv + 3 * W.off_r;
+  float s[6] = {0, 0, 0, 0, 0, 0}, cmp[6] = {0, 0, 0, 0, 0, 0};
+  int m = (int)(((long long)q * lane) % nr);
+  const int step = (int)(((long long)q * 32) % nr);
+  for (int j = lane; j < nr; j += 32) {
+    const float2 t = tw[m];
+    for (int f = 0; f < 3; ++f) {
+      const float a = v0[(long long)f * nr + j];
+      const float terms[2] = {a * t.x, a * t.y};
+      for (int c = 0; c < 2; ++c) {
+        const int i = 2 * f + c;
+        const float y = terms[c] - cmp[i];
+        const float tt = s[i] + y;
+        cmp[i] = (tt - s[i]) - y;
+        s[i] = tt;
+      }
+    }
+    m += step;
+    if (m >= nr) m -= nr;
+  }
+  for (int i = 0; i < 6; ++i) {
+    s[i] -= cmp[i];
+    for (int o = 16; o > 0; o >>= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
+  }
+  if (lane == 0)
+    for (int f = 0; f < 3; ++f)
+      Ek[3 * W.off_r + (long long)f * nr + q] =
+          make_double2(-f32_to_f64(s[2 * f]) / nr, -f32_to_f64(s[2 * f + 1]) / nr);
 }
 
 // FFTG of the three sampled fields of every wire: Ek[q] = -(1/Nr) sum_j v_j e^{-2 pi i q j/Nr}.
@@ -356,7 +403,7 @@ __global__ void k_stage3(int nx, const double2* Ex, const double2* E, double2* g
   gy[2LL * nx + j] = E[nx + j];
 }
 
-__global__ void k_twr(const WireDev* wires, double2* twr) {
+__global__ void k_twr(const WireDev* wires, double2* twr, float2* twrf) {
   const int w = blockIdx.y;
   const WireDev W = wires[w];
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -364,6 +411,7 @@ __global__ void k_twr(const WireDev* wires, double2* twr) {
   double s, c;
   sincospi(-2.0 * (double)m / (double)W.nr, &s, &c);
   twr[W.off_r + m] = make_double2(c, s);
+  twrf[W.off_r + m] = make_float2(f64_to_f32(c), f64_to_f32(s));
 }
 
 void run_splines(const SplBatch& b, int nprob, int nmax, cudaStream_t s) {
@@ -406,15 +454,20 @@ SplBatch wire_batch(SbeCouple* cp) {
 
 }  // namespace
 
-int couple_sample(SbeCouple* cp, const double2* Ex, const double2* E, cudaStream_t s) {
+int couple_sample(SbeCouple* cp, const double2* Ex, const double2* E, int precision,
+                  cudaStream_t s) {
   SbeCtx* c = cp->ctx;
   const int nx = cp->p->nx;
   k_stage3<<<(nx + 255) / 256, 256, 0, s>>>(nx, Ex, E, cp->g_y);
   run_splines(grid_batch(cp), 3, nx, s);
   k_couple_eval<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(
-      c->d_wires, nx, cp->p->x, cp->g_y, cp->g_coef, cp->wx, c->r, c->window, cp->wv);
-  k_couple_fftg<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twr, cp->wv,
-                                                                 cp->Ek);
+      c->d_wires, nx, cp->p->x, cp->g_y, cp->g_coef, cp->wx, c->r, c->window, cp->wv, cp->wvf);
+  if (precision == SBE_PREC_MIXED)
+    k_couple_fftg_f<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
+                                                                     cp->wvf, cp->Ek);
+  else
+    k_couple_fftg<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twr, cp->wv,
+                                                                   cp->Ek);
   return cuda_check(cudaGetLastError(), "couple sample");
 }
 
@@ -477,7 +530,9 @@ int sbe_couple_create(SbeCtx* c, SbePstd* p, const double* wire_x, const SbeCoup
       {(void**)&cp->w_c2, sizeof(double2) * 5 * R},
       {(void**)&cp->w_coef, sizeof(double2) * 15 * R},
       {(void**)&cp->twr, sizeof(double2) * R},
+      {(void**)&cp->twrf, sizeof(float2) * R},
       {(void**)&cp->wv, sizeof(double2) * 3 * R},
+      {(void**)&cp->wvf, sizeof(float) * 3 * R},
       {(void**)&cp->Ek, sizeof(double2) * 3 * R},
       {(void**)&cp->dEk, sizeof(double2) * 3 * R},
       {(void**)&cp->src, sizeof(double2) * 5 * R},
@@ -525,7 +580,7 @@ int sbe_couple_create(SbeCtx* c, SbePstd* p, const double* wire_x, const SbeCoup
   k_spl_factors<<<1, 32, 0, s>>>(1, p->x, nullptr, nullptr, p->nx, cp->g_b, cp->g_t);
   k_spl_factors<<<(c->nw + 31) / 32, 32, 0, s>>>(c->nw, c->r, cp->wfn, cp->wfl, 0, cp->w_b,
                                                  cp->w_t);
-  k_twr<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, cp->twr);
+  k_twr<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, cp->twr, cp->twrf);
   int rc = cuda_check(cudaGetLastError(), "sbe_couple_create");
   if (rc == SBE_OK) rc = cuda_check(cudaStreamSynchronize(s), "sbe_couple_create: tables");
   if (rc) {
@@ -582,7 +637,7 @@ int sbe_couple_sample(SbeCouple* cp, const double* Ex, const double* E, void* st
   if (rc) return rc;
   if (!Ex || !E) return fail(SBE_ERR_ARG, "sbe_couple_sample: null field");
   return couple_sample(cp, reinterpret_cast<const double2*>(Ex),
-                       reinterpret_cast<const double2*>(E), as_stream(stream));
+                       reinterpret_cast<const double2*>(E), SBE_PREC_FP64, as_stream(stream));
 }
 
 int sbe_couple_deposit(SbeCouple* cp, void* stream) {
@@ -600,7 +655,8 @@ int sbe_couple_step(SbeCouple* cp, double* P, double* C, double* D, double* E, d
   SbePstd* p = cp->p;
   const int nx = p->nx;
   // 1. fields at t_n on the wires
-  if ((rc = couple_sample(cp, reinterpret_cast<double2*>(Ex), reinterpret_cast<double2*>(E), s)))
+  if ((rc = couple_sample(cp, reinterpret_cast<double2*>(Ex), reinterpret_cast<double2*>(E),
+                          precision, s)))
     return rc;
   // 2. H^{n+1/2}
   if ((rc = sbe_pstd_update_h(p, E, H, dt, stream))) return rc;

@@ -156,6 +156,9 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
               double2* dP, double2* dC, double2* dD, cudaStream_t s);
 void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
                            cudaStream_t s);
+void launch_sources_final(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
+                          cudaStream_t s);
+void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s);
 void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int transpose,
                    const int* e, __half* dst, int mat, int nplanes, int real_only,
                    cudaStream_t s);

@@ -149,6 +149,11 @@ void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_
   k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, dt, c->ne, c->nh);
 }
 
+// the relaxation/normalisation kernel alone (rates already in c->wrate)
+void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s) {
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, dt, c->ne, c->nh);
+}
+
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s) {
   k_phonon_rates<<<dim3(c->wires[w].nk, 1), 128, 0, s>>>(c->d_wires, w, c->ne, c->nh, c->vs,
                                                          c->eps, c->EP, c->HP, c->wrate);
@@ -597,6 +602,11 @@ int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* 
 }  // namespace sbe
 
 namespace sbe {
+void launch_sources_final(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
+                          cudaStream_t s) {
+  k_src_final<<<c->nw, 256, 0, s>>>(c->d_wires, -1, c->r, ne, nh, src);
+}
+
 void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
                            cudaStream_t s) {
   k_src_reduce<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, -1, c->expikr,

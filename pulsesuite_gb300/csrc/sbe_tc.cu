@@ -109,9 +109,12 @@ __device__ __forceinline__ float2 scaled2<float2>(float2 v, int e) {
   return make_float2(f32_ldexp(v.x, e), f32_ldexp(v.y, e));
 }
 
+// With tpart set (double input only), the block also writes the 63 diagonal sums
+// of its 32 x 32 tile to tpart[((b * 2 + which) * T + bi) * T + bj][l], local
+// diagonal l = c - r + 31, for the traces of C and D.
 template <typename T>
 __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int matN, int matT,
-                            int nbatch) {
+                            int nbatch, float2* tpart = nullptr, int which = 0) {
   __shared__ T tile[32][33];
   const int b = blockIdx.z;
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
@@ -139,6 +142,45 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int m
       put_hilo(base + 2 * plane, plane, v.y);
     }
   }
+  if (tpart) {
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid < 63) {
+      const int l = tid - 31;   // c - r
+      float sr = 0.f, si = 0.f;
+      for (int rr = 0; rr < 32; ++rr) {
+        const int cc = rr + l;
+        if (cc < 0 || cc >= 32) continue;
+        const float2 v = scaled2<T>(tile[rr][cc], 0);
+        sr += v.x;
+        si += v.y;
+      }
+      const int Tn = gridDim.x;
+      tpart[((((long long)b * 2 + which) * Tn + blockIdx.y) * Tn + blockIdx.x) * 63 + tid] =
+          make_float2(sr, si);
+    }
+  }
+}
+
+// Traces tr_d = sum over the 63-diagonal tile partials along diagonal d, fixed
+// order: trf[b][which][d + nk] (SBEs.py:1094-1103 direct terms).
+__global__ void k_trace_reduce(int nk, const float2* tpart, float2* trf) {
+  const int b = blockIdx.z, which = blockIdx.y;
+  const int dd = blockIdx.x * blockDim.x + threadIdx.x;   // d + nk - 1
+  if (dd >= 2 * nk - 1) return;
+  const int d = dd - (nk - 1);
+  const int Tn = (nk + 31) / 32;
+  const float2* part = tpart + ((long long)b * 2 + which) * Tn * Tn * 63;
+  float sr = 0.f, si = 0.f;
+  for (int o = -(Tn - 1); o < Tn; ++o) {
+    const int l = d - 32 * o + 31;
+    if (l < 0 || l >= 63) continue;
+    for (int bi = max(0, -o); bi < Tn && bi + o < Tn; ++bi) {
+      const float2 v = part[((long long)bi * Tn + bi + o) * 63 + l];
+      sr += v.x;
+      si += v.y;
+    }
+  }
+  trf[(long long)b * 4 * nk + which * 2 * nk + d + nk] = make_float2(sr, si);
 }
 
 void launch_exponents(const double2* X, long long per_batch, long long bstride, int nbatch,
@@ -178,6 +220,16 @@ struct Mixed {
   float* gamf = nullptr;   // 2 x nw x nk GamE, GamH
   float2* dgf = nullptr;   // 4 x nw x nk: hi and lo parts of the peeled Hee, Hhh diagonals
   double2 *dgE = nullptr, *dgH = nullptr;  // the peeled diagonals in FP64
+  // constant FP32 tables (built once): EP, EP^T, HP, HP^T scaled by 2^sP[w];
+  // Expikr; |xe|, |xh|
+  float *epf = nullptr, *eptf = nullptr, *hpf = nullptr, *hptf = nullptr;
+  float2* ekrf = nullptr;
+  float* xef = nullptr;     // 2 x nw x nk
+  int* sP = nullptr;        // nw phonon-table exponents
+  // per-step FP32 tables
+  float* phf = nullptr;     // 2 x nw x nk: Vep(d) 2^-sP, Vhp(d) 2^-sP
+  float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
+  float2* tpart = nullptr;  // nw x 2 x T x T x 63 partial diagonal sums (T = ceil(nk/32))
   CUtensorMap mapA, mapB, mapTA, mapSB, mapEB;
   int* eS() { return ints; }
   int* eH() { return ints + nw; }
@@ -206,6 +258,9 @@ void mixed_free(SbeCtx* c) {
   cudaFree(m->mx);
   cudaFree(m->kf);
   cudaFree(m->dgE);
+  cudaFree(m->epf);
+  cudaFree(m->ekrf);
+  cudaFree(m->tpart);
   delete m;
   c->mixed = nullptr;
 }
@@ -226,6 +281,70 @@ __global__ void k_eplanes(const WireDev* wires, const double2* expikr, __half* d
 __global__ void k_fill_int(int* p, int n, int v) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
+}
+
+// real absmax per wire of a packed Nk x Nk real table, as the FP64 bit pattern
+// (the phonon tables exceed the FP32 range)
+__global__ void k_absmax_r(const double* X, long long per, unsigned long long* out) {
+  const int b = blockIdx.y;
+  const double* x = X + (long long)b * per;
+  unsigned long long m = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per;
+       i += (long long)gridDim.x * blockDim.x)
+    m = max(m, absbits(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out + b, m);
+}
+
+// sP[b] = -(E + 1) for max |EP|, |HP| in [2^E, 2^(E+1)): the scaled tables lie
+// in [0, 1)
+__global__ void k_phon_exp(int nb, const unsigned long long* mx, int* sP) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const unsigned long long m = mx[b];
+  const int ex = (int)((m >> 52) & 0x7FF);
+  sP[b] = (ex == 0) ? 0 : -((ex - 1023) + 1);
+}
+
+// EP, EP^T, HP, HP^T of every wire as scaled FP32 (coalesced transposes via tiles)
+__global__ void k_phon_tables(int nk, const double* EP, const double* HP, const int* sP,
+                              float* epf, float* eptf, float* hpf, float* hptf) {
+  __shared__ double te[32][33], th[32][33];
+  const int b = blockIdx.z;
+  const long long mb = (long long)b * nk * nk;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int e = sP[b];
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    const bool ok = r < nk && c < nk;
+    const double ve = ok ? EP[mb + (long long)r * nk + c] : 0.0;
+    const double vh = ok ? HP[mb + (long long)r * nk + c] : 0.0;
+    te[i][threadIdx.x] = ve;
+    th[i][threadIdx.x] = vh;
+    if (ok) {
+      epf[mb + (long long)r * nk + c] = f64_to_f32(ve, e);
+      hpf[mb + (long long)r * nk + c] = f64_to_f32(vh, e);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = c0 + i, c = r0 + threadIdx.x;   // row c0 + i of the transpose
+    if (r < nk && c < nk) {
+      eptf[mb + (long long)r * nk + c] = f64_to_f32(te[threadIdx.x][i], e);
+      hptf[mb + (long long)r * nk + c] = f64_to_f32(th[threadIdx.x][i], e);
+    }
+  }
+}
+
+__global__ void k_const_f(const WireDev* wires, const double2* expikr, long long tot_kr,
+                          float2* ekrf, const double* xeh, float* xef, int nw) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < tot_kr) ekrf[i] = f64_to_f32(expikr[i]);
+  if (i < 2ll * nw * wires[0].nk) {
+    const int nk = wires[0].nk;
+    const int b = (int)(i / (2 * nk)), j = (int)(i % (2 * nk));
+    xef[i] = fabsf(f64_to_f32(xeh[2 * wires[b].off_vec + j]));
+  }
 }
 
 static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
@@ -285,8 +404,44 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
     mixed_free(c);
     return rc;
   }
+  // constant FP32 tables and per-step FP32 scratch
+  const int T = (nk + 31) / 32;
+  const size_t cbytes = sizeof(float) * (4 * tm + 2 * (size_t)nw * nk + 2 * (size_t)nw * nk +
+                                         4 * (size_t)nw * nk) +
+                        sizeof(int) * (size_t)nw + sizeof(unsigned long long) * (size_t)nw + 64;
+  void* cblock = nullptr;
+  if (cudaMalloc(&cblock, cbytes) != cudaSuccess ||
+      cudaMalloc(&m->ekrf, sizeof(float2) * (size_t)c->tot_kr) != cudaSuccess ||
+      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * T * T * 63) != cudaSuccess) {
+    if (cblock) cudaFree(cblock);
+    m->epf = nullptr;
+    c->mixed = m;
+    mixed_free(c);
+    return fail(SBE_ERR_OOM, "mixed path: table allocation failed");
+  }
+  m->epf = static_cast<float*>(cblock);
+  m->eptf = m->epf + tm;
+  m->hpf = m->eptf + tm;
+  m->hptf = m->hpf + tm;
+  m->xef = m->hptf + tm;
+  m->phf = m->xef + 2 * (size_t)nw * nk;
+  m->gtab = m->phf + 2 * (size_t)nw * nk;
+  m->sP = reinterpret_cast<int*>(m->gtab + 4 * (size_t)nw * nk);
+  unsigned long long* mx64 = reinterpret_cast<unsigned long long*>(
+      (reinterpret_cast<uintptr_t>(m->sP + nw) + 7) & ~uintptr_t(7));
+  // sheared planes: zero once; stages write only the in-band part
+  cudaMemsetAsync(m->spl, 0, sizeof(__half) * 3 * 2 * nw * 4 * mm, s);
   k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(c->d_wires, c->expikr, m->epl, nw);
   k_fill_int<<<(nw + 127) / 128, 128, 0, s>>>(m->eE(), nw, 13);
+  cudaMemsetAsync(mx64, 0, sizeof(unsigned long long) * nw, s);
+  k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->EP, (long long)mm, mx64);
+  k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->HP, (long long)mm, mx64);
+  k_phon_exp<<<(nw + 127) / 128, 128, 0, s>>>(nw, mx64, m->sP);
+  k_phon_tables<<<dim3(T, T, nw), dim3(32, 8), 0, s>>>(nk, c->EP, c->HP, m->sP, m->epf, m->eptf,
+                                                      m->hpf, m->hptf);
+  const long long nconst = std::max<long long>(c->tot_kr, 2ll * nw * nk);
+  k_const_f<<<(unsigned)((nconst + 255) / 256), 256, 0, s>>>(c->d_wires, c->expikr, c->tot_kr,
+                                                             m->ekrf, c->xeh, m->xef, nw);
   c->mixed = m;
   return cuda_check(cudaGetLastError(), "mixed workspace");
 }
@@ -327,24 +482,238 @@ __global__ void k_vs_max(const WireDev* wires, const double* vs, unsigned* mx) {
 
 // hbar A and hbar B in FP32 (dephasing.py:714-743 contraction matrices A[k][j] =
 // Dh[j - k][k], B[k][j] = De[j - k][k], j != k) and max(2 hbar |A|, 2 hbar |B|).
+// The block's sources Dh[q][k], q = j - k + Nk in a 63-wide band, k in its 32
+// rows, are read row by row (coalesced) into shared memory.
 __global__ void k_hab(const WireDev* wires, const double* De, const double* Dh, float* habf,
                       long long tot_mat, unsigned* mx) {
+  __shared__ double ta[63][33], tb[63][33];
   const WireDev W = wires[blockIdx.z];
   const int nk = W.nk;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
+  const int j0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int qbase = j0 - k0 - 31 + nk;
+  const bool on_w = (W.flags & SBE_F_OFFDIAGDPH) != 0;
+  for (int qq = threadIdx.y; qq < 63; qq += blockDim.y) {
+    const int q = qbase + qq, k = k0 + threadIdx.x;
+    const bool ok = on_w && q >= 0 && q <= 2 * nk && k < nk;
+    const long long di = W.off_dd + (long long)q * nk + k;
+    ta[qq][threadIdx.x] = ok ? Dh[di] : 0.0;
+    tb[qq][threadIdx.x] = ok ? De[di] : 0.0;
+  }
+  __syncthreads();
+  const float hb = (float)kHbar;
   float m = 0.f;
-  if (j < nk && row < nk) {
-    const bool on = (W.flags & SBE_F_OFFDIAGDPH) && j != row;
-    const long long di = W.off_dd + (long long)(j - row + nk) * nk + row;
-    const float ha = on ? (float)kHbar * f64_to_f32(Dh[di]) : 0.f;
-    const float hb = on ? (float)kHbar * f64_to_f32(De[di]) : 0.f;
-    const long long o = W.off_mat + (long long)row * nk + j;
+  const int j = j0 + threadIdx.x;
+  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+    const int k = k0 + kk;
+    if (k >= nk || j >= nk) continue;
+    const int qq = (j - k) - (j0 - k0) + 31;
+    const float ha = (j != k) ? hb * f64_to_f32(ta[qq][kk]) : 0.f;
+    const float hh = (j != k) ? hb * f64_to_f32(tb[qq][kk]) : 0.f;
+    const long long o = W.off_mat + (long long)k * nk + j;
     habf[o] = ha;
-    habf[tot_mat + o] = hb;
-    m = 2.f * fmaxf(fabsf(ha), fabsf(hb));
+    habf[tot_mat + o] = hh;
+    m = fmaxf(m, 2.f * fmaxf(fabsf(ha), fabsf(hh)));
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(m));
+}
+
+// Per-step weights of CalcGammaE/H (dephasing.py:29-103) per q: (pi/hbar) V^2 |x|
+// with V = Vxx2 at iq[q]: [0] vee^2 |xe|, [1] veh^2 |xh|, [2] vhh^2 |xh|, [3] veh^2 |xe|.
+__global__ void k_gamma_tab(const WireDev* wires, const double* vs, const int* iq,
+                            const double* xeh, float* gtab, int nw) {
+  const WireDev W = wires[blockIdx.y];
+  const int nk = W.nk, b = blockIdx.y;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nk) return;
+  const double* v = vs + 3 * W.off_vec;
+  const int i = iq[W.off_vec + q];
+  const double pih = kPi / kHbar;
+  const double veh = v[i], vee = v[nk + i], vhh = v[2 * nk + i];
+  const double xe = fabs(xeh[2 * W.off_vec + q]), xh = fabs(xeh[2 * W.off_vec + nk + q]);
+  const long long o = (long long)b * nk + q, st = (long long)nw * nk;
+  gtab[o] = f64_to_f32(pih * vee * vee * xe);
+  gtab[st + o] = f64_to_f32(pih * veh * veh * xh);
+  gtab[2 * st + o] = f64_to_f32(pih * vhh * vhh * xh);
+  gtab[3 * st + o] = f64_to_f32(pih * veh * veh * xe);
+}
+
+// CalcGammaE/H in FP32 (same sums and index maps as k_gamma); one warp per (wire,
+// k), lanes over q; occupations (real parts) staged in shared memory.
+__global__ void k_gamma_f(const WireDev* wires, const double2* ne, const double2* nh,
+                          const int* maps, const float* gtab, float* gamf, int nw) {
+  extern __shared__ float occ[];
+  const WireDev W = wires[blockIdx.y];
+  const int nk = W.nk, b = blockIdx.y;
+  float* pe = occ;
+  float* ph = occ + nk;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    pe[i] = f64_to_f32(ne[W.off_vec + i].x);
+    ph[i] = f64_to_f32(nh[W.off_vec + i].x);
+  }
+  __syncthreads();
+  const int k = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (k >= nk) return;
+  const long long vo = (long long)b * nk, st1 = (long long)nw * nk;
+  if (!(W.flags & SBE_F_DIAGDPH)) {
+    if (lane == 0) {
+      gamf[vo + k] = (float)W.gam_e;
+      gamf[st1 + vo + k] = (float)W.gam_h;
+    }
+    return;
+  }
+  const long long st = (long long)nk * nk;
+  const int* m = maps + 6 * W.off_mat + (long long)k * nk;
+  const float* g0 = gtab + vo;
+  const float* g1 = gtab + st1 + vo;
+  const float* g2 = gtab + 2 * st1 + vo;
+  const float* g3 = gtab + 3 * st1 + vo;
+  float ge = 0.f, gh = 0.f;
+  for (int q = lane; q < nk; q += 32) {
+    const int i0 = m[q], i1 = m[st + q], i2 = m[2 * st + q], i3 = m[3 * st + q];
+    const int i4 = m[4 * st + q], i5 = m[5 * st + q];
+    const bool k0ok = i0 >= 0 && i0 < nk;
+    if (k0ok) {
+      const float a = pe[i0], bb = ph[i0];
+      ge += g0[q] * (a * (1.f - a));
+      gh += g2[q] * (bb * (1.f - bb));
+    }
+    const bool ok1 = i1 >= 0 && i1 < nk, ok2 = i2 >= 0 && i2 < nk, ok3 = i3 >= 0 && i3 < nk;
+    const bool ok4 = i4 >= 0 && i4 < nk, ok5 = i5 >= 0 && i5 < nk;
+    if (ok3 && ok2 && ok1) {
+      const float n1 = ph[i3], n2 = ph[i2], n3 = pe[i1];
+      ge += g1[q] * (n1 * (1.f - n2) * n3 + (1.f - n1) * n2 * (1.f - n3));
+    }
+    if (ok5 && ok4 && ok1) {
+      const float e1 = pe[i5], e2 = pe[i4], h3 = ph[i1];
+      gh += g3[q] * (e1 * (1.f - e2) * h3 + (1.f - e1) * e2 * (1.f - h3));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ge += __shfl_down_sync(0xffffffffu, ge, o);
+    gh += __shfl_down_sync(0xffffffffu, gh, o);
+  }
+  if (lane == 0) {
+    gamf[vo + k] = ge;
+    gamf[st1 + vo + k] = gh;
+  }
+}
+
+// Per-step phonon coupling per |k - k'| (phonons.py:140-268): Vep(d) = VC_ee(d) /
+// E1D(d) Vscale and Vhp for holes, scaled by 2^-sP to pair with the FP32 tables.
+__global__ void k_phon_tab(const WireDev* wires, const double* vs, const double* eps,
+                           const int* sP, float* phf, int nw) {
+  const WireDev W = wires[blockIdx.y];
+  const int nk = W.nk, b = blockIdx.y;
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nk) return;
+  const double* v = vs + 3 * W.off_vec;
+  const double ep = eps[W.off_vec + d];
+  phf[(long long)b * nk + d] = f64_to_f32(v[nk + d] / ep * W.vscale, -sP[b]);
+  phf[((long long)nw + b) * nk + d] = f64_to_f32(v[2 * nk + d] / ep * W.vscale, -sP[b]);
+}
+
+// MBPE / MBPH (phonons.py:157-268) in FP32 from the scaled tables: Win, Wout of
+// electrons and holes at the occupations in ne, nh (real parts) into wrate (FP64).
+__global__ void k_phonon_rates_f(const WireDev* wires, const double2* nev, const double2* nhv,
+                                 const float* phf, const float* epf, const float* eptf,
+                                 const float* hpf, const float* hptf, double* wrate, int nw) {
+  extern __shared__ float occ[];
+  const WireDev W = wires[blockIdx.y];
+  const int nk = W.nk, b = blockIdx.y, k = blockIdx.x;
+  float* pe = occ;
+  float* ph = occ + nk;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    pe[i] = f64_to_f32(nev[W.off_vec + i].x);
+    ph[i] = f64_to_f32(nhv[W.off_vec + i].x);
+  }
+  __syncthreads();
+  const float* ve = phf + (long long)b * nk;
+  const float* vh = phf + ((long long)nw + b) * nk;
+  const long long row = W.off_mat + (long long)k * nk;
+  float wie = 0.f, woe = 0.f, wih = 0.f, woh = 0.f;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    const float a = pe[i], c = ph[i];
+    if (k >= i) {
+      const float v = ve[k - i];
+      wie += v * a * epf[row + i];
+      woe += v * (1.f - a) * eptf[row + i];
+    }
+    if (i >= k) {
+      const float v = vh[i - k];
+      wih += v * c * hpf[row + i];
+      woh += v * (1.f - c) * hptf[row + i];
+    }
+  }
+  __shared__ float red[4][4];
+  float vals[4] = {wie, woe, wih, woh};
+  for (int j = 0; j < 4; ++j)
+    for (int o = 16; o > 0; o >>= 1) vals[j] += __shfl_down_sync(0xffffffffu, vals[j], o);
+  if ((threadIdx.x & 31) == 0)
+    for (int j = 0; j < 4; ++j) red[j][threadIdx.x >> 5] = vals[j];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    wrate[4 * W.off_vec + threadIdx.x * nk + k] = f32_to_f64(t);
+  }
+}
+
+// max(|re|, |im|) of the diagonals of C and D into mx[b] (after the relaxation
+// step has rewritten them)
+__global__ void k_diag_max(const WireDev* wires, const double2* C, const double2* D,
+                           unsigned* mx) {
+  const WireDev W = wires[blockIdx.x];
+  unsigned long long m = 0;
+  for (int k = threadIdx.x; k < W.nk; k += blockDim.x) {
+    const long long o = W.off_mat + (long long)k * W.nk + k;
+    const double2 a = C[o], d = D[o];
+    m = max(m, max(max(absbits(a.x), absbits(a.y)), max(absbits(d.x), absbits(d.y))));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.x, bits_to_fmax(m));
+}
+
+// QWPolarization3 / QWRho5 reduction (qwoptics.py:809-1071) from the FP32 source
+// GEMM outputs G[k][r] = sum_k' X[k][k'] e^{i k' r}: sums over k in FP32, the
+// physical prefactors in FP64 per r.
+__global__ void k_src_reduce_f(const WireDev* wires, const float2* ekrf, const float2* G,
+                               long long tot_kr, const double* win, double2* src) {
+  const WireDev W = wires[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= W.nr) return;
+  const int nk = W.nk, nr = W.nr;
+  const float2* E = ekrf + W.off_kr;
+  const float2* Gp = G + W.off_kr;
+  const float2* Gc = G + tot_kr + W.off_kr;
+  const float2* Gd = G + 2 * tot_kr + W.off_kr;
+  float sx = 0.f, sy = 0.f, ser = 0.f, sei = 0.f, shr = 0.f, shi = 0.f;
+  for (int k = 0; k < nk; ++k) {
+    const long long o = (long long)k * nr + r;
+    const float2 e = E[o];             // conj taken below
+    const float2 gp = Gp[o], gc = Gc[o], gd = Gd[o];
+    const float re_part = e.x * gp.x + e.y * gp.y;
+    sx += (k & 1) ? -re_part : re_part;
+    sy += re_part;
+    ser += e.x * gc.x + e.y * gc.y;
+    sei += e.x * gc.y - e.y * gc.x;
+    shr += e.x * gd.x + e.y * gd.y;
+    shi += e.x * gd.y - e.y * gd.x;
+  }
+  const double w = win[W.off_r + r];
+  double2* out = src + 5 * W.off_r;
+  const bool optics = (W.flags & SBE_F_OPTICS) != 0;
+  const double pf = 2 * W.ehint / W.area / W.L;
+  const double px = optics ? (W.dcv * f32_to_f64(sx)) * w : 0.0;
+  const double py = optics ? (W.dcv * f32_to_f64(sy)) * w * W.yw : 0.0;
+  const double pz = optics ? (-W.dcv * f32_to_f64(sy)) * w * W.zsign : 0.0;
+  out[r] = make_double2(px * pf, 0.0);
+  out[nr + r] = make_double2(py * pf, 0.0);
+  out[2 * nr + r] = make_double2(pz * pf, 0.0);
+  const double f = w / (2.0 * W.L);
+  out[3 * nr + r] = make_double2(f32_to_f64(ser) * f, f32_to_f64(sei) * f);
+  out[4 * nr + r] = make_double2(f32_to_f64(shr) * f, f32_to_f64(shi) * f);
 }
 
 __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH, float* gamf,
@@ -375,6 +744,9 @@ __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* 
   const int t0 = blockIdx.x * 32, dd0 = blockIdx.y * 32;
   const int rbase = t0 + dd0 - (nk - 1);
   const int tx = threadIdx.x;
+  // blocks whose source rows all lie outside the matrix hold only zeros, which
+  // the buffer keeps from its initialisation
+  if (rbase + 62 < 0 || rbase >= nk) return;
   for (int rr = threadIdx.y; rr < 63; rr += blockDim.y) {
     const int r = rbase + rr, c = t0 + tx;
     tile[rr][tx] = (r >= 0 && r < nk && c < nk) ? X[(long long)r * nk + c] : make_double2(0, 0);
@@ -388,6 +760,8 @@ __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* 
   for (int ddl = threadIdx.y; ddl < 32; ddl += blockDim.y) {
     const int dd = dd0 + ddl;
     if (dd >= 2 * nk) break;
+    const int r = rbase + tx + ddl;
+    if (r < 0 || r >= nk) continue;   // out of band: stays zero
     const double2 v = tile[tx + ddl][tx];
     put_hilo(base + (long long)(2 * dd) * nk + tp, plane, f64_to_f32(v.x, eb));
     put_hilo(base + (long long)(2 * dd + 1) * nk + tp, plane, f64_to_f32(v.y, eb));
@@ -434,9 +808,10 @@ __global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* 
                           float2* dgf, unsigned* mx) {
   const WireDev& W = wires[blockIdx.z];
   const int nk = W.nk, b = blockIdx.z, nw = gridDim.z;
-  const int k2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int k1 = blockIdx.y;
   float hmax = 0.f;
+  for (int it = 0; it < 4; ++it) {
+  const int k2 = blockIdx.x * blockDim.x * 4 + it * blockDim.x + threadIdx.x;
   if (k1 < nk && k2 < nk) {
     float2 heh = make_float2(0.f, 0.f), hee = heh, hhh = heh;
     if (W.flags & SBE_F_OPTICS) {
@@ -501,8 +876,10 @@ __global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* 
     }
     hf[tot_mat + o] = hee;
     hf[2 * tot_mat + o] = hhh;
-    hmax = fmaxf(fmaxf(fmaxf(fabsf(heh.x), fabsf(heh.y)), fmaxf(fabsf(hee.x), fabsf(hee.y))),
-                 fmaxf(fabsf(hhh.x), fabsf(hhh.y)));
+    hmax = fmaxf(hmax, fmaxf(fmaxf(fmaxf(fabsf(heh.x), fabsf(heh.y)),
+                                   fmaxf(fabsf(hee.x), fabsf(hee.y))),
+                             fmaxf(fabsf(hhh.x), fabsf(hhh.y))));
+  }
   }
   __shared__ float red[4];
   for (int o = 16; o > 0; o >>= 1) hmax = fmaxf(hmax, __shfl_down_sync(0xffffffffu, hmax, o));
@@ -581,8 +958,9 @@ __global__ void k_antiherm(int nk, const float2* W, const double2* X, const floa
 
 // RK4 stage update of the mixed path: the stage derivative k and the sums
 // k1 + 2 k2 + 2 k3 are FP32 (they carry the RHS's FP32-accumulated precision);
-// the state is FP64 and only the additions to it are FP64.  Stages 1-3 also
-// measure the next stage state's maximum per wire into mx[b].
+// the state is FP64 and only the additions to it are FP64.  Every stage also
+// measures the maximum of the state it writes (the next stage state, or the new
+// state after stage 4) per wire into mx[b].
 // grid (blocks per wire, wires).
 __global__ void k_rk4_mixed(long long per, int stage, float dt, double2* X, float2* acc,
                             double2* xs, const float2* k, unsigned* mx) {
@@ -607,10 +985,13 @@ __global__ void k_rk4_mixed(long long per, int stage, float dt, double2* X, floa
     } else {
       const float2 a = acc[i];
       const float s = dt / 6.f;
-      X[i] = make_double2(x.x + f32_to_f64(s * (a.x + kv.x)), x.y + f32_to_f64(s * (a.y + kv.y)));
+      const double2 v =
+          make_double2(x.x + f32_to_f64(s * (a.x + kv.x)), x.y + f32_to_f64(s * (a.y + kv.y)));
+      X[i] = v;
+      m = max(m, max(absbits(v.x), absbits(v.y)));
     }
   }
-  if (stage < 4) {
+  {
     __shared__ unsigned long long red[8];
     for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -656,22 +1037,39 @@ static void exponents_from(Mixed* m, const unsigned* mx, int* e, cudaStream_t s)
 static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
-  launch_prep_scalar(c, C, D, s);
-  launch_gamma(c, -1, s);
-  cudaMemsetAsync(m->mxAB(), 0, sizeof(unsigned) * nw, s);
-  if (c->any_offdiag) {
-    ProfScope ps(c, 3, s);
-    launch_offdiag_D(c, -1, nullptr, true, s);
-  }
-  k_hab<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(c->d_wires, c->De, c->Dh, m->habf,
-                                                       c->tot_mat, m->mxAB());
-  k_gam_f<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->gamE, c->gamH, m->gamf, nw);
+  launch_prep_scalar(c, C, D, s);   // occupations, screening (FP64, O(Nk) per wire)
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
   k_vs_max<<<nw, 256, 0, s>>>(c->d_wires, c->vs, m->mxH());
   exponents_from(m, m->mxH(), m->eT(), s);
   k_toeplitz_planes<<<dim3((nk + 127) / 128, nk, 3 * nw), 128, 0, s>>>(c->d_wires, c->vs, m->eT(),
                                                                        m->tpl, nw, m->vsf);
+  k_gamma_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->iq, c->xeh,
+                                                         m->gtab, nw);
+  k_gamma_f<<<dim3((nk + 7) / 8, nw), 256, sizeof(float) * 2 * nk, s>>>(
+      c->d_wires, c->ne, c->nh, c->maps, m->gtab, m->gamf, nw);
+  k_phon_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->eps, m->sP, m->phf,
+                                                        nw);
+  cudaMemsetAsync(m->mxAB(), 0, sizeof(unsigned) * nw, s);
+  if (c->any_offdiag) {
+    ProfScope ps(c, 3, s);
+    launch_offdiag_D(c, -1, nullptr, true, s);
+  }
+  const int T = (nk + 31) / 32;
+  k_hab<<<dim3(T, T, nw), dim3(32, 8), 0, s>>>(c->d_wires, c->De, c->Dh, m->habf, c->tot_mat,
+                                               m->mxAB());
   return cuda_check(cudaGetLastError(), "mixed prep");
+}
+
+// Relaxation (phonon in/out rates of the new occupations, FP32 sums) and charge
+// normalisation after the step (SBEs.py:5677-5702), then the state maximum.
+static void mixed_relax(SbeCtx* c, double2* C, double2* D, double dt, cudaStream_t s) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  const int nk = m->nk, nw = m->nw;
+  launch_extract_diag(c, C, D, s);
+  k_phonon_rates_f<<<dim3(nk, nw), 128, sizeof(float) * 2 * nk, s>>>(
+      c->d_wires, c->ne, c->nh, m->phf, m->epf, m->eptf, m->hpf, m->hptf, c->wrate, nw);
+  launch_relax_only(c, C, D, dt, s);
+  k_diag_max<<<nw, 256, 0, s>>>(c->d_wires, C, D, m->mxS());
 }
 
 // One stage RHS of every wire at state (P, C, D) and wire-k field Ek (FP64);
@@ -696,12 +1094,12 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   const double2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eS(), m->planes, M_P, M_PT, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eS(), m->planes, M_C, -1, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eS(), m->planes, M_D, -1, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eS(), m->planes, M_C, -1, nw, m->tpart, 0);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eS(), m->planes, M_D, -1, nw, m->tpart, 1);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
   k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
-  k_traces_f<<<dim3(2 * nk - 1, 2, nw), 32, 0, s>>>(c->d_wires, C, D, m->trf);
+  k_trace_reduce<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, m->tpart, m->trf);
   int rc = SBE_OK;
   const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
   if (have_x) {
@@ -722,7 +1120,7 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
     }
   }
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
-  k_h_build<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
+  k_h_build<<<dim3((nk + 511) / 512, nk, nw), 128, 0, s>>>(
       c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, m->xsh, have_x, m->hf, tm, m->dgE, m->dgH,
       m->dgf, m->mxH());
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
@@ -766,27 +1164,32 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 
-// Sources of the new state through the engine: G = [P; C; conj(D)] E.
+// Sources of the new state through the engine: G = [P; C; conj(D)] E (FP32
+// outputs), then the per-r reductions.  mxS holds the state maximum when
+// state_max_ready is set.
 static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const double2* D,
-                         double2* src, cudaStream_t s) {
+                         double2* src, int state_max_ready, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   const long long mm = (long long)nk * nk;
-  cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-  absmax_into(P, mm, nw, m->mxS(), s);
-  absmax_into(C, mm, nw, m->mxS(), s);
-  absmax_into(D, mm, nw, m->mxS(), s);
+  if (!state_max_ready) {
+    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+    absmax_into(P, mm, nw, m->mxS(), s);
+    absmax_into(C, mm, nw, m->mxS(), s);
+    absmax_into(D, mm, nw, m->mxS(), s);
+  }
   exponents_from(m, m->mxS(), m->eS(), s);
   const double2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   for (int i = 0; i < 3; ++i)
     k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->planes, 2 * i, -1, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
+  float2* gf = reinterpret_cast<float2*>(c->G);
   for (int i = 0; i < 3; ++i) {
     tc::Term t{2 * i, 0, i == 2 ? 1 : 0, 0, 1};
     tc::EpiArgs e{};
-    e.kind = tc::EPI_RAW;
-    e.out = c->G + i * c->tot_kr;
+    e.kind = tc::EPI_RAWF;
+    e.outf2 = gf + i * c->tot_kr;
     e.out_bstride = (long long)nk * m->nr;
     e.escale = m->ess();
     e.err = m->err();
@@ -794,7 +1197,9 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     int rc = gemm(m, m->mapA, m->mapEB, nk, m->nr, nk, 1, 1, &t, 0, e, s);
     if (rc) return rc;
   }
-  launch_sources_reduce(c, c->ne, c->nh, src, s);
+  k_src_reduce_f<<<dim3((m->nr + 127) / 128, nw), 128, 0, s>>>(c->d_wires, m->ekrf, gf, c->tot_kr,
+                                                              c->window, src);
+  launch_sources_final(c, c->ne, c->nh, src, s);
   return cuda_check(cudaGetLastError(), "mixed sources");
 }
 
@@ -844,15 +1249,15 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
     rc = mixed_stage(c, xp, xc, xd, c->ekst, st > 1, s);
     if (rc) return rc;
-    // RK4 update; stages 1-3 also measure the next stage state's maximum
-    if (st < 4) cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
+    // RK4 update; every stage also measures the maximum of the state it writes
+    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
     double2* X[3] = {P, C, D};
     for (int i = 0; i < 3; ++i)
       k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(per, st, (float)dt, X[i], m->accf + i * n,
                                                   c->xs + i * n, m->kf + i * n, m->mxS());
   }
-  launch_relax_norm(c, C, D, dt, false, s);
-  return mixed_sources(c, P, C, D, src, s);
+  mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
+  return mixed_sources(c, P, C, D, src, 1, s);
 }
 
 }  // namespace sbe

@@ -105,6 +105,7 @@ def test_graph_replay_matches_direct_step(prec):
         torch.cuda.synchronize()
         outs.append((P, C, D, src))
     for a, b in zip(*outs):
+        assert torch.isfinite(a).all()
         assert torch.equal(a, b)
 
 
