@@ -112,9 +112,16 @@ __device__ __forceinline__ float2 scaled2<float2>(float2 v, int e) {
 // With tpart set (double input only), the block also writes the 63 diagonal sums
 // of its 32 x 32 tile to tpart[((b * 2 + which) * T + bi) * T + bj][l], local
 // diagonal l = c - r + 31, for the traces of C and D.
+// With cdf set, the diagonal is left out of the planes (written as zero) and the
+// hi / lo FP32 parts of its real part go to cdf[b * nk + k] and
+// cdf[nbatch * nk + b * nk + k].
+__device__ __forceinline__ double dvalue(double2 v) { return v.x; }
+__device__ __forceinline__ double dvalue(float2 v) { return f32_to_f64(v.x); }
+
 template <typename T>
 __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int matN, int matT,
-                            int nbatch, float2* tpart = nullptr, int which = 0) {
+                            int nbatch, float2* tpart = nullptr, int which = 0,
+                            float* cdf = nullptr) {
   __shared__ T tile[32][33];
   const int b = blockIdx.z;
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
@@ -136,7 +143,16 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int m
       // pass 0: row r0 + i of X;  pass 1: row c0 + i of X^T (= column c0 + i of X)
       const int r = (pass ? c0 : r0) + i, c = (pass ? r0 : c0) + threadIdx.x;
       if (r >= nk || c >= nk) continue;
-      const float2 v = scaled2<T>(pass ? tile[threadIdx.x][i] : tile[i][threadIdx.x], eb);
+      float2 v = scaled2<T>(pass ? tile[threadIdx.x][i] : tile[i][threadIdx.x], eb);
+      if (cdf && r == c) {
+        v = make_float2(0.f, 0.f);
+        if (pass == 0) {
+          const double d = dvalue(tile[i][threadIdx.x]);
+          const float hi = f64_to_f32(d);
+          cdf[(long long)b * nk + r] = hi;
+          cdf[((long long)nbatch + b) * nk + r] = f64_to_f32(d - f32_to_f64(hi));
+        }
+      }
       __half* base = (pass ? bt : bn) + (long long)r * nk + c;
       put_hilo(base, plane, v.x);
       put_hilo(base + 2 * plane, plane, v.y);
@@ -230,7 +246,8 @@ struct Mixed {
   float* phf = nullptr;     // 2 x nw x nk: Vep(d) 2^-sP, Vhp(d) 2^-sP
   float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
   float2* tpart = nullptr;  // nw x 2 x T x T x 63 partial diagonal sums (T = ceil(nk/32))
-  CUtensorMap mapA, mapB, mapTA, mapSB, mapEB;
+  float* cdf = nullptr;     // 4 x nw x nk: hi / lo parts of Re C_kk and Re D_kk (stage state)
+  CUtensorMap mapA, mapB, mapTA, mapSB, mapEB, mapB64;
   int* eS() { return ints; }
   int* eH() { return ints + nw; }
   int* eT() { return ints + 2 * nw; }
@@ -239,9 +256,11 @@ struct Mixed {
   int* esx() { return ints + 5 * nw; }
   int* ess() { return ints + 6 * nw; }
   int* err() { return ints + 7 * nw; }
+  int* eO() { return ints + 8 * nw; }   // commutator state operands (diagonals of C, D peeled)
   unsigned* mxH() { return mx; }
   unsigned* mxS() { return mx + nw; }
   unsigned* mxAB() { return mx + 2 * nw; }
+  unsigned* mxO() { return mx + 3 * nw; }  // max over P and the off-diagonal C, D
 };
 
 enum { M_P = 0, M_PT, M_C, M_CT, M_D, M_DT, M_EH, M_EHT, M_EE, M_EET, M_HH, M_HHT, M_EEX, M_HHX };
@@ -370,8 +389,8 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
             cudaMalloc(&m->spl, sizeof(__half) * 3 * 2 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->epl, sizeof(__half) * 4 * nw * (size_t)m->nr * nk) == cudaSuccess &&
             cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 4 * mm) == cudaSuccess &&
-            cudaMalloc(&m->ints, sizeof(int) * 8 * nw) == cudaSuccess &&
-            cudaMalloc(&m->mx, sizeof(unsigned) * 3 * nw) == cudaSuccess &&
+            cudaMalloc(&m->ints, sizeof(int) * 9 * nw) == cudaSuccess &&
+            cudaMalloc(&m->mx, sizeof(unsigned) * 4 * nw) == cudaSuccess &&
             cudaMalloc(&fblock, fbytes) == cudaSuccess &&
             cudaMalloc(&m->dgE, sizeof(double2) * 2 * nw * nk) == cudaSuccess;
   m->kf = static_cast<float2*>(fblock);
@@ -389,13 +408,14 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   m->vsf = m->habf + 2 * tm;
   m->gamf = m->vsf + 3 * (size_t)nw * nk;
   m->dgH = m->dgE + (size_t)nw * nk;
-  cudaMemsetAsync(m->ints, 0, sizeof(int) * 8 * nw, s);
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 3 * nw, s);
+  cudaMemsetAsync(m->ints, 0, sizeof(int) * 9 * nw, s);
+  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 4 * nw, s);
   TcPlanes pl{m->planes, 14, 4, nw, nk, nk};
   TcPlanes tp{m->tpl, 3, 2, nw, nk, nk};
   TcPlanes sp{m->spl, 3, 2, nw, 4 * nk, nk};
   TcPlanes ep{m->epl, 1, 4, nw, m->nr, nk};
   int rc = tc_make_maps(pl, pl, &m->mapA, &m->mapB);
+  if (!rc) rc = tc_make_map_split(pl, &m->mapB64);
   if (!rc) rc = tc_make_maps(tp, sp, &m->mapTA, &m->mapSB);
   CUtensorMap dummy;
   if (!rc) rc = tc_make_maps(tp, ep, &dummy, &m->mapEB);
@@ -407,7 +427,7 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   // constant FP32 tables and per-step FP32 scratch
   const int T = (nk + 31) / 32;
   const size_t cbytes = sizeof(float) * (4 * tm + 2 * (size_t)nw * nk + 2 * (size_t)nw * nk +
-                                         4 * (size_t)nw * nk) +
+                                         4 * (size_t)nw * nk + 4 * (size_t)nw * nk) +
                         sizeof(int) * (size_t)nw + sizeof(unsigned long long) * (size_t)nw + 64;
   void* cblock = nullptr;
   if (cudaMalloc(&cblock, cbytes) != cudaSuccess ||
@@ -426,7 +446,8 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   m->xef = m->hptf + tm;
   m->phf = m->xef + 2 * (size_t)nw * nk;
   m->gtab = m->phf + 2 * (size_t)nw * nk;
-  m->sP = reinterpret_cast<int*>(m->gtab + 4 * (size_t)nw * nk);
+  m->cdf = m->gtab + 4 * (size_t)nw * nk;
+  m->sP = reinterpret_cast<int*>(m->cdf + 4 * (size_t)nw * nk);
   unsigned long long* mx64 = reinterpret_cast<unsigned long long*>(
       (reinterpret_cast<uintptr_t>(m->sP + nw) + 7) & ~uintptr_t(7));
   // sheared planes: zero once; stages write only the in-band part
@@ -444,6 +465,30 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
                                                              m->ekrf, c->xeh, m->xef, nw);
   c->mixed = m;
   return cuda_check(cudaGetLastError(), "mixed workspace");
+}
+
+// maxima of a batch of Nk x Nk matrices: all elements into mx[b], and (when
+// peel) the off-diagonal elements into mo[b] (all elements when !peel)
+__global__ void k_absmax2(const double2* X, int nk, int peel, unsigned* mx, unsigned* mo) {
+  const int b = blockIdx.y;
+  const long long per = (long long)nk * nk;
+  const double2* x = X + (long long)b * per;
+  unsigned long long m = 0, o = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = x[i];
+    const unsigned long long a = max(absbits(v.x), absbits(v.y));
+    m = max(m, a);
+    if (!peel || (i % (nk + 1)) != 0) o = max(o, a);
+  }
+  for (int k = 16; k > 0; k >>= 1) {
+    m = max(m, __shfl_down_sync(0xffffffffu, m, k));
+    o = max(o, __shfl_down_sync(0xffffffffu, o, k));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(mx + b, bits_to_fmax(m));
+    atomicMax(mo + b, bits_to_fmax(o));
+  }
 }
 
 static void absmax_into(const double2* X, long long per, int nw, unsigned* mx, cudaStream_t s) {
@@ -912,46 +957,71 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
   }
 }
 
-// dC (dD) from W = C Hee'^T + P^H Heh^T (V = D Hhh'^T + conj(P) Heh): for
-// Hermitian C, Hee (D, Hhh) the four terms of dCdt (dDdt) are W - W^H, so
-//   dX[i][j] = (W[i][j] - conj(W[j][i]) + (g[j] - g[i]) X[i][j]) / (i hbar)
-// with g the peeled diagonal.  The result is exactly anti-Hermitian, which
-// keeps C and D Hermitian.  A block owns the tile pair (bi, bj), (bj, bi) with
-// bi <= bj and reads each W element once.  W holds FP32 accumulator values; the
-// diagonal difference g[j] - g[i] comes from the hi / lo FP32 parts of g (the hi
-// parts of two close energies differ exactly).
-__global__ void k_antiherm(int nk, const float2* W, const double2* X, const float2* ghi,
-                           const float2* glo, float2* out) {
-  __shared__ float2 ta[32][33], tb[32][33];
+// dC (dD) from W = C' Hee'^T + P^H Heh^T (V = D' Hhh'^T + conj(P) Heh), where C'
+// (D') is C (D) without its diagonal c (d): for Hermitian C, Hee (D, Hhh) the four
+// terms of dCdt (dDdt) are W - W^H plus the peeled diagonal's (c_i - c_j) Hee'[j][i],
+//   dX[i][j] = (W[i][j] - conj(W[j][i]) + (c_i - c_j) H'[j][i] + (g[j] - g[i]) X[i][j])
+//              / (i hbar)
+// with g the peeled energy diagonal.  Near equilibrium c_i - c_j is small against
+// c_i H' and is formed from the hi / lo FP32 parts of c (the hi parts of close
+// occupations differ exactly), so it does not carry the GEMM's rounding.  The
+// result is exactly anti-Hermitian, which keeps C and D Hermitian.  A block owns
+// the tile pair (bi, bj), (bj, bi) with bi <= bj and reads each W and H' element
+// once.  W holds FP32 accumulator values; g[j] - g[i] comes from the hi / lo
+// FP32 parts of g.
+__global__ void k_antiherm(int nk, const float2* W, const float2* W2, const float2* Hp,
+                           const double2* X, const float2* ghi, const float2* glo,
+                           const float* chi, const float* clo, float2* out) {
+  // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results
+  __shared__ float2 tb[32][33], hb[32][33], vt[32][33];
   const int bi = blockIdx.y, bj = blockIdx.x;
   if (bi > bj) return;
   const int b = blockIdx.z;
   const int i0 = bi * 32, j0 = bj * 32;
   const long long mb = (long long)b * nk * nk;
   const float2* w = W + mb;
+  const float2* w2 = W2 + mb;
+  const float2* hp = Hp + mb;
   for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int ia = i0 + r, ja = j0 + threadIdx.x;
-    ta[r][threadIdx.x] = (ia < nk && ja < nk) ? w[(long long)ia * nk + ja] : make_float2(0, 0);
     const int ib = j0 + r, jb = i0 + threadIdx.x;
-    tb[r][threadIdx.x] = (ib < nk && jb < nk) ? w[(long long)ib * nk + jb] : make_float2(0, 0);
+    const bool okb = ib < nk && jb < nk;
+    const long long ob = (long long)ib * nk + jb;
+    tb[r][threadIdx.x] = okb ? make_float2(w[ob].x + w2[ob].x, w[ob].y + w2[ob].y)
+                             : make_float2(0, 0);
+    hb[r][threadIdx.x] = okb ? hp[(long long)ib * nk + jb] : make_float2(0, 0);
   }
   __syncthreads();
   const float ih = (float)(1.0 / kHbar);
   const float2* gh = ghi + (long long)b * nk;
   const float2* gl = glo + (long long)b * nk;
-  for (int pass = 0; pass < (bi == bj ? 1 : 2); ++pass) {
-    const int ri0 = pass ? j0 : i0, cj0 = pass ? i0 : j0;
-    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-      const int i = ri0 + r, j = cj0 + threadIdx.x;
-      if (i >= nk || j >= nk) continue;
-      const float2 a = pass ? tb[r][threadIdx.x] : ta[r][threadIdx.x];      // W[i][j]
-      const float2 bt = pass ? ta[threadIdx.x][r] : tb[threadIdx.x][r];     // W[j][i]
-      const float2 x = f64_to_f32(X[mb + (long long)i * nk + j]);
-      const float dr = (gh[j].x - gh[i].x) + (gl[j].x - gl[i].x);
-      const float di = (gh[j].y - gh[i].y) + (gl[j].y - gl[i].y);
-      const float re = (a.x - bt.x) + (dr * x.x - di * x.y);
-      const float im = (a.y + bt.y) + (dr * x.y + di * x.x);
-      out[mb + (long long)i * nk + j] = make_float2(im * ih, -re * ih);
+  const float* ch = chi + (long long)b * nk;
+  const float* cl = clo + (long long)b * nk;
+  // the tile (i0.., j0..): i <= j wherever it is written
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = i0 + r, j = j0 + threadIdx.x;
+    if (i >= nk || j >= nk) continue;
+    const long long oa = (long long)i * nk + j;
+    const float2 a = make_float2(w[oa].x + w2[oa].x, w[oa].y + w2[oa].y);   // W[i][j]
+    const float2 bt = tb[threadIdx.x][r];                   // W[j][i]
+    const float2 hji = hb[threadIdx.x][r];                  // H'[j][i]
+    const float2 x = f64_to_f32(X[mb + (long long)i * nk + j]);
+    const float dr = (gh[j].x - gh[i].x) + (gl[j].x - gl[i].x);
+    const float di = (gh[j].y - gh[i].y) + (gl[j].y - gl[i].y);
+    const float dc = (ch[i] - ch[j]) + (cl[i] - cl[j]);
+    const float re = (a.x - bt.x) + dc * hji.x + (dr * x.x - di * x.y);
+    const float im = (a.y + bt.y) + dc * hji.y + (dr * x.y + di * x.x);
+    const float2 v = make_float2(im * ih, -re * ih);
+    vt[r][threadIdx.x] = v;
+    if (bi < bj || j >= i) out[mb + (long long)i * nk + j] = v;
+  }
+  __syncthreads();
+  // the mirror tile as the conjugate transpose: dX is Hermitian by construction
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = j0 + r, j = i0 + threadIdx.x;
+    if (i >= nk || j >= nk) continue;
+    if (bi < bj || i > j) {
+      const float2 v = vt[threadIdx.x][r];
+      out[mb + (long long)i * nk + j] = make_float2(v.x, -v.y);
     }
   }
 }
@@ -962,11 +1032,12 @@ __global__ void k_antiherm(int nk, const float2* W, const double2* X, const floa
 // measures the maximum of the state it writes (the next stage state, or the new
 // state after stage 4) per wire into mx[b].
 // grid (blocks per wire, wires).
-__global__ void k_rk4_mixed(long long per, int stage, float dt, double2* X, float2* acc,
-                            double2* xs, const float2* k, unsigned* mx) {
+__global__ void k_rk4_mixed(int nk, int peel, int stage, float dt, double2* X, float2* acc,
+                            double2* xs, const float2* k, unsigned* mx, unsigned* mo) {
   const int b = blockIdx.y;
+  const long long per = (long long)nk * nk;
   const long long o = (long long)b * per;
-  unsigned long long m = 0;
+  unsigned long long m = 0, mof = 0;
   const float f = (stage == 1 || stage == 2) ? 0.5f * dt : dt;
   for (long long i = o + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < o + per;
        i += (long long)gridDim.x * blockDim.x) {
@@ -981,24 +1052,38 @@ __global__ void k_rk4_mixed(long long per, int stage, float dt, double2* X, floa
       }
       const double2 v = make_double2(x.x + f32_to_f64(f * kv.x), x.y + f32_to_f64(f * kv.y));
       xs[i] = v;
-      m = max(m, max(absbits(v.x), absbits(v.y)));
+      const unsigned long long a = max(absbits(v.x), absbits(v.y));
+      m = max(m, a);
+      if (!peel || ((i - o) % (nk + 1)) != 0) mof = max(mof, a);
     } else {
       const float2 a = acc[i];
       const float s = dt / 6.f;
       const double2 v =
           make_double2(x.x + f32_to_f64(s * (a.x + kv.x)), x.y + f32_to_f64(s * (a.y + kv.y)));
       X[i] = v;
-      m = max(m, max(absbits(v.x), absbits(v.y)));
+      const unsigned long long av = max(absbits(v.x), absbits(v.y));
+      m = max(m, av);
+      if (!peel || ((i - o) % (nk + 1)) != 0) mof = max(mof, av);
     }
   }
   {
-    __shared__ unsigned long long red[8];
-    for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __shared__ unsigned long long red[2][8];
+    for (int off = 16; off > 0; off >>= 1) {
+      m = max(m, __shfl_down_sync(0xffffffffu, m, off));
+      mof = max(mof, __shfl_down_sync(0xffffffffu, mof, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = m;
+      red[1][threadIdx.x >> 5] = mof;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, red[w]);
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+        m = max(m, red[0][w]);
+        mof = max(mof, red[1][w]);
+      }
       atomicMax(mx + b, bits_to_fmax(m));
+      atomicMax(mo + b, bits_to_fmax(mof));
     }
   }
 }
@@ -1014,8 +1099,12 @@ __global__ void k_add_int(int n, const int* a, const int* b, int* out) {
 }
 
 static int gemm(Mixed* m, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, int cplx,
-                int nterms, const tc::Term* t, int kskip, const tc::EpiArgs& e, cudaStream_t s) {
+                int nterms, const tc::Term* t, int kskip, const tc::EpiArgs& e, cudaStream_t s,
+                int split = 0, int kb_lo = 0, int kb_hi = 0) {
   tc::GemmDesc d{};
+  d.split = split;
+  d.kb_lo = kb_lo;
+  d.kb_hi = kb_hi;
   d.M = M;
   d.N = N;
   d.K = K;
@@ -1084,18 +1173,27 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   const WireDev& W0 = c->wires[0];
   // state exponent and planes: P and P^T from one read; C and D need only their
   // own layout (C^T = conj C and D^T = conj D for the Hermitian C and D)
+  // eS: full state maximum (sheared exchange operands); eO: maximum over P and
+  // the off-diagonal C, D (commutator operands; the diagonals of C and D are
+  // peeled off and applied exactly in the epilogues)
   if (!state_max_ready) {
     cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-    absmax_into(P, mm, nw, m->mxS(), s);
-    absmax_into(C, mm, nw, m->mxS(), s);
-    absmax_into(D, mm, nw, m->mxS(), s);
+    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
+    const int blocks = (int)std::min<long long>((mm + 255) / 256, 128);
+    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(P, nk, 0, m->mxS(), m->mxO());
+    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(C, nk, 1, m->mxS(), m->mxO());
+    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(D, nk, 1, m->mxS(), m->mxO());
   }
   exponents_from(m, m->mxS(), m->eS(), s);
+  exponents_from(m, m->mxO(), m->eO(), s);
   const double2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eS(), m->planes, M_P, M_PT, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eS(), m->planes, M_C, -1, nw, m->tpart, 0);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eS(), m->planes, M_D, -1, nw, m->tpart, 1);
+  const long long vn = (long long)nw * nk;
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->planes, M_P, M_PT, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->planes, M_C, -1, nw, m->tpart, 0,
+                                         m->cdf);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->planes, M_D, -1, nw, m->tpart, 1,
+                                         m->cdf + 2 * vn);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
   k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
@@ -1128,7 +1226,7 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->planes, M_EH, M_EHT, nw);
   k_hplanes<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
       m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->planes, nw);
-  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eH(), m->esc());
+  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eO(), m->eH(), m->esc());
   // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
   // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
   const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_D, M_EH, 1, 0, -1},
@@ -1137,8 +1235,11 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
   const tc::Term* tl[3] = {tP, tC, tD};
   const int nt[3] = {4, 2, 2};
+  // W and V as two K halves each (partials summed in the anti-Hermitian pass):
+  // wf = [W lo, W hi, V lo, V hi]
   float2* wf = reinterpret_cast<float2*>(c->G);
-  float2* out[3] = {m->kf, wf, wf + tm};
+  float2* out[3] = {m->kf, wf, wf + 2 * tm};
+  const int nkb = (nk + tc::BK - 1) / tc::BK, kh = nkb / 2;
   for (int w = 0; w < 3; ++w) {
     tc::EpiArgs e{};
     e.kind = (w == 0) ? tc::EPI_RHSF : tc::EPI_RAWF;
@@ -1150,17 +1251,30 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
     e.hehf = m->hf;
     e.dgf = m->dgf;
     e.gamf = m->gamf;
+    e.cdf = m->cdf;
     e.nk = nk;
     e.nw = nw;
     e.err = m->err();
     ProfScope ps(c, 0, s);
-    rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, nt[w], tl[w], 0, e, s);
+    // W and V (dC, dD) in split-accumulator mode: their W - W^H is a small
+    // difference of large products near equilibrium
+    if (w == 0) {
+      rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, nt[w], tl[w], 0, e, s);
+    } else {
+      rc = gemm(m, m->mapA, m->mapB64, nk, nk, nk, 1, nt[w], tl[w], 0, e, s, 1, 0, kh);
+      if (!rc) {
+        tc::EpiArgs e2 = e;
+        e2.outf2 = out[w] + tm;
+        rc = gemm(m, m->mapA, m->mapB64, nk, nk, nk, 1, nt[w], tl[w], 0, e2, s, 1, kh, nkb);
+      }
+    }
     if (rc) return rc;
   }
   const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
-  const long long vn = (long long)nw * nk;
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, C, m->dgf, m->dgf + vn, m->kf + tm);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + tm, D, m->dgf + 2 * vn, m->dgf + 3 * vn, m->kf + 2 * tm);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
+                               m->cdf + vn, m->kf + tm);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, m->hf + 2 * tm, D, m->dgf + 2 * vn,
+                               m->dgf + 3 * vn, m->cdf + 2 * vn, m->cdf + 3 * vn, m->kf + 2 * tm);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 
@@ -1249,12 +1363,14 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
     rc = mixed_stage(c, xp, xc, xd, c->ekst, st > 1, s);
     if (rc) return rc;
-    // RK4 update; every stage also measures the maximum of the state it writes
+    // RK4 update; every stage also measures the maxima of the state it writes
     cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
+    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * m->nw, s);
     double2* X[3] = {P, C, D};
     for (int i = 0; i < 3; ++i)
-      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(per, st, (float)dt, X[i], m->accf + i * n,
-                                                  c->xs + i * n, m->kf + i * n, m->mxS());
+      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(m->nk, i > 0, st, (float)dt, X[i],
+                                                  m->accf + i * n, c->xs + i * n,
+                                                  m->kf + i * n, m->mxS(), m->mxO());
   }
   mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
   return mixed_sources(c, P, C, D, src, 1, s);

@@ -182,9 +182,12 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
     return;
   }
   if (e.kind == EPI_RHSF) {
-    // dP[kh=m][ke=n] = (G + (hh[kh] + ee[ke]) P + Heh[ke][kh])/(i hbar) - (gE+gH) P in
-    // FP32 (the peeled diagonal energies add, so no cancellation), from the FP64
-    // stage state P converted on the integer pipe.
+    // dP[kh=m][ke=n] = (G + (hh[kh] + ee[ke]) P + (1 - c[ke] - d[kh]) Heh[ke][kh])
+    //                 / (i hbar) - (gE+gH) P
+    // in FP32 (the peeled diagonal energies add, so no cancellation), from the FP64
+    // stage state P converted on the integer pipe.  G holds the products with the
+    // off-diagonal C', D'; the peeled occupations c, d enter through the
+    // Pauli-blocking factor of the driving term Heh^T - Heh^T diag(c) - (Heh diag(d))^T.
     const int nk = e.nk, nw = e.nw;
     const long long mb = (long long)b * nk * nk, vb = (long long)b * nk, vn = (long long)nw * nk;
     const float ih = (float)(1.0 / 1.0545718176461565e-34);
@@ -192,6 +195,7 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
     const double2* X = e.X + mb + (long long)m * nk;
     const float2 gh = e.dgf[2 * vn + vb + m], gl = e.dgf[3 * vn + vb + m];
     const float gamH = e.gamf[vn + vb + m];
+    const float dh = e.cdf[2 * vn + vb + m], dl = e.cdf[3 * vn + vb + m];
     float2* o = e.outf2 + mb + (long long)m * nk;
 #pragma unroll 4
     for (int j = 0; j < 16; ++j) {
@@ -199,7 +203,9 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
       if (n >= nk) break;
       const float gr = f32_ldexp(re[j], es), gi = f32_ldexp(im[j], es);
       const float2 x = f64_to_f32(X[n]);
-      const float2 h = e.hehf[mb + (long long)n * nk + m];
+      const float2 h0 = e.hehf[mb + (long long)n * nk + m];
+      const float pb = ((1.f - e.cdf[vb + n]) - dh) - (e.cdf[vn + vb + n] + dl);
+      const float2 h = make_float2(pb * h0.x, pb * h0.y);
       const float2 eh = e.dgf[vb + n], el = e.dgf[vn + vb + n];
       const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
       const float ar = gr + (der * x.x - dei * x.y) + h.x;
@@ -270,14 +276,16 @@ __device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m
 // ---------------------------------------------------------------------------
 // the kernel
 
+template <int BNT, bool SPLIT>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
               const GemmDesc d, const EpiArgs e) {
+  constexpr int BTB = BNT * BK * 2;   // B tile bytes per plane
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const int npl = d.complex_mode ? 4 : 2;
-  const int stage_bytes = npl * (A_TILE_BYTES + B_TILE_BYTES);
+  const int stage_bytes = npl * (A_TILE_BYTES + BTB);
   const int nstage = (192 * 1024) / stage_bytes;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + nstage * stage_bytes);
   uint64_t* empty = full + 8;
@@ -287,18 +295,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x & 31;
   const int b = blockIdx.z;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BNT;
   const uint32_t ncols = d.complex_mode ? 512 : 256;
 
   // K range of this tile (the sheared exchange operand is zero outside it)
   int kb_begin = 0, kb_end = (d.K + BK - 1) / BK;
   if (d.kskip) {
     const int nk = d.nk_shear;
-    int dd_lo = n0 / 2, dd_hi = min((n0 + BN) / 2, 2 * nk - 1) - 1;
+    int dd_lo = n0 / 2, dd_hi = min((n0 + BNT) / 2, 2 * nk - 1) - 1;
     int dlo = dd_lo - (nk - 1), dhi = dd_hi - (nk - 1);
     int tlo = max(0, -dhi), thi = min(nk - 1, nk - 1 - dlo);
     kb_begin = tlo / BK;
     kb_end = (thi >= tlo) ? thi / BK + 1 : kb_begin;
+  }
+  if (d.kb_hi > d.kb_lo) {
+    kb_begin = d.kb_lo;
+    kb_end = d.kb_hi;
   }
   const int nkb = kb_end - kb_begin;
   const int n_iters = d.nterms * nkb;
@@ -334,12 +346,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
       for (int p = 0; p < npl; ++p) {
         tma_load_5d(sa + p * A_TILE_BYTES, &ma, &full[s], kb * BK, m0, b, p, T.a_mat);
-        tma_load_5d(sb + p * B_TILE_BYTES, &mb, &full[s], kb * BK, n0, b, p, T.b_mat);
+        tma_load_5d(sb + p * BTB, &mb, &full[s], kb * BK, n0, b, p, T.b_mat);
       }
     }
   } else if (warp == 1 && lane == 0 && n_iters > 0) {
     // ---------------- MMA issuer ----------------
-    const uint32_t id_pos = idesc_f16(BM, BN, 0), id_neg = idesc_f16(BM, BN, 1);
+    const uint32_t id_pos = idesc_f16(BM, BNT, 0), id_neg = idesc_f16(BM, BNT, 1);
     const uint32_t acc_re = tmem, acc_im = tmem + 256;
     bool first = true;
     for (int it = 0; it < n_iters; ++it) {
@@ -354,13 +366,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       for (int k16 = 0; k16 < BK / 16; ++k16) {
         const uint32_t ko = k16 * 32;   // bytes along the 64-byte row
         auto A = [&](int p) { return sw64_desc(sa + p * A_TILE_BYTES + ko); };
-        auto B = [&](int p) { return sw64_desc(sb + p * B_TILE_BYTES + ko); };
+        auto B = [&](int p) { return sw64_desc(sb + p * BTB + ko); };
         const uint32_t acc = first ? 0u : 1u;
         if (!d.complex_mode) {
           const uint32_t id = T.sign < 0 ? id_neg : id_pos;
           umma_f16(acc_re, A(0), B(0), id, acc);
           umma_f16(acc_re, A(0), B(1), id, 1u);
           umma_f16(acc_re, A(1), B(0), id, 1u);
+        } else if (SPLIT) {
+          // accumulators (64 columns each): rr hi*hi, rr hi*lo+lo*hi, ii .., .., ri .., ..,
+          // ir .., ..: every truncating chain is a third to a sixth as long
+          const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
+          const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
+          const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
+          const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
+          const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
+          umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
+          umma_f16(tmem + 1 * BNT, A(0), B(1), irr, acc);
+          umma_f16(tmem + 1 * BNT, A(1), B(0), irr, 1u);
+          umma_f16(tmem + 2 * BNT, A(2), B(2), iii, acc);
+          umma_f16(tmem + 3 * BNT, A(2), B(3), iii, acc);
+          umma_f16(tmem + 3 * BNT, A(3), B(2), iii, 1u);
+          umma_f16(tmem + 4 * BNT, A(0), B(2), iri, acc);
+          umma_f16(tmem + 5 * BNT, A(0), B(3), iri, acc);
+          umma_f16(tmem + 5 * BNT, A(1), B(2), iri, 1u);
+          umma_f16(tmem + 6 * BNT, A(2), B(0), iir, acc);
+          umma_f16(tmem + 7 * BNT, A(2), B(1), iir, acc);
+          umma_f16(tmem + 7 * BNT, A(3), B(0), iir, 1u);
         } else {
           // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
           const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
@@ -395,9 +427,27 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc_fence_after();
     if (ok) {
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-      for (int c = 0; c < BN / 16; ++c) {
+      for (int c = 0; c < BNT / 16; ++c) {
         float re[16], im[16];
-        if (n_iters > 0) {
+        if (SPLIT && n_iters > 0) {
+          float t0[16], t1[16];
+          tmem_ld16(lane_addr + 0 * BNT + c * 16, re);
+          tmem_ld16(lane_addr + 1 * BNT + c * 16, t0);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) re[j] += t0[j];
+          tmem_ld16(lane_addr + 2 * BNT + c * 16, t0);
+          tmem_ld16(lane_addr + 3 * BNT + c * 16, t1);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) re[j] += t0[j] + t1[j];
+          tmem_ld16(lane_addr + 4 * BNT + c * 16, im);
+          tmem_ld16(lane_addr + 5 * BNT + c * 16, t0);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) im[j] += t0[j];
+          tmem_ld16(lane_addr + 6 * BNT + c * 16, t0);
+          tmem_ld16(lane_addr + 7 * BNT + c * 16, t1);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) im[j] += t0[j] + t1[j];
+        } else if (n_iters > 0) {
           tmem_ld16(lane_addr + c * 16, re);
           if (d.complex_mode) tmem_ld16(lane_addr + 256 + c * 16, im);
           else {
@@ -468,8 +518,10 @@ static const int kTcSmem = 192 * 1024 + 1024 + 256;
 int tc_gemm_init() {
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(tc::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kTcSmem) != cudaSuccess)
+    if (cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN_SPLIT, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess)
       return fail(SBE_ERR_CUDA, "tc_gemm: cannot raise the shared-memory limit");
     attr = true;
   }
@@ -481,9 +533,18 @@ int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorM
   const int smem = kTcSmem;
   int rc = tc_gemm_init();
   if (rc) return rc;
-  dim3 grid((d.N + tc::BN - 1) / tc::BN, (d.M + tc::BM - 1) / tc::BM, d.batch);
-  tc::k_tc_gemm<<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
+  if (d.split) {
+    if (!d.complex_mode || d.kskip)
+      return fail(SBE_ERR_ARG, "tc_gemm: split-accumulator mode is complex and unskipped only");
+    dim3 grid((d.N + tc::BN_SPLIT - 1) / tc::BN_SPLIT, (d.M + tc::BM - 1) / tc::BM, d.batch);
+    tc::k_tc_gemm<tc::BN_SPLIT, true><<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
+  } else {
+    dim3 grid((d.N + tc::BN - 1) / tc::BN, (d.M + tc::BM - 1) / tc::BM, d.batch);
+    tc::k_tc_gemm<tc::BN, false><<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
+  }
   return cuda_check(cudaGetLastError(), "tc_gemm launch");
 }
+
+int tc_make_map_split(const TcPlanes& b, CUtensorMap* mb) { return make_map(b, tc::BN_SPLIT, mb); }
 
 }  // namespace sbe

@@ -22,6 +22,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BN = 256;
+constexpr int BN_SPLIT = 64;   // N tile of the split-accumulator mode
 constexpr int BK = 32;
 constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
@@ -77,6 +78,7 @@ struct EpiArgs {
   const float2* hehf;         // Heh in FP32 [ke][kh] per batch
   const float2* dgf;          // peeled diagonals: [4][nw][nk] Hee hi, Hee lo, Hhh hi, Hhh lo
   const float* gamf;          // [2][nw][nk] GamE, GamH
+  const float* cdf;           // [4][nw][nk] hi, lo of Re C_kk, then hi, lo of Re D_kk
   int nw;
 };
 
@@ -88,6 +90,14 @@ struct GemmDesc {
   int batch;
   int kskip;                  // exchange: K range limited by the sheared N tile
   int nk_shear;               // exchange: Nk of the shear
+  // split-accumulator mode (complex only): N tile 64 and eight FP32 accumulators,
+  // one per (real product, hi*hi or hi*lo + lo*hi) pair, summed in the epilogue.
+  // The tensor core's accumulation truncates; splitting the sums shortens each
+  // truncating chain (for products whose result is a small difference of large
+  // sums, e.g. the W - W^H form of dC, dD).
+  int split;
+  // K range override in BK blocks (kb_hi > kb_lo): a split-K partial product
+  int kb_lo, kb_hi;
 };
 
 }  // namespace tc
@@ -99,6 +109,8 @@ struct TcPlanes {
 };
 
 int tc_make_maps(const TcPlanes& a, const TcPlanes& b, CUtensorMap* ma, CUtensorMap* mb);
+// tensor map of a B operand for the split-accumulator mode (64-row box)
+int tc_make_map_split(const TcPlanes& b, CUtensorMap* mb);
 int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorMap& mb,
                    const tc::EpiArgs& e, cudaStream_t s);
 
