@@ -60,9 +60,10 @@ MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta
 FLAGS = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
              LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel err"
-# dram__bytes_read.sum + dram__bytes_write.sum of one 2-term commutator launch,
-# 8 wires x Nk = 512 (ncu), per wire
-TRAFFIC_PER_WIRE = (67.17e6 + 4.10e6) / 8
+# dram__bytes_read.sum + dram__bytes_write.sum of the commutator launches of one RHS
+# evaluation (dP: 184.87 + 1.60 MB; W, V halves: 4 x 33.6 MB read, 0.92 MB written in
+# all), 8 wires x Nk = 512 (ncu), per wire
+TRAFFIC_PER_EVAL_WIRE = (184.87e6 + 1.60e6 + 134.50e6 + 0.92e6) / 8
 
 
 def wire_L(nk, kmax):
@@ -384,28 +385,31 @@ def gpu_arm(args, wl):
 
     peaks, pk_kind = measured_peaks()
     comm_ms, comm_n = prof[0]
-    per_launch_s = comm_ms / max(comm_n, 1) / 1e3
-    # algorithmic work of a1-a3 (dP, dC, dD as 12 complex Nk^3 products, 96 Nk^3 flop per
-    # wire per RHS evaluation) over the 3 commutator launches of an evaluation
-    useful = 32.0 * nk ** 3 * nw
-    # executed: 8 complex products per evaluation (W - W^H form) x 4 real products x 3
-    # hi/lo terms x 2 Nk^3 = 192 Nk^3 per evaluation, 64 Nk^3 per launch
-    executed = 64.0 * nk ** 3 * nw
-    achieved = useful / per_launch_s / 1e12
+    evals = 4 * args.steps                  # RHS evaluations in the timed region
+    per_eval_s = comm_ms / evals / 1e3      # commutator GEMM time of one evaluation
+    # algorithmic work of a1-a3 per RHS evaluation: dP, dC, dD as 12 complex Nk^3
+    # products = 96 Nk^3 flop per wire
+    useful = 96.0 * nk ** 3 * nw
+    # executed: 8 complex products (W - W^H form) x 4 real products x 3 hi/lo terms x
+    # 2 Nk^3 = 192 Nk^3 per wire
+    executed = 192.0 * nk ** 3 * nw
+    achieved = useful / per_eval_s / 1e12
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     roof = {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)", "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_kind": f"{pk_kind} bf16 dense sustained (fp16 dense has the same rate)",
-            "executed_tflops": executed / per_launch_s / 1e12,
-            "executed_frac": executed / per_launch_s / 1e12 / peak,
-            "avg_launch_ms": per_launch_s * 1e3, "launches": comm_n,
-            "traffic": TRAFFIC_PER_WIRE * nw,
-            "traffic_note": "dram read+write bytes of one 2-term commutator launch from an "
-                            "ncu capture of the 8-wire case, scaled by wires",
+            "executed_tflops": executed / per_eval_s / 1e12,
+            "executed_frac": executed / per_eval_s / 1e12 / peak,
+            "ms_per_rhs_eval": per_eval_s * 1e3, "launches": comm_n,
+            "avg_launch_ms": comm_ms / max(comm_n, 1),
+            "traffic": TRAFFIC_PER_EVAL_WIRE * nw,
+            "traffic_note": "DRAM read+write bytes of the commutator launches of one RHS "
+                            "evaluation (ncu, 8-wire case, scaled by wires)",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
-                           "12 complex Nk^3 products) over its 3 commutator launches = 32*Nk^3 "
-                           "per launch; executed 64*Nk^3 per launch (8 complex products per "
-                           "evaluation x 4 real products x 3 hi/lo terms)"}
+                           "12 complex Nk^3 products) over the summed CUDA-event time of the "
+                           "evaluation's commutator launches (dP; W and V as two K halves each "
+                           "in split-accumulator mode); executed 192*Nk^3 (8 complex products "
+                           "x 4 real products x 3 hi/lo terms)"}
     other = {name: {"ms_per_step": prof[c][0] / args.steps, "launches": prof[c][1]}
              for c, name in ((1, "exchange_gemm"), (2, "source_gemm"), (3, "dephasing_fp32"))}
     other["pstd_field_step"] = {"ms_per_step": pstd_ms, "launches": 6}
