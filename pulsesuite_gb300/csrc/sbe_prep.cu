@@ -248,6 +248,10 @@ __global__ void k_occf(const WireDev* wires, const double2* ne, const double2* n
   occf[2 * W.off_vec + W.nk + k] = (float)hypot(nh[W.off_vec + k].x, nh[W.off_vec + k].y);
 }
 
+// One block per (q, species, wire) and up to 512 k; each thread sums four
+// consecutive k, so that the per-p shared-memory loads (the Lorentzian window and
+// the paired occupation weights, read as one float2 broadcast) serve four outputs:
+// the loop was bound by shared-memory loads, not by FMA.
 __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const float* occf,
                                                      const float* dconst, const float* dpre,
                                                      double* De, double* Dh) {
@@ -257,15 +261,12 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
   const int qi = blockIdx.y;
   if (qi > 2 * nk) return;
   const int q = qi - nk;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   extern __shared__ float sh[];
-  float* na = sh;              // |n_a|
-  float* nb = na + nk;         // |n_b|
-  float* Ltab = nb + nk;       // 2nk entries: m - mlo
-  float* Aa = Ltab + 2 * nk;   // per-p weights (a-a)
-  float* Ba = Aa + nk;
-  float* Ab = Ba + nk;         // per-p weights (a-b)
-  float* Bb = Ab + nk;
+  float* na = sh;                                        // |n_a|
+  float* nb = na + nk;                                   // |n_b|
+  float* Ltab = nb + nk;                                 // 2nk entries: m - mlo
+  float2* wa = reinterpret_cast<float2*>(Ltab + 2 * nk); // (Aa, Ba) per p (a-a)
+  float2* wb = wa + nk;                                  // (Ab, Bb) per p (a-b)
   // |n_e|, |n_h| as FP32 (formed once per step by k_occf)
   const float* pa = occf + 2 * W.off_vec + (which == 0 ? 0 : nk);
   const float* pb = occf + 2 * W.off_vec + (which == 0 ? nk : 0);
@@ -291,48 +292,81 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
     int pm = p - q, pp = p + q;
     bool okm = pm >= 0 && pm < nk, okp = pp >= 0 && pp < nk;
     float a_pm = okm ? na[pm] : 0.f, b_pp = okp ? nb[pp] : 0.f;
-    Aa[p] = okm ? a_pm * (1.f - na[p]) : 0.f;
-    Ba[p] = okm ? (1.f - a_pm) * na[p] : 0.f;
-    Ab[p] = okp ? b_pp * (1.f - nb[p]) : 0.f;
-    Bb[p] = okp ? (1.f - b_pp) * nb[p] : 0.f;
+    wa[p] = make_float2(okm ? a_pm * (1.f - na[p]) : 0.f, okm ? (1.f - a_pm) * na[p] : 0.f);
+    wb[p] = make_float2(okp ? b_pp * (1.f - nb[p]) : 0.f, okp ? (1.f - b_pp) * nb[p] : 0.f);
   }
   __syncthreads();
-  if (k >= nk) return;
-  float acc = 0.f;
-  if (k + q >= 0 && k + q < nk) {
-    const float nak = na[k];
+  double* D = (which == 0 ? De : Dh) + W.off_dd;
+  for (int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4; k0 < nk;
+       k0 += gridDim.x * blockDim.x * 4) {
+    float sa[4] = {0.f, 0.f, 0.f, 0.f}, sb[4] = {0.f, 0.f, 0.f, 0.f};
     if (vaa != 0.f) {
-      int plo = max(q + 1, 0), phi = min(q + nk - 1, nk - 1);
-      float sa = 0.f, sb = 0.f;
-      const int base = k + q - mlo;   // Ltab index of m = k - p + q is base - p
+      const int plo = max(q + 1, 0), phi = min(q + nk - 1, nk - 1);
+      // L index of (k, p) is k - p + nk - 1; the window holds k0 .. k0 + 3 at this p
+      float l[4];
+      const int i0 = k0 - plo + nk - 1;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) l[j] = (i0 + j < 2 * nk) ? Ltab[i0 + j] : 0.f;
       for (int p = plo; p <= phi; ++p) {
-        float L = Ltab[base - p];
-        sa = fmaf(L, Aa[p], sa);
-        sb = fmaf(L, Ba[p], sb);
+        const float2 w2 = wa[p];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          sa[j] = fmaf(l[j], w2.x, sa[j]);
+          sb[j] = fmaf(l[j], w2.y, sb[j]);
+        }
+        // next p: index - 1
+        const int in = i0 - (p + 1 - plo);
+#pragma unroll
+        for (int j = 3; j > 0; --j) l[j] = l[j - 1];
+        l[0] = (in >= 0) ? Ltab[in] : 0.f;
       }
-      acc += vaa * ((1.f - nak) * sa + nak * sb);
+    }
+    float acc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float nak = (k0 + j < nk) ? na[k0 + j] : 0.f;
+      acc[j] = vaa * ((1.f - nak) * sa[j] + nak * sb[j]);
+      sa[j] = 0.f;
+      sb[j] = 0.f;
     }
     if (vab != 0.f) {
-      int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
+      const int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
       const int c = -2 * W.dnk - 1 + q;
-      const float fk = (float)(2 * k + c);
-      const float ka = bah * fk, kal = bal * fk;   // exact head product + tail
+      float ka[4], kal[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float fk = (float)(2 * (k0 + j) + c);
+        ka[j] = bah * fk;   // exact head product
+        kal[j] = bal * fk;  // tail
+      }
       const float fq = (float)q;
-      float sa = 0.f, sb = 0.f;
       float fp = (float)(2 * plo + c);   // exact small integers, stepped by 2
       for (int p = plo; p <= phi; ++p, fp += 2.0f) {
-        float s = (ka + bbh * fp) + fmaf(bbl, fp, kal);
-        float u = fq * s;
-        float L;   // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L) : "f"(fmaf(u, u, 1.0f)));
-        sa = fmaf(L, Ab[p], sa);
-        sb = fmaf(L, Bb[p], sb);
+        const float2 w2 = wb[p];
+        const float hb = bbh * fp;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float sv = (ka[j] + hb) + fmaf(bbl, fp, kal[j]);
+          const float u = fq * sv;
+          float L;   // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L) : "f"(fmaf(u, u, 1.0f)));
+          sa[j] = fmaf(L, w2.x, sa[j]);
+          sb[j] = fmaf(L, w2.y, sb[j]);
+        }
       }
-      acc += vab * ((1.f - nak) * sa + nak * sb);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = k0 + j;
+      if (k >= nk) continue;
+      float v = 0.f;
+      if (k + q >= 0 && k + q < nk) {
+        const float nak = na[k];
+        v = acc[j] + vab * ((1.f - nak) * sa[j] + nak * sb[j]);
+      }
+      D[(long long)qi * nk + k] = (double)v;
     }
   }
-  double* D = (which == 0 ? De : Dh) + W.off_dd;
-  D[(long long)qi * nk + k] = (double)acc;
 }
 
 // Constants of k_offdiag_D32 (FP64, once per step): per (wire, species)
@@ -370,7 +404,7 @@ void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaSt
                                                                  c->occf);
     k_deph_consts<<<dim3((c->nk_max + 127) / 128, 2 * c->nw), 128, 0, s>>>(c->d_wires, c->vs,
                                                                           c->dconst, c->dpre);
-    k_offdiag_D32<<<dim3((c->nk_max + 127) / 128, 2 * c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
+    k_offdiag_D32<<<dim3((c->nk_max + 511) / 512, 2 * c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
         c->d_wires, c->occf, c->dconst, c->dpre, c->De, c->Dh);
     return;
   }
