@@ -159,9 +159,6 @@ void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, doub
 void launch_sources_final(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
                           cudaStream_t s);
 void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s);
-void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int transpose,
-                   const int* e, __half* dst, int mat, int nplanes, int real_only,
-                   cudaStream_t s);
 int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
               const double2* dEk, double dt, double2* src, cudaStream_t s);
 void launch_rk4_axpy(SbeCtx* c, int stage, double dt, double2* P, double2* C, double2* D,

@@ -61,8 +61,7 @@ __device__ __forceinline__ void put_hilo(__half* base, long long plane, float v)
 // optionally transposed.  dst layout [mat][plane][batch][rows][K]; planes
 // re_hi, re_lo, im_hi, im_lo (complex) or hi, lo of the real part.
 __global__ void k_planes(const double2* X, long long bstride, int nk, int transpose,
-                         const int* e, __half* dst, int mat, int nplanes, int nbatch,
-                         int real_only) {
+                         const int* e, tc::PlaneSet dst, int mat, int real_only) {
   __shared__ double2 tile[32][33];
   const int b = blockIdx.z;
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
@@ -75,25 +74,23 @@ __global__ void k_planes(const double2* X, long long bstride, int nk, int transp
   }
   __syncthreads();
   const int eb = e[b];
-  const long long plane = (long long)nbatch * nk * nk;
-  __half* base = dst + ((long long)mat * nplanes) * plane + (long long)b * nk * nk;
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);   // next plane
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     int r = r0 + i, c = c0 + threadIdx.x;
     if (r >= nk || c >= nk) continue;
     double2 v = transpose ? tile[threadIdx.x][i] : tile[i][threadIdx.x];
-    long long o = (long long)r * nk + c;
+    __half* base = dst.ptr + tc::plane_elem(dst, mat, 0, b, r, c);
     // exact scaling and one rounding to FP32 (24 bits >= the 22 the planes keep)
-    put_hilo(base + o, plane, f64_to_f32(v.x, eb));
-    if (!real_only) put_hilo(base + 2 * plane + o, plane, f64_to_f32(v.y, eb));
+    put_hilo(base, pstride, f64_to_f32(v.x, eb));
+    if (!real_only) put_hilo(base + 2 * pstride, pstride, f64_to_f32(v.y, eb));
   }
 }
 
 void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int transpose,
-                   const int* e, __half* dst, int mat, int nplanes, int real_only,
+                   const int* e, const tc::PlaneSet& dst, int mat, int real_only,
                    cudaStream_t s) {
   dim3 blk(32, 8), grid((nk + 31) / 32, (nk + 31) / 32, nbatch);
-  k_planes<<<grid, blk, 0, s>>>(X, bstride, nk, transpose, e, dst, mat, nplanes, nbatch,
-                                real_only);
+  k_planes<<<grid, blk, 0, s>>>(X, bstride, nk, transpose, e, dst, mat, real_only);
 }
 
 // Both layouts of a batch of Nk x Nk complex matrices from one read: planes of X
@@ -119,7 +116,7 @@ __device__ __forceinline__ double dvalue(double2 v) { return v.x; }
 __device__ __forceinline__ double dvalue(float2 v) { return f32_to_f64(v.x); }
 
 template <typename T>
-__global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int matN, int matT,
+__global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, int matN, int matT,
                             int nbatch, float2* tpart = nullptr, int which = 0,
                             float* cdf = nullptr) {
   __shared__ T tile[32][33];
@@ -135,9 +132,7 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int m
   }
   __syncthreads();
   const int eb = e[b];
-  const long long plane = (long long)nbatch * nk * nk;
-  __half* bn = dst + (long long)matN * 4 * plane + (long long)b * nk * nk;
-  __half* bt = dst + (long long)(matT < 0 ? 0 : matT) * 4 * plane + (long long)b * nk * nk;
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     for (int pass = 0; pass < (matT < 0 ? 1 : 2); ++pass) {
       // pass 0: row r0 + i of X;  pass 1: row c0 + i of X^T (= column c0 + i of X)
@@ -153,9 +148,9 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, __half* dst, int m
           cdf[((long long)nbatch + b) * nk + r] = f64_to_f32(d - f32_to_f64(hi));
         }
       }
-      __half* base = (pass ? bt : bn) + (long long)r * nk + c;
-      put_hilo(base, plane, v.x);
-      put_hilo(base + 2 * plane, plane, v.y);
+      __half* base = dst.ptr + tc::plane_elem(dst, pass ? matT : matN, 0, b, r, c);
+      put_hilo(base, pstride, v.x);
+      put_hilo(base + 2 * pstride, pstride, v.y);
     }
   }
   if (tpart) {
@@ -222,7 +217,7 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 // Wf (W, V of the W - W^H form, in the G buffer).
 struct Mixed {
   int nk = 0, nw = 0, nr = 0;
-  __half *planes = nullptr, *tpl = nullptr, *spl = nullptr, *epl = nullptr;
+  tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
   float* xsh = nullptr;    // exchange sums in the sheared layout: 3 x Nw x Nk x 4Nk
   int* ints = nullptr;     // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
   unsigned* mx = nullptr;  // [0, nw): Hamiltonian maximum; [nw, 2nw): state; [2nw, 3nw): hbar A/B
@@ -247,7 +242,6 @@ struct Mixed {
   float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
   float2* tpart = nullptr;  // nw x 2 x T x T x 63 partial diagonal sums (T = ceil(nk/32))
   float* cdf = nullptr;     // 4 x nw x nk: hi / lo parts of Re C_kk and Re D_kk (stage state)
-  CUtensorMap mapA, mapB, mapTA, mapSB, mapEB, mapB64;
   int* eS() { return ints; }
   int* eH() { return ints + nw; }
   int* eT() { return ints + 2 * nw; }
@@ -268,10 +262,10 @@ enum { M_P = 0, M_PT, M_C, M_CT, M_D, M_DT, M_EH, M_EHT, M_EE, M_EET, M_HH, M_HH
 void mixed_free(SbeCtx* c) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   if (!m) return;
-  cudaFree(m->planes);
-  cudaFree(m->tpl);
-  cudaFree(m->spl);
-  cudaFree(m->epl);
+  cudaFree(m->pl.ptr);
+  cudaFree(m->tp.ptr);
+  cudaFree(m->sp.ptr);
+  cudaFree(m->ep.ptr);
   cudaFree(m->xsh);
   cudaFree(m->ints);
   cudaFree(m->mx);
@@ -285,16 +279,16 @@ void mixed_free(SbeCtx* c) {
 }
 
 // E^T planes: Y[r][k] = Expikr[k][r] (|E| = 1, exponent 13).
-__global__ void k_eplanes(const WireDev* wires, const double2* expikr, __half* dst, int nw) {
+__global__ void k_eplanes(const WireDev* wires, const double2* expikr, tc::PlaneSet dst, int nw) {
   const WireDev W = wires[blockIdx.z];
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   int r = blockIdx.y;
   if (k >= W.nk || r >= W.nr) return;
   double2 v = expikr[W.off_kr + (long long)k * W.nr + r];
-  const long long plane = (long long)nw * W.nr * W.nk;
-  long long o = (long long)blockIdx.z * W.nr * W.nk + (long long)r * W.nk + k;
-  put_hilo(dst + o, plane, f64_to_f32(v.x, 13));
-  put_hilo(dst + 2 * plane + o, plane, f64_to_f32(v.y, 13));
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
+  __half* base = dst.ptr + tc::plane_elem(dst, 0, 0, blockIdx.z, r, k);
+  put_hilo(base, pstride, f64_to_f32(v.x, 13));
+  put_hilo(base + 2 * pstride, pstride, f64_to_f32(v.y, 13));
 }
 
 __global__ void k_fill_int(int* p, int n, int v) {
@@ -384,10 +378,14 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
                                           4 * (size_t)nw * nk) +
                         sizeof(float) * (2 * tm + 3 * (size_t)nw * nk + 2 * (size_t)nw * nk);
   void* fblock = nullptr;
-  bool ok = cudaMalloc(&m->planes, sizeof(__half) * 14 * 4 * nw * mm) == cudaSuccess &&
-            cudaMalloc(&m->tpl, sizeof(__half) * 3 * 2 * nw * mm) == cudaSuccess &&
-            cudaMalloc(&m->spl, sizeof(__half) * 3 * 2 * nw * 4 * mm) == cudaSuccess &&
-            cudaMalloc(&m->epl, sizeof(__half) * 4 * nw * (size_t)m->nr * nk) == cudaSuccess &&
+  m->pl = tc::make_planeset(nullptr, 14, 4, nw, nk, nk);
+  m->tp = tc::make_planeset(nullptr, 3, 2, nw, nk, nk);
+  m->sp = tc::make_planeset(nullptr, 3, 2, nw, 4 * nk, nk);
+  m->ep = tc::make_planeset(nullptr, 1, 4, nw, m->nr, nk);
+  bool ok = cudaMalloc(&m->pl.ptr, tc::planeset_bytes(m->pl)) == cudaSuccess &&
+            cudaMalloc(&m->tp.ptr, tc::planeset_bytes(m->tp)) == cudaSuccess &&
+            cudaMalloc(&m->sp.ptr, tc::planeset_bytes(m->sp)) == cudaSuccess &&
+            cudaMalloc(&m->ep.ptr, tc::planeset_bytes(m->ep)) == cudaSuccess &&
             cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 4 * mm) == cudaSuccess &&
             cudaMalloc(&m->ints, sizeof(int) * 9 * nw) == cudaSuccess &&
             cudaMalloc(&m->mx, sizeof(unsigned) * 4 * nw) == cudaSuccess &&
@@ -410,20 +408,10 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   m->dgH = m->dgE + (size_t)nw * nk;
   cudaMemsetAsync(m->ints, 0, sizeof(int) * 9 * nw, s);
   cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 4 * nw, s);
-  TcPlanes pl{m->planes, 14, 4, nw, nk, nk};
-  TcPlanes tp{m->tpl, 3, 2, nw, nk, nk};
-  TcPlanes sp{m->spl, 3, 2, nw, 4 * nk, nk};
-  TcPlanes ep{m->epl, 1, 4, nw, m->nr, nk};
-  int rc = tc_make_maps(pl, pl, &m->mapA, &m->mapB);
-  if (!rc) rc = tc_make_map_split(pl, &m->mapB64);
-  if (!rc) rc = tc_make_maps(tp, sp, &m->mapTA, &m->mapSB);
-  CUtensorMap dummy;
-  if (!rc) rc = tc_make_maps(tp, ep, &dummy, &m->mapEB);
-  if (rc) {
-    c->mixed = m;
-    mixed_free(c);
-    return rc;
-  }
+  // the padding of every plane set stays zero: producers write only inside
+  cudaMemsetAsync(m->pl.ptr, 0, tc::planeset_bytes(m->pl), s);
+  cudaMemsetAsync(m->tp.ptr, 0, tc::planeset_bytes(m->tp), s);
+  cudaMemsetAsync(m->ep.ptr, 0, tc::planeset_bytes(m->ep), s);
   // constant FP32 tables and per-step FP32 scratch
   const int T = (nk + 31) / 32;
   const size_t cbytes = sizeof(float) * (4 * tm + 2 * (size_t)nw * nk + 2 * (size_t)nw * nk +
@@ -451,8 +439,8 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   unsigned long long* mx64 = reinterpret_cast<unsigned long long*>(
       (reinterpret_cast<uintptr_t>(m->sP + nw) + 7) & ~uintptr_t(7));
   // sheared planes: zero once; stages write only the in-band part
-  cudaMemsetAsync(m->spl, 0, sizeof(__half) * 3 * 2 * nw * 4 * mm, s);
-  k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(c->d_wires, c->expikr, m->epl, nw);
+  cudaMemsetAsync(m->sp.ptr, 0, tc::planeset_bytes(m->sp), s);
+  k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(c->d_wires, c->expikr, m->ep, nw);
   k_fill_int<<<(nw + 127) / 128, 128, 0, s>>>(m->eE(), nw, 13);
   cudaMemsetAsync(mx64, 0, sizeof(unsigned long long) * nw, s);
   k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->EP, (long long)mm, mx64);
@@ -502,7 +490,7 @@ static void absmax_into(const double2* X, long long per, int nw, unsigned* mx, c
 // Toeplitz exchange planes T_n[t][t'] = vs_n(|t - t'|) (t != t'), real; and the
 // FP32 copy of vs for the direct terms.
 __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const int* e,
-                                  __half* dst, int nw, float* vsf) {
+                                  tc::PlaneSet dst, int nw, float* vsf) {
   const int b = blockIdx.z / 3, n = blockIdx.z % 3;
   const WireDev W = wires[b];
   const int nk = W.nk;
@@ -513,8 +501,8 @@ __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const 
   const double vd = vs[3 * W.off_vec + n * nk + d];
   if (t == 0) vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(vd);
   const float v = (d == 0) ? 0.f : f64_to_f32(vd, e[b]);
-  const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
-  put_hilo(dst + (long long)n * 2 * plane + (long long)b * mm + (long long)t * nk + tp, plane, v);
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
+  put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, t, tp), pstride, v);
 }
 
 __global__ void k_vs_max(const WireDev* wires, const double* vs, unsigned* mx) {
@@ -782,7 +770,7 @@ __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH
 // (row stride 32 double2: diagonal reads are free of bank conflicts).
 // blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire.
 __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* X1,
-                              const double2* X2, const int* e, __half* dst) {
+                              const double2* X2, const int* e, tc::PlaneSet dst) {
   __shared__ double2 tile[63][32];
   const int n = blockIdx.z / nw, b = blockIdx.z % nw;
   const double2* X = (n == 0 ? X0 : n == 1 ? X1 : X2) + (long long)b * nk * nk;
@@ -798,8 +786,7 @@ __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* 
   }
   __syncthreads();
   const int eb = e[b];
-  const long long rows = 4ll * nk, plane = (long long)nw * rows * nk;
-  __half* base = dst + (long long)n * 2 * plane + (long long)b * rows * nk;
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
   const int tp = t0 + tx;
   if (tp >= nk) return;
   for (int ddl = threadIdx.y; ddl < 32; ddl += blockDim.y) {
@@ -808,8 +795,9 @@ __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* 
     const int r = rbase + tx + ddl;
     if (r < 0 || r >= nk) continue;   // out of band: stays zero
     const double2 v = tile[tx + ddl][tx];
-    put_hilo(base + (long long)(2 * dd) * nk + tp, plane, f64_to_f32(v.x, eb));
-    put_hilo(base + (long long)(2 * dd + 1) * nk + tp, plane, f64_to_f32(v.y, eb));
+    put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, 2 * dd, tp), pstride, f64_to_f32(v.x, eb));
+    put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, 2 * dd + 1, tp), pstride,
+             f64_to_f32(v.y, eb));
   }
 }
 
@@ -939,21 +927,22 @@ __global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* 
 // Planes of Hee', Hhh' (slots M_EE, M_HH) and of Hee' + i hbar B, Hhh' + i hbar A
 // (slots M_EEX, M_HHX) from the FP32 values.
 __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA, const float* hB,
-                          int nk, const int* e, __half* dst, int nw) {
+                          int nk, const int* e, tc::PlaneSet dst, int nw) {
   const int b = blockIdx.z;
   const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
   if (c >= nk || r >= nk) return;
-  const long long mm = (long long)nk * nk, plane = (long long)nw * mm;
+  const long long mm = (long long)nk * nk;
   const long long o = (long long)b * mm + (long long)r * nk + c;
+  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
   const int eb = e[b];
   const float2 a = hee[o], h = hhh[o];
   const float bb = hB[o], aa = hA[o];
   const float v[4][2] = {{a.x, a.y}, {h.x, h.y}, {a.x, a.y + bb}, {h.x, h.y + aa}};
   const int slot[4] = {M_EE, M_HH, M_EEX, M_HHX};
   for (int i = 0; i < 4; ++i) {
-    __half* base = dst + (long long)slot[i] * 4 * plane + o;
-    put_hilo(base, plane, f32_ldexp(v[i][0], eb));
-    put_hilo(base + 2 * plane, plane, f32_ldexp(v[i][1], eb));
+    __half* base = dst.ptr + tc::plane_elem(dst, slot[i], 0, b, r, c);
+    put_hilo(base, pstride, f32_ldexp(v[i][0], eb));
+    put_hilo(base + 2 * pstride, pstride, f32_ldexp(v[i][1], eb));
   }
 }
 
@@ -1023,6 +1012,50 @@ __global__ void k_antiherm(int nk, const float2* W, const float2* W2, const floa
       const float2 v = vt[threadIdx.x][r];
       out[mb + (long long)i * nk + j] = make_float2(v.x, -v.y);
     }
+  }
+}
+
+// dP of a stage from the FP32 commutator sums G (the engine's scaled products with
+// the off-diagonal C', D'), following dpdt (SBEs.py:1942-1965):
+//   dP[kh][ke] = (G + (1 - c[ke] - d[kh]) Heh[ke][kh] + (hh[kh] + ee[ke]) P) / (i hbar)
+//                - (GamE[ke] + GamH[kh]) P
+// in FP32 from the FP64 stage state P (converted on the integer pipe).  The peeled
+// occupations c, d enter through the Pauli-blocking factor of the driving term and
+// the peeled energy diagonals ee, hh as hi + lo FP32 parts.  32 x 32 tiles; Heh^T
+// goes through shared memory so that every global access runs along rows.
+__global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, const double2* X,
+                        const float2* dgf, const float* gamf, const float* cdf, float2* out) {
+  __shared__ float2 ht[32][33];
+  const int b = blockIdx.z;
+  const int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
+  const long long mb = (long long)b * nk * nk, vb = (long long)b * nk, vn = (long long)nw * nk;
+  const int tx = threadIdx.x;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int n = n0 + r, m = m0 + tx;
+    ht[r][tx] = (n < nk && m < nk) ? hehf[mb + (long long)n * nk + m] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int n = n0 + tx;
+  if (n >= nk) return;
+  const float ih = (float)(1.0 / kHbar);
+  const float2 eh = dgf[vb + n], el = dgf[vn + vb + n];
+  const float gamE = gamf[vb + n];
+  const float chi = cdf[vb + n], clo = cdf[vn + vb + n];
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int m = m0 + r;
+    if (m >= nk) break;
+    const long long o = mb + (long long)m * nk + n;
+    const float2 h0 = ht[tx][r];   // Heh[ke = n][kh = m]
+    const float pb = ((1.f - chi) - cdf[2 * vn + vb + m]) - (clo + cdf[3 * vn + vb + m]);
+    const float2 g = G[o];
+    const float ax = g.x + pb * h0.x, ay = g.y + pb * h0.y;
+    const float2 x = f64_to_f32(X[o]);
+    const float2 gh = dgf[2 * vn + vb + m], gl = dgf[3 * vn + vb + m];
+    const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
+    const float ar = ax + (der * x.x - dei * x.y);
+    const float ai = ay + (der * x.y + dei * x.x);
+    const float gam = gamE + gamf[vn + vb + m];
+    out[o] = make_float2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
   }
 }
 
@@ -1098,13 +1131,15 @@ __global__ void k_add_int(int n, const int* a, const int* b, int* out) {
   if (i < n) out[i] = a[i] + b[i];
 }
 
-static int gemm(Mixed* m, const CUtensorMap& A, const CUtensorMap& B, int M, int N, int K, int cplx,
-                int nterms, const tc::Term* t, int kskip, const tc::EpiArgs& e, cudaStream_t s,
-                int split = 0, int kb_lo = 0, int kb_hi = 0) {
-  tc::GemmDesc d{};
+static tc::GemmJob job(Mixed* m, const tc::PlaneSet& A, const tc::PlaneSet& B, int M, int N,
+                       int K, int cplx, int nterms, const tc::Term* t, int kskip,
+                       const tc::EpiArgs& e, int split = 0, int ksplit = 1) {
+  tc::GemmJob j{};
+  tc::GemmDesc& d = j.d;
+  d.A = A;
+  d.B = B;
   d.split = split;
-  d.kb_lo = kb_lo;
-  d.kb_hi = kb_hi;
+  d.ksplit = ksplit;
   d.M = M;
   d.N = N;
   d.K = K;
@@ -1114,7 +1149,8 @@ static int gemm(Mixed* m, const CUtensorMap& A, const CUtensorMap& B, int M, int
   d.batch = m->nw;
   d.kskip = kskip;
   d.nk_shear = m->nk;
-  return tc_gemm_launch(d, A, B, e, s);
+  j.e = e;
+  return j;
 }
 
 static void exponents_from(Mixed* m, const unsigned* mx, int* e, cudaStream_t s) {
@@ -1131,7 +1167,7 @@ static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_
   k_vs_max<<<nw, 256, 0, s>>>(c->d_wires, c->vs, m->mxH());
   exponents_from(m, m->mxH(), m->eT(), s);
   k_toeplitz_planes<<<dim3((nk + 127) / 128, nk, 3 * nw), 128, 0, s>>>(c->d_wires, c->vs, m->eT(),
-                                                                       m->tpl, nw, m->vsf);
+                                                                       m->tp, nw, m->vsf);
   k_gamma_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->iq, c->xeh,
                                                          m->gtab, nw);
   k_gamma_f<<<dim3((nk + 7) / 8, nw), 256, sizeof(float) * 2 * nk, s>>>(
@@ -1189,10 +1225,10 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   const double2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   const long long vn = (long long)nw * nk;
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->planes, M_P, M_PT, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->planes, M_C, -1, nw, m->tpart, 0,
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw, m->tpart, 0,
                                          m->cdf);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->planes, M_D, -1, nw, m->tpart, 1,
+  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw, m->tpart, 1,
                                          m->cdf + 2 * vn);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
@@ -1203,7 +1239,9 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   if (have_x) {
     k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
     k_shear_tiles<<<dim3((nk + 31) / 32, (2 * nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
-        nk, nw, P, C, D, m->eS(), m->spl);
+        nk, nw, P, C, D, m->eS(), m->sp);
+    // the three exchange products (eh, ee, hh) as one persistent launch
+    tc::GemmJob jobs[3];
     for (int n = 0; n < 3; ++n) {
       tc::Term t{n, n, 0, 0, 1};
       tc::EpiArgs e{};
@@ -1212,10 +1250,11 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
       e.out_bstride = 4 * mm;
       e.escale = m->esx();
       e.err = m->err();
-      ProfScope ps(c, 1, s);
-      rc = gemm(m, m->mapTA, m->mapSB, nk, 4 * nk, nk, 0, 1, &t, 1, e, s);
-      if (rc) return rc;
+      jobs[n] = job(m, m->tp, m->sp, nk, 4 * nk, nk, 0, 1, &t, 1, e);
     }
+    ProfScope ps(c, 1, s);
+    rc = tc_gemm_launch(jobs, 3, s);
+    if (rc) return rc;
   }
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
   k_h_build<<<dim3((nk + 511) / 512, nk, nw), 128, 0, s>>>(
@@ -1223,9 +1262,9 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
       m->dgf, m->mxH());
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
   k_exponents2<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH());
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->planes, M_EH, M_EHT, nw);
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->pl, M_EH, M_EHT, nw);
   k_hplanes<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
-      m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->planes, nw);
+      m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->pl, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eO(), m->eH(), m->esc());
   // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
   // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
@@ -1238,39 +1277,35 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   // W and V as two K halves each (partials summed in the anti-Hermitian pass):
   // wf = [W lo, W hi, V lo, V hi]
   float2* wf = reinterpret_cast<float2*>(c->G);
-  float2* out[3] = {m->kf, wf, wf + 2 * tm};
-  const int nkb = (nk + tc::BK - 1) / tc::BK, kh = nkb / 2;
+  float2* gp = wf + 4 * tm;   // dP commutator sums (the buffer holds 12 tm float2)
+  float2* out[3] = {gp, wf, wf + 2 * tm};
+  // dP (one launch), then W and V in split-accumulator mode as two K halves each
+  // (one launch; their W - W^H is a small difference of large products near
+  // equilibrium)
+  tc::GemmJob jobs[3];
   for (int w = 0; w < 3; ++w) {
     tc::EpiArgs e{};
-    e.kind = (w == 0) ? tc::EPI_RHSF : tc::EPI_RAWF;
-    e.which = w;
+    e.kind = tc::EPI_RAWF;
     e.outf2 = out[w];
     e.out_bstride = mm;
+    e.ks_stride = tm;
     e.escale = m->esc();
-    e.X = st[w];
-    e.hehf = m->hf;
-    e.dgf = m->dgf;
-    e.gamf = m->gamf;
-    e.cdf = m->cdf;
-    e.nk = nk;
-    e.nw = nw;
     e.err = m->err();
+    jobs[w] = (w == 0) ? job(m, m->pl, m->pl, nk, nk, nk, 1, nt[w], tl[w], 0, e)
+                       : job(m, m->pl, m->pl, nk, nk, nk, 1, nt[w], tl[w], 0, e, 1, 2);
+  }
+  {
     ProfScope ps(c, 0, s);
-    // W and V (dC, dD) in split-accumulator mode: their W - W^H is a small
-    // difference of large products near equilibrium
-    if (w == 0) {
-      rc = gemm(m, m->mapA, m->mapB, nk, nk, nk, 1, nt[w], tl[w], 0, e, s);
-    } else {
-      rc = gemm(m, m->mapA, m->mapB64, nk, nk, nk, 1, nt[w], tl[w], 0, e, s, 1, 0, kh);
-      if (!rc) {
-        tc::EpiArgs e2 = e;
-        e2.outf2 = out[w] + tm;
-        rc = gemm(m, m->mapA, m->mapB64, nk, nk, nk, 1, nt[w], tl[w], 0, e2, s, 1, kh, nkb);
-      }
-    }
+    rc = tc_gemm_launch(jobs, 1, s);
+    if (rc) return rc;
+  }
+  {
+    ProfScope ps(c, 0, s);
+    rc = tc_gemm_launch(jobs + 1, 2, s);
     if (rc) return rc;
   }
   const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
+  k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp, m->hf, st[0], m->dgf, m->gamf, m->cdf, m->kf);
   k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
                                m->cdf + vn, m->kf + tm);
   k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, m->hf + 2 * tm, D, m->dgf + 2 * vn,
@@ -1296,9 +1331,10 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
   const double2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   for (int i = 0; i < 3; ++i)
-    k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->planes, 2 * i, -1, nw);
+    k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->pl, 2 * i, -1, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
   float2* gf = reinterpret_cast<float2*>(c->G);
+  tc::GemmJob jobs[3];
   for (int i = 0; i < 3; ++i) {
     tc::Term t{2 * i, 0, i == 2 ? 1 : 0, 0, 1};
     tc::EpiArgs e{};
@@ -1307,8 +1343,11 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     e.out_bstride = (long long)nk * m->nr;
     e.escale = m->ess();
     e.err = m->err();
+    jobs[i] = job(m, m->pl, m->ep, nk, m->nr, nk, 1, 1, &t, 0, e);
+  }
+  {
     ProfScope ps(c, 2, s);
-    int rc = gemm(m, m->mapA, m->mapEB, nk, m->nr, nk, 1, 1, &t, 0, e, s);
+    int rc = tc_gemm_launch(jobs, 3, s);
     if (rc) return rc;
   }
   k_src_reduce_f<<<dim3((m->nr + 127) / 128, nw), 128, 0, s>>>(c->d_wires, m->ekrf, gf, c->tot_kr,
@@ -1430,14 +1469,15 @@ extern "C" int sbe_tc_selftest(int nk, int nbatch, const double* A, const double
   cudaStream_t s = as_stream(stream);
   const int npl = complex_mode ? 4 : 2;
   const long long mm = (long long)nk * nk;
-  __half* planes = nullptr;
+  tc::PlaneSet ps = tc::make_planeset(nullptr, 2, npl, nbatch, nk, nk);
   int* ints = nullptr;
   unsigned* mx = nullptr;
-  size_t pbytes = sizeof(__half) * 2 * npl * nbatch * mm;
-  if (cudaMallocAsync(&planes, pbytes, s) != cudaSuccess ||
+  const size_t pbytes = tc::planeset_bytes(ps);
+  if (cudaMallocAsync(&ps.ptr, pbytes, s) != cudaSuccess ||
       cudaMallocAsync(&ints, sizeof(int) * (3 * nbatch + 1), s) != cudaSuccess ||
       cudaMallocAsync(&mx, sizeof(unsigned) * nbatch, s) != cudaSuccess)
     return fail(SBE_ERR_OOM, "sbe_tc_selftest: scratch");
+  cudaMemsetAsync(ps.ptr, 0, pbytes, s);
   int* eA = ints;
   int* eB = ints + nbatch;
   int* es = ints + 2 * nbatch;
@@ -1450,36 +1490,29 @@ extern "C" int sbe_tc_selftest(int nk, int nbatch, const double* A, const double
   // op(A)[m][k]: transposed for T/H; op(B)[k][n] as B-operand rows n: Y[n][k]
   const int tA = (opA == 1 || opA == 3), cA = (opA == 2 || opA == 3);
   const int tB = !(opB == 1 || opB == 3), cB = (opB == 2 || opB == 3);
-  launch_planes(a2, mm, nk, nbatch, tA, eA, planes, 0, npl, !complex_mode, s);
-  launch_planes(b2, mm, nk, nbatch, tB, eB, planes, 1, npl, !complex_mode, s);
-  TcPlanes pl;
-  pl.ptr = planes;
-  pl.nmat = 2;
-  pl.nplanes = npl;
-  pl.batch = nbatch;
-  pl.rows = nk;
-  pl.K = nk;
-  CUtensorMap ma, mb;
-  int rc = tc_make_maps(pl, pl, &ma, &mb);
-  if (rc) return rc;
+  launch_planes(a2, mm, nk, nbatch, tA, eA, ps, 0, !complex_mode, s);
+  launch_planes(b2, mm, nk, nbatch, tB, eB, ps, 1, !complex_mode, s);
+  int rc = SBE_OK;
   tc::GemmDesc d{};
   d.M = d.N = d.K = nk;
   d.complex_mode = complex_mode ? 1 : 0;
   d.nterms = 1;
   d.t[0] = tc::Term{0, 1, cA, cB, 1};
   d.batch = nbatch;
+  d.A = ps;
+  d.B = ps;
   tc::EpiArgs e{};
   e.kind = tc::EPI_RAW;
   e.out = (double2*)out;
   e.out_bstride = mm;
   e.escale = es;
   e.err = err;
-  rc = tc_gemm_launch(d, ma, mb, e, s);
+  rc = tc_gemm_launch(d, e, s);
   if (rc) return rc;
   int herr = 0;
   cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
   rc = cuda_check(cudaStreamSynchronize(s), "sbe_tc_selftest");
-  cudaFreeAsync(planes, s);
+  cudaFreeAsync(ps.ptr, s);
   cudaFreeAsync(ints, s);
   cudaFreeAsync(mx, s);
   if (rc) return rc;

@@ -1,6 +1,4 @@
-// tcgen05 / TMA / TMEM split-precision GEMM engine (see tc_gemm.cuh).
-#include <cudaTypedefs.h>
-
+// tcgen05 / bulk-copy / TMEM split-precision GEMM engine (see tc_gemm.cuh).
 #include "sbe_ctx.cuh"
 #include "fp_bits.cuh"
 #include "tc_gemm.cuh"
@@ -22,6 +20,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
@@ -54,13 +56,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
   }
 }
 
-__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int c0, int c1, int c2, int c3, int c4) {
+// contiguous global -> shared copy completing on an mbarrier (16-byte aligned,
+// size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
   asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4),
-      "r"(smem_u32(bar))
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -135,197 +138,166 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N, int negA) {
 // ---------------------------------------------------------------------------
 // epilogues
 
-__device__ __forceinline__ double2 cmuld(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// One 16-column chunk of accumulators of row m (re[], im[]: FP32).
-__device__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b, int m, int n0,
-                               const float* re, const float* im) {
-  if (m >= d.M) return;
-  const double sc = ldexp(1.0, -e.escale[b]);
+// Epilogue of one 32-column chunk (columns n0 .. n0 + 31) of the warp's 32 rows
+// mrow0 + lane.  re[j], im[j] arrive in the TMEM orientation (lane = row, j =
+// column); the terms indexed along rows are added there, then the chunk is
+// transposed through the warp's shared-memory scratch (32 x 33 float2) so that
+// every global access of the column pass runs along n (lane = column).
+__device__ __forceinline__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b,
+                                               int mrow0, int n0, long long ooff, float* re,
+                                               float* im, float2* scr) {
+  const int lane = threadIdx.x & 31;
+  const int es = -e.escale[b];
   if (e.kind == EPI_F32) {
-    float* o = e.outf + (long long)b * e.out_bstride + (long long)m * d.N + n0;
-    const float scf = (float)sc;
-    if (n0 + 16 <= d.N) {
+    // real mode: each lane stores its row's 128 contiguous bytes directly
+    const int m = mrow0 + lane;
+    if (m >= d.M) return;
+    float* o = e.outf + ooff + (long long)b * e.out_bstride + (long long)m * d.N + n0;
+    if (n0 + 32 <= d.N) {
       float4* o4 = reinterpret_cast<float4*>(o);
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-        o4[j] = make_float4(re[4 * j] * scf, re[4 * j + 1] * scf, re[4 * j + 2] * scf,
-                            re[4 * j + 3] * scf);
+      for (int j = 0; j < 8; ++j)
+        o4[j] = make_float4(f32_ldexp(re[4 * j], es), f32_ldexp(re[4 * j + 1], es),
+                            f32_ldexp(re[4 * j + 2], es), f32_ldexp(re[4 * j + 3], es));
     } else {
-      for (int j = 0; j < 16 && n0 + j < d.N; ++j) o[j] = re[j] * scf;
+      for (int j = 0; j < 32 && n0 + j < d.N; ++j) o[j] = f32_ldexp(re[j], es);
     }
     return;
   }
-  if (e.kind == EPI_RAW) {
-    // exact widening and power-of-two scaling on the integer pipe
-    double2* o = e.out + (long long)b * e.out_bstride + (long long)m * d.N;
-    const int es = -e.escale[b];
+  // ---- row pass
+  if (e.kind != EPI_RAW) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      int n = n0 + j;
-      if (n < d.N)
-        o[n] = make_double2(f32_to_f64_scaled(re[j], es),
-                            d.complex_mode ? f32_to_f64_scaled(im[j], es) : 0.0);
+    for (int j = 0; j < 32; ++j) {
+      re[j] = f32_ldexp(re[j], es);
+      im[j] = f32_ldexp(im[j], es);
     }
-    return;
   }
-  if (e.kind == EPI_RAWF) {
-    float2* o = e.outf2 + (long long)b * e.out_bstride + (long long)m * d.N;
-    const int es = -e.escale[b];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      int n = n0 + j;
-      if (n < d.N) o[n] = make_float2(f32_ldexp(re[j], es), f32_ldexp(im[j], es));
-    }
-    return;
-  }
-  if (e.kind == EPI_RHSF) {
-    // dP[kh=m][ke=n] = (G + (hh[kh] + ee[ke]) P + (1 - c[ke] - d[kh]) Heh[ke][kh])
-    //                 / (i hbar) - (gE+gH) P
-    // in FP32 (the peeled diagonal energies add, so no cancellation), from the FP64
-    // stage state P converted on the integer pipe.  G holds the products with the
-    // off-diagonal C', D'; the peeled occupations c, d enter through the
-    // Pauli-blocking factor of the driving term Heh^T - Heh^T diag(c) - (Heh diag(d))^T.
-    const int nk = e.nk, nw = e.nw;
-    const long long mb = (long long)b * nk * nk, vb = (long long)b * nk, vn = (long long)nw * nk;
-    const float ih = (float)(1.0 / 1.0545718176461565e-34);
-    const int es = -e.escale[b];
-    const double2* X = e.X + mb + (long long)m * nk;
-    const float2 gh = e.dgf[2 * vn + vb + m], gl = e.dgf[3 * vn + vb + m];
-    const float gamH = e.gamf[vn + vb + m];
-    const float dh = e.cdf[2 * vn + vb + m], dl = e.cdf[3 * vn + vb + m];
-    float2* o = e.outf2 + mb + (long long)m * nk;
-#pragma unroll 4
-    for (int j = 0; j < 16; ++j) {
-      const int n = n0 + j;
-      if (n >= nk) break;
-      const float gr = f32_ldexp(re[j], es), gi = f32_ldexp(im[j], es);
-      const float2 x = f64_to_f32(X[n]);
-      const float2 h0 = e.hehf[mb + (long long)n * nk + m];
-      const float pb = ((1.f - e.cdf[vb + n]) - dh) - (e.cdf[vn + vb + n] + dl);
-      const float2 h = make_float2(pb * h0.x, pb * h0.y);
-      const float2 eh = e.dgf[vb + n], el = e.dgf[vn + vb + n];
-      const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
-      const float ar = gr + (der * x.x - dei * x.y) + h.x;
-      const float ai = gi + (der * x.y + dei * x.x) + h.y;
-      const float gam = e.gamf[vb + n] + gamH;
-      o[n] = make_float2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
-    }
-    return;
-  }
-  if (e.kind == EPI_RHS) {
-    // RHS of the state X: out = G/(i hbar) * sc + diagonal (peeled) terms, FP64.
-    const int nk = e.nk;
-    const long long mb = (long long)b * nk * nk;
-    const double ih = 1.0 / 1.0545718176461565e-34;
-    const double2* X = e.X + mb;
-    const double2* gE = e.dgE + (long long)b * nk;
-    const double2* gH = e.dgH + (long long)b * nk;
-    double2* o = e.out + mb + (long long)m * nk;
-#pragma unroll 4
-    for (int j = 0; j < 16; ++j) {
-      int n = n0 + j;
-      if (n >= nk) break;
-      double gr = re[j] * sc, gi = im[j] * sc;        // G = accumulated products (J)
-      double2 x = X[(long long)m * nk + n];
-      double2 v;
-      if (e.which == 0) {
-        // dP[kh=m][ke=n]: (G + (hh[kh] + ee[ke]) P + Heh[ke][kh])/(i hbar) - (gE+gH) P
-        double2 h = e.Heh[mb + (long long)n * nk + m];
-        double2 de = make_double2(gH[m].x + gE[n].x, gH[m].y + gE[n].y);
-        double2 dx = cmuld(de, x);
-        double ar = gr + dx.x + h.x, ai = gi + dx.y + h.y;
-        double gam = e.gamE[(long long)b * nk + n] + e.gamH[(long long)b * nk + m];
-        v = make_double2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
+  for (int j = 0; j < 32; ++j) scr[j * 33 + lane] = make_float2(re[j], im[j]);
+  __syncwarp();
+  // ---- column pass
+  const int n = n0 + lane;
+  const int rmax = min(32, d.M - mrow0);
+  if (n < d.N) {
+    const long long base = ooff + (long long)b * e.out_bstride + (long long)mrow0 * d.N + n;
+#pragma unroll 8
+    for (int r = 0; r < rmax; ++r) {
+      const float2 v = scr[lane * 33 + r];
+      const long long o = base + (long long)r * d.N;
+      if (e.kind == EPI_RAWF) {
+        e.outf2[o] = v;
       } else {
-        const double2* g = (e.which == 1) ? gE : gH;
-        double2 de = make_double2(g[n].x - g[m].x, g[n].y - g[m].y);   // (e[k2] - e[k1]) X
-        double2 dx = cmuld(de, x);
-        double ar = gr + dx.x, ai = gi + dx.y;
-        v = make_double2(ai * ih, -ar * ih);
-      }
-      o[n] = v;
-    }
-    return;
-  }
-  if (e.kind == EPI_EXCH) {
-    // exchange GEMM output: column n = 2*dd + c (dd = d + nk - 1, c = re/im) of
-    // row t; H[t][t+d] gets the exchange sum X.  Real mode: only re[] used.
-    const int nk = e.nk;
-    double2* H = e.out + (long long)b * e.out_bstride;
-#pragma unroll
-    for (int j = 0; j < 16; j += 2) {
-      int n = n0 + j;
-      int dd = n >> 1;
-      int dshift = dd - (nk - 1);
-      int k2 = m + dshift;
-      if (dd >= 2 * nk - 1 || k2 < 0 || k2 >= nk) continue;
-      double xr = re[j] * sc, xi = re[j + 1] * sc;
-      long long o = (long long)m * nk + k2;
-      if (e.which == 0) {
-        H[o] = make_double2(H[o].x + xr, H[o].y + xi);
-      } else if (e.lf || dshift == 0) {
-        H[o] = make_double2(H[o].x - xr, H[o].y - xi);
+        // EPI_RAW: exact widening and power-of-two scaling on the integer pipe
+        e.out[o] = make_double2(f32_to_f64_scaled(v.x, es),
+                                d.complex_mode ? f32_to_f64_scaled(v.y, es) : 0.0);
       }
     }
   }
+  __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
 // the kernel
 
+// One output tile of the launch's tile list.
+struct TileInfo {
+  int job, b, m0, n0, ks, kb_begin, nkb, n_iters;
+};
+
+template <int BNT>
+__device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) {
+  TileInfo ti;
+  int j = 0;
+  while (j + 1 < L.njobs && t >= L.tile_base[j + 1]) ++j;
+  const GemmDesc& d = L.job[j].d;
+  long long r = t - L.tile_base[j];
+  const int tn = (d.N + BNT - 1) / BNT, tm = (d.M + BM - 1) / BM;
+  ti.job = j;
+  ti.n0 = (int)(r % tn) * BNT;
+  r /= tn;
+  ti.m0 = (int)(r % tm) * BM;
+  r /= tm;
+  ti.b = (int)(r % d.batch);
+  ti.ks = (int)(r / d.batch);
+  // K blocks of this part
+  const int nkb_all = (d.K + BK - 1) / BK, ksplit = d.ksplit > 1 ? d.ksplit : 1;
+  int kb_begin = ti.ks * nkb_all / ksplit, kb_end = (ti.ks + 1) * nkb_all / ksplit;
+  if (d.kskip) {
+    // the sheared exchange operand is zero outside the band of this N tile
+    const int nk = d.nk_shear;
+    const int dd_lo = ti.n0 / 2, dd_hi = min((ti.n0 + BNT) / 2, 2 * nk - 1) - 1;
+    const int dlo = dd_lo - (nk - 1), dhi = dd_hi - (nk - 1);
+    const int tlo = max(0, -dhi), thi = min(nk - 1, nk - 1 - dlo);
+    kb_begin = max(kb_begin, tlo / BK);
+    kb_end = (thi >= tlo) ? min(kb_end, thi / BK + 1) : kb_begin;
+  }
+  ti.kb_begin = kb_begin;
+  ti.nkb = max(0, kb_end - kb_begin);
+  ti.n_iters = d.nterms * ti.nkb;
+  return ti;
+}
+
+constexpr int SCR_BYTES = 4 * 32 * 33 * 8;   // epilogue transpose scratch, 4 warps
+constexpr int STAGE_AREA = 192 * 1024;
+
 template <int BNT, bool SPLIT>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
-              const GemmDesc d, const EpiArgs e) {
+    k_tc_gemm(const __grid_constant__ GemmLaunch L) {
   constexpr int BTB = BNT * BK * 2;   // B tile bytes per plane
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  const int npl = d.complex_mode ? 4 : 2;
+  const bool cplx = L.job[0].d.complex_mode != 0;
+  const int npl = cplx ? 4 : 2;
   const int stage_bytes = npl * (A_TILE_BYTES + BTB);
-  const int nstage = (192 * 1024) / stage_bytes;
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + nstage * stage_bytes);
+  const int nstage = STAGE_AREA / stage_bytes;
+  // accumulator columns of one tile; two tiles in flight when they fit twice
+  const int tile_cols = SPLIT ? 8 * BNT : (cplx ? 2 * BNT : BNT);
+  const int nbuf = tile_cols <= 256 ? 2 : 1;
+  float2* scr_all = reinterpret_cast<float2*>(smem + STAGE_AREA);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGE_AREA + SCR_BYTES);
   uint64_t* empty = full + 8;
-  uint64_t* accb = empty + 8;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* tfull = empty + 8;
+  uint64_t* tempty = tfull + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  int* err = L.job[0].e.err;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x & 31;
-  const int b = blockIdx.z;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BNT;
-  const uint32_t ncols = d.complex_mode ? 512 : 256;
-
-  // K range of this tile (the sheared exchange operand is zero outside it)
-  int kb_begin = 0, kb_end = (d.K + BK - 1) / BK;
-  if (d.kskip) {
-    const int nk = d.nk_shear;
-    int dd_lo = n0 / 2, dd_hi = min((n0 + BNT) / 2, 2 * nk - 1) - 1;
-    int dlo = dd_lo - (nk - 1), dhi = dd_hi - (nk - 1);
-    int tlo = max(0, -dhi), thi = min(nk - 1, nk - 1 - dlo);
-    kb_begin = tlo / BK;
-    kb_end = (thi >= tlo) ? thi / BK + 1 : kb_begin;
-  }
-  if (d.kb_hi > d.kb_lo) {
-    kb_begin = d.kb_lo;
-    kb_end = d.kb_hi;
-  }
-  const int nkb = kb_end - kb_begin;
-  const int n_iters = d.nterms * nkb;
+  const long long ntiles = L.tile_base[L.njobs];
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < nstage; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accb, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 4);   // one arrival per epilogue warp
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    tmem_alloc(tmem_slot, ncols);
+    tmem_alloc(tmem_slot, 512);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -333,132 +305,209 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0 && n_iters > 0) {
-    // ---------------- TMA producer ----------------
-    for (int it = 0; it < n_iters; ++it) {
-      const int s = it % nstage;
-      const uint32_t ph = (uint32_t)((it / nstage) & 1);
-      if (!mbar_wait(&empty[s], ph ^ 1u, e.err, abort_flag)) break;
-      const Term T = d.t[it / nkb];
-      const int kb = kb_begin + it % nkb;
-      uint8_t* sa = smem + s * stage_bytes;
-      uint8_t* sb = sa + npl * A_TILE_BYTES;
-      mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
-      for (int p = 0; p < npl; ++p) {
-        tma_load_5d(sa + p * A_TILE_BYTES, &ma, &full[s], kb * BK, m0, b, p, T.a_mat);
-        tma_load_5d(sb + p * BTB, &mb, &full[s], kb * BK, n0, b, p, T.b_mat);
+  if (warp == 0 && lane == 0) {
+    // ---------------- bulk-copy producer ----------------
+    long long g = 0;   // stage-ring position (runs on across tiles)
+    bool ok = true;
+    for (long long t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+      const TileInfo ti = tile_info<BNT>(L, t);
+      const GemmDesc& d = L.job[ti.job].d;
+      for (int it = 0; it < ti.n_iters; ++it, ++g) {
+        const int s = (int)(g % nstage);
+        const uint32_t ph = (uint32_t)((g / nstage) & 1);
+        if (!mbar_wait(&empty[s], ph ^ 1u, err, abort_flag)) {
+          ok = false;
+          break;
+        }
+        const Term T = d.t[it / ti.nkb];
+        const int kb = ti.kb_begin + it % ti.nkb;
+        uint8_t* sa = smem + s * stage_bytes;
+        uint8_t* sb = sa + npl * A_TILE_BYTES;
+        mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+        const long long ta = ((long long)kb * d.A.rows_pad + ti.m0) * BK;   // tile start in a slab
+        const long long tb = ((long long)kb * d.B.rows_pad + ti.n0) * BK;
+        for (int p = 0; p < npl; ++p) {
+          const __half* ga = d.A.ptr +
+                             ((long long)(T.a_mat * d.A.nplanes + p) * d.A.batch + ti.b) *
+                                 plane_slab(d.A) + ta;
+          const __half* gb = d.B.ptr +
+                             ((long long)(T.b_mat * d.B.nplanes + p) * d.B.batch + ti.b) *
+                                 plane_slab(d.B) + tb;
+          bulk_load(sa + p * A_TILE_BYTES, ga, A_TILE_BYTES, &full[s]);
+          bulk_load(sb + p * BTB, gb, BTB, &full[s]);
+        }
       }
     }
-  } else if (warp == 1 && lane == 0 && n_iters > 0) {
+    // no copy may still be landing in shared memory when the CTA exits: wait
+    // (bounded) for the last stages issued
+    for (long long q = max(0ll, g - nstage); q < g; ++q) {
+      volatile int never = 0;
+      mbar_wait(&full[q % nstage], (uint32_t)((q / nstage) & 1), err, &never);
+    }
+  } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
     const uint32_t id_pos = idesc_f16(BM, BNT, 0), id_neg = idesc_f16(BM, BNT, 1);
-    const uint32_t acc_re = tmem, acc_im = tmem + 256;
-    bool first = true;
-    for (int it = 0; it < n_iters; ++it) {
-      const int s = it % nstage;
-      const uint32_t ph = (uint32_t)((it / nstage) & 1);
-      if (!mbar_wait(&full[s], ph, e.err, abort_flag)) break;
+    long long g = 0;
+    int lt = 0;
+    bool ok = true;
+    for (long long t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++lt) {
+      const TileInfo ti = tile_info<BNT>(L, t);
+      const GemmDesc& d = L.job[ti.job].d;
+      const int buf = lt % nbuf, use = lt / nbuf;
+      if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) break;
       tc_fence_after();
-      const Term T = d.t[it / nkb];
-      const uint32_t sa = smem_u32(smem + s * stage_bytes);
-      const uint32_t sb = sa + npl * A_TILE_BYTES;
-#pragma unroll
-      for (int k16 = 0; k16 < BK / 16; ++k16) {
-        const uint32_t ko = k16 * 32;   // bytes along the 64-byte row
-        auto A = [&](int p) { return sw64_desc(sa + p * A_TILE_BYTES + ko); };
-        auto B = [&](int p) { return sw64_desc(sb + p * BTB + ko); };
-        const uint32_t acc = first ? 0u : 1u;
-        if (!d.complex_mode) {
-          const uint32_t id = T.sign < 0 ? id_neg : id_pos;
-          umma_f16(acc_re, A(0), B(0), id, acc);
-          umma_f16(acc_re, A(0), B(1), id, 1u);
-          umma_f16(acc_re, A(1), B(0), id, 1u);
-        } else if (SPLIT) {
-          // accumulators (64 columns each): rr hi*hi, rr hi*lo+lo*hi, ii .., .., ri .., ..,
-          // ir .., ..: every truncating chain is a third to a sixth as long
-          const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
-          const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
-          const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
-          const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
-          const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
-          umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
-          umma_f16(tmem + 1 * BNT, A(0), B(1), irr, acc);
-          umma_f16(tmem + 1 * BNT, A(1), B(0), irr, 1u);
-          umma_f16(tmem + 2 * BNT, A(2), B(2), iii, acc);
-          umma_f16(tmem + 3 * BNT, A(2), B(3), iii, acc);
-          umma_f16(tmem + 3 * BNT, A(3), B(2), iii, 1u);
-          umma_f16(tmem + 4 * BNT, A(0), B(2), iri, acc);
-          umma_f16(tmem + 5 * BNT, A(0), B(3), iri, acc);
-          umma_f16(tmem + 5 * BNT, A(1), B(2), iri, 1u);
-          umma_f16(tmem + 6 * BNT, A(2), B(0), iir, acc);
-          umma_f16(tmem + 7 * BNT, A(2), B(1), iir, acc);
-          umma_f16(tmem + 7 * BNT, A(3), B(0), iir, 1u);
-        } else {
-          // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
-          const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
-          const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
-          const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
-          const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
-          const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
-          umma_f16(acc_re, A(0), B(0), irr, acc);
-          umma_f16(acc_re, A(0), B(1), irr, 1u);
-          umma_f16(acc_re, A(1), B(0), irr, 1u);
-          umma_f16(acc_re, A(2), B(2), iii, 1u);
-          umma_f16(acc_re, A(2), B(3), iii, 1u);
-          umma_f16(acc_re, A(3), B(2), iii, 1u);
-          umma_f16(acc_im, A(0), B(2), iri, acc);
-          umma_f16(acc_im, A(0), B(3), iri, 1u);
-          umma_f16(acc_im, A(1), B(2), iri, 1u);
-          umma_f16(acc_im, A(2), B(0), iir, 1u);
-          umma_f16(acc_im, A(2), B(1), iir, 1u);
-          umma_f16(acc_im, A(3), B(0), iir, 1u);
+      const uint32_t acc_re = tmem + buf * 256, acc_im = tmem + 256;
+      bool first = true;
+      for (int it = 0; it < ti.n_iters; ++it, ++g) {
+        const int s = (int)(g % nstage);
+        const uint32_t ph = (uint32_t)((g / nstage) & 1);
+        if (!mbar_wait(&full[s], ph, err, abort_flag)) {
+          ok = false;
+          break;
         }
-        first = false;
+        tc_fence_after();
+        const Term T = d.t[it / ti.nkb];
+        const uint32_t sa = smem_u32(smem + s * stage_bytes);
+        const uint32_t sb = sa + npl * A_TILE_BYTES;
+#pragma unroll
+        for (int k16 = 0; k16 < BK / 16; ++k16) {
+          const uint32_t ko = k16 * 32;   // bytes along the 64-byte row
+          auto A = [&](int p) { return sw64_desc(sa + p * A_TILE_BYTES + ko); };
+          auto B = [&](int p) { return sw64_desc(sb + p * BTB + ko); };
+          const uint32_t acc = first ? 0u : 1u;
+          if (!cplx) {
+            const uint32_t id = T.sign < 0 ? id_neg : id_pos;
+            umma_f16(acc_re, A(0), B(0), id, acc);
+            umma_f16(acc_re, A(0), B(1), id, 1u);
+            umma_f16(acc_re, A(1), B(0), id, 1u);
+          } else {
+            // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
+            const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
+            const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
+            const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
+            const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
+            const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
+            if (SPLIT) {
+              // accumulators (BNT columns each): rr hi*hi, rr hi*lo+lo*hi, ii .., ..,
+              // ri .., .., ir .., ..: every truncating chain is a third to a sixth as long
+              umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
+              umma_f16(tmem + 1 * BNT, A(0), B(1), irr, acc);
+              umma_f16(tmem + 1 * BNT, A(1), B(0), irr, 1u);
+              umma_f16(tmem + 2 * BNT, A(2), B(2), iii, acc);
+              umma_f16(tmem + 3 * BNT, A(2), B(3), iii, acc);
+              umma_f16(tmem + 3 * BNT, A(3), B(2), iii, 1u);
+              umma_f16(tmem + 4 * BNT, A(0), B(2), iri, acc);
+              umma_f16(tmem + 5 * BNT, A(0), B(3), iri, acc);
+              umma_f16(tmem + 5 * BNT, A(1), B(2), iri, 1u);
+              umma_f16(tmem + 6 * BNT, A(2), B(0), iir, acc);
+              umma_f16(tmem + 7 * BNT, A(2), B(1), iir, acc);
+              umma_f16(tmem + 7 * BNT, A(3), B(0), iir, 1u);
+            } else {
+              umma_f16(acc_re, A(0), B(0), irr, acc);
+              umma_f16(acc_re, A(0), B(1), irr, 1u);
+              umma_f16(acc_re, A(1), B(0), irr, 1u);
+              umma_f16(acc_re, A(2), B(2), iii, 1u);
+              umma_f16(acc_re, A(2), B(3), iii, 1u);
+              umma_f16(acc_re, A(3), B(2), iii, 1u);
+              umma_f16(acc_im, A(0), B(2), iri, acc);
+              umma_f16(acc_im, A(0), B(3), iri, 1u);
+              umma_f16(acc_im, A(1), B(2), iri, 1u);
+              umma_f16(acc_im, A(2), B(0), iir, 1u);
+              umma_f16(acc_im, A(2), B(1), iir, 1u);
+              umma_f16(acc_im, A(3), B(0), iir, 1u);
+            }
+          }
+          first = false;
+        }
+        umma_commit(&empty[s]);
       }
-      umma_commit(&empty[s]);
+      // accumulators of this tile complete (a tile without K blocks leaves tensor
+      // memory untouched and its epilogue stores zeros)
+      if (ti.n_iters > 0)
+        umma_commit(&tfull[buf]);
+      else
+        mbar_arrive(&tfull[buf]);
     }
-    umma_commit(accb);
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
     const int q = warp & 3;                 // TMEM lane quarter of this warp
-    const int m = m0 + 32 * q + lane;
-    bool ok = true;
-    if (n_iters > 0) ok = mbar_wait(accb, 0, e.err, abort_flag);
-    tc_fence_after();
-    if (ok) {
-      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-      for (int c = 0; c < BNT / 16; ++c) {
-        float re[16], im[16];
-        if (SPLIT && n_iters > 0) {
-          float t0[16], t1[16];
-          tmem_ld16(lane_addr + 0 * BNT + c * 16, re);
-          tmem_ld16(lane_addr + 1 * BNT + c * 16, t0);
+    float2* scr = scr_all + (warp - 2) * (32 * 33);
+    int lt = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const TileInfo ti = tile_info<BNT>(L, t);
+      const GemmDesc& d = L.job[ti.job].d;
+      const EpiArgs& e = L.job[ti.job].e;
+      const int buf = lt % nbuf, use = lt / nbuf;
+      const int mrow0 = ti.m0 + 32 * q;
+      const long long ooff = (long long)ti.ks * e.ks_stride;
+      if (!mbar_wait(&tfull[buf], (uint32_t)(use & 1), err, abort_flag)) break;
+      tc_fence_after();
+      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
+      const bool have = ti.n_iters > 0;
+      if (SPLIT) {
+        // read and sum all eight accumulators, release tensor memory, then store
+        float re[BNT / 32][32], im[BNT / 32][32];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) re[j] += t0[j];
-          tmem_ld16(lane_addr + 2 * BNT + c * 16, t0);
-          tmem_ld16(lane_addr + 3 * BNT + c * 16, t1);
+        for (int c = 0; c < BNT / 32; ++c) {
+          if (have) {
+            // re = (rr hh + rr hl/lh) + (ii hh + ii hl/lh), im likewise from ri, ir
 #pragma unroll
-          for (int j = 0; j < 16; ++j) re[j] += t0[j] + t1[j];
-          tmem_ld16(lane_addr + 4 * BNT + c * 16, im);
-          tmem_ld16(lane_addr + 5 * BNT + c * 16, t0);
+            for (int h = 0; h < 2; ++h) {
+              const uint32_t a0 = lane_addr + c * 32 + h * 16;
+              float* r = re[c] + h * 16;
+              float* i = im[c] + h * 16;
+              float t0[16], t1[16];
+              tmem_ld16(a0 + 0 * BNT, r);
+              tmem_ld16(a0 + 1 * BNT, t0);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) im[j] += t0[j];
-          tmem_ld16(lane_addr + 6 * BNT + c * 16, t0);
-          tmem_ld16(lane_addr + 7 * BNT + c * 16, t1);
+              for (int j = 0; j < 16; ++j) r[j] += t0[j];
+              tmem_ld16(a0 + 2 * BNT, t0);
+              tmem_ld16(a0 + 3 * BNT, t1);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) im[j] += t0[j] + t1[j];
-        } else if (n_iters > 0) {
-          tmem_ld16(lane_addr + c * 16, re);
-          if (d.complex_mode) tmem_ld16(lane_addr + 256 + c * 16, im);
-          else {
+              for (int j = 0; j < 16; ++j) r[j] += t0[j] + t1[j];
+              tmem_ld16(a0 + 4 * BNT, i);
+              tmem_ld16(a0 + 5 * BNT, t0);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) im[j] = 0.f;
+              for (int j = 0; j < 16; ++j) i[j] += t0[j];
+              tmem_ld16(a0 + 6 * BNT, t0);
+              tmem_ld16(a0 + 7 * BNT, t1);
+#pragma unroll
+              for (int j = 0; j < 16; ++j) i[j] += t0[j] + t1[j];
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) re[c][j] = im[c][j] = 0.f;
           }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
         }
-        epilogue_chunk(d, e, b, m, n0 + c * 16, re, im);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[buf]);
+#pragma unroll
+        for (int c = 0; c < BNT / 32; ++c)
+          epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re[c], im[c], scr);
+      } else {
+        for (int c = 0; c < BNT / 32; ++c) {
+          float re[32], im[32];
+          if (have) {
+            tmem_ld32(lane_addr + c * 32, re);
+            if (cplx) {
+              tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 32, im);
+            } else {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) im[j] = 0.f;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) re[j] = im[j] = 0.f;
+          }
+          if (c == BNT / 32 - 1) {
+            // last read of this tile's accumulators
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
+          }
+          epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re, im, scr);
+        }
       }
     }
   }
@@ -466,7 +515,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, ncols);
+    tmem_dealloc(tmem, 512);
   }
 }
 
@@ -475,45 +524,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // ---------------------------------------------------------------------------
 // host side
 
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
-
-static int make_map(const TcPlanes& t, int box_rows, CUtensorMap* m) {
-  auto fn = encode_fn();
-  if (!fn) return fail(SBE_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
-  if (t.K % 8 != 0) return fail(SBE_ERR_UNSUPPORTED, "plane K must be a multiple of 8");
-  cuuint64_t dims[5] = {(cuuint64_t)t.K, (cuuint64_t)t.rows, (cuuint64_t)t.batch,
-                        (cuuint64_t)t.nplanes, (cuuint64_t)t.nmat};
-  cuuint64_t row = (cuuint64_t)t.K * 2;
-  cuuint64_t strides[4] = {row, row * t.rows, row * t.rows * t.batch,
-                           row * t.rows * t.batch * t.nplanes};
-  cuuint32_t box[5] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows, 1, 1, 1};
-  cuuint32_t es[5] = {1, 1, 1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, (void*)t.ptr, dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS)
-    return fail(SBE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-  return SBE_OK;
-}
-
-int tc_make_maps(const TcPlanes& a, const TcPlanes& b, CUtensorMap* ma, CUtensorMap* mb) {
-  int rc = make_map(a, tc::BM, ma);
-  if (rc) return rc;
-  return make_map(b, tc::BN, mb);
-}
-
-static const int kTcSmem = 192 * 1024 + 1024 + 256;
+static const int kTcSmem = 1024 + tc::STAGE_AREA + tc::SCR_BYTES + 256;
 
 int tc_gemm_init() {
   static bool attr = false;
@@ -528,23 +539,68 @@ int tc_gemm_init() {
   return SBE_OK;
 }
 
-int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorMap& mb,
-                   const tc::EpiArgs& e, cudaStream_t s) {
-  const int smem = kTcSmem;
+static int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+// every bulk copy stays inside the plane sets: tiles of the launch grid lie in
+// the padded rows, K-blocks in the padded K, terms in the allocated matrices
+static bool job_ok(const tc::GemmDesc& d) {
+  const int npl = d.complex_mode ? 4 : 2;
+  bool ok = d.A.ptr && d.B.ptr && d.M > 0 && d.N > 0 && d.K > 0 && d.M <= d.A.rows &&
+            d.N <= d.B.rows && d.K <= d.A.K && d.K <= d.B.K && d.batch > 0 &&
+            d.batch <= d.A.batch && d.batch <= d.B.batch && d.A.nplanes >= npl &&
+            d.B.nplanes >= npl && d.nterms >= 1 && d.nterms <= tc::MAX_TERMS &&
+            d.A.rows_pad % 256 == 0 && d.B.rows_pad % 256 == 0 && d.A.K_pad % tc::BK == 0 &&
+            d.B.K_pad % tc::BK == 0 && d.ksplit >= 0 && d.ksplit <= 64;
+  for (int i = 0; ok && i < d.nterms; ++i)
+    ok = d.t[i].a_mat >= 0 && d.t[i].a_mat < d.A.nmat && d.t[i].b_mat >= 0 &&
+         d.t[i].b_mat < d.B.nmat;
+  return ok;
+}
+
+int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   int rc = tc_gemm_init();
   if (rc) return rc;
-  if (d.split) {
-    if (!d.complex_mode || d.kskip)
+  if (njobs < 1 || njobs > tc::MAX_JOBS) return fail(SBE_ERR_ARG, "tc_gemm: 1 to 4 jobs per launch");
+  tc::GemmLaunch L{};
+  L.njobs = njobs;
+  const bool split = jobs[0].d.split != 0;
+  const int cplx = jobs[0].d.complex_mode;
+  const int bnt = split ? tc::BN_SPLIT : tc::BN;
+  long long nt = 0;
+  for (int j = 0; j < njobs; ++j) {
+    const tc::GemmDesc& d = jobs[j].d;
+    if (!job_ok(d)) return fail(SBE_ERR_ARG, "tc_gemm: operand plane sets do not cover the launch");
+    if ((d.split != 0) != split || d.complex_mode != cplx)
+      return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode");
+    if (split && (!d.complex_mode || d.kskip))
       return fail(SBE_ERR_ARG, "tc_gemm: split-accumulator mode is complex and unskipped only");
-    dim3 grid((d.N + tc::BN_SPLIT - 1) / tc::BN_SPLIT, (d.M + tc::BM - 1) / tc::BM, d.batch);
-    tc::k_tc_gemm<tc::BN_SPLIT, true><<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
-  } else {
-    dim3 grid((d.N + tc::BN - 1) / tc::BN, (d.M + tc::BM - 1) / tc::BM, d.batch);
-    tc::k_tc_gemm<tc::BN, false><<<grid, tc::NUM_THREADS, smem, s>>>(ma, mb, d, e);
+    if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
+    L.job[j] = jobs[j];
+    L.tile_base[j] = nt;
+    nt += (long long)((d.N + bnt - 1) / bnt) * ((d.M + tc::BM - 1) / tc::BM) * d.batch *
+          (d.ksplit > 1 ? d.ksplit : 1);
   }
+  L.tile_base[njobs] = nt;
+  const int grid = (int)std::min<long long>(nt, num_sms());
+  if (split)
+    tc::k_tc_gemm<tc::BN_SPLIT, true><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
+  else
+    tc::k_tc_gemm<tc::BN, false><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
   return cuda_check(cudaGetLastError(), "tc_gemm launch");
 }
 
-int tc_make_map_split(const TcPlanes& b, CUtensorMap* mb) { return make_map(b, tc::BN_SPLIT, mb); }
+int tc_gemm_launch(const tc::GemmDesc& d, const tc::EpiArgs& e, cudaStream_t s) {
+  tc::GemmJob j{d, e};
+  return tc_gemm_launch(&j, 1, s);
+}
 
 }  // namespace sbe

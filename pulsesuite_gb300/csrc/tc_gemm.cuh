@@ -8,12 +8,19 @@
 // textbook formula (conjugation and sign by the MMA's operand-negate bit), all
 // accumulated in FP32 in tensor memory.
 //
-// Tiles: BM = 128 rows, BN = 256 columns, BK = 32 (64-byte rows, TMA
-// SWIZZLE_64B, K-major on both operands).  Warp roles: warp 0 issues TMA loads,
-// warp 1 owns tensor memory and issues tcgen05.mma from one thread, warps 2-5
-// read the accumulators (tcgen05.ld) and run the epilogue.
+// Tiles: BM = 128 rows, BN = 256 (or 64) columns, BK = 32 (64-byte rows,
+// K-major on both operands, 64-byte swizzle).  The planes live in global memory
+// in the tile layout of PlaneSet: every operand tile is one contiguous chunk,
+// moved to shared memory with a single cp.async.bulk.
+//
+// The kernel is persistent: one CTA per SM walks a list of output tiles that
+// may span several GEMMs of the same shape class (jobs) and K parts of each.
+// Warp roles: warp 0 issues the bulk copies through a ring of stages that runs
+// on across tiles, warp 1 owns tensor memory and issues tcgen05.mma from one
+// thread, warps 2-5 read the accumulators (tcgen05.ld) and run the epilogue of
+// tile i while the copies (and, when the accumulators fit twice in tensor
+// memory, the MMAs) of tile i + 1 proceed.
 #pragma once
-#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cstdint>
 
@@ -28,8 +35,44 @@ constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
 constexpr int NUM_THREADS = 192;
 constexpr int MAX_TERMS = 4;
+constexpr int MAX_JOBS = 4;
 // bounded waits: an iteration limit after which the kernel flags an error
 constexpr long long WAIT_LIMIT = 1ll << 28;
+
+// Operand planes in the tile layout.  Slab (mat, plane, batch) holds a rows x K
+// FP16 matrix as K-blocks of 32 columns; K-block kb stores all rows_pad rows of
+// 64 bytes contiguously, swizzled in 512-byte atoms (16-byte chunk c of row r at
+// chunk c ^ ((r >> 1) & 3)), which is the shared-memory image the tensor core's
+// 64-byte-swizzle K-major descriptor reads.  A tile of R rows starting at a row
+// multiple of 64 in K-block kb is then the contiguous R x 64 bytes at
+// (kb * rows_pad + row0) * 32 elements.  rows_pad is a multiple of 256, K_pad of
+// 32; the padding is zero.
+struct PlaneSet {
+  __half* ptr;
+  int nmat, nplanes, batch, rows, K, rows_pad, K_pad;
+};
+
+__host__ __device__ inline long long plane_slab(const PlaneSet& p) {
+  return (long long)p.rows_pad * p.K_pad;
+}
+// element offset of (r, k) within a slab
+__host__ __device__ inline long long tile_off(int rows_pad, int r, int k) {
+  const long long byte = ((long long)(k >> 5) * rows_pad + r) * 64 + (k & 31) * 2;
+  return (byte ^ (((byte >> 7) & 3) << 4)) >> 1;
+}
+// element offset of (r, k) of slab (mat, plane, batch)
+__host__ __device__ inline long long plane_elem(const PlaneSet& p, int mat, int plane, int b,
+                                                int r, int k) {
+  return ((long long)(mat * p.nplanes + plane) * p.batch + b) * plane_slab(p) +
+         tile_off(p.rows_pad, r, k);
+}
+inline PlaneSet make_planeset(__half* ptr, int nmat, int nplanes, int batch, int rows, int K) {
+  PlaneSet p{ptr, nmat, nplanes, batch, rows, K, (rows + 255) / 256 * 256, (K + 31) / 32 * 32};
+  return p;
+}
+inline size_t planeset_bytes(const PlaneSet& p) {
+  return sizeof(__half) * (size_t)p.nmat * p.nplanes * p.batch * plane_slab(p);
+}
 
 // One term of a GEMM: accumulate sign * op(A[a_mat]) * op(B[b_mat]).
 struct Term {
@@ -39,47 +82,20 @@ struct Term {
 };
 
 enum Epi : int {
-  EPI_RAW = 0,      // out[b][m][n] = (re, im) * 2^-(ea[b]+eb[b])      (self-test)
-  EPI_RHS = 1,      // stage RHS of P, C or D (see sbe_tc.cu)
-  EPI_EXCH = 2,     // exchange Hamiltonian assembly (see sbe_tc.cu)
-  EPI_F32 = 3,      // outf[b][m][n] = acc * 2^-escale[b] as FP32 (real mode)
-  EPI_RHSF = 4,     // stage RHS of P in FP32 (see sbe_tc.cu)
-  EPI_RAWF = 5,     // outf2[b][m][n] = (re, im) * 2^-escale[b] as FP32 complex
+  EPI_RAW = 0,      // out[b][m][n] = (re, im) * 2^-escale[b] as FP64 (self-test)
+  EPI_F32 = 1,      // outf[b][m][n] = acc * 2^-escale[b] as FP32 (real mode)
+  EPI_RAWF = 2,     // outf2[b][m][n] = (re, im) * 2^-escale[b] as FP32 complex
 };
 
 struct EpiArgs {
   int kind;
-  int which;                  // RHS: 0 dP, 1 dC, 2 dD;  EXCH: 0 eh, 1 ee, 2 hh
-  double2* out;               // FP64 complex output (per batch stride out_bstride)
-  float* outf;                // FP32 output (EPI_F32, per batch stride out_bstride)
+  double2* out;               // EPI_RAW output (per batch stride out_bstride)
+  float* outf;                // EPI_F32 output (per batch stride out_bstride)
+  float2* outf2;              // EPI_RAWF output (per batch stride out_bstride)
   long long out_bstride;
+  long long ks_stride;        // output offset (elements) between the K parts of a split-K GEMM
   const int* escale;          // per batch exponent of the product scale (e_A + e_B)
-  // RHS epilogue inputs (per batch strides = nk*nk or nk)
-  const double2* X;           // the state matrix whose diagonal terms are added (P, C or D)
-  const double2* Heh;         // FP64 Heh (dP only)
-  const double2* dgE;         // diagonal of Hee (per batch, nk), peeled off the GEMM operand
-  const double2* dgH;         // diagonal of Hhh
-  const double* gamE;
-  const double* gamH;
-  // exchange epilogue
-  const double2* Ek;          // per batch 3 x nr wire-k fields
-  const double* Eenergy;      // per batch Ee or Eh
-  const double2* tr;          // per batch traces [2][2nk]
-  const double* vs;           // per batch screened V by d [3][nk]
-  double2* H3;                // per batch Heh, Hee, Hhh (stride nk*nk, 3 consecutive blocks)
-  int nk, nr;
-  int lf, excitons, optics;
-  double gap, ehint, dcv;
-  const int* yw;              // per batch yw(w)
-  const int* zsign;           // per batch (-1)^w
   int* err;                   // error flag (bounded waits)
-  // FP32 outputs and inputs of EPI_RHSF / EPI_RAWF
-  float2* outf2;
-  const float2* hehf;         // Heh in FP32 [ke][kh] per batch
-  const float2* dgf;          // peeled diagonals: [4][nw][nk] Hee hi, Hee lo, Hhh hi, Hhh lo
-  const float* gamf;          // [2][nw][nk] GamE, GamH
-  const float* cdf;           // [4][nw][nk] hi, lo of Re C_kk, then hi, lo of Re D_kk
-  int nw;
 };
 
 struct GemmDesc {
@@ -96,22 +112,29 @@ struct GemmDesc {
   // truncating chain (for products whose result is a small difference of large
   // sums, e.g. the W - W^H form of dC, dD).
   int split;
-  // K range override in BK blocks (kb_hi > kb_lo): a split-K partial product
-  int kb_lo, kb_hi;
+  // split-K: the K blocks are cut into ksplit parts, each a separate output tile
+  // written at out + ks * ks_stride (ksplit 0 counts as 1)
+  int ksplit;
+  PlaneSet A, B;              // operand planes (A: M rows, B: N rows, both K-major)
+};
+
+struct GemmJob {
+  GemmDesc d;
+  EpiArgs e;
+};
+
+// one launch: the concatenated tile lists of njobs jobs (same complex/split mode)
+struct GemmLaunch {
+  GemmJob job[MAX_JOBS];
+  long long tile_base[MAX_JOBS + 1];
+  int njobs;
 };
 
 }  // namespace tc
 
-// Host API of the engine (sbe_tc.cu).
-struct TcPlanes {
-  __half* ptr = nullptr;      // [mat][plane][batch][rows][K]
-  int nmat = 0, nplanes = 0, batch = 0, rows = 0, K = 0;
-};
-
-int tc_make_maps(const TcPlanes& a, const TcPlanes& b, CUtensorMap* ma, CUtensorMap* mb);
-// tensor map of a B operand for the split-accumulator mode (64-row box)
-int tc_make_map_split(const TcPlanes& b, CUtensorMap* mb);
-int tc_gemm_launch(const tc::GemmDesc& d, const CUtensorMap& ma, const CUtensorMap& mb,
-                   const tc::EpiArgs& e, cudaStream_t s);
+// Host API of the engine.
+int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s);
+int tc_gemm_launch(const tc::GemmDesc& d, const tc::EpiArgs& e, cudaStream_t s);
+int tc_gemm_init();
 
 }  // namespace sbe

@@ -59,7 +59,9 @@ def rel(a, b):
     return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
 
 
-@pytest.mark.parametrize("nk", [64, 128, 256])
+# 16 and 32: one K block (the first split-K half of W and V is empty); 48, 96: an
+# uneven split of two and three K blocks
+@pytest.mark.parametrize("nk", [16, 32, 48, 64, 96, 128, 256])
 def test_mixed_rhs_vs_fp64(nk):
     from pulsesuite_gb300 import _lib
     nw = 3
