@@ -282,6 +282,14 @@ int sbe_tc_selftest(int nk, int nbatch, const double* A, const double* B, int op
  * d_out[i] = fp64(f_in[i]).                                                    */
 int sbe_convert_selftest(const double* d_in, const float* f_in, long long n, float* f_out,
                          double* d_out, void* stream);
+/* Diagnostic entry, no counterpart in the reference: the off-diagonal dephasing
+ * matrices De, Dh [2Nk+1][Nk] per wire (packed like the context's wires) of the
+ * occupations of the states C, D, from the FP64 sums (fp32 = 0, the literal
+ * reference loops of dephasing.py:227-317) or from the FP32 sums of the
+ * mixed-precision path (fp32 = 1).  Needs a context whose wires all have the
+ * OffDiagDph flag.                                                              */
+int sbe_deph_selftest(SbeCtx* ctx, const double* C, const double* D, int fp32, double* De,
+                      double* Dh, void* stream);
 
 #ifdef __cplusplus
 }

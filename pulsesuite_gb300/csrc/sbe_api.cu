@@ -437,6 +437,18 @@ int sbe_offdiag(SbeCtx* c, int w, const double* ne, const double* nh, const doub
   return cuda_check(cudaGetLastError(), "sbe_offdiag");
 }
 
+int sbe_deph_selftest(SbeCtx* c, const double* C, const double* D, int fp32, double* De,
+                      double* Dh, void* stream) {
+  if (!c || !C || !D || !De || !Dh) return fail(SBE_ERR_ARG, "sbe_deph_selftest: null pointer");
+  cudaStream_t s = as_stream(stream);
+  launch_prep_scalar(c, reinterpret_cast<const double2*>(C), reinterpret_cast<const double2*>(D),
+                     s);
+  launch_offdiag_D(c, -1, nullptr, fp32 != 0, s);
+  copy_in(De, c->De, 8 * (size_t)c->tot_dd, s);
+  copy_in(Dh, c->Dh, 8 * (size_t)c->tot_dd, s);
+  return cuda_check(cudaGetLastError(), "sbe_deph_selftest");
+}
+
 int sbe_phonon_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
                      const double* E1D, double* WinE, double* WoutE, double* WinH, double* WoutH,
                      void* stream) {

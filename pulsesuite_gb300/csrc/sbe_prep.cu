@@ -1,6 +1,7 @@
 // Per-step preparation of every wire: occupations, screening, diagonal and
 // off-diagonal dephasing, and the Hartree-Fock Hamiltonians (FP64).
 #include "sbe_ctx.cuh"
+#include "fp_bits.cuh"
 
 namespace sbe {
 
@@ -248,19 +249,26 @@ __global__ void k_occf(const WireDev* wires, const double2* ne, const double2* n
   occf[2 * W.off_vec + W.nk + k] = (float)hypot(nh[W.off_vec + k].x, nh[W.off_vec + k].y);
 }
 
-// One block per (q, species, wire) and up to 512 k; each thread sums four
+// One block per (q >= 0, species, wire) and up to 512 k; each thread sums four
 // consecutive k, so that the per-p shared-memory loads (the Lorentzian window and
-// the paired occupation weights, read as one float2 broadcast) serve four outputs:
-// the loop was bound by shared-memory loads, not by FMA.
+// the paired occupation weights, read as one float2 broadcast) serve four outputs.
+//
+// The rows -q come from the sums of row q.  With p' = p - q (a-a) or p' = p + q
+// (a-b) the term (-q, k + q, p') has the Lorentzian argument -u(q, k, p) and the
+// two occupation weights of (q, k, p) swapped, over the same p range, except
+// that the a-a range of row -q also holds p' = 0 (p = q), which row q leaves out
+// (p - q >= 1 in the reference loops).  So
+//   sa(-q, k + q) = sb(q, k) [+ the a-a term p = q],  sb(-q, k + q) = sa(q, k) [+ ..]
+// and a block writes D[q][k] and D[-q][k + q] for every k with k + q < Nk, and
+// the zeros of both rows elsewhere; the Lorentzian sums are formed once.
 __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const float* occf,
                                                      const float* dconst, const float* dpre,
                                                      double* De, double* Dh) {
   const int wi = blockIdx.z >> 1, which = blockIdx.z & 1;   // 0 De, 1 Dh
   const WireDev& W = wires[wi];
   const int nk = W.nk;
-  const int qi = blockIdx.y;
-  if (qi > 2 * nk) return;
-  const int q = qi - nk;
+  const int q = blockIdx.y;   // 0 .. nk; row -q from the same sums
+  if (q > nk) return;
   extern __shared__ float sh[];
   float* na = sh;                                        // |n_a|
   float* nb = na + nk;                                   // |n_b|
@@ -297,6 +305,10 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
   }
   __syncthreads();
   double* D = (which == 0 ? De : Dh) + W.off_dd;
+  double* Dp = D + (long long)(nk + q) * nk;   // row q
+  double* Dm = D + (long long)(nk - q) * nk;   // row -q
+  // the a-a term p = q of row -q (absent from row q): L(alpha q k) weights
+  const float n0a = na[0], nqa = (q < nk) ? na[q] : 0.f;
   for (int k0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4; k0 < nk;
        k0 += gridDim.x * blockDim.x * 4) {
     float sa[4] = {0.f, 0.f, 0.f, 0.f}, sb[4] = {0.f, 0.f, 0.f, 0.f};
@@ -321,14 +333,9 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
         l[0] = (in >= 0) ? Ltab[in] : 0.f;
       }
     }
-    float acc[4];
+    float ta[4], tb[4];   // a-b sums
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float nak = (k0 + j < nk) ? na[k0 + j] : 0.f;
-      acc[j] = vaa * ((1.f - nak) * sa[j] + nak * sb[j]);
-      sa[j] = 0.f;
-      sb[j] = 0.f;
-    }
+    for (int j = 0; j < 4; ++j) ta[j] = tb[j] = 0.f;
     if (vab != 0.f) {
       const int plo = max(0, -q), phi = min(nk - 1, nk - 1 - q);
       const int c = -2 * W.dnk - 1 + q;
@@ -350,8 +357,8 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
           const float u = fq * sv;
           float L;   // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
           asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L) : "f"(fmaf(u, u, 1.0f)));
-          sa[j] = fmaf(L, w2.x, sa[j]);
-          sb[j] = fmaf(L, w2.y, sb[j]);
+          ta[j] = fmaf(L, w2.x, ta[j]);
+          tb[j] = fmaf(L, w2.y, tb[j]);
         }
       }
     }
@@ -359,12 +366,26 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
     for (int j = 0; j < 4; ++j) {
       const int k = k0 + j;
       if (k >= nk) continue;
-      float v = 0.f;
-      if (k + q >= 0 && k + q < nk) {
-        const float nak = na[k];
-        v = acc[j] + vab * ((1.f - nak) * sa[j] + nak * sb[j]);
+      if (k + q >= nk) {
+        // row q outside the band; row -q at k' = k - (nk - q) < q is zero too
+        Dp[k] = 0.0;
+        if (q > 0) Dm[k - (nk - q)] = 0.0;
+        continue;
       }
-      D[(long long)qi * nk + k] = (double)v;
+      const float nak = na[k];
+      const float vq = vaa * ((1.f - nak) * sa[j] + nak * sb[j]) +
+                       vab * ((1.f - nak) * ta[j] + nak * tb[j]);
+      Dp[k] = f32_to_f64(vq);
+      if (q > 0) {
+        // row -q at k + q: swapped sums plus the a-a term p = q
+        const float lq = Ltab[k + nk - 1 - q];   // L(alpha q k)
+        const float xa = sb[j] + lq * ((1.f - n0a) * nqa);
+        const float xb = sa[j] + lq * (n0a * (1.f - nqa));
+        const float nk2 = na[k + q];
+        const float vm = vaa * ((1.f - nk2) * xa + nk2 * xb) +
+                         vab * ((1.f - nk2) * tb[j] + nk2 * ta[j]);
+        Dm[k + q] = f32_to_f64(vm);
+      }
     }
   }
 }
@@ -404,7 +425,7 @@ void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaSt
                                                                  c->occf);
     k_deph_consts<<<dim3((c->nk_max + 127) / 128, 2 * c->nw), 128, 0, s>>>(c->d_wires, c->vs,
                                                                           c->dconst, c->dpre);
-    k_offdiag_D32<<<dim3((c->nk_max + 511) / 512, 2 * c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
+    k_offdiag_D32<<<dim3((c->nk_max + 511) / 512, c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
         c->d_wires, c->occf, c->dconst, c->dpre, c->De, c->Dh);
     return;
   }

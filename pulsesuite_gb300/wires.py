@@ -256,6 +256,17 @@ class WireContext:
         """Capture one rk4_step on these buffers into a CUDA graph (RK4Graph)."""
         return RK4Graph(self, P, C, D, Ek0, dEk, dt, src_out, precision)
 
+    def deph(self, C, D, fp32=False):
+        """Off-diagonal dephasing matrices (De, Dh), packed [2Nk+1][Nk] per wire, of the
+        occupations of C, D: the FP64 reference sums or the mixed path's FP32 sums."""
+        n = sum((2 * s.nk + 1) * s.nk for s in self.specs)
+        De = torch.empty(n, dtype=torch.float64, device="cuda")
+        Dh = torch.empty_like(De)
+        _lib.check(self.lib.sbe_deph_selftest(self.handle, _lib.ptr(C), _lib.ptr(D), int(bool(fp32)),
+                                              _lib.ptr(De), _lib.ptr(Dh), _lib.stream_handle()),
+                   "sbe_deph_selftest")
+        return De, Dh
+
     def check(self):
         """Wait for the current stream and raise if a device-side bounded wait gave up."""
         _lib.check(self.lib.sbe_ctx_check(self.handle, _lib.stream_handle()), "sbe_ctx_check")

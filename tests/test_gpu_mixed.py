@@ -146,3 +146,30 @@ def test_mixed_rk4_pulse_vs_fp64(nk):
         assert rel(nem, ne64) < 1e-5
         assert rel(ctx.mat(Pm, w), ctx.mat(P64, w)) < 1e-5
         assert rel(ctx.rvec(sm, w, 5)[:3], ctx.rvec(s64, w, 5)[:3]) < 1e-5
+
+
+@pytest.mark.parametrize("nk", [16, 48, 256])
+def test_fp32_dephasing_sums_vs_fp64(nk):
+    """The mixed path's FP32 off-diagonal dephasing sums (rows -q formed from the
+    sums of row q) against the FP64 reference loops, every row and wire."""
+    nw = 2
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(100 + nk)
+    st = [seeded(rng, nk) for _ in range(nw)]
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    De64, Dh64 = ctx.deph(C, D, fp32=False)
+    De32, Dh32 = ctx.deph(C, D, fp32=True)
+    ctx.check()
+    rows = 2 * nk + 1
+    for a, b, n in ((De32, De64, "De"), (Dh32, Dh64, "Dh")):
+        a = a.reshape(nw, rows, nk)
+        b = b.reshape(nw, rows, nk)
+        # the band structure (zeros where k + q leaves the grid) is exact
+        assert torch.equal(a == 0, b == 0), n
+        for w in range(nw):
+            e = rel(a[w], b[w])
+            assert e < 2e-6, (nk, n, w, e)
+            # rows q and -q separately: a wrong mirror shows in one half only
+            for half in (slice(0, nk), slice(nk + 1, rows)):
+                assert rel(a[w, half], b[w, half]) < 2e-6, (nk, n, w, half)
