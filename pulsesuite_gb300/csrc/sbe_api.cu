@@ -60,6 +60,10 @@ static WireDev derive(const SbeWireDesc& d, int nk_check_only = 0) {
   W.nmax = std::min(ae / 2.0, ah / 2.0) / kPi * 0.99;
   W.pol_scale = 2.0 * W.ehint / W.area / W.L;
   W.rho_scale = 2.0 * kE0 * W.ehint / W.area;
+  const float ed = (float)(W.ehint * W.dcv);
+  W.ed_x = ed;
+  W.ed_y = -ed * (float)W.yw;
+  W.ed_z = ed * (float)W.zsign;
   return W;
 }
 

@@ -36,6 +36,10 @@ struct WireDev {
   double vscale, n0ph, nmax;   // phonon Vscale, Bose N0, screening clamp
   double pol_scale;            // 2 ehint / (area L)
   double rho_scale;            // 2 e0 ehint / area
+  // FP32 coupling constants of the mixed path (host-rounded once): the dipole
+  // term -ehint Xcv of Heh as the x, y, z weights ed_x (odd k; even k: -ed_x),
+  // ed_y, ed_z
+  float ed_x, ed_y, ed_z, padf;
 };
 
 struct SbeCtxImpl;

@@ -93,8 +93,7 @@ void launch_planes(const double2* X, long long bstride, int nk, int nbatch, int 
   k_planes<<<grid, blk, 0, s>>>(X, bstride, nk, transpose, e, dst, mat, real_only);
 }
 
-// Both layouts of a batch of Nk x Nk complex matrices from one read: planes of X
-// into matrix slot matN and of X^T into slot matT (matT < 0: none), same scale.
+// a complex value scaled by 2^e and rounded once to FP32
 template <typename T>
 __device__ __forceinline__ float2 scaled2(T v, int e);
 template <>
@@ -110,16 +109,58 @@ __device__ __forceinline__ float2 scaled2<float2>(float2 v, int e) {
 // of its 32 x 32 tile to tpart[((b * 2 + which) * T + bi) * T + bj][l], local
 // diagonal l = c - r + 31, for the traces of C and D.
 // With cdf set, the diagonal is left out of the planes (written as zero) and the
-// hi / lo FP32 parts of its real part go to cdf[b * nk + k] and
-// cdf[nbatch * nk + b * nk + k].
+// hi / lo FP32 parts of its real part (from dg[b * nk + k] in FP64 when given) go
+// to cdf[b * nk + k] and cdf[nbatch * nk + b * nk + k].
 __device__ __forceinline__ double dvalue(double2 v) { return v.x; }
 __device__ __forceinline__ double dvalue(float2 v) { return f32_to_f64(v.x); }
 
+// FP16 hi / lo of one FP32 value pair (re, im): planes re_hi, re_lo, im_hi, im_lo
+__device__ __forceinline__ void hilo4(float2 v, __half* h0, __half* h1, __half* h2, __half* h3) {
+  const __half2 hi = __float22half2_rn(v);
+  const float2 hf = __half22float2(hi);
+  const __half2 lo = __float22half2_rn(make_float2(v.x - hf.x, v.y - hf.y));
+  *h0 = __low2half(hi);
+  *h1 = __low2half(lo);
+  *h2 = __high2half(hi);
+  *h3 = __high2half(lo);
+}
+
+// Store the 32 x 32 plane tiles hs[plane][row][k] (row stride 40 halves) of rows
+// r0.., K-block kb: four lanes write the 64 bytes of one row (16-byte stores).
+__device__ __forceinline__ void store_tiles(const __half (*hs)[32][40], int npl,
+                                            const tc::PlaneSet& dst, int mat, int b, int r0,
+                                            int kb, int tid, int nthreads) {
+  for (int t = tid; t < npl * 128; t += nthreads) {
+    const int pl = t >> 7, rr = (t >> 2) & 31, j = t & 3;
+    const uint4 v = *reinterpret_cast<const uint4*>(&hs[pl][rr][8 * j]);
+    *reinterpret_cast<uint4*>(dst.ptr + tc::chunk_elem(dst, mat, pl, b, r0 + rr, kb, j)) = v;
+  }
+}
+
+// The same tiles transposed: row r0 + cc of the destination holds column cc of hs.
+__device__ __forceinline__ void store_tiles_t(const __half (*hs)[32][40], int npl,
+                                              const tc::PlaneSet& dst, int mat, int b, int r0,
+                                              int kb, int tid, int nthreads) {
+  for (int t = tid; t < npl * 128; t += nthreads) {
+    const int pl = t >> 7, cc = (t >> 2) & 31, j = t & 3;
+    __align__(16) __half v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = hs[pl][8 * j + i][cc];
+    *reinterpret_cast<uint4*>(dst.ptr + tc::chunk_elem(dst, mat, pl, b, r0 + cc, kb, j)) =
+        *reinterpret_cast<const uint4*>(v);
+  }
+}
+
+// Both layouts of a batch of Nk x Nk complex matrices from one read: planes of X
+// into matrix slot matN and of X^T into slot matT (matT < 0: none), same scale.
+// The block converts its 32 x 32 tile once into shared-memory plane tiles and
+// writes both layouts with 16-byte stores.
 template <typename T>
 __global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, int matN, int matT,
                             int nbatch, float2* tpart = nullptr, int which = 0,
-                            float* cdf = nullptr) {
+                            float* cdf = nullptr, const double* dg = nullptr) {
   __shared__ T tile[32][33];
+  __shared__ __align__(16) __half hs[4][32][40];
   const int b = blockIdx.z;
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
   const T* x = X + (long long)b * nk * nk;
@@ -132,29 +173,24 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, 
   }
   __syncthreads();
   const int eb = e[b];
-  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-    for (int pass = 0; pass < (matT < 0 ? 1 : 2); ++pass) {
-      // pass 0: row r0 + i of X;  pass 1: row c0 + i of X^T (= column c0 + i of X)
-      const int r = (pass ? c0 : r0) + i, c = (pass ? r0 : c0) + threadIdx.x;
-      if (r >= nk || c >= nk) continue;
-      float2 v = scaled2<T>(pass ? tile[threadIdx.x][i] : tile[i][threadIdx.x], eb);
-      if (cdf && r == c) {
-        v = make_float2(0.f, 0.f);
-        if (pass == 0) {
-          const double d = dvalue(tile[i][threadIdx.x]);
-          const float hi = f64_to_f32(d);
-          cdf[(long long)b * nk + r] = hi;
-          cdf[((long long)nbatch + b) * nk + r] = f64_to_f32(d - f32_to_f64(hi));
-        }
-      }
-      __half* base = dst.ptr + tc::plane_elem(dst, pass ? matT : matN, 0, b, r, c);
-      put_hilo(base, pstride, v.x);
-      put_hilo(base + 2 * pstride, pstride, v.y);
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    float2 v = scaled2<T>(tile[i][threadIdx.x], eb);
+    if (cdf && r == c && r < nk) {
+      v = make_float2(0.f, 0.f);
+      const double d = dg ? dg[(long long)b * nk + r] : dvalue(tile[i][threadIdx.x]);
+      const float hi = f64_to_f32(d);
+      cdf[(long long)b * nk + r] = hi;
+      cdf[((long long)nbatch + b) * nk + r] = f64_to_f32(d - f32_to_f64(hi));
     }
+    hilo4(v, &hs[0][i][threadIdx.x], &hs[1][i][threadIdx.x], &hs[2][i][threadIdx.x],
+          &hs[3][i][threadIdx.x]);
   }
+  __syncthreads();
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+  store_tiles(hs, 4, dst, matN, b, r0, c0 >> 5, tid, nth);
+  if (matT >= 0) store_tiles_t(hs, 4, dst, matT, b, c0, r0 >> 5, tid, nth);
   if (tpart) {
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     if (tid < 63) {
       const int l = tid - 31;   // c - r
       float sr = 0.f, si = 0.f;
@@ -242,6 +278,7 @@ struct Mixed {
   float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
   float2* tpart = nullptr;  // nw x 2 x T x T x 63 partial diagonal sums (T = ceil(nk/32))
   float* cdf = nullptr;     // 4 x nw x nk: hi / lo parts of Re C_kk and Re D_kk (stage state)
+  double* xdg = nullptr;    // 2 x nw x nk: Re C_kk, Re D_kk of the stage state in FP64
   int* eS() { return ints; }
   int* eH() { return ints + nw; }
   int* eT() { return ints + 2 * nw; }
@@ -274,6 +311,7 @@ void mixed_free(SbeCtx* c) {
   cudaFree(m->epf);
   cudaFree(m->ekrf);
   cudaFree(m->tpart);
+  cudaFree(m->xdg);
   delete m;
   c->mixed = nullptr;
 }
@@ -420,7 +458,8 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   void* cblock = nullptr;
   if (cudaMalloc(&cblock, cbytes) != cudaSuccess ||
       cudaMalloc(&m->ekrf, sizeof(float2) * (size_t)c->tot_kr) != cudaSuccess ||
-      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * T * T * 63) != cudaSuccess) {
+      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * T * T * 63) != cudaSuccess ||
+      cudaMalloc(&m->xdg, sizeof(double) * 2 * (size_t)nw * nk) != cudaSuccess) {
     if (cblock) cudaFree(cblock);
     m->epf = nullptr;
     c->mixed = m;
@@ -457,17 +496,40 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
 
 // maxima of a batch of Nk x Nk matrices: all elements into mx[b], and (when
 // peel) the off-diagonal elements into mo[b] (all elements when !peel)
-__global__ void k_absmax2(const double2* X, int nk, int peel, unsigned* mx, unsigned* mo) {
+// Stage-1 state of the mixed path: the FP32 copy xf of a batch of Nk x Nk FP64
+// matrices (round to nearest; every stage consumer rounds the state to FP32),
+// its maxima mx (all elements) and mo (off-diagonal only when peel), and with dg
+// set the FP64 real diagonal (the occupations of C and D, which the peeled terms
+// use beyond FP32).  The diagonal is tracked by a row / column counter stepped
+// with the grid stride (no division per element).
+__global__ void k_state_in(const double2* X, int nk, int peel, unsigned* mx, unsigned* mo,
+                           float2* xf, double* dg) {
   const int b = blockIdx.y;
   const long long per = (long long)nk * nk;
   const double2* x = X + (long long)b * per;
+  float2* y = xf + (long long)b * per;
   unsigned long long m = 0, o = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per;
-       i += (long long)gridDim.x * blockDim.x) {
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long S = (long long)gridDim.x * blockDim.x;
+  int row = (int)(i0 / nk), col = (int)(i0 % nk);
+  const int srow = (int)(S / nk), scol = (int)(S % nk);
+  for (long long i = i0; i < per; i += S) {
     const double2 v = x[i];
+    y[i] = f64_to_f32(v);
     const unsigned long long a = max(absbits(v.x), absbits(v.y));
     m = max(m, a);
-    if (!peel || (i % (nk + 1)) != 0) o = max(o, a);
+    if (row == col) {
+      if (dg) dg[(long long)b * nk + row] = v.x;
+      if (!peel) o = max(o, a);
+    } else {
+      o = max(o, a);
+    }
+    col += scol;
+    row += srow;
+    if (col >= nk) {
+      col -= nk;
+      ++row;
+    }
   }
   for (int k = 16; k > 0; k >>= 1) {
     m = max(m, __shfl_down_sync(0xffffffffu, m, k));
@@ -491,18 +553,31 @@ static void absmax_into(const double2* X, long long per, int nw, unsigned* mx, c
 // FP32 copy of vs for the direct terms.
 __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const int* e,
                                   tc::PlaneSet dst, int nw, float* vsf) {
+  // block (32, 8) over a 32 x 32 tile (rows t, columns t')
+  __shared__ __align__(16) __half hs[2][32][40];
   const int b = blockIdx.z / 3, n = blockIdx.z % 3;
   const WireDev W = wires[b];
   const int nk = W.nk;
-  int tp = blockIdx.x * blockDim.x + threadIdx.x;
-  int t = blockIdx.y;
-  if (tp >= nk || t >= nk) return;
-  int d = t > tp ? t - tp : tp - t;
-  const double vd = vs[3 * W.off_vec + n * nk + d];
-  if (t == 0) vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(vd);
-  const float v = (d == 0) ? 0.f : f64_to_f32(vd, e[b]);
-  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
-  put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, t, tp), pstride, v);
+  const int t0 = blockIdx.y * 32, c0 = blockIdx.x * 32, tx = threadIdx.x;
+  if (t0 >= nk || c0 >= nk) return;
+  const int eb = e[b];
+  const double* v = vs + 3 * W.off_vec + n * nk;
+  const int tp = c0 + tx;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int t = t0 + i;
+    float f = 0.f;
+    if (t < nk && tp < nk) {
+      const int d = t > tp ? t - tp : tp - t;
+      const double vd = v[d];
+      if (t == 0) vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(vd);
+      f = (d == 0) ? 0.f : f64_to_f32(vd, eb);
+    }
+    const __half hi = __float2half_rn(f);
+    hs[0][i][tx] = hi;
+    hs[1][i][tx] = __float2half_rn(f - __half2float(hi));
+  }
+  __syncthreads();
+  store_tiles(hs, 2, dst, n, b, t0, c0 >> 5, threadIdx.y * 32 + tx, 32 * blockDim.y);
 }
 
 __global__ void k_vs_max(const WireDev* wires, const double* vs, unsigned* mx) {
@@ -710,43 +785,64 @@ __global__ void k_diag_max(const WireDev* wires, const double2* C, const double2
 
 // QWPolarization3 / QWRho5 reduction (qwoptics.py:809-1071) from the FP32 source
 // GEMM outputs G[k][r] = sum_k' X[k][k'] e^{i k' r}: sums over k in FP32, the
-// physical prefactors in FP64 per r.
+// physical prefactors in FP64 per r.  Block (32 r) x (8 k-groups): thread (x, y)
+// sums k = y, y + 8, ... of point r, the eight partial sums meet in shared memory.
 __global__ void k_src_reduce_f(const WireDev* wires, const float2* ekrf, const float2* G,
                                long long tot_kr, const double* win, double2* src) {
+  __shared__ float part[6][8][33];
   const WireDev W = wires[blockIdx.y];
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= W.nr) return;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int r = blockIdx.x * 32 + tx;
   const int nk = W.nk, nr = W.nr;
-  const float2* E = ekrf + W.off_kr;
-  const float2* Gp = G + W.off_kr;
-  const float2* Gc = G + tot_kr + W.off_kr;
-  const float2* Gd = G + 2 * tot_kr + W.off_kr;
   float sx = 0.f, sy = 0.f, ser = 0.f, sei = 0.f, shr = 0.f, shi = 0.f;
-  for (int k = 0; k < nk; ++k) {
-    const long long o = (long long)k * nr + r;
-    const float2 e = E[o];             // conj taken below
-    const float2 gp = Gp[o], gc = Gc[o], gd = Gd[o];
-    const float re_part = e.x * gp.x + e.y * gp.y;
-    sx += (k & 1) ? -re_part : re_part;
-    sy += re_part;
-    ser += e.x * gc.x + e.y * gc.y;
-    sei += e.x * gc.y - e.y * gc.x;
-    shr += e.x * gd.x + e.y * gd.y;
-    shi += e.x * gd.y - e.y * gd.x;
+  if (r < nr) {
+    const float2* E = ekrf + W.off_kr;
+    const float2* Gp = G + W.off_kr;
+    const float2* Gc = G + tot_kr + W.off_kr;
+    const float2* Gd = G + 2 * tot_kr + W.off_kr;
+#pragma unroll 4
+    for (int k = ty; k < nk; k += 8) {
+      const long long o = (long long)k * nr + r;
+      const float2 e = E[o];             // conj taken below
+      const float2 gp = Gp[o], gc = Gc[o], gd = Gd[o];
+      const float re_part = e.x * gp.x + e.y * gp.y;
+      sx += (k & 1) ? -re_part : re_part;
+      sy += re_part;
+      ser += e.x * gc.x + e.y * gc.y;
+      sei += e.x * gc.y - e.y * gc.x;
+      shr += e.x * gd.x + e.y * gd.y;
+      shi += e.x * gd.y - e.y * gd.x;
+    }
+  }
+  part[0][ty][tx] = sx;
+  part[1][ty][tx] = sy;
+  part[2][ty][tx] = ser;
+  part[3][ty][tx] = sei;
+  part[4][ty][tx] = shr;
+  part[5][ty][tx] = shi;
+  __syncthreads();
+  if (ty != 0 || r >= nr) return;
+  float v[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    float a = 0.f;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) a += part[i][g][tx];
+    v[i] = a;
   }
   const double w = win[W.off_r + r];
   double2* out = src + 5 * W.off_r;
   const bool optics = (W.flags & SBE_F_OPTICS) != 0;
   const double pf = 2 * W.ehint / W.area / W.L;
-  const double px = optics ? (W.dcv * f32_to_f64(sx)) * w : 0.0;
-  const double py = optics ? (W.dcv * f32_to_f64(sy)) * w * W.yw : 0.0;
-  const double pz = optics ? (-W.dcv * f32_to_f64(sy)) * w * W.zsign : 0.0;
+  const double px = optics ? (W.dcv * f32_to_f64(v[0])) * w : 0.0;
+  const double py = optics ? (W.dcv * f32_to_f64(v[1])) * w * W.yw : 0.0;
+  const double pz = optics ? (-W.dcv * f32_to_f64(v[1])) * w * W.zsign : 0.0;
   out[r] = make_double2(px * pf, 0.0);
   out[nr + r] = make_double2(py * pf, 0.0);
   out[2 * nr + r] = make_double2(pz * pf, 0.0);
   const double f = w / (2.0 * W.L);
-  out[3 * nr + r] = make_double2(f32_to_f64(ser) * f, f32_to_f64(sei) * f);
-  out[4 * nr + r] = make_double2(f32_to_f64(shr) * f, f32_to_f64(shi) * f);
+  out[3 * nr + r] = make_double2(f32_to_f64(v[2]) * f, f32_to_f64(v[3]) * f);
+  out[4 * nr + r] = make_double2(f32_to_f64(v[4]) * f, f32_to_f64(v[5]) * f);
 }
 
 __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH, float* gamf,
@@ -769,11 +865,12 @@ __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH
 // read row by row (coalesced) into shared memory and then read along diagonals
 // (row stride 32 double2: diagonal reads are free of bank conflicts).
 // blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire.
-__global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* X1,
-                              const double2* X2, const int* e, tc::PlaneSet dst) {
-  __shared__ double2 tile[63][32];
+__global__ void k_shear_tiles(int nk, int nw, const float2* X0, const float2* X1,
+                              const float2* X2, const int* e, tc::PlaneSet dst) {
+  __shared__ float2 tile[63][32];
+  __shared__ __align__(16) __half hs[2][64][40];   // hi, lo of rows 2 dd0 .. 2 dd0 + 63
   const int n = blockIdx.z / nw, b = blockIdx.z % nw;
-  const double2* X = (n == 0 ? X0 : n == 1 ? X1 : X2) + (long long)b * nk * nk;
+  const float2* X = (n == 0 ? X0 : n == 1 ? X1 : X2) + (long long)b * nk * nk;
   const int t0 = blockIdx.x * 32, dd0 = blockIdx.y * 32;
   const int rbase = t0 + dd0 - (nk - 1);
   const int tx = threadIdx.x;
@@ -782,47 +879,34 @@ __global__ void k_shear_tiles(int nk, int nw, const double2* X0, const double2* 
   if (rbase + 62 < 0 || rbase >= nk) return;
   for (int rr = threadIdx.y; rr < 63; rr += blockDim.y) {
     const int r = rbase + rr, c = t0 + tx;
-    tile[rr][tx] = (r >= 0 && r < nk && c < nk) ? X[(long long)r * nk + c] : make_double2(0, 0);
+    tile[rr][tx] = (r >= 0 && r < nk && c < nk) ? X[(long long)r * nk + c] : make_float2(0, 0);
   }
   __syncthreads();
   const int eb = e[b];
-  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
-  const int tp = t0 + tx;
-  if (tp >= nk) return;
   for (int ddl = threadIdx.y; ddl < 32; ddl += blockDim.y) {
-    const int dd = dd0 + ddl;
-    if (dd >= 2 * nk) break;
-    const int r = rbase + tx + ddl;
-    if (r < 0 || r >= nk) continue;   // out of band: stays zero
-    const double2 v = tile[tx + ddl][tx];
-    put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, 2 * dd, tp), pstride, f64_to_f32(v.x, eb));
-    put_hilo(dst.ptr + tc::plane_elem(dst, n, 0, b, 2 * dd + 1, tp), pstride,
-             f64_to_f32(v.y, eb));
+    // element (dd0 + ddl, t0 + tx) of the shear: source row rbase + tx + ddl (the
+    // tile is zero outside the band and the matrix)
+    const float2 t = tile[tx + ddl][tx];
+    const float2 v = make_float2(f32_ldexp(t.x, eb), f32_ldexp(t.y, eb));
+    const __half2 hi = __float22half2_rn(v);
+    const float2 hf = __half22float2(hi);
+    const __half2 lo = __float22half2_rn(make_float2(v.x - hf.x, v.y - hf.y));
+    hs[0][2 * ddl][tx] = __low2half(hi);
+    hs[1][2 * ddl][tx] = __low2half(lo);
+    hs[0][2 * ddl + 1][tx] = __high2half(hi);
+    hs[1][2 * ddl + 1][tx] = __high2half(lo);
+  }
+  __syncthreads();
+  const int tid = threadIdx.y * blockDim.x + tx, nth = blockDim.x * blockDim.y;
+  for (int t = tid; t < 2 * 64 * 4; t += nth) {
+    const int pl = t >> 8, rr = (t >> 2) & 63, j = t & 3;
+    const uint4 v = *reinterpret_cast<const uint4*>(&hs[pl][rr][8 * j]);
+    *reinterpret_cast<uint4*>(dst.ptr + tc::chunk_elem(dst, n, pl, b, 2 * dd0 + rr, t0 >> 5, j)) =
+        v;
   }
 }
 
-// Diagonal traces tr_d(X) = sum_k X[k][k+d] of C and D (SBEs.py:1094-1103) in
-// FP32, layout per wire [2][2Nk] with entry d + Nk; and the stage field in FP32.
-__global__ void k_traces_f(const WireDev* wires, const double2* C, const double2* D, float2* trf) {
-  const WireDev W = wires[blockIdx.z];
-  const int nk = W.nk;
-  const int d = (int)blockIdx.x - (nk - 1);
-  if ((int)blockIdx.x >= 2 * nk - 1) return;
-  const double2* X = (blockIdx.y == 0 ? C : D) + W.off_mat;
-  const int k0 = d >= 0 ? 0 : -d, k1 = d >= 0 ? nk - 1 - d : nk - 1;
-  float sr = 0.f, si = 0.f;
-  for (int k = k0 + threadIdx.x; k <= k1; k += 32) {
-    const float2 v = f64_to_f32(X[(long long)k * nk + k + d]);
-    sr += v.x;
-    si += v.y;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sr += __shfl_down_sync(0xffffffffu, sr, o);
-    si += __shfl_down_sync(0xffffffffu, si, o);
-  }
-  if (threadIdx.x == 0)
-    trf[(long long)blockIdx.z * 4 * nk + blockIdx.y * 2 * nk + d + nk] = make_float2(sr, si);
-}
+// The stage field in FP32.
 
 __global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -852,9 +936,8 @@ __global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* 
       if (q < 0) q += W.nr;
       const float2* ek = ekf + 3 * W.off_r;
       const float2 ex = ek[q], ey = ek[W.nr + q], ez = ek[2 * W.nr + q];
-      const float ed = (float)(W.ehint * W.dcv);
-      const float sx = (k2 & 1) ? ed : -ed;               // -ehint Xcv
-      const float sy = -ed * (float)W.yw, sz = ed * (float)W.zsign;
+      const float sx = (k2 & 1) ? W.ed_x : -W.ed_x;       // -ehint Xcv
+      const float sy = W.ed_y, sz = W.ed_z;
       heh.x = sx * ex.x + sy * ey.x + sz * ez.x;
       heh.y = sx * ex.y + sy * ey.y + sz * ez.y;
     }
@@ -928,21 +1011,40 @@ __global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* 
 // (slots M_EEX, M_HHX) from the FP32 values.
 __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA, const float* hB,
                           int nk, const int* e, tc::PlaneSet dst, int nw) {
+  // block (32, 8) over a 32 x 32 tile; each slot's planes go through shared memory
+  __shared__ __align__(16) __half hs[4][32][40];
   const int b = blockIdx.z;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
-  if (c >= nk || r >= nk) return;
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32, tx = threadIdx.x, ty = threadIdx.y;
   const long long mm = (long long)nk * nk;
-  const long long o = (long long)b * mm + (long long)r * nk + c;
-  const long long pstride = (long long)dst.batch * tc::plane_slab(dst);
   const int eb = e[b];
-  const float2 a = hee[o], h = hhh[o];
-  const float bb = hB[o], aa = hA[o];
-  const float v[4][2] = {{a.x, a.y}, {h.x, h.y}, {a.x, a.y + bb}, {h.x, h.y + aa}};
+  float2 a[4], h[4];
+  float aa[4], bb[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int r = r0 + ty + 8 * k, c = c0 + tx;
+    const bool in = r < nk && c < nk;
+    const long long o = (long long)b * mm + (long long)r * nk + c;
+    a[k] = in ? hee[o] : make_float2(0.f, 0.f);
+    h[k] = in ? hhh[o] : make_float2(0.f, 0.f);
+    bb[k] = in ? hB[o] : 0.f;
+    aa[k] = in ? hA[o] : 0.f;
+  }
   const int slot[4] = {M_EE, M_HH, M_EEX, M_HHX};
-  for (int i = 0; i < 4; ++i) {
-    __half* base = dst.ptr + tc::plane_elem(dst, slot[i], 0, b, r, c);
-    put_hilo(base, pstride, f32_ldexp(v[i][0], eb));
-    put_hilo(base + 2 * pstride, pstride, f32_ldexp(v[i][1], eb));
+  const int tid = ty * 32 + tx;
+  for (int sl = 0; sl < 4; ++sl) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = ty + 8 * k;
+      const float2 v = sl == 0 ? a[k]
+                       : sl == 1 ? h[k]
+                       : sl == 2 ? make_float2(a[k].x, a[k].y + bb[k])
+                                 : make_float2(h[k].x, h[k].y + aa[k]);
+      hilo4(make_float2(f32_ldexp(v.x, eb), f32_ldexp(v.y, eb)), &hs[0][i][tx], &hs[1][i][tx],
+            &hs[2][i][tx], &hs[3][i][tx]);
+    }
+    __syncthreads();
+    store_tiles(hs, 4, dst, slot[sl], b, r0, c0 >> 5, tid, 256);
+    __syncthreads();
   }
 }
 
@@ -959,7 +1061,7 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
 // once.  W holds FP32 accumulator values; g[j] - g[i] comes from the hi / lo
 // FP32 parts of g.
 __global__ void k_antiherm(int nk, const float2* W, const float2* W2, const float2* Hp,
-                           const double2* X, const float2* ghi, const float2* glo,
+                           const float2* X, const float2* ghi, const float2* glo,
                            const float* chi, const float* clo, float2* out) {
   // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results
   __shared__ float2 tb[32][33], hb[32][33], vt[32][33];
@@ -993,7 +1095,7 @@ __global__ void k_antiherm(int nk, const float2* W, const float2* W2, const floa
     const float2 a = make_float2(w[oa].x + w2[oa].x, w[oa].y + w2[oa].y);   // W[i][j]
     const float2 bt = tb[threadIdx.x][r];                   // W[j][i]
     const float2 hji = hb[threadIdx.x][r];                  // H'[j][i]
-    const float2 x = f64_to_f32(X[mb + (long long)i * nk + j]);
+    const float2 x = X[mb + (long long)i * nk + j];
     const float dr = (gh[j].x - gh[i].x) + (gl[j].x - gl[i].x);
     const float di = (gh[j].y - gh[i].y) + (gl[j].y - gl[i].y);
     const float dc = (ch[i] - ch[j]) + (cl[i] - cl[j]);
@@ -1019,11 +1121,11 @@ __global__ void k_antiherm(int nk, const float2* W, const float2* W2, const floa
 // the off-diagonal C', D'), following dpdt (SBEs.py:1942-1965):
 //   dP[kh][ke] = (G + (1 - c[ke] - d[kh]) Heh[ke][kh] + (hh[kh] + ee[ke]) P) / (i hbar)
 //                - (GamE[ke] + GamH[kh]) P
-// in FP32 from the FP64 stage state P (converted on the integer pipe).  The peeled
+// in FP32 from the FP32 stage state P.  The peeled
 // occupations c, d enter through the Pauli-blocking factor of the driving term and
 // the peeled energy diagonals ee, hh as hi + lo FP32 parts.  32 x 32 tiles; Heh^T
 // goes through shared memory so that every global access runs along rows.
-__global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, const double2* X,
+__global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, const float2* X,
                         const float2* dgf, const float* gamf, const float* cdf, float2* out) {
   __shared__ float2 ht[32][33];
   const int b = blockIdx.z;
@@ -1049,7 +1151,7 @@ __global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, con
     const float pb = ((1.f - chi) - cdf[2 * vn + vb + m]) - (clo + cdf[3 * vn + vb + m]);
     const float2 g = G[o];
     const float ax = g.x + pb * h0.x, ay = g.y + pb * h0.y;
-    const float2 x = f64_to_f32(X[o]);
+    const float2 x = X[o];
     const float2 gh = dgf[2 * vn + vb + m], gl = dgf[3 * vn + vb + m];
     const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
     const float ar = ax + (der * x.x - dei * x.y);
@@ -1060,47 +1162,60 @@ __global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, con
 }
 
 // RK4 stage update of the mixed path: the stage derivative k and the sums
-// k1 + 2 k2 + 2 k3 are FP32 (they carry the RHS's FP32-accumulated precision);
-// the state is FP64 and only the additions to it are FP64.  Every stage also
-// measures the maximum of the state it writes (the next stage state, or the new
-// state after stage 4) per wire into mx[b].
-// grid (blocks per wire, wires).
+// k1 + 2 k2 + 2 k3 are FP32 (they carry the RHS's FP32-accumulated precision).
+// Stages 1-3 write the next stage state in FP32 (xf = fp32(X) + f k: within an
+// FP32 ulp of the rounded FP64 sum, which is all its consumers use) and, with dg
+// set, its real diagonal in FP64; stage 4 adds to the FP64 state.  Every stage
+// also measures the maximum of the state it writes per wire into mx[b] (mo: the
+// off-diagonal part when peel).  grid (blocks per wire, wires).
 __global__ void k_rk4_mixed(int nk, int peel, int stage, float dt, double2* X, float2* acc,
-                            double2* xs, const float2* k, unsigned* mx, unsigned* mo) {
+                            float2* xf, double* dg, const float2* k, unsigned* mx,
+                            unsigned* mo) {
   const int b = blockIdx.y;
   const long long per = (long long)nk * nk;
   const long long o = (long long)b * per;
-  unsigned long long m = 0, mof = 0;
+  unsigned m = 0, mof = 0;   // FP32 magnitude patterns
   const float f = (stage == 1 || stage == 2) ? 0.5f * dt : dt;
-  for (long long i = o + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < o + per;
-       i += (long long)gridDim.x * blockDim.x) {
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long S = (long long)gridDim.x * blockDim.x;
+  int row = (int)(i0 / nk), col = (int)(i0 % nk);
+  const int srow = (int)(S / nk), scol = (int)(S % nk);
+  for (long long j = i0; j < per; j += S) {
+    const long long i = o + j;
     const float2 kv = k[i];
     const double2 x = X[i];
+    unsigned a;
     if (stage < 4) {
       if (stage == 1) {
         acc[i] = kv;
       } else {
-        const float2 a = acc[i];
-        acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
+        const float2 av = acc[i];
+        acc[i] = make_float2(av.x + 2.f * kv.x, av.y + 2.f * kv.y);
       }
-      const double2 v = make_double2(x.x + f32_to_f64(f * kv.x), x.y + f32_to_f64(f * kv.y));
-      xs[i] = v;
-      const unsigned long long a = max(absbits(v.x), absbits(v.y));
-      m = max(m, a);
-      if (!peel || ((i - o) % (nk + 1)) != 0) mof = max(mof, a);
+      const float2 xs = f64_to_f32(x);
+      const float2 v = make_float2(xs.x + f * kv.x, xs.y + f * kv.y);
+      xf[i] = v;
+      if (dg && row == col) dg[(long long)b * nk + row] = x.x + f32_to_f64(f * kv.x);
+      a = max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu);
     } else {
-      const float2 a = acc[i];
-      const float s = dt / 6.f;
-      const double2 v =
-          make_double2(x.x + f32_to_f64(s * (a.x + kv.x)), x.y + f32_to_f64(s * (a.y + kv.y)));
+      const float2 av = acc[i];
+      const float sc = dt / 6.f;
+      const double2 v = make_double2(x.x + f32_to_f64(sc * (av.x + kv.x)),
+                                     x.y + f32_to_f64(sc * (av.y + kv.y)));
       X[i] = v;
-      const unsigned long long av = max(absbits(v.x), absbits(v.y));
-      m = max(m, av);
-      if (!peel || ((i - o) % (nk + 1)) != 0) mof = max(mof, av);
+      a = bits_to_fmax(max(absbits(v.x), absbits(v.y)));
+    }
+    m = max(m, a);
+    if (!peel || row != col) mof = max(mof, a);
+    col += scol;
+    row += srow;
+    if (col >= nk) {
+      col -= nk;
+      ++row;
     }
   }
   {
-    __shared__ unsigned long long red[2][8];
+    __shared__ unsigned red[2][8];
     for (int off = 16; off > 0; off >>= 1) {
       m = max(m, __shfl_down_sync(0xffffffffu, m, off));
       mof = max(mof, __shfl_down_sync(0xffffffffu, mof, off));
@@ -1115,8 +1230,8 @@ __global__ void k_rk4_mixed(int nk, int peel, int stage, float dt, double2* X, f
         m = max(m, red[0][w]);
         mof = max(mof, red[1][w]);
       }
-      atomicMax(mx + b, bits_to_fmax(m));
-      atomicMax(mo + b, bits_to_fmax(mof));
+      atomicMax(mx + b, m);
+      atomicMax(mo + b, mof);
     }
   }
 }
@@ -1166,8 +1281,8 @@ static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
   k_vs_max<<<nw, 256, 0, s>>>(c->d_wires, c->vs, m->mxH());
   exponents_from(m, m->mxH(), m->eT(), s);
-  k_toeplitz_planes<<<dim3((nk + 127) / 128, nk, 3 * nw), 128, 0, s>>>(c->d_wires, c->vs, m->eT(),
-                                                                       m->tp, nw, m->vsf);
+  k_toeplitz_planes<<<dim3((nk + 31) / 32, (nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
+      c->d_wires, c->vs, m->eT(), m->tp, nw, m->vsf);
   k_gamma_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->iq, c->xeh,
                                                          m->gtab, nw);
   k_gamma_f<<<dim3((nk + 7) / 8, nw), 256, sizeof(float) * 2 * nk, s>>>(
@@ -1201,8 +1316,27 @@ static void mixed_relax(SbeCtx* c, double2* C, double2* D, double dt, cudaStream
 // the derivatives go to m->kf (FP32).  When state_max_ready is set, mxS already
 // holds the per-wire maximum of the state (written by the previous stage's
 // update); otherwise it is measured here.
-static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const double2* D,
-                       const double2* Ek, int state_max_ready, cudaStream_t s) {
+// Stage-1 state of the mixed path from the FP64 state: FP32 copies in xf, the
+// FP64 diagonals of C and D, and the maxima the stage's exponents need.
+static void mixed_state_in(SbeCtx* c, const double2* P, const double2* C, const double2* D,
+                           cudaStream_t s) {
+  Mixed* m = static_cast<Mixed*>(c->mixed);
+  const int nk = m->nk, nw = m->nw;
+  const long long mm = (long long)nk * nk, tm = c->tot_mat, vn = (long long)nw * nk;
+  float2* xf = reinterpret_cast<float2*>(c->xs);
+  cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+  cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
+  const int blocks = (int)std::min<long long>((mm + 255) / 256, 128);
+  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(P, nk, 0, m->mxS(), m->mxO(), xf, nullptr);
+  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(C, nk, 1, m->mxS(), m->mxO(), xf + tm, m->xdg);
+  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(D, nk, 1, m->mxS(), m->mxO(), xf + 2 * tm,
+                                              m->xdg + vn);
+}
+
+// One RHS evaluation of the mixed path on the FP32 stage state (P, C, D; the
+// FP64 diagonals of C and D in dgC, dgD; the state maxima already in mxS, mxO).
+static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2* D,
+                       const double* dgC, const double* dgD, const double2* Ek, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   const long long mm = (long long)nk * nk, tm = c->tot_mat;
@@ -1212,24 +1346,16 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   // eS: full state maximum (sheared exchange operands); eO: maximum over P and
   // the off-diagonal C, D (commutator operands; the diagonals of C and D are
   // peeled off and applied exactly in the epilogues)
-  if (!state_max_ready) {
-    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
-    const int blocks = (int)std::min<long long>((mm + 255) / 256, 128);
-    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(P, nk, 0, m->mxS(), m->mxO());
-    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(C, nk, 1, m->mxS(), m->mxO());
-    k_absmax2<<<dim3(blocks, nw), 256, 0, s>>>(D, nk, 1, m->mxS(), m->mxO());
-  }
   exponents_from(m, m->mxS(), m->eS(), s);
   exponents_from(m, m->mxO(), m->eO(), s);
-  const double2* st[3] = {P, C, D};
+  const float2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   const long long vn = (long long)nw * nk;
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw, m->tpart, 0,
-                                         m->cdf);
-  k_planes_nt<double2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw, m->tpart, 1,
-                                         m->cdf + 2 * vn);
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw, m->tpart, 0,
+                                        m->cdf, dgC);
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw, m->tpart, 1,
+                                        m->cdf + 2 * vn, dgD);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
   k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
@@ -1263,7 +1389,7 @@ static int mixed_stage(SbeCtx* c, const double2* P, const double2* C, const doub
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
   k_exponents2<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH());
   k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->pl, M_EH, M_EHT, nw);
-  k_hplanes<<<dim3((nk + 127) / 128, nk, nw), 128, 0, s>>>(
+  k_hplanes<<<dim3((nk + 31) / 32, (nk + 31) / 32, nw), dim3(32, 8), 0, s>>>(
       m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->pl, nw);
   k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eO(), m->eH(), m->esc());
   // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
@@ -1350,8 +1476,8 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     int rc = tc_gemm_launch(jobs, 3, s);
     if (rc) return rc;
   }
-  k_src_reduce_f<<<dim3((m->nr + 127) / 128, nw), 128, 0, s>>>(c->d_wires, m->ekrf, gf, c->tot_kr,
-                                                              c->window, src);
+  k_src_reduce_f<<<dim3((m->nr + 31) / 32, nw), dim3(32, 8), 0, s>>>(c->d_wires, m->ekrf, gf,
+                                                                    c->tot_kr, c->window, src);
   launch_sources_final(c, c->ne, c->nh, src, s);
   return cuda_check(cudaGetLastError(), "mixed sources");
 }
@@ -1370,10 +1496,12 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
   if (rc) return rc;
   rc = mixed_prep(c, C, D, s);
   if (rc) return rc;
-  rc = mixed_stage(c, P, C, D, Ek, 0, s);
-  if (rc) return rc;
   Mixed* m = static_cast<Mixed*>(c->mixed);
-  const long long n = c->tot_mat;
+  const long long n = c->tot_mat, vn = (long long)m->nw * m->nk;
+  mixed_state_in(c, P, C, D, s);
+  const float2* xf = reinterpret_cast<const float2*>(c->xs);
+  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, s);
+  if (rc) return rc;
   const int g = (int)((n + 255) / 256);
   k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf, dP);
   k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf + n, dC);
@@ -1392,24 +1520,21 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   const long long per = (long long)m->nk * m->nk;
   const int bpw = (int)std::min<long long>((per + 255) / 256, 64);
   const double frac[4] = {0.0, 0.5, 0.5, 1.0};
+  const long long vn = (long long)m->nw * m->nk;
+  float2* xf = reinterpret_cast<float2*>(c->xs);
+  mixed_state_in(c, P, C, D, s);
   for (int st = 1; st <= 4; ++st) {
-    const double2 *xp = P, *xc = C, *xd = D;
-    if (st > 1) {
-      xp = c->xs;
-      xc = c->xs + n;
-      xd = c->xs + 2 * n;
-    }
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
-    rc = mixed_stage(c, xp, xc, xd, c->ekst, st > 1, s);
+    rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, c->ekst, s);
     if (rc) return rc;
     // RK4 update; every stage also measures the maxima of the state it writes
     cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
     cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * m->nw, s);
     double2* X[3] = {P, C, D};
     for (int i = 0; i < 3; ++i)
-      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(m->nk, i > 0, st, (float)dt, X[i],
-                                                  m->accf + i * n, c->xs + i * n,
-                                                  m->kf + i * n, m->mxS(), m->mxO());
+      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(
+          m->nk, i > 0, st, (float)dt, X[i], m->accf + i * n, xf + i * n,
+          i > 0 ? m->xdg + (i - 1) * vn : nullptr, m->kf + i * n, m->mxS(), m->mxO());
   }
   mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
   return mixed_sources(c, P, C, D, src, 1, s);

@@ -66,6 +66,13 @@ __host__ __device__ inline long long plane_elem(const PlaneSet& p, int mat, int 
   return ((long long)(mat * p.nplanes + plane) * p.batch + b) * plane_slab(p) +
          tile_off(p.rows_pad, r, k);
 }
+// element offset of the 16-byte chunk j (columns 8j .. 8j + 7 of K-block kb) of
+// row r in slab (mat, plane, batch): the chunk stays contiguous under the swizzle
+__host__ __device__ inline long long chunk_elem(const PlaneSet& p, int mat, int plane, int b,
+                                                int r, int kb, int j) {
+  return ((long long)(mat * p.nplanes + plane) * p.batch + b) * plane_slab(p) +
+         ((long long)kb * p.rows_pad + r) * 32 + 8 * (j ^ ((r >> 1) & 3));
+}
 inline PlaneSet make_planeset(__half* ptr, int nmat, int nplanes, int batch, int rows, int K) {
   PlaneSet p{ptr, nmat, nplanes, batch, rows, K, (rows + 255) / 256 * 256, (K + 31) / 32 * 32};
   return p;
