@@ -919,10 +919,12 @@ __global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
 // dd = k2 - k1 + Nk - 1, read along rows (coalesced in k2).  The diagonal of
 // Hee / Hhh (gap + kinetic energy) is formed in FP64 into dgE / dgH and split into
 // FP32 hi / lo parts (dgf).  The block maximum of the operands goes to mx[b].
-__global__ void k_h_build(const WireDev* wires, const float2* ekf, const float* vsf,
-                          const double* Ee, const double* Eh, const float2* trf, const float* xsh,
-                          int have_x, float2* hf, long long tot_mat, double2* dgE, double2* dgH,
-                          float2* dgf, unsigned* mx) {
+__global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __restrict__ ekf,
+                          const float* __restrict__ vsf, const double* __restrict__ Ee,
+                          const double* __restrict__ Eh, const float2* __restrict__ trf,
+                          const float* __restrict__ xsh, int have_x, float2* __restrict__ hf,
+                          long long tot_mat, double2* __restrict__ dgE, double2* __restrict__ dgH,
+                          float2* __restrict__ dgf, unsigned* __restrict__ mx) {
   const WireDev& W = wires[blockIdx.z];
   const int nk = W.nk, b = blockIdx.z, nw = gridDim.z;
   const int k1 = blockIdx.y;
@@ -1058,60 +1060,98 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
 // occupations differ exactly), so it does not carry the GEMM's rounding.  The
 // result is exactly anti-Hermitian, which keeps C and D Hermitian.  A block owns
 // the tile pair (bi, bj), (bj, bi) with bi <= bj and reads each W and H' element
-// once.  W holds FP32 accumulator values; g[j] - g[i] comes from the hi / lo
-// FP32 parts of g.
-__global__ void k_antiherm(int nk, const float2* W, const float2* W2, const float2* Hp,
-                           const float2* X, const float2* ghi, const float2* glo,
-                           const float* chi, const float* clo, float2* out) {
-  // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results
+// once.  W arrives as three FP32 partials (the hi*hi products of the two K
+// halves and the hi*lo + lo*hi products); g[j] - g[i] comes from the hi / lo FP32
+// parts of g.
+__global__ void __launch_bounds__(256) k_antiherm(
+    int nk, const float2* __restrict__ W, const float2* __restrict__ W2,
+    const float2* __restrict__ W3, const float2* __restrict__ Hp, const float2* __restrict__ X,
+    const float2* __restrict__ ghi, const float2* __restrict__ glo, const float* __restrict__ chi,
+    const float* __restrict__ clo, float2* __restrict__ out) {
+  // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results;
+  // gv / cv: g (hi, lo) and c (hi, lo) at the tile's rows i0.. (0) and columns j0.. (1)
   __shared__ float2 tb[32][33], hb[32][33], vt[32][33];
+  __shared__ float2 gv[2][2][32];
+  __shared__ float cv[2][2][32];
   const int bi = blockIdx.y, bj = blockIdx.x;
   if (bi > bj) return;
-  const int b = blockIdx.z;
+  const int b = blockIdx.z, tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = bi * 32, j0 = bj * 32;
   const long long mb = (long long)b * nk * nk;
-  const float2* w = W + mb;
-  const float2* w2 = W2 + mb;
-  const float2* hp = Hp + mb;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int ib = j0 + r, jb = i0 + threadIdx.x;
-    const bool okb = ib < nk && jb < nk;
-    const long long ob = (long long)ib * nk + jb;
-    tb[r][threadIdx.x] = okb ? make_float2(w[ob].x + w2[ob].x, w[ob].y + w2[ob].y)
-                             : make_float2(0, 0);
-    hb[r][threadIdx.x] = okb ? hp[(long long)ib * nk + jb] : make_float2(0, 0);
+  if (ty < 2) {
+    const int k = (ty == 0 ? i0 : j0) + tx;
+    const long long v = (long long)b * nk + (k < nk ? k : 0);
+    gv[ty][0][tx] = ghi[v];
+    gv[ty][1][tx] = glo[v];
+    cv[ty][0][tx] = chi[v];
+    cv[ty][1][tx] = clo[v];
+  }
+  // the mirror tile: four rows per thread, loads issued together
+  {
+    float2 w[4][3], h[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int ib = j0 + ty + 8 * q, jb = i0 + tx;
+      const bool ok = ib < nk && jb < nk;
+      const long long ob = mb + (long long)(ok ? ib : 0) * nk + (ok ? jb : 0);
+      w[q][0] = W[ob];
+      w[q][1] = W2[ob];
+      w[q][2] = W3[ob];
+      h[q] = Hp[ob];
+      if (!ok) w[q][0] = w[q][1] = w[q][2] = h[q] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      tb[ty + 8 * q][tx] = make_float2((w[q][0].x + w[q][1].x) + w[q][2].x,
+                                       (w[q][0].y + w[q][1].y) + w[q][2].y);
+      hb[ty + 8 * q][tx] = h[q];
+    }
   }
   __syncthreads();
   const float ih = (float)(1.0 / kHbar);
-  const float2* gh = ghi + (long long)b * nk;
-  const float2* gl = glo + (long long)b * nk;
-  const float* ch = chi + (long long)b * nk;
-  const float* cl = clo + (long long)b * nk;
   // the tile (i0.., j0..): i <= j wherever it is written
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int i = i0 + r, j = j0 + threadIdx.x;
-    if (i >= nk || j >= nk) continue;
-    const long long oa = (long long)i * nk + j;
-    const float2 a = make_float2(w[oa].x + w2[oa].x, w[oa].y + w2[oa].y);   // W[i][j]
-    const float2 bt = tb[threadIdx.x][r];                   // W[j][i]
-    const float2 hji = hb[threadIdx.x][r];                  // H'[j][i]
-    const float2 x = X[mb + (long long)i * nk + j];
-    const float dr = (gh[j].x - gh[i].x) + (gl[j].x - gl[i].x);
-    const float di = (gh[j].y - gh[i].y) + (gl[j].y - gl[i].y);
-    const float dc = (ch[i] - ch[j]) + (cl[i] - cl[j]);
-    const float re = (a.x - bt.x) + dc * hji.x + (dr * x.x - di * x.y);
-    const float im = (a.y + bt.y) + dc * hji.y + (dr * x.y + di * x.x);
-    const float2 v = make_float2(im * ih, -re * ih);
-    vt[r][threadIdx.x] = v;
-    if (bi < bj || j >= i) out[mb + (long long)i * nk + j] = v;
+  {
+    float2 w[4][3], x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = i0 + ty + 8 * q, j = j0 + tx;
+      const bool ok = i < nk && j < nk;
+      const long long oa = mb + (long long)(ok ? i : 0) * nk + (ok ? j : 0);
+      w[q][0] = W[oa];
+      w[q][1] = W2[oa];
+      w[q][2] = W3[oa];
+      x[q] = X[oa];
+    }
+    const float2 gjh = gv[1][0][tx], gjl = gv[1][1][tx];
+    const float cjh = cv[1][0][tx], cjl = cv[1][1][tx];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = ty + 8 * q;
+      const int i = i0 + r, j = j0 + tx;
+      const float2 a = make_float2((w[q][0].x + w[q][1].x) + w[q][2].x,
+                                   (w[q][0].y + w[q][1].y) + w[q][2].y);   // W[i][j]
+      const float2 bt = tb[tx][r];                   // W[j][i]
+      const float2 hji = hb[tx][r];                  // H'[j][i]
+      const float2 gih = gv[0][0][r], gil = gv[0][1][r];
+      const float dr = (gjh.x - gih.x) + (gjl.x - gil.x);
+      const float di = (gjh.y - gih.y) + (gjl.y - gil.y);
+      const float dc = (cv[0][0][r] - cjh) + (cv[0][1][r] - cjl);
+      const float re = (a.x - bt.x) + dc * hji.x + (dr * x[q].x - di * x[q].y);
+      const float im = (a.y + bt.y) + dc * hji.y + (dr * x[q].y + di * x[q].x);
+      const float2 v = make_float2(im * ih, -re * ih);
+      vt[r][tx] = v;
+      if (i < nk && j < nk && (bi < bj || j >= i)) out[mb + (long long)i * nk + j] = v;
+    }
   }
   __syncthreads();
   // the mirror tile as the conjugate transpose: dX is Hermitian by construction
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int i = j0 + r, j = i0 + threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = ty + 8 * q;
+    const int i = j0 + r, j = i0 + tx;
     if (i >= nk || j >= nk) continue;
     if (bi < bj || i > j) {
-      const float2 v = vt[threadIdx.x][r];
+      const float2 v = vt[tx][r];
       out[mb + (long long)i * nk + j] = make_float2(v.x, -v.y);
     }
   }
@@ -1125,39 +1165,69 @@ __global__ void k_antiherm(int nk, const float2* W, const float2* W2, const floa
 // occupations c, d enter through the Pauli-blocking factor of the driving term and
 // the peeled energy diagonals ee, hh as hi + lo FP32 parts.  32 x 32 tiles; Heh^T
 // goes through shared memory so that every global access runs along rows.
-__global__ void k_rhs_p(int nk, int nw, const float2* G, const float2* hehf, const float2* X,
-                        const float2* dgf, const float* gamf, const float* cdf, float2* out) {
+__global__ void __launch_bounds__(256) k_rhs_p(
+    int nk, int nw, const float2* __restrict__ G, const float2* __restrict__ hehf,
+    const float2* __restrict__ X, const float2* __restrict__ dgf, const float* __restrict__ gamf,
+    const float* __restrict__ cdf, float2* __restrict__ out) {
   __shared__ float2 ht[32][33];
+  // per-row (kh = m0 + r) values: hh hi, lo; GamH; d hi, lo
+  __shared__ float2 rg[2][32];
+  __shared__ float rv[3][32];
   const int b = blockIdx.z;
   const int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
   const long long mb = (long long)b * nk * nk, vb = (long long)b * nk, vn = (long long)nw * nk;
-  const int tx = threadIdx.x;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int n = n0 + r, m = m0 + tx;
-    ht[r][tx] = (n < nk && m < nk) ? hehf[mb + (long long)n * nk + m] : make_float2(0.f, 0.f);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  {
+    float2 h[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int n = n0 + ty + 8 * q, m = m0 + tx;
+      const bool ok = n < nk && m < nk;
+      h[q] = hehf[mb + (long long)(ok ? n : 0) * nk + (ok ? m : 0)];
+      if (!ok) h[q] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ht[ty + 8 * q][tx] = h[q];
+  }
+  if (ty == 0) {
+    const long long v = vb + (m0 + tx < nk ? m0 + tx : 0);
+    rg[0][tx] = dgf[2 * vn + v];
+    rg[1][tx] = dgf[3 * vn + v];
+    rv[0][tx] = gamf[vn + v];
+    rv[1][tx] = cdf[2 * vn + v];
+    rv[2][tx] = cdf[3 * vn + v];
   }
   __syncthreads();
   const int n = n0 + tx;
-  if (n >= nk) return;
+  const bool on = n < nk;
   const float ih = (float)(1.0 / kHbar);
-  const float2 eh = dgf[vb + n], el = dgf[vn + vb + n];
-  const float gamE = gamf[vb + n];
-  const float chi = cdf[vb + n], clo = cdf[vn + vb + n];
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int m = m0 + r;
-    if (m >= nk) break;
-    const long long o = mb + (long long)m * nk + n;
+  const long long vnn = vb + (on ? n : 0);
+  const float2 eh = dgf[vnn], el = dgf[vn + vnn];
+  const float gamE = gamf[vnn];
+  const float chi = cdf[vnn], clo = cdf[vn + vnn];
+  float2 g[4], x[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int m = m0 + ty + 8 * q;
+    const bool ok = on && m < nk;
+    const long long o = mb + (long long)(ok ? m : 0) * nk + (ok ? n : 0);
+    g[q] = G[o];
+    x[q] = X[o];
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = ty + 8 * q, m = m0 + r;
+    if (!on || m >= nk) continue;
     const float2 h0 = ht[tx][r];   // Heh[ke = n][kh = m]
-    const float pb = ((1.f - chi) - cdf[2 * vn + vb + m]) - (clo + cdf[3 * vn + vb + m]);
-    const float2 g = G[o];
-    const float ax = g.x + pb * h0.x, ay = g.y + pb * h0.y;
-    const float2 x = X[o];
-    const float2 gh = dgf[2 * vn + vb + m], gl = dgf[3 * vn + vb + m];
+    const float pb = ((1.f - chi) - rv[1][r]) - (clo + rv[2][r]);
+    const float ax = g[q].x + pb * h0.x, ay = g[q].y + pb * h0.y;
+    const float2 gh = rg[0][r], gl = rg[1][r];
     const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
-    const float ar = ax + (der * x.x - dei * x.y);
-    const float ai = ay + (der * x.y + dei * x.x);
-    const float gam = gamE + gamf[vn + vb + m];
-    out[o] = make_float2(ai * ih - gam * x.x, -ar * ih - gam * x.y);
+    const float ar = ax + (der * x[q].x - dei * x[q].y);
+    const float ai = ay + (der * x[q].y + dei * x[q].x);
+    const float gam = gamE + rv[0][r];
+    out[mb + (long long)m * nk + n] =
+        make_float2(ai * ih - gam * x[q].x, -ar * ih - gam * x[q].y);
   }
 }
 
@@ -1248,12 +1318,14 @@ __global__ void k_add_int(int n, const int* a, const int* b, int* out) {
 
 static tc::GemmJob job(Mixed* m, const tc::PlaneSet& A, const tc::PlaneSet& B, int M, int N,
                        int K, int cplx, int nterms, const tc::Term* t, int kskip,
-                       const tc::EpiArgs& e, int split = 0, int ksplit = 1) {
+                       const tc::EpiArgs& e, int mode = tc::MODE_FULL, int xonly = 0,
+                       int ksplit = 1) {
   tc::GemmJob j{};
   tc::GemmDesc& d = j.d;
   d.A = A;
   d.B = B;
-  d.split = split;
+  d.mode = mode;
+  d.xonly = xonly;
   d.ksplit = ksplit;
   d.M = M;
   d.N = N;
@@ -1400,42 +1472,52 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
   const tc::Term* tl[3] = {tP, tC, tD};
   const int nt[3] = {4, 2, 2};
-  // W and V as two K halves each (partials summed in the anti-Hermitian pass):
-  // wf = [W lo, W hi, V lo, V hi]
-  float2* wf = reinterpret_cast<float2*>(c->G);
-  float2* gp = wf + 4 * tm;   // dP commutator sums (the buffer holds 12 tm float2)
-  float2* out[3] = {gp, wf, wf + 2 * tm};
-  // dP (one launch), then W and V in split-accumulator mode as two K halves each
-  // (one launch; their W - W^H is a small difference of large products near
-  // equilibrium)
-  tc::GemmJob jobs[3];
-  for (int w = 0; w < 3; ++w) {
+  // G buffer (FP32 complex, tm each): [W hh K-half 0, W hh K-half 1, V hh 0, V hh 1,
+  // dP sums, W cross terms, V cross terms]; the partials of W and V meet in the
+  // anti-Hermitian pass
+  float2* wf = reinterpret_cast<float2*>(c->G);   // the buffer holds 12 tm float2
+  float2* gp = wf + 4 * tm;
+  float2* wx = wf + 5 * tm;
+  float2* vx = wf + 6 * tm;
+  auto epi = [&](float2* out) {
     tc::EpiArgs e{};
     e.kind = tc::EPI_RAWF;
-    e.outf2 = out[w];
+    e.outf2 = out;
     e.out_bstride = mm;
     e.ks_stride = tm;
     e.escale = m->esc();
     e.err = m->err();
-    jobs[w] = (w == 0) ? job(m, m->pl, m->pl, nk, nk, nk, 1, nt[w], tl[w], 0, e)
-                       : job(m, m->pl, m->pl, nk, nk, nk, 1, nt[w], tl[w], 0, e, 1, 2);
-  }
+    return e;
+  };
+  // dP and the hi*lo + lo*hi parts of W and V in one launch; the hi*hi parts of W
+  // and V (their W - W^H is a small difference of large products near
+  // equilibrium) as two K halves each with one accumulator per real product
+  tc::GemmJob full[3] = {job(m, m->pl, m->pl, nk, nk, nk, 1, nt[0], tl[0], 0, epi(gp)),
+                         job(m, m->pl, m->pl, nk, nk, nk, 1, nt[1], tl[1], 0, epi(wx),
+                             tc::MODE_FULL, 1),
+                         job(m, m->pl, m->pl, nk, nk, nk, 1, nt[2], tl[2], 0, epi(vx),
+                             tc::MODE_FULL, 1)};
+  tc::GemmJob hh[2] = {job(m, m->pl, m->pl, nk, nk, nk, 1, nt[1], tl[1], 0, epi(wf),
+                           tc::MODE_HH, 0, 2),
+                       job(m, m->pl, m->pl, nk, nk, nk, 1, nt[2], tl[2], 0, epi(wf + 2 * tm),
+                           tc::MODE_HH, 0, 2)};
   {
     ProfScope ps(c, 0, s);
-    rc = tc_gemm_launch(jobs, 1, s);
+    rc = tc_gemm_launch(full, 3, s);
     if (rc) return rc;
   }
   {
     ProfScope ps(c, 0, s);
-    rc = tc_gemm_launch(jobs + 1, 2, s);
+    rc = tc_gemm_launch(hh, 2, s);
     if (rc) return rc;
   }
   const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
   k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp, m->hf, st[0], m->dgf, m->gamf, m->cdf, m->kf);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, wx, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
                                m->cdf + vn, m->kf + tm);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, m->hf + 2 * tm, D, m->dgf + 2 * vn,
-                               m->dgf + 3 * vn, m->cdf + 2 * vn, m->cdf + 3 * vn, m->kf + 2 * tm);
+  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, vx, m->hf + 2 * tm, D,
+                               m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn, m->cdf + 3 * vn,
+                               m->kf + 2 * tm);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 

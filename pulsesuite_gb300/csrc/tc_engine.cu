@@ -258,19 +258,21 @@ __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) 
 constexpr int SCR_BYTES = 4 * 32 * 33 * 8;   // epilogue transpose scratch, 4 warps
 constexpr int STAGE_AREA = 192 * 1024;
 
-template <int BNT, bool SPLIT>
+template <int BNT, int MODE>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_tc_gemm(const __grid_constant__ GemmLaunch L) {
   constexpr int BTB = BNT * BK * 2;   // B tile bytes per plane
+  constexpr bool HH = (MODE == MODE_HH);
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const bool cplx = L.job[0].d.complex_mode != 0;
-  const int npl = cplx ? 4 : 2;
+  // planes per operand tile in shared memory (MODE_HH: re_hi, im_hi)
+  const int npl = HH ? 2 : (cplx ? 4 : 2);
   const int stage_bytes = npl * (A_TILE_BYTES + BTB);
-  const int nstage = STAGE_AREA / stage_bytes;
+  const int nstage = min(8, STAGE_AREA / stage_bytes);
   // accumulator columns of one tile; two tiles in flight when they fit twice
-  const int tile_cols = SPLIT ? 8 * BNT : (cplx ? 2 * BNT : BNT);
+  const int tile_cols = HH ? 4 * BNT : (cplx ? 2 * BNT : BNT);
   const int nbuf = tile_cols <= 256 ? 2 : 1;
   float2* scr_all = reinterpret_cast<float2*>(smem + STAGE_AREA);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGE_AREA + SCR_BYTES);
@@ -327,11 +329,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const long long ta = ((long long)kb * d.A.rows_pad + ti.m0) * BK;   // tile start in a slab
         const long long tb = ((long long)kb * d.B.rows_pad + ti.n0) * BK;
         for (int p = 0; p < npl; ++p) {
+          const int src = HH ? 2 * p : p;   // MODE_HH: planes re_hi, im_hi
           const __half* ga = d.A.ptr +
-                             ((long long)(T.a_mat * d.A.nplanes + p) * d.A.batch + ti.b) *
+                             ((long long)(T.a_mat * d.A.nplanes + src) * d.A.batch + ti.b) *
                                  plane_slab(d.A) + ta;
           const __half* gb = d.B.ptr +
-                             ((long long)(T.b_mat * d.B.nplanes + p) * d.B.batch + ti.b) *
+                             ((long long)(T.b_mat * d.B.nplanes + src) * d.B.batch + ti.b) *
                                  plane_slab(d.B) + tb;
           bulk_load(sa + p * A_TILE_BYTES, ga, A_TILE_BYTES, &full[s]);
           bulk_load(sb + p * BTB, gb, BTB, &full[s]);
@@ -353,6 +356,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     for (long long t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++lt) {
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
+      const bool hh = !d.xonly;
       const int buf = lt % nbuf, use = lt / nbuf;
       if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) break;
       tc_fence_after();
@@ -381,38 +385,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             umma_f16(acc_re, A(0), B(1), id, 1u);
             umma_f16(acc_re, A(1), B(0), id, 1u);
           } else {
-            // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
             const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
             const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
             const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
             const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
             const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
-            if (SPLIT) {
-              // accumulators (BNT columns each): rr hi*hi, rr hi*lo+lo*hi, ii .., ..,
-              // ri .., .., ir .., ..: every truncating chain is a third to a sixth as long
+            if (HH) {
+              // planes 0 re_hi, 1 im_hi; accumulators (BNT columns each) rr, ii, ri, ir
               umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
-              umma_f16(tmem + 1 * BNT, A(0), B(1), irr, acc);
-              umma_f16(tmem + 1 * BNT, A(1), B(0), irr, 1u);
-              umma_f16(tmem + 2 * BNT, A(2), B(2), iii, acc);
-              umma_f16(tmem + 3 * BNT, A(2), B(3), iii, acc);
-              umma_f16(tmem + 3 * BNT, A(3), B(2), iii, 1u);
-              umma_f16(tmem + 4 * BNT, A(0), B(2), iri, acc);
-              umma_f16(tmem + 5 * BNT, A(0), B(3), iri, acc);
-              umma_f16(tmem + 5 * BNT, A(1), B(2), iri, 1u);
-              umma_f16(tmem + 6 * BNT, A(2), B(0), iir, acc);
-              umma_f16(tmem + 7 * BNT, A(2), B(1), iir, acc);
-              umma_f16(tmem + 7 * BNT, A(3), B(0), iir, 1u);
+              umma_f16(tmem + 1 * BNT, A(1), B(1), iii, acc);
+              umma_f16(tmem + 2 * BNT, A(0), B(1), iri, acc);
+              umma_f16(tmem + 3 * BNT, A(1), B(0), iir, acc);
             } else {
-              umma_f16(acc_re, A(0), B(0), irr, acc);
-              umma_f16(acc_re, A(0), B(1), irr, 1u);
+              // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
+              uint32_t ar = acc, ai = acc;
+              if (hh) {
+                umma_f16(acc_re, A(0), B(0), irr, ar);
+                umma_f16(acc_re, A(2), B(2), iii, 1u);
+                umma_f16(acc_im, A(0), B(2), iri, ai);
+                umma_f16(acc_im, A(2), B(0), iir, 1u);
+                ar = ai = 1u;
+              }
+              umma_f16(acc_re, A(0), B(1), irr, ar);
               umma_f16(acc_re, A(1), B(0), irr, 1u);
-              umma_f16(acc_re, A(2), B(2), iii, 1u);
               umma_f16(acc_re, A(2), B(3), iii, 1u);
               umma_f16(acc_re, A(3), B(2), iii, 1u);
-              umma_f16(acc_im, A(0), B(2), iri, acc);
-              umma_f16(acc_im, A(0), B(3), iri, 1u);
+              umma_f16(acc_im, A(0), B(3), iri, ai);
               umma_f16(acc_im, A(1), B(2), iri, 1u);
-              umma_f16(acc_im, A(2), B(0), iir, 1u);
               umma_f16(acc_im, A(2), B(1), iir, 1u);
               umma_f16(acc_im, A(3), B(0), iir, 1u);
             }
@@ -444,70 +443,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
       const bool have = ti.n_iters > 0;
-      if (SPLIT) {
-        // read and sum all eight accumulators, release tensor memory, then store
-        float re[BNT / 32][32], im[BNT / 32][32];
+      for (int c = 0; c < BNT / 32; ++c) {
+        float re[32], im[32];
+        if (have && HH) {
+          // re = rr + ii, im = ri + ir (signs applied by the MMAs)
+          float t0[32];
+          tmem_ld32(lane_addr + 0 * BNT + c * 32, re);
+          tmem_ld32(lane_addr + 1 * BNT + c * 32, t0);
 #pragma unroll
-        for (int c = 0; c < BNT / 32; ++c) {
-          if (have) {
-            // re = (rr hh + rr hl/lh) + (ii hh + ii hl/lh), im likewise from ri, ir
+          for (int j = 0; j < 32; ++j) re[j] += t0[j];
+          tmem_ld32(lane_addr + 2 * BNT + c * 32, im);
+          tmem_ld32(lane_addr + 3 * BNT + c * 32, t0);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const uint32_t a0 = lane_addr + c * 32 + h * 16;
-              float* r = re[c] + h * 16;
-              float* i = im[c] + h * 16;
-              float t0[16], t1[16];
-              tmem_ld16(a0 + 0 * BNT, r);
-              tmem_ld16(a0 + 1 * BNT, t0);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) r[j] += t0[j];
-              tmem_ld16(a0 + 2 * BNT, t0);
-              tmem_ld16(a0 + 3 * BNT, t1);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) r[j] += t0[j] + t1[j];
-              tmem_ld16(a0 + 4 * BNT, i);
-              tmem_ld16(a0 + 5 * BNT, t0);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) i[j] += t0[j];
-              tmem_ld16(a0 + 6 * BNT, t0);
-              tmem_ld16(a0 + 7 * BNT, t1);
-#pragma unroll
-              for (int j = 0; j < 16; ++j) i[j] += t0[j] + t1[j];
-            }
+          for (int j = 0; j < 32; ++j) im[j] += t0[j];
+        } else if (have) {
+          tmem_ld32(lane_addr + c * 32, re);
+          if (cplx) {
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 32, im);
           } else {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) re[c][j] = im[c][j] = 0.f;
+            for (int j = 0; j < 32; ++j) im[j] = 0.f;
           }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) re[j] = im[j] = 0.f;
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&tempty[buf]);
-#pragma unroll
-        for (int c = 0; c < BNT / 32; ++c)
-          epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re[c], im[c], scr);
-      } else {
-        for (int c = 0; c < BNT / 32; ++c) {
-          float re[32], im[32];
-          if (have) {
-            tmem_ld32(lane_addr + c * 32, re);
-            if (cplx) {
-              tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 32, im);
-            } else {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) im[j] = 0.f;
-            }
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) re[j] = im[j] = 0.f;
-          }
-          if (c == BNT / 32 - 1) {
-            // last read of this tile's accumulators
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[buf]);
-          }
-          epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re, im, scr);
+        if (c == BNT / 32 - 1) {
+          // last read of this tile's accumulators
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[buf]);
         }
+        epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re, im, scr);
       }
     }
   }
@@ -529,9 +496,9 @@ static const int kTcSmem = 1024 + tc::STAGE_AREA + tc::SCR_BYTES + 256;
 int tc_gemm_init() {
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN, false>,
+    if (cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN, tc::MODE_FULL>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN_SPLIT, true>,
+        cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN_HH, tc::MODE_HH>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess)
       return fail(SBE_ERR_CUDA, "tc_gemm: cannot raise the shared-memory limit");
     attr = true;
@@ -572,17 +539,18 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   if (njobs < 1 || njobs > tc::MAX_JOBS) return fail(SBE_ERR_ARG, "tc_gemm: 1 to 4 jobs per launch");
   tc::GemmLaunch L{};
   L.njobs = njobs;
-  const bool split = jobs[0].d.split != 0;
+  const int mode = jobs[0].d.mode;
   const int cplx = jobs[0].d.complex_mode;
-  const int bnt = split ? tc::BN_SPLIT : tc::BN;
+  if (mode != tc::MODE_FULL && mode != tc::MODE_HH) return fail(SBE_ERR_ARG, "tc_gemm: bad mode");
+  const int bnt = mode == tc::MODE_HH ? tc::BN_HH : tc::BN;
   long long nt = 0;
   for (int j = 0; j < njobs; ++j) {
     const tc::GemmDesc& d = jobs[j].d;
     if (!job_ok(d)) return fail(SBE_ERR_ARG, "tc_gemm: operand plane sets do not cover the launch");
-    if ((d.split != 0) != split || d.complex_mode != cplx)
+    if (d.mode != mode || d.complex_mode != cplx)
       return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode");
-    if (split && (!d.complex_mode || d.kskip))
-      return fail(SBE_ERR_ARG, "tc_gemm: split-accumulator mode is complex and unskipped only");
+    if ((mode == tc::MODE_HH || d.xonly) && (!d.complex_mode || d.kskip))
+      return fail(SBE_ERR_ARG, "tc_gemm: hi*hi and cross-term modes are complex and unskipped only");
     if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
     L.job[j] = jobs[j];
     L.tile_base[j] = nt;
@@ -591,10 +559,10 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   }
   L.tile_base[njobs] = nt;
   const int grid = (int)std::min<long long>(nt, num_sms());
-  if (split)
-    tc::k_tc_gemm<tc::BN_SPLIT, true><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
+  if (mode == tc::MODE_HH)
+    tc::k_tc_gemm<tc::BN_HH, tc::MODE_HH><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
   else
-    tc::k_tc_gemm<tc::BN, false><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
+    tc::k_tc_gemm<tc::BN, tc::MODE_FULL><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
   return cuda_check(cudaGetLastError(), "tc_gemm launch");
 }
 

@@ -29,7 +29,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BN = 256;
-constexpr int BN_SPLIT = 64;   // N tile of the split-accumulator mode
+constexpr int BN_HH = 128;     // N tile of the hi*hi mode
 constexpr int BK = 32;
 constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
@@ -105,6 +105,8 @@ struct EpiArgs {
   int* err;                   // error flag (bounded waits)
 };
 
+enum Mode : int { MODE_FULL = 0, MODE_HH = 1 };
+
 struct GemmDesc {
   int M, N, K;                // per batch
   int complex_mode;           // 1: 4 planes per matrix, 2 accumulators; 0: 2 planes, 1 acc
@@ -113,12 +115,16 @@ struct GemmDesc {
   int batch;
   int kskip;                  // exchange: K range limited by the sheared N tile
   int nk_shear;               // exchange: Nk of the shear
-  // split-accumulator mode (complex only): N tile 64 and eight FP32 accumulators,
-  // one per (real product, hi*hi or hi*lo + lo*hi) pair, summed in the epilogue.
-  // The tensor core's accumulation truncates; splitting the sums shortens each
-  // truncating chain (for products whose result is a small difference of large
-  // sums, e.g. the W - W^H form of dC, dD).
-  int split;
+  // Product modes.  MODE_FULL: hi*hi + hi*lo + lo*hi (N tile 256); with xonly set
+  // (complex only) the hi*hi products are left out.  MODE_HH (complex only): the
+  // hi*hi products alone, N tile 128, one FP32 accumulator per real product
+  // (rr, ii, ri, ir), summed in the epilogue.  The tensor core's accumulation
+  // truncates at every MMA, so a product whose result is a small difference of
+  // large sums (the W - W^H form of dC, dD) takes its hi*hi part in MODE_HH with
+  // split-K (short truncating chains) and its hi*lo + lo*hi part, 2^-11 smaller,
+  // through xonly.
+  int mode;
+  int xonly;
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
   // written at out + ks * ks_stride (ksplit 0 counts as 1)
   int ksplit;
@@ -130,7 +136,7 @@ struct GemmJob {
   EpiArgs e;
 };
 
-// one launch: the concatenated tile lists of njobs jobs (same complex/split mode)
+// one launch: the concatenated tile lists of njobs jobs (same mode and complex flag)
 struct GemmLaunch {
   GemmJob job[MAX_JOBS];
   long long tile_base[MAX_JOBS + 1];
