@@ -162,10 +162,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 // transposed through the warp's shared-memory scratch (32 x 33 float2) so that
 // every global access of the column pass runs along n (lane = column).
 __device__ __forceinline__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b,
-                                               int mrow0, int n0, long long ooff, float* re,
-                                               float* im, float2* scr) {
+                                               int mrow0, int n0, long long ooff, int es,
+                                               float* re, float* im, float2* scr) {
   const int lane = threadIdx.x & 31;
-  const int es = -e.escale[b];
   if (e.kind == EPI_F32) {
     // real mode: each lane stores its row's 128 contiguous bytes directly
     const int m = mrow0 + lane;
@@ -279,8 +278,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   uint64_t* empty = full + 8;
   uint64_t* tfull = empty + 8;
   uint64_t* tempty = tfull + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+  // tile queue: the producer takes tiles from the launch's counter (dynamic
+  // scheduling) and hands each tile index to the MMA issuer and the epilogue
+  uint64_t* qfull = tempty + 2;
+  uint64_t* qempty = qfull + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(qempty + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* tq = abort_flag + 1;   // 4 queue entries
   int* err = L.job[0].e.err;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x & 31;
@@ -294,6 +298,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
       mbar_init(&tempty[i], 4);   // one arrival per epilogue warp
+    }
+    for (int i = 0; i < 4; ++i) {
+      mbar_init(&qfull[i], 1);
+      mbar_init(&qempty[i], 5);   // the MMA issuer and one arrival per epilogue warp
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -311,7 +319,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- bulk-copy producer ----------------
     long long g = 0;   // stage-ring position (runs on across tiles)
     bool ok = true;
-    for (long long t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+    for (int k = 0; ok; ++k) {
+      const int qs = k & 3;
+      if (!mbar_wait(&qempty[qs], (uint32_t)(((k >> 2) & 1) ^ 1), err, abort_flag)) break;
+      const long long t = atomicAdd(L.sched, 1);
+      tq[qs] = t < ntiles ? (int)t : -1;
+      mbar_arrive(&qfull[qs]);   // release: the entry is visible to the waiters
+      if (t >= ntiles) break;
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       for (int it = 0; it < ti.n_iters; ++it, ++g) {
@@ -351,9 +365,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- MMA issuer ----------------
     const uint32_t id_pos = idesc_f16(BM, BNT, 0), id_neg = idesc_f16(BM, BNT, 1);
     long long g = 0;
-    int lt = 0;
     bool ok = true;
-    for (long long t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++lt) {
+    for (int lt = 0; ok; ++lt) {
+      const int qs = lt & 3;
+      if (!mbar_wait(&qfull[qs], (uint32_t)((lt >> 2) & 1), err, abort_flag)) break;
+      const int t = tq[qs];
+      mbar_arrive(&qempty[qs]);
+      if (t < 0) break;
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const bool hh = !d.xonly;
@@ -431,14 +449,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- epilogue ----------------
     const int q = warp & 3;                 // TMEM lane quarter of this warp
     float2* scr = scr_all + (warp - 2) * (32 * 33);
-    int lt = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+    for (int lt = 0;; ++lt) {
+      const int qs = lt & 3;
+      if (!mbar_wait(&qfull[qs], (uint32_t)((lt >> 2) & 1), err, abort_flag)) break;
+      const int t = tq[qs];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&qempty[qs]);
+      if (t < 0) break;
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const EpiArgs& e = L.job[ti.job].e;
       const int buf = lt % nbuf, use = lt / nbuf;
       const int mrow0 = ti.m0 + 32 * q;
       const long long ooff = (long long)ti.ks * e.ks_stride;
+      // the tile's scale, loaded before the wait (a dependent load per chunk would
+      // cost a memory latency each)
+      const int es = -e.escale[ti.b];
       if (!mbar_wait(&tfull[buf], (uint32_t)(use & 1), err, abort_flag)) break;
       tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
@@ -474,7 +500,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, re, im, scr);
+        epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, es, re, im, scr);
       }
     }
   }
@@ -491,10 +517,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // ---------------------------------------------------------------------------
 // host side
 
-static const int kTcSmem = 1024 + tc::STAGE_AREA + tc::SCR_BYTES + 256;
+static const int kTcSmem = 1024 + tc::STAGE_AREA + tc::SCR_BYTES + 512;
+
+// per-launch tile counters of the dynamic scheduler (cycled; each launch zeroes its own)
+static int* g_sched = nullptr;
+static unsigned g_sched_seq = 0;
+constexpr int kSchedSlots = 1024;
 
 int tc_gemm_init() {
   static bool attr = false;
+  if (!g_sched && cudaMalloc(&g_sched, sizeof(int) * kSchedSlots) != cudaSuccess) {
+    g_sched = nullptr;
+    return fail(SBE_ERR_OOM, "tc_gemm: scheduler counters");
+  }
   if (!attr) {
     if (cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN, tc::MODE_FULL>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
@@ -558,6 +593,10 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
           (d.ksplit > 1 ? d.ksplit : 1);
   }
   L.tile_base[njobs] = nt;
+  if (nt == 0) return SBE_OK;
+  L.sched = g_sched + (g_sched_seq++ % kSchedSlots);
+  if (cudaMemsetAsync(L.sched, 0, sizeof(int), s) != cudaSuccess)
+    return cuda_check(cudaGetLastError(), "tc_gemm scheduler reset");
   const int grid = (int)std::min<long long>(nt, num_sms());
   if (mode == tc::MODE_HH)
     tc::k_tc_gemm<tc::BN_HH, tc::MODE_HH><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);

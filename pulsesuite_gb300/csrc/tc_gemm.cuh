@@ -141,6 +141,7 @@ struct GemmLaunch {
   GemmJob job[MAX_JOBS];
   long long tile_base[MAX_JOBS + 1];
   int njobs;
+  int* sched;                 // tile counter of this launch (zeroed before it)
 };
 
 }  // namespace tc
