@@ -328,30 +328,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (t >= ntiles) break;
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
-      for (int it = 0; it < ti.n_iters; ++it, ++g) {
-        const int s = (int)(g % nstage);
-        const uint32_t ph = (uint32_t)((g / nstage) & 1);
-        if (!mbar_wait(&empty[s], ph ^ 1u, err, abort_flag)) {
-          ok = false;
-          break;
-        }
-        const Term T = d.t[it / ti.nkb];
-        const int kb = ti.kb_begin + it % ti.nkb;
-        uint8_t* sa = smem + s * stage_bytes;
-        uint8_t* sb = sa + npl * A_TILE_BYTES;
-        mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
-        const long long ta = ((long long)kb * d.A.rows_pad + ti.m0) * BK;   // tile start in a slab
-        const long long tb = ((long long)kb * d.B.rows_pad + ti.n0) * BK;
-        for (int p = 0; p < npl; ++p) {
-          const int src = HH ? 2 * p : p;   // MODE_HH: planes re_hi, im_hi
-          const __half* ga = d.A.ptr +
-                             ((long long)(T.a_mat * d.A.nplanes + src) * d.A.batch + ti.b) *
-                                 plane_slab(d.A) + ta;
-          const __half* gb = d.B.ptr +
-                             ((long long)(T.b_mat * d.B.nplanes + src) * d.B.batch + ti.b) *
-                                 plane_slab(d.B) + tb;
-          bulk_load(sa + p * A_TILE_BYTES, ga, A_TILE_BYTES, &full[s]);
-          bulk_load(sb + p * BTB, gb, BTB, &full[s]);
+      // slab strides (elements) of the operand planes; K-block kb of a tile starts
+      // at kb * rows_pad * BK within its slab
+      const long long sA = plane_slab(d.A), sB = plane_slab(d.B);
+      const long long kstepA = (long long)d.A.rows_pad * BK, kstepB = (long long)d.B.rows_pad * BK;
+      const int pstep = HH ? 2 : 1;   // MODE_HH loads planes re_hi, im_hi
+      int s = (int)(g % nstage);
+      uint32_t ph = (uint32_t)((g / nstage) & 1);
+      for (int term = 0; ok && term < d.nterms && ti.nkb > 0; ++term) {
+        const Term T = d.t[term];
+        const __half* ga0 = d.A.ptr + ((long long)T.a_mat * d.A.nplanes * d.A.batch + ti.b) * sA +
+                            ((long long)ti.kb_begin * d.A.rows_pad + ti.m0) * BK;
+        const __half* gb0 = d.B.ptr + ((long long)T.b_mat * d.B.nplanes * d.B.batch + ti.b) * sB +
+                            ((long long)ti.kb_begin * d.B.rows_pad + ti.n0) * BK;
+        const long long pA = (long long)pstep * d.A.batch * sA, pB = (long long)pstep * d.B.batch * sB;
+        for (int kk = 0; kk < ti.nkb; ++kk, ++g) {
+          if (!mbar_wait(&empty[s], ph ^ 1u, err, abort_flag)) {
+            ok = false;
+            break;
+          }
+          uint8_t* sa = smem + s * stage_bytes;
+          uint8_t* sb = sa + npl * A_TILE_BYTES;
+          mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+          const __half* ga = ga0 + kk * kstepA;
+          const __half* gb = gb0 + kk * kstepB;
+          for (int p = 0; p < npl; ++p) {
+            bulk_load(sa + p * A_TILE_BYTES, ga + p * pA, A_TILE_BYTES, &full[s]);
+            bulk_load(sb + p * BTB, gb + p * pB, BTB, &full[s]);
+          }
+          if (++s == nstage) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
       }
     }
@@ -380,35 +388,37 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tc_fence_after();
       const uint32_t acc_re = tmem + buf * 256, acc_im = tmem + 256;
       bool first = true;
-      for (int it = 0; it < ti.n_iters; ++it, ++g) {
-        const int s = (int)(g % nstage);
-        const uint32_t ph = (uint32_t)((g / nstage) & 1);
-        if (!mbar_wait(&full[s], ph, err, abort_flag)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const Term T = d.t[it / ti.nkb];
-        const uint32_t sa = smem_u32(smem + s * stage_bytes);
-        const uint32_t sb = sa + npl * A_TILE_BYTES;
+      int s = (int)(g % nstage);
+      uint32_t ph = (uint32_t)((g / nstage) & 1);
+      for (int term = 0; ok && term < d.nterms && ti.nkb > 0; ++term) {
+        const Term T = d.t[term];
+        const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
+        const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
+        const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
+        const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
+        const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
+        for (int kk = 0; kk < ti.nkb; ++kk, ++g) {
+          if (!mbar_wait(&full[s], ph, err, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          // descriptors of the stage's planes: the start-address field (16-byte
+          // units, bits 0-13) takes the plane and K offsets without carry
+          const uint64_t da = sw64_desc(smem_u32(smem + s * stage_bytes));
+          const uint64_t db = da + (uint64_t)((npl * A_TILE_BYTES) >> 4);
 #pragma unroll
-        for (int k16 = 0; k16 < BK / 16; ++k16) {
-          const uint32_t ko = k16 * 32;   // bytes along the 64-byte row
-          auto A = [&](int p) { return sw64_desc(sa + p * A_TILE_BYTES + ko); };
-          auto B = [&](int p) { return sw64_desc(sb + p * BTB + ko); };
-          const uint32_t acc = first ? 0u : 1u;
-          if (!cplx) {
-            const uint32_t id = T.sign < 0 ? id_neg : id_pos;
-            umma_f16(acc_re, A(0), B(0), id, acc);
-            umma_f16(acc_re, A(0), B(1), id, 1u);
-            umma_f16(acc_re, A(1), B(0), id, 1u);
-          } else {
-            const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
-            const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
-            const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
-            const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
-            const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
-            if (HH) {
+          for (int k16 = 0; k16 < BK / 16; ++k16) {
+            const uint32_t ko = k16 * 2;   // 32 bytes along the 64-byte row
+            auto A = [&](int p) { return da + (uint64_t)(p * (A_TILE_BYTES >> 4) + ko); };
+            auto B = [&](int p) { return db + (uint64_t)(p * (BTB >> 4) + ko); };
+            const uint32_t acc = first ? 0u : 1u;
+            if (!cplx) {
+              const uint32_t id = T.sign < 0 ? id_neg : id_pos;
+              umma_f16(acc_re, A(0), B(0), id, acc);
+              umma_f16(acc_re, A(0), B(1), id, 1u);
+              umma_f16(acc_re, A(1), B(0), id, 1u);
+            } else if (HH) {
               // planes 0 re_hi, 1 im_hi; accumulators (BNT columns each) rr, ii, ri, ir
               umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
               umma_f16(tmem + 1 * BNT, A(1), B(1), iii, acc);
@@ -433,10 +443,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               umma_f16(acc_im, A(2), B(1), iir, 1u);
               umma_f16(acc_im, A(3), B(0), iir, 1u);
             }
+            first = false;
           }
-          first = false;
+          umma_commit(&empty[s]);
+          if (++s == nstage) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
-        umma_commit(&empty[s]);
       }
       // accumulators of this tile complete (a tile without K blocks leaves tensor
       // memory untouched and its epilogue stores zeros)
