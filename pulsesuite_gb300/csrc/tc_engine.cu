@@ -156,33 +156,44 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Epilogue parameters of one tile, read from the launch parameters once per tile
+// (values in registers: a parameter read inside the chunk loop would put a
+// dependent load into every chunk).  Output pointers are offset to the tile's
+// batch entry and K part.
+struct EpiTile {
+  int kind, M, N, cplx, es;
+  float* of;      // EPI_F32
+  float2* of2;    // EPI_RAWF
+  double2* od;    // EPI_RAW
+};
+
+__device__ __forceinline__ EpiTile epi_tile(const GemmDesc& d, const EpiArgs& e, int b, int ks) {
+  EpiTile t;
+  t.kind = e.kind;
+  t.M = d.M;
+  t.N = d.N;
+  t.cplx = d.complex_mode;
+  t.es = -e.escale[b];
+  const long long off = (long long)ks * e.ks_stride + (long long)b * e.out_bstride;
+  t.of = e.outf ? e.outf + off : nullptr;
+  t.of2 = e.outf2 ? e.outf2 + off : nullptr;
+  t.od = e.out ? e.out + off : nullptr;
+  return t;
+}
+
 // Epilogue of one 32-column chunk (columns n0 .. n0 + 31) of the warp's 32 rows
 // mrow0 + lane.  re[j], im[j] arrive in the TMEM orientation (lane = row, j =
-// column); the terms indexed along rows are added there, then the chunk is
-// transposed through the warp's shared-memory scratch (32 x 33 float2) so that
-// every global access of the column pass runs along n (lane = column).
-__device__ __forceinline__ void epilogue_chunk(const GemmDesc& d, const EpiArgs& e, int b,
-                                               int mrow0, int n0, long long ooff, int es,
-                                               float* re, float* im, float2* scr) {
+// column); the chunk is transposed through the warp's shared-memory scratch
+// (32 x 33 float2) so that every global store runs along n (lane = column).  The
+// column pass reads all 32 values into registers before it stores (shared and
+// global accesses through generic pointers would otherwise serialise on the
+// shared-memory latency, one row at a time).
+__device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int n0, float* re,
+                                               float* im, float2* scr) {
   const int lane = threadIdx.x & 31;
-  if (e.kind == EPI_F32) {
-    // real mode: each lane stores its row's 128 contiguous bytes directly
-    const int m = mrow0 + lane;
-    if (m >= d.M) return;
-    float* o = e.outf + ooff + (long long)b * e.out_bstride + (long long)m * d.N + n0;
-    if (n0 + 32 <= d.N) {
-      float4* o4 = reinterpret_cast<float4*>(o);
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        o4[j] = make_float4(f32_ldexp(re[4 * j], es), f32_ldexp(re[4 * j + 1], es),
-                            f32_ldexp(re[4 * j + 2], es), f32_ldexp(re[4 * j + 3], es));
-    } else {
-      for (int j = 0; j < 32 && n0 + j < d.N; ++j) o[j] = f32_ldexp(re[j], es);
-    }
-    return;
-  }
+  const int es = t.es;
   // ---- row pass
-  if (e.kind != EPI_RAW) {
+  if (t.kind != EPI_RAW) {
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
       re[j] = f32_ldexp(re[j], es);
@@ -193,24 +204,33 @@ __device__ __forceinline__ void epilogue_chunk(const GemmDesc& d, const EpiArgs&
   for (int j = 0; j < 32; ++j) scr[j * 33 + lane] = make_float2(re[j], im[j]);
   __syncwarp();
   // ---- column pass
-  const int n = n0 + lane;
-  const int rmax = min(32, d.M - mrow0);
-  if (n < d.N) {
-    const long long base = ooff + (long long)b * e.out_bstride + (long long)mrow0 * d.N + n;
-#pragma unroll 8
-    for (int r = 0; r < rmax; ++r) {
-      const float2 v = scr[lane * 33 + r];
-      const long long o = base + (long long)r * d.N;
-      if (e.kind == EPI_RAWF) {
-        e.outf2[o] = v;
-      } else {
-        // EPI_RAW: exact widening and power-of-two scaling on the integer pipe
-        e.out[o] = make_double2(f32_to_f64_scaled(v.x, es),
-                                d.complex_mode ? f32_to_f64_scaled(v.y, es) : 0.0);
-      }
-    }
-  }
+  float2 v[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) v[r] = scr[lane * 33 + r];
   __syncwarp();
+  const int n = n0 + lane;
+  const int rmax = min(32, t.M - mrow0);
+  if (n >= t.N) return;
+  const long long base = (long long)mrow0 * t.N + n;
+  if (t.kind == EPI_RAWF) {
+    float2* o = t.of2 + base;
+#pragma unroll
+    for (int r = 0; r < 32; ++r)
+      if (r < rmax) o[(long long)r * t.N] = v[r];
+  } else if (t.kind == EPI_F32) {
+    float* o = t.of + base;
+#pragma unroll
+    for (int r = 0; r < 32; ++r)
+      if (r < rmax) o[(long long)r * t.N] = v[r].x;
+  } else {
+    // EPI_RAW: exact widening and power-of-two scaling on the integer pipe
+    double2* o = t.od + base;
+#pragma unroll
+    for (int r = 0; r < 32; ++r)
+      if (r < rmax)
+        o[(long long)r * t.N] = make_double2(f32_to_f64_scaled(v[r].x, es),
+                                             t.cplx ? f32_to_f64_scaled(v[r].y, es) : 0.0);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -475,10 +495,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const EpiArgs& e = L.job[ti.job].e;
       const int buf = lt % nbuf, use = lt / nbuf;
       const int mrow0 = ti.m0 + 32 * q;
-      const long long ooff = (long long)ti.ks * e.ks_stride;
-      // the tile's scale, loaded before the wait (a dependent load per chunk would
-      // cost a memory latency each)
-      const int es = -e.escale[ti.b];
+      const EpiTile et = epi_tile(d, e, ti.b, ti.ks);   // before the wait
       if (!mbar_wait(&tfull[buf], (uint32_t)(use & 1), err, abort_flag)) break;
       tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
@@ -514,7 +531,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        epilogue_chunk(d, e, ti.b, mrow0, ti.n0 + c * 32, ooff, es, re, im, scr);
+        epilogue_chunk(et, mrow0, ti.n0 + c * 32, re, im, scr);
       }
     }
   }
