@@ -502,33 +502,36 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
 // set the FP64 real diagonal (the occupations of C and D, which the peeled terms
 // use beyond FP32).  The diagonal is tracked by a row / column counter stepped
 // with the grid stride (no division per element).
-__global__ void k_state_in(const double2* X, int nk, int peel, unsigned* mx, unsigned* mo,
-                           float2* xf, double* dg) {
+__global__ void __launch_bounds__(256) k_state_in(const double2* __restrict__ X, int nk, int peel,
+                                                  unsigned* __restrict__ mx,
+                                                  unsigned* __restrict__ mo,
+                                                  float2* __restrict__ xf, double* __restrict__ dg) {
   const int b = blockIdx.y;
   const long long per = (long long)nk * nk;
   const double2* x = X + (long long)b * per;
   float2* y = xf + (long long)b * per;
   unsigned long long m = 0, o = 0;
-  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // four elements per thread and pass, loads issued together
   const long long S = (long long)gridDim.x * blockDim.x;
-  int row = (int)(i0 / nk), col = (int)(i0 % nk);
-  const int srow = (int)(S / nk), scol = (int)(S % nk);
-  for (long long i = i0; i < per; i += S) {
-    const double2 v = x[i];
-    y[i] = f64_to_f32(v);
-    const unsigned long long a = max(absbits(v.x), absbits(v.y));
-    m = max(m, a);
-    if (row == col) {
-      if (dg) dg[(long long)b * nk + row] = v.x;
-      if (!peel) o = max(o, a);
-    } else {
-      o = max(o, a);
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < per; i0 += 4 * S) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long long i = i0 + u * S;
+      v[u] = i < per ? x[i] : make_double2(0.0, 0.0);
     }
-    col += scol;
-    row += srow;
-    if (col >= nk) {
-      col -= nk;
-      ++row;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long long i = i0 + u * S;
+      if (i >= per) break;
+      y[i] = f64_to_f32(v[u]);
+      const unsigned long long a = max(absbits(v[u].x), absbits(v[u].y));
+      m = max(m, a);
+      // the diagonal: i = k (nk + 1)  (nk^2 < 2^31)
+      const int ii = (int)i;
+      const bool diag = (ii % (nk + 1)) == 0;
+      if (diag && dg) dg[(long long)b * nk + ii / (nk + 1)] = v[u].x;
+      if (!(diag && peel)) o = max(o, a);
     }
   }
   for (int k = 16; k > 0; k >>= 1) {

@@ -138,24 +138,6 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N, int negA) {
 // ---------------------------------------------------------------------------
 // epilogues
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // Epilogue parameters of one tile, read from the launch parameters once per tile
 // (values in registers: a parameter read inside the chunk loop would put a
 // dependent load into every chunk).  Output pointers are offset to the tile's
@@ -181,13 +163,15 @@ __device__ __forceinline__ EpiTile epi_tile(const GemmDesc& d, const EpiArgs& e,
   return t;
 }
 
-// Epilogue of one 32-column chunk (columns n0 .. n0 + 31) of the warp's 32 rows
+// Epilogue of one 16-column chunk (columns n0 .. n0 + 15) of the warp's 32 rows
 // mrow0 + lane.  re[j], im[j] arrive in the TMEM orientation (lane = row, j =
 // column); the chunk is transposed through the warp's shared-memory scratch
-// (32 x 33 float2) so that every global store runs along n (lane = column).  The
-// column pass reads all 32 values into registers before it stores (shared and
-// global accesses through generic pointers would otherwise serialise on the
-// shared-memory latency, one row at a time).
+// (32 x 16 float2, column slot j ^ (row & 15) so that both passes are free of
+// bank conflicts) so that every global store runs along n: in the column pass
+// lanes 0-15 and 16-31 take the columns of two rows at a time.  The column pass
+// reads its 16 values into registers before it stores (shared and global
+// accesses through generic pointers would otherwise serialise on the
+// shared-memory latency).
 __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int n0, float* re,
                                                float* im, float2* scr) {
   const int lane = threadIdx.x & 31;
@@ -195,41 +179,46 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
   // ---- row pass
   if (t.kind != EPI_RAW) {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < 16; ++j) {
       re[j] = f32_ldexp(re[j], es);
       im[j] = f32_ldexp(im[j], es);
     }
   }
 #pragma unroll
-  for (int j = 0; j < 32; ++j) scr[j * 33 + lane] = make_float2(re[j], im[j]);
+  for (int j = 0; j < 16; ++j) scr[lane * 16 + (j ^ (lane & 15))] = make_float2(re[j], im[j]);
   __syncwarp();
-  // ---- column pass
-  float2 v[32];
+  // ---- column pass: lane -> column j, rows rh, rh + 2, ...
+  const int j = lane & 15, rh = lane >> 4;
+  float2 v[16];
 #pragma unroll
-  for (int r = 0; r < 32; ++r) v[r] = scr[lane * 33 + r];
+  for (int i = 0; i < 16; ++i) {
+    const int r = 2 * i + rh;
+    v[i] = scr[r * 16 + (j ^ (r & 15))];
+  }
   __syncwarp();
-  const int n = n0 + lane;
+  const int n = n0 + j;
   const int rmax = min(32, t.M - mrow0);
   if (n >= t.N) return;
-  const long long base = (long long)mrow0 * t.N + n;
+  const long long base = (long long)(mrow0 + rh) * t.N + n;
+  const long long rs = 2 * (long long)t.N;
   if (t.kind == EPI_RAWF) {
     float2* o = t.of2 + base;
 #pragma unroll
-    for (int r = 0; r < 32; ++r)
-      if (r < rmax) o[(long long)r * t.N] = v[r];
+    for (int i = 0; i < 16; ++i)
+      if (2 * i + rh < rmax) o[i * rs] = v[i];
   } else if (t.kind == EPI_F32) {
     float* o = t.of + base;
 #pragma unroll
-    for (int r = 0; r < 32; ++r)
-      if (r < rmax) o[(long long)r * t.N] = v[r].x;
+    for (int i = 0; i < 16; ++i)
+      if (2 * i + rh < rmax) o[i * rs] = v[i].x;
   } else {
     // EPI_RAW: exact widening and power-of-two scaling on the integer pipe
     double2* o = t.od + base;
 #pragma unroll
-    for (int r = 0; r < 32; ++r)
-      if (r < rmax)
-        o[(long long)r * t.N] = make_double2(f32_to_f64_scaled(v[r].x, es),
-                                             t.cplx ? f32_to_f64_scaled(v[r].y, es) : 0.0);
+    for (int i = 0; i < 16; ++i)
+      if (2 * i + rh < rmax)
+        o[i * rs] = make_double2(f32_to_f64_scaled(v[i].x, es),
+                                 t.cplx ? f32_to_f64_scaled(v[i].y, es) : 0.0);
   }
 }
 
@@ -274,7 +263,8 @@ __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) 
   return ti;
 }
 
-constexpr int SCR_BYTES = 4 * 32 * 33 * 8;   // epilogue transpose scratch, 4 warps
+constexpr int EPI_WARPS = 8;
+constexpr int SCR_BYTES = EPI_WARPS * 32 * 16 * 8;   // epilogue transpose scratch per warp
 constexpr int STAGE_AREA = 192 * 1024;
 
 template <int BNT, int MODE>
@@ -317,11 +307,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 4);   // one arrival per epilogue warp
+      mbar_init(&tempty[i], EPI_WARPS);   // one arrival per epilogue warp
     }
     for (int i = 0; i < 4; ++i) {
       mbar_init(&qfull[i], 1);
-      mbar_init(&qempty[i], 5);   // the MMA issuer and one arrival per epilogue warp
+      mbar_init(&qempty[i], 1 + EPI_WARPS);   // the MMA issuer and each epilogue warp
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -482,7 +472,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
     const int q = warp & 3;                 // TMEM lane quarter of this warp
-    float2* scr = scr_all + (warp - 2) * (32 * 33);
+    float2* scr = scr_all + (warp - 2) * (32 * 16);
+    const int half = (warp - 2) >> 2;         // column half of the tile
     for (int lt = 0;; ++lt) {
       const int qs = lt & 3;
       if (!mbar_wait(&qfull[qs], (uint32_t)((lt >> 2) & 1), err, abort_flag)) break;
@@ -500,38 +491,40 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
       const bool have = ti.n_iters > 0;
-      for (int c = 0; c < BNT / 32; ++c) {
-        float re[32], im[32];
+      constexpr int NCH = BNT / 32;   // 16-column chunks per column half
+      for (int cc = 0; cc < NCH; ++cc) {
+        const int c = half * NCH + cc;   // chunk of the tile
+        float re[16], im[16];
         if (have && HH) {
           // re = rr + ii, im = ri + ir (signs applied by the MMAs)
-          float t0[32];
-          tmem_ld32(lane_addr + 0 * BNT + c * 32, re);
-          tmem_ld32(lane_addr + 1 * BNT + c * 32, t0);
+          float t0[16];
+          tmem_ld16(lane_addr + 0 * BNT + c * 16, re);
+          tmem_ld16(lane_addr + 1 * BNT + c * 16, t0);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) re[j] += t0[j];
-          tmem_ld32(lane_addr + 2 * BNT + c * 32, im);
-          tmem_ld32(lane_addr + 3 * BNT + c * 32, t0);
+          for (int j = 0; j < 16; ++j) re[j] += t0[j];
+          tmem_ld16(lane_addr + 2 * BNT + c * 16, im);
+          tmem_ld16(lane_addr + 3 * BNT + c * 16, t0);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) im[j] += t0[j];
+          for (int j = 0; j < 16; ++j) im[j] += t0[j];
         } else if (have) {
-          tmem_ld32(lane_addr + c * 32, re);
+          tmem_ld16(lane_addr + c * 16, re);
           if (cplx) {
-            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 32, im);
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 16, im);
           } else {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) im[j] = 0.f;
+            for (int j = 0; j < 16; ++j) im[j] = 0.f;
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) re[j] = im[j] = 0.f;
+          for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
         }
-        if (c == BNT / 32 - 1) {
-          // last read of this tile's accumulators
+        if (cc == NCH - 1) {
+          // last read of this tile's accumulators by this warp
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        epilogue_chunk(et, mrow0, ti.n0 + c * 32, re, im, scr);
+        epilogue_chunk(et, mrow0, ti.n0 + c * 16, re, im, scr);
       }
     }
   }

@@ -17,9 +17,10 @@
 // may span several GEMMs of the same shape class (jobs) and K parts of each.
 // Warp roles: warp 0 issues the bulk copies through a ring of stages that runs
 // on across tiles, warp 1 owns tensor memory and issues tcgen05.mma from one
-// thread, warps 2-5 read the accumulators (tcgen05.ld) and run the epilogue of
-// tile i while the copies (and, when the accumulators fit twice in tensor
-// memory, the MMAs) of tile i + 1 proceed.
+// thread, warps 2-9 read the accumulators (tcgen05.ld; two warps per TMEM lane
+// quarter, one per column half) and run the epilogue of tile i while the copies
+// (and, when the accumulators fit twice in tensor memory, the MMAs) of tile
+// i + 1 proceed.
 #pragma once
 #include <cuda_fp16.h>
 #include <cstdint>
@@ -33,7 +34,7 @@ constexpr int BN_HH = 128;     // N tile of the hi*hi mode
 constexpr int BK = 32;
 constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
-constexpr int NUM_THREADS = 192;
+constexpr int NUM_THREADS = 320;   // producer warp, MMA warp, 8 epilogue warps
 constexpr int MAX_TERMS = 4;
 constexpr int MAX_JOBS = 4;
 // bounded waits: an iteration limit after which the kernel flags an error
