@@ -61,9 +61,9 @@ FLAGS = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, 
              LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel err"
 # dram__bytes_read.sum + dram__bytes_write.sum of the commutator launches of one RHS
-# evaluation (dP: 184.87 + 1.60 MB; W, V halves: 4 x 33.6 MB read, 0.92 MB written in
-# all), 8 wires x Nk = 512 (ncu), per wire
-TRAFFIC_PER_EVAL_WIRE = (184.87e6 + 1.60e6 + 134.50e6 + 0.92e6) / 8
+# evaluation (dP with the hi*lo + lo*hi products of W and V: 200.05 + 22.92 MB; the
+# hi*hi products of W and V: 67.20 + 14.03 MB), 8 wires x Nk = 512 (ncu), per wire
+TRAFFIC_PER_EVAL_WIRE = (200.05e6 + 22.92e6 + 67.20e6 + 14.03e6) / 8
 
 
 def wire_L(nk, kmax):
@@ -407,9 +407,10 @@ def gpu_arm(args, wl):
                             "evaluation (ncu, 8-wire case, scaled by wires)",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
                            "12 complex Nk^3 products) over the summed CUDA-event time of the "
-                           "evaluation's commutator launches (dP; W and V as two K halves each "
-                           "in split-accumulator mode); executed 192*Nk^3 (8 complex products "
-                           "x 4 real products x 3 hi/lo terms)"}
+                           "evaluation's two commutator launches (dP with the hi*lo + lo*hi "
+                           "products of W and V; the hi*hi products of W and V as two K halves "
+                           "with one accumulator per real product); executed 192*Nk^3 (8 complex "
+                           "products x 4 real products x 3 hi/lo terms)"}
     other = {name: {"ms_per_step": prof[c][0] / args.steps, "launches": prof[c][1]}
              for c, name in ((1, "exchange_gemm"), (2, "source_gemm"), (3, "dephasing_fp32"))}
     other["pstd_field_step"] = {"ms_per_step": pstd_ms, "launches": 6}
