@@ -182,6 +182,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   add((void**)&c->occf, 4 * 2 * ov);
   add((void**)&c->dconst, 4 * 16 * (size_t)n_wires);
   add((void**)&c->dpre, 4 * 4 * ov);
+  add((void**)&c->dwl, sizeof(int) * (size_t)n_wires);
   size_t total = 0;
   for (auto& p : parts) total += (p.bytes + 255) / 256 * 256;
   if (cudaMalloc(&c->arena, total) != cudaSuccess) {
@@ -205,6 +206,28 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   }
   cudaMemcpyAsync(c->d_wires, c->wires.data(), sizeof(WireDev) * n_wires, cudaMemcpyHostToDevice,
                   s);
+  // dephasing groups: wires whose Lorentzian factors coincide (same Nk, masses, grid
+  // spacing and broadening rates) share them in the FP32 dephasing sums
+  {
+    std::vector<int> order;
+    std::vector<char> used(n_wires, 0);
+    for (int a = 0; a < n_wires; ++a) {
+      if (used[a]) continue;
+      const WireDev& A = c->wires[a];
+      const int first = (int)order.size();
+      for (int b = a; b < n_wires; ++b) {
+        const WireDev& B = c->wires[b];
+        if (used[b] || B.nk != A.nk || B.dnk != A.dnk || B.me != A.me || B.mh != A.mh ||
+            B.dkr != A.dkr || B.gam_e != A.gam_e || B.gam_h != A.gam_h || B.gam_eh != A.gam_eh)
+          continue;
+        used[b] = 1;
+        order.push_back(b);
+      }
+      c->dgroups.emplace_back(first, (int)order.size() - first);
+    }
+    c->dwl_host = order;
+    cudaMemcpyAsync(c->dwl, c->dwl_host.data(), sizeof(int) * n_wires, cudaMemcpyHostToDevice, s);
+  }
   int rc = build_tables(c, s);
   if (rc == SBE_OK) rc = cuda_check(cudaStreamSynchronize(s), "sbe_ctx_create: table build");
   if (rc != SBE_OK) {

@@ -50,6 +50,12 @@ struct SbeCtx {
   float* dconst = nullptr;               // 16*nw FP32 dephasing constants
   float* dpre = nullptr;                 // 4*tot_vec FP32 dephasing prefactors per |q|
 
+  int* dwl = nullptr;                    // nw wire indices, grouped (dephasing groups)
+  // groups of wires with identical dephasing constants (Nk, masses, grid, rates):
+  // (first index into dwl, count)
+  std::vector<std::pair<int, int>> dgroups;
+  std::vector<int> dwl_host;              // host copy of dwl
+
   int any_offdiag = 0;                   // some wire has OffDiagDph on
   void* mixed = nullptr;                 // mixed-precision workspace (sbe_tc.cu)
 

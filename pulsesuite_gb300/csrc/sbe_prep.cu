@@ -261,10 +261,11 @@ __global__ void k_occf(const WireDev* wires, const double2* ne, const double2* n
 //   sa(-q, k + q) = sb(q, k) [+ the a-a term p = q],  sb(-q, k + q) = sa(q, k) [+ ..]
 // and a block writes D[q][k] and D[-q][k + q] for every k with k + q < Nk, and
 // the zeros of both rows elsewhere; the Lorentzian sums are formed once.
-__global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const float* occf,
+__global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const int* wl,
+                                                     const float* occf,
                                                      const float* dconst, const float* dpre,
                                                      double* De, double* Dh) {
-  const int wi = blockIdx.z >> 1, which = blockIdx.z & 1;   // 0 De, 1 Dh
+  const int wi = wl[blockIdx.z >> 1], which = blockIdx.z & 1;   // 0 De, 1 Dh
   const WireDev& W = wires[wi];
   const int nk = W.nk;
   const int q = blockIdx.y;   // 0 .. nk; row -q from the same sums
@@ -390,6 +391,198 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
   }
 }
 
+// The same sums for a group of NW wires that share their Lorentzian factors (same
+// Nk, masses, grid and rates): each Lorentzian is formed once and applied to every
+// wire's occupation weights, which carry the per-wire prefactors V_aa(q)^2 /
+// (hbar b_aa), V_ab(q)^2 / (hbar b_ab) (folded in, so one pair of sums per wire:
+// X = (vaa sa + vab ta, vaa sb + vab tb)).  Each thread sums KPT consecutive k for
+// all NW wires, so that every shared-memory weight load (32 p at a time, [p][wire]
+// as float2, read as float4) feeds 2 KPT FMAs; the a-a Lorentzian window slides in
+// registers.  Rows q and -q as in k_offdiag_D32.  grid (Nk / (128 KPT), Nk + 1, species).
+template <int NW, int KPT>
+__global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, const int* wl,
+                                                      int nwl, const float* occf,
+                                                      const float* dconst, const float* dpre,
+                                                      double* De, double* Dh) {
+  constexpr int PC = 32;   // p per shared-memory chunk
+  const int which = blockIdx.z;
+  const WireDev& W0 = wires[wl[0]];
+  const int nk = W0.nk;
+  const int q = blockIdx.y;
+  if (q > nk) return;
+  extern __shared__ __align__(16) float sh[];
+  float2* ws = reinterpret_cast<float2*>(sh);   // [PC][NW]
+  float* Ltab = sh + 2 * PC * NW;               // 2nk entries: m - mlo
+  __shared__ float svaa[NW], svab[NW], sn0[NW], snq[NW];
+  __shared__ int soa[NW], sob[NW];              // occupation offsets of species a, b
+  const int tid = threadIdx.x;
+  const float* cw = dconst + (long long)(2 * wl[0] + which) * 8;
+  const float alpha = cw[0] * (float)q;
+  const float bah = cw[1], bal = cw[2], bbh = cw[3], bbl = cw[4];
+  const int mlo = -nk + 1 + q;
+  for (int i = tid; i < 2 * nk; i += blockDim.x) {
+    const float u = alpha * (float)(mlo + i);
+    Ltab[i] = 1.0f / (1.0f + u * u);
+  }
+  const bool inq = q >= 1 && q < nk;   // V(q) vanishes at q = 0 and |q| = Nk
+  if (tid < NW) {
+    float vaa = 0.f, vab = 0.f, n0 = 0.f, nq = 0.f;
+    int oa = 0, ob = 0;
+    if (tid < nwl) {
+      const WireDev& W = wires[wl[tid]];
+      oa = (int)(2 * W.off_vec + (which == 0 ? 0 : nk));
+      ob = (int)(2 * W.off_vec + (which == 0 ? nk : 0));
+      const float* pq = dpre + 2 * (2 * W.off_vec + (long long)which * nk);
+      if (inq) {
+        vaa = pq[2 * q];
+        vab = pq[2 * q + 1];
+      }
+      n0 = occf[oa];
+      nq = q < nk ? occf[oa + q] : 0.f;
+    }
+    svaa[tid] = vaa;
+    svab[tid] = vab;
+    sn0[tid] = n0;
+    snq[tid] = nq;
+    soa[tid] = oa;
+    sob[tid] = ob;
+  }
+  const int k0 = (blockIdx.x * blockDim.x + tid) * KPT;   // this thread's first k
+  float ax[KPT][NW], ay[KPT][NW];
+#pragma unroll
+  for (int j = 0; j < KPT; ++j)
+#pragma unroll
+    for (int w = 0; w < NW; ++w) ax[j][w] = ay[j][w] = 0.f;
+  if (inq) {
+    // a-a: p in [q + 1, Nk - 1], Lorentzian of alpha q (k - p + q) from the table;
+    // index of (k, p) is k - p + Nk - 1: the window holds k0 .. k0 + KPT - 1
+    float l[KPT];
+    {
+      const int i0 = k0 - (q + 1) + nk - 1;
+#pragma unroll
+      for (int j = 0; j < KPT; ++j) l[j] = 0.f;
+      __syncthreads();   // the table is complete
+#pragma unroll
+      for (int j = 0; j < KPT; ++j)
+        if (i0 + j >= 0 && i0 + j < 2 * nk) l[j] = Ltab[i0 + j];
+    }
+    for (int p0 = q + 1; p0 < nk; p0 += PC) {
+      __syncthreads();
+      for (int i = tid; i < PC * NW; i += blockDim.x) {
+        const int pp = i / NW, w = i % NW, p = p0 + pp;
+        float2 v = make_float2(0.f, 0.f);
+        if (p < nk && w < nwl) {
+          const float* na = occf + soa[w];
+          const float npm = na[p - q], np_ = na[p], f = svaa[w];
+          v = make_float2(f * (npm * (1.f - np_)), f * ((1.f - npm) * np_));
+        }
+        ws[i] = v;
+      }
+      __syncthreads();
+      const int pend = min(PC, nk - p0);
+      for (int pp = 0; pp < pend; ++pp) {
+        const float4* w4 = reinterpret_cast<const float4*>(ws + pp * NW);
+#pragma unroll
+        for (int w2 = 0; w2 < NW / 2; ++w2) {
+          const float4 v = w4[w2];
+#pragma unroll
+          for (int j = 0; j < KPT; ++j) {
+            ax[j][2 * w2] = fmaf(l[j], v.x, ax[j][2 * w2]);
+            ay[j][2 * w2] = fmaf(l[j], v.y, ay[j][2 * w2]);
+            ax[j][2 * w2 + 1] = fmaf(l[j], v.z, ax[j][2 * w2 + 1]);
+            ay[j][2 * w2 + 1] = fmaf(l[j], v.w, ay[j][2 * w2 + 1]);
+          }
+        }
+        // next p: every index - 1
+#pragma unroll
+        for (int j = KPT - 1; j > 0; --j) l[j] = l[j - 1];
+        const int in = k0 - (p0 + pp + 1) + nk - 1;
+        l[0] = (in >= 0 && in < 2 * nk) ? Ltab[in] : 0.f;
+      }
+    }
+    // a-b: p in [0, Nk - 1 - q], u = q (A (2k + c) + B (2p + c)) with exact heads
+    const int c = -2 * W0.dnk - 1 + q;
+    float ka[KPT], kal[KPT];
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+      const float fk = (float)(2 * (k0 + j) + c);
+      ka[j] = bah * fk;   // exact head product
+      kal[j] = bal * fk;  // tail
+    }
+    const float fq = (float)q;
+    const int phi = nk - 1 - q;
+    for (int p0 = 0; p0 <= phi; p0 += PC) {
+      __syncthreads();
+      for (int i = tid; i < PC * NW; i += blockDim.x) {
+        const int pp = i / NW, w = i % NW, p = p0 + pp;
+        float2 v = make_float2(0.f, 0.f);
+        if (p <= phi && w < nwl) {
+          const float* nb = occf + sob[w];
+          const float npq = nb[p + q], np_ = nb[p], f = svab[w];
+          v = make_float2(f * (npq * (1.f - np_)), f * ((1.f - npq) * np_));
+        }
+        ws[i] = v;
+      }
+      __syncthreads();
+      const int pend = min(PC, phi + 1 - p0);
+      float fp = (float)(2 * p0 + c);   // exact small integers, stepped by 2
+      for (int pp = 0; pp < pend; ++pp, fp += 2.0f) {
+        const float hb = bbh * fp, tb = bbl * fp;
+        float L[KPT];
+#pragma unroll
+        for (int j = 0; j < KPT; ++j) {
+          const float sv = (ka[j] + hb) + (kal[j] + tb);
+          const float u = fq * sv;
+          // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L[j]) : "f"(fmaf(u, u, 1.0f)));
+        }
+        const float4* w4 = reinterpret_cast<const float4*>(ws + pp * NW);
+#pragma unroll
+        for (int w2 = 0; w2 < NW / 2; ++w2) {
+          const float4 v = w4[w2];
+#pragma unroll
+          for (int j = 0; j < KPT; ++j) {
+            ax[j][2 * w2] = fmaf(L[j], v.x, ax[j][2 * w2]);
+            ay[j][2 * w2] = fmaf(L[j], v.y, ay[j][2 * w2]);
+            ax[j][2 * w2 + 1] = fmaf(L[j], v.z, ax[j][2 * w2 + 1]);
+            ay[j][2 * w2 + 1] = fmaf(L[j], v.w, ay[j][2 * w2 + 1]);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < KPT; ++j) {
+    const int k = k0 + j;
+    if (k >= nk) break;
+    const float lq = q > 0 ? Ltab[k + nk - 1 - q] : 0.f;   // L(alpha q k): a-a term p = q of row -q
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      if (w >= nwl) break;
+      const WireDev& W = wires[wl[w]];
+      double* D = (which == 0 ? De : Dh) + W.off_dd;
+      double* Dp = D + (long long)(nk + q) * nk;   // row q
+      double* Dm = D + (long long)(nk - q) * nk;   // row -q
+      const float* na = occf + soa[w];
+      if (k + q >= nk) {
+        Dp[k] = 0.0;
+        if (q > 0) Dm[k - (nk - q)] = 0.0;
+        continue;
+      }
+      const float nak = na[k];
+      Dp[k] = f32_to_f64((1.f - nak) * ax[j][w] + nak * ay[j][w]);
+      if (q > 0) {
+        const float f = svaa[w] * lq;
+        const float xa = ay[j][w] + f * ((1.f - sn0[w]) * snq[w]);
+        const float xb = ax[j][w] + f * (sn0[w] * (1.f - snq[w]));
+        const float nk2 = na[k + q];
+        Dm[k + q] = f32_to_f64((1.f - nk2) * xa + nk2 * xb);
+      }
+    }
+  }
+}
+
 // Constants of k_offdiag_D32 (FP64, once per step): per (wire, species)
 // [2 c_a dkr^2 / b_aa, head/tail of c_a dkr^2 / b_ab, head/tail of c_b dkr^2 / b_ab]
 // and per |q| the prefactors V_aa(q)^2 / (hbar b_aa) and V_ab(q)^2 / (hbar b_ab)
@@ -420,13 +613,36 @@ __global__ void k_deph_consts(const WireDev* wires, const double* vs, float* dco
 
 void launch_offdiag_D(SbeCtx* c, int w_only, const double* g3, bool fp32, cudaStream_t s) {
   if (fp32 && w_only < 0 && !g3) {
-    size_t smem = sizeof(float) * 8 * (size_t)c->nk_max;
     k_occf<<<dim3((c->nk_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, c->ne, c->nh,
                                                                  c->occf);
     k_deph_consts<<<dim3((c->nk_max + 127) / 128, 2 * c->nw), 128, 0, s>>>(c->d_wires, c->vs,
                                                                           c->dconst, c->dpre);
-    k_offdiag_D32<<<dim3((c->nk_max + 511) / 512, c->nk_max + 1, 2 * c->nw), 128, smem, s>>>(
-        c->d_wires, c->occf, c->dconst, c->dpre, c->De, c->Dh);
+    // groups of 4 or more wires share the Lorentzian factors (chunks of up to 16
+    // wires); the other wires take the per-wire kernel, one launch each
+    for (const auto& g : c->dgroups) {
+      const int gk = c->wires[c->dwl_host[g.first]].nk;
+      if (g.second < 4) {
+        const size_t sm1 = sizeof(float) * 8 * (size_t)gk;
+        for (int i = 0; i < g.second; ++i)
+          k_offdiag_D32<<<dim3((gk + 511) / 512, gk + 1, 2), 128, sm1, s>>>(
+              c->d_wires, c->dwl + g.first + i, c->occf, c->dconst, c->dpre, c->De, c->Dh);
+        continue;
+      }
+      const dim3 grid((gk + 511) / 512, gk + 1, 2);   // 128 threads x 4 k
+      for (int o = 0; o < g.second; o += 16) {
+        const int n = std::min(16, g.second - o);
+        const int* wl = c->dwl + g.first + o;
+        if (n <= 8) {
+          const size_t sm = sizeof(float) * (2 * 32 * 8 + 2 * (size_t)gk);
+          k_offdiag_D32g<8, 4><<<grid, 128, sm, s>>>(c->d_wires, wl, n, c->occf, c->dconst,
+                                                      c->dpre, c->De, c->Dh);
+        } else {
+          const size_t sm = sizeof(float) * (2 * 32 * 16 + 2 * (size_t)gk);
+          k_offdiag_D32g<16, 4><<<grid, 128, sm, s>>>(c->d_wires, wl, n, c->occf, c->dconst,
+                                                       c->dpre, c->De, c->Dh);
+        }
+      }
+    }
     return;
   }
   dim3 g((c->nk_max + 127) / 128, 2 * (2 * c->nk_max + 1), w_only >= 0 ? 1 : c->nw);

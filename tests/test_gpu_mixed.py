@@ -148,28 +148,58 @@ def test_mixed_rk4_pulse_vs_fp64(nk):
         assert rel(ctx.rvec(sm, w, 5)[:3], ctx.rvec(s64, w, 5)[:3]) < 1e-5
 
 
-@pytest.mark.parametrize("nk", [16, 48, 256])
-def test_fp32_dephasing_sums_vs_fp64(nk):
-    """The mixed path's FP32 off-diagonal dephasing sums (rows -q formed from the
-    sums of row q) against the FP64 reference loops, every row and wire."""
-    nw = 2
-    ctx, _ = make_ctx(nk, nw)
-    rng = np.random.default_rng(100 + nk)
-    st = [seeded(rng, nk) for _ in range(nw)]
-    C = ctx.pack([s[1] for s in st])
-    D = ctx.pack([s[2] for s in st])
+def _deph_check(ctx, nks, C, D):
     De64, Dh64 = ctx.deph(C, D, fp32=False)
     De32, Dh32 = ctx.deph(C, D, fp32=True)
     ctx.check()
-    rows = 2 * nk + 1
-    for a, b, n in ((De32, De64, "De"), (Dh32, Dh64, "Dh")):
-        a = a.reshape(nw, rows, nk)
-        b = b.reshape(nw, rows, nk)
-        # the band structure (zeros where k + q leaves the grid) is exact
-        assert torch.equal(a == 0, b == 0), n
-        for w in range(nw):
-            e = rel(a[w], b[w])
-            assert e < 2e-6, (nk, n, w, e)
+    off = 0
+    for w, nk in enumerate(nks):
+        rows = 2 * nk + 1
+        n = rows * nk
+        for a, b, name in ((De32, De64, "De"), (Dh32, Dh64, "Dh")):
+            aw = a[off:off + n].reshape(rows, nk)
+            bw = b[off:off + n].reshape(rows, nk)
+            # the band structure (zeros where k + q leaves the grid) is exact
+            assert torch.equal(aw == 0, bw == 0), (name, w)
+            e = rel(aw, bw)
+            assert e < 2e-6, (nk, name, w, e)
             # rows q and -q separately: a wrong mirror shows in one half only
             for half in (slice(0, nk), slice(nk + 1, rows)):
-                assert rel(a[w, half], b[w, half]) < 2e-6, (nk, n, w, half)
+                assert rel(aw[half], bw[half]) < 2e-6, (nk, name, w, half)
+        off += n
+
+
+# 2 wires: the per-wire kernel; 6 and 20 identical wires: one group sharing its
+# Lorentzian factors (chunks of 8 and 32 wires, partly filled)
+@pytest.mark.parametrize("nk,nw", [(16, 2), (48, 2), (256, 2), (48, 6), (256, 20)])
+def test_fp32_dephasing_sums_vs_fp64(nk, nw):
+    """The mixed path's FP32 off-diagonal dephasing sums (rows -q formed from the
+    sums of row q) against the FP64 reference loops, every row and wire."""
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(100 + nk + nw)
+    st = [seeded(rng, nk) for _ in range(nw)]
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    _deph_check(ctx, [nk] * nw, C, D)
+
+
+def test_fp32_dephasing_mixed_groups():
+    """Wires of two lengths and two masses: a group of five, a group of four and two
+    single wires, interleaved in the context."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk = 48
+    L0 = np.pi / (3e9 / (nk / 2 - 0.5))
+    kinds = [0, 1, 0, 2, 0, 1, 0, 1, 3, 0, 1]
+    specs = []
+    for w, kd in enumerate(kinds):
+        mat = dict(MAT)
+        L = L0 * (1.25 if kd in (1, 3) else 1.0)
+        if kd >= 2:
+            mat["me"] = 0.07 * O.ME0 if kd == 2 else 0.06 * O.ME0
+        specs.append(WireSpec(nk=nk, L=L, temp=300.0, wire_index=w + 1, flags=dict(ALL), **mat))
+    ctx = WireContext(specs)
+    rng = np.random.default_rng(7)
+    st = [seeded(rng, nk) for _ in kinds]
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    _deph_check(ctx, [nk] * len(kinds), C, D)
