@@ -1053,6 +1053,72 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
   }
 }
 
+// RK4 stage update fused into the element-wise RHS passes (k_rhs_p, k_antiherm):
+// the stage derivative k of an element is used where it is formed.  The
+// arithmetic is that of the RK4 of the mixed path: FP32 k and sums k1 + 2 k2 +
+// 2 k3; stages 1-3 write the next stage state in FP32 (xf = fp32(X) + f k) and,
+// for C and D, its real diagonal in FP64; stage 4 adds to the FP64 state.  The
+// maxima of the written state (all elements in mx, off-diagonal ones in mo when
+// peel) feed the next stage's exponents.  stage 0: no update (the RHS is stored).
+struct Rk4Ctl {
+  int stage, peel;
+  float dt;
+  double2* X;      // FP64 state of this matrix, all wires
+  float2* acc;     // RK4 sums
+  float2* xf;      // next stage state (FP32); may alias the pass's stage-state input
+  double* dg;      // FP64 diagonal of the next stage state (C, D) or nullptr
+  unsigned* mx;
+  unsigned* mo;
+};
+
+__device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, float2 kv, bool diag,
+                                               long long dgi) {
+  const double2 x = r.X[i];
+  if (r.stage < 4) {
+    const float f = (r.stage == 1 || r.stage == 2) ? 0.5f * r.dt : r.dt;
+    if (r.stage == 1) {
+      r.acc[i] = kv;
+    } else {
+      const float2 a = r.acc[i];
+      r.acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
+    }
+    const float2 xs = f64_to_f32(x);
+    const float2 v = make_float2(xs.x + f * kv.x, xs.y + f * kv.y);
+    r.xf[i] = v;
+    if (diag && r.dg) r.dg[dgi] = x.x + f32_to_f64(f * kv.x);
+    return max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu);
+  }
+  const float2 a = r.acc[i];
+  const float sc = r.dt / 6.f;
+  const double2 v = make_double2(x.x + f32_to_f64(sc * (a.x + kv.x)),
+                                 x.y + f32_to_f64(sc * (a.y + kv.y)));
+  r.X[i] = v;
+  return bits_to_fmax(max(absbits(v.x), absbits(v.y)));
+}
+
+// block maxima of the written states -> one atomic per block (blockDim 256)
+__device__ __forceinline__ void rk4_block_max(const Rk4Ctl& r, int b, unsigned m, unsigned mof) {
+  __shared__ unsigned red[2][8];
+  for (int off = 16; off > 0; off >>= 1) {
+    m = max(m, __shfl_down_sync(0xffffffffu, m, off));
+    mof = max(mof, __shfl_down_sync(0xffffffffu, mof, off));
+  }
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((t & 31) == 0) {
+    red[0][t >> 5] = m;
+    red[1][t >> 5] = mof;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int w = 1; w < 8; ++w) {
+      m = max(m, red[0][w]);
+      mof = max(mof, red[1][w]);
+    }
+    atomicMax(r.mx + b, m);
+    atomicMax(r.mo + b, mof);
+  }
+}
+
 // dC (dD) from W = C' Hee'^T + P^H Heh^T (V = D' Hhh'^T + conj(P) Heh), where C'
 // (D') is C (D) without its diagonal c (d): for Hermitian C, Hee (D, Hhh) the four
 // terms of dCdt (dDdt) are W - W^H plus the peeled diagonal's (c_i - c_j) Hee'[j][i],
@@ -1068,9 +1134,9 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
 // parts of g.
 __global__ void __launch_bounds__(256) k_antiherm(
     int nk, const float2* __restrict__ W, const float2* __restrict__ W2,
-    const float2* __restrict__ W3, const float2* __restrict__ Hp, const float2* __restrict__ X,
+    const float2* __restrict__ W3, const float2* __restrict__ Hp, const float2* X,
     const float2* __restrict__ ghi, const float2* __restrict__ glo, const float* __restrict__ chi,
-    const float* __restrict__ clo, float2* __restrict__ out) {
+    const float* __restrict__ clo, float2* out, Rk4Ctl rk) {
   // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results;
   // gv / cv: g (hi, lo) and c (hi, lo) at the tile's rows i0.. (0) and columns j0.. (1)
   __shared__ float2 tb[32][33], hb[32][33], vt[32][33];
@@ -1112,6 +1178,7 @@ __global__ void __launch_bounds__(256) k_antiherm(
   }
   __syncthreads();
   const float ih = (float)(1.0 / kHbar);
+  unsigned mxv = 0, mov = 0;
   // the tile (i0.., j0..): i <= j wherever it is written
   {
     float2 w[4][3], x[4];
@@ -1143,7 +1210,16 @@ __global__ void __launch_bounds__(256) k_antiherm(
       const float im = (a.y + bt.y) + dc * hji.y + (dr * x[q].y + di * x[q].x);
       const float2 v = make_float2(im * ih, -re * ih);
       vt[r][tx] = v;
-      if (i < nk && j < nk && (bi < bj || j >= i)) out[mb + (long long)i * nk + j] = v;
+      if (i < nk && j < nk && (bi < bj || j >= i)) {
+        const long long o = mb + (long long)i * nk + j;
+        if (rk.stage == 0) {
+          out[o] = v;
+        } else {
+          const unsigned a = rk4_update(rk, o, v, i == j, (long long)b * nk + i);
+          mxv = max(mxv, a);
+          if (!rk.peel || i != j) mov = max(mov, a);
+        }
+      }
     }
   }
   __syncthreads();
@@ -1155,9 +1231,17 @@ __global__ void __launch_bounds__(256) k_antiherm(
     if (i >= nk || j >= nk) continue;
     if (bi < bj || i > j) {
       const float2 v = vt[tx][r];
-      out[mb + (long long)i * nk + j] = make_float2(v.x, -v.y);
+      const long long o = mb + (long long)i * nk + j;
+      if (rk.stage == 0) {
+        out[o] = make_float2(v.x, -v.y);
+      } else {
+        const unsigned a = rk4_update(rk, o, make_float2(v.x, -v.y), false, 0);
+        mxv = max(mxv, a);
+        mov = max(mov, a);
+      }
     }
   }
+  if (rk.stage != 0) rk4_block_max(rk, b, mxv, mov);
 }
 
 // dP of a stage from the FP32 commutator sums G (the engine's scaled products with
@@ -1170,8 +1254,8 @@ __global__ void __launch_bounds__(256) k_antiherm(
 // goes through shared memory so that every global access runs along rows.
 __global__ void __launch_bounds__(256) k_rhs_p(
     int nk, int nw, const float2* __restrict__ G, const float2* __restrict__ hehf,
-    const float2* __restrict__ X, const float2* __restrict__ dgf, const float* __restrict__ gamf,
-    const float* __restrict__ cdf, float2* __restrict__ out) {
+    const float2* X, const float2* __restrict__ dgf, const float* __restrict__ gamf,
+    const float* __restrict__ cdf, float2* out, Rk4Ctl rk) {
   __shared__ float2 ht[32][33];
   // per-row (kh = m0 + r) values: hh hi, lo; GamH; d hi, lo
   __shared__ float2 rg[2][32];
@@ -1204,6 +1288,7 @@ __global__ void __launch_bounds__(256) k_rhs_p(
   const int n = n0 + tx;
   const bool on = n < nk;
   const float ih = (float)(1.0 / kHbar);
+  unsigned mxv = 0, mov = 0;
   const long long vnn = vb + (on ? n : 0);
   const float2 eh = dgf[vnn], el = dgf[vn + vnn];
   const float gamE = gamf[vnn];
@@ -1229,84 +1314,17 @@ __global__ void __launch_bounds__(256) k_rhs_p(
     const float ar = ax + (der * x[q].x - dei * x[q].y);
     const float ai = ay + (der * x[q].y + dei * x[q].x);
     const float gam = gamE + rv[0][r];
-    out[mb + (long long)m * nk + n] =
-        make_float2(ai * ih - gam * x[q].x, -ar * ih - gam * x[q].y);
-  }
-}
-
-// RK4 stage update of the mixed path: the stage derivative k and the sums
-// k1 + 2 k2 + 2 k3 are FP32 (they carry the RHS's FP32-accumulated precision).
-// Stages 1-3 write the next stage state in FP32 (xf = fp32(X) + f k: within an
-// FP32 ulp of the rounded FP64 sum, which is all its consumers use) and, with dg
-// set, its real diagonal in FP64; stage 4 adds to the FP64 state.  Every stage
-// also measures the maximum of the state it writes per wire into mx[b] (mo: the
-// off-diagonal part when peel).  grid (blocks per wire, wires).
-__global__ void k_rk4_mixed(int nk, int peel, int stage, float dt, double2* X, float2* acc,
-                            float2* xf, double* dg, const float2* k, unsigned* mx,
-                            unsigned* mo) {
-  const int b = blockIdx.y;
-  const long long per = (long long)nk * nk;
-  const long long o = (long long)b * per;
-  unsigned m = 0, mof = 0;   // FP32 magnitude patterns
-  const float f = (stage == 1 || stage == 2) ? 0.5f * dt : dt;
-  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long S = (long long)gridDim.x * blockDim.x;
-  int row = (int)(i0 / nk), col = (int)(i0 % nk);
-  const int srow = (int)(S / nk), scol = (int)(S % nk);
-  for (long long j = i0; j < per; j += S) {
-    const long long i = o + j;
-    const float2 kv = k[i];
-    const double2 x = X[i];
-    unsigned a;
-    if (stage < 4) {
-      if (stage == 1) {
-        acc[i] = kv;
-      } else {
-        const float2 av = acc[i];
-        acc[i] = make_float2(av.x + 2.f * kv.x, av.y + 2.f * kv.y);
-      }
-      const float2 xs = f64_to_f32(x);
-      const float2 v = make_float2(xs.x + f * kv.x, xs.y + f * kv.y);
-      xf[i] = v;
-      if (dg && row == col) dg[(long long)b * nk + row] = x.x + f32_to_f64(f * kv.x);
-      a = max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu);
+    const float2 kv = make_float2(ai * ih - gam * x[q].x, -ar * ih - gam * x[q].y);
+    const long long o = mb + (long long)m * nk + n;
+    if (rk.stage == 0) {
+      out[o] = kv;
     } else {
-      const float2 av = acc[i];
-      const float sc = dt / 6.f;
-      const double2 v = make_double2(x.x + f32_to_f64(sc * (av.x + kv.x)),
-                                     x.y + f32_to_f64(sc * (av.y + kv.y)));
-      X[i] = v;
-      a = bits_to_fmax(max(absbits(v.x), absbits(v.y)));
-    }
-    m = max(m, a);
-    if (!peel || row != col) mof = max(mof, a);
-    col += scol;
-    row += srow;
-    if (col >= nk) {
-      col -= nk;
-      ++row;
+      const unsigned a = rk4_update(rk, o, kv, false, 0);
+      mxv = max(mxv, a);
+      mov = max(mov, a);
     }
   }
-  {
-    __shared__ unsigned red[2][8];
-    for (int off = 16; off > 0; off >>= 1) {
-      m = max(m, __shfl_down_sync(0xffffffffu, m, off));
-      mof = max(mof, __shfl_down_sync(0xffffffffu, mof, off));
-    }
-    if ((threadIdx.x & 31) == 0) {
-      red[0][threadIdx.x >> 5] = m;
-      red[1][threadIdx.x >> 5] = mof;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-        m = max(m, red[0][w]);
-        mof = max(mof, red[1][w]);
-      }
-      atomicMax(mx + b, m);
-      atomicMax(mo + b, mof);
-    }
-  }
+  if (rk.stage != 0) rk4_block_max(rk, b, mxv, mov);
 }
 
 __global__ void k_f32_to_f64(long long n, const float2* a, double2* out) {
@@ -1410,8 +1428,12 @@ static void mixed_state_in(SbeCtx* c, const double2* P, const double2* C, const 
 
 // One RHS evaluation of the mixed path on the FP32 stage state (P, C, D; the
 // FP64 diagonals of C and D in dgC, dgD; the state maxima already in mxS, mxO).
+// With stage 1-4 the RK4 update of that stage is fused into the element-wise
+// passes (X64: the FP64 states P, C, D; the next stage state goes to the FP32
+// stage buffer and its maxima to mxS, mxO); stage 0 stores the RHS in kf.
 static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2* D,
-                       const double* dgC, const double* dgD, const double2* Ek, cudaStream_t s) {
+                       const double* dgC, const double* dgD, const double2* Ek, int stage,
+                       float dt, double2* const* X64, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   const long long mm = (long long)nk * nk, tm = c->tot_mat;
@@ -1423,6 +1445,12 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   // peeled off and applied exactly in the epilogues)
   exponents_from(m, m->mxS(), m->eS(), s);
   exponents_from(m, m->mxO(), m->eO(), s);
+  if (stage > 0) {
+    // consumed by the exponents above: the fused RK4 update collects the next
+    // stage state's maxima in them
+    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
+  }
   const float2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   const long long vn = (long long)nw * nk;
@@ -1515,12 +1543,26 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
     if (rc) return rc;
   }
   const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
-  k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp, m->hf, st[0], m->dgf, m->gamf, m->cdf, m->kf);
+  Rk4Ctl rk[3];
+  float2* xf = reinterpret_cast<float2*>(c->xs);
+  for (int i = 0; i < 3; ++i) {
+    rk[i] = Rk4Ctl{};
+    rk[i].stage = stage;
+    rk[i].peel = i > 0;
+    rk[i].dt = dt;
+    rk[i].X = X64 ? X64[i] : nullptr;
+    rk[i].acc = m->accf + i * tm;
+    rk[i].xf = xf + i * tm;
+    rk[i].dg = i > 0 ? m->xdg + (i - 1) * vn : nullptr;
+    rk[i].mx = m->mxS();
+    rk[i].mo = m->mxO();
+  }
+  k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp, m->hf, st[0], m->dgf, m->gamf, m->cdf, m->kf, rk[0]);
   k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, wx, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
-                               m->cdf + vn, m->kf + tm);
+                               m->cdf + vn, m->kf + tm, rk[1]);
   k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, vx, m->hf + 2 * tm, D,
                                m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn, m->cdf + 3 * vn,
-                               m->kf + 2 * tm);
+                               m->kf + 2 * tm, rk[2]);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 
@@ -1585,7 +1627,7 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
   const long long n = c->tot_mat, vn = (long long)m->nw * m->nk;
   mixed_state_in(c, P, C, D, s);
   const float2* xf = reinterpret_cast<const float2*>(c->xs);
-  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, s);
+  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, 0, 0.f, nullptr, s);
   if (rc) return rc;
   const int g = (int)((n + 255) / 256);
   k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf, dP);
@@ -1602,24 +1644,17 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   if (rc) return rc;
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const long long n = c->tot_mat;
-  const long long per = (long long)m->nk * m->nk;
-  const int bpw = (int)std::min<long long>((per + 255) / 256, 64);
   const double frac[4] = {0.0, 0.5, 0.5, 1.0};
   const long long vn = (long long)m->nw * m->nk;
   float2* xf = reinterpret_cast<float2*>(c->xs);
   mixed_state_in(c, P, C, D, s);
+  double2* X64[3] = {P, C, D};
   for (int st = 1; st <= 4; ++st) {
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
-    rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, c->ekst, s);
+    // the RHS of this stage and its RK4 update (fused into the element-wise passes)
+    rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, c->ekst, st, (float)dt, X64,
+                     s);
     if (rc) return rc;
-    // RK4 update; every stage also measures the maxima of the state it writes
-    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * m->nw, s);
-    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * m->nw, s);
-    double2* X[3] = {P, C, D};
-    for (int i = 0; i < 3; ++i)
-      k_rk4_mixed<<<dim3(bpw, m->nw), 256, 0, s>>>(
-          m->nk, i > 0, st, (float)dt, X[i], m->accf + i * n, xf + i * n,
-          i > 0 ? m->xdg + (i - 1) * vn : nullptr, m->kf + i * n, m->mxS(), m->mxO());
   }
   mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
   return mixed_sources(c, P, C, D, src, 1, s);
