@@ -52,6 +52,10 @@ WORKLOADS = {
     "profile": dict(nw=8, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
                     dt=0.05e-15, spacing=100e-9, nx=16384, dx=10e-9, n_abc=128,
                     abc=0.05, x_src=-2.5e-6),
+    # 16 wires: state matrices larger than L2 (201 MB in FP64), a few GB on the device
+    "profile16": dict(nw=16, nk=512, kmax=3e9, temp=300.0, E0=5e7, tau=50e-15, det=20e-3,
+                      dt=0.05e-15, spacing=100e-9, nx=16384, dx=10e-9, n_abc=128,
+                      abc=0.05, x_src=-2.5e-6),
 }
 
 MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta0=6e-9,

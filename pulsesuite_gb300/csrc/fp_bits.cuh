@@ -11,25 +11,20 @@ namespace sbe {
 
 // round-to-nearest-even of x * 2^e to FP32 (e is added to the exponent, so the
 // scaling is exact).  Results below the FP32 normal range (|x 2^e| < 2^-126)
-// become signed zero; overflow gives infinity; NaN stays NaN.
+// become signed zero; overflow gives infinity; NaN stays NaN.  The 52-bit
+// mantissa is rounded to 23 bits with one 64-bit integer add (ties to even); a
+// carry out of the mantissa runs into the exponent field.
 __device__ __forceinline__ float f64_to_f32(double x, int e = 0) {
-  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned sign = hi & 0x80000000u;
-  const int ex = (int)((hi >> 20) & 0x7FFu);
-  if (ex == 0) return __uint_as_float(sign);
-  if (ex == 0x7FF)
-    return __uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u));
-  int fe = ex - 1023 + 127 + e;
-  unsigned m23 = ((hi & 0xFFFFFu) << 3) | (lo >> 29);   // top 23 of the 52 mantissa bits
-  const unsigned rem = lo & 0x1FFFFFFFu;                 // the 29 dropped bits
-  m23 += (rem > 0x10000000u) | ((rem == 0x10000000u) & (m23 & 1u));
-  if (m23 == 0x800000u) {
-    m23 = 0;
-    ++fe;
-  }
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const unsigned long long a = u & 0x7FFFFFFFFFFFFFFFull;
+  if (a >= 0x7FF0000000000000ull)   // infinity or NaN
+    return __uint_as_float(sign | 0x7F800000u | (a != 0x7FF0000000000000ull ? 0x400000u : 0u));
+  const unsigned long long r = (a + 0x0FFFFFFFull + ((a >> 29) & 1ull)) >> 29;
+  const int fe = (int)(r >> 23) - (1023 - 127) + e;
   if (fe >= 255) return __uint_as_float(sign | 0x7F800000u);
   if (fe <= 0) return __uint_as_float(sign);
-  return __uint_as_float(sign | ((unsigned)fe << 23) | m23);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | ((unsigned)r & 0x7FFFFFu));
 }
 
 // x * 2^e for FP32 by two exact power-of-two multiplies (|e| <= 252, result in

@@ -507,40 +507,62 @@ __global__ void __launch_bounds__(256) k_state_in(const double2* __restrict__ X,
                                                   unsigned* __restrict__ mo,
                                                   float2* __restrict__ xf, double* __restrict__ dg) {
   const int b = blockIdx.y;
-  const long long per = (long long)nk * nk;
+  const int per = nk * nk;   // < 2^31
   const double2* x = X + (long long)b * per;
   float2* y = xf + (long long)b * per;
-  unsigned long long m = 0, o = 0;
-  // four elements per thread and pass, loads issued together
-  const long long S = (long long)gridDim.x * blockDim.x;
-  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < per; i0 += 4 * S) {
+  unsigned m = 0, o = 0;   // FP32 magnitude patterns
+  // four elements per thread and pass (stride S), loads issued together; the
+  // diagonal is tracked by row / column counters stepped with S (no division per
+  // element)
+  const int S = gridDim.x * blockDim.x;
+  const int srow = S / nk, scol = S % nk;
+  const int i00 = blockIdx.x * blockDim.x + threadIdx.x;
+  int row = i00 / nk, col = i00 % nk;
+  for (int i0 = i00; i0 < per; i0 += 4 * S) {
     double2 v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const long long i = i0 + u * S;
+      const int i = i0 + u * S;
       v[u] = i < per ? x[i] : make_double2(0.0, 0.0);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const long long i = i0 + u * S;
-      if (i >= per) break;
-      y[i] = f64_to_f32(v[u]);
-      const unsigned long long a = max(absbits(v[u].x), absbits(v[u].y));
-      m = max(m, a);
-      // the diagonal: i = k (nk + 1)  (nk^2 < 2^31)
-      const int ii = (int)i;
-      const bool diag = (ii % (nk + 1)) == 0;
-      if (diag && dg) dg[(long long)b * nk + ii / (nk + 1)] = v[u].x;
-      if (!(diag && peel)) o = max(o, a);
+      const int i = i0 + u * S;
+      if (i < per) {
+        const float2 f = f64_to_f32(v[u]);
+        y[i] = f;
+        const unsigned a = max(__float_as_uint(f.x) & 0x7FFFFFFFu, __float_as_uint(f.y) & 0x7FFFFFFFu);
+        m = max(m, a);
+        const bool diag = row == col;
+        if (diag && dg) dg[(long long)b * nk + row] = v[u].x;
+        if (!(diag && peel)) o = max(o, a);
+      }
+      col += scol;
+      row += srow;
+      if (col >= nk) {
+        col -= nk;
+        ++row;
+      }
     }
   }
+  // one atomic pair per block: same-address atomics of all blocks serialise in L2
+  __shared__ unsigned red[2][8];
   for (int k = 16; k > 0; k >>= 1) {
     m = max(m, __shfl_down_sync(0xffffffffu, m, k));
     o = max(o, __shfl_down_sync(0xffffffffu, o, k));
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(mx + b, bits_to_fmax(m));
-    atomicMax(mo + b, bits_to_fmax(o));
+    red[0][threadIdx.x >> 5] = m;
+    red[1][threadIdx.x >> 5] = o;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      m = max(m, red[0][w]);
+      o = max(o, red[1][w]);
+    }
+    atomicMax(mx + b, m);
+    atomicMax(mo + b, o);
   }
 }
 
@@ -922,6 +944,8 @@ __global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
 // dd = k2 - k1 + Nk - 1, read along rows (coalesced in k2).  The diagonal of
 // Hee / Hhh (gap + kinetic energy) is formed in FP64 into dgE / dgH and split into
 // FP32 hi / lo parts (dgf).  The block maximum of the operands goes to mx[b].
+constexpr int HB_ROWS = 1;
+
 __global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __restrict__ ekf,
                           const float* __restrict__ vsf, const double* __restrict__ Ee,
                           const double* __restrict__ Eh, const float2* __restrict__ trf,
@@ -930,8 +954,10 @@ __global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __res
                           float2* __restrict__ dgf, unsigned* __restrict__ mx) {
   const WireDev& W = wires[blockIdx.z];
   const int nk = W.nk, b = blockIdx.z, nw = gridDim.z;
-  const int k1 = blockIdx.y;
   float hmax = 0.f;
+  // HB_ROWS rows per block
+  for (int rr = 0; rr < HB_ROWS; ++rr) {
+  const int k1 = blockIdx.y * HB_ROWS + rr;
   for (int it = 0; it < 4; ++it) {
   const int k2 = blockIdx.x * blockDim.x * 4 + it * blockDim.x + threadIdx.x;
   if (k1 < nk && k2 < nk) {
@@ -1000,6 +1026,7 @@ __global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __res
     hmax = fmaxf(hmax, fmaxf(fmaxf(fmaxf(fabsf(heh.x), fabsf(heh.y)),
                                    fmaxf(fabsf(hee.x), fabsf(hee.y))),
                              fmaxf(fabsf(hhh.x), fabsf(hhh.y))));
+  }
   }
   }
   __shared__ float red[4];
@@ -1486,7 +1513,7 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
     if (rc) return rc;
   }
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
-  k_h_build<<<dim3((nk + 511) / 512, nk, nw), 128, 0, s>>>(
+  k_h_build<<<dim3((nk + 511) / 512, (nk + HB_ROWS - 1) / HB_ROWS, nw), 128, 0, s>>>(
       c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, m->xsh, have_x, m->hf, tm, m->dgE, m->dgH,
       m->dgf, m->mxH());
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
@@ -1594,6 +1621,7 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     e.kind = tc::EPI_RAWF;
     e.outf2 = gf + i * c->tot_kr;
     e.out_bstride = (long long)nk * m->nr;
+    e.ldo = m->nr;
     e.escale = m->ess();
     e.err = m->err();
     jobs[i] = job(m, m->pl, m->ep, nk, m->nr, nk, 1, 1, &t, 0, e);
@@ -1603,6 +1631,7 @@ static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const do
     int rc = tc_gemm_launch(jobs, 3, s);
     if (rc) return rc;
   }
+
   k_src_reduce_f<<<dim3((m->nr + 31) / 32, nw), dim3(32, 8), 0, s>>>(c->d_wires, m->ekrf, gf,
                                                                     c->tot_kr, c->window, src);
   launch_sources_final(c, c->ne, c->nh, src, s);

@@ -143,7 +143,7 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N, int negA) {
 // dependent load into every chunk).  Output pointers are offset to the tile's
 // batch entry and K part.
 struct EpiTile {
-  int kind, M, N, cplx, es;
+  int kind, M, N, ld, cplx, es;
   float* of;      // EPI_F32
   float2* of2;    // EPI_RAWF
   double2* od;    // EPI_RAW
@@ -154,6 +154,7 @@ __device__ __forceinline__ EpiTile epi_tile(const GemmDesc& d, const EpiArgs& e,
   t.kind = e.kind;
   t.M = d.M;
   t.N = d.N;
+  t.ld = e.ldo > 0 ? e.ldo : d.N;
   t.cplx = d.complex_mode;
   t.es = -e.escale[b];
   const long long off = (long long)ks * e.ks_stride + (long long)b * e.out_bstride;
@@ -199,8 +200,8 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
   const int n = n0 + j;
   const int rmax = min(32, t.M - mrow0);
   if (n >= t.N) return;
-  const long long base = (long long)(mrow0 + rh) * t.N + n;
-  const long long rs = 2 * (long long)t.N;
+  const long long base = (long long)(mrow0 + rh) * t.ld + n;
+  const long long rs = 2 * (long long)t.ld;
   if (t.kind == EPI_RAWF) {
     float2* o = t.of2 + base;
 #pragma unroll

@@ -102,6 +102,7 @@ struct EpiArgs {
   float2* outf2;              // EPI_RAWF output (per batch stride out_bstride)
   long long out_bstride;
   long long ks_stride;        // output offset (elements) between the K parts of a split-K GEMM
+  int ldo;                    // output row stride in elements (0: N)
   const int* escale;          // per batch exponent of the product scale (e_A + e_B)
   int* err;                   // error flag (bounded waits)
 };
