@@ -254,7 +254,7 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 struct Mixed {
   int nk = 0, nw = 0, nr = 0;
   tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
-  float* xsh = nullptr;    // exchange sums in the sheared layout: 3 x Nw x Nk x 4Nk
+  float* xsh = nullptr;    // exchange sums, un-sheared: 3 x Nw x Nk x Nk complex (FP32)
   int* ints = nullptr;     // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
   unsigned* mx = nullptr;  // [0, nw): Hamiltonian maximum; [nw, 2nw): state; [2nw, 3nw): hbar A/B
   float2* kf = nullptr;    // 3 x tot_mat stage derivatives
@@ -424,7 +424,7 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
             cudaMalloc(&m->tp.ptr, tc::planeset_bytes(m->tp)) == cudaSuccess &&
             cudaMalloc(&m->sp.ptr, tc::planeset_bytes(m->sp)) == cudaSuccess &&
             cudaMalloc(&m->ep.ptr, tc::planeset_bytes(m->ep)) == cudaSuccess &&
-            cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 4 * mm) == cudaSuccess &&
+            cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 2 * mm) == cudaSuccess &&
             cudaMalloc(&m->ints, sizeof(int) * 9 * nw) == cudaSuccess &&
             cudaMalloc(&m->mx, sizeof(unsigned) * 4 * nw) == cudaSuccess &&
             cudaMalloc(&fblock, fbytes) == cudaSuccess &&
@@ -940,8 +940,8 @@ __global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
 
 // H = Meh + diagonal energies + direct Coulomb terms + exchange sums
 // (SBEs.py:1044-1131) in FP32: Heh, Hee' and Hhh' (diagonal removed) into hf.
-// The exchange sums come from the sheared FP32 GEMM output xsh[n][b][k1][2 dd + c],
-// dd = k2 - k1 + Nk - 1, read along rows (coalesced in k2).  The diagonal of
+// The exchange sums come from the FP32 GEMM output xsh[n][b][k1][k2] (the engine's
+// epilogue un-shears the columns dd = k2 - k1 + Nk - 1 of the product).  The diagonal of
 // Hee / Hhh (gap + kinetic energy) is formed in FP64 into dgE / dgH and split into
 // FP32 hi / lo parts (dgf).  The block maximum of the operands goes to mx[b].
 constexpr int HB_ROWS = 1;
@@ -949,7 +949,7 @@ constexpr int HB_ROWS = 1;
 __global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __restrict__ ekf,
                           const float* __restrict__ vsf, const double* __restrict__ Ee,
                           const double* __restrict__ Eh, const float2* __restrict__ trf,
-                          const float* __restrict__ xsh, int have_x, float2* __restrict__ hf,
+                          const float2* __restrict__ xsh, int have_x, float2* __restrict__ hf,
                           long long tot_mat, double2* __restrict__ dgE, double2* __restrict__ dgH,
                           float2* __restrict__ dgf, unsigned* __restrict__ mx) {
   const WireDev& W = wires[blockIdx.z];
@@ -988,15 +988,14 @@ __global__ void k_h_build(const WireDev* __restrict__ wires, const float2* __res
     }
     float2 xc = make_float2(0.f, 0.f), xd = xc;
     if (have_x) {
-      const long long ms = (long long)nk * 4 * nk;
-      const long long rowo = ((long long)b * nk + k1) * 4 * nk + 2 * (k2 - k1 + nk - 1);
-      const long long plane = (long long)nw * ms;
-      const float2 xe = *reinterpret_cast<const float2*>(xsh + rowo);
+      const long long plane = (long long)nw * nk * nk;
+      const long long xo = ((long long)b * nk + k1) * nk + k2;
+      const float2 xe = xsh[xo];
       heh.x += xe.x;
       heh.y += xe.y;
       if (lf || d == 0) {
-        xc = *reinterpret_cast<const float2*>(xsh + plane + rowo);
-        xd = *reinterpret_cast<const float2*>(xsh + 2 * plane + rowo);
+        xc = xsh[plane + xo];
+        xd = xsh[2 * plane + xo];
       }
     }
     const long long o = W.off_mat + (long long)k1 * nk + k2;
@@ -1502,8 +1501,10 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
       tc::Term t{n, n, 0, 0, 1};
       tc::EpiArgs e{};
       e.kind = tc::EPI_F32;
-      e.outf = m->xsh + (long long)n * nw * 4 * mm;
-      e.out_bstride = 4 * mm;
+      e.outf = m->xsh + (long long)n * nw * 2 * mm;
+      e.out_bstride = 2 * mm;
+      e.ldo = 2 * nk;
+      e.unshear = nk;
       e.escale = m->esx();
       e.err = m->err();
       jobs[n] = job(m, m->tp, m->sp, nk, 4 * nk, nk, 0, 1, &t, 1, e);
@@ -1514,7 +1515,8 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   }
   cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
   k_h_build<<<dim3((nk + 511) / 512, (nk + HB_ROWS - 1) / HB_ROWS, nw), 128, 0, s>>>(
-      c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, m->xsh, have_x, m->hf, tm, m->dgE, m->dgH,
+      c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, reinterpret_cast<const float2*>(m->xsh),
+      have_x, m->hf, tm, m->dgE, m->dgH,
       m->dgf, m->mxH());
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
   k_exponents2<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH());

@@ -15,7 +15,7 @@ namespace tc {
 // dependent load into every chunk).  Output pointers are offset to the tile's
 // batch entry and K part.
 struct EpiTile {
-  int kind, M, N, ld, cplx, es;
+  int kind, M, N, ld, cplx, es, unshear;
   float* of;      // EPI_F32
   float2* of2;    // EPI_RAWF
   double2* od;    // EPI_RAW
@@ -29,6 +29,7 @@ __device__ __forceinline__ EpiTile epi_tile(const GemmDesc& d, const EpiArgs& e,
   t.ld = e.ldo > 0 ? e.ldo : d.N;
   t.cplx = d.complex_mode;
   t.es = -e.escale[b];
+  t.unshear = e.unshear;
   const long long off = (long long)ks * e.ks_stride + (long long)b * e.out_bstride;
   t.of = e.outf ? e.outf + off : nullptr;
   t.of2 = e.outf2 ? e.outf2 + off : nullptr;
@@ -79,6 +80,17 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
 #pragma unroll
     for (int i = 0; i < 16; ++i)
       if (2 * i + rh < rmax) o[i * rs] = v[i];
+  } else if (t.kind == EPI_F32 && t.unshear) {
+    // row r = mrow0 + rh + 2i, diagonal n >> 1: complex column k2 = r + (n >> 1) -
+    // (unshear - 1); consecutive lanes store consecutive floats of one row
+    const int k20 = mrow0 + rh + (n >> 1) - (t.unshear - 1);
+    float* o = t.of + (long long)(mrow0 + rh) * t.ld + 2 * k20 + (n & 1);
+    const long long rs2 = 2 * (long long)t.ld + 4;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int k2 = k20 + 2 * i;
+      if (2 * i + rh < rmax && k2 >= 0 && k2 < t.unshear) o[i * rs2] = v[i].x;
+    }
   } else if (t.kind == EPI_F32) {
     float* o = t.of + base;
 #pragma unroll
@@ -101,6 +113,7 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
 // One output tile of the launch's tile list.
 struct TileInfo {
   int job, b, m0, n0, ks, kb_begin, nkb, n_iters;
+  bool dead;   // exchange tile whose outputs all lie outside the un-sheared matrix
 };
 
 template <int BNT>
@@ -129,6 +142,12 @@ __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) 
     const int tlo = max(0, -dhi), thi = min(nk - 1, nk - 1 - dlo);
     kb_begin = max(kb_begin, tlo / BK);
     kb_end = (thi >= tlo) ? min(kb_end, thi / BK + 1) : kb_begin;
+    // output (m, dd) is element [m][m + dd - (Nk - 1)] of the Hamiltonian: the tile
+    // is used only if some m + dd of it lies in [Nk - 1, 2 Nk - 2]
+    const int m_hi = min(ti.m0 + BM, d.M) - 1;
+    ti.dead = (dd_lo + ti.m0 > 2 * nk - 2) || (dd_hi + m_hi < nk - 1);
+  } else {
+    ti.dead = false;
   }
   ti.kb_begin = kb_begin;
   ti.nkb = max(0, kb_end - kb_begin);
@@ -154,6 +173,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   const int stage_bytes = npl * (A_TILE_BYTES + BTB);
   const int nstage = min(8, STAGE_AREA / stage_bytes);
   // accumulator columns of one tile; two tiles in flight when they fit twice
+  // (MODE_HH: B's re and im plane tiles lie back to back in shared memory, so one
+  // MMA of N = 2 BNT per A plane forms two real products: 4 BNT columns)
   const int tile_cols = HH ? 4 * BNT : (cplx ? 2 * BNT : BNT);
   const int nbuf = tile_cols <= 256 ? 2 : 1;
   float2* scr_all = reinterpret_cast<float2*>(smem + STAGE_AREA);
@@ -205,7 +226,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     for (int k = 0; ok; ++k) {
       const int qs = k & 3;
       if (!mbar_wait(&qempty[qs], (uint32_t)(((k >> 2) & 1) ^ 1), err, abort_flag)) break;
-      const long long t = atomicAdd(L.sched, 1);
+      long long t = atomicAdd(L.sched, 1);
+      while (t < ntiles && tile_info<BNT>(L, t).dead) t = atomicAdd(L.sched, 1);
       tq[qs] = t < ntiles ? (int)t : -1;
       mbar_arrive(&qfull[qs]);   // release: the entry is visible to the waiters
       if (t >= ntiles) break;
@@ -254,7 +276,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
-    const uint32_t id_pos = idesc_f16(BM, BNT, 0), id_neg = idesc_f16(BM, BNT, 1);
+    constexpr int MMA_N = HH ? 2 * BNT : BNT;
+    const uint32_t id_pos = idesc_f16(BM, MMA_N, 0), id_neg = idesc_f16(BM, MMA_N, 1);
     long long g = 0;
     bool ok = true;
     for (int lt = 0; ok; ++lt) {
@@ -302,11 +325,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               umma_f16(acc_re, A(0), B(1), id, 1u);
               umma_f16(acc_re, A(1), B(0), id, 1u);
             } else if (HH) {
-              // planes 0 re_hi, 1 im_hi; accumulators (BNT columns each) rr, ii, ri, ir
-              umma_f16(tmem + 0 * BNT, A(0), B(0), irr, acc);
-              umma_f16(tmem + 1 * BNT, A(1), B(1), iii, acc);
-              umma_f16(tmem + 2 * BNT, A(0), B(1), iri, acc);
-              umma_f16(tmem + 3 * BNT, A(1), B(0), iir, acc);
+              // planes 0 re_hi, 1 im_hi; B(0) spans B's re and im tiles.  Columns of
+              // the tile's buffer: [rr | ri] from A re, [ir | -ii] from A im (B is
+              // never conjugated here, so ri takes rr's sign and ii the negative of
+              // ir's; the epilogue forms re = rr - (-ii), im = ri + ir)
+              umma_f16(acc_re, A(0), B(0), irr, acc);
+              umma_f16(acc_re + 2 * BNT, A(1), B(0), iir, acc);
             } else {
               // planes 0 re_hi, 1 re_lo, 2 im_hi, 3 im_lo
               uint32_t ar = acc, ai = acc;
@@ -369,14 +393,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int c = half * NCH + cc;   // chunk of the tile
         float re[16], im[16];
         if (have && HH) {
-          // re = rr + ii, im = ri + ir (signs applied by the MMAs)
+          // buffer columns [rr | ri | ir | -ii] (BNT each): re = rr + ii, im = ri + ir
           float t0[16];
           tmem_ld16(lane_addr + 0 * BNT + c * 16, re);
-          tmem_ld16(lane_addr + 1 * BNT + c * 16, t0);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) re[j] += t0[j];
-          tmem_ld16(lane_addr + 2 * BNT + c * 16, im);
           tmem_ld16(lane_addr + 3 * BNT + c * 16, t0);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) re[j] -= t0[j];
+          tmem_ld16(lane_addr + 1 * BNT + c * 16, im);
+          tmem_ld16(lane_addr + 2 * BNT + c * 16, t0);
 #pragma unroll
           for (int j = 0; j < 16; ++j) im[j] += t0[j];
         } else if (have) {
@@ -484,6 +508,9 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
     if ((mode == tc::MODE_HH || d.xonly) && (!d.complex_mode || d.kskip))
       return fail(SBE_ERR_ARG, "tc_gemm: hi*hi and cross-term modes are complex and unskipped only");
     if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
+    if (mode == tc::MODE_HH)
+      for (int i = 0; i < d.nterms; ++i)
+        if (d.t[i].b_conj) return fail(SBE_ERR_ARG, "tc_gemm: hi*hi mode takes B unconjugated");
     L.job[j] = jobs[j];
     L.tile_base[j] = nt;
     nt += (long long)((d.N + bnt - 1) / bnt) * ((d.M + tc::BM - 1) / tc::BM) * d.batch *

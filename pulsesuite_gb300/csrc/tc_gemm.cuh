@@ -30,7 +30,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BN = 256;
-constexpr int BN_HH = 128;     // N tile of the hi*hi mode
+constexpr int BN_HH = 128;     // N tile of the hi*hi mode (MMA N = 256 over re and im of B)
 constexpr int BK = 32;
 constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
@@ -105,6 +105,11 @@ struct EpiArgs {
   int ldo;                    // output row stride in elements (0: N)
   const int* escale;          // per batch exponent of the product scale (e_A + e_B)
   int* err;                   // error flag (bounded waits)
+  // EPI_F32 of the exchange products (0: off): column n of row m is component
+  // n & 1 of diagonal dd = n >> 1, stored un-sheared as component n & 1 of the
+  // complex element [m][m + dd - (unshear - 1)] of an unshear x unshear matrix
+  // (row stride ldo floats); elements outside that matrix are not stored
+  int unshear;
 };
 
 enum Mode : int { MODE_FULL = 0, MODE_HH = 1 };
@@ -118,9 +123,10 @@ struct GemmDesc {
   int kskip;                  // exchange: K range limited by the sheared N tile
   int nk_shear;               // exchange: Nk of the shear
   // Product modes.  MODE_FULL: hi*hi + hi*lo + lo*hi (N tile 256); with xonly set
-  // (complex only) the hi*hi products are left out.  MODE_HH (complex only): the
-  // hi*hi products alone, N tile 128, one FP32 accumulator per real product
-  // (rr, ii, ri, ir), summed in the epilogue.  The tensor core's accumulation
+  // (complex only) the hi*hi products are left out.  MODE_HH (complex only, B never
+  // conjugated): the hi*hi products alone, N tile 64, one FP32 accumulator per real
+  // product (rr, ri, ir, ii: one MMA of N = 128 per A plane over B's re and im
+  // tiles), summed in the epilogue; 256 TMEM columns, so two tiles in flight.  The tensor core's accumulation
   // truncates at every MMA, so a product whose result is a small difference of
   // large sums (the W - W^H form of dC, dD) takes its hi*hi part in MODE_HH with
   // split-K (short truncating chains) and its hi*lo + lo*hi part, 2^-11 smaller,
