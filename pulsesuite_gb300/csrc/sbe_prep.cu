@@ -399,8 +399,25 @@ __global__ void __launch_bounds__(128) k_offdiag_D32(const WireDev* wires, const
 // all NW wires, so that every shared-memory weight load (32 p at a time, [p][wire]
 // as float2, read as float4) feeds 2 KPT FMAs; the a-a Lorentzian window slides in
 // registers.  Rows q and -q as in k_offdiag_D32.  grid (Nk / (128 KPT), Nk + 1, species).
+// Packed FP32 pairs (PTX f32x2, sm_100 and later): one fma.rn.f32x2 forms two
+// IEEE FP32 fused multiply-adds (each rounded as fmaf) from one issue slot.
+__device__ __forceinline__ unsigned long long f2_splat(float a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ void f2_fma(unsigned long long& d, unsigned long long a,
+                                       unsigned long long b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long a) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a));
+  return r;
+}
+
 template <int NW, int KPT>
-__global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, const int* wl,
+__global__ void __launch_bounds__(128, 2) k_offdiag_D32g(const WireDev* wires, const int* wl,
                                                       int nwl, const float* occf,
                                                       const float* dconst, const float* dpre,
                                                       double* De, double* Dh) {
@@ -448,11 +465,13 @@ __global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, cons
     sob[tid] = ob;
   }
   const int k0 = (blockIdx.x * blockDim.x + tid) * KPT;   // this thread's first k
-  float ax[KPT][NW], ay[KPT][NW];
+  // sums (x, y) of wire w at k0 + j as one packed FP32 pair; the weights of a
+  // wire are the pair (x, y) in shared memory, so one f32x2 FMA updates both
+  unsigned long long acc[KPT][NW];
 #pragma unroll
   for (int j = 0; j < KPT; ++j)
 #pragma unroll
-    for (int w = 0; w < NW; ++w) ax[j][w] = ay[j][w] = 0.f;
+    for (int w = 0; w < NW; ++w) acc[j][w] = 0ull;
   if (inq) {
     // a-a: p in [q + 1, Nk - 1], Lorentzian of alpha q (k - p + q) from the table;
     // index of (k, p) is k - p + Nk - 1: the window holds k0 .. k0 + KPT - 1
@@ -481,16 +500,17 @@ __global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, cons
       __syncthreads();
       const int pend = min(PC, nk - p0);
       for (int pp = 0; pp < pend; ++pp) {
-        const float4* w4 = reinterpret_cast<const float4*>(ws + pp * NW);
+        const ulonglong2* w4 = reinterpret_cast<const ulonglong2*>(ws + pp * NW);
+        unsigned long long ll[KPT];
+#pragma unroll
+        for (int j = 0; j < KPT; ++j) ll[j] = f2_splat(l[j]);
 #pragma unroll
         for (int w2 = 0; w2 < NW / 2; ++w2) {
-          const float4 v = w4[w2];
+          const ulonglong2 v = w4[w2];
 #pragma unroll
           for (int j = 0; j < KPT; ++j) {
-            ax[j][2 * w2] = fmaf(l[j], v.x, ax[j][2 * w2]);
-            ay[j][2 * w2] = fmaf(l[j], v.y, ay[j][2 * w2]);
-            ax[j][2 * w2 + 1] = fmaf(l[j], v.z, ax[j][2 * w2 + 1]);
-            ay[j][2 * w2 + 1] = fmaf(l[j], v.w, ay[j][2 * w2 + 1]);
+            f2_fma(acc[j][2 * w2], ll[j], v.x);
+            f2_fma(acc[j][2 * w2 + 1], ll[j], v.y);
           }
         }
         // next p: every index - 1
@@ -536,16 +556,17 @@ __global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, cons
           // 1/(1+u^2) >= 1e-38: the approximate reciprocal (~1 ulp) suffices
           asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(L[j]) : "f"(fmaf(u, u, 1.0f)));
         }
-        const float4* w4 = reinterpret_cast<const float4*>(ws + pp * NW);
+        const ulonglong2* w4 = reinterpret_cast<const ulonglong2*>(ws + pp * NW);
+        unsigned long long ll[KPT];
+#pragma unroll
+        for (int j = 0; j < KPT; ++j) ll[j] = f2_splat(L[j]);
 #pragma unroll
         for (int w2 = 0; w2 < NW / 2; ++w2) {
-          const float4 v = w4[w2];
+          const ulonglong2 v = w4[w2];
 #pragma unroll
           for (int j = 0; j < KPT; ++j) {
-            ax[j][2 * w2] = fmaf(L[j], v.x, ax[j][2 * w2]);
-            ay[j][2 * w2] = fmaf(L[j], v.y, ay[j][2 * w2]);
-            ax[j][2 * w2 + 1] = fmaf(L[j], v.z, ax[j][2 * w2 + 1]);
-            ay[j][2 * w2 + 1] = fmaf(L[j], v.w, ay[j][2 * w2 + 1]);
+            f2_fma(acc[j][2 * w2], ll[j], v.x);
+            f2_fma(acc[j][2 * w2 + 1], ll[j], v.y);
           }
         }
       }
@@ -571,11 +592,12 @@ __global__ void __launch_bounds__(128) k_offdiag_D32g(const WireDev* wires, cons
         continue;
       }
       const float nak = na[k];
-      Dp[k] = f32_to_f64((1.f - nak) * ax[j][w] + nak * ay[j][w]);
+      const float2 sxy = f2_unpack(acc[j][w]);
+      Dp[k] = f32_to_f64((1.f - nak) * sxy.x + nak * sxy.y);
       if (q > 0) {
         const float f = svaa[w] * lq;
-        const float xa = ay[j][w] + f * ((1.f - sn0[w]) * snq[w]);
-        const float xb = ax[j][w] + f * (sn0[w] * (1.f - snq[w]));
+        const float xa = sxy.y + f * ((1.f - sn0[w]) * snq[w]);
+        const float xb = sxy.x + f * (sn0[w] * (1.f - snq[w]));
         const float nk2 = na[k + q];
         Dm[k + q] = f32_to_f64((1.f - nk2) * xa + nk2 * xb);
       }
