@@ -238,6 +238,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const long long sA = plane_slab(d.A), sB = plane_slab(d.B);
       const long long kstepA = (long long)d.A.rows_pad * BK, kstepB = (long long)d.B.rows_pad * BK;
       const int pstep = HH ? 2 : 1;   // MODE_HH loads planes re_hi, im_hi
+      // a last N tile narrower than BNT (MODE_FULL) loads only the B rows its
+      // MMAs read, rounded up to the 64-row tile granule
+      const int nrem = d.N - ti.n0;
+      const int bbytes = (HH || nrem >= BNT) ? BTB : ((nrem + 63) & ~63) * BK * 2;
+      const uint32_t tx_bytes = (uint32_t)(npl * (A_TILE_BYTES + bbytes));
       int s = (int)(g % nstage);
       uint32_t ph = (uint32_t)((g / nstage) & 1);
       for (int term = 0; ok && term < d.nterms && ti.nkb > 0; ++term) {
@@ -254,12 +259,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
           uint8_t* sa = smem + s * stage_bytes;
           uint8_t* sb = sa + npl * A_TILE_BYTES;
-          mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+          mbar_expect_tx(&full[s], tx_bytes);
           const __half* ga = ga0 + kk * kstepA;
           const __half* gb = gb0 + kk * kstepB;
           for (int p = 0; p < npl; ++p) {
             bulk_load(sa + p * A_TILE_BYTES, ga + p * pA, A_TILE_BYTES, &full[s]);
-            bulk_load(sb + p * BTB, gb + p * pB, BTB, &full[s]);
+            bulk_load(sb + p * BTB, gb + p * pB, bbytes, &full[s]);
           }
           if (++s == nstage) {
             s = 0;
@@ -277,7 +282,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
     constexpr int MMA_N = HH ? 2 * BNT : BNT;
-    const uint32_t id_pos = idesc_f16(BM, MMA_N, 0), id_neg = idesc_f16(BM, MMA_N, 1);
+    const uint32_t id_pos_full = idesc_f16(BM, MMA_N, 0), id_neg_full = idesc_f16(BM, MMA_N, 1);
     long long g = 0;
     bool ok = true;
     for (int lt = 0; ok; ++lt) {
@@ -289,6 +294,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const bool hh = !d.xonly;
+      // a last N tile narrower than BNT (MODE_FULL): MMAs of N rounded up to 16
+      const int nrem = d.N - ti.n0;
+      const bool narrow = !HH && nrem < BNT;
+      const uint32_t id_pos = narrow ? idesc_f16(BM, (nrem + 15) & ~15, 0) : id_pos_full;
+      const uint32_t id_neg = narrow ? idesc_f16(BM, (nrem + 15) & ~15, 1) : id_neg_full;
       const int buf = lt % nbuf, use = lt / nbuf;
       if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) break;
       tc_fence_after();
@@ -391,6 +401,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       constexpr int NCH = BNT / 32;   // 16-column chunks per column half
       for (int cc = 0; cc < NCH; ++cc) {
         const int c = half * NCH + cc;   // chunk of the tile
+        if (ti.n0 + c * 16 >= d.N) {
+          // chunk beyond the matrix: nothing to read or store
+          if (cc == NCH - 1) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[buf]);
+          }
+          continue;
+        }
         float re[16], im[16];
         if (have && HH) {
           // buffer columns [rr | ri | ir | -ii] (BNT each): re = rr + ii, im = ri + ir
