@@ -105,9 +105,6 @@ __device__ __forceinline__ float2 scaled2<float2>(float2 v, int e) {
   return make_float2(f32_ldexp(v.x, e), f32_ldexp(v.y, e));
 }
 
-// With tpart set (double input only), the block also writes the 63 diagonal sums
-// of its 32 x 32 tile to tpart[((b * 2 + which) * T + bi) * T + bj][l], local
-// diagonal l = c - r + 31, for the traces of C and D.
 // With cdf set, the diagonal is left out of the planes (written as zero) and the
 // hi / lo FP32 parts of its real part (from dg[b * nk + k] in FP64 when given) go
 // to cdf[b * nk + k] and cdf[nbatch * nk + b * nk + k].
@@ -153,27 +150,35 @@ __device__ __forceinline__ void store_tiles_t(const __half (*hs)[32][40], int np
 
 // Both layouts of a batch of Nk x Nk complex matrices from one read: planes of X
 // into matrix slot matN and of X^T into slot matT (matT < 0: none), same scale.
-// The block converts its 32 x 32 tile once into shared-memory plane tiles and
-// writes both layouts with 16-byte stores.
+// The block (32 x 8 threads) converts its 32 x 32 tile once into shared-memory
+// plane tiles and writes both layouts with 16-byte stores.
 template <typename T>
 __global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, int matN, int matT,
-                            int nbatch, float2* tpart = nullptr, int which = 0,
-                            float* cdf = nullptr, const double* dg = nullptr) {
+                            int nbatch, float* cdf = nullptr, const double* dg = nullptr) {
   __shared__ T tile[32][33];
   __shared__ __align__(16) __half hs[4][32][40];
   const int b = blockIdx.z;
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
   const T* x = X + (long long)b * nk * nk;
-  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-    const int r = r0 + i, c = c0 + threadIdx.x;
-    T z;
-    z.x = 0;
-    z.y = 0;
-    tile[i][threadIdx.x] = (r < nk && c < nk) ? x[(long long)r * nk + c] : z;
+  {
+    // block (32, 8): four rows per thread, all loads issued before the stores
+    T v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int r = r0 + threadIdx.y + 8 * k, c = c0 + threadIdx.x;
+      T z;
+      z.x = 0;
+      z.y = 0;
+      v[k] = (r < nk && c < nk) ? x[(long long)r * nk + c] : z;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tile[threadIdx.y + 8 * k][threadIdx.x] = v[k];
   }
   __syncthreads();
   const int eb = e[b];
-  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = threadIdx.y + 8 * k;
     const int r = r0 + i, c = c0 + threadIdx.x;
     float2 v = scaled2<T>(tile[i][threadIdx.x], eb);
     if (cdf && r == c && r < nk) {
@@ -190,44 +195,23 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, 
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
   store_tiles(hs, 4, dst, matN, b, r0, c0 >> 5, tid, nth);
   if (matT >= 0) store_tiles_t(hs, 4, dst, matT, b, c0, r0 >> 5, tid, nth);
-  if (tpart) {
-    if (tid < 63) {
-      const int l = tid - 31;   // c - r
-      float sr = 0.f, si = 0.f;
-      for (int rr = 0; rr < 32; ++rr) {
-        const int cc = rr + l;
-        if (cc < 0 || cc >= 32) continue;
-        const float2 v = scaled2<T>(tile[rr][cc], 0);
-        sr += v.x;
-        si += v.y;
-      }
-      const int Tn = gridDim.x;
-      tpart[((((long long)b * 2 + which) * Tn + blockIdx.y) * Tn + blockIdx.x) * 63 + tid] =
-          make_float2(sr, si);
-    }
-  }
 }
 
-// Traces tr_d = sum over the 63-diagonal tile partials along diagonal d, fixed
-// order: trf[b][which][d + nk] (SBEs.py:1094-1103 direct terms).
-__global__ void k_trace_reduce(int nk, const float2* tpart, float2* trf) {
+// Traces from the diagonal partials of k_shear_tiles: diagonal dd = k1 - k2 + Nk - 1
+// of X (row k1, column k2) is trace index d + Nk with d = k2 - k1, summed over the
+// nb column blocks in a fixed order into trf[b][which][d + Nk] (SBEs.py:1094-1103).
+__global__ void k_trace_from_shear(int nk, int nb, int ndd, const float2* dpart, float2* trf) {
   const int b = blockIdx.z, which = blockIdx.y;
-  const int dd = blockIdx.x * blockDim.x + threadIdx.x;   // d + nk - 1
+  const int dd = blockIdx.x * blockDim.x + threadIdx.x;
   if (dd >= 2 * nk - 1) return;
-  const int d = dd - (nk - 1);
-  const int Tn = (nk + 31) / 32;
-  const float2* part = tpart + ((long long)b * 2 + which) * Tn * Tn * 63;
+  const float2* part = dpart + (((long long)b * 2 + which) * ndd + dd) * nb;
   float sr = 0.f, si = 0.f;
-  for (int o = -(Tn - 1); o < Tn; ++o) {
-    const int l = d - 32 * o + 31;
-    if (l < 0 || l >= 63) continue;
-    for (int bi = max(0, -o); bi < Tn && bi + o < Tn; ++bi) {
-      const float2 v = part[((long long)bi * Tn + bi + o) * 63 + l];
-      sr += v.x;
-      si += v.y;
-    }
+  for (int i = 0; i < nb; ++i) {
+    const float2 v = part[i];
+    sr += v.x;
+    si += v.y;
   }
-  trf[(long long)b * 4 * nk + which * 2 * nk + d + nk] = make_float2(sr, si);
+  trf[(long long)b * 4 * nk + which * 2 * nk + (2 * nk - 1 - dd)] = make_float2(sr, si);
 }
 
 void launch_exponents(const double2* X, long long per_batch, long long bstride, int nbatch,
@@ -276,7 +260,7 @@ struct Mixed {
   // per-step FP32 tables
   float* phf = nullptr;     // 2 x nw x nk: Vep(d) 2^-sP, Vhp(d) 2^-sP
   float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
-  float2* tpart = nullptr;  // nw x 2 x T x T x 63 partial diagonal sums (T = ceil(nk/32))
+  float2* tpart = nullptr;  // nw x 2 x 32 ceil(2nk/32) x T diagonal partials (T = ceil(nk/32))
   float* cdf = nullptr;     // 4 x nw x nk: hi / lo parts of Re C_kk and Re D_kk (stage state)
   double* xdg = nullptr;    // 2 x nw x nk: Re C_kk, Re D_kk of the stage state in FP64
   int* eS() { return ints; }
@@ -458,7 +442,8 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   void* cblock = nullptr;
   if (cudaMalloc(&cblock, cbytes) != cudaSuccess ||
       cudaMalloc(&m->ekrf, sizeof(float2) * (size_t)c->tot_kr) != cudaSuccess ||
-      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * T * T * 63) != cudaSuccess ||
+      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * 32 * ((2 * nk + 31) / 32) * T) !=
+          cudaSuccess ||
       cudaMalloc(&m->xdg, sizeof(double) * 2 * (size_t)nw * nk) != cudaSuccess) {
     if (cblock) cudaFree(cblock);
     m->epf = nullptr;
@@ -588,7 +573,9 @@ __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const 
   const int eb = e[b];
   const double* v = vs + 3 * W.off_vec + n * nk;
   const int tp = c0 + tx;
-  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = threadIdx.y + 8 * k;
     const int t = t0 + i;
     float f = 0.f;
     if (t < nk && tp < nk) {
@@ -625,18 +612,33 @@ __global__ void k_hab(const WireDev* wires, const double* De, const double* Dh, 
   const int j0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   const int qbase = j0 - k0 - 31 + nk;
   const bool on_w = (W.flags & SBE_F_OFFDIAGDPH) != 0;
-  for (int qq = threadIdx.y; qq < 63; qq += blockDim.y) {
-    const int q = qbase + qq, k = k0 + threadIdx.x;
-    const bool ok = on_w && q >= 0 && q <= 2 * nk && k < nk;
-    const long long di = W.off_dd + (long long)q * nk + k;
-    ta[qq][threadIdx.x] = ok ? Dh[di] : 0.0;
-    tb[qq][threadIdx.x] = ok ? De[di] : 0.0;
+  {
+    // block (32, 8): eight rows per thread, all loads issued before the stores
+    double va[8], vb[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int qq = threadIdx.y + 8 * i, q = qbase + qq, k = k0 + threadIdx.x;
+      const bool ok = on_w && qq < 63 && q >= 0 && q <= 2 * nk && k < nk;
+      const long long di = W.off_dd + (long long)q * nk + k;
+      va[i] = ok ? Dh[di] : 0.0;
+      vb[i] = ok ? De[di] : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int qq = threadIdx.y + 8 * i;
+      if (qq < 63) {
+        ta[qq][threadIdx.x] = va[i];
+        tb[qq][threadIdx.x] = vb[i];
+      }
+    }
   }
   __syncthreads();
   const float hb = (float)kHbar;
   float m = 0.f;
   const int j = j0 + threadIdx.x;
-  for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int kk = threadIdx.y + 8 * i;
     const int k = k0 + kk;
     if (k >= nk || j >= nk) continue;
     const int qq = (j - k) - (j0 - k0) + 31;
@@ -647,8 +649,15 @@ __global__ void k_hab(const WireDev* wires, const double* De, const double* Dh, 
     habf[tot_mat + o] = hh;
     m = fmaxf(m, 2.f * fmaxf(fabsf(ha), fabsf(hh)));
   }
+  // one atomic per block (same-address atomics serialise)
+  __shared__ float red[8];
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(mx + blockIdx.z, __float_as_uint(m));
+  if (threadIdx.x == 0) red[threadIdx.y] = m;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+    atomicMax(mx + blockIdx.z, __float_as_uint(m));
+  }
 }
 
 // Per-step weights of CalcGammaE/H (dephasing.py:29-103) per q: (pi/hbar) V^2 |x|
@@ -889,9 +898,13 @@ __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH
 // lie in rows t0 + dd0 - (Nk - 1) ... + 62 of columns t0 ... t0 + 31, which are
 // read row by row (coalesced) into shared memory and then read along diagonals
 // (row stride 32 double2: diagonal reads are free of bank conflicts).
-// blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire.
+// blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire; block (32, 8).
+// For C and D the block also writes the sums of its 32 values of every diagonal
+// (unscaled FP32, a fixed butterfly order) to
+// dpart[((b * 2 + n - 1) * 32 gridDim.y + dd) * gridDim.x + blockIdx.x]; the
+// traces of the direct Coulomb terms are their sums over blockIdx.x.
 __global__ void k_shear_tiles(int nk, int nw, const float2* X0, const float2* X1,
-                              const float2* X2, const int* e, tc::PlaneSet dst) {
+                              const float2* X2, const int* e, tc::PlaneSet dst, float2* dpart) {
   __shared__ float2 tile[63][32];
   __shared__ __align__(16) __half hs[2][64][40];   // hi, lo of rows 2 dd0 .. 2 dd0 + 63
   const int n = blockIdx.z / nw, b = blockIdx.z % nw;
@@ -899,19 +912,46 @@ __global__ void k_shear_tiles(int nk, int nw, const float2* X0, const float2* X1
   const int t0 = blockIdx.x * 32, dd0 = blockIdx.y * 32;
   const int rbase = t0 + dd0 - (nk - 1);
   const int tx = threadIdx.x;
+  float2* dp = n > 0 ? dpart + (((long long)b * 2 + n - 1) * 32 * gridDim.y + dd0) * gridDim.x +
+                           blockIdx.x
+                     : nullptr;
   // blocks whose source rows all lie outside the matrix hold only zeros, which
   // the buffer keeps from its initialisation
-  if (rbase + 62 < 0 || rbase >= nk) return;
-  for (int rr = threadIdx.y; rr < 63; rr += blockDim.y) {
-    const int r = rbase + rr, c = t0 + tx;
-    tile[rr][tx] = (r >= 0 && r < nk && c < nk) ? X[(long long)r * nk + c] : make_float2(0, 0);
+  if (rbase + 62 < 0 || rbase >= nk) {
+    const int t = threadIdx.y * blockDim.x + tx;
+    if (dp && t < 32) dp[(long long)t * gridDim.x] = make_float2(0.f, 0.f);
+    return;
+  }
+  {
+    // block (32, 8): eight rows per thread, all loads issued before the stores
+    float2 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int rr = threadIdx.y + 8 * k, r = rbase + rr, c = t0 + tx;
+      const bool ok = rr < 63 && r >= 0 && r < nk && c < nk;
+      v[k] = ok ? X[(long long)r * nk + c] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (threadIdx.y + 8 * k < 63) tile[threadIdx.y + 8 * k][tx] = v[k];
   }
   __syncthreads();
   const int eb = e[b];
-  for (int ddl = threadIdx.y; ddl < 32; ddl += blockDim.y) {
+#pragma unroll
+  for (int kd = 0; kd < 4; ++kd) {
+    const int ddl = threadIdx.y + 8 * kd;
     // element (dd0 + ddl, t0 + tx) of the shear: source row rbase + tx + ddl (the
     // tile is zero outside the band and the matrix)
     const float2 t = tile[tx + ddl][tx];
+    if (dp) {
+      float sr = t.x, si = t.y;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+      }
+      if (tx == 0) dp[(long long)ddl * gridDim.x] = make_float2(sr, si);
+    }
     const float2 v = make_float2(f32_ldexp(t.x, eb), f32_ldexp(t.y, eb));
     const __half2 hi = __float22half2_rn(v);
     const float2 hf = __half22float2(hi);
@@ -1481,20 +1521,23 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   const long long vn = (long long)nw * nk;
   k_planes_nt<float2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw, m->tpart, 0,
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw,
                                         m->cdf, dgC);
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw, m->tpart, 1,
+  k_planes_nt<float2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw,
                                         m->cdf + 2 * vn, dgD);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
   k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
-  k_trace_reduce<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, m->tpart, m->trf);
   int rc = SBE_OK;
   const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
   if (have_x) {
     k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
-    k_shear_tiles<<<dim3((nk + 31) / 32, (2 * nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
-        nk, nw, P, C, D, m->eS(), m->sp);
+    // the traces of C and D (direct terms) come from the shear's diagonal partials
+    const int nb = (nk + 31) / 32, ndd = 32 * ((2 * nk + 31) / 32);
+    k_shear_tiles<<<dim3(nb, ndd / 32, 3 * nw), dim3(32, 8), 0, s>>>(nk, nw, P, C, D, m->eS(),
+                                                                   m->sp, m->tpart);
+    k_trace_from_shear<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, nb, ndd,
+                                                                             m->tpart, m->trf);
     // the three exchange products (eh, ee, hh) as one persistent launch
     tc::GemmJob jobs[3];
     for (int n = 0; n < 3; ++n) {
