@@ -197,6 +197,18 @@ __global__ void k_planes_nt(const T* X, int nk, const int* e, tc::PlaneSet dst, 
   if (matT >= 0) store_tiles_t(hs, 4, dst, matT, b, c0, r0 >> 5, tid, nth);
 }
 
+// Band of the sheared state planes (k_shear_tiles): the first dd block of the
+// t' block at t0 whose source rows can reach the matrix, and whether the block
+// (t0, dd0) holds any element of it.
+__host__ __device__ inline int shear_first_block(int nk, int t0) {
+  const int lo = nk - 63 - t0;   // lowest dd whose 63 source rows reach row 0
+  return lo > 0 ? lo / 32 : 0;
+}
+__host__ __device__ inline bool shear_block_live(int nk, int t0, int dd0) {
+  const int rbase = t0 + dd0 - (nk - 1);
+  return rbase + 62 >= 0 && rbase < nk;
+}
+
 // Traces from the diagonal partials of k_shear_tiles: diagonal dd = k1 - k2 + Nk - 1
 // of X (row k1, column k2) is trace index d + Nk with d = k2 - k1, summed over the
 // nb column blocks in a fixed order into trf[b][which][d + Nk] (SBEs.py:1094-1103).
@@ -207,6 +219,7 @@ __global__ void k_trace_from_shear(int nk, int nb, int ndd, const float2* dpart,
   const float2* part = dpart + (((long long)b * 2 + which) * ndd + dd) * nb;
   float sr = 0.f, si = 0.f;
   for (int i = 0; i < nb; ++i) {
+    if (!shear_block_live(nk, 32 * i, dd & ~31)) continue;   // no block, all zero
     const float2 v = part[i];
     sr += v.x;
     si += v.y;
@@ -897,61 +910,62 @@ __global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH
 // A block writes dd in [dd0, dd0 + 32) x t' in [t0, t0 + 32); the source elements
 // lie in rows t0 + dd0 - (Nk - 1) ... + 62 of columns t0 ... t0 + 31, which are
 // read row by row (coalesced) into shared memory and then read along diagonals
-// (row stride 32 double2: diagonal reads are free of bank conflicts).
-// blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire; block (32, 8).
-// For C and D the block also writes the sums of its 32 values of every diagonal
-// (unscaled FP32, a fixed butterfly order) to
-// dpart[((b * 2 + n - 1) * 32 gridDim.y + dd) * gridDim.x + blockIdx.x]; the
-// traces of the direct Coulomb terms are their sums over blockIdx.x.
-__global__ void k_shear_tiles(int nk, int nw, const float2* X0, const float2* X1,
+// (row stride 32 float2: diagonal reads are free of bank conflicts).
+// The grid covers only the band: blockIdx.y counts the dd blocks from
+// shear_first_block(t0) on (the other blocks hold zeros, which the buffer keeps
+// from its initialisation); blockIdx.z = matrix n (0 P, 1 C, 2 D) * Nw + wire;
+// block (32, 8).
+// For C and D the block also writes the sum of its 32 values of every diagonal
+// (unscaled FP32, in the fixed order t' = ddl, ddl + 1, ... cyclically) to
+// dpart[((b * 2 + n - 1) * ndd + dd) * gridDim.x + blockIdx.x]; the traces of the
+// direct Coulomb terms are their sums over the blocks that exist.
+__global__ void k_shear_tiles(int nk, int nw, int ndd, const float2* X0, const float2* X1,
                               const float2* X2, const int* e, tc::PlaneSet dst, float2* dpart) {
   __shared__ float2 tile[63][32];
   __shared__ __align__(16) __half hs[2][64][40];   // hi, lo of rows 2 dd0 .. 2 dd0 + 63
   const int n = blockIdx.z / nw, b = blockIdx.z % nw;
+  const int t0 = blockIdx.x * 32;
+  const int dd0 = (shear_first_block(nk, t0) + blockIdx.y) * 32;
+  if (dd0 >= ndd || !shear_block_live(nk, t0, dd0)) return;
   const float2* X = (n == 0 ? X0 : n == 1 ? X1 : X2) + (long long)b * nk * nk;
-  const int t0 = blockIdx.x * 32, dd0 = blockIdx.y * 32;
   const int rbase = t0 + dd0 - (nk - 1);
-  const int tx = threadIdx.x;
-  float2* dp = n > 0 ? dpart + (((long long)b * 2 + n - 1) * 32 * gridDim.y + dd0) * gridDim.x +
-                           blockIdx.x
-                     : nullptr;
-  // blocks whose source rows all lie outside the matrix hold only zeros, which
-  // the buffer keeps from its initialisation
-  if (rbase + 62 < 0 || rbase >= nk) {
-    const int t = threadIdx.y * blockDim.x + tx;
-    if (dp && t < 32) dp[(long long)t * gridDim.x] = make_float2(0.f, 0.f);
-    return;
-  }
+  const int tx = threadIdx.x, ty = threadIdx.y;
   {
-    // block (32, 8): eight rows per thread, all loads issued before the stores
+    // eight rows per thread, all loads issued before the stores
+    const int c = t0 + tx;
     float2 v[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const int rr = threadIdx.y + 8 * k, r = rbase + rr, c = t0 + tx;
+      const int rr = ty + 8 * k, r = rbase + rr;
       const bool ok = rr < 63 && r >= 0 && r < nk && c < nk;
       v[k] = ok ? X[(long long)r * nk + c] : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (threadIdx.y + 8 * k < 63) tile[threadIdx.y + 8 * k][tx] = v[k];
+      if (ty + 8 * k < 63) tile[ty + 8 * k][tx] = v[k];
   }
   __syncthreads();
+  if (n > 0 && ty == 0) {
+    // diagonal partials: lane ddl starts at t' = ddl, so that the 32 lanes read
+    // 32 different banks pairs at every step
+    float sr = 0.f, si = 0.f;
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int t = (tx + i) & 31;
+      const float2 v = tile[t + tx][t];
+      sr += v.x;
+      si += v.y;
+    }
+    dpart[(((long long)b * 2 + n - 1) * ndd + dd0 + tx) * gridDim.x + blockIdx.x] =
+        make_float2(sr, si);
+  }
   const int eb = e[b];
 #pragma unroll
   for (int kd = 0; kd < 4; ++kd) {
-    const int ddl = threadIdx.y + 8 * kd;
+    const int ddl = ty + 8 * kd;
     // element (dd0 + ddl, t0 + tx) of the shear: source row rbase + tx + ddl (the
     // tile is zero outside the band and the matrix)
     const float2 t = tile[tx + ddl][tx];
-    if (dp) {
-      float sr = t.x, si = t.y;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(0xffffffffu, sr, o);
-        si += __shfl_xor_sync(0xffffffffu, si, o);
-      }
-      if (tx == 0) dp[(long long)ddl * gridDim.x] = make_float2(sr, si);
-    }
     const float2 v = make_float2(f32_ldexp(t.x, eb), f32_ldexp(t.y, eb));
     const __half2 hi = __float22half2_rn(v);
     const float2 hf = __half22float2(hi);
@@ -962,8 +976,12 @@ __global__ void k_shear_tiles(int nk, int nw, const float2* X0, const float2* X1
     hs[1][2 * ddl + 1][tx] = __high2half(lo);
   }
   __syncthreads();
-  const int tid = threadIdx.y * blockDim.x + tx, nth = blockDim.x * blockDim.y;
-  for (int t = tid; t < 2 * 64 * 4; t += nth) {
+  // 2 planes x 64 rows x 4 chunks of 16 bytes: two per thread; the rows of a plane
+  // are contiguous in K-block t0 / 32
+  const int tid = ty * 32 + tx;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int t = tid + 256 * u;
     const int pl = t >> 8, rr = (t >> 2) & 63, j = t & 3;
     const uint4 v = *reinterpret_cast<const uint4*>(&hs[pl][rr][8 * j]);
     *reinterpret_cast<uint4*>(dst.ptr + tc::chunk_elem(dst, n, pl, b, 2 * dd0 + rr, t0 >> 5, j)) =
@@ -1130,6 +1148,7 @@ struct Rk4Ctl {
   int stage, peel;
   float dt;
   double2* X;      // FP64 state of this matrix, all wires
+  const float2* x0;  // FP32 copy of the step-start state (stages 1-3)
   float2* acc;     // RK4 sums
   float2* xf;      // next stage state (FP32); may alias the pass's stage-state input
   double* dg;      // FP64 diagonal of the next stage state (C, D) or nullptr
@@ -1139,7 +1158,6 @@ struct Rk4Ctl {
 
 __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, float2 kv, bool diag,
                                                long long dgi) {
-  const double2 x = r.X[i];
   if (r.stage < 4) {
     const float f = (r.stage == 1 || r.stage == 2) ? 0.5f * r.dt : r.dt;
     if (r.stage == 1) {
@@ -1148,12 +1166,13 @@ __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, flo
       const float2 a = r.acc[i];
       r.acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
     }
-    const float2 xs = f64_to_f32(x);
+    const float2 xs = r.x0[i];   // fp32 of the FP64 state, converted once per step
     const float2 v = make_float2(xs.x + f * kv.x, xs.y + f * kv.y);
     r.xf[i] = v;
-    if (diag && r.dg) r.dg[dgi] = x.x + f32_to_f64(f * kv.x);
+    if (diag && r.dg) r.dg[dgi] = r.X[i].x + f32_to_f64(f * kv.x);
     return max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu);
   }
+  const double2 x = r.X[i];
   const float2 a = r.acc[i];
   const float sc = r.dt / 6.f;
   const double2 v = make_double2(x.x + f32_to_f64(sc * (a.x + kv.x)),
@@ -1534,8 +1553,15 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
     k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
     // the traces of C and D (direct terms) come from the shear's diagonal partials
     const int nb = (nk + 31) / 32, ndd = 32 * ((2 * nk + 31) / 32);
-    k_shear_tiles<<<dim3(nb, ndd / 32, 3 * nw), dim3(32, 8), 0, s>>>(nk, nw, P, C, D, m->eS(),
-                                                                   m->sp, m->tpart);
+    int ny = 0;   // dd blocks of the band per t' block
+    for (int i = 0; i < nb; ++i) {
+      int cnt = 0;
+      for (int j = shear_first_block(nk, 32 * i); 32 * j < ndd; ++j)
+        if (shear_block_live(nk, 32 * i, 32 * j)) cnt = j - shear_first_block(nk, 32 * i) + 1;
+      ny = std::max(ny, cnt);
+    }
+    k_shear_tiles<<<dim3(nb, ny, 3 * nw), dim3(32, 8), 0, s>>>(nk, nw, ndd, P, C, D, m->eS(),
+                                                              m->sp, m->tpart);
     k_trace_from_shear<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, nb, ndd,
                                                                              m->tpart, m->trf);
     // the three exchange products (eh, ee, hh) as one persistent launch
@@ -1616,15 +1642,18 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   }
   const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
   Rk4Ctl rk[3];
-  float2* xf = reinterpret_cast<float2*>(c->xs);
+  // stage buffers (FP32, 3 tm each): the step-start state, then the stage states
+  float2* x0 = reinterpret_cast<float2*>(c->xs);
+  float2* xn = x0 + 3 * tm;
   for (int i = 0; i < 3; ++i) {
     rk[i] = Rk4Ctl{};
     rk[i].stage = stage;
     rk[i].peel = i > 0;
     rk[i].dt = dt;
     rk[i].X = X64 ? X64[i] : nullptr;
+    rk[i].x0 = x0 + i * tm;
     rk[i].acc = m->accf + i * tm;
-    rk[i].xf = xf + i * tm;
+    rk[i].xf = xn + i * tm;
     rk[i].dg = i > 0 ? m->xdg + (i - 1) * vn : nullptr;
     rk[i].mx = m->mxS();
     rk[i].mo = m->mxO();
@@ -1720,13 +1749,16 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   const long long n = c->tot_mat;
   const double frac[4] = {0.0, 0.5, 0.5, 1.0};
   const long long vn = (long long)m->nw * m->nk;
-  float2* xf = reinterpret_cast<float2*>(c->xs);
+  // FP32 stage buffers in the FP64 stage-state block (6 tm float2): the step-start
+  // state (kept for the RK4 updates), then the stage states of stages 2-4
+  float2* x0 = reinterpret_cast<float2*>(c->xs);
   mixed_state_in(c, P, C, D, s);
   double2* X64[3] = {P, C, D};
   for (int st = 1; st <= 4; ++st) {
     launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
     // the RHS of this stage and its RK4 update (fused into the element-wise passes)
-    rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, c->ekst, st, (float)dt, X64,
+    float2* xs = st == 1 ? x0 : x0 + 3 * n;
+    rc = mixed_stage(c, xs, xs + n, xs + 2 * n, m->xdg, m->xdg + vn, c->ekst, st, (float)dt, X64,
                      s);
     if (rc) return rc;
   }
