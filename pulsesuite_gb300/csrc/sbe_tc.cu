@@ -43,12 +43,36 @@ __global__ void k_exponents(int nb, const unsigned* mx, int* e, const int* add, 
   if (sum) sum[b] = v + (add ? add[b] : 0);
 }
 
-// e[b] from the larger of two maxima (same rule as k_exponents)
-__global__ void k_exponents2(int nb, const unsigned* mx1, const unsigned* mx2, int* e) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
+// The exponents of one stage in one launch (one thread per wire): eS from the
+// full state maximum, eO from the off-diagonal one, esx = eT + eS (exchange
+// products); with reset set the maxima are cleared for the fused RK4 update of
+// the stage, which collects the next state's maxima in them; mxH is cleared for
+// the stage's Hamiltonian.
+__global__ void k_stage_exponents(int nb, unsigned* mxS, unsigned* mxO, unsigned* mxH, int* eS,
+                                  int* eO, const int* eT, int* esx, int reset) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb) return;
-  float m = fmaxf(__uint_as_float(mx1[b]), __uint_as_float(mx2[b])) * 1.0001f;
-  e[b] = (m > 0.f) ? 14 - (int)ceilf(log2f(m)) : 0;
+  const float ms = __uint_as_float(mxS[b]) * 1.0001f, mo = __uint_as_float(mxO[b]) * 1.0001f;
+  const int vs = (ms > 0.f) ? 14 - (int)ceilf(log2f(ms)) : 0;
+  eS[b] = vs;
+  eO[b] = (mo > 0.f) ? 14 - (int)ceilf(log2f(mo)) : 0;
+  esx[b] = eT[b] + vs;
+  mxH[b] = 0u;
+  if (reset) {
+    mxS[b] = 0u;
+    mxO[b] = 0u;
+  }
+}
+
+// e[b] from the larger of two maxima (rule of k_exponents) and sum[b] = e[b] + add[b]
+__global__ void k_exponents2_sum(int nb, const unsigned* mx1, const unsigned* mx2, int* e,
+                                 const int* add, int* sum) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float m = fmaxf(__uint_as_float(mx1[b]), __uint_as_float(mx2[b])) * 1.0001f;
+  const int v = (m > 0.f) ? 14 - (int)ceilf(log2f(m)) : 0;
+  e[b] = v;
+  sum[b] = v + add[b];
 }
 
 __device__ __forceinline__ void put_hilo(__half* base, long long plane, float v) {
@@ -991,9 +1015,18 @@ __global__ void k_shear_tiles(int nk, int nw, int ndd, const float2* X0, const f
 
 // The stage field in FP32.
 
-__global__ void k_field_f(long long n, const double2* ek, float2* ekf) {
+__global__ void k_field_f(long long n, const double2* ek, const double2* dek, double frac,
+                          float2* ekf) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) ekf[i] = f64_to_f32(ek[i]);
+  if (i >= n) return;
+  double2 a = ek[i];
+  if (dek) {
+    // stage field Ek0 + frac dEk in FP64 (as the FP64 path's stage field)
+    const double2 d = dek[i];
+    a.x += frac * d.x;
+    a.y += frac * d.y;
+  }
+  ekf[i] = f64_to_f32(a);
 }
 
 // H = Meh + diagonal energies + direct Coulomb terms + exchange sums
@@ -1512,13 +1545,14 @@ static void mixed_state_in(SbeCtx* c, const double2* P, const double2* C, const 
 }
 
 // One RHS evaluation of the mixed path on the FP32 stage state (P, C, D; the
-// FP64 diagonals of C and D in dgC, dgD; the state maxima already in mxS, mxO).
-// With stage 1-4 the RK4 update of that stage is fused into the element-wise
+// FP64 diagonals of C and D in dgC, dgD; the state maxima already in mxS, mxO)
+// with the wire-k field Ek + frac dEk (dEk may be null).  With stage 1-4 the RK4 update of that stage is fused into the element-wise
 // passes (X64: the FP64 states P, C, D; the next stage state goes to the FP32
 // stage buffer and its maxima to mxS, mxO); stage 0 stores the RHS in kf.
 static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2* D,
-                       const double* dgC, const double* dgD, const double2* Ek, int stage,
-                       float dt, double2* const* X64, cudaStream_t s) {
+                       const double* dgC, const double* dgD, const double2* Ek,
+                       const double2* dEk, double frac, int stage, float dt,
+                       double2* const* X64, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   const long long mm = (long long)nk * nk, tm = c->tot_mat;
@@ -1528,14 +1562,8 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
   // eS: full state maximum (sheared exchange operands); eO: maximum over P and
   // the off-diagonal C, D (commutator operands; the diagonals of C and D are
   // peeled off and applied exactly in the epilogues)
-  exponents_from(m, m->mxS(), m->eS(), s);
-  exponents_from(m, m->mxO(), m->eO(), s);
-  if (stage > 0) {
-    // consumed by the exponents above: the fused RK4 update collects the next
-    // stage state's maxima in them
-    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
-  }
+  k_stage_exponents<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxS(), m->mxO(), m->mxH(), m->eS(),
+                                                     m->eO(), m->eT(), m->esx(), stage > 0);
   const float2* st[3] = {P, C, D};
   const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
   const long long vn = (long long)nw * nk;
@@ -1546,11 +1574,11 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
                                         m->cdf + 2 * vn, dgD);
   // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
   // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
-  k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, m->ekf);
+  k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, dEk, frac,
+                                                               m->ekf);
   int rc = SBE_OK;
   const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
   if (have_x) {
-    k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eT(), m->eS(), m->esx());
     // the traces of C and D (direct terms) come from the shear's diagonal partials
     const int nb = (nk + 31) / 32, ndd = 32 * ((2 * nk + 31) / 32);
     int ny = 0;   // dd blocks of the band per t' block
@@ -1582,17 +1610,16 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
     rc = tc_gemm_launch(jobs, 3, s);
     if (rc) return rc;
   }
-  cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
   k_h_build<<<dim3((nk + 511) / 512, (nk + HB_ROWS - 1) / HB_ROWS, nw), 128, 0, s>>>(
       c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, reinterpret_cast<const float2*>(m->xsh),
       have_x, m->hf, tm, m->dgE, m->dgH,
       m->dgf, m->mxH());
   // H exponent: max over the operands and the step's 2 hbar |A|, |B|
-  k_exponents2<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH());
+  k_exponents2_sum<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH(), m->eO(),
+                                                    m->esc());
   k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->pl, M_EH, M_EHT, nw);
   k_hplanes<<<dim3((nk + 31) / 32, (nk + 31) / 32, nw), dim3(32, 8), 0, s>>>(
       m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->pl, nw);
-  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eO(), m->eH(), m->esc());
   // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
   // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
   const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_D, M_EH, 1, 0, -1},
@@ -1730,7 +1757,8 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
   const long long n = c->tot_mat, vn = (long long)m->nw * m->nk;
   mixed_state_in(c, P, C, D, s);
   const float2* xf = reinterpret_cast<const float2*>(c->xs);
-  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, 0, 0.f, nullptr, s);
+  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, nullptr, 0.0, 0, 0.f,
+                   nullptr, s);
   if (rc) return rc;
   const int g = (int)((n + 255) / 256);
   k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf, dP);
@@ -1755,11 +1783,11 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   mixed_state_in(c, P, C, D, s);
   double2* X64[3] = {P, C, D};
   for (int st = 1; st <= 4; ++st) {
-    launch_stage_field(c, Ek0, dEk, frac[st - 1], s);
-    // the RHS of this stage and its RK4 update (fused into the element-wise passes)
+    // the RHS of this stage (stage field Ek0 + frac dEk) and its RK4 update (fused
+    // into the element-wise passes)
     float2* xs = st == 1 ? x0 : x0 + 3 * n;
-    rc = mixed_stage(c, xs, xs + n, xs + 2 * n, m->xdg, m->xdg + vn, c->ekst, st, (float)dt, X64,
-                     s);
+    rc = mixed_stage(c, xs, xs + n, xs + 2 * n, m->xdg, m->xdg + vn, Ek0, dEk, frac[st - 1], st,
+                     (float)dt, X64, s);
     if (rc) return rc;
   }
   mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
