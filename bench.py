@@ -67,7 +67,7 @@ METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel 
 # dram__bytes_read.sum + dram__bytes_write.sum of the commutator launches of one RHS
 # evaluation (dP with the hi*lo + lo*hi products of W and V: 200.05 + 22.92 MB; the
 # hi*hi products of W and V: 67.20 + 14.03 MB), 8 wires x Nk = 512 (ncu), per wire
-TRAFFIC_PER_EVAL_WIRE = (200.05e6 + 22.92e6 + 67.20e6 + 14.03e6) / 8
+TRAFFIC_PER_EVAL_WIRE = (201.83e6 + 22.94e6 + 67.18e6 + 17.63e6) / 8
 
 
 def wire_L(nk, kmax):
