@@ -607,23 +607,28 @@ __global__ void k_toeplitz_planes(const WireDev* wires, const double* vs, const 
   const int nk = W.nk;
   const int t0 = blockIdx.y * 32, c0 = blockIdx.x * 32, tx = threadIdx.x;
   if (t0 >= nk || c0 >= nk) return;
+  __shared__ __half th[2][64];   // hi, lo of the tile's 63 diagonals t - t' - (t0 - c0) + 31
   const int eb = e[b];
   const double* v = vs + 3 * W.off_vec + n * nk;
   const int tp = c0 + tx;
+  const int tid = threadIdx.y * 32 + tx;
+  if (tid < 63) {
+    const int dd = tid - 31 + t0 - c0, d = dd < 0 ? -dd : dd;
+    const float f = (d == 0 || d >= nk) ? 0.f : f64_to_f32(v[d], eb);
+    const __half hi = __float2half_rn(f);
+    th[0][tid] = hi;
+    th[1][tid] = __float2half_rn(f - __half2float(hi));
+  }
+  if (t0 == 0 && threadIdx.y == 0 && tp < nk)
+    vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(v[tp]);
+  __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int i = threadIdx.y + 8 * k;
-    const int t = t0 + i;
-    float f = 0.f;
-    if (t < nk && tp < nk) {
-      const int d = t > tp ? t - tp : tp - t;
-      const double vd = v[d];
-      if (t == 0) vsf[((long long)b * 3 + n) * nk + tp] = f64_to_f32(vd);
-      f = (d == 0) ? 0.f : f64_to_f32(vd, eb);
-    }
-    const __half hi = __float2half_rn(f);
-    hs[0][i][tx] = hi;
-    hs[1][i][tx] = __float2half_rn(f - __half2float(hi));
+    const bool in = t0 + i < nk && tp < nk;
+    const int j = i - tx + 31;
+    hs[0][i][tx] = in ? th[0][j] : __float2half_rn(0.f);
+    hs[1][i][tx] = in ? th[1][j] : __float2half_rn(0.f);
   }
   __syncthreads();
   store_tiles(hs, 2, dst, n, b, t0, c0 >> 5, threadIdx.y * 32 + tx, 32 * blockDim.y);
@@ -871,18 +876,31 @@ __global__ void k_src_reduce_f(const WireDev* wires, const float2* ekrf, const f
     const float2* Gp = G + W.off_kr;
     const float2* Gc = G + tot_kr + W.off_kr;
     const float2* Gd = G + 2 * tot_kr + W.off_kr;
-#pragma unroll 4
-    for (int k = ty; k < nk; k += 8) {
-      const long long o = (long long)k * nr + r;
-      const float2 e = E[o];             // conj taken below
-      const float2 gp = Gp[o], gc = Gc[o], gd = Gd[o];
-      const float re_part = e.x * gp.x + e.y * gp.y;
-      sx += (k & 1) ? -re_part : re_part;
-      sy += re_part;
-      ser += e.x * gc.x + e.y * gc.y;
-      sei += e.x * gc.y - e.y * gc.x;
-      shr += e.x * gd.x + e.y * gd.y;
-      shi += e.x * gd.y - e.y * gd.x;
+    // rows k = ty + 8 i in batches of four, all loads of a batch issued before
+    // the sums (same order of the sums as one row at a time)
+    for (int k0 = ty; k0 < nk; k0 += 32) {
+      float2 e[4], gp[4], gc[4], gd[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 8 * u;
+        const long long o = (long long)(k < nk ? k : 0) * nr + r;
+        e[u] = E[o];             // conj taken below
+        gp[u] = Gp[o];
+        gc[u] = Gc[o];
+        gd[u] = Gd[o];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 8 * u;
+        if (k >= nk) break;
+        const float re_part = e[u].x * gp[u].x + e[u].y * gp[u].y;
+        sx += (k & 1) ? -re_part : re_part;
+        sy += re_part;
+        ser += e[u].x * gc[u].x + e[u].y * gc[u].y;
+        sei += e[u].x * gc[u].y - e[u].y * gc[u].x;
+        shr += e[u].x * gd[u].x + e[u].y * gd[u].y;
+        shi += e[u].x * gd[u].y - e[u].y * gd[u].x;
+      }
     }
   }
   part[0][ty][tx] = sx;
