@@ -32,6 +32,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -287,8 +288,10 @@ def gpu_arm(args, wl):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local, os.path.join(ROOT, "gpurun_out", f"clocks_{rank}.csv")) \
-        if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ClockSampler(local, "/tmp/clk.csv")
+    # the raw nvidia-smi samples go to SBE_CLOCKS_DIR (default: the temp dir); the
+    # JSON line carries their summary
+    clk_dir = os.environ.get("SBE_CLOCKS_DIR", tempfile.gettempdir())
+    clocks = ClockSampler(local, os.path.join(clk_dir, f"clocks_{rank}.csv"))
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()

@@ -1,7 +1,7 @@
 """CPU FP64 restatement of the PulseSuite quantum-wire SBE path (the oracle).
 
 TEST INFRASTRUCTURE ONLY.  This module is imported by ``tests/``, by
-``__graft_entry__.smoke()`` (as the checker) and by ``bench.py``'s CPU baseline
+``__graft_entry__.smoke()`` (to check the CUDA path) and by ``bench.py``'s CPU baseline
 and reference arm; nothing in ``pulsesuite_gb300`` imports or calls it.
 
 Every function restates, in vectorised NumPy, the arithmetic of one function of
