@@ -858,14 +858,161 @@ def qw2prop(r, Px, Py, Pz, re, rh, RR, plasmonics):
 # ----------------------------------------------------------------------------
 
 
-def relax(ne, nh, VC, E1D, pt, dt, ehs, phonon, small=SMALL):
-    """SBEs.py:5228-5325 _relaxation (EHs terms not included: flag must be off)."""
-    if ehs:
-        raise NotImplementedError("carrier-carrier scattering (EHs) is not in the oracle")
-    if not phonon:
+def mb_value(kind, a, b, d, Ee, Eh, ge, gh, lorentz):
+    """coulomb.py:367-499 CalcMBArrays: the builder's value for 0-based (a, b, d).
+
+    kind "eh": k30 = d + b - a, E = Ee[a] + Eh[b] - Eh[k30] - Ee[d], broadening
+    geh = (ge + gh) / 2; "ee" / "hh": k30 = a + b - d with Ee (ge) / Eh (gh).
+    UnDel[a+1, d+1] UnDel[b+1, k30+1] is (a != d) in both cases.  Zero where k30
+    leaves [0, N).  Lorentzian 2 g / (E^2 + (hbar g)^2) or (2 pi / hbar) GaussDelta(E,
+    hbar g) (coulomb.py:245-262).  a, b, d are integer arrays of one shape.
+    """
+    n = len(Ee)
+    if kind == "eh":
+        k30 = d + b - a
+        g = (ge + gh) / 2.0
+    else:
+        k30 = a + b - d
+        g = ge if kind == "ee" else gh
+    ok = (k30 >= 0) & (k30 < n) & (a >= 0) & (b >= 0) & (d >= 0) & (a < n) & (b < n) & (d < n)
+    aa, bb, dd, cc = [np.where(ok, x, 0) for x in (a, b, d, k30)]
+    if kind == "eh":
+        E = Ee[aa] + Eh[bb] - Eh[cc] - Ee[dd]
+    elif kind == "ee":
+        E = Ee[aa] + Ee[bb] - Ee[cc] - Ee[dd]
+    else:
+        E = Eh[aa] + Eh[bb] - Eh[cc] - Eh[dd]
+    und = (aa != dd).astype(float)
+    if lorentz:
+        v = 2.0 * g * und * und / (E ** 2 + (HBAR * g) ** 2)
+    else:
+        hb = HBAR * g
+        v = 2.0 * np.pi / HBAR * und * und * (1.0 / (np.sqrt(np.pi) * hb) * np.exp(-((E / hb) ** 2)))
+    return np.where(ok, v, 0.0)
+
+
+def _mb_store(kind, x, y, z, mb):
+    """Table entry C[x, y, z] of the (N+1)^3 array as the scattering loops read it.
+
+    Quirk kept (coulomb.py:957-1071): the loops index the 1-based table with
+    k - 1, so storage index x holds the builder's 0-based x - 1 (0 for x = 0).
+    """
+    return mb_value(kind, x - 1, y - 1, z - 1, mb["Ee"], mb["Eh"], mb["ge"], mb["gh"],
+                    mb["lorentz"]) * ((x >= 1) & (y >= 1) & (z >= 1))
+
+
+def _vsq_full(VC, c):
+    return VC[:, :, c] ** 2
+
+
+def mbce(ne0, nh0, VC, mb):
+    """coulomb.py:957-1011 _MBCE_core (via CoulombModule.MBCE, :1298-1311):
+    returns (Win_add, Wout_add) of the electrons, Nk each."""
+    n = len(ne0)
+    ne = np.zeros(n + 1)
+    nh = np.zeros(n + 1)
+    ne[1:] = np.abs(np.real(ne0))
+    nh[1:] = np.abs(np.real(nh0))
+    Veh2 = _vsq_full(VC, 0)
+    Vee2 = _vsq_full(VC, 1)
+    q1, q2 = np.meshgrid(np.arange(1, n + 1), np.arange(1, n + 1), indexing="ij")
+    win = np.zeros(n)
+    wout = np.zeros(n)
+    for k in range(1, n + 1):
+        kp, k1 = q1, q2
+        k1p = kp + k1 - k
+        ok = (k1p >= 1) & (k1p <= n)
+        k1pc = np.where(ok, k1p, 0)
+        t1 = (Veh2[k - 1, k1 - 1] * (1.0 - nh[kp]) * nh[k1pc] * ne[k1]
+              * _mb_store("eh", k - 1, kp - 1, k1 - 1, mb))
+        s = np.sum(np.where(ok, t1, 0.0))
+        k1p = kp + k - k1
+        ok = (k1p >= 1) & (k1p <= n)
+        k1pc = np.where(ok, k1p, 0)
+        t2 = (Veh2[k1 - 1, k - 1] * (1.0 - ne[k1]) * (1.0 - nh[kp]) * nh[k1pc]
+              * _mb_store("eh", k1 - 1, kp - 1, k - 1, mb))
+        so = np.sum(np.where(ok, t2, 0.0))
+        k2, k4 = q1, q2
+        k30 = k + k2 - k4
+        ok = (k30 >= 1) & (k30 <= n)
+        k30c = np.where(ok, k30, 0)
+        t3 = (Vee2[k - 1, k4 - 1] * (1.0 - ne[k2]) * ne[k30c] * ne[k4]
+              * _mb_store("ee", k - 1, k2 - 1, k4 - 1, mb))
+        s += np.sum(np.where(ok, t3, 0.0))
+        k30 = k4 + k2 - k
+        ok = (k30 >= 1) & (k30 <= n)
+        k30c = np.where(ok, k30, 0)
+        t4 = (Vee2[k4 - 1, k - 1] * (1.0 - ne[k4]) * (1.0 - ne[k2]) * ne[k30c]
+              * _mb_store("ee", k4 - 1, k2 - 1, k - 1, mb))
+        so += np.sum(np.where(ok, t4, 0.0))
+        win[k - 1] = s
+        wout[k - 1] = so
+    return win, wout
+
+
+def mbch(ne0, nh0, VC, mb):
+    """coulomb.py:1014-1071 _MBCH_core (via CoulombModule.MBCH, :1313-1326):
+    returns (Win_add, Wout_add) of the holes, Nk each."""
+    n = len(ne0)
+    ne = np.zeros(n + 1)
+    nh = np.zeros(n + 1)
+    ne[1:] = np.abs(np.real(ne0))
+    nh[1:] = np.abs(np.real(nh0))
+    Veh2 = _vsq_full(VC, 0)
+    Vhh2 = _vsq_full(VC, 2)
+    q1, q2 = np.meshgrid(np.arange(1, n + 1), np.arange(1, n + 1), indexing="ij")
+    win = np.zeros(n)
+    wout = np.zeros(n)
+    for kp in range(1, n + 1):
+        k, k1 = q1, q2
+        k1p = kp + k1 - k
+        ok = (k1p >= 1) & (k1p <= n)
+        k1pc = np.where(ok, k1p, 0)
+        t1 = (Veh2[k - 1, k1 - 1] * (1.0 - ne[k]) * nh[k1pc] * ne[k1]
+              * _mb_store("eh", k - 1, kp - 1, k1 - 1, mb))
+        s = np.sum(np.where(ok, t1, 0.0))
+        k1p = kp + k - k1
+        ok = (k1p >= 1) & (k1p <= n)
+        k1pc = np.where(ok, k1p, 0)
+        t2 = (Veh2[k1 - 1, k - 1] * (1.0 - ne[k]) * (1.0 - nh[k1pc]) * ne[k1]
+              * _mb_store("eh", k - 1, k1pc - 1, k1 - 1, mb))
+        so = np.sum(np.where(ok, t2, 0.0))
+        k2p, k4p = q1, q2
+        k3p = kp + k2p - k4p
+        ok = (k3p >= 1) & (k3p <= n)
+        k3pc = np.where(ok, k3p, 0)
+        t3 = (Vhh2[kp - 1, k4p - 1] * (1.0 - nh[k2p]) * nh[k3pc] * nh[k4p]
+              * _mb_store("hh", kp - 1, k2p - 1, k4p - 1, mb))
+        s += np.sum(np.where(ok, t3, 0.0))
+        k3p = k4p + k2p - kp
+        ok = (k3p >= 1) & (k3p <= n)
+        k3pc = np.where(ok, k3p, 0)
+        t4 = (Vhh2[k4p - 1, kp - 1] * (1.0 - nh[k4p]) * (1.0 - nh[k2p]) * nh[k3pc]
+              * _mb_store("hh", k4p - 1, k2p - 1, kp - 1, mb))
+        so += np.sum(np.where(ok, t4, 0.0))
+        win[kp - 1] = s
+        wout[kp - 1] = so
+    return win, wout
+
+
+def relax(ne, nh, VC, E1D, pt, dt, ehs, phonon, small=SMALL, mb=None):
+    """SBEs.py:5228-5325 _relaxation with RelaxationE/H (SBEs.py:1709-1835): the
+    carrier-carrier rates (EHs; ``mb`` = dict(Ee, Eh, ge, gh, lorentz)) first, then
+    the phonon rates added."""
+    if not (phonon or ehs):
         return ne, nh
-    we_in, we_out = mbpe(np.real(ne), VC, E1D, pt)
-    wh_in, wh_out = mbph(np.real(nh), VC, E1D, pt)
+    n = len(ne)
+    we_in, we_out, wh_in, wh_out = (np.zeros(n) for _ in range(4))
+    if ehs:
+        a, b = mbce(np.real(ne), np.real(nh), VC, mb)
+        we_in, we_out = we_in + a, we_out + b
+        a, b = mbch(np.real(ne), np.real(nh), VC, mb)
+        wh_in, wh_out = wh_in + a, wh_out + b
+    if phonon:
+        a, b = mbpe(np.real(ne), VC, E1D, pt)
+        we_in, we_out = we_in + a, we_out + b
+        a, b = mbph(np.real(nh), VC, E1D, pt)
+        wh_in, wh_out = wh_in + a, wh_out + b
     We = we_in + we_out
     Wh = wh_in + wh_out
     ne = np.exp(-We * dt) * ((-1 + np.exp(We * dt) + ne) * we_in + ne * we_out) / (We + small)
@@ -889,6 +1036,9 @@ class Wire:
         self.temp = temp
         self.ct = coulomb_tables(self.g, self.c, p["epsr"], p["Delta0"], p["me"], p["mh"])
         self.pt = phonon_tables(self.c["Ee"], self.c["Eh"], p["epsr"], p["Gph"], p["Oph"], temp)
+        # carrier-carrier scattering tables are evaluated on the fly (mb_value)
+        self.mb = dict(Ee=self.c["Ee"], Eh=self.c["Eh"], ge=p["gam_e"], gh=p["gam_h"],
+                       lorentz=bool(self.flags.get("LorentzDelta", False)))
         self.dt = dephasing_tables(self.g["kr"], p["me"], p["mh"])
         self.window = qw_window(self.g["r"], L)
         self.E = expikr(self.g["kr"], self.g["r"])
@@ -976,7 +1126,7 @@ class Wire:
                    for x, a, b, cc, d in zip(X, k1, k2, k3, k4)]
         if f["EHs"] or f["Phonon"]:
             ne3, nh3 = relax(np.diag(C).copy(), np.diag(D).copy(), VC, E1D, self.pt, dt,
-                             f["EHs"], f["Phonon"])
+                             f["EHs"], f["Phonon"], mb=self.mb)
             C[np.diag_indices(nk)] = ne3
             D[np.diag_indices(nk)] = nh3
         ne3 = np.abs(np.diag(C)).astype(complex)
@@ -1037,7 +1187,7 @@ class Solver:
         p3 = p1 + dP * dt * 2.0
         if f["EHs"] or f["Phonon"]:
             ne3, nh3 = relax(np.diag(C3).copy(), np.diag(D3).copy(), pr["VC"], pr["E1D"],
-                             wi.pt, dt, f["EHs"], f["Phonon"])
+                             wi.pt, dt, f["EHs"], f["Phonon"], mb=wi.mb)
             C3[np.diag_indices(g["nk"])] = ne3
             D3[np.diag_indices(g["nk"])] = nh3
         ne3 = np.abs(np.diag(C3)).astype(complex)

@@ -19,6 +19,9 @@ kernels_nkN     CalcH (``SBEs._CalcH_fallback``) for every flag combination and
 coulomb_nkN     ``coulomb.CoulombModule`` tables (V0, Chi1D, qe, qh) and
                 ``CalcScreenedArrays`` with and without screening; K0 samples.
 phonon_nkN      ``phonons.InitializePhonons`` tables and ``MBPE``/``MBPH``.
+mbc_nkN         ``coulomb.CoulombModule`` carrier-carrier scattering ``MBCE``/``MBCH``
+                (and the ``CalcMBArrays`` tables) with Gaussian and Lorentzian
+                broadening.  ``make_golden.py <src> mbc`` writes these alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
                 ``OffDiagDephasing2``.
 qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
@@ -235,6 +238,34 @@ def case_phonon(nk, temp, seed, VC, E1D):
     return out
 
 
+def case_mbc(nk, seed, VC):
+    """coulomb.CoulombModule(...).MBCE / MBCH with both broadenings."""
+    from pulsesuite.PSTD3D import coulomb
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    ne = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    nh = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    out = dict(kr=g["kr"], Ee=d["Ee"], Eh=d["Eh"], ge=MAT["gam_e"] * 1.3, gh=MAT["gam_h"] * 0.8,
+               VC=VC, ne=ne, nh=nh)
+    for lz in (0, 1):
+        cm = coulomb.CoulombModule(g["r"], g["kr"], g["L"], MAT["Delta0"], d["me"], d["mh"],
+                                   d["Ee"], d["Eh"], out["ge"], out["gh"], d["alphae"],
+                                   d["alphah"], MAT["epsr"], g["Qr"], g["kkp"], True,
+                                   LorentzDelta=bool(lz))
+        w = [rng.uniform(0, 1e11, nk) for _ in range(4)]
+        out.update({f"WinE0_l{lz}": w[0].copy(), f"WoutE0_l{lz}": w[1].copy(),
+                    f"WinH0_l{lz}": w[2].copy(), f"WoutH0_l{lz}": w[3].copy()})
+        cm.MBCE(np.real(ne), np.real(nh), g["kr"], d["Ee"], d["Eh"], VC, MAT["gam_eh"],
+                out["ge"], w[0], w[1])
+        cm.MBCH(np.real(ne), np.real(nh), g["kr"], d["Ee"], d["Eh"], VC, MAT["gam_eh"],
+                out["gh"], w[2], w[3])
+        out.update({f"WinE_l{lz}": w[0], f"WoutE_l{lz}": w[1], f"WinH_l{lz}": w[2],
+                    f"WoutH_l{lz}": w[3], f"Ceh_l{lz}": cm.Ceh, f"Cee_l{lz}": cm.Cee,
+                    f"Chh_l{lz}": cm.Chh})
+    return out
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -441,6 +472,7 @@ def main():
     ref_src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PULSESUITE_SRC")
     if not ref_src or not os.path.isdir(ref_src):
         raise SystemExit("usage: make_golden.py /path/to/pulsesuite/src")
+    only = sys.argv[2] if len(sys.argv) > 2 else None   # e.g. "mbc": that case alone
     with tempfile.TemporaryDirectory() as tmp:
         _install_stubs(tmp)
         sys.path.insert(0, tmp)
@@ -452,6 +484,13 @@ def main():
         sink = io.StringIO()
         try:
             with contextlib.redirect_stdout(sink):
+                for nk, seed in ((8, 20), (13, 21)):
+                    if only in (None, "mbc"):
+                        co = case_coulomb(nk, seed)
+                        mb = case_mbc(nk, seed + 400, co["VC1_s1"])
+                        np.savez_compressed(os.path.join(HERE, f"mbc_nk{nk}.npz"), **mb)
+                if only == "mbc":
+                    return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))
                 for nk, seed in ((8, 20), (16, 21), (30, 22)):

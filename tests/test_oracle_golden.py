@@ -85,6 +85,24 @@ def test_phonons(nk):
     assert rel(g["WoutH0"] + ho, g["WoutH"]) < TOL
 
 
+@pytest.mark.parametrize("nk", [8, 13])
+@pytest.mark.parametrize("lorentz", [0, 1])
+def test_carrier_scattering(nk, lorentz):
+    """MBCE / MBCH (carrier-carrier scattering, EHs) and the CalcMBArrays tables."""
+    g = golden(f"mbc_nk{nk}")
+    mb = dict(Ee=g["Ee"], Eh=g["Eh"], ge=float(g["ge"]), gh=float(g["gh"]), lorentz=bool(lorentz))
+    a, b, d = np.meshgrid(np.arange(nk), np.arange(nk), np.arange(nk), indexing="ij")
+    for kind, key in (("eh", "Ceh"), ("ee", "Cee"), ("hh", "Chh")):
+        ref = g[f"{key}_l{lorentz}"]
+        assert not ref[0].any() and not ref[:, 0].any() and not ref[:, :, 0].any()
+        assert rel(O.mb_value(kind, a, b, d, g["Ee"], g["Eh"], mb["ge"], mb["gh"], mb["lorentz"]),
+                   ref[1:, 1:, 1:]) < TOL, key
+    wi, wo = O.mbce(g["ne"], g["nh"], g["VC"], mb)
+    hi, ho = O.mbch(g["ne"], g["nh"], g["VC"], mb)
+    for name, mine in (("WinE", wi), ("WoutE", wo), ("WinH", hi), ("WoutH", ho)):
+        assert rel(g[f"{name}0_l{lorentz}"] + mine, g[f"{name}_l{lorentz}"]) < TOL, name
+
+
 @pytest.mark.parametrize("nk", [8, 16, 30])
 def test_dephasing(nk):
     g = golden(f"dephasing_nk{nk}")
