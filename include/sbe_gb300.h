@@ -42,6 +42,7 @@ extern "C" {
 #define SBE_F_DIAGDPH    (1 << 8)
 #define SBE_F_OFFDIAGDPH (1 << 9)
 #define SBE_F_RECOMB     (1 << 10)
+#define SBE_F_LORENTZ    (1 << 11)  /* LorentzDelta of mb.params: Lorentzian broadening of the EHs rates */
 
 /* Precision of the RHS contractions. */
 #define SBE_PREC_FP64  0  /* plain FP64 SIMT (drop-in path and on-device reference) */
@@ -119,6 +120,12 @@ int sbe_offdiag(SbeCtx* ctx, int w, const double* ne, const double* nh, const do
 int sbe_phonon_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
                      const double* E1D, double* WinE, double* WoutE, double* WinH,
                      double* WoutH, void* stream);
+/* coulomb.py:1298/1313 MBCE/MBCH (carrier-carrier scattering, EHs; tables of
+ * CalcMBArrays, coulomb.py:367, evaluated on the fly, Lorentzian broadening with
+ * SBE_F_LORENTZ in the wire's flags, else Gaussian): Win/Wout accumulated in place.
+ * ne, nh c128 Nk (|Re| used); VC (Nk*Nk*3).                                   */
+int sbe_carrier_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
+                      double* WinE, double* WoutE, double* WinH, double* WoutH, void* stream);
 /* qwoptics.py:809 QWPolarization3 and 942 QWRho5 (with x 2 e0 ehint/area), real
  * space (before FFTG): Px, Py, Pz, re, rh (c128 Nr).  ne/nh c128 Nk.         */
 int sbe_sources(SbeCtx* ctx, int w, const double* P, const double* C, const double* D,

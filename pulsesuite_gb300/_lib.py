@@ -13,10 +13,11 @@ LIB_PATH = os.path.join(HERE, "libsbe_gb300.so")
 
 # flag bits (mb.params order)
 F_OPTICS, F_EXCITONS, F_EHS, F_SCREENED, F_PHONON, F_DCTRANS, F_LF, F_FREEPOT, F_DIAGDPH, \
-    F_OFFDIAGDPH, F_RECOMB = (1 << i for i in range(11))
+    F_OFFDIAGDPH, F_RECOMB, F_LORENTZ = (1 << i for i in range(12))
 FLAG_BITS = dict(Optics=F_OPTICS, Excitons=F_EXCITONS, EHs=F_EHS, Screened=F_SCREENED,
                  Phonon=F_PHONON, DCTrans=F_DCTRANS, LF=F_LF, FreePot=F_FREEPOT,
-                 DiagDph=F_DIAGDPH, OffDiagDph=F_OFFDIAGDPH, Recomb=F_RECOMB)
+                 DiagDph=F_DIAGDPH, OffDiagDph=F_OFFDIAGDPH, Recomb=F_RECOMB,
+                 LorentzDelta=F_LORENTZ)
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -25,7 +26,8 @@ PREC_MIXED = 1
 EXPORTS = (
     "sbe_last_error", "sbe_version", "sbe_constants", "sbe_ctx_create", "sbe_ctx_destroy",
     "sbe_ctx_layout", "sbe_ctx_table", "sbe_dpdt", "sbe_dCdt", "sbe_dDdt", "sbe_calch",
-    "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_sources",
+    "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_carrier_rates",
+    "sbe_sources",
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
     "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
     "sbe_ctx_profile", "sbe_ctx_profile_read", "sbe_prop2qw_noalloc", "sbe_ctx_check",
@@ -94,6 +96,7 @@ def load(path=LIB_PATH):
         "sbe_gamma": [P, I, P, P, P, P, P, P],
         "sbe_offdiag": [P, I, P, P, P, P, P, P, P, P, P],
         "sbe_phonon_rates": [P, I, P, P, P, P, P, P, P, P, P],
+        "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, P],
         "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
         "sbe_prop2qw": [P, I, P, I, P, P, P],
         "sbe_prop2qw_noalloc": [P, I, P, I, P, P, P],

@@ -87,7 +87,7 @@ int sbe_constants(double* out5) {
   return SBE_OK;
 }
 
-static const int kUnsupportedFlags = SBE_F_EHS | SBE_F_DCTRANS | SBE_F_RECOMB | SBE_F_FREEPOT;
+static const int kUnsupportedFlags = SBE_F_DCTRANS | SBE_F_RECOMB | SBE_F_FREEPOT;
 
 int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out) {
   if (!wires || n_wires <= 0 || !out) return fail(SBE_ERR_ARG, "sbe_ctx_create: bad arguments");
@@ -109,7 +109,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
     if (d.flags & kUnsupportedFlags) {
       delete c;
       return fail(SBE_ERR_UNSUPPORTED,
-                  "sbe_ctx_create: EHs, DCTrans, Recomb and FreePot are not built (wire " +
+                  "sbe_ctx_create: DCTrans, Recomb and FreePot are not built (wire " +
                       std::to_string(w) + ")");
     }
     WireDev W = derive(d);
@@ -492,6 +492,24 @@ int sbe_phonon_rates(SbeCtx* c, int w, const double* ne, const double* nh, const
   // accumulate into the caller's arrays (MBPE/MBPH add to Win/Wout)
   sbe::add_rates(c->wrate + 4 * W.off_vec, W.nk, WinE, WoutE, WinH, WoutH, s);
   return cuda_check(cudaGetLastError(), "sbe_phonon_rates");
+}
+
+int sbe_carrier_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
+                      double* WinE, double* WoutE, double* WinH, double* WoutH, void* stream) {
+  int rc = check_w(c, w, "sbe_carrier_rates");
+  if (rc) return rc;
+  if (!ne || !nh || !VC || !WinE || !WoutE || !WinH || !WoutH)
+    return fail(SBE_ERR_ARG, "sbe_carrier_rates: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const WireDev& W = c->wires[w];
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  set_vc(c, w, VC, nullptr, s);
+  cudaMemsetAsync(c->wrate + 4 * W.off_vec, 0, sizeof(double) * 4 * W.nk, s);
+  launch_mbc_rates(c, w, s, true);
+  // accumulate into the caller's arrays (MBCE/MBCH add to Win/Wout)
+  sbe::add_rates(c->wrate + 4 * W.off_vec, W.nk, WinE, WoutE, WinH, WoutH, s);
+  return cuda_check(cudaGetLastError(), "sbe_carrier_rates");
 }
 
 int sbe_sources(SbeCtx* c, int w, const double* P, const double* C, const double* D,

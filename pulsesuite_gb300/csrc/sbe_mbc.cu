@@ -1,0 +1,187 @@
+// Carrier-carrier scattering rates (flag EHs): MBCE / MBCH of coulomb.py:957-1071
+// (called by RelaxationE / RelaxationH, SBEs.py:1709-1835) with the values of the
+// CalcMBArrays tables (coulomb.py:367-499) evaluated where they are used instead
+// of stored as three (Nk+1)^3 arrays.
+#include "sbe_ctx.cuh"
+#include "sbe_internal.cuh"
+#include "fp_bits.cuh"
+
+namespace sbe {
+
+namespace {
+
+// CalcMBArrays for 0-based (a, b, d) of the builder (kind 0: Ceh, 1: Cee, 2: Chh):
+// k30 = d + b - a (eh) or a + b - d (ee, hh); UnDel[a+1][d+1] UnDel[b+1][k30+1]
+// is (a != d); zero where k30 leaves [0, Nk).  Lorentzian 2 g / (E^2 + (hbar g)^2)
+// or (2 pi / hbar) GaussDelta(E, hbar g) (coulomb.py:245-262), g = (ge + gh) / 2 for
+// eh.  Operations in the reference's order.
+__device__ __forceinline__ double mb_value64(int kind, int a, int b, int d, int n,
+                                             const double* Ee, const double* Eh, double ge,
+                                             double gh, bool lorentz) {
+  if (a < 0 || b < 0 || d < 0 || a == d) return 0.0;
+  const int c = kind == 0 ? d + b - a : a + b - d;
+  if (c < 0 || c >= n) return 0.0;
+  double E, g;
+  if (kind == 0) {
+    E = ((Ee[a] + Eh[b]) - Eh[c]) - Ee[d];
+    g = (ge + gh) / 2.0;
+  } else if (kind == 1) {
+    E = ((Ee[a] + Ee[b]) - Ee[c]) - Ee[d];
+    g = ge;
+  } else {
+    E = ((Eh[a] + Eh[b]) - Eh[c]) - Eh[d];
+    g = gh;
+  }
+  const double hg = kHbar * g;
+  if (lorentz) return 2.0 * g / (E * E + hg * hg);
+  const double x = E / hg;
+  return kTwoPi / kHbar * (1.0 / (sqrt(kPi) * hg) * exp(-(x * x)));
+}
+
+// Table entry C[x][y][z] as the scattering loops read it: the loops index the
+// 1-based table with k - 1, so storage index x holds the builder's x - 1 (a quirk
+// of the reference, kept) and index 0 is zero.
+__device__ __forceinline__ double mb_store64(int kind, int x, int y, int z, int n,
+                                             const double* Ee, const double* Eh, double ge,
+                                             double gh, bool lorentz) {
+  return mb_value64(kind, x - 1, y - 1, z - 1, n, Ee, Eh, ge, gh, lorentz);
+}
+
+// VC[i][j]^2 of the screened tables: the reference's V(q) arrays are lower
+// triangular on its grid (V[k1][k2] = v[k1 - k2] for k1 >= k2, else 0), and the
+// context keeps v by k1 - k2 >= 0.
+__device__ __forceinline__ double vsq_at(const double* v2, int i, int j) {
+  return i >= j ? v2[i - j] : 0.0;
+}
+
+// One block per (row, wire, species): species 0 electrons (MBCE, row k), 1 holes
+// (MBCH, row kp); the threads walk the Nk^2 pairs (q1, q2) of the row; the block
+// sums (fixed tree) are added to wrate (Win, Wout of the species).
+__global__ void __launch_bounds__(256) k_mbc_rates64(const WireDev* wires, int w_only,
+                                                     const double2* nev, const double2* nhv,
+                                                     const double* vs, const double* Ee,
+                                                     const double* Eh, double* wrate,
+                                                     int all) {
+  const WireDev W = wires[w_only >= 0 ? w_only : blockIdx.y];
+  const int n = W.nk;
+  const int row = blockIdx.x + 1;   // 1-based k (electrons) or kp (holes)
+  if (row > n || !(all || (W.flags & SBE_F_EHS))) return;
+  const bool holes = blockIdx.z == 1;
+  extern __shared__ double sh[];
+  double* ne = sh;              // [0, n]: 1-based occupations, ne[0] = 0
+  double* nh = sh + (n + 1);
+  double* v2 = sh + 2 * (n + 1);   // [3][n]: VC^2 by k1 - k2 >= 0 (eh, ee, hh)
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) {
+    ne[i] = i == 0 ? 0.0 : fabs(nev[W.off_vec + i - 1].x);
+    nh[i] = i == 0 ? 0.0 : fabs(nhv[W.off_vec + i - 1].x);
+  }
+  for (int i = threadIdx.x; i < 3 * n; i += blockDim.x) {
+    const double v = vs[3 * W.off_vec + i];
+    v2[i] = v * v;
+  }
+  __syncthreads();
+  const double* E_e = Ee + W.off_vec;
+  const double* E_h = Eh + W.off_vec;
+  const double ge = W.gam_e, gh = W.gam_h;
+  const bool lz = (W.flags & SBE_F_LORENTZ) != 0;
+  const double* veh = v2;
+  const double* vxx = v2 + (holes ? 2 : 1) * n;
+  double win = 0.0, wout = 0.0;
+  const long long npair = (long long)n * n;
+  for (long long p = threadIdx.x; p < npair; p += blockDim.x) {
+    const int q1 = (int)(p / n) + 1, q2 = (int)(p % n) + 1;
+    if (!holes) {
+      const int k = row;
+      {
+        const int kp = q1, k1 = q2;
+        const int k1p = kp + k1 - k;
+        if (k1p >= 1 && k1p <= n) {
+          const double cv = mb_store64(0, k - 1, kp - 1, k1 - 1, n, E_e, E_h, ge, gh, lz);
+          win += vsq_at(veh, k, k1) * (1.0 - nh[kp]) * nh[k1p] * ne[k1] * cv;
+        }
+        const int k1q = kp + k - k1;
+        if (k1q >= 1 && k1q <= n) {
+          const double cv = mb_store64(0, k1 - 1, kp - 1, k - 1, n, E_e, E_h, ge, gh, lz);
+          wout += vsq_at(veh, k1, k) * (1.0 - ne[k1]) * (1.0 - nh[kp]) * nh[k1q] * cv;
+        }
+      }
+      {
+        const int k2 = q1, k4 = q2;
+        const int k30 = k + k2 - k4;
+        if (k30 >= 1 && k30 <= n) {
+          const double cv = mb_store64(1, k - 1, k2 - 1, k4 - 1, n, E_e, E_h, ge, gh, lz);
+          win += vsq_at(vxx, k, k4) * (1.0 - ne[k2]) * ne[k30] * ne[k4] * cv;
+        }
+        const int k31 = k4 + k2 - k;
+        if (k31 >= 1 && k31 <= n) {
+          const double cv = mb_store64(1, k4 - 1, k2 - 1, k - 1, n, E_e, E_h, ge, gh, lz);
+          wout += vsq_at(vxx, k4, k) * (1.0 - ne[k4]) * (1.0 - ne[k2]) * ne[k31] * cv;
+        }
+      }
+    } else {
+      const int kp = row;
+      {
+        const int k = q1, k1 = q2;
+        const int k1p = kp + k1 - k;
+        if (k1p >= 1 && k1p <= n) {
+          const double cv = mb_store64(0, k - 1, kp - 1, k1 - 1, n, E_e, E_h, ge, gh, lz);
+          win += vsq_at(veh, k, k1) * (1.0 - ne[k]) * nh[k1p] * ne[k1] * cv;
+        }
+        const int k1q = kp + k - k1;
+        if (k1q >= 1 && k1q <= n) {
+          const double cv = mb_store64(0, k - 1, k1q - 1, k1 - 1, n, E_e, E_h, ge, gh, lz);
+          wout += vsq_at(veh, k1, k) * (1.0 - ne[k]) * (1.0 - nh[k1q]) * ne[k1] * cv;
+        }
+      }
+      {
+        const int k2p = q1, k4p = q2;
+        const int k3p = kp + k2p - k4p;
+        if (k3p >= 1 && k3p <= n) {
+          const double cv = mb_store64(2, kp - 1, k2p - 1, k4p - 1, n, E_e, E_h, ge, gh, lz);
+          win += vsq_at(vxx, kp, k4p) * (1.0 - nh[k2p]) * nh[k3p] * nh[k4p] * cv;
+        }
+        const int k3q = k4p + k2p - kp;
+        if (k3q >= 1 && k3q <= n) {
+          const double cv = mb_store64(2, k4p - 1, k2p - 1, kp - 1, n, E_e, E_h, ge, gh, lz);
+          wout += vsq_at(vxx, k4p, kp) * (1.0 - nh[k4p]) * (1.0 - nh[k2p]) * nh[k3q] * cv;
+        }
+      }
+    }
+  }
+  __shared__ double red[2][256];
+  red[0][threadIdx.x] = win;
+  red[1][threadIdx.x] = wout;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + o];
+      red[1][threadIdx.x] += red[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double* wr = wrate + 4 * W.off_vec + (holes ? 2 : 0) * n;
+    wr[row - 1] += red[0][0];
+    wr[n + row - 1] += red[1][0];
+  }
+}
+
+}  // namespace
+
+// Adds the carrier-carrier in/out rates of every wire with EHs on (or of wire
+// w_only; with all set, whatever its flags) to wrate, at the occupations in ne,
+// nh and the screened V in vs.
+void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all) {
+  bool any = false;
+  for (int w = 0; w < c->nw; ++w)
+    if ((w_only < 0 || w == w_only) && (all || (c->wires[w].flags & SBE_F_EHS))) any = true;
+  if (!any) return;
+  const int nk = w_only >= 0 ? c->wires[w_only].nk : c->nk_max;
+  const size_t sm = sizeof(double) * (2 * (size_t)(nk + 1) + 3 * (size_t)nk);
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_mbc_rates64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_mbc_rates64<<<dim3(nk, w_only >= 0 ? 1 : c->nw, 2), 256, sm, s>>>(
+      c->d_wires, w_only, c->ne, c->nh, c->vs, c->Ee, c->Eh, c->wrate, all ? 1 : 0);
+}
+
+}  // namespace sbe

@@ -51,6 +51,11 @@ __global__ void k_phonon_rates(const WireDev* wires, int w_only, const double2* 
   const int nk = W.nk;
   int k = blockIdx.x;
   if (k >= nk) return;
+  if (!(W.flags & SBE_F_PHONON)) {
+    // no phonon rates: the carrier-carrier rates (EHs) are added to zeros
+    if (threadIdx.x < 4) wrate[4 * W.off_vec + threadIdx.x * nk + k] = 0.0;
+    return;
+  }
   const double* v1 = vs + 3 * W.off_vec + nk;
   const double* v2 = vs + 3 * W.off_vec + 2 * nk;
   const double* ep = eps + W.off_vec;
@@ -93,7 +98,7 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
                              double dt, double2* ne_out, double2* nh_out) {
   const WireDev W = wires[blockIdx.x];
   const int nk = W.nk;
-  const bool relax = (W.flags & SBE_F_PHONON) != 0;
+  const bool relax = (W.flags & (SBE_F_PHONON | SBE_F_EHS)) != 0;
   __shared__ double red[2][256];
   double se = 0.0, sh = 0.0;
   for (int k = threadIdx.x; k < nk; k += blockDim.x) {
@@ -146,6 +151,7 @@ void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_
   launch_extract_diag(c, C3, D3, s);
   k_phonon_rates<<<dim3(c->nk_max, c->nw), 128, 0, s>>>(c->d_wires, -1, c->ne, c->nh, c->vs,
                                                         c->eps, c->EP, c->HP, c->wrate);
+  launch_mbc_rates(c, -1, s);
   k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, dt, c->ne, c->nh);
 }
 

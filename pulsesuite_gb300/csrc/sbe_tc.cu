@@ -806,6 +806,11 @@ __global__ void k_phonon_rates_f(const WireDev* wires, const double2* nev, const
   extern __shared__ float occ[];
   const WireDev W = wires[blockIdx.y];
   const int nk = W.nk, b = blockIdx.y, k = blockIdx.x;
+  if (!(W.flags & SBE_F_PHONON)) {
+    // no phonon rates: the carrier-carrier rates (EHs) are added to zeros
+    if (threadIdx.x < 4) wrate[4 * W.off_vec + threadIdx.x * nk + k] = 0.0;
+    return;
+  }
   float* pe = occ;
   float* ph = occ + nk;
   for (int i = threadIdx.x; i < nk; i += blockDim.x) {
@@ -1537,6 +1542,7 @@ static void mixed_relax(SbeCtx* c, double2* C, double2* D, double dt, cudaStream
   launch_extract_diag(c, C, D, s);
   k_phonon_rates_f<<<dim3(nk, nw), 128, sizeof(float) * 2 * nk, s>>>(
       c->d_wires, c->ne, c->nh, m->phf, m->epf, m->eptf, m->hpf, m->hptf, c->wrate, nw);
+  launch_mbc_rates(c, -1, s);
   launch_relax_only(c, C, D, dt, s);
   k_diag_max<<<nw, 256, 0, s>>>(c->d_wires, C, D, m->mxS());
 }

@@ -215,6 +215,13 @@ class WireContext:
                                              _lib.ptr(WoutE), _lib.ptr(WinH), _lib.ptr(WoutH),
                                              _lib.stream_handle()), "sbe_phonon_rates")
 
+    def carrier_rates(self, w, ne, nh, VC, WinE, WoutE, WinH, WoutH):
+        """coulomb.py:1298/1313 MBCE/MBCH: adds the carrier-carrier rates to Win/Wout."""
+        _lib.check(self.lib.sbe_carrier_rates(self.handle, w, _lib.ptr(ne), _lib.ptr(nh),
+                                              _lib.ptr(VC), _lib.ptr(WinE), _lib.ptr(WoutE),
+                                              _lib.ptr(WinH), _lib.ptr(WoutH),
+                                              _lib.stream_handle()), "sbe_carrier_rates")
+
     def sources(self, w, P, C, D, ne, nh):
         nr = 2 * self.nk[w] + 2
         out = [torch.empty(nr, dtype=CDTYPE, device=self.device) for _ in range(5)]

@@ -259,3 +259,51 @@ def test_batched_rhs_and_rk4_vs_oracle(nk):
         s5 = host(c.rvec(src, w, 5))
         for i in range(5):
             assert rel(O.fftg(s5[i]), ref[3 + i]) < SCREEN, (w, i)
+
+
+@pytest.mark.parametrize("nk", [8, 13])
+@pytest.mark.parametrize("lorentz", [0, 1])
+def test_carrier_rates_vs_golden(nk, lorentz):
+    """MBCE / MBCH through sbe_carrier_rates against the reference's own rates."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    g = golden(f"mbc_nk{nk}")
+    L = np.pi / (g["kr"][1] - g["kr"][0])
+    mat = dict(MAT, gam_e=float(g["ge"]), gam_h=float(g["gh"]))
+    flags = dict(ALL, EHs=True, LorentzDelta=bool(lorentz))
+    c = WireContext([WireSpec(nk=nk, L=L, wire_index=1, flags=flags, **mat)])
+    w = [dev(g[f"{n}0_l{lorentz}"]) for n in ("WinE", "WoutE", "WinH", "WoutH")]
+    c.carrier_rates(0, dev(g["ne"]), dev(g["nh"]), dev(g["VC"]), *w)
+    for t, n in zip(w, ("WinE", "WoutE", "WinH", "WoutH")):
+        assert rel(host(t), g[f"{n}_l{lorentz}"]) < TIGHT, n
+
+
+@pytest.mark.parametrize("lorentz", [0, 1])
+def test_rk4_with_carrier_scattering_vs_oracle(lorentz):
+    """One RK4 step with EHs on (carrier-carrier rates in the relaxation), FP64 path."""
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    nw = 2
+    flags = dict(ALL, EHs=True, LorentzDelta=bool(lorentz))
+    c = ctx_for(nk, L, nw=nw, flags=flags)
+    rng = np.random.default_rng(9)
+    wires = [O.Wire(nk, L, MAT, flags) for _ in range(nw)]
+    states = [_seeded_state(rng, nk) for _ in range(nw)]
+    fields = [_uniform_field_k(wires[w], 1e7 * (w + 1)) for w in range(nw)]
+    dfields = [_uniform_field_k(wires[w], -3e5 * (w + 1)) for w in range(nw)]
+    P = c.pack([s[0] for s in states])
+    C = c.pack([s[1] for s in states])
+    D = c.pack([s[2] for s in states])
+    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
+    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    dt = 0.1e-15
+    src = c.zeros_r(5)
+    c.rk4_step(P, C, D, Ek, dEk, dt, src)
+    for w in range(nw):
+        ref = wires[w].rk4_step(*states[w], fields[w], dfields[w], dt, w + 1)
+        # the carrier-carrier rates moved the occupations measurably
+        ref_ph = O.Wire(nk, L, MAT, dict(ALL)).rk4_step(*states[w], fields[w], dfields[w], dt,
+                                                        w + 1)
+        assert rel(np.diag(ref[1]), np.diag(ref_ph[1])) > 1e-8
+        assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
+        assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
+        assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
