@@ -123,9 +123,11 @@ int sbe_phonon_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, con
 /* coulomb.py:1298/1313 MBCE/MBCH (carrier-carrier scattering, EHs; tables of
  * CalcMBArrays, coulomb.py:367, evaluated on the fly, Lorentzian broadening with
  * SBE_F_LORENTZ in the wire's flags, else Gaussian): Win/Wout accumulated in place.
- * ne, nh c128 Nk (|Re| used); VC (Nk*Nk*3).                                   */
+ * ne, nh c128 Nk (|Re| used); VC (Nk*Nk*3).  precision SBE_PREC_FP64 (the
+ * reference's arithmetic) or SBE_PREC_MIXED (FP32, exact integer energy sums).   */
 int sbe_carrier_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
-                      double* WinE, double* WoutE, double* WinH, double* WoutH, void* stream);
+                      double* WinE, double* WoutE, double* WinH, double* WoutH, int precision,
+                      void* stream);
 /* qwoptics.py:809 QWPolarization3 and 942 QWRho5 (with x 2 e0 ehint/area), real
  * space (before FFTG): Px, Py, Pz, re, rh (c128 Nr).  ne/nh c128 Nk.         */
 int sbe_sources(SbeCtx* ctx, int w, const double* P, const double* C, const double* D,

@@ -96,7 +96,7 @@ def load(path=LIB_PATH):
         "sbe_gamma": [P, I, P, P, P, P, P, P],
         "sbe_offdiag": [P, I, P, P, P, P, P, P, P, P, P],
         "sbe_phonon_rates": [P, I, P, P, P, P, P, P, P, P, P],
-        "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, P],
+        "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, I, P],
         "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
         "sbe_prop2qw": [P, I, P, I, P, P, P],
         "sbe_prop2qw_noalloc": [P, I, P, I, P, P, P],

@@ -495,18 +495,21 @@ int sbe_phonon_rates(SbeCtx* c, int w, const double* ne, const double* nh, const
 }
 
 int sbe_carrier_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
-                      double* WinE, double* WoutE, double* WinH, double* WoutH, void* stream) {
+                      double* WinE, double* WoutE, double* WinH, double* WoutH, int precision,
+                      void* stream) {
   int rc = check_w(c, w, "sbe_carrier_rates");
   if (rc) return rc;
   if (!ne || !nh || !VC || !WinE || !WoutE || !WinH || !WoutH)
     return fail(SBE_ERR_ARG, "sbe_carrier_rates: null pointer");
+  if (precision != SBE_PREC_FP64 && precision != SBE_PREC_MIXED)
+    return fail(SBE_ERR_ARG, "sbe_carrier_rates: precision must be SBE_PREC_FP64 or SBE_PREC_MIXED");
   cudaStream_t s = as_stream(stream);
   const WireDev& W = c->wires[w];
   copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
   copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
   set_vc(c, w, VC, nullptr, s);
   cudaMemsetAsync(c->wrate + 4 * W.off_vec, 0, sizeof(double) * 4 * W.nk, s);
-  launch_mbc_rates(c, w, s, true);
+  launch_mbc_rates(c, w, s, true, precision == SBE_PREC_MIXED);
   // accumulate into the caller's arrays (MBCE/MBCH add to Win/Wout)
   sbe::add_rates(c->wrate + 4 * W.off_vec, W.nk, WinE, WoutE, WinH, WoutH, s);
   return cuda_check(cudaGetLastError(), "sbe_carrier_rates");

@@ -154,7 +154,8 @@ void launch_extract_diag(SbeCtx* c, const double2* C, const double2* D, cudaStre
 void launch_screen(SbeCtx* c, int w_only, cudaStream_t s);
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s);
 // sbe_mbc.cu: carrier-carrier scattering rates (EHs) added to wrate
-void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all = false);
+void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all = false,
+                      bool fp32 = false);
 void launch_leap_shuffle(SbeCtx* c, double2* const* st, cudaStream_t s);
 void add_rates(const double* wrate, int nk, double* a, double* b, double* cc, double* d,
                cudaStream_t s);

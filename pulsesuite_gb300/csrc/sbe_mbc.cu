@@ -166,17 +166,227 @@ __global__ void __launch_bounds__(256) k_mbc_rates64(const WireDev* wires, int w
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 variant (mixed path).  On the reference grid k = dkr (i - dnk - 1/2) the
+// energies are c u_i^2 with the odd integers u_i = 2 (i - dnk) - 1 and
+// c = hbar^2 dkr^2 / (8 m), so the energy sums of the tables are exact integer
+// forms: with the builder's (a, b, d),
+//   eh: E = 2 (a - d) [ce (u_a + u_d) + ch (2 u_b + u_d - u_a)]
+//   ee: E = 8 ce (a - d) (d - b),   hh: E = 8 ch (a - d) (d - b).
+// x = E / (hbar g) is formed from these integers and split constants (head
+// products exact), so the Lorentzian 1 / (1 + x^2) or the Gaussian exp(-x^2)
+// carries no cancellation of the FP64 energies.  V^2 is scaled by its maximum per
+// kind; the prefactors (2 g / (hbar g)^2 or (2 pi / hbar) / (sqrt(pi) hbar g)) and
+// the V^2 scale are applied in FP64 to the block sums.  Per thread, FP32 sums over
+// 32 pairs are added to FP64 accumulators.
+
+struct MbcConst {
+  float aeh, ael, ahh, ahl;   // x_eh = 2 (a - d) (ae (u_a + u_d) + ah (2 u_b + u_d - u_a))
+  float bee, bhh;             // x_ee = bee (a - d)(d - b), x_hh = bhh (a - d)(d - b)
+  double peh, pee, phh;       // prefactor x V^2 scale per kind
+};
+
+__device__ __forceinline__ float split_head(double v) {
+  // v rounded to 9 significant bits: its product with an integer of magnitude
+  // below 2^15 is exact in FP32
+  const float f = (float)v;
+  return __uint_as_float(__float_as_uint(f) & 0xFFFF8000u);
+}
+
+__device__ __forceinline__ float lor_or_gauss(float x, bool lz) {
+  const float x2 = x * x;
+  if (lz) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + x2));
+    return r;
+  }
+  return __expf(-x2);
+}
+
+__global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w_only,
+                                                     const double2* nev, const double2* nhv,
+                                                     const double* vs, double* wrate, int all) {
+  const WireDev W = wires[w_only >= 0 ? w_only : blockIdx.y];
+  const int n = W.nk;
+  const int row = blockIdx.x + 1;
+  if (row > n || !(all || (W.flags & SBE_F_EHS))) return;
+  const bool holes = blockIdx.z == 1;
+  const bool lz = (W.flags & SBE_F_LORENTZ) != 0;
+  extern __shared__ float shf[];
+  float* ne = shf;                 // [0, n], ne[0] = 0
+  float* nh = shf + (n + 1);
+  float* veh = shf + 2 * (n + 1);  // V_eh^2 / max, by k1 - k2 >= 0
+  float* vxx = veh + n;            // V_ee^2 or V_hh^2 / max
+  __shared__ MbcConst K;
+  __shared__ double vmax[2][8];
+  const double* vsw = vs + 3 * W.off_vec;
+  const double* vx = vsw + (holes ? 2 : 1) * n;
+  double m0 = 0.0, m1 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    m0 = fmax(m0, vsw[i] * vsw[i]);
+    m1 = fmax(m1, vx[i] * vx[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m0 = fmax(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    vmax[0][threadIdx.x >> 5] = m0;
+    vmax[1][threadIdx.x >> 5] = m1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      vmax[0][0] = fmax(vmax[0][0], vmax[0][w]);
+      vmax[1][0] = fmax(vmax[1][0], vmax[1][w]);
+    }
+    const double geh = (W.gam_e + W.gam_h) / 2.0;
+    const double c0 = kHbar * kHbar * W.dkr * W.dkr / 8.0;
+    const double ce = c0 / W.me, ch = c0 / W.mh;
+    const double ae = ce / (kHbar * geh), ah = ch / (kHbar * geh);
+    K.aeh = split_head(ae);
+    K.ael = (float)(ae - (double)K.aeh);
+    K.ahh = split_head(ah);
+    K.ahl = (float)(ah - (double)K.ahh);
+    K.bee = (float)(8.0 * ce / (kHbar * W.gam_e));
+    K.bhh = (float)(8.0 * ch / (kHbar * W.gam_h));
+    auto pref = [&](double g) {
+      const double hg = kHbar * g;
+      return lz ? 2.0 * g / (hg * hg) : kTwoPi / kHbar * (1.0 / (sqrt(kPi) * hg));
+    };
+    K.peh = pref(geh) * vmax[0][0];
+    K.pee = pref(W.gam_e) * vmax[1][0];
+    K.phh = pref(W.gam_h) * vmax[1][0];
+  }
+  __syncthreads();
+  const double s0 = vmax[0][0] > 0.0 ? 1.0 / vmax[0][0] : 0.0;
+  const double s1 = vmax[1][0] > 0.0 ? 1.0 / vmax[1][0] : 0.0;
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) {
+    ne[i] = i == 0 ? 0.f : (float)fabs(nev[W.off_vec + i - 1].x);
+    nh[i] = i == 0 ? 0.f : (float)fabs(nhv[W.off_vec + i - 1].x);
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    veh[i] = (float)(vsw[i] * vsw[i] * s0);
+    vxx[i] = (float)(vx[i] * vx[i] * s1);
+  }
+  __syncthreads();
+  const MbcConst k = K;
+  const int dnk2 = 2 * W.dnk + 1;   // u_i = 2 i - dnk2 (builder index i)
+  // x of the eh table at builder (a, b, d)
+  auto x_eh = [&](int a, int b, int d) {
+    const int ua = 2 * a - dnk2, ud = 2 * d - dnk2, ub = 2 * b - dnk2;
+    const float i1 = (float)(ua + ud), i2 = (float)(2 * ub + ud - ua);
+    const float s = (k.aeh * i1 + k.ahh * i2) + (k.ael * i1 + k.ahl * i2);
+    return (float)(2 * (a - d)) * s;
+  };
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};   // win eh, win xx, wout eh, wout xx
+  float part[4] = {0.f, 0.f, 0.f, 0.f};
+  const int npair = n * n;
+  int cnt = 0;
+  for (int p = threadIdx.x; p < npair; p += blockDim.x) {
+    const int q1 = p % n + 1, q2 = p / n + 1;
+    if (!holes) {
+      const int kk = row;
+      if (q2 < kk) {
+        // Win: eh with (kp, k1) = (q1, q2), ee with (k2, k4) = (q1, q2)
+        const int k1p = q1 + q2 - kk;   // >= 2 for a nonzero table value
+        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k1p >= 2)
+          part[0] += veh[kk - q2] * (1.f - nh[q1]) * nh[k1p] * ne[q2] *
+                     lor_or_gauss(x_eh(kk - 2, q1 - 2, q2 - 2), lz);
+        const int k30 = kk + q1 - q2;
+        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k30 <= n && k30 >= 2)
+          part[1] += vxx[kk - q2] * (1.f - ne[q1]) * ne[k30] * ne[q2] *
+                     lor_or_gauss(k.bee * (float)((kk - q2) * (q2 - q1)), lz);
+      } else if (q2 > kk) {
+        // Wout: eh with (kp, k1) = (q1, q2), ee with (k2, k4) = (q1, q2)
+        const int k1q = q1 + kk - q2;
+        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k1q >= 2)
+          part[2] += veh[q2 - kk] * (1.f - ne[q2]) * (1.f - nh[q1]) * nh[k1q] *
+                     lor_or_gauss(x_eh(q2 - 2, q1 - 2, kk - 2), lz);
+        const int k31 = q2 + q1 - kk;
+        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k31 <= n && k31 >= 2)
+          part[3] += vxx[q2 - kk] * (1.f - ne[q2]) * (1.f - ne[q1]) * ne[k31] *
+                     lor_or_gauss(k.bee * (float)((q2 - kk) * (kk - q1)), lz);
+      }
+    } else {
+      const int kp = row;
+      if (kp >= 2 && q1 >= 2 && q2 >= 2) {
+        if (q1 > q2) {
+          // Win eh: (k, k1) = (q1, q2), k1p = kp + k1 - k
+          const int k1p = kp + q2 - q1;
+          if (k1p >= 2)
+            part[0] += veh[q1 - q2] * (1.f - ne[q1]) * nh[k1p] * ne[q2] *
+                       lor_or_gauss(x_eh(q1 - 2, kp - 2, q2 - 2), lz);
+        } else if (q2 > q1) {
+          // Wout eh: (k, k1) = (q1, q2), k1q = kp + k - k1
+          const int k1q = kp + q1 - q2;
+          if (k1q >= 2)
+            part[2] += veh[q2 - q1] * (1.f - ne[q1]) * (1.f - nh[k1q]) * ne[q2] *
+                       lor_or_gauss(x_eh(q1 - 2, k1q - 2, q2 - 2), lz);
+        }
+        if (q2 < kp) {
+          // Win hh: (k2p, k4p) = (q1, q2), k3p = kp + k2p - k4p
+          const int k3p = kp + q1 - q2;
+          if (k3p <= n)
+            part[1] += vxx[kp - q2] * (1.f - nh[q1]) * nh[k3p] * nh[q2] *
+                       lor_or_gauss(k.bhh * (float)((kp - q2) * (q2 - q1)), lz);
+        } else if (q2 > kp) {
+          // Wout hh: k3q = k4p + k2p - kp
+          const int k3q = q2 + q1 - kp;
+          if (k3q <= n && k3q >= 2)
+            part[3] += vxx[q2 - kp] * (1.f - nh[q2]) * (1.f - nh[q1]) * nh[k3q] *
+                       lor_or_gauss(k.bhh * (float)((q2 - kp) * (kp - q1)), lz);
+        }
+      }
+    }
+    if (++cnt == 32) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc[j] += (double)part[j];
+        part[j] = 0.f;
+      }
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) acc[j] += (double)part[j];
+  __shared__ double red[4][256];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) red[j][threadIdx.x] = acc[j];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) red[j][threadIdx.x] += red[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double px = holes ? k.phh : k.pee;
+    double* wr = wrate + 4 * W.off_vec + (holes ? 2 : 0) * n;
+    wr[row - 1] += k.peh * red[0][0] + px * red[1][0];
+    wr[n + row - 1] += k.peh * red[2][0] + px * red[3][0];
+  }
+}
+
 }  // namespace
 
 // Adds the carrier-carrier in/out rates of every wire with EHs on (or of wire
 // w_only; with all set, whatever its flags) to wrate, at the occupations in ne,
 // nh and the screened V in vs.
-void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all) {
+void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all, bool fp32) {
   bool any = false;
   for (int w = 0; w < c->nw; ++w)
     if ((w_only < 0 || w == w_only) && (all || (c->wires[w].flags & SBE_F_EHS))) any = true;
   if (!any) return;
   const int nk = w_only >= 0 ? c->wires[w_only].nk : c->nk_max;
+  if (fp32) {
+    const size_t smf = sizeof(float) * (2 * (size_t)(nk + 1) + 2 * (size_t)nk);
+    if (smf > 48 * 1024)
+      cudaFuncSetAttribute(k_mbc_rates32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+    k_mbc_rates32<<<dim3(nk, w_only >= 0 ? 1 : c->nw, 2), 256, smf, s>>>(
+        c->d_wires, w_only, c->ne, c->nh, c->vs, c->wrate, all ? 1 : 0);
+    return;
+  }
   const size_t sm = sizeof(double) * (2 * (size_t)(nk + 1) + 3 * (size_t)nk);
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_mbc_rates64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

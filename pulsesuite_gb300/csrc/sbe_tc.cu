@@ -1542,7 +1542,7 @@ static void mixed_relax(SbeCtx* c, double2* C, double2* D, double dt, cudaStream
   launch_extract_diag(c, C, D, s);
   k_phonon_rates_f<<<dim3(nk, nw), 128, sizeof(float) * 2 * nk, s>>>(
       c->d_wires, c->ne, c->nh, m->phf, m->epf, m->eptf, m->hpf, m->hptf, c->wrate, nw);
-  launch_mbc_rates(c, -1, s);
+  launch_mbc_rates(c, -1, s, false, true);
   launch_relax_only(c, C, D, dt, s);
   k_diag_max<<<nw, 256, 0, s>>>(c->d_wires, C, D, m->mxS());
 }

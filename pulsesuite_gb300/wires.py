@@ -215,11 +215,13 @@ class WireContext:
                                              _lib.ptr(WoutE), _lib.ptr(WinH), _lib.ptr(WoutH),
                                              _lib.stream_handle()), "sbe_phonon_rates")
 
-    def carrier_rates(self, w, ne, nh, VC, WinE, WoutE, WinH, WoutH):
-        """coulomb.py:1298/1313 MBCE/MBCH: adds the carrier-carrier rates to Win/Wout."""
+    def carrier_rates(self, w, ne, nh, VC, WinE, WoutE, WinH, WoutH, precision="fp64"):
+        """coulomb.py:1298/1313 MBCE/MBCH: adds the carrier-carrier rates to Win/Wout
+        (precision "fp64" or "mixed")."""
+        prec = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
         _lib.check(self.lib.sbe_carrier_rates(self.handle, w, _lib.ptr(ne), _lib.ptr(nh),
                                               _lib.ptr(VC), _lib.ptr(WinE), _lib.ptr(WoutE),
-                                              _lib.ptr(WinH), _lib.ptr(WoutH),
+                                              _lib.ptr(WinH), _lib.ptr(WoutH), prec,
                                               _lib.stream_handle()), "sbe_carrier_rates")
 
     def sources(self, w, P, C, D, ne, nh):

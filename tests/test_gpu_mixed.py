@@ -111,12 +111,13 @@ def test_graph_replay_matches_direct_step(prec):
         assert torch.equal(a, b)
 
 
-@pytest.mark.parametrize("nk", [64, 128])
-def test_mixed_rk4_pulse_vs_fp64(nk):
-    """40 RK4 steps through the rising edge of a pulse, mixed vs FP64."""
+@pytest.mark.parametrize("nk,ehs", [(64, False), (128, False), (64, True)])
+def test_mixed_rk4_pulse_vs_fp64(nk, ehs):
+    """40 RK4 steps through the rising edge of a pulse, mixed vs FP64 (with ehs: the
+    carrier-carrier rates in the relaxation, FP32 kernel against the FP64 one)."""
     from pulsesuite_gb300 import _lib
     nw = 2
-    ctx, _ = make_ctx(nk, nw)
+    ctx, _ = make_ctx(nk, nw, flags=dict(ALL, EHs=ehs))
     rng = np.random.default_rng(3)
     st = [seeded(rng, nk, 1e-4) for _ in range(nw)]
     states = {}
