@@ -166,7 +166,7 @@ def config_of(wl, impl):
                         f"tau={wl['tau']*1e15:.0f} fs, T={wl['temp']:.0f} K, "
                         f"RK4 dt={wl['dt']*1e15:.2f} fs",
             "wires": wl["nw"], "nk": wl["nk"], "nr": 2 * wl["nk"] + 2, "nx": wl["nx"],
-            "flags": "Optics Excitons Screened Phonon LF DiagDph OffDiagDph",
+            "flags": " ".join(k for k, v in FLAGS.items() if v),
             "integrator": "RK4 (coefficients frozen per step) + reference relaxation/normalisation",
             "l2": "inputs larger than L2 (FP64 state 403 MB, FP16 operand planes 1.9 GB per stage)",
             "impl": impl}
@@ -465,7 +465,12 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--ehs", action="store_true",
+                    help="carrier-carrier scattering (EHs) on in every wire (not the default "
+                         "workload's flags)")
     args = ap.parse_args()
+    if args.ehs:
+        FLAGS["EHs"] = True
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         reference_arm(args, wl)

@@ -281,71 +281,68 @@ __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w
   };
   double acc[4] = {0.0, 0.0, 0.0, 0.0};   // win eh, win xx, wout eh, wout xx
   float part[4] = {0.f, 0.f, 0.f, 0.f};
-  const int npair = n * n;
-  int cnt = 0;
-  for (int p = threadIdx.x; p < npair; p += blockDim.x) {
-    const int q1 = p % n + 1, q2 = p / n + 1;
-    if (!holes) {
-      const int kk = row;
-      if (q2 < kk) {
-        // Win: eh with (kp, k1) = (q1, q2), ee with (k2, k4) = (q1, q2)
-        const int k1p = q1 + q2 - kk;   // >= 2 for a nonzero table value
-        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k1p >= 2)
-          part[0] += veh[kk - q2] * (1.f - nh[q1]) * nh[k1p] * ne[q2] *
-                     lor_or_gauss(x_eh(kk - 2, q1 - 2, q2 - 2), lz);
-        const int k30 = kk + q1 - q2;
-        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k30 <= n && k30 >= 2)
-          part[1] += vxx[kk - q2] * (1.f - ne[q1]) * ne[k30] * ne[q2] *
-                     lor_or_gauss(k.bee * (float)((kk - q2) * (q2 - q1)), lz);
-      } else if (q2 > kk) {
-        // Wout: eh with (kp, k1) = (q1, q2), ee with (k2, k4) = (q1, q2)
-        const int k1q = q1 + kk - q2;
-        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k1q >= 2)
-          part[2] += veh[q2 - kk] * (1.f - ne[q2]) * (1.f - nh[q1]) * nh[k1q] *
-                     lor_or_gauss(x_eh(q2 - 2, q1 - 2, kk - 2), lz);
-        const int k31 = q2 + q1 - kk;
-        if (kk >= 2 && q1 >= 2 && q2 >= 2 && k31 <= n && k31 >= 2)
-          part[3] += vxx[q2 - kk] * (1.f - ne[q2]) * (1.f - ne[q1]) * ne[k31] *
-                     lor_or_gauss(k.bee * (float)((q2 - kk) * (kk - q1)), lz);
-      }
-    } else {
-      const int kp = row;
-      if (kp >= 2 && q1 >= 2 && q2 >= 2) {
-        if (q1 > q2) {
-          // Win eh: (k, k1) = (q1, q2), k1p = kp + k1 - k
-          const int k1p = kp + q2 - q1;
-          if (k1p >= 2)
-            part[0] += veh[q1 - q2] * (1.f - ne[q1]) * nh[k1p] * ne[q2] *
-                       lor_or_gauss(x_eh(q1 - 2, kp - 2, q2 - 2), lz);
-        } else if (q2 > q1) {
-          // Wout eh: (k, k1) = (q1, q2), k1q = kp + k - k1
-          const int k1q = kp + q1 - q2;
-          if (k1q >= 2)
-            part[2] += veh[q2 - q1] * (1.f - ne[q1]) * (1.f - nh[k1q]) * ne[q2] *
-                       lor_or_gauss(x_eh(q1 - 2, k1q - 2, q2 - 2), lz);
+  // warp w takes q2 = 2 + w, 2 + w + 8, ...; its lanes walk the q1 range in which
+  // the term's indices are valid and its table value can be nonzero (q1, q2, the
+  // row and the third index at least 2 for the one-lower table read, the third
+  // index within [1, Nk], V^2 of a nonnegative index difference)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int r = row;
+  if (r >= 2) {
+    for (int q2 = 2 + warp; q2 <= n; q2 += nwarp) {
+      if (!holes) {
+        if (q2 < r) {
+          const float ve = veh[r - q2], vx2 = vxx[r - q2], nq2 = ne[q2];
+          // Win eh: (kp, k1) = (q1, q2), k1p = q1 + q2 - r
+          for (int q1 = max(2, r - q2 + 2) + lane; q1 <= n; q1 += 32)
+            part[0] += ve * (1.f - nh[q1]) * nh[q1 + q2 - r] * nq2 *
+                       lor_or_gauss(x_eh(r - 2, q1 - 2, q2 - 2), lz);
+          // Win ee: (k2, k4) = (q1, q2), k30 = r + q1 - q2
+          for (int q1 = 2 + lane; q1 <= n - r + q2; q1 += 32)
+            part[1] += vx2 * (1.f - ne[q1]) * ne[r + q1 - q2] * nq2 *
+                       lor_or_gauss(k.bee * (float)((r - q2) * (q2 - q1)), lz);
+        } else if (q2 > r) {
+          const float ve = veh[q2 - r], vx2 = vxx[q2 - r], mq2 = 1.f - ne[q2];
+          // Wout eh: (kp, k1) = (q1, q2), k1q = q1 + r - q2
+          for (int q1 = max(2, q2 - r + 2) + lane; q1 <= n; q1 += 32)
+            part[2] += ve * mq2 * (1.f - nh[q1]) * nh[q1 + r - q2] *
+                       lor_or_gauss(x_eh(q2 - 2, q1 - 2, r - 2), lz);
+          // Wout ee: (k2, k4) = (q1, q2), k31 = q2 + q1 - r
+          for (int q1 = 2 + lane; q1 <= n + r - q2; q1 += 32)
+            part[3] += vx2 * mq2 * (1.f - ne[q1]) * ne[q2 + q1 - r] *
+                       lor_or_gauss(k.bee * (float)((q2 - r) * (r - q1)), lz);
         }
-        if (q2 < kp) {
-          // Win hh: (k2p, k4p) = (q1, q2), k3p = kp + k2p - k4p
-          const int k3p = kp + q1 - q2;
-          if (k3p <= n)
-            part[1] += vxx[kp - q2] * (1.f - nh[q1]) * nh[k3p] * nh[q2] *
-                       lor_or_gauss(k.bhh * (float)((kp - q2) * (q2 - q1)), lz);
-        } else if (q2 > kp) {
-          // Wout hh: k3q = k4p + k2p - kp
-          const int k3q = q2 + q1 - kp;
-          if (k3q <= n && k3q >= 2)
-            part[3] += vxx[q2 - kp] * (1.f - nh[q2]) * (1.f - nh[q1]) * nh[k3q] *
-                       lor_or_gauss(k.bhh * (float)((q2 - kp) * (kp - q1)), lz);
+      } else {
+        const float nq2 = ne[q2];
+        // Win eh (q1 > q2): (k, k1) = (q1, q2), k1p = r + q2 - q1
+        for (int q1 = q2 + 1 + lane; q1 <= min(n, r + q2 - 2); q1 += 32)
+          part[0] += veh[q1 - q2] * (1.f - ne[q1]) * nh[r + q2 - q1] * nq2 *
+                     lor_or_gauss(x_eh(q1 - 2, r - 2, q2 - 2), lz);
+        // Wout eh (q1 < q2): k1q = r + q1 - q2
+        for (int q1 = max(2, q2 - r + 2) + lane; q1 < q2; q1 += 32) {
+          const int k1q = r + q1 - q2;
+          part[2] += veh[q2 - q1] * (1.f - ne[q1]) * (1.f - nh[k1q]) * nq2 *
+                     lor_or_gauss(x_eh(q1 - 2, k1q - 2, q2 - 2), lz);
+        }
+        if (q2 < r) {
+          const float vx2 = vxx[r - q2], hq2 = nh[q2];
+          // Win hh: (k2p, k4p) = (q1, q2), k3p = r + q1 - q2
+          for (int q1 = 2 + lane; q1 <= n - r + q2; q1 += 32)
+            part[1] += vx2 * (1.f - nh[q1]) * nh[r + q1 - q2] * hq2 *
+                       lor_or_gauss(k.bhh * (float)((r - q2) * (q2 - q1)), lz);
+        } else if (q2 > r) {
+          const float vx2 = vxx[q2 - r], mq2 = 1.f - nh[q2];
+          // Wout hh: k3q = q2 + q1 - r
+          for (int q1 = 2 + lane; q1 <= n + r - q2; q1 += 32)
+            part[3] += vx2 * mq2 * (1.f - nh[q1]) * nh[q2 + q1 - r] *
+                       lor_or_gauss(k.bhh * (float)((q2 - r) * (r - q1)), lz);
         }
       }
-    }
-    if (++cnt == 32) {
+      // per q2 row (at most Nk / 32 terms per lane and sum): FP64 accumulation
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         acc[j] += (double)part[j];
         part[j] = 0.f;
       }
-      cnt = 0;
     }
   }
 #pragma unroll
