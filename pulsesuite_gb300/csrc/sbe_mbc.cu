@@ -177,8 +177,8 @@ __global__ void __launch_bounds__(256) k_mbc_rates64(const WireDev* wires, int w
 // products exact), so the Lorentzian 1 / (1 + x^2) or the Gaussian exp(-x^2)
 // carries no cancellation of the FP64 energies.  V^2 is scaled by its maximum per
 // kind; the prefactors (2 g / (hbar g)^2 or (2 pi / hbar) / (sqrt(pi) hbar g)) and
-// the V^2 scale are applied in FP64 to the block sums.  Per thread, FP32 sums over
-// 32 pairs are added to FP64 accumulators.
+// the V^2 scale are applied in FP64 to the block sums.  Per thread, the FP32 sums of
+// one q2 row are added with compensation (Kahan); the block sums are FP64.
 
 struct MbcConst {
   float aeh, ael, ahh, ahl;   // x_eh = 2 (a - d) (ae (u_a + u_d) + ah (2 u_b + u_d - u_a))
@@ -279,8 +279,8 @@ __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w
     const float s = (k.aeh * i1 + k.ahh * i2) + (k.ael * i1 + k.ahl * i2);
     return (float)(2 * (a - d)) * s;
   };
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};   // win eh, win xx, wout eh, wout xx
-  float part[4] = {0.f, 0.f, 0.f, 0.f};
+  // sums: win eh, win xx, wout eh, wout xx
+  float part[4] = {0.f, 0.f, 0.f, 0.f}, accs[4] = {0.f, 0.f, 0.f, 0.f}, comp[4] = {0.f, 0.f, 0.f, 0.f};
   // warp w takes q2 = 2 + w, 2 + w + 8, ...; its lanes walk the q1 range in which
   // the term's indices are valid and its table value can be nonzero (q1, q2, the
   // row and the third index at least 2 for the one-lower table read, the third
@@ -337,16 +337,21 @@ __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w
                        lor_or_gauss(k.bhh * (float)((q2 - r) * (r - q1)), lz);
         }
       }
-      // per q2 row (at most Nk / 32 terms per lane and sum): FP64 accumulation
+      // per q2 row (at most Nk / 32 terms per lane and sum): compensated FP32
+      // accumulation (an FP64 add per row and sum kept the FP64 pipe busy)
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        acc[j] += (double)part[j];
+        const float y = part[j] - comp[j];
+        const float t = accs[j] + y;
+        comp[j] = (t - accs[j]) - y;
+        accs[j] = t;
         part[j] = 0.f;
       }
     }
   }
+  double acc[4];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) acc[j] += (double)part[j];
+  for (int j = 0; j < 4; ++j) acc[j] = (double)accs[j] - (double)comp[j];
   __shared__ double red[4][256];
 #pragma unroll
   for (int j = 0; j < 4; ++j) red[j][threadIdx.x] = acc[j];
