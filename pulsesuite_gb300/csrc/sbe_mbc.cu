@@ -193,9 +193,10 @@ __device__ __forceinline__ float split_head(double v) {
   return __uint_as_float(__float_as_uint(f) & 0xFFFF8000u);
 }
 
-__device__ __forceinline__ float lor_or_gauss(float x, bool lz) {
+template <bool LZ>
+__device__ __forceinline__ float lor_or_gauss(float x) {
   const float x2 = x * x;
-  if (lz) {
+  if (LZ) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + x2));
     return r;
@@ -203,6 +204,54 @@ __device__ __forceinline__ float lor_or_gauss(float x, bool lz) {
   return __expf(-x2);
 }
 
+// Gaussian broadening: terms with |x| > MBC_XCUT (exp(-x^2) < 6e-19 of the
+// largest) are left out; their FP32 value is below the sums' rounding.
+constexpr float MBC_XCUT = 6.5f;
+
+__device__ __forceinline__ int clamp_int(float v) {
+  return (int)fminf(fmaxf(v, -1.0e6f), 1.0e6f);
+}
+
+// q in [lo, hi] with |2 (q - q2) (P q + Q)| <= MBC_XCUT (P != 0): the parabola
+// 2 P (q - m)^2 - 2 P h^2 (roots q2 and -Q / P, midpoint m, half distance h) lies
+// within +-X on [m - R+, m - R-] and [m + R-, m + R+], R+- = sqrt(h^2 +- X / (2P))
+// (one interval when h^2 <= X / (2P)); bounds widened by 2; empty: lo > hi.
+__device__ __forceinline__ void band_quad(float P, float Q, int q2, int lo, int hi, int& l1,
+                                          int& h1, int& l2, int& h2) {
+  if (P < 0.f) {
+    P = -P;
+    Q = -Q;
+  }
+  const float qs = -__fdividef(Q, P);   // band bounds carry a margin: fast divisions
+  const float m = 0.5f * ((float)q2 + qs), h = 0.5f * (qs - (float)q2);
+  const float t = __fdividef(MBC_XCUT, 2.f * P);
+  const float Rp = sqrtf(h * h + t), hm = h * h - t;
+  l1 = max(lo, clamp_int(floorf(m - Rp)) - 2);
+  h2 = min(hi, clamp_int(ceilf(m + Rp)) + 2);
+  if (hm <= 0.f) {
+    h1 = h2;
+    l2 = 1;
+    h2 = 0;
+    return;
+  }
+  const float Rm = sqrtf(hm);
+  h1 = min(hi, clamp_int(ceilf(m - Rm)) + 2);
+  l2 = max(lo, clamp_int(floorf(m + Rm)) - 2);
+  if (l2 <= h1 + 1) {   // the two intervals touch: one
+    h1 = max(h1, h2);
+    l2 = 1;
+    h2 = 0;
+  }
+}
+
+// q1 range of |m (C + s q1)| <= MBC_XCUT (m > 0, s > 0), widened by 2
+__device__ __forceinline__ void band_linear(float m, float C, float s, int& lo, int& hi) {
+  const float c = __fdividef(MBC_XCUT, m), is = __fdividef(1.f, s);
+  lo = max(lo, clamp_int(floorf((-c - C) * is)) - 2);
+  hi = min(hi, clamp_int(ceilf((c - C) * is)) + 2);
+}
+
+template <bool LZ>
 __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w_only,
                                                      const double2* nev, const double2* nhv,
                                                      const double* vs, double* wrate, int all) {
@@ -210,8 +259,9 @@ __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w
   const int n = W.nk;
   const int row = blockIdx.x + 1;
   if (row > n || !(all || (W.flags & SBE_F_EHS))) return;
-  const bool holes = blockIdx.z == 1;
   const bool lz = (W.flags & SBE_F_LORENTZ) != 0;
+  if (lz != LZ) return;   // the other instantiation takes this wire
+  const bool holes = blockIdx.z == 1;
   extern __shared__ float shf[];
   float* ne = shf;                 // [0, n], ne[0] = 0
   float* nh = shf + (n + 1);
@@ -288,53 +338,109 @@ __global__ void __launch_bounds__(256) k_mbc_rates32(const WireDev* wires, int w
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int r = row;
   if (r >= 2) {
+    // eh band (Gaussian): x = 2 (a - d) S with S linear in b = q1 - 2 at fixed (a, d)
+    const float ah_f = k.ahh + k.ahl, ae_f = k.aeh + k.ael;
+    auto eh_band = [&](int a, int d, int& lo, int& hi) {
+      if (LZ) return;
+      const int ua = 2 * a - dnk2, ud = 2 * d - dnk2;
+      const float C = ae_f * (float)(ua + ud) + ah_f * (float)(ud - ua - 2 * dnk2 - 8);
+      band_linear((float)(2 * (a - d)), C, 4.f * ah_f, lo, hi);
+    };
+    // xx band (Gaussian): x = beta m (q - q1) with m > 0: |q - q1| <= w
+    auto xx_band = [&](float beta, int m, int q, int& lo, int& hi) {
+      if (LZ) return;
+      const int w = clamp_int(__fdividef(MBC_XCUT, beta * (float)m)) + 2;
+      lo = max(lo, q - w);
+      hi = min(hi, q + w);
+    };
     for (int q2 = 2 + warp; q2 <= n; q2 += nwarp) {
       if (!holes) {
         if (q2 < r) {
           const float ve = veh[r - q2], vx2 = vxx[r - q2], nq2 = ne[q2];
           // Win eh: (kp, k1) = (q1, q2), k1p = q1 + q2 - r
-          for (int q1 = max(2, r - q2 + 2) + lane; q1 <= n; q1 += 32)
+          int lo = max(2, r - q2 + 2), hi = n;
+          eh_band(r - 2, q2 - 2, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[0] += ve * (1.f - nh[q1]) * nh[q1 + q2 - r] * nq2 *
-                       lor_or_gauss(x_eh(r - 2, q1 - 2, q2 - 2), lz);
+                       lor_or_gauss<LZ>(x_eh(r - 2, q1 - 2, q2 - 2));
           // Win ee: (k2, k4) = (q1, q2), k30 = r + q1 - q2
-          for (int q1 = 2 + lane; q1 <= n - r + q2; q1 += 32)
+          lo = 2;
+          hi = n - r + q2;
+          xx_band(k.bee, r - q2, q2, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[1] += vx2 * (1.f - ne[q1]) * ne[r + q1 - q2] * nq2 *
-                       lor_or_gauss(k.bee * (float)((r - q2) * (q2 - q1)), lz);
+                       lor_or_gauss<LZ>(k.bee * (float)((r - q2) * (q2 - q1)));
         } else if (q2 > r) {
           const float ve = veh[q2 - r], vx2 = vxx[q2 - r], mq2 = 1.f - ne[q2];
           // Wout eh: (kp, k1) = (q1, q2), k1q = q1 + r - q2
-          for (int q1 = max(2, q2 - r + 2) + lane; q1 <= n; q1 += 32)
+          int lo = max(2, q2 - r + 2), hi = n;
+          eh_band(q2 - 2, r - 2, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[2] += ve * mq2 * (1.f - nh[q1]) * nh[q1 + r - q2] *
-                       lor_or_gauss(x_eh(q2 - 2, q1 - 2, r - 2), lz);
+                       lor_or_gauss<LZ>(x_eh(q2 - 2, q1 - 2, r - 2));
           // Wout ee: (k2, k4) = (q1, q2), k31 = q2 + q1 - r
-          for (int q1 = 2 + lane; q1 <= n + r - q2; q1 += 32)
+          lo = 2;
+          hi = n + r - q2;
+          xx_band(k.bee, q2 - r, r, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[3] += vx2 * mq2 * (1.f - ne[q1]) * ne[q2 + q1 - r] *
-                       lor_or_gauss(k.bee * (float)((q2 - r) * (r - q1)), lz);
+                       lor_or_gauss<LZ>(k.bee * (float)((q2 - r) * (r - q1)));
         }
       } else {
         const float nq2 = ne[q2];
+        // eh terms: x = 2 (q1 - q2) (P q1 + Q) is quadratic in q1; (Gaussian) the
+        // loops walk the band of |x| <= MBC_XCUT and skip what lies beyond the cut
+        const int ud = 2 * (q2 - 2) - dnk2, ub = 2 * (r - 2) - dnk2;
+        int l1, h1, l2, h2;
         // Win eh (q1 > q2): (k, k1) = (q1, q2), k1p = r + q2 - q1
-        for (int q1 = q2 + 1 + lane; q1 <= min(n, r + q2 - 2); q1 += 32)
-          part[0] += veh[q1 - q2] * (1.f - ne[q1]) * nh[r + q2 - q1] * nq2 *
-                     lor_or_gauss(x_eh(q1 - 2, r - 2, q2 - 2), lz);
+        l1 = q2 + 1;
+        h1 = min(n, r + q2 - 2);
+        l2 = 1;
+        h2 = 0;
+        if (!LZ)
+          band_quad(2.f * (ae_f - ah_f),
+                    (ae_f - ah_f) * (float)(-4 - dnk2) + ae_f * (float)ud + ah_f * (float)(2 * ub + ud),
+                    q2, l1, h1, l1, h1, l2, h2);
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+          for (int q1 = (j ? l2 : l1) + lane; q1 <= (j ? h2 : h1); q1 += 32) {
+            const float x = x_eh(q1 - 2, r - 2, q2 - 2);
+            if (!LZ && fabsf(x) > MBC_XCUT) continue;
+            part[0] += veh[q1 - q2] * (1.f - ne[q1]) * nh[r + q2 - q1] * nq2 * lor_or_gauss<LZ>(x);
+          }
         // Wout eh (q1 < q2): k1q = r + q1 - q2
-        for (int q1 = max(2, q2 - r + 2) + lane; q1 < q2; q1 += 32) {
-          const int k1q = r + q1 - q2;
-          part[2] += veh[q2 - q1] * (1.f - ne[q1]) * (1.f - nh[k1q]) * nq2 *
-                     lor_or_gauss(x_eh(q1 - 2, k1q - 2, q2 - 2), lz);
-        }
+        l1 = max(2, q2 - r + 2);
+        h1 = q2 - 1;
+        l2 = 1;
+        h2 = 0;
+        if (!LZ)
+          band_quad(2.f * (ae_f + ah_f),
+                    (ae_f + ah_f) * (float)(-4 - dnk2 + ud) + 4.f * ah_f * (float)(r - q2), q2,
+                    l1, h1, l1, h1, l2, h2);
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+          for (int q1 = (j ? l2 : l1) + lane; q1 <= (j ? h2 : h1); q1 += 32) {
+            const int k1q = r + q1 - q2;
+            const float x = x_eh(q1 - 2, k1q - 2, q2 - 2);
+            if (!LZ && fabsf(x) > MBC_XCUT) continue;
+            part[2] += veh[q2 - q1] * (1.f - ne[q1]) * (1.f - nh[k1q]) * nq2 * lor_or_gauss<LZ>(x);
+          }
         if (q2 < r) {
           const float vx2 = vxx[r - q2], hq2 = nh[q2];
           // Win hh: (k2p, k4p) = (q1, q2), k3p = r + q1 - q2
-          for (int q1 = 2 + lane; q1 <= n - r + q2; q1 += 32)
+          int lo = 2, hi = n - r + q2;
+          xx_band(k.bhh, r - q2, q2, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[1] += vx2 * (1.f - nh[q1]) * nh[r + q1 - q2] * hq2 *
-                       lor_or_gauss(k.bhh * (float)((r - q2) * (q2 - q1)), lz);
+                       lor_or_gauss<LZ>(k.bhh * (float)((r - q2) * (q2 - q1)));
         } else if (q2 > r) {
           const float vx2 = vxx[q2 - r], mq2 = 1.f - nh[q2];
           // Wout hh: k3q = q2 + q1 - r
-          for (int q1 = 2 + lane; q1 <= n + r - q2; q1 += 32)
+          int lo = 2, hi = n + r - q2;
+          xx_band(k.bhh, q2 - r, r, lo, hi);
+          for (int q1 = lo + lane; q1 <= hi; q1 += 32)
             part[3] += vx2 * mq2 * (1.f - nh[q1]) * nh[q2 + q1 - r] *
-                       lor_or_gauss(k.bhh * (float)((q2 - r) * (r - q1)), lz);
+                       lor_or_gauss<LZ>(k.bhh * (float)((q2 - r) * (r - q1)));
         }
       }
       // per q2 row (at most Nk / 32 terms per lane and sum): compensated FP32
@@ -383,10 +489,23 @@ void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all, bool fp32
   const int nk = w_only >= 0 ? c->wires[w_only].nk : c->nk_max;
   if (fp32) {
     const size_t smf = sizeof(float) * (2 * (size_t)(nk + 1) + 2 * (size_t)nk);
-    if (smf > 48 * 1024)
-      cudaFuncSetAttribute(k_mbc_rates32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
-    k_mbc_rates32<<<dim3(nk, w_only >= 0 ? 1 : c->nw, 2), 256, smf, s>>>(
-        c->d_wires, w_only, c->ne, c->nh, c->vs, c->wrate, all ? 1 : 0);
+    if (smf > 48 * 1024) {
+      cudaFuncSetAttribute(k_mbc_rates32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smf);
+      cudaFuncSetAttribute(k_mbc_rates32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smf);
+    }
+    // one instantiation per broadening; each skips the other's wires
+    bool gauss = false, lor = false;
+    for (int w = 0; w < c->nw; ++w)
+      if (w_only < 0 || w == w_only) (c->wires[w].flags & SBE_F_LORENTZ ? lor : gauss) = true;
+    const dim3 grid(nk, w_only >= 0 ? 1 : c->nw, 2);
+    if (gauss)
+      k_mbc_rates32<false><<<grid, 256, smf, s>>>(c->d_wires, w_only, c->ne, c->nh, c->vs,
+                                                   c->wrate, all ? 1 : 0);
+    if (lor)
+      k_mbc_rates32<true><<<grid, 256, smf, s>>>(c->d_wires, w_only, c->ne, c->nh, c->vs,
+                                                  c->wrate, all ? 1 : 0);
     return;
   }
   const size_t sm = sizeof(double) * (2 * (size_t)(nk + 1) + 3 * (size_t)nk);
