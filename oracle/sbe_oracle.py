@@ -995,10 +995,61 @@ def mbch(ne0, nh0, VC, mb):
     return win, wout
 
 
-def relax(ne, nh, VC, E1D, pt, dt, ehs, phonon, small=SMALL, mb=None):
+EMISSION_TEMP = 77.0   # emission.py:28 _Temp: the module's own temperature, never set by SBEs.py
+
+
+def emission_tables(dcv, epsr, geh, ehint, temp=EMISSION_TEMP):
+    """emission.py:35-91 InitializeEmission with CalcHOmega (:220-255): the photon
+    energy grid HOmega (midpoints, dhw) and the pre-calculated ``square`` array."""
+    kBT = KB * temp
+    hg = HBAR * geh
+    hwmax = (kBT + hg) * 4.0
+    dhw = min(kBT, hg) / 20.0
+    nw = int(np.ceil(hwmax / dhw))
+    if nw < 10:
+        raise ValueError("temperature too low for the emission grid")
+    how = np.array([0.0 + (n + 0.5) * dhw for n in range(nw)])
+    lrtz = (hg / np.pi) / (how ** 2 + hg ** 2)
+    square = (3.0 * dcv ** 2 * ehint / EPS0 / np.sqrt(epsr) * ehint / HBAR * lrtz
+              * np.exp(-how / KB / temp))
+    return dict(HOmega=how, square=square, dhw=how[1] - how[0])
+
+
+def coulomb_ec(ne, nh, VC):
+    """emission.py:133-171 Ec: Coulomb energy correction per k (ne, nh real)."""
+    n = len(ne)
+    Veh, Vee, Vhh = VC[:, :, 0], VC[:, :, 1], VC[:, :, 2]
+    idel = 1.0 - np.eye(n)
+    out = np.zeros(n)
+    for k in range(n):
+        out[k] = (np.sum(ne * (Vee[k, k] - Vee[:, k]) + nh * (Vhh[k, k] - Vhh[:, k]))
+                  + np.sum(ne * Veh[k, k] * idel[:, k] - nh * Veh[k, k] * idel[:, k])
+                  - Veh[k, k])
+    return out
+
+
+def spont_emission(ne, nh, Ee, Eh, gap, VC, et):
+    """emission.py:94-131 SpontEmission with SpontIntegral (:174-198) and rho0
+    (:201-217): Rsp per k."""
+    Ek = gap + Ee + Eh + coulomb_ec(np.real(ne), np.real(nh), VC)
+    how, sq = et["HOmega"], et["square"]
+    rsp = np.zeros(len(ne))
+    for k in range(len(ne)):
+        hw = how + Ek[k]
+        rsp[k] = np.sum(hw * (hw ** 2 / (C0 ** 3 * PI ** 2 * HBAR ** 3)) * sq) * et["dhw"]
+    return rsp
+
+
+def relax(ne, nh, VC, E1D, pt, dt, ehs, phonon, small=SMALL, mb=None, rsp=None):
     """SBEs.py:5228-5325 _relaxation with RelaxationE/H (SBEs.py:1709-1835): the
     carrier-carrier rates (EHs; ``mb`` = dict(Ee, Eh, ge, gh, lorentz)) first, then
-    the phonon rates added."""
+    the phonon rates added; with ``rsp`` (Recomb) the spontaneous-emission decay
+    after them (SBEs.py:5322-5325)."""
+    if rsp is not None:
+        ne, nh = relax(ne, nh, VC, E1D, pt, dt, ehs, phonon, small, mb)
+        ne = ne * np.exp(-rsp * nh * dt)
+        nh = nh * np.exp(-rsp * ne * dt)
+        return ne, nh
     if not (phonon or ehs):
         return ne, nh
     n = len(ne)
@@ -1039,6 +1090,9 @@ class Wire:
         # carrier-carrier scattering tables are evaluated on the fly (mb_value)
         self.mb = dict(Ee=self.c["Ee"], Eh=self.c["Eh"], ge=p["gam_e"], gh=p["gam_h"],
                        lorentz=bool(self.flags.get("LorentzDelta", False)))
+        # SBEs.py:4905-4915: emission tables when Recomb is on
+        self.et = (emission_tables(abs(self.c["dcv"]), p["epsr"], p["gam_eh"], self.c["ehint"])
+                   if self.flags.get("Recomb", False) else None)
         self.dt = dephasing_tables(self.g["kr"], p["me"], p["mh"])
         self.window = qw_window(self.g["r"], L)
         self.E = expikr(self.g["kr"], self.g["r"])
@@ -1066,8 +1120,11 @@ class Wire:
         if f["OffDiagDph"]:
             gv = np.array([prm["gam_eh"], prm["gam_e"], prm["gam_h"]])
             OffP, _, _ = offdiag_dephasing2(ne, nh, p2, c["Ee"], c["Eh"], gv, VC)
+        # SBEs.py:5203-5226: spontaneous emission rates of the prepared occupations
+        Rsp = (spont_emission(ne, nh, c["Ee"], c["Eh"], prm["gap"], VC, self.et)
+               if f.get("Recomb", False) else None)
         return dict(Heh=Heh, Hee=Hee, Hhh=Hhh, VC=VC, E1D=E1D, GamE=GamE, GamH=GamH,
-                    OffP=OffP, Meh=Meh)
+                    OffP=OffP, Meh=Meh, Rsp=Rsp)
 
     def rhs(self, P, C, D, Ex, Ey, Ez, w):
         pr = self.prepare(P, C, D, Ex, Ey, Ez, w)
@@ -1099,6 +1156,8 @@ class Wire:
         if f["DiagDph"]:
             GamE = gamma_e(g["kr"], ne, nh, VC, self.dt)
             GamH = gamma_h(g["kr"], ne, nh, VC, self.dt)
+        Rsp = (spont_emission(ne, nh, c["Ee"], c["Eh"], prm["gap"], VC, self.et)
+               if f.get("Recomb", False) else None)
         De = Dh = None
         if f["OffDiagDph"]:
             gv = np.array([prm["gam_eh"], prm["gam_e"], prm["gam_h"]])
@@ -1124,9 +1183,9 @@ class Wire:
         k4 = f_rhs(*[x + dt * k for x, k in zip(X, k3)], 1.0)
         P, C, D = [x + dt / 6.0 * (a + 2.0 * b + 2.0 * cc + d)
                    for x, a, b, cc, d in zip(X, k1, k2, k3, k4)]
-        if f["EHs"] or f["Phonon"]:
+        if f["EHs"] or f["Phonon"] or f.get("Recomb", False):
             ne3, nh3 = relax(np.diag(C).copy(), np.diag(D).copy(), VC, E1D, self.pt, dt,
-                             f["EHs"], f["Phonon"], mb=self.mb)
+                             f["EHs"], f["Phonon"], mb=self.mb, rsp=Rsp)
             C[np.diag_indices(nk)] = ne3
             D[np.diag_indices(nk)] = nh3
         ne3 = np.abs(np.diag(C)).astype(complex)
@@ -1185,9 +1244,9 @@ class Solver:
         C3 = C1 + dC * dt * 2.0
         D3 = D1 + dD * dt * 2.0
         p3 = p1 + dP * dt * 2.0
-        if f["EHs"] or f["Phonon"]:
+        if f["EHs"] or f["Phonon"] or f.get("Recomb", False):
             ne3, nh3 = relax(np.diag(C3).copy(), np.diag(D3).copy(), pr["VC"], pr["E1D"],
-                             wi.pt, dt, f["EHs"], f["Phonon"], mb=wi.mb)
+                             wi.pt, dt, f["EHs"], f["Phonon"], mb=wi.mb, rsp=pr["Rsp"])
             C3[np.diag_indices(g["nk"])] = ne3
             D3[np.diag_indices(g["nk"])] = nh3
         ne3 = np.abs(np.diag(C3)).astype(complex)

@@ -22,6 +22,8 @@ phonon_nkN      ``phonons.InitializePhonons`` tables and ``MBPE``/``MBPH``.
 mbc_nkN         ``coulomb.CoulombModule`` carrier-carrier scattering ``MBCE``/``MBCH``
                 (and the ``CalcMBArrays`` tables) with Gaussian and Lorentzian
                 broadening.  ``make_golden.py <src> mbc`` writes these alone.
+emission_nkN    ``emission.InitializeEmission`` tables and ``SpontEmission`` (Recomb);
+                ``make_golden.py <src> emission`` writes these alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
                 ``OffDiagDephasing2``.
 qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
@@ -266,6 +268,24 @@ def case_mbc(nk, seed, VC):
     return out
 
 
+def case_emission(nk, seed, VC):
+    """emission.InitializeEmission + SpontEmission (Recomb)."""
+    from pulsesuite.PSTD3D import emission
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    ne = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    nh = rng.uniform(0.0, 0.4, nk) + 1j * rng.uniform(-1e-3, 1e-3, nk)
+    geh = MAT["gam_eh"] * 1.2
+    emission.InitializeEmission(g["kr"], d["Ee"], d["Eh"], abs(d["dcv"]), MAT["epsr"], geh,
+                                d["ehint"])
+    Rsp = np.zeros(nk)
+    emission.SpontEmission(ne, nh, d["Ee"], d["Eh"], d["gap"], geh, VC, Rsp)
+    return dict(kr=g["kr"], Ee=d["Ee"], Eh=d["Eh"], gap=d["gap"], dcv=d["dcv"],
+                ehint=d["ehint"], epsr=MAT["epsr"], geh=geh, VC=VC, ne=ne, nh=nh, Rsp=Rsp,
+                HOmega=emission._HOmega, square=emission._square, RScale=emission._RScale)
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -489,7 +509,11 @@ def main():
                         co = case_coulomb(nk, seed)
                         mb = case_mbc(nk, seed + 400, co["VC1_s1"])
                         np.savez_compressed(os.path.join(HERE, f"mbc_nk{nk}.npz"), **mb)
-                if only == "mbc":
+                    if only in (None, "emission"):
+                        co = case_coulomb(nk, seed)
+                        em = case_emission(nk, seed + 500, co["VC1_s1"])
+                        np.savez_compressed(os.path.join(HERE, f"emission_nk{nk}.npz"), **em)
+                if only in ("mbc", "emission"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

@@ -103,6 +103,17 @@ def test_carrier_scattering(nk, lorentz):
         assert rel(g[f"{name}0_l{lorentz}"] + mine, g[f"{name}_l{lorentz}"]) < TOL, name
 
 
+@pytest.mark.parametrize("nk", [8, 13])
+def test_spont_emission(nk):
+    """InitializeEmission tables and SpontEmission (Recomb)."""
+    g = golden(f"emission_nk{nk}")
+    et = O.emission_tables(abs(float(g["dcv"])), float(g["epsr"]), float(g["geh"]),
+                           float(g["ehint"]))
+    assert rel(et["HOmega"], g["HOmega"]) < TOL and rel(et["square"], g["square"]) < TOL
+    rsp = O.spont_emission(g["ne"], g["nh"], g["Ee"], g["Eh"], float(g["gap"]), g["VC"], et)
+    assert rel(rsp, g["Rsp"]) < TOL
+
+
 @pytest.mark.parametrize("nk", [8, 16, 30])
 def test_dephasing(nk):
     g = golden(f"dephasing_nk{nk}")
