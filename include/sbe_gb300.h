@@ -120,6 +120,11 @@ int sbe_offdiag(SbeCtx* ctx, int w, const double* ne, const double* nh, const do
 int sbe_phonon_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
                      const double* E1D, double* WinE, double* WoutE, double* WinH,
                      double* WoutH, void* stream);
+/* emission.py:94 SpontEmission (Recomb) with the tables of InitializeEmission
+ * (emission.py:35, the module's 77 K): Rsp (f64 Nk) at ne, nh (c128 Nk, real parts
+ * used) and VC (Nk*Nk*3).  The wire must have SBE_F_RECOMB.                    */
+int sbe_spont_emission(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
+                       double* Rsp, void* stream);
 /* coulomb.py:1298/1313 MBCE/MBCH (carrier-carrier scattering, EHs; tables of
  * CalcMBArrays, coulomb.py:367, evaluated on the fly, Lorentzian broadening with
  * SBE_F_LORENTZ in the wire's flags, else Gaussian): Win/Wout accumulated in place.

@@ -27,7 +27,7 @@ EXPORTS = (
     "sbe_last_error", "sbe_version", "sbe_constants", "sbe_ctx_create", "sbe_ctx_destroy",
     "sbe_ctx_layout", "sbe_ctx_table", "sbe_dpdt", "sbe_dCdt", "sbe_dDdt", "sbe_calch",
     "sbe_screened_arrays", "sbe_gamma", "sbe_offdiag", "sbe_phonon_rates", "sbe_carrier_rates",
-    "sbe_sources",
+    "sbe_spont_emission", "sbe_sources",
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
     "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
     "sbe_ctx_profile", "sbe_ctx_profile_read", "sbe_prop2qw_noalloc", "sbe_ctx_check",
@@ -97,6 +97,7 @@ def load(path=LIB_PATH):
         "sbe_offdiag": [P, I, P, P, P, P, P, P, P, P, P],
         "sbe_phonon_rates": [P, I, P, P, P, P, P, P, P, P, P],
         "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, I, P],
+        "sbe_spont_emission": [P, I, P, P, P, P, P],
         "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
         "sbe_prop2qw": [P, I, P, I, P, P, P],
         "sbe_prop2qw_noalloc": [P, I, P, I, P, P, P],

@@ -87,7 +87,7 @@ int sbe_constants(double* out5) {
   return SBE_OK;
 }
 
-static const int kUnsupportedFlags = SBE_F_DCTRANS | SBE_F_RECOMB | SBE_F_FREEPOT;
+static const int kUnsupportedFlags = SBE_F_DCTRANS | SBE_F_FREEPOT;
 
 int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out) {
   if (!wires || n_wires <= 0 || !out) return fail(SBE_ERR_ARG, "sbe_ctx_create: bad arguments");
@@ -109,7 +109,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
     if (d.flags & kUnsupportedFlags) {
       delete c;
       return fail(SBE_ERR_UNSUPPORTED,
-                  "sbe_ctx_create: DCTrans, Recomb and FreePot are not built (wire " +
+                  "sbe_ctx_create: DCTrans and FreePot are not built (wire " +
                       std::to_string(w) + ")");
     }
     WireDev W = derive(d);
@@ -174,6 +174,27 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   add((void**)&c->dC, C16 * om);
   add((void**)&c->dD, C16 * om);
   add((void**)&c->wrate, D8 * 4 * ov);
+  add((void**)&c->rsp, D8 * ov);
+  // emission tables (Recomb): InitializeEmission on the host, per wire
+  std::vector<double> emis_host;
+  for (auto& W : c->wires) {
+    W.emis_nw = 0;
+    W.emis_dhw = 0.0;
+    W.off_emis = (long long)emis_host.size();
+    if (!(W.flags & SBE_F_RECOMB)) continue;
+    int nwv = 0;
+    double dhw = 0.0;
+    std::vector<double> t = emission_table(W, &nwv, &dhw);
+    if (nwv < 10) {
+      delete c;
+      return fail(SBE_ERR_ARG, "sbe_ctx_create: temperature too low for the emission grid "
+                               "(emission.py CalcHOmega)");
+    }
+    W.emis_nw = nwv;
+    W.emis_dhw = dhw;
+    emis_host.insert(emis_host.end(), t.begin(), t.end());
+  }
+  add((void**)&c->emis, D8 * std::max<size_t>(emis_host.size(), 1));
   add((void**)&c->G, C16 * 3 * okr);
   add((void**)&c->kacc, C16 * 3 * om);
   add((void**)&c->xs, C16 * 3 * om);
@@ -206,6 +227,11 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   }
   cudaMemcpyAsync(c->d_wires, c->wires.data(), sizeof(WireDev) * n_wires, cudaMemcpyHostToDevice,
                   s);
+  if (!emis_host.empty()) {
+    cudaMemcpyAsync(c->emis, emis_host.data(), sizeof(double) * emis_host.size(),
+                    cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);   // the host vector is released at the end of this call
+  }
   // dephasing groups: wires whose Lorentzian factors coincide (same Nk, masses, grid
   // spacing and broadening rates) share them in the FP32 dephasing sums
   {
@@ -492,6 +518,24 @@ int sbe_phonon_rates(SbeCtx* c, int w, const double* ne, const double* nh, const
   // accumulate into the caller's arrays (MBPE/MBPH add to Win/Wout)
   sbe::add_rates(c->wrate + 4 * W.off_vec, W.nk, WinE, WoutE, WinH, WoutH, s);
   return cuda_check(cudaGetLastError(), "sbe_phonon_rates");
+}
+
+int sbe_spont_emission(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
+                       double* Rsp, void* stream) {
+  int rc = check_w(c, w, "sbe_spont_emission");
+  if (rc) return rc;
+  if (!ne || !nh || !VC || !Rsp) return fail(SBE_ERR_ARG, "sbe_spont_emission: null pointer");
+  const WireDev& W = c->wires[w];
+  if (!(W.flags & SBE_F_RECOMB))
+    return fail(SBE_ERR_ARG, "sbe_spont_emission: the wire was created without Recomb "
+                             "(no emission tables)");
+  cudaStream_t s = as_stream(stream);
+  copy_in(c->ne + W.off_vec, ne, 16 * W.nk, s);
+  copy_in(c->nh + W.off_vec, nh, 16 * W.nk, s);
+  set_vc(c, w, VC, nullptr, s);
+  launch_spont(c, w, s);
+  copy_in(Rsp, c->rsp + W.off_vec, 8 * W.nk, s);
+  return cuda_check(cudaGetLastError(), "sbe_spont_emission");
 }
 
 int sbe_carrier_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,

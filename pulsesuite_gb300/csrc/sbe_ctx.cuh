@@ -1,5 +1,6 @@
 // Host-side context of libsbe_gb300: per-wire descriptors and the device arena.
 #pragma once
+#include <vector>
 #include <functional>
 
 #include "sbe_internal.cuh"
@@ -41,6 +42,8 @@ struct SbeCtx {
   double2* tr = nullptr;                 // 4*tot_vec diagonal traces (C, D) per wire [2][2nk]
   double2 *dP = nullptr, *dC = nullptr, *dD = nullptr;     // tot_mat
   double* wrate = nullptr;               // 4*tot_vec Win/Wout e/h
+  double* rsp = nullptr;                 // tot_vec spontaneous emission rates (Recomb)
+  double* emis = nullptr;                // emission tables (per wire emis_nw values)
   double2* G = nullptr;                  // 3*tot_kr source GEMM outputs
   double2* kacc = nullptr;               // 3*tot_mat RK4 accumulator
   double2* xs = nullptr;                 // 3*tot_mat RK4 stage state
@@ -153,6 +156,10 @@ void launch_sources(SbeCtx* c, const double2* P, const double2* C, const double2
 void launch_extract_diag(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s);
 void launch_screen(SbeCtx* c, int w_only, cudaStream_t s);
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s);
+// sbe_emission.cu: spontaneous emission rates (Recomb) of the prepared occupations
+void launch_spont(SbeCtx* c, int w_only, cudaStream_t s);
+// the InitializeEmission table of one wire (host, FP64): nw values, spacing dhw
+std::vector<double> emission_table(const WireDev& W, int* nw, double* dhw);
 // sbe_mbc.cu: carrier-carrier scattering rates (EHs) added to wrate
 void launch_mbc_rates(SbeCtx* c, int w_only, cudaStream_t s, bool all = false,
                       bool fp32 = false);

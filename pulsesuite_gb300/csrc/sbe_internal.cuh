@@ -40,6 +40,11 @@ struct WireDev {
   // term -ehint Xcv of Heh as the x, y, z weights ed_x (odd k; even k: -ed_x),
   // ed_y, ed_z
   float ed_x, ed_y, ed_z, padf;
+  // spontaneous emission (Recomb): photon-energy grid of InitializeEmission
+  // (emis_nw midpoints, spacing emis_dhw) and its table at off_emis
+  int emis_nw, pad3;
+  double emis_dhw;
+  long long off_emis;
 };
 
 struct SbeCtxImpl;

@@ -65,6 +65,7 @@ void launch_screen(SbeCtx* c, int w_only, cudaStream_t s) {
 void launch_prep_scalar(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
   launch_extract_diag(c, C, D, s);
   launch_screen(c, -1, s);
+  launch_spont(c, -1, s);   // Recomb: SBEs.py:5203-5226
 }
 
 // Expand to the reference's (Nk, Nk, 3) VC and (Nk, Nk) E1D of wire w.

@@ -94,8 +94,15 @@ __global__ void k_phonon_rates(const WireDev* wires, int w_only, const double2* 
 // in/out rates, then the charge normalisation ne = |C_kk| scaled to the common
 // mean.  One block per wire.  The normalised occupations are left in ne/nh for
 // the sources.
+__device__ __forceinline__ double2 cexp_d(double2 z) {
+  const double m = exp(z.x);
+  double sn, cs;
+  sincos(z.y, &sn, &cs);
+  return make_double2(m * cs, m * sn);
+}
+
 __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, const double* wrate,
-                             double dt, double2* ne_out, double2* nh_out) {
+                             const double* rsp, double dt, double2* ne_out, double2* nh_out) {
   const WireDev W = wires[blockIdx.x];
   const int nk = W.nk;
   const bool relax = (W.flags & (SBE_F_PHONON | SBE_F_EHS)) != 0;
@@ -115,6 +122,13 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
                         ee * (ne.y * wie + ne.y * woe) / den_e);
       nh = make_double2(he * ((-1 + hp + nh.x) * wih + nh.x * woh) / den_h,
                         he * (nh.y * wih + nh.y * woh) / den_h);
+    }
+    if (W.flags & SBE_F_RECOMB) {
+      // SBEs.py:5322-5325: ne exp(-Rsp nh dt), then nh exp(-Rsp ne dt) with the new ne
+      // (complex occupations, complex exponential)
+      const double r = rsp[W.off_vec + k];
+      ne = cmul(ne, cexp_d(make_double2(-r * nh.x * dt, -r * nh.y * dt)));
+      nh = cmul(nh, cexp_d(make_double2(-r * ne.x * dt, -r * ne.y * dt)));
     }
     double ae = hypot(ne.x, ne.y), ah = hypot(nh.x, nh.y);
     ne_out[W.off_vec + k] = make_double2(ae, 0.0);
@@ -152,12 +166,14 @@ void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_
   k_phonon_rates<<<dim3(c->nk_max, c->nw), 128, 0, s>>>(c->d_wires, -1, c->ne, c->nh, c->vs,
                                                         c->eps, c->EP, c->HP, c->wrate);
   launch_mbc_rates(c, -1, s);
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, dt, c->ne, c->nh);
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne,
+                                     c->nh);
 }
 
 // the relaxation/normalisation kernel alone (rates already in c->wrate)
 void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s) {
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, dt, c->ne, c->nh);
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne,
+                                     c->nh);
 }
 
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s) {

@@ -224,6 +224,14 @@ class WireContext:
                                               _lib.ptr(WinH), _lib.ptr(WoutH), prec,
                                               _lib.stream_handle()), "sbe_carrier_rates")
 
+    def spont_emission(self, w, ne, nh, VC):
+        """emission.py:94 SpontEmission: Rsp of wire w (needs Recomb in its flags)."""
+        rsp = torch.empty(self.nk[w], dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_spont_emission(self.handle, w, _lib.ptr(ne), _lib.ptr(nh),
+                                               _lib.ptr(VC), _lib.ptr(rsp),
+                                               _lib.stream_handle()), "sbe_spont_emission")
+        return rsp
+
     def sources(self, w, P, C, D, ne, nh):
         nr = 2 * self.nk[w] + 2
         out = [torch.empty(nr, dtype=CDTYPE, device=self.device) for _ in range(5)]

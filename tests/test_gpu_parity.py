@@ -314,3 +314,42 @@ def test_rk4_with_carrier_scattering_vs_oracle(lorentz):
         assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
         assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
         assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
+
+
+@pytest.mark.parametrize("nk", [8, 13])
+def test_spont_emission_vs_golden(nk):
+    """SpontEmission (Recomb) through sbe_spont_emission against the reference's Rsp."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    g = golden(f"emission_nk{nk}")
+    L = np.pi / (g["kr"][1] - g["kr"][0])
+    mat = dict(MAT, gam_eh=float(g["geh"]))
+    c = WireContext([WireSpec(nk=nk, L=L, wire_index=1, flags=dict(ALL, Recomb=True), **mat)])
+    rsp = c.spont_emission(0, dev(g["ne"]), dev(g["nh"]), dev(g["VC"]))
+    assert rel(host(rsp), g["Rsp"]) < TIGHT
+
+
+def test_rk4_with_recombination_vs_oracle():
+    """One RK4 step with Recomb (and EHs) on, FP64 path, against the oracle."""
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    nw = 2
+    flags = dict(ALL, Recomb=True, EHs=True)
+    c = ctx_for(nk, L, nw=nw, flags=flags)
+    rng = np.random.default_rng(13)
+    wires = [O.Wire(nk, L, MAT, flags) for _ in range(nw)]
+    states = [_seeded_state(rng, nk) for _ in range(nw)]
+    fields = [_uniform_field_k(wires[w], 1e7 * (w + 1)) for w in range(nw)]
+    dfields = [_uniform_field_k(wires[w], -3e5 * (w + 1)) for w in range(nw)]
+    P = c.pack([s[0] for s in states])
+    C = c.pack([s[1] for s in states])
+    D = c.pack([s[2] for s in states])
+    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
+    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    dt = 0.1e-15
+    src = c.zeros_r(5)
+    c.rk4_step(P, C, D, Ek, dEk, dt, src)
+    for w in range(nw):
+        ref = wires[w].rk4_step(*states[w], fields[w], dfields[w], dt, w + 1)
+        assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
+        assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
+        assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
