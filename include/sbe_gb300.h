@@ -63,6 +63,8 @@ typedef struct {
   double epsr;       /* background dielectric constant                         */
   double Oph, Gph;   /* LO phonon frequency and damping (rad/s)                */
   double temp;       /* lattice temperature (K) (phonons.py:22)                */
+  double Edc;        /* DC field along the wire (V/m), qw.params (SBEs.py:1317);
+                        used by DC transport (SBE_F_DCTRANS)                   */
 } SbeWireDesc;
 
 typedef struct SbeCtx SbeCtx;

@@ -995,6 +995,30 @@ def mbch(ne0, nh0, VC, mb):
     return win, wout
 
 
+def dc_karray(nk, dky):
+    """dcfield.py:39-58 GetKArray(Nk, (Nk - 1) dky) of DCFieldModule (:778)."""
+    L = (nk - 1) * dky
+    dk = 2.0 * PI / L if L > 0 else 1.0
+    k = np.arange(nk, dtype=float) * dk
+    return k - k[nk // 2]
+
+
+def dc_transport(X, Edc, Eac, dt, dky, lf):
+    """dcfield.py:1154-1236 ShiftN1D / ShiftN2D / Transport (DCTrans on): returns the
+    shifted matrix (LF: the whole matrix; else the diagonal alone)."""
+    dk = -E0 * (Edc + Eac) / HBAR * dt
+    Y = dc_karray(X.shape[0], dky)
+    if lf:
+        F = np.fft.fft2(X)
+        F = F * np.exp(-1j * (Y[:, None] + Y[None, :]) * dk)
+        return np.fft.ifft2(F)
+    d = np.fft.fft(np.diag(X).copy())
+    d = d * np.exp(-1j * Y * dk)
+    out = X.copy()
+    np.fill_diagonal(out, np.fft.ifft(d))
+    return out
+
+
 EMISSION_TEMP = 77.0   # emission.py:28 _Temp: the module's own temperature, never set by SBEs.py
 
 
@@ -1183,11 +1207,17 @@ class Wire:
         k4 = f_rhs(*[x + dt * k for x, k in zip(X, k3)], 1.0)
         P, C, D = [x + dt / 6.0 * (a + 2.0 * b + 2.0 * cc + d)
                    for x, a, b, cc, d in zip(X, k1, k2, k3, k4)]
-        if f["EHs"] or f["Phonon"] or f.get("Recomb", False):
+        if f["EHs"] or f["Phonon"]:   # SBEs.py:5677 (the Recomb decay is inside)
             ne3, nh3 = relax(np.diag(C).copy(), np.diag(D).copy(), VC, E1D, self.pt, dt,
                              f["EHs"], f["Phonon"], mb=self.mb, rsp=Rsp)
             C[np.diag_indices(nk)] = ne3
             D[np.diag_indices(nk)] = nh3
+        if f.get("DCTrans", False):
+            # SBEs.py:5686-5690 with the step-start field (q = 0 at index 0)
+            eac = np.real(Ek0[0][0])
+            dky = g["kr"][2] - g["kr"][1]
+            C, D, P = [dc_transport(X, prm.get("Edc", 0.0), eac, dt, dky, f["LF"])
+                       for X in (C, D, P)]
         ne3 = np.abs(np.diag(C)).astype(complex)
         nh3 = np.abs(np.diag(D)).astype(complex)
         total = (np.sum(np.abs(ne3)) + np.sum(np.abs(nh3))) / 2.0
@@ -1244,11 +1274,17 @@ class Solver:
         C3 = C1 + dC * dt * 2.0
         D3 = D1 + dD * dt * 2.0
         p3 = p1 + dP * dt * 2.0
-        if f["EHs"] or f["Phonon"] or f.get("Recomb", False):
+        if f["EHs"] or f["Phonon"]:   # SBEs.py:5677 (the Recomb decay is inside)
             ne3, nh3 = relax(np.diag(C3).copy(), np.diag(D3).copy(), pr["VC"], pr["E1D"],
                              wi.pt, dt, f["EHs"], f["Phonon"], mb=wi.mb, rsp=pr["Rsp"])
             C3[np.diag_indices(g["nk"])] = ne3
             D3[np.diag_indices(g["nk"])] = nh3
+        if f.get("DCTrans", False):
+            # SBEs.py:5686-5690
+            eac = np.real(Ex[g["NQ0"]])
+            dky = g["kr"][2] - g["kr"][1]
+            C3, D3, p3 = [dc_transport(X, wi.p.get("Edc", 0.0), eac, dt, dky, f["LF"])
+                          for X in (C3, D3, p3)]
         ne3 = np.abs(np.diag(C3)).astype(complex)
         nh3 = np.abs(np.diag(D3)).astype(complex)
         total = (np.sum(np.abs(ne3)) + np.sum(np.abs(nh3))) / 2.0

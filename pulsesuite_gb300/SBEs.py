@@ -171,7 +171,8 @@ class SBESolver:
             spec = WireSpec(nk=nk, L=self.L, Delta0=self.Delta0, gap=self.gap, me=self.me,
                             mh=self.mh, HO=self.HO, gam_e=self.gam_e, gam_h=self.gam_h,
                             gam_eh=self.gam_eh, epsr=self.epsr, Oph=self.Oph, Gph=self.Gph,
-                            temp=temp, wire_index=w, flags=cflags)
+                            temp=temp, Edc=float(getattr(self, "Edc", 0.0)), wire_index=w,
+                            flags=cflags)
             self.contexts.append(WireContext([spec]))
         c0 = self.contexts[0]
         self.kr = c0.table(0, "kr").cpu().numpy()

@@ -46,7 +46,7 @@ class SbeWireDesc(ctypes.Structure):
                 ("gap", ctypes.c_double), ("me", ctypes.c_double), ("mh", ctypes.c_double),
                 ("HO", ctypes.c_double), ("gam_e", ctypes.c_double), ("gam_h", ctypes.c_double),
                 ("gam_eh", ctypes.c_double), ("epsr", ctypes.c_double), ("Oph", ctypes.c_double),
-                ("Gph", ctypes.c_double), ("temp", ctypes.c_double)]
+                ("Gph", ctypes.c_double), ("temp", ctypes.c_double), ("Edc", ctypes.c_double)]
 
 
 class SbePstdDesc(ctypes.Structure):

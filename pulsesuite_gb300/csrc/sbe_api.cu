@@ -48,6 +48,7 @@ static WireDev derive(const SbeWireDesc& d, int nk_check_only = 0) {
   W.Oph = d.Oph;
   W.Gph = d.Gph;
   W.temp = d.temp;
+  W.Edc = d.Edc;
   W.dcv = std::sqrt((kE0 * kHbar) * (kE0 * kHbar) / (6.0 * kMe0 * d.gap) * (kMe0 / d.me - 1.0));
   W.alphae = std::sqrt(d.me * d.HO) / kHbar;
   W.alphah = std::sqrt(d.mh * d.HO) / kHbar;
@@ -87,7 +88,7 @@ int sbe_constants(double* out5) {
   return SBE_OK;
 }
 
-static const int kUnsupportedFlags = SBE_F_DCTRANS | SBE_F_FREEPOT;
+static const int kUnsupportedFlags = SBE_F_FREEPOT;
 
 int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out) {
   if (!wires || n_wires <= 0 || !out) return fail(SBE_ERR_ARG, "sbe_ctx_create: bad arguments");
@@ -109,7 +110,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
     if (d.flags & kUnsupportedFlags) {
       delete c;
       return fail(SBE_ERR_UNSUPPORTED,
-                  "sbe_ctx_create: DCTrans and FreePot are not built (wire " +
+                  "sbe_ctx_create: FreePot is not built (wire " +
                       std::to_string(w) + ")");
     }
     WireDev W = derive(d);
@@ -175,6 +176,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   add((void**)&c->dD, C16 * om);
   add((void**)&c->wrate, D8 * 4 * ov);
   add((void**)&c->rsp, D8 * ov);
+  add((void**)&c->dcs, C16 * ov);
   // emission tables (Recomb): InitializeEmission on the host, per wire
   std::vector<double> emis_host;
   for (auto& W : c->wires) {
@@ -649,7 +651,7 @@ int sbe_leapfrog_step(SbeCtx* c, double* const* state9, const double* Ek, double
   prep_frozen(c, st[2], st[5], st[8], s);
   launch_calch_ctx(c, st[2], st[5], st[8], (const double2*)Ek, s);
   launch_rhs64_ctx(c, st[2], st[5], st[8], c->dP, c->dC, c->dD, s);
-  launch_leapfrog(c, st, dt, s);
+  launch_leapfrog(c, st, (const double2*)Ek, dt, s);
   launch_sources(c, st[0], st[3], st[6], c->ne, c->nh, (double2*)src_out, s);
   launch_leap_shuffle(c, st, s);
   return cuda_check(cudaGetLastError(), "sbe_leapfrog_step");
@@ -680,7 +682,7 @@ int sbe_rk4_step(SbeCtx* c, double* P, double* C, double* D, const double* Ek0, 
     launch_rhs64_ctx(c, xp, xc, xd, c->dP, c->dC, c->dD, s);
     launch_rk4_axpy(c, st, dt, p, cc, d, s);
   }
-  launch_relax_norm(c, cc, d, dt, false, s);
+  launch_relax_norm(c, p, cc, d, (const double2*)Ek0, dt, s);
   launch_sources(c, p, cc, d, c->ne, c->nh, (double2*)src_out, s);
   return cuda_check(cudaGetLastError(), "sbe_rk4_step");
 }

@@ -43,6 +43,7 @@ struct SbeCtx {
   double2 *dP = nullptr, *dC = nullptr, *dD = nullptr;     // tot_mat
   double* wrate = nullptr;               // 4*tot_vec Win/Wout e/h
   double* rsp = nullptr;                 // tot_vec spontaneous emission rates (Recomb)
+  double2* dcs = nullptr;                // tot_vec DC transport shift kernel s(m) per wire
   double* emis = nullptr;                // emission tables (per wire emis_nw values)
   double2* G = nullptr;                  // 3*tot_kr source GEMM outputs
   double2* kacc = nullptr;               // 3*tot_mat RK4 accumulator
@@ -147,9 +148,12 @@ void launch_sources_gemm64(SbeCtx* c, const GemmBatch& b, cudaStream_t s);
 void launch_rhs64_ctx(SbeCtx* c, const double2* P, const double2* C, const double2* D,
                       double2* dP, double2* dC, double2* dD, cudaStream_t s);
 // sbe_step.cu
-void launch_leapfrog(SbeCtx* c, double2* const* st9, double dt, cudaStream_t s);
-void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_scheme,
-                       cudaStream_t s);
+void launch_leapfrog(SbeCtx* c, double2* const* st9, const double2* Ek, double dt,
+                     cudaStream_t s);
+// relaxation (rates in wrate, Recomb decay), DC transport of P, C, D (SBE_F_DCTRANS,
+// field Ek at q = 0) and charge normalisation, in the reference's order
+void launch_relax_norm(SbeCtx* c, double2* P3, double2* C3, double2* D3, const double2* Ek,
+                       double dt, cudaStream_t s);
 void launch_sources(SbeCtx* c, const double2* P, const double2* C, const double2* D,
                     const double2* ne, const double2* nh, double2* src, cudaStream_t s,
                     int w_only = -1);
@@ -174,7 +178,12 @@ void launch_sources_reduce(SbeCtx* c, const double2* ne, const double2* nh, doub
                            cudaStream_t s);
 void launch_sources_final(SbeCtx* c, const double2* ne, const double2* nh, double2* src,
                           cudaStream_t s);
-void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s);
+void launch_relax_only(SbeCtx* c, double2* P3, double2* C3, double2* D3, const double2* Ek,
+                       double dt, cudaStream_t s);
+// sbe_dc.cu: DC transport (dcfield.py:1154-1236 Transport) of P, C, D
+bool any_dc(const SbeCtx* c);
+void launch_dc_transport(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek,
+                         double dt, cudaStream_t s);
 int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
               const double2* dEk, double dt, double2* src, cudaStream_t s);
 void launch_rk4_axpy(SbeCtx* c, int stage, double dt, double2* P, double2* C, double2* D,

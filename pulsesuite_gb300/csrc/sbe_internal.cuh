@@ -31,7 +31,7 @@ struct WireDev {
   int dnk, pad;
   long long off_mat, off_vec, off_r, off_dd, off_kr, off_tab;  // off_tab: shared-table set
   double L, dkr, dr_grid, Delta0, gap, me, mh, HO;
-  double gam_e, gam_h, gam_eh, epsr, Oph, Gph, temp;
+  double gam_e, gam_h, gam_eh, epsr, Oph, Gph, temp, Edc;
   double dcv, alphae, alphah, ehint, area, qc;
   double vscale, n0ph, nmax;   // phonon Vscale, Bose N0, screening clamp
   double pol_scale;            // 2 ehint / (area L)

@@ -101,11 +101,17 @@ __device__ __forceinline__ double2 cexp_d(double2 z) {
   return make_double2(m * cs, m * sn);
 }
 
+// mode 0: relaxation and normalisation; 1: relaxation only (the relaxed complex
+// diagonals back into C3, D3); 2: normalisation only.
 __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, const double* wrate,
-                             const double* rsp, double dt, double2* ne_out, double2* nh_out) {
+                             const double* rsp, double dt, double2* ne_out, double2* nh_out,
+                             int mode) {
   const WireDev W = wires[blockIdx.x];
   const int nk = W.nk;
-  const bool relax = (W.flags & (SBE_F_PHONON | SBE_F_EHS)) != 0;
+  const bool relax = mode != 2 && (W.flags & (SBE_F_PHONON | SBE_F_EHS)) != 0;
+  // the decay is part of the relaxation, which runs only with Phonon or EHs
+  // (SBEs.py:5677, 5322)
+  const bool recomb = relax && (W.flags & SBE_F_RECOMB) != 0;
   __shared__ double red[2][256];
   double se = 0.0, sh = 0.0;
   for (int k = threadIdx.x; k < nk; k += blockDim.x) {
@@ -123,12 +129,17 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
       nh = make_double2(he * ((-1 + hp + nh.x) * wih + nh.x * woh) / den_h,
                         he * (nh.y * wih + nh.y * woh) / den_h);
     }
-    if (W.flags & SBE_F_RECOMB) {
+    if (recomb) {
       // SBEs.py:5322-5325: ne exp(-Rsp nh dt), then nh exp(-Rsp ne dt) with the new ne
       // (complex occupations, complex exponential)
       const double r = rsp[W.off_vec + k];
       ne = cmul(ne, cexp_d(make_double2(-r * nh.x * dt, -r * nh.y * dt)));
       nh = cmul(nh, cexp_d(make_double2(-r * ne.x * dt, -r * ne.y * dt)));
+    }
+    if (mode == 1) {
+      C3[o] = ne;
+      D3[o] = nh;
+      continue;
     }
     double ae = hypot(ne.x, ne.y), ah = hypot(nh.x, nh.y);
     ne_out[W.off_vec + k] = make_double2(ae, 0.0);
@@ -136,6 +147,7 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
     se += ae;
     sh += ah;
   }
+  if (mode == 1) return;   // block-uniform
   red[0][threadIdx.x] = se;
   red[1][threadIdx.x] = sh;
   __syncthreads();
@@ -159,21 +171,27 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
   }
 }
 
-void launch_relax_norm(SbeCtx* c, double2* C3, double2* D3, double dt, bool ref_scheme,
-                       cudaStream_t s) {
-  (void)ref_scheme;
+void launch_relax_norm(SbeCtx* c, double2* P3, double2* C3, double2* D3, const double2* Ek,
+                       double dt, cudaStream_t s) {
   launch_extract_diag(c, C3, D3, s);
   k_phonon_rates<<<dim3(c->nk_max, c->nw), 128, 0, s>>>(c->d_wires, -1, c->ne, c->nh, c->vs,
                                                         c->eps, c->EP, c->HP, c->wrate);
   launch_mbc_rates(c, -1, s);
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne,
-                                     c->nh);
+  launch_relax_only(c, P3, C3, D3, Ek, dt, s);
 }
 
-// the relaxation/normalisation kernel alone (rates already in c->wrate)
-void launch_relax_only(SbeCtx* c, double2* C3, double2* D3, double dt, cudaStream_t s) {
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne,
-                                     c->nh);
+// relaxation (rates already in c->wrate), DC transport and normalisation
+// (SBEs.py:5677-5702: relaxation, Transport of C3, D3, p3, charge normalisation)
+void launch_relax_only(SbeCtx* c, double2* P3, double2* C3, double2* D3, const double2* Ek,
+                       double dt, cudaStream_t s) {
+  if (!any_dc(c)) {
+    k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh,
+                                       0);
+    return;
+  }
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh, 1);
+  launch_dc_transport(c, P3, C3, D3, Ek, dt, s);
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh, 2);
 }
 
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s) {
@@ -181,13 +199,14 @@ void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s) {
                                                          c->eps, c->EP, c->HP, c->wrate);
 }
 
-void launch_leapfrog(SbeCtx* c, double2* const* st, double dt, cudaStream_t s) {
+void launch_leapfrog(SbeCtx* c, double2* const* st, const double2* Ek, double dt,
+                     cudaStream_t s) {
   // st: YY1, YY2, YY3, CC1, CC2, CC3, DD1, DD2, DD3
   int blocks = (int)std::min<long long>(((long long)c->nk_max * c->nk_max + 255) / 256, 4096);
   dim3 g(blocks, c->nw);
   k_leap_update<<<g, 256, 0, s>>>(c->d_wires, st[0], st[1], c->dP, st[3], st[4], c->dC, st[6],
                                   st[7], c->dD, dt);
-  launch_relax_norm(c, st[3], st[6], dt, true, s);
+  launch_relax_norm(c, st[0], st[3], st[6], Ek, dt, s);
 }
 
 void launch_leap_shuffle(SbeCtx* c, double2* const* st, cudaStream_t s) {

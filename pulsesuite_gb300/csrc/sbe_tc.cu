@@ -427,6 +427,12 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
       return fail(SBE_ERR_UNSUPPORTED,
                   "mixed path: all wires of a context must share Nk and flags (group by Nk)");
   if (nk % 8) return fail(SBE_ERR_UNSUPPORTED, "mixed path: Nk must be a multiple of 8");
+  // the operand planes take C^T = conj C, D^T = conj D; the reference's DC transport
+  // (dcfield.py:1196-1206: the centred Y against the FFT's natural order) leaves C, D
+  // non-Hermitian, so DCTrans runs on the FP64 path only
+  if (any_dc(c))
+    return fail(SBE_ERR_UNSUPPORTED,
+                "mixed path: DCTrans leaves C and D non-Hermitian; use the FP64 path");
   Mixed* m = new Mixed();
   m->nk = nk;
   m->nw = nw;
@@ -1536,14 +1542,15 @@ static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_
 
 // Relaxation (phonon in/out rates of the new occupations, FP32 sums) and charge
 // normalisation after the step (SBEs.py:5677-5702), then the state maximum.
-static void mixed_relax(SbeCtx* c, double2* C, double2* D, double dt, cudaStream_t s) {
+static void mixed_relax(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek,
+                        double dt, cudaStream_t s) {
   Mixed* m = static_cast<Mixed*>(c->mixed);
   const int nk = m->nk, nw = m->nw;
   launch_extract_diag(c, C, D, s);
   k_phonon_rates_f<<<dim3(nk, nw), 128, sizeof(float) * 2 * nk, s>>>(
       c->d_wires, c->ne, c->nh, m->phf, m->epf, m->eptf, m->hpf, m->hptf, c->wrate, nw);
   launch_mbc_rates(c, -1, s, false, true);
-  launch_relax_only(c, C, D, dt, s);
+  launch_relax_only(c, P, C, D, Ek, dt, s);
   k_diag_max<<<nw, 256, 0, s>>>(c->d_wires, C, D, m->mxS());
 }
 
@@ -1814,8 +1821,9 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
                      (float)dt, X64, s);
     if (rc) return rc;
   }
-  mixed_relax(c, C, D, dt, s);   // the new diagonals join the maximum
-  return mixed_sources(c, P, C, D, src, 1, s);
+  mixed_relax(c, P, C, D, Ek0, dt, s);   // the new diagonals join the maximum
+  // DC transport moves every element: the sources then measure the maximum themselves
+  return mixed_sources(c, P, C, D, src, any_dc(c) ? 0 : 1, s);
 }
 
 }  // namespace sbe

@@ -36,6 +36,7 @@ class WireSpec:
     Oph: float = 36e-3 * E0 / HBAR
     Gph: float = 3e-3 * E0 / HBAR
     temp: float = 77.0
+    Edc: float = 0.0
     wire_index: int = 1
     flags: dict = field(default_factory=lambda: dict(
         Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DCTrans=False,
@@ -56,7 +57,7 @@ class WireSpec:
         return _lib.SbeWireDesc(self.nk, self.wire_index, self.flag_bits(), 0, self.L,
                                 self.Delta0, self.gap, self.me, self.mh, self.HO, self.gam_e,
                                 self.gam_h, self.gam_eh, self.epsr, self.Oph, self.Gph,
-                                self.temp)
+                                self.temp, self.Edc)
 
 
 class RK4Graph:

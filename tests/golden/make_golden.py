@@ -24,6 +24,8 @@ mbc_nkN         ``coulomb.CoulombModule`` carrier-carrier scattering ``MBCE``/``
                 broadening.  ``make_golden.py <src> mbc`` writes these alone.
 emission_nkN    ``emission.InitializeEmission`` tables and ``SpontEmission`` (Recomb);
                 ``make_golden.py <src> emission`` writes these alone.
+dc_nkN          ``dcfield.DCFieldModule.Transport`` (DCTrans) of a matrix with and
+                without LF; ``make_golden.py <src> dc`` writes these alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
                 ``OffDiagDephasing2``.
 qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
@@ -286,6 +288,22 @@ def case_emission(nk, seed, VC):
                 HOmega=emission._HOmega, square=emission._square, RScale=emission._RScale)
 
 
+def case_dc(nk, seed):
+    """dcfield.DCFieldModule.Transport (DCTrans) with and without LF."""
+    from pulsesuite.PSTD3D import dcfield
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    dm = dcfield.DCFieldModule(g["kr"], d["me"], d["mh"], datadir=None)
+    out = dict(kr=g["kr"], Edc=3.0e5, Eac=-1.2e5, dt=0.5e-15, Y=dm.Y)
+    for lf in (0, 1):
+        C = herm_state(rng, nk, 0.3) + cnormal(rng, (nk, nk), 1e-3)
+        out[f"C_in_l{lf}"] = C.copy()
+        dm.Transport(C, out["Edc"], out["Eac"], out["dt"], True, bool(lf))
+        out[f"C_out_l{lf}"] = C
+    return out
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -513,7 +531,10 @@ def main():
                         co = case_coulomb(nk, seed)
                         em = case_emission(nk, seed + 500, co["VC1_s1"])
                         np.savez_compressed(os.path.join(HERE, f"emission_nk{nk}.npz"), **em)
-                if only in ("mbc", "emission"):
+                    if only in (None, "dc"):
+                        np.savez_compressed(os.path.join(HERE, f"dc_nk{nk}.npz"),
+                                            **case_dc(nk, seed + 600))
+                if only in ("mbc", "emission", "dc"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

@@ -29,11 +29,11 @@ ALL = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, DC
            LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 
 
-def make_ctx(nk, nw, temp=300.0, flags=None):
+def make_ctx(nk, nw, temp=300.0, flags=None, edc=0.0):
     from pulsesuite_gb300.wires import WireContext, WireSpec
     L = np.pi / (3e9 / (nk / 2 - 0.5))
-    specs = [WireSpec(nk=nk, L=L, temp=temp, wire_index=w + 1, flags=dict(flags or ALL), **MAT)
-             for w in range(nw)]
+    specs = [WireSpec(nk=nk, L=L, temp=temp, wire_index=w + 1, flags=dict(flags or ALL),
+                      Edc=edc, **MAT) for w in range(nw)]
     return WireContext(specs), L
 
 
@@ -109,6 +109,27 @@ def test_graph_replay_matches_direct_step(prec):
     for a, b in zip(*outs):
         assert torch.isfinite(a).all()
         assert torch.equal(a, b)
+
+
+def test_mixed_rejects_dc_transport():
+    """DCTrans leaves C and D non-Hermitian (the reference's shift pairs the centred
+    k array with the FFT's natural order); the mixed path's operands assume Hermitian
+    C and D, so it refuses such a context and the FP64 path still steps it."""
+    from pulsesuite_gb300 import _lib
+    nk, nw = 64, 2
+    ctx, _ = make_ctx(nk, nw, flags=dict(ALL, DCTrans=True), edc=5e7)
+    st = [seeded(np.random.default_rng(4), nk, 1e-4) for _ in range(nw)]
+    P = ctx.pack([s[0] for s in st])
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    Ek = fields(ctx, [1e7, 2e7])
+    src = ctx.zeros_r(5)
+    with pytest.raises(_lib.SbeError, match="DCTrans"):
+        ctx.rk4_step(P, C, D, Ek, Ek * 0, 0.1e-15, src, _lib.PREC_MIXED)
+    C0 = C.clone()
+    ctx.rk4_step(P, C, D, Ek, Ek * 0, 0.1e-15, src, _lib.PREC_FP64)
+    ctx.check()
+    assert torch.isfinite(C).all() and not torch.equal(C, C0)
 
 
 @pytest.mark.parametrize("nk,ehs", [(64, False), (128, False), (64, True)])

@@ -353,3 +353,80 @@ def test_rk4_with_recombination_vs_oracle():
         assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
         assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
         assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
+
+
+@pytest.mark.parametrize("lf", [True, False])
+def test_rk4_with_dc_transport_vs_oracle(lf):
+    """One RK4 step with DCTrans on (the shift of P, C, D after the relaxation; with LF
+    off only the diagonals), FP64 path, against the oracle.  LF off also runs Recomb
+    without Phonon or EHs: no relaxation, so no decay."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    nw = 2
+    flags = dict(ALL, DCTrans=True, LF=lf)
+    if not lf:
+        flags.update(Phonon=False, EHs=False, Recomb=True)
+    edc = [4e7, -2.5e7]
+    c = WireContext([WireSpec(nk=nk, L=L, temp=77.0, wire_index=w + 1, flags=dict(flags),
+                              Edc=edc[w], **MAT) for w in range(nw)])
+    rng = np.random.default_rng(17)
+    wires = [O.Wire(nk, L, dict(MAT, Edc=edc[w]), flags) for w in range(nw)]
+    states = [_seeded_state(rng, nk) for _ in range(nw)]
+
+    def fld(w, ex, ey):
+        wk = O.fftg(wires[w].window)
+        return [ex * wk, ey * wk, np.zeros_like(wk)]
+
+    fields = [fld(w, 3e7 * (w + 1), 1e7) for w in range(nw)]
+    dfields = [fld(w, -2e5, 3e5) for w in range(nw)]
+    P = c.pack([s[0] for s in states])
+    C = c.pack([s[1] for s in states])
+    D = c.pack([s[2] for s in states])
+    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
+    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    dt = 0.1e-15
+    src = c.zeros_r(5)
+    c.rk4_step(P, C, D, Ek, dEk, dt, src)
+    for w in range(nw):
+        ref = wires[w].rk4_step(*states[w], fields[w], dfields[w], dt, w + 1)
+        nodc = O.Wire(nk, L, dict(MAT, Edc=edc[w]), dict(flags, DCTrans=False)).rk4_step(
+            *states[w], fields[w], dfields[w], dt, w + 1)
+        assert rel(nodc[1], ref[1]) > 1e-4   # the shift is visible at this tolerance
+        assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
+        assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
+        assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
+
+
+def test_solver_leapfrog_dc_vs_oracle():
+    """Three QWCalculator steps with DCTrans on (and Edc), SBESolver against the
+    oracle's solver, from the reference's saved initial state and fields."""
+    from pulsesuite_gb300 import SBEs
+    g = golden("solver_step")
+    prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
+               mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
+               epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR, Edc=6e7,
+               jmax=100000, ntmax=100000)
+    flags = dict(SOLVER_FLAGS, DCTrans=1)
+    rr = g["rr"]
+    s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
+                       flags=flags)
+    ref = O.Solver(s.Nk, prm["L"], prm, {k: bool(v) for k, v in flags.items()}, 2,
+                   float(g["E0"]))
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        setattr(s, nm, g["init_" + nm])
+        setattr(ref, nm, g["init_" + nm].copy())
+    dt = float(g["dt"])
+    for n in range(3):
+        for w in (1, 2):
+            outs = [np.zeros(len(rr), complex) for _ in range(4)]
+            s.QWCalculator(g[f"s{n}_Exx"], g[f"s{n}_Eyy"], g[f"s{n}_Ezz"],
+                           np.zeros(len(rr), complex), rr, None, dt, w, *outs, [False], [False])
+            exp = ref.qw_calculator(g[f"s{n}_Exx"], g[f"s{n}_Eyy"], g[f"s{n}_Ezz"],
+                                    np.zeros(len(rr), complex), rr, dt, w)
+            for a, b, nm in zip(outs, exp, ("Pxx", "Pyy", "Pzz", "Rho")):
+                assert rel(a, b) < SCREEN, (n, w, nm)
+        for nm in ("YY1", "CC1", "DD1", "CC3"):
+            assert rel(getattr(s, nm), getattr(ref, nm)) < SCREEN, (n, nm)
+    assert rel(ref.CC3, g["s2_CC3"]) > 1e-6   # the transport changed the state
+    s.close()

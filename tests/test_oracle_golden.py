@@ -152,6 +152,21 @@ def test_qwoptics(nk):
             assert rel(a, g[f"q2p_{n}_{pl}"]) < 1e-14, (pl, n)
 
 
+@pytest.mark.parametrize("nk", [8, 13])
+def test_dc_transport(nk):
+    """DCFieldModule.Transport (DCTrans) with and without LF, and its k array."""
+    g = golden(f"dc_nk{nk}")
+    dky = g["kr"][2] - g["kr"][1]
+    assert rel(O.dc_karray(nk, dky), g["Y"]) < 1e-15
+    for lf in (0, 1):
+        out = O.dc_transport(g[f"C_in_l{lf}"], float(g["Edc"]), float(g["Eac"]), float(g["dt"]),
+                             dky, lf)
+        assert rel(out, g[f"C_out_l{lf}"]) < 1e-14, lf
+        if not lf:   # off the diagonal the matrix is untouched
+            off = ~np.eye(nk, dtype=bool)
+            assert np.array_equal(out[off], g[f"C_in_l{lf}"][off])
+
+
 SOLVER_PARAMS = dict(gap=1.52 * O.E0, me=0.067 * O.ME0, mh=0.45 * O.ME0, HO=100e-3 * O.E0,
                      Delta0=6e-9, gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9,
                      Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR)
