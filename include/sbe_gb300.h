@@ -178,7 +178,8 @@ int sbe_leapfrog_step(SbeCtx* ctx, double* const* state9, const double* Ek, doub
  * k space at the step start Ek0 and its change per step dEk (both 3 x c128 Nr per
  * wire; stage fields Ek0 + c dEk).  Relaxation, charge normalisation and the
  * sources of the new state follow (as in the reference step).  precision:
- * SBE_PREC_FP64 or SBE_PREC_MIXED.                                             */
+ * SBE_PREC_FP64 or SBE_PREC_MIXED (SBE_ERR_UNSUPPORTED for a context with
+ * SBE_F_DCTRANS: the reference's transport leaves C, D non-Hermitian).        */
 int sbe_rk4_step(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0,
                  const double* dEk, double dt, int precision, double* src_out, void* stream);
 /* The coherent RHS of every wire at the given state/field (preparation included),
