@@ -308,6 +308,21 @@ int sbe_convert_selftest(const double* d_in, const float* f_in, long long n, flo
 int sbe_deph_selftest(SbeCtx* ctx, const double* C, const double* D, int fp32, double* De,
                       double* Dh, void* stream);
 
+/* ---- backup files of the state (host only, no device call) ---------------- */
+/* Text of SBEs.py:5524-5546 write_sbes_data (WriteSBEsData :6046): one line
+ * "re im\n" per complex element, each number as Python's repr of a float64
+ * (f"{np.real(val)} {np.imag(val)}").  values: count c128 in host memory, in the
+ * file's order (per wire, k2 outer, k1 inner); out needs 50 bytes per value;
+ * *written = bytes produced.  threads <= 0: all host threads.                  */
+int sbe_backup_format(const double* values, long long count, char* out, long long cap,
+                      long long* written, int threads);
+/* SBEs.py:5548-5569 read_sbes_data (ReadSBEsData :6051): the first count lines of
+ * text, two numbers each (Python float() spellings; further tokens on a line
+ * ignored), into values (count c128).  SBE_ERR_ARG on fewer lines or a line that
+ * does not start with two numbers.                                              */
+int sbe_backup_parse(const char* text, long long len, double* values, long long count,
+                     int threads);
+
 #ifdef __cplusplus
 }
 #endif

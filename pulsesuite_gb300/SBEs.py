@@ -263,29 +263,27 @@ class SBESolver:
             Rho[:] = 0.0
 
     def write_sbes_data(self, n):
-        """SBEs.py:5524-5546: dataQW/backup/{CC,DD,YY}{1,2,3}.n.dat, 're im' per line,
-        loop order w, k2, k1."""
+        """SBEs.py:5524-5546: dataQW/backup/{CC,DD,YY}{1,2,3}.n.dat, 're im' per line
+        (Python float repr), loop order w, k2, k1.  The level is transposed on the
+        GPU, copied once and formatted by the library's threaded writer."""
         os.makedirs("dataQW/backup/", exist_ok=True)
         for key in ("CC1", "CC2", "CC3", "DD1", "DD2", "DD3", "YY1", "YY2", "YY3"):
-            arr = getattr(self, key)
-            with open(f"dataQW/backup/{key}.{n}.dat", "w", encoding="utf-8") as f:
-                for w in range(arr.shape[2]):
-                    for k2 in range(self.Nk):
-                        for k1 in range(self.Nk):
-                            v = arr[k1, k2, w]
-                            f.write(f"{np.real(v)} {np.imag(v)}\n")
+            i = _LEVELS.index(key)
+            lev = torch.stack([self._st[w][i].t() for w in range(self.Nw)]).contiguous()
+            text = _lib.backup_format(lev.cpu().numpy())
+            with open(f"dataQW/backup/{key}.{n}.dat", "wb") as f:
+                f.write(text)
 
     def read_sbes_data(self, Nt):
         """SBEs.py:5548-5569: inverse of write_sbes_data."""
+        nk, nw = self.Nk, self.Nw
         for key in ("CC1", "CC2", "CC3", "DD1", "DD2", "DD3", "YY1", "YY2", "YY3"):
-            arr = np.zeros((self.Nk, self.Nk, self.Nw), dtype=complex)
-            with open(f"dataQW/backup/{key}.{Nt}.dat", "r", encoding="utf-8") as f:
-                for w in range(self.Nw):
-                    for k2 in range(self.Nk):
-                        for k1 in range(self.Nk):
-                            a, b = f.readline().split()
-                            arr[k1, k2, w] = float(a) + 1j * float(b)
-            setattr(self, key, arr)
+            i = _LEVELS.index(key)
+            with open(f"dataQW/backup/{key}.{Nt}.dat", "rb") as f:
+                vals = _lib.backup_parse(f.read(), nw * nk * nk).reshape(nw, nk, nk)
+            for w in range(nw):
+                lev = torch.as_tensor(vals[w], dtype=CDTYPE, device="cuda")
+                self._st[w][i].copy_(lev.t())
 
     def close(self):
         for c in getattr(self, "contexts", []):

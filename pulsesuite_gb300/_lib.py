@@ -37,6 +37,7 @@ EXPORTS = (
     "sbe_couple_destroy", "sbe_couple_buffers", "sbe_couple_set_step", "sbe_couple_reset",
     "sbe_couple_sample",
     "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
+    "sbe_backup_format", "sbe_backup_parse",
 )
 
 
@@ -84,6 +85,8 @@ def load(path=LIB_PATH):
     lib.sbe_version.restype = I
     sig = {
         "sbe_constants": [P],
+        "sbe_backup_format": [P, ctypes.c_longlong, P, ctypes.c_longlong, P, I],
+        "sbe_backup_parse": [P, ctypes.c_longlong, P, ctypes.c_longlong, I],
         "sbe_ctx_create": [P, I, P, P],
         "sbe_ctx_destroy": [P],
         "sbe_ctx_layout": [P, P, P, P],
@@ -161,3 +164,26 @@ def stream_handle(stream=None):
     import torch
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def backup_format(values, threads=0):
+    """Backup-file text of complex values (host), one "re im" line each, numbers as
+    Python's repr (SBEs.py:5524-5546 write_sbes_data); returns a memoryview of bytes."""
+    import numpy as np
+    v = np.ascontiguousarray(values, dtype=np.complex128).reshape(-1)
+    out = np.empty(max(50 * v.size, 1), dtype=np.uint8)
+    n = ctypes.c_longlong(0)
+    check(load().sbe_backup_format(v.ctypes.data, v.size, out.ctypes.data, out.size,
+                                   ctypes.byref(n), int(threads)), "sbe_backup_format")
+    return memoryview(out)[:n.value]
+
+
+def backup_parse(text, count, threads=0):
+    """Inverse of backup_format: the first count lines of text (bytes) as complex128
+    (SBEs.py:5548-5569 read_sbes_data)."""
+    import numpy as np
+    b = np.frombuffer(bytes(text), dtype=np.uint8)
+    out = np.empty(count, dtype=np.complex128)
+    check(load().sbe_backup_parse(b.ctypes.data if b.size else None, b.size, out.ctypes.data,
+                                  int(count), int(threads)), "sbe_backup_parse")
+    return out

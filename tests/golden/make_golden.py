@@ -26,6 +26,8 @@ emission_nkN    ``emission.InitializeEmission`` tables and ``SpontEmission`` (Re
                 ``make_golden.py <src> emission`` writes these alone.
 dc_nkN          ``dcfield.DCFieldModule.Transport`` (DCTrans) of a matrix with and
                 without LF; ``make_golden.py <src> dc`` writes these alone.
+backup_nk6      ``SBESolver.write_sbes_data`` files of nine levels (text and arrays);
+                ``make_golden.py <src> backup`` writes it alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
                 ``OffDiagDephasing2``.
 qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
@@ -42,6 +44,7 @@ import io
 import os
 import sys
 import tempfile
+import types
 import contextlib
 
 import numpy as np
@@ -304,6 +307,46 @@ def case_dc(nk, seed):
     return out
 
 
+def backup_values(rng, shape):
+    """Complex values over the float64 range for the backup-format case: random
+    mantissas at exponents from subnormal to near overflow, plus the edges of the
+    repr's positional/scientific switch, signed zeros and integers."""
+    n = int(np.prod(shape))
+    mag = 10.0 ** rng.uniform(-320, 307, 2 * n)
+    v = rng.standard_normal(2 * n) * mag
+    edge = [0.0, -0.0, 1.0, -2.0, 0.1 + 0.2, 1e-4, 1e-5, 9.999e-5, 1e15, 1e16, 9999999999999998.0,
+            123456789012345678.0, 5e-324, -2.2250738585072014e-308, 1.7976931348623157e308,
+            0.5, 1 / 3, 2.0 ** 52, 2.0 ** 53 + 2, 1e22, 1e23, 3.0e-7, 12345.678]
+    v[:len(edge)] = edge
+    z = np.empty(n, dtype=complex)
+    z.real = v[0::2]   # (re + 1j * im would drop the sign of -0.0)
+    z.imag = v[1::2]
+    return z.reshape(shape)
+
+
+def case_backup(nk, nw, seed):
+    """SBESolver.write_sbes_data (SBEs.py:5524-5546) of nine levels: the files' text
+    and the arrays it was written from."""
+    from pulsesuite.PSTD3D import SBEs
+    rng = np.random.default_rng(seed)
+    keys = ["CC1", "CC2", "CC3", "DD1", "DD2", "DD3", "YY1", "YY2", "YY3"]
+    obj = types.SimpleNamespace(Nk=nk)
+    for k in keys:
+        setattr(obj, k, backup_values(rng, (nk, nk, nw)))
+    SBEs.SBESolver.write_sbes_data(obj, 7)
+    out = dict(nk=nk, nw=nw, n=7)
+    for k in keys:
+        out["arr_" + k] = getattr(obj, k)
+        with open(f"dataQW/backup/{k}.7.dat", "rb") as f:
+            out["txt_" + k] = np.frombuffer(f.read(), dtype=np.uint8)
+    # read_sbes_data forms float(re) + 1j * float(im): signed zeros do not all survive
+    back = types.SimpleNamespace(Nk=nk, **{k: np.zeros((nk, nk, nw), complex) for k in keys})
+    SBEs.SBESolver.read_sbes_data(back, 7)
+    for k in keys:
+        out["back_" + k] = getattr(back, k)
+    return out
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -534,7 +577,10 @@ def main():
                     if only in (None, "dc"):
                         np.savez_compressed(os.path.join(HERE, f"dc_nk{nk}.npz"),
                                             **case_dc(nk, seed + 600))
-                if only in ("mbc", "emission", "dc"):
+                if only in (None, "backup"):
+                    np.savez_compressed(os.path.join(HERE, "backup_nk6.npz"),
+                                        **case_backup(6, 2, 700))
+                if only in ("mbc", "emission", "dc", "backup"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

@@ -430,3 +430,35 @@ def test_solver_leapfrog_dc_vs_oracle():
             assert rel(getattr(s, nm), getattr(ref, nm)) < SCREEN, (n, nm)
     assert rel(ref.CC3, g["s2_CC3"]) > 1e-6   # the transport changed the state
     s.close()
+
+
+def test_solver_backup_files_round_trip(tmp_path, monkeypatch):
+    """write_sbes_data / read_sbes_data (SBEs.py:5524-5569) of the GPU solver's nine
+    levels: the files hold the reference writer's text of the levels, and reading
+    them back restores every level."""
+    from pulsesuite_gb300 import SBEs
+    g = golden("solver_step")
+    prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
+               mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
+               epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR, Edc=0.0,
+               jmax=100000, ntmax=100000)
+    rr = g["rr"]
+    s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
+                       flags=SOLVER_FLAGS)
+    levels = ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3")
+    for nm in levels:
+        setattr(s, nm, g["s1_" + nm])
+    monkeypatch.chdir(tmp_path)
+    s.write_sbes_data(12)
+    for nm in levels:
+        arr = getattr(s, nm)
+        want = "".join(f"{np.real(arr[k1, k2, w])} {np.imag(arr[k1, k2, w])}\n"
+                       for w in range(arr.shape[2]) for k2 in range(s.Nk) for k1 in range(s.Nk))
+        with open(f"dataQW/backup/{nm}.12.dat", encoding="utf-8") as f:
+            assert f.read() == want, nm
+    for nm in levels:
+        setattr(s, nm, np.zeros_like(g["s1_" + nm]))
+    s.read_sbes_data(12)
+    for nm in levels:
+        assert np.array_equal(getattr(s, nm), g["s1_" + nm]), nm
+    s.close()
