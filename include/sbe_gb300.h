@@ -127,6 +127,20 @@ int sbe_phonon_rates(SbeCtx* ctx, int w, const double* ne, const double* nh, con
  * used) and VC (Nk*Nk*3).  The wire must have SBE_F_RECOMB.                    */
 int sbe_spont_emission(SbeCtx* ctx, int w, const double* ne, const double* nh, const double* VC,
                        double* Rsp, void* stream);
+/* The per-step statistics of wire w that SBEs.py:5769-5809 appends to
+ * dataQW/info.WW.t.dat and dataQW/EP.WW.t.dat, reduced on the device.  C2, D2:
+ * the packed middle-level state (ne2 = |C2_kk|, nh2 = |D2_kk|); src: the packed
+ * real-space sources (per wire 5 x c128 Nr: Px, Py, Pz, re, rh); Ek: the packed
+ * wire-k field (3 x c128 Nr); VC (Nk*Nk*3) or NULL for the last step's screened
+ * interaction.  out23 (device): CalcVD e/h (dcfield.py:128), densities 2 sum n / L,
+ * TotalEnergy e (with the gap)/h in eV, Temperature e/h (usefulsubs.py:1185-1253),
+ * max |FFTG re|, max |FFTG rh| (the reference takes them over its wire-k arrays),
+ * GetEDrift (0: SBEs never sets it), momenta 2 hbar sum (ne-nh) k,
+ * hbar sum ne k, -hbar sum nh k, CalcI0 (dcfield.py:1110), CalcI0n e and h
+ * (:103, real parts; their imaginary parts are 0); then Re iFFTG(Ex, Ey, Ez)[Nr/2]
+ * and Re Px, Py, Pz [Nr/2].                                                     */
+int sbe_wire_info(SbeCtx* ctx, int w, const double* C2, const double* D2, const double* src,
+                  const double* Ek, const double* VC, double* out23, void* stream);
 /* coulomb.py:1298/1313 MBCE/MBCH (carrier-carrier scattering, EHs; tables of
  * CalcMBArrays, coulomb.py:367, evaluated on the fly, Lorentzian broadening with
  * SBE_F_LORENTZ in the wire's flags, else Gaussian): Win/Wout accumulated in place.

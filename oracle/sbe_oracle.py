@@ -1019,6 +1019,64 @@ def dc_transport(X, Edc, Eac, dt, dky, lf):
     return out
 
 
+def ek_renorm(n, En, V):
+    """dcfield.py:339-344 _EkReNorm_jit: Ec(k) = En(k) + sum_k' n(k') (V[k,k] - V[k,k']) / 2."""
+    return En + (np.diag(V) * np.sum(n) - V @ n) / 2.0
+
+
+def drift_vt(n, Ec, dkk):
+    """dcfield.py:348-359 _DriftVt_jit: centred dE/dk, linear ends, <dE/dk> / hbar."""
+    nk = len(n)
+    d = np.zeros(nk)
+    d[1:nk - 1] = (Ec[2:] - Ec[:nk - 2]) / 2.0 / dkk
+    d[0] = 2.0 * d[1] - d[2]
+    d[nk - 1] = 2.0 * d[nk - 2] - d[nk - 3]
+    return float(np.real(np.sum(d * n) / (1e-100 + np.sum(n)) / HBAR))
+
+
+def wire_info(ne2, nh2, re, rh, Ek, src3, kr, me, mh, Ee, Eh, gap, L, dkr, VC):
+    """The columns after the time of dataQW/info.WW.t.dat and dataQW/EP.WW.t.dat
+    (SBEs.py:5769-5809): CalcVD (dcfield.py:128-151), densities, TotalEnergy and
+    Temperature (usefulsubs.py:1185-1253, small = 1e-100), max |Re|, |Rh|, GetEDrift
+    (the DC module's ERate: 0, SBEs never sets it), momenta, CalcI0 (dcfield.py:1110-1148
+    with EkReNorm/DriftVt), CalcI0n (dcfield.py:103-125, complex); EP: the real parts
+    of iFFTG(E)[Nr/2] and iFFTG(P)[Nr/2].  re, rh, the fields and the sources are the
+    wire-k arrays the reference holds at that point."""
+    def vd(m, n):
+        return np.sum(np.real(n) * HBAR * kr / m) / np.sum(np.real(n) + 1e-200)
+
+    def temp(n, E):
+        return 2.0 * np.real(np.sum(n * E) / (np.sum(n) + 1e-100)) / KB
+
+    def i0n(n, m):
+        dk = kr[1] - kr[0] if len(kr) > 1 else 1.0
+        return -E0 * np.sum(n * kr * HBAR / m) * 2.0 * dk
+
+    ve = drift_vt(np.real(ne2), ek_renorm(np.real(ne2), Ee, VC[:, :, 1]), dkr)
+    vh = drift_vt(np.real(nh2), ek_renorm(np.real(nh2), Eh, VC[:, :, 2]), dkr)
+    i0 = np.real(-E0 * (ve + vh) * np.sum(ne2) * dkr * 2.0)
+    info = [vd(me, ne2), vd(mh, nh2), np.real(2 * np.sum(ne2) / L), np.real(2 * np.sum(nh2) / L),
+            np.real(np.sum(ne2 * (Ee + gap))) / E0, np.real(np.sum(nh2 * Eh)) / E0,
+            temp(ne2, Ee), temp(nh2, Eh), np.max(np.abs(re)), np.max(np.abs(rh)), 0.0,
+            np.real(HBAR * np.sum((ne2 - nh2) * kr)) * 2.0, np.real(HBAR * np.sum(ne2 * kr)),
+            np.real(-HBAR * np.sum(nh2 * kr)), i0, i0n(ne2, me), i0n(1 - nh2, -mh)]
+    nr = len(Ek[0])
+    ep = [np.real(ifftg(E)[nr // 2]) for E in list(Ek) + list(src3)]
+    return info, ep
+
+
+def info_line(t, info):
+    """One line of dataQW/info.WW.t.dat as SBEs.py:5772-5791 formats it (the two
+    CalcI0n columns are complex and print as complex numbers)."""
+    vals = [t] + list(info)
+    return "".join(f"{v:18.6e} " for v in vals[:-1]) + f"{vals[-1]:18.6e}\n"
+
+
+def ep_line(t, ep):
+    """One line of dataQW/EP.WW.t.dat (SBEs.py:5800-5809)."""
+    return " ".join(f"{v:18.6e}" for v in [t] + list(ep)) + "\n"
+
+
 EMISSION_TEMP = 77.0   # emission.py:28 _Temp: the module's own temperature, never set by SBEs.py
 
 
@@ -1296,6 +1354,12 @@ class Solver:
         C2 = (C1 + C3) / 2.0
         D2 = (D1 + D3) / 2.0
         Px, Py, Pz, re, rh = wi.sources(p3, C3, D3, ne3, nh3, w)
+        # SBEs.py:5769-5809: the statistics of info.WW.t.dat and EP.WW.t.dat
+        ne2 = np.abs(np.diag(C2)).astype(complex)
+        nh2 = np.abs(np.diag(D2)).astype(complex)
+        self.last_info = wire_info(ne2, nh2, re, rh, (Ex, Ey, Ez), (Px, Py, Pz), g["kr"],
+                                   wi.p["me"], wi.p["mh"], wi.c["Ee"], wi.c["Eh"], wi.p["gap"],
+                                   g["L"], PI / g["L"], pr["VC"])   # dkr (SBEs.py:4755)
         self.YY1[:, :, i], self.YY2[:, :, i], self.YY3[:, :, i] = p1, p2, p3
         self.CC1[:, :, i], self.CC2[:, :, i], self.CC3[:, :, i] = C1, C2, C3
         self.DD1[:, :, i], self.DD2[:, :, i], self.DD3[:, :, i] = D1, D2, D3

@@ -159,6 +159,8 @@ class SBESolver:
         for k, v in f.items():
             setattr(self, k, v)
         self.Emax0 = Emaxxx
+        # the reference appends dataQW/info.WW.t.dat and EP.WW.t.dat every step
+        self.write_info = True
         kmax = np.sqrt(1.2 * self.gap * 2.0 * self.me / (HBAR ** 2))
         self.dkr = TWOPI / (2.0 * self.L)
         if nk is None:
@@ -250,8 +252,11 @@ class SBESolver:
                              dtype=CDTYPE, device="cuda").contiguous()
         Ek = ctx.prop2qw(0, RR, f4)                       # (4, Nr): Ex, Ey, Ez, Vr in wire k space
         src = torch.empty((5, self.Nr), dtype=CDTYPE, device="cuda")
-        ctx.leapfrog_step(self._st[w - 1], Ek[:3].contiguous(), dt, src)
+        Ek3 = Ek[:3].contiguous()
+        ctx.leapfrog_step(self._st[w - 1], Ek3, dt, src)
         out = ctx.qw2prop(0, RR, src, self.LF).cpu().numpy()
+        if self.write_info:
+            self._write_info(ctx, w, dt, src, Ek3)
         Pxx[:] = out[0]
         Pyy[:] = out[1]
         Pzz[:] = out[2]
@@ -261,6 +266,20 @@ class SBESolver:
             Pyy[:] = 0.0
             Pzz[:] = 0.0
             Rho[:] = 0.0
+
+    def _write_info(self, ctx, w, dt, src, Ek3):
+        """SBEs.py:5769-5809: append this step's line to dataQW/info.WW.t.dat and to
+        dataQW/EP.WW.t.dat (statistics reduced on the device by sbe_wire_info; the
+        CalcI0n columns print as complex numbers, as the reference's do)."""
+        st = self._st[w - 1]
+        v = ctx.wire_info(0, st[4], st[7], src, Ek3)
+        t = self.xxx * dt
+        info = [t] + [float(x) for x in v[:15]] + [complex(v[15], 0.0), complex(v[16], 0.0)]
+        os.makedirs("dataQW", exist_ok=True)
+        with open(f"dataQW/info.{w:02d}.t.dat", "a", encoding="utf-8") as f:
+            f.write("".join(f"{x:18.6e} " for x in info[:-1]) + f"{info[-1]:18.6e}\n")
+        with open(f"dataQW/EP.{w:02d}.t.dat", "a", encoding="utf-8") as f:
+            f.write(" ".join(f"{x:18.6e}" for x in [t] + [float(x) for x in v[17:23]]) + "\n")
 
     def write_sbes_data(self, n):
         """SBEs.py:5524-5546: dataQW/backup/{CC,DD,YY}{1,2,3}.n.dat, 're im' per line

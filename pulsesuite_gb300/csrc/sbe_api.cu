@@ -540,6 +540,17 @@ int sbe_spont_emission(SbeCtx* c, int w, const double* ne, const double* nh, con
   return cuda_check(cudaGetLastError(), "sbe_spont_emission");
 }
 
+int sbe_wire_info(SbeCtx* c, int w, const double* C2, const double* D2, const double* src,
+                  const double* Ek, const double* VC, double* out23, void* stream) {
+  int rc = check_w(c, w, "sbe_wire_info");
+  if (rc) return rc;
+  if (!C2 || !D2 || !src || !Ek || !out23) return fail(SBE_ERR_ARG, "sbe_wire_info: null pointer");
+  cudaStream_t s = as_stream(stream);
+  if (VC) set_vc(c, w, VC, nullptr, s);
+  return launch_wire_info(c, w, (const double2*)C2, (const double2*)D2, (const double2*)src,
+                          (const double2*)Ek, out23, s);
+}
+
 int sbe_carrier_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
                       double* WinE, double* WoutE, double* WinH, double* WoutH, int precision,
                       void* stream) {

@@ -180,6 +180,9 @@ void launch_sources_final(SbeCtx* c, const double2* ne, const double2* nh, doubl
                           cudaStream_t s);
 void launch_relax_only(SbeCtx* c, double2* P3, double2* C3, double2* D3, const double2* Ek,
                        double dt, cudaStream_t s);
+// sbe_info.cu: per-step statistics of wire w (info / EP columns) into out (23 doubles)
+int launch_wire_info(SbeCtx* c, int w, const double2* C2, const double2* D2, const double2* src,
+                     const double2* Ek, double* out, cudaStream_t s);
 // sbe_dc.cu: DC transport (dcfield.py:1154-1236 Transport) of P, C, D
 bool any_dc(const SbeCtx* c);
 void launch_dc_transport(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek,

@@ -233,6 +233,15 @@ class WireContext:
                                                _lib.stream_handle()), "sbe_spont_emission")
         return rsp
 
+    def wire_info(self, w, C2, D2, src, Ek, VC=None):
+        """The per-step statistics of wire w (the info and EP columns of SBEs.py:5769-5809)
+        as 23 numbers on the host (see sbe_wire_info)."""
+        out = torch.empty(23, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_wire_info(self.handle, w, _lib.ptr(C2), _lib.ptr(D2),
+                                          _lib.ptr(src), _lib.ptr(Ek), _lib.ptr(VC), _lib.ptr(out),
+                                          _lib.stream_handle()), "sbe_wire_info")
+        return out.cpu().numpy()
+
     def sources(self, w, P, C, D, ne, nh):
         nr = 2 * self.nk[w] + 2
         out = [torch.empty(nr, dtype=CDTYPE, device=self.device) for _ in range(5)]

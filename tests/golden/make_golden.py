@@ -28,6 +28,8 @@ dc_nkN          ``dcfield.DCFieldModule.Transport`` (DCTrans) of a matrix with a
                 without LF; ``make_golden.py <src> dc`` writes these alone.
 backup_nk6      ``SBESolver.write_sbes_data`` files of nine levels (text and arrays);
                 ``make_golden.py <src> backup`` writes it alone.
+info_nkN        the statistics of dataQW/info.WW.t.dat and EP.WW.t.dat from the
+                reference's helpers; ``make_golden.py <src> info`` writes these alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
                 ``OffDiagDephasing2``.
 qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
@@ -347,6 +349,49 @@ def case_backup(nk, nw, seed):
     return out
 
 
+def case_info(nk, seed):
+    """The statistics of dataQW/info.WW.t.dat and EP.WW.t.dat from the reference's
+    own helpers (dcfield CalcVD, CalcI0, CalcI0n; usefulsubs TotalEnergy, Temperature,
+    iFFTG) on seeded occupations, sources, fields and a screened VC."""
+    from scipy.constants import e as E0, hbar as HBAR
+    from pulsesuite.PSTD3D import dcfield, usefulsubs
+    rng = np.random.default_rng(seed)
+    g = wire_grid(nk)
+    d = derived(g)
+    kr, L = g["kr"], g["L"]
+    nr = 2 * nk + 2
+    me, mh, gap = d["me"], d["mh"], 1.52 * E0
+    Ee = (HBAR * kr) ** 2 / (2 * me)
+    Eh = (HBAR * kr) ** 2 / (2 * mh)
+    ne2 = np.abs(rng.uniform(0, 0.3, nk) * np.exp(-(kr / kr.max()) ** 2)).astype(complex)
+    nh2 = np.abs(rng.uniform(0, 0.2, nk) * np.exp(-(kr / kr.max() - 0.1) ** 2)).astype(complex)
+    VC = np.abs(rng.standard_normal((nk, nk, 3))) * 1e-21
+    re = cnormal(rng, nr, 1e3)
+    rh = cnormal(rng, nr, 2e3)
+    Ek = [cnormal(rng, nr, 1e6) for _ in range(3)]
+    src3 = [cnormal(rng, nr, 1e-3) for _ in range(3)]
+    dkr = np.pi / L
+    dm = dcfield.DCFieldModule(kr, me, mh, datadir=None)
+    dcfield._instance = dm
+    info = [dcfield.CalcVD(kr, me, ne2), dcfield.CalcVD(kr, mh, nh2),
+            np.real(2 * np.sum(ne2) / L), np.real(2 * np.sum(nh2) / L),
+            usefulsubs.TotalEnergy(ne2, Ee + gap) / E0, usefulsubs.TotalEnergy(nh2, Eh) / E0,
+            usefulsubs.Temperature(ne2, Ee), usefulsubs.Temperature(nh2, Eh),
+            np.max(np.abs(re)), np.max(np.abs(rh)), dm.GetEDrift(),
+            np.real(HBAR * np.sum((ne2 - nh2) * kr)) * 2.0, np.real(HBAR * np.sum(ne2 * kr)),
+            np.real(-HBAR * np.sum(nh2 * kr)),
+            np.real(dm.CalcI0(ne2, nh2, Ee, Eh, VC, dkr, kr, 0.0)),
+            dcfield.CalcI0n(ne2, me, kr), dcfield.CalcI0n(1 - nh2, -mh, kr)]
+    ep = []   # SBEs.py:5793-5809: iFFTG of the wire-k fields and sources, then [Nr // 2]
+    for E in Ek + src3:
+        x = E.copy()
+        usefulsubs.iFFTG(x)
+        ep.append(np.real(x[nr // 2]))
+    return dict(kr=kr, L=L, me=me, mh=mh, gap=gap, Ee=Ee, Eh=Eh, ne2=ne2, nh2=nh2, VC=VC,
+                re=re, rh=rh, Ek=np.array(Ek), src3=np.array(src3), dkr=dkr,
+                info=np.array(info, dtype=complex), ep=np.array(ep))
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -577,10 +622,14 @@ def main():
                     if only in (None, "dc"):
                         np.savez_compressed(os.path.join(HERE, f"dc_nk{nk}.npz"),
                                             **case_dc(nk, seed + 600))
+                if only in (None, "info"):
+                    for nk, seed in ((8, 800), (13, 801)):
+                        np.savez_compressed(os.path.join(HERE, f"info_nk{nk}.npz"),
+                                            **case_info(nk, seed))
                 if only in (None, "backup"):
                     np.savez_compressed(os.path.join(HERE, "backup_nk6.npz"),
                                         **case_backup(6, 2, 700))
-                if only in ("mbc", "emission", "dc", "backup"):
+                if only in ("mbc", "emission", "dc", "backup", "info"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

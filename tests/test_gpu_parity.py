@@ -179,9 +179,10 @@ SOLVER_FLAGS = dict(Optics=1, Excitons=1, EHs=0, Screened=1, Phonon=1, DCTrans=0
                     FreePot=0, DiagDph=1, OffDiagDph=1, Recomb=0, ignorewire=0)
 
 
-def test_solver_leapfrog_vs_golden():
+def test_solver_leapfrog_vs_golden(tmp_path, monkeypatch):
     """Three reference QWCalculator steps on two wires (SBESolver drop-in)."""
     from pulsesuite_gb300 import SBEs
+    monkeypatch.chdir(tmp_path)   # the solver appends dataQW/info and EP files
     g = golden("solver_step")
     prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
                mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
@@ -398,10 +399,25 @@ def test_rk4_with_dc_transport_vs_oracle(lf):
         assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
 
 
-def test_solver_leapfrog_dc_vs_oracle():
+def _last_line(path):
+    with open(path, encoding="utf-8") as f:
+        return f.read().splitlines()[-1].split()
+
+
+def _close_printed(tokens, want):
+    """Printed %18.6e values against the expected numbers (7 significant digits)."""
+    assert len(tokens) == len(want)
+    for tok, w in zip(tokens, want):
+        got = complex(tok) if tok.endswith("j") else float(tok)
+        assert abs(got - w) <= 1e-6 * abs(w) + 1e-300, (tok, w)
+
+
+def test_solver_leapfrog_dc_vs_oracle(tmp_path, monkeypatch):
     """Three QWCalculator steps with DCTrans on (and Edc), SBESolver against the
-    oracle's solver, from the reference's saved initial state and fields."""
+    oracle's solver, from the reference's saved initial state and fields; each step's
+    dataQW/info.WW.t.dat and EP.WW.t.dat lines against the oracle's statistics."""
     from pulsesuite_gb300 import SBEs
+    monkeypatch.chdir(tmp_path)
     g = golden("solver_step")
     prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
                mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
@@ -426,6 +442,10 @@ def test_solver_leapfrog_dc_vs_oracle():
                                     np.zeros(len(rr), complex), rr, dt, w)
             for a, b, nm in zip(outs, exp, ("Pxx", "Pyy", "Pzz", "Rho")):
                 assert rel(a, b) < SCREEN, (n, w, nm)
+            info, ep = ref.last_info
+            t = s.xxx * dt
+            _close_printed(_last_line(f"dataQW/info.{w:02d}.t.dat"), [t] + list(info))
+            _close_printed(_last_line(f"dataQW/EP.{w:02d}.t.dat"), [t] + list(ep))
         for nm in ("YY1", "CC1", "DD1", "CC3"):
             assert rel(getattr(s, nm), getattr(ref, nm)) < SCREEN, (n, nm)
     assert rel(ref.CC3, g["s2_CC3"]) > 1e-6   # the transport changed the state
@@ -462,3 +482,31 @@ def test_solver_backup_files_round_trip(tmp_path, monkeypatch):
     for nm in levels:
         assert np.array_equal(getattr(s, nm), g["s1_" + nm]), nm
     s.close()
+
+
+def test_wire_info_vs_oracle():
+    """sbe_wire_info on a seeded state, sources and field against the oracle's
+    statistics (FP64, all 23 numbers), with the format of the reference's lines."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    c = WireContext([WireSpec(nk=nk, L=L, temp=77.0, wire_index=1, flags=dict(ALL), **MAT)])
+    wire = O.Wire(nk, L, MAT, ALL)
+    rng = np.random.default_rng(31)
+    P, C, D = _seeded_state(rng, nk)
+    nr = 2 * nk + 2
+    src = (rng.standard_normal((5, nr)) + 1j * rng.standard_normal((5, nr))) * 1e-3
+    Ek = [(rng.standard_normal(nr) + 1j * rng.standard_normal(nr)) * 1e6 for _ in range(3)]
+    ne = np.abs(np.diag(C)).astype(complex)
+    nh = np.abs(np.diag(D)).astype(complex)
+    VC, _ = O.screened_arrays(wire.ct, True, L, ne, nh)
+    v = c.wire_info(0, c.pack([C]), c.pack([D]), dev(src.reshape(-1)),
+                    dev(np.concatenate(Ek)), dev(VC.reshape(-1)))
+    # the oracle takes the sources in wire-k space, as the reference holds them
+    ks = [O.fftg(x) for x in src]
+    info, ep = O.wire_info(ne, nh, ks[3], ks[4], Ek, ks[:3], wire.g["kr"], MAT["me"],
+                           MAT["mh"], wire.c["Ee"], wire.c["Eh"], MAT["gap"], L, np.pi / L, VC)
+    want = [np.real(x) for x in info] + list(ep)
+    for i, (a, b) in enumerate(zip(v, want)):
+        assert abs(a - b) <= 1e-12 * abs(b) + 1e-300, (i, a, b)
+    assert np.imag(info[15]) == 0.0 and np.imag(info[16]) == 0.0

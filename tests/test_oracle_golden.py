@@ -167,6 +167,23 @@ def test_dc_transport(nk):
             assert np.array_equal(out[off], g[f"C_in_l{lf}"][off])
 
 
+@pytest.mark.parametrize("nk", [8, 13])
+def test_wire_info_statistics(nk):
+    """The info.WW.t.dat / EP.WW.t.dat statistics against the reference's helpers,
+    and the line format of SBEs.py:5772-5809."""
+    g = golden(f"info_nk{nk}")
+    info, ep = O.wire_info(g["ne2"], g["nh2"], g["re"], g["rh"], list(g["Ek"]), list(g["src3"]),
+                           g["kr"], float(g["me"]), float(g["mh"]), g["Ee"], g["Eh"],
+                           float(g["gap"]), float(g["L"]), float(g["dkr"]), g["VC"])
+    for i, (a, b) in enumerate(zip(info, g["info"])):
+        assert abs(a - b) <= 1e-13 * abs(b), i
+    assert rel(np.array(ep), g["ep"]) < 1e-15
+    line = O.info_line(2e-15, info)
+    assert line == O.info_line(2e-15, list(g["info"][:15].real) + list(g["info"][15:]))
+    assert len(line.split()) == 18 and line.split()[-1].endswith("j")
+    assert O.ep_line(2e-15, ep).count("e") == 7
+
+
 SOLVER_PARAMS = dict(gap=1.52 * O.E0, me=0.067 * O.ME0, mh=0.45 * O.ME0, HO=100e-3 * O.E0,
                      Delta0=6e-9, gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9,
                      Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR)
