@@ -322,6 +322,22 @@ int sbe_convert_selftest(const double* d_in, const float* f_in, long long n, flo
 int sbe_deph_selftest(SbeCtx* ctx, const double* C, const double* D, int fp32, double* De,
                       double* Dh, void* stream);
 
+/* ---- 3-D field <-> wire coupling pieces (device pointers, c128 interleaved) -- */
+/* rhoPJ.py:491-515 CalcJfx: J[0] = 0, J[i] = J[i-1] - ((new_i - prev_i) / dt) dx
+ * (c128 n each).                                                                */
+int sbe_calc_jfx(long long n, const double* rho_new, const double* rho_prev, double dt,
+                 double dx, double* J, void* stream);
+/* rhoPJ.py:655-702 QWPlacement: Fgrid[i][j][k] = gx_i gy_j gz_k Fwire_i (Fgrid c128
+ * nx*ny*nz, C order; Fwire c128 nx; gates f64).                                 */
+int sbe_qw_placement(int nx, int ny, int nz, const double* Fwire, const double* gx,
+                     const double* gy, const double* gz, double* Fgrid, void* stream);
+/* usefulsubs.py:1996-2075 EAtXYZ with locator (:1803-1830), batched: out[p] (c128) =
+ * trilinear sample of f (c128 nx*ny*nz, C order) on the ascending axes x, y, z at
+ * pts[3p..3p+2]; a singleton axis takes its one plane.                         */
+int sbe_e_at_xyz(const double* f, const double* x, int nx, const double* y, int ny,
+                 const double* z, int nz, const double* pts, int npts, double* out,
+                 void* stream);
+
 /* ---- backup files of the state (host only, no device call) ---------------- */
 /* Text of SBEs.py:5524-5546 write_sbes_data (WriteSBEsData :6046): one line
  * "re im\n" per complex element, each number as Python's repr of a float64

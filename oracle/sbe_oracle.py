@@ -1077,6 +1077,48 @@ def ep_line(t, ep):
     return " ".join(f"{v:18.6e}" for v in [t] + list(ep)) + "\n"
 
 
+def calc_jfx(rho_new, rho_prev, dt, dx):
+    """rhoPJ.py:491-515 CalcJfx."""
+    d = (np.asarray(rho_new) - np.asarray(rho_prev)) / dt
+    J = np.zeros(len(d), dtype=complex)
+    for i in range(1, len(d)):
+        J[i] = J[i - 1] - d[i] * dx
+    return J
+
+
+def qw_placement(fwire, gx, gy, gz):
+    """rhoPJ.py:655-702 QWPlacement (returns the grid)."""
+    g = (np.asarray(gx)[:, None, None] * np.asarray(gy)[None, :, None]) * np.asarray(gz)[None, None, :]
+    return 0.0 + g * np.asarray(fwire)[:, None, None]
+
+
+def locator(x, x0):
+    """usefulsubs.py:1803-1830."""
+    return max(0, min(int(np.searchsorted(x, x0, side="right")) - 1, len(x) - 2))
+
+
+def e_at_xyz(f, x, y, z, x0, y0, z0):
+    """usefulsubs.py:1996-2075 EAtXYZ (a singleton axis takes its one plane)."""
+    idx, ws = [], []
+    for a, a0 in ((x, x0), (y, y0), (z, z0)):
+        if len(a) == 1:
+            idx.append(0)
+            ws.append((1.0, 0.0))
+        else:
+            i = locator(a, a0)
+            al = (a0 - a[i]) / (a[i + 1] - a[i])
+            idx.append(i)
+            ws.append((1.0 - al, al))
+    f0 = 0.0 + 0.0j
+    for r in range(2):
+        for q in range(2):
+            for p in range(2):
+                if (p and len(x) == 1) or (q and len(y) == 1) or (r and len(z) == 1):
+                    continue
+                f0 = f0 + ws[0][p] * ws[1][q] * ws[2][r] * f[idx[0] + p, idx[1] + q, idx[2] + r]
+    return f0
+
+
 EMISSION_TEMP = 77.0   # emission.py:28 _Temp: the module's own temperature, never set by SBEs.py
 
 

@@ -37,7 +37,8 @@ EXPORTS = (
     "sbe_couple_destroy", "sbe_couple_buffers", "sbe_couple_set_step", "sbe_couple_reset",
     "sbe_couple_sample",
     "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
-    "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info",
+    "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info", "sbe_calc_jfx",
+    "sbe_qw_placement", "sbe_e_at_xyz",
 )
 
 
@@ -102,6 +103,9 @@ def load(path=LIB_PATH):
         "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, I, P],
         "sbe_spont_emission": [P, I, P, P, P, P, P],
         "sbe_wire_info": [P, I, P, P, P, P, P, P, P],
+        "sbe_calc_jfx": [ctypes.c_longlong, P, P, Dbl, Dbl, P, P],
+        "sbe_qw_placement": [I, I, I, P, P, P, P, P, P],
+        "sbe_e_at_xyz": [P, P, I, P, I, P, I, P, I, P, P],
         "sbe_sources": [P, I, P, P, P, P, P, P, P, P, P, P, P],
         "sbe_prop2qw": [P, I, P, I, P, P, P],
         "sbe_prop2qw_noalloc": [P, I, P, I, P, P, P],

@@ -28,6 +28,8 @@ dc_nkN          ``dcfield.DCFieldModule.Transport`` (DCTrans) of a matrix with a
                 without LF; ``make_golden.py <src> dc`` writes these alone.
 backup_nk6      ``SBESolver.write_sbes_data`` files of nine levels (text and arrays);
                 ``make_golden.py <src> backup`` writes it alone.
+coupling3d      rhoPJ CalcJfx / QWPlacement and usefulsubs EAtXYZ on seeded inputs;
+                ``make_golden.py <src> coupling3d`` writes it alone.
 info_nkN        the statistics of dataQW/info.WW.t.dat and EP.WW.t.dat from the
                 reference's helpers; ``make_golden.py <src> info`` writes these alone.
 dephasing_nkN   ``dephasing.DephasingModule`` index maps, ``CalcGammaE/H`` and
@@ -392,6 +394,32 @@ def case_info(nk, seed):
                 info=np.array(info, dtype=complex), ep=np.array(ep))
 
 
+def case_coupling3d(seed):
+    """rhoPJ CalcJfx and QWPlacement, usefulsubs EAtXYZ of the reference on seeded
+    inputs (points inside, on and outside the grid)."""
+    from pulsesuite.PSTD3D import rhoPJ, usefulsubs
+    rng = np.random.default_rng(seed)
+    n = 257
+    rn, rp = cnormal(rng, n, 1.0), cnormal(rng, n, 1.0)
+    J = rhoPJ.CalcJfx(rn.copy(), rp.copy(), 1e-16, 5e-9)
+    nx, ny, nz = 7, 5, 4
+    fw = cnormal(rng, nx, 1.0)
+    gx, gy, gz = rng.uniform(0, 1, nx), rng.uniform(-1, 1, ny), np.exp(-rng.uniform(0, 3, nz))
+    grid = np.zeros((nx, ny, nz), dtype=complex)
+    rhoPJ.QWPlacement(fw, gx, gy, gz, grid)
+    x = np.sort(rng.uniform(-1, 1, 9))
+    y = np.linspace(-2.0, 3.0, 6)
+    z = np.cumsum(rng.uniform(0.1, 1.0, 5))
+    f = cnormal(rng, (9, 6, 5), 1.0)
+    pts = np.stack([rng.uniform(-1.3, 1.3, 40), rng.uniform(-2.5, 3.5, 40),
+                    rng.uniform(0.0, z[-1] + 0.5, 40)], axis=1)
+    pts[:5] = [[x[0], y[0], z[0]], [x[-1], y[-1], z[-1]], [x[3], y[2], z[1]],
+               [-5.0, 10.0, 0.0], [x[4], y[4] + 1e-9, z[2]]]
+    val = np.array([usefulsubs.EAtXYZ(f, x, y, z, *p) for p in pts])
+    return dict(rn=rn, rp=rp, J=J, dt=1e-16, dx=5e-9, fw=fw, gx=gx, gy=gy, gz=gz, grid=grid,
+                x=x, y=y, z=z, f=f, pts=pts, val=val)
+
+
 def case_dephasing(nk, seed, VC):
     from pulsesuite.PSTD3D import dephasing
     rng = np.random.default_rng(seed)
@@ -626,10 +654,13 @@ def main():
                     for nk, seed in ((8, 800), (13, 801)):
                         np.savez_compressed(os.path.join(HERE, f"info_nk{nk}.npz"),
                                             **case_info(nk, seed))
+                if only in (None, "coupling3d"):
+                    np.savez_compressed(os.path.join(HERE, "coupling3d.npz"),
+                                        **case_coupling3d(900))
                 if only in (None, "backup"):
                     np.savez_compressed(os.path.join(HERE, "backup_nk6.npz"),
                                         **case_backup(6, 2, 700))
-                if only in ("mbc", "emission", "dc", "backup", "info"):
+                if only in ("mbc", "emission", "dc", "backup", "info", "coupling3d"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

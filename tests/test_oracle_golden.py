@@ -184,6 +184,16 @@ def test_wire_info_statistics(nk):
     assert O.ep_line(2e-15, ep).count("e") == 7
 
 
+def test_coupling3d_pieces():
+    """CalcJfx, QWPlacement and EAtXYZ (with locator) against the reference."""
+    g = golden("coupling3d")
+    assert np.array_equal(O.calc_jfx(g["rn"], g["rp"], float(g["dt"]), float(g["dx"])), g["J"])
+    grid = O.qw_placement(g["fw"], g["gx"], g["gy"], g["gz"])
+    assert np.array_equal(grid.view(np.int64), g["grid"].view(np.int64))
+    val = np.array([O.e_at_xyz(g["f"], g["x"], g["y"], g["z"], *p) for p in g["pts"]])
+    assert np.array_equal(val.view(np.int64), g["val"].view(np.int64))
+
+
 SOLVER_PARAMS = dict(gap=1.52 * O.E0, me=0.067 * O.ME0, mh=0.45 * O.ME0, HO=100e-3 * O.E0,
                      Delta0=6e-9, gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9,
                      Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR)
