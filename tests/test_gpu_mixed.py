@@ -1,6 +1,6 @@
 """Mixed-precision (tcgen05) RHS and RK4 step vs the FP64 GPU path (needs a GPU).
 
-Bars (the benchmark spec's tolerances): RHS relative Frobenius error <= 1e-6;
+Accuracy bars of the mixed path: RHS relative Frobenius error <= 1e-6;
 observables after a pulse segment <= 1e-5 relative to the FP64 run.
 """
 
