@@ -46,3 +46,21 @@ def test_constants_and_errors_without_gpu(lib_path):
     assert b"null" in lib.sbe_last_error()
     assert lib.sbe_dpdt(0, None, None, None, None, None, None, None, None, None, None, None) == 1
     assert lib.sbe_ctx_create(None, 0, None, None) == 1
+
+
+def test_new_entry_points_check_arguments_without_gpu(lib_path):
+    """DC, statistics, backup and coupling entry points reject bad arguments on the
+    host, before any device call."""
+    from pulsesuite_gb300 import _lib
+    lib = _lib.load(lib_path)
+    assert lib.sbe_wire_info(None, 0, None, None, None, None, None, None, None) == 1
+    assert b"bad context" in lib.sbe_last_error()
+    assert lib.sbe_calc_jfx(-1, None, None, 1.0, 1.0, None, None) == 1
+    assert lib.sbe_calc_jfx(4, None, None, 1.0, 1.0, None, None) == 1
+    assert lib.sbe_calc_jfx(0, None, None, 1.0, 1.0, None, None) == 0     # nothing to do
+    assert lib.sbe_qw_placement(2, 2, 2, None, None, None, None, None, None) == 1
+    assert lib.sbe_e_at_xyz(None, None, 0, None, 1, None, 1, None, 0, None, None) == 1
+    assert lib.sbe_backup_format(None, 3, None, 0, None, 0) == 1
+    n = ctypes.c_longlong(-1)
+    assert lib.sbe_backup_format(None, 0, None, 0, ctypes.byref(n), 0) == 0 and n.value == 0
+    assert lib.sbe_backup_parse(None, 0, None, 0, 0) == 0
