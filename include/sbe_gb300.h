@@ -168,11 +168,13 @@ int sbe_qw2prop(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* sr
  * Same arguments and results as sbe_prop2qw, for callers that must not allocate
  * device memory (a host code whose pool owns all device memory, or a loop that
  * must not take the allocator's lock): the scratch is one static device array
- * per device, so nothing is allocated or freed.  Limits: n_rr <=
- * SBE_NOALLOC_MAX_GRID, wire Nr <= SBE_NOALLOC_MAX_NR; larger calls return an
- * error before any launch.  The first call on a device looks the array up
- * (cudaGetSymbolAddress); make it before any stream capture.  Calls that overlap
- * in time on one device (other streams, threads or contexts) race on the shared
+ * per CUDA context (each context loads its own copy of the library's module), so
+ * nothing is allocated or freed.  Limits: n_rr <= SBE_NOALLOC_MAX_GRID, wire
+ * Nr <= SBE_NOALLOC_MAX_NR; larger calls return an error before any launch.
+ * Every call looks the array up in the current context (cudaGetSymbolAddress,
+ * nothing cached, so a reset or new context is safe); the first call in a
+ * context may load the module, so make it before any stream capture.  Calls of
+ * one context that overlap in time (other streams or threads) race on the shared
  * scratch; calls on one stream are ordered.                                    */
 #define SBE_NOALLOC_MAX_GRID 8192
 #define SBE_NOALLOC_MAX_NR 2050

@@ -94,26 +94,98 @@ int pick_threads(int threads, long long work) {
   return (int)std::max<long long>(1, std::min<long long>(t, work / 65536 + 1));
 }
 
-bool is_space(char ch) { return ch == ' ' || ch == '\t' || ch == '\r'; }
+// the ASCII whitespace of Python's str.split() (the reader splits each line with it)
+bool is_space(char ch) {
+  return ch == ' ' || ch == '\t' || ch == '\r' || ch == '\v' || ch == '\f' ||
+         (ch >= '\x1c' && ch <= '\x1f');
+}
 
-// one number at p (Python float() spellings: digits, inf, nan, optional sign)
-const char* parse_num(const char* p, const char* end, double* out) {
-  while (p < end && is_space(*p)) ++p;
-  if (p >= end) return nullptr;
-  const bool neg = *p == '-';
-  const char* q = p + ((*p == '-' || *p == '+') ? 1 : 0);
-  double v = 0.0;
-  auto r = std::from_chars(q, end, v);
-  if (r.ec != std::errc() || r.ptr == q) {
-    // from_chars reports out-of-range values as errors; Python reads them as 0 / inf
-    if (r.ec == std::errc::result_out_of_range) {
-      v = std::strtod(std::string(q, r.ptr).c_str(), nullptr);
-    } else {
-      return nullptr;
+bool is_digit(char ch) { return ch >= '0' && ch <= '9'; }
+
+bool ieq(const char* b, const char* e, const char* word) {
+  for (; b < e && *word; ++b, ++word)
+    if ((*b | 0x20) != *word) return false;
+  return b == e && !*word;
+}
+
+// Python float() of the token [b, e): an optional sign, then "inf", "infinity" or
+// "nan" in any case, or a decimal literal whose digit groups may hold single
+// underscores between digits (digits [. digits] [e [sign] digits], either side of the
+// point may be empty but not both).  Anything else (a second sign, "nan(...)", hex,
+// a misplaced underscore) is rejected as float() rejects it.
+bool py_float(const char* b, const char* e, double* out) {
+  if (b >= e) return false;
+  const bool neg = *b == '-';
+  if (*b == '-' || *b == '+') ++b;
+  if (b >= e) return false;
+  if (ieq(b, e, "inf") || ieq(b, e, "infinity")) {
+    *out = neg ? -HUGE_VAL : HUGE_VAL;
+    return true;
+  }
+  if (ieq(b, e, "nan")) {
+    *out = neg ? -NAN : NAN;
+    return true;
+  }
+  // grammar check; a digit group is digit (["_"] digit)*
+  bool under = false;
+  auto group = [&](const char*& p) {
+    if (p >= e || !is_digit(*p)) return false;
+    ++p;
+    while (p < e) {
+      if (is_digit(*p)) {
+        ++p;
+      } else if (*p == '_' && p + 1 < e && is_digit(p[1])) {
+        under = true;
+        p += 2;
+      } else {
+        break;
+      }
     }
+    return true;
+  };
+  const char* p = b;
+  const bool int_any = group(p);
+  bool frac_any = false;
+  if (p < e && *p == '.') {
+    ++p;
+    frac_any = group(p);
+  }
+  if (!int_any && !frac_any) return false;
+  if (p < e && (*p == 'e' || *p == 'E')) {
+    ++p;
+    if (p < e && (*p == '+' || *p == '-')) ++p;
+    if (!group(p)) return false;
+  }
+  if (p != e) return false;
+  std::string clean;
+  if (under) {
+    for (const char* c = b; c < e; ++c)
+      if (*c != '_') clean.push_back(*c);
+    b = clean.data();
+    e = b + clean.size();
+  }
+  double v = 0.0;
+  const auto r = std::from_chars(b, e, v);
+  if (r.ptr != e) return false;
+  if (r.ec == std::errc::result_out_of_range) {
+    // Python reads out-of-range literals as 0 or inf
+    v = std::strtod(std::string(b, e).c_str(), nullptr);
+  } else if (r.ec != std::errc()) {
+    return false;
   }
   *out = neg ? -v : v;
-  return r.ptr;
+  return true;
+}
+
+// the next whitespace-separated token of the line at p (nullptr: none before the
+// line's end) parsed as Python's float() does; returns the end of the token
+const char* parse_num(const char* p, const char* end, double* out, bool* ok) {
+  while (p < end && is_space(*p)) ++p;
+  if (p >= end || *p == '\n') return nullptr;
+  const char* q = p;
+  while (q < end && !is_space(*q) && *q != '\n') ++q;
+  *ok = py_float(p, q, out);
+  return q;
 }
 
 }  // namespace
@@ -190,9 +262,10 @@ extern "C" int sbe_backup_parse(const char* text, long long len, double* values,
   auto parse = [&](int t) {
     const char* p = cut[t];
     for (long long i = first[t]; i < std::min(first[t + 1], count); ++i) {
-      const char* q = parse_num(p, cut[t + 1], &values[2 * i]);
-      if (q) q = parse_num(q, cut[t + 1], &values[2 * i + 1]);
-      if (!q || (q < cut[t + 1] && !is_space(*q) && *q != '\n')) {
+      bool ok0 = false, ok1 = false;
+      const char* q = parse_num(p, cut[t + 1], &values[2 * i], &ok0);
+      if (q) q = parse_num(q, cut[t + 1], &values[2 * i + 1], &ok1);
+      if (!q || !ok0 || !ok1) {
         bad[t] = i;
         return;
       }

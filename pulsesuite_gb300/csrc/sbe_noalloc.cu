@@ -12,17 +12,18 @@
 // Nr <= SBE_NOALLOC_MAX_NR (2050 wire points, Nk <= 1024).  Larger calls are
 // rejected with SBE_ERR_ARG / SBE_ERR_UNSUPPORTED before anything is launched.
 //
-// The scratch is one array per device shared by every caller: two calls whose
-// kernels overlap in time (different streams, threads or contexts on the same
-// device) race on it and give wrong results.  Calls on one stream are ordered and
-// safe.  No element of the scratch needs to start at zero: every element a kernel
-// reads was written earlier in the same call.
+// The scratch is one array per CUDA context: every context that loads this library
+// on a device holds its own copy of the module and so of the array, until the
+// context is destroyed or the process exits.  All calls made in one context share
+// that array: two calls whose kernels overlap in time (different streams or host
+// threads of the same context) race on it and give wrong results.  Calls on one
+// stream are ordered and safe.  No element of the scratch needs to start at zero:
+// every element a kernel reads was written earlier in the same call.
 //
-// The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (this may load the library's device code on that device);
-// make that first call before any stream capture.
-
-#include <mutex>
+// Every call looks up the array's device address in the calling thread's current
+// context with cudaGetSymbolAddress, so nothing is cached that a destroyed or reset
+// context could leave stale.  The first call in a context may load the library's
+// device code into it; make that first call before any stream capture.
 
 #include "sbe_ctx.cuh"
 
@@ -36,27 +37,14 @@ constexpr long long kTmpElems = 4LL * kMaxNr;      // 4 resampled fields on the 
 // 1.70 MB of complex128 scratch: spline coefficients, then the windowed fields.
 static __device__ __align__(256) double2 g_prop2qw_scratch[kCoefElems + kTmpElems];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_lock;
-double2* g_ptr[kMaxDevices] = {};
-
-// Device address of the scratch on the current device (looked up once per device).
+// Device address of the scratch in the current context (looked up on every call).
 int scratch_ptr(double2** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return sbe::cuda_check(e, "sbe_prop2qw_noalloc: cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices)
-    return sbe::fail(SBE_ERR_UNSUPPORTED, "sbe_prop2qw_noalloc: device ordinal out of range");
-  std::lock_guard<std::mutex> guard(g_lock);
-  if (!g_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_prop2qw_scratch);
-    if (e != cudaSuccess || !p)
-      return sbe::cuda_check(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
-                             "sbe_prop2qw_noalloc: cudaGetSymbolAddress");
-    g_ptr[dev] = static_cast<double2*>(p);
-  }
-  *out = g_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_prop2qw_scratch);
+  if (e != cudaSuccess || !p)
+    return sbe::cuda_check(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                           "sbe_prop2qw_noalloc: cudaGetSymbolAddress");
+  *out = static_cast<double2*>(p);
   return SBE_OK;
 }
 

@@ -78,6 +78,32 @@ def test_parse_spellings_and_errors(lib):
         lib.backup_parse(b"1x 2\n", 1)
 
 
+ODD_TOKENS = ["+-1", "-+1", "--1", "++1", "1_0", "1__0", "_1", "1_", "1_.5", "1._5", "1.5_",
+              "1e1_0", "1e_10", "1_0e-1_1", ".5", "5.", ".", "-.", "1.e5", ".e5", "e5", "1e",
+              "1e+", "INF", "-Infinity", "+nan", "-NaN", "nan(1)", "infin", "infinityx",
+              "0x1p3", "1.5x", "0_0.0_0", "00012", "1e400", "-1e-400", "1E5", "+.5e-3"]
+
+
+@pytest.mark.parametrize("tok", ODD_TOKENS)
+def test_parse_accepts_what_python_float_accepts(lib, tok):
+    """read_sbes_data reads each number with Python float(): every odd ASCII spelling
+    is accepted or refused as float() does, with the same value when accepted (float()
+    also takes non-ASCII decimal digits, which the library's reader refuses)."""
+    text = f"{tok} 2\n".encode()
+    try:
+        want = float(tok)
+    except ValueError:
+        with pytest.raises(lib.SbeError, match="line 1"):
+            lib.backup_parse(text, 1)
+        return
+    got = lib.backup_parse(text, 1)[0]
+    w = want + 2j
+    if np.isnan(want):
+        assert np.isnan(got.real) and got.imag == 2.0
+    else:
+        assert _bits(np.array([got])).tolist() == _bits(np.array([w])).tolist()
+
+
 def test_large_level_round_trip(lib):
     """A 32-wire Nk = 256 level: threaded write then read gives the values back."""
     rng = np.random.default_rng(1)
