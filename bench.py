@@ -148,7 +148,7 @@ def reference_arm(args, wl):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(wl, "reference"),
+            "config": config_of(wl),
             "cpu_baseline": {"value": v, "unit": "wire-steps/s", "cores": os.cpu_count(),
                              "kind": "port",
                              "sample": f"one wire of the {wl['nw']}-wire batch, Nk={wl['nk']}, "
@@ -159,7 +159,7 @@ def reference_arm(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def config_of(wl, impl):
+def config_of(wl):
     return {"workload": f"{wl['nw']} wires x Nk={wl['nk']} GaAs-like quantum wires every "
                         f"{wl['spacing']*1e9:.0f} nm on a 1-D PSTD grid Nx={wl['nx']} "
                         f"dx={wl['dx']*1e9:.0f} nm, pulse E0={wl['E0']:.0e} V/m "
@@ -168,8 +168,7 @@ def config_of(wl, impl):
             "wires": wl["nw"], "nk": wl["nk"], "nr": 2 * wl["nk"] + 2, "nx": wl["nx"],
             "flags": " ".join(k for k, v in FLAGS.items() if v),
             "integrator": "RK4 (coefficients frozen per step) + reference relaxation/normalisation",
-            "l2": "inputs larger than L2 (FP64 state 403 MB, FP16 operand planes 1.9 GB per stage)",
-            "impl": impl}
+            "l2": "inputs larger than L2 (FP64 state 403 MB, FP16 operand planes 1.9 GB per stage)"}
 
 
 # ---------------------------------------------------------------------------
@@ -411,7 +410,9 @@ def gpu_arm(args, wl):
             "avg_launch_ms": comm_ms / max(comm_n, 1),
             "traffic": TRAFFIC_PER_EVAL_WIRE * nw,
             "traffic_note": "DRAM read+write bytes of the commutator launches of one RHS "
-                            "evaluation (ncu, 8-wire case, scaled by wires)",
+                            "evaluation: dram__bytes_read.sum + dram__bytes_write.sum of an ncu "
+                            "capture of the 8-wire case (profiles/k_tc_gemm_multiwire_nk512.md), "
+                            "scaled by wires; a constant of this file, refreshed with the profile",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
                            "12 complex Nk^3 products) over the summed CUDA-event time of the "
                            "evaluation's two commutator launches (dP with the hi*lo + lo*hi "
@@ -434,7 +435,7 @@ def gpu_arm(args, wl):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
-                "data": "synthetic", "config": config_of(wl, args.precision),
+                "data": "synthetic", "config": config_of(wl), "precision": args.precision,
                 "clocks": clk,
                 "e2e": {"value": e2e_val, "unit": "wire-steps/s",
                         "h2d_bytes_per_step": int(3 * nx * 16),
@@ -462,7 +463,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS))
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--ehs", action="store_true",

@@ -38,6 +38,9 @@ qwoptics_nkN    ``qwoptics.QWOptics`` polarisation/charge sources, ``Prop2QW``
                 and ``QW2Prop`` (cubic-spline resampling + FFTG).
 solver_step     ``SBEs.SBESolver`` built from params files, several
                 ``QWCalculator`` leapfrog steps on two wires.
+solver_100      the same solver run for 100 leapfrog steps: the fields of every step,
+                the sources of every tenth step and the nine state levels at the end;
+                ``make_golden.py <src> solver100`` writes it alone.
 pstd            Pieces of the field step: ``usefulsubs.dfdx1D`` on FFT-order
                 wavenumbers (``libpulsesuite.helpers.GetKArray``), the grids of
                 ``typespace`` and ``helpers``, and ``rhoPJ.ElongfromRho`` on an
@@ -600,6 +603,51 @@ def case_solver(L, nsteps, dt, E0, seed):
     return out
 
 
+def case_solver100(L, nsteps, dt, E0, seed):
+    """nsteps reference leapfrog steps (SBESolver + QWCalculator, two wires): fields of
+    every step (real, along rr), sources of every tenth step and the last, and the nine
+    state levels after the last step."""
+    from pulsesuite.PSTD3D import SBEs
+    rng = np.random.default_rng(seed)
+    os.makedirs("params", exist_ok=True)
+    with open("params/qw.params", "w") as f:
+        f.write(QW_PARAMS.format(L=repr(L)))
+    with open("params/mb.params", "w") as f:
+        f.write(MB_PARAMS)
+    nrr = 64
+    rr = np.linspace(-1.25 * L, 1.25 * L, nrr)
+    qrr = np.zeros(nrr)
+    s = SBEs.SBESolver(qrr, rr, 0.0, E0, 800e-9, 2, True)
+    nk = s.Nk
+    for w in range(2):
+        for arr in (s.YY1, s.YY2, s.YY3):
+            arr[:, :, w] = cnormal(rng, (nk, nk), 1e-3)
+        for arr in (s.CC1, s.CC2, s.CC3, s.DD1, s.DD2, s.DD3):
+            arr[:, :, w] = herm_state(rng, nk, 0.05)
+    out = dict(L=L, dt=dt, E0=E0, rr=rr, nk=nk, nsteps=nsteps)
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        out[f"init_{nm}"] = getattr(s, nm).copy()
+    amp = rng.uniform(0.5, 1.5, (nsteps, 3, 2))
+    fields = np.empty((nsteps, 3, nrr))
+    for n in range(nsteps):
+        for c in range(3):
+            fields[n, c] = E0 * amp[n, c, 0] * np.cos(2 * np.pi * rr / (3 * L) + amp[n, c, 1])
+    out["fields"] = fields
+    for n in range(nsteps):
+        Exx, Eyy, Ezz = (fields[n, c] + 0j for c in range(3))
+        Vrr = np.zeros(nrr, complex)
+        for w in (1, 2):
+            srcs = [np.zeros(nrr, complex) for _ in range(4)]
+            s.QWCalculator(Exx, Eyy, Ezz, Vrr, rr, qrr, dt, w, *srcs, [True], [False])
+            if n % 10 == 9 or n == nsteps - 1:
+                for a, nm in zip(srcs, ("Pxx", "Pyy", "Pzz", "Rho")):
+                    out[f"s{n}_w{w}_{nm}"] = a
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        out[f"end_{nm}"] = getattr(s, nm).copy()
+    s.close()
+    return out
+
+
 def case_pstd(nx, dx, seed):
     from pulsesuite.PSTD3D import rhoPJ, typespace, usefulsubs
     from pulsesuite.libpulsesuite import helpers
@@ -660,7 +708,11 @@ def main():
                 if only in (None, "backup"):
                     np.savez_compressed(os.path.join(HERE, "backup_nk6.npz"),
                                         **case_backup(6, 2, 700))
-                if only in ("mbc", "emission", "dc", "backup", "info", "coupling3d"):
+                if only in (None, "solver100"):
+                    np.savez_compressed(os.path.join(HERE, "solver_100.npz"),
+                                        **case_solver100(14.5e-9, 100, 0.1e-15, 2e7, 41))
+                if only in ("mbc", "emission", "dc", "backup", "info", "coupling3d",
+                            "solver100"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

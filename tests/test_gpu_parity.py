@@ -208,6 +208,36 @@ def test_solver_leapfrog_vs_golden(tmp_path, monkeypatch):
     s.close()
 
 
+def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch):
+    """100 reference QWCalculator steps on two wires (SBESolver drop-in, FP64 path):
+    the sources of every tenth step and the nine state levels at the end <= 1e-10."""
+    from pulsesuite_gb300 import SBEs
+    monkeypatch.chdir(tmp_path)
+    g = golden("solver_100")
+    prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
+               mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
+               epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR, Edc=0.0,
+               jmax=100000, ntmax=100000)
+    rr, f = g["rr"], g["fields"]
+    s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
+                       flags=SOLVER_FLAGS)
+    assert s.Nk == int(g["nk"])
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        setattr(s, nm, g["init_" + nm])
+    dt = float(g["dt"])
+    for n in range(int(g["nsteps"])):
+        for w in (1, 2):
+            outs = [np.zeros(len(rr), complex) for _ in range(4)]
+            s.QWCalculator(f[n, 0] + 0j, f[n, 1] + 0j, f[n, 2] + 0j, np.zeros(len(rr), complex),
+                           rr, None, dt, w, *outs, [False], [False])
+            if f"s{n}_w{w}_Pxx" in g:
+                for a, nm in zip(outs, ("Pxx", "Pyy", "Pzz", "Rho")):
+                    assert rel(a, g[f"s{n}_w{w}_{nm}"]) < SCREEN, (n, w, nm)
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        assert rel(getattr(s, nm), g[f"end_{nm}"]) < SCREEN, nm
+    s.close()
+
+
 def _seeded_state(rng, nk):
     z = rng.standard_normal((nk, nk)) + 1j * rng.standard_normal((nk, nk))
     q, _ = np.linalg.qr(z)

@@ -222,6 +222,29 @@ def test_solver_leapfrog_steps():
             assert rel(getattr(s, nm), g[f"s{n}_{nm}"]) < 1e-14, (n, nm)
 
 
+def test_solver_leapfrog_100_steps():
+    """100 QWCalculator steps on two wires: sources of every tenth step and the nine
+    state levels at the end (the reference scheme over a long run)."""
+    g = golden("solver_100")
+    L = float(g["L"])
+    nk = O.grid_from_params(L, SOLVER_PARAMS["gap"], SOLVER_PARAMS["me"])
+    assert nk == int(g["nk"])
+    s = O.Solver(nk, L, SOLVER_PARAMS, SOLVER_FLAGS, 2, float(g["E0"]))
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        setattr(s, nm, g["init_" + nm].copy())
+    rr, dt, f = g["rr"], float(g["dt"]), g["fields"]
+    nsteps = int(g["nsteps"])
+    for n in range(nsteps):
+        for w in (1, 2):
+            out = s.qw_calculator(f[n, 0] + 0j, f[n, 1] + 0j, f[n, 2] + 0j,
+                                  np.zeros(len(rr), complex), rr, dt, w)
+            if f"s{n}_w{w}_Pxx" in g:
+                for a, nm in zip(out, ("Pxx", "Pyy", "Pzz", "Rho")):
+                    assert rel(a, g[f"s{n}_w{w}_{nm}"]) < 1e-12, (n, w, nm)
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        assert rel(getattr(s, nm), g[f"end_{nm}"]) < 1e-12, nm
+
+
 def test_constants_match_scipy():
     sc = pytest.importorskip("scipy.constants")
     assert O.HBAR == sc.hbar and O.E0 == sc.e and O.KB == sc.k
