@@ -59,6 +59,13 @@ WORKLOADS = {
                       abc=0.05, x_src=-2.5e-6),
 }
 
+# Uneven sweep of independent wires in a local field: 512 wires drawn with
+# numpy default_rng(3): Nk from {64, 96, 128, 192, 256, 384, 512} with weights
+# proportional to 1/Nk, E0 log-uniform in [1e5, 1e8] V/m, detuning hbar w0 - Eg
+# uniform in [-30, 100] meV, tau uniform in [30, 300] fs, T uniform in [10, 300] K;
+# RK4 dt = 0.1 fs; each wire's pulse peaks at t = 2 tau from t = 0.
+SWEEP = dict(nw=512, nks=(64, 96, 128, 192, 256, 384, 512), kmax=3e9, dt=0.1e-15, seed=3)
+
 MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta0=6e-9,
            gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9, Oph=36e-3 * E0C / HBAR,
            Gph=3e-3 * E0C / HBAR)
@@ -137,9 +144,84 @@ def cpu_wire_steps(wl, nsteps, warm):
     return times[warm:]
 
 
+def sweep_wires():
+    """Per-wire Nk, E0 (V/m), detuning (J), tau (s) and T (K) of the sweep workload."""
+    rng = np.random.default_rng(SWEEP["seed"])
+    nks = np.array(SWEEP["nks"])
+    p = (1.0 / nks) / np.sum(1.0 / nks)
+    n = SWEEP["nw"]
+    nk = rng.choice(nks, size=n, p=p)
+    E0 = 10.0 ** rng.uniform(5.0, 8.0, n)
+    det = rng.uniform(-30e-3, 100e-3, n) * E0C
+    tau = rng.uniform(30e-15, 300e-15, n)
+    temp = rng.uniform(10.0, 300.0, n)
+    return nk, E0, det, tau, temp
+
+
+def sweep_fields(t, E0, det, tau):
+    """Local field of every wire at time t: E0 exp(-((t - 2 tau)/tau)^2) cos(w0 (t - 2 tau))."""
+    w0 = (MAT["gap"] + det) / HBAR
+    x = t - 2.0 * tau
+    return E0 * np.exp(-(x / tau) ** 2) * np.cos(w0 * x)
+
+
+def sweep_config():
+    nk, _, _, _, _ = sweep_wires()
+    counts = {int(k): int(np.sum(nk == k)) for k in SWEEP["nks"]}
+    return {"workload": f"{SWEEP['nw']} independent GaAs-like wires in a local field, Nk drawn "
+                        "from {64,96,128,192,256,384,512} with weights 1/Nk (default_rng(3)), "
+                        "E0 log-uniform 1e5-1e8 V/m, detuning U[-30,100] meV, tau U[30,300] fs, "
+                        "T U[10,300] K, RK4 dt=0.10 fs",
+            "wires": SWEEP["nw"], "nk_counts": counts,
+            "flags": " ".join(k for k, v in FLAGS.items() if v),
+            "integrator": "RK4 (coefficients frozen per step) + reference relaxation/normalisation",
+            "l2": "inputs larger than L2 (FP64 state %.0f MB)" %
+                  (3 * 16 * float(np.sum(nk.astype(float) ** 2)) / 1e6)}
+
+
+def cpu_sweep_rate():
+    """CPU wire-steps/s of the sweep from one timed oracle RK4 step of one wire of each Nk
+    (the wire-step time of the workload = sum over its wires of the time of their Nk)."""
+    from oracle import sbe_oracle as O
+    nk_all, E0, det, tau, temp = sweep_wires()
+    per_nk = {}
+    for nk in SWEEP["nks"]:
+        w = int(np.nonzero(nk_all == nk)[0][0])
+        L = wire_L(nk, SWEEP["kmax"])
+        wire = O.Wire(int(nk), L, MAT, FLAGS, float(temp[w]))
+        fe = O.fermi(wire.c["Ee"] + MAT["gap"] / 2.0, float(temp[w]))
+        P = np.zeros((nk, nk), complex)
+        C = np.diag(fe).astype(complex)
+        wk = O.fftg(wire.window)
+        z = np.zeros_like(wk)
+        e0 = sweep_fields(0.0, E0[w], det[w], tau[w])
+        t0 = time.perf_counter()
+        wire.rk4_step(P, C, C.copy(), [z, e0 * wk, z], [z, 0 * wk, z], SWEEP["dt"], 1)
+        per_nk[int(nk)] = time.perf_counter() - t0
+    total = float(sum(per_nk[int(k)] for k in nk_all))
+    return SWEEP["nw"] / total, per_nk
+
+
 def reference_arm(args, wl):
     rank, world, local = env()
     if rank != 0:
+        return
+    if wl is None:
+        v, per_nk = cpu_sweep_rate()
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "wire-steps/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * SWEEP["nw"] / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": sweep_config(),
+                "cpu_baseline": {"value": v, "unit": "wire-steps/s", "cores": os.cpu_count(),
+                                 "kind": "port",
+                                 "sample": "one RK4 step of one wire of each Nk (NumPy FP64 "
+                                           "restatement), summed over the workload's wires: "
+                                           + ", ".join(f"Nk={k}: {t:.3f} s"
+                                                       for k, t in per_nk.items())},
+                "e2e": {"value": v, "unit": "wire-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     times = cpu_wire_steps(wl, args.steps, args.warmup)
     tot = sum(times)
@@ -260,6 +342,9 @@ def gpu_arm(args, wl):
                                           w0=w0_of(wl), tpeak=0.0),
                        t0=t_start, longitudinal=True)
     E0h, H0h = incident_state(wl, x, x_src, t_start, dt)
+    # GEMM tiles of the mixed path from the autotuner (cached per device and shape)
+    cache = args.tile_cache or os.path.join(tempfile.gettempdir(), "sbe_tiles.json")
+    tiles = ctx.autotune(cache) if prec == _lib.PREC_MIXED else []
 
     fe = 1.0 / (np.exp((ctx.table(0, "Ee").cpu().numpy() + MAT["gap"] / 2.0) / 1.380649e-23
                        / wl["temp"]) + 1.0)
@@ -443,12 +528,192 @@ def gpu_arm(args, wl):
                 "gpu_launches": int(n_kernels * args.steps),
                 "gpu_launches_per_step": int(n_kernels),
                 "graph_replay_ms_per_step": graph_ms,
-                "roofline": roof, "other_kernels": other,
+                "roofline": roof, "other_kernels": other, "tiles": tiles,
                 "fp64_gpu": {"value": fp64_val, "unit": "wire-steps/s", "ms_per_step": fp64_ms,
                              "steps": n64},
                 "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
                 "rhs_rel_err_vs_fp64": rhs_err,
                 "wire_field_peak_k": field_peak,
+                "cpu_baseline": cpu}
+    print(json.dumps(line_out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def sweep_arm(args):
+    """The uneven sweep on the mixed path: one RK4 step of all 512 wires per step, the
+    GEMMs of all Nk buckets in one persistent launch per kind, tiles from the
+    autotuner."""
+    import torch
+    import __graft_entry__ as ge
+    rank, world, local = env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    ge.build()
+    from pulsesuite_gb300 import _lib
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk, E0, det, tau, temp = sweep_wires()
+    nw, dt = SWEEP["nw"], SWEEP["dt"]
+    specs = [WireSpec(nk=int(nk[w]), L=wire_L(int(nk[w]), SWEEP["kmax"]), temp=float(temp[w]),
+                      wire_index=w + 1, flags=dict(FLAGS), **MAT) for w in range(nw)]
+    t_ctx = time.perf_counter()
+    ctx = WireContext(specs)
+    t_ctx = time.perf_counter() - t_ctx
+    prec = _lib.PREC_MIXED if args.precision == "mixed" else _lib.PREC_FP64
+    cache = args.tile_cache or os.path.join(tempfile.gettempdir(), "sbe_tiles.json")
+    t_tune = time.perf_counter()
+    tiles = ctx.autotune(cache) if prec == _lib.PREC_MIXED else []
+    t_tune = time.perf_counter() - t_tune
+
+    def fresh():
+        P = ctx.zeros_state()
+        ds = []
+        for w in range(nw):
+            Ee = ctx.table(w, "Ee").cpu().numpy()
+            x = np.minimum((Ee + MAT["gap"] / 2.0) / (1.380649e-23 * temp[w]), 700.0)
+            ds.append(np.diag(1.0 / (np.exp(x) + 1.0)).astype(complex))
+        return P, ctx.pack(ds), ctx.pack(ds)
+
+    nsteps = args.warmup + args.steps
+    # per-step field amplitudes of every wire (host), resident on the device for `value`
+    amps = np.stack([sweep_fields(n * dt, E0, det, tau) for n in range(nsteps + 1)])
+    e0_dev = torch.as_tensor(amps[:-1]).cuda()
+    de_dev = torch.as_tensor(amps[1:] - amps[:-1]).cuda()
+    P, C, D = fresh()
+    Ek0, dEk = ctx.zeros_r(3), ctx.zeros_r(3)
+    src = ctx.zeros_r(5)
+    ctx.rk4_step(P.clone(), C.clone(), D.clone(), Ek0, dEk, dt, src.clone(), prec)
+    graph = ctx.rk4_graph(P, C, D, Ek0, dEk, dt, src, prec)
+    for n in range(args.warmup):
+        ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
+        graph.launch()
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    for cat in range(4):
+        ctx.profile_read(cat)
+    clk_dir = os.environ.get("SBE_CLOCKS_DIR", tempfile.gettempdir())
+    clocks = ClockSampler(local, os.path.join(clk_dir, f"clocks_sweep_{rank}.csv"))
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record()
+    for n in range(args.warmup, nsteps):
+        ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
+        graph.launch()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    prof = {cat: ctx.profile_read(cat) for cat in range(4)}
+    ctx.profile(False)
+    ctx.check()
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * nw * args.steps / (ms / 1e3)
+
+    # end to end: the step's field amplitudes from pinned host memory, the wires'
+    # real-space sources (Px, Py, Pz, re, rh) back to pinned host memory every step
+    h_e0 = torch.as_tensor(amps[:-1]).pin_memory()
+    h_de = torch.as_tensor(amps[1:] - amps[:-1]).pin_memory()
+    d_e0 = torch.empty(nw, dtype=torch.float64, device="cuda")
+    d_de = torch.empty(nw, dtype=torch.float64, device="cuda")
+    h_src = torch.empty(src.numel(), dtype=torch.complex128).pin_memory()
+    torch.cuda.synchronize()
+    e0e = torch.cuda.Event(enable_timing=True)
+    e1e = torch.cuda.Event(enable_timing=True)
+    e0e.record()
+    for n in range(args.warmup, nsteps):
+        d_e0.copy_(h_e0[n], non_blocking=True)
+        d_de.copy_(h_de[n], non_blocking=True)
+        ctx.local_field(d_e0, d_de, 1, Ek0, dEk)
+        graph.launch()
+        h_src.copy_(src, non_blocking=True)
+    e1e.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0e.elapsed_time(e1e)
+    graph.close()
+
+    # RHS error against FP64 at the current state (every wire)
+    ctx.local_field(e0_dev[nsteps - 1], None, 1, Ek0, None)
+    r64 = ctx.rhs(P, C, D, Ek0, _lib.PREC_FP64)
+    rmx = ctx.rhs(P, C, D, Ek0, _lib.PREC_MIXED)
+    errs = []
+    for a, b in zip(rmx, r64):
+        for w in range(nw):
+            bw = ctx.mat(b, w)
+            nb = float(torch.linalg.norm(bw))
+            if nb > 0:
+                errs.append(float(torch.linalg.norm(ctx.mat(a, w) - bw)) / nb)
+    rhs_err = max(errs)
+
+    # the plain FP64 GPU path on the same wires and state
+    fp64_ms = fp64_val = None
+    if not args.no_fp64:
+        st64 = (P.clone(), C.clone(), D.clone())
+        s64 = ctx.zeros_r(5)
+        ctx.rk4_step(*st64, Ek0, dEk, dt, s64, _lib.PREC_FP64)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        n64 = max(1, args.fp64_steps)
+        f0.record()
+        for _ in range(n64):
+            ctx.rk4_step(*st64, Ek0, dEk, dt, s64, _lib.PREC_FP64)
+        f1.record()
+        torch.cuda.synchronize()
+        fp64_ms = f0.elapsed_time(f1) / n64
+        fp64_val = world * nw / (fp64_ms / 1e3)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, pk_kind = measured_peaks()
+    peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    sum_nk3 = float(np.sum(nk.astype(float) ** 3))
+    comm_ms, comm_n = prof[0]
+    per_eval_s = comm_ms / (4 * args.steps) / 1e3
+    achieved = 96.0 * sum_nk3 / per_eval_s / 1e12
+    step_tflops = 496.0 * sum_nk3 * (args.steps / (ms / 1e3)) / 1e12
+    cpu = None
+    if not args.no_cpu:
+        v, per_nk = cpu_sweep_rate()
+        cpu = {"value": v, "unit": "wire-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one RK4 step of one wire of each Nk (NumPy FP64 restatement), summed "
+                         "over the workload's wires"}
+    line_out = {"metric": METRIC, "value": value, "unit": "wire-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
+                "data": "synthetic", "config": sweep_config(), "precision": args.precision,
+                "clocks": clk,
+                "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
+                        "h2d_bytes_per_step": int(2 * 8 * nw),
+                        "d2h_bytes_per_step": int(src.numel() * 16)},
+                "gpu_launches_per_step": None,
+                "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)",
+                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                             "frac": achieved / peak,
+                             "peak_kind": f"{pk_kind} bf16 dense sustained",
+                             "ms_per_rhs_eval": per_eval_s * 1e3, "launches": comm_n,
+                             "traffic": None,
+                             "step_tflops": step_tflops, "step_frac": step_tflops / peak,
+                             "flops_model": "96*sum(Nk^3) per RHS evaluation over the commutator "
+                                            "launches; step: 496*sum(Nk^3) per step"},
+                "other_kernels": {name: {"ms_per_step": prof[c][0] / args.steps,
+                                         "launches": prof[c][1]}
+                                  for c, name in ((1, "exchange_gemm"), (2, "source_gemm"),
+                                                  (3, "dephasing_fp32"))},
+                "tiles": tiles, "autotune_s": t_tune, "ctx_create_s": t_ctx,
+                "fp64_gpu": {"value": fp64_val, "unit": "wire-steps/s", "ms_per_step": fp64_ms},
+                "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
+                "rhs_rel_err_vs_fp64": rhs_err,
                 "cpu_baseline": cpu}
     print(json.dumps(line_out), flush=True)
     if dist:
@@ -462,7 +727,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS) + ["sweep"])
+    ap.add_argument("--tile-cache", default=None,
+                    help="JSON tile cache of the autotuner (default: in the temp directory)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -472,9 +739,11 @@ def main():
     args = ap.parse_args()
     if args.ehs:
         FLAGS["EHs"] = True
-    wl = WORKLOADS[args.workload]
+    wl = WORKLOADS.get(args.workload)
     if args.impl == "reference":
         reference_arm(args, wl)
+    elif wl is None:
+        sweep_arm(args)
     else:
         gpu_arm(args, wl)
 

@@ -81,7 +81,9 @@ int sbe_constants(double* out5);
  * InitializeDephasing (dephasing.py:472), QWOptics (qwoptics.py:575).        */
 int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx** out);
 int sbe_ctx_destroy(SbeCtx* ctx);
-/* Per-wire sizes/offsets (elements) of the packed state: out[3*w+0] = Nk,
+/* The packed buffers group the wires by Nk (ascending; the caller's order within
+ * one Nk), so that the wires of one Nk are contiguous (the mixed path's buckets).
+ * Per-wire sizes/offsets (elements) of the packed state: out[3*w+0] = Nk,
  * out[3*w+1] = offset of wire w's Nk*Nk block, out[3*w+2] = offset of its Nr block. */
 int sbe_ctx_layout(const SbeCtx* ctx, long long* out, long long* total_mat, long long* total_r);
 /* Copy one table of wire w into dst (device). which: 0 kr, 1 r, 2 Ee, 3 Eh,
@@ -195,9 +197,18 @@ int sbe_leapfrog_step(SbeCtx* ctx, double* const* state9, const double* Ek, doub
  * wire; stage fields Ek0 + c dEk).  Relaxation, charge normalisation and the
  * sources of the new state follow (as in the reference step).  precision:
  * SBE_PREC_FP64 or SBE_PREC_MIXED (SBE_ERR_UNSUPPORTED for a context with
- * SBE_F_DCTRANS: the reference's transport leaves C, D non-Hermitian).        */
+ * SBE_F_DCTRANS: the reference's transport leaves C, D non-Hermitian; the mixed
+ * path also needs one flag set over the context and every Nk a multiple of 8; the
+ * Nk may differ between wires).                                                */
 int sbe_rk4_step(SbeCtx* ctx, double* P, double* C, double* D, const double* Ek0,
                  const double* dEk, double dt, int precision, double* src_out, void* stream);
+/* A local field uniform along every wire (the local-field drivers of the reference,
+ * sbetestprop.py:184-198, whose Prop2QW of a constant field is E FFTG(window),
+ * qwoptics.py:667-715): component comp (0 x, 1 y, 2 z) of wire w's Ek0 is e0[w]
+ * FFTG(window_w), the others 0; dEk (may be NULL) likewise from de.  e0, de:
+ * device arrays of one amplitude (V/m) per wire, in the caller's wire order.     */
+int sbe_local_field(SbeCtx* ctx, const double* e0, const double* de, int comp, double* Ek0,
+                    double* dEk, void* stream);
 /* The coherent RHS of every wire at the given state/field (preparation included),
  * for parity checks.                                                           */
 int sbe_rhs(SbeCtx* ctx, const double* P, const double* C, const double* D, const double* Ek,
@@ -215,6 +226,21 @@ int sbe_rk4_graph_create(SbeCtx* ctx, double* P, double* C, double* D, const dou
                          SbeGraph** out, long long* n_kernels);
 int sbe_graph_launch(SbeGraph* g, void* stream);
 int sbe_graph_destroy(SbeGraph* g);
+
+/* ---- tile autotuner of the mixed path (no counterpart in the reference) ------
+ * The reference runs its wires one after another (rhoPJ.py:306-343,
+ * sbetestprop.py:204-209); here the wires of one Nk form a bucket and each GEMM
+ * kind of a stage runs as one persistent launch over all buckets.  sbe_autotune
+ * chooses, per bucket, the N tile (256 or 128) of the exchange, commutator and
+ * source GEMMs by timing both on the context's workspace, and caches the choice in
+ * the JSON file cache_json (NULL: no cache) under a key of the device and the
+ * context's (Nk, wires) buckets: a later call with a matching entry loads it and
+ * times nothing.  Without a call every GEMM uses the 256 tile.  Synchronises the
+ * device; not capturable.  sbe_ctx_tiles: per bucket (ascending Nk) 5 ints
+ * (Nk, wires, exchange tile, commutator tile, source tile) into out (cap ints);
+ * *nbuckets = 0 before the mixed workspace exists.                              */
+int sbe_autotune(SbeCtx* ctx, const char* cache_json);
+int sbe_ctx_tiles(const SbeCtx* ctx, int* out, int cap, int* nbuckets);
 
 /* ---- 1-D PSTD field grid --------------------------------------------------------
  * The reference has no 1-D Maxwell stepper; these entries assemble its pieces:

@@ -210,3 +210,82 @@ class CoupledLine:
             Ex = elong(rho, Pg[0], self.p.q, self.p.epsr)
         self.n += 1
         return E, H, Ex, srcs
+
+
+# ---------------------------------------------------------------------------
+# 3-D grid (six field components on nx x ny x nz, C order, z fastest)
+
+
+def elong3d(rho, Px, Py, Pz, qx, qy, qz, epsr):
+    """rhoPJ.py:703-880 ElongfromRho on a 3-D grid, with the wavenumber tables the
+    caller passes (the reference passes its centred GetKxArray/GetKyArray/GetKzArray,
+    typespace.py:958-1030): small = (qx[1] - qx[0]) / 1e4 (:779); in k space
+    rho_B = -i q.P, rho_term = -i rho / (eps (q^2 + small)), P_term = -(q.P) / (eps
+    (q^2 + small)); the nine fields (rho + P, P, rho) x q_c and rho_B back in real space.
+    Returns (E_PRho (3,..), E_P (3,..), E_Rho (3,..), RhoBound, P_k (3,..)), P_k being
+    the transformed P that the reference leaves in its input arrays."""
+    small = (qx[1] - qx[0]) / 1e4
+    inv_eps = 1.0 / (EPS0 * epsr)
+    rk = np.fft.fftn(np.asarray(rho, complex))
+    pk = [np.fft.fftn(np.asarray(p, complex)) for p in (Px, Py, Pz)]
+    QX, QY, QZ = np.meshgrid(qx, qy, qz, indexing="ij")
+    qs = QX ** 2 + QY ** 2 + QZ ** 2 + small
+    qdotp = QX * pk[0] + QY * pk[1] + QZ * pk[2]
+    rho_b = -1j * qdotp
+    rho_term = -1j * rk * inv_eps / qs
+    p_term = -qdotp * inv_eps / qs
+    q3 = (QX, QY, QZ)
+    e_prho = np.stack([np.fft.ifftn((rho_term + p_term) * q) for q in q3])
+    e_p = np.stack([np.fft.ifftn(p_term * q) for q in q3])
+    e_rho = np.stack([np.fft.ifftn(rho_term * q) for q in q3])
+    return e_prho, e_p, e_rho, np.fft.ifftn(rho_b), np.stack(pk)
+
+
+def abc_mask3(n, n_abc, strength):
+    """Absorbing mask of a 3-D grid: the 1-D mask of each axis multiplied together
+    (ApplyABC multiplies the field by the mask, usefulsubs.py:584-609)."""
+    m = [abc_mask(nn, na, strength) for nn, na in zip(n, n_abc)]
+    return m[0][:, None, None] * m[1][None, :, None] * m[2][None, None, :]
+
+
+class Pstd3D:
+    """Field state E = (Ex, Ey, Ez), H = (Hx, Hy, Hz), each (3, nx, ny, nz) complex.
+    Leapfrog of the curl equations with spectral derivatives (the q-space derivative
+    f (i q) of usefulsubs.py:233-380 along each axis): H^{n+1/2} = H^{n-1/2} - dt/mu0
+    curl E^n, E^{n+1} = mask (E^n + dt/eps (curl H^{n+1/2} - J))."""
+
+    def __init__(self, n, d, epsr, n_abc=(0, 0, 0), strength=0.0):
+        self.n, self.d, self.epsr = tuple(n), tuple(d), epsr
+        grids = [pstd_grid(nn, dd) for nn, dd in zip(n, d)]
+        self.x = [g[0] for g in grids]
+        self.q = [g[1] for g in grids]
+        self.mask = abc_mask3(n, n_abc, strength)
+        self.masked = any(a > 0 for a in n_abc)
+        self.Q = np.meshgrid(*self.q, indexing="ij")
+
+    def curl(self, F):
+        fk = [np.fft.fftn(F[c]) for c in range(3)]
+        qx, qy, qz = self.Q
+        ck = [1j * (qy * fk[2] - qz * fk[1]), 1j * (qz * fk[0] - qx * fk[2]),
+              1j * (qx * fk[1] - qy * fk[0])]
+        return np.stack([np.fft.ifftn(c) for c in ck])
+
+    def update_h(self, E, H, dt):
+        H = H - (dt / MU0) * self.curl(E)
+        return H * self.mask if self.masked else H
+
+    def update_e(self, E, H, J, dt):
+        ie = dt / (EPS0 * self.epsr)
+        E = E + ie * self.curl(H)
+        if J is not None:
+            E = E - ie * J
+        return E * self.mask if self.masked else E
+
+    def step(self, E, H, J, dt):
+        H = self.update_h(E, H, dt)
+        return self.update_e(E, H, J, dt), H
+
+    def energy(self, E, H_prev, H_next):
+        e = EPS0 * self.epsr * np.sum(np.abs(E) ** 2)
+        h = MU0 * np.sum(np.real(H_prev * np.conj(H_next)))
+        return e + h

@@ -38,7 +38,8 @@ EXPORTS = (
     "sbe_couple_sample",
     "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
     "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info", "sbe_calc_jfx",
-    "sbe_qw_placement", "sbe_e_at_xyz",
+    "sbe_qw_placement", "sbe_e_at_xyz", "sbe_autotune", "sbe_ctx_tiles",
+    "sbe_local_field",
 )
 
 
@@ -139,6 +140,9 @@ def load(path=LIB_PATH):
         "sbe_couple_deposit": [P, P],
         "sbe_couple_step": [P, P, P, P, P, P, P, Dbl, I, P],
         "sbe_couple_graph_create": [P, P, P, P, P, P, P, Dbl, I, P, P],
+        "sbe_autotune": [P, ctypes.c_char_p],
+        "sbe_local_field": [P, P, P, I, P, P, P],
+        "sbe_ctx_tiles": [P, P, I, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

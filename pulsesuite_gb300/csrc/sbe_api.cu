@@ -1,5 +1,6 @@
 // C ABI of libsbe_gb300: context management and the entry points declared in
 // include/sbe_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -99,7 +100,6 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   SbeCtx* c = new SbeCtx();
   c->nw = n_wires;
   c->desc.assign(wires, wires + n_wires);
-  long long om = 0, ov = 0, orr = 0, odd = 0, okr = 0;
   for (int w = 0; w < n_wires; ++w) {
     const SbeWireDesc& d = wires[w];
     if (d.nk < 4 || d.nk > 4096 || !(d.L > 0) || !(d.me > 0) || !(d.mh > 0) || !(d.HO > 0) ||
@@ -114,21 +114,32 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
                       std::to_string(w) + ")");
     }
     WireDev W = derive(d);
+    W.off_tab = w;
+    c->nk_max = std::max(c->nk_max, W.nk);
+    c->nr_max = std::max(c->nr_max, W.nr);
+    if (d.flags & SBE_F_OFFDIAGDPH) c->any_offdiag = 1;
+    c->wires.push_back(W);
+  }
+  // packed layout: wires grouped by Nk (ascending, stable), so that the wires of one
+  // Nk are one contiguous block of every packed buffer (the mixed path's buckets);
+  // a context of one Nk keeps the order of its wires
+  c->order.resize(n_wires);
+  for (int w = 0; w < n_wires; ++w) c->order[w] = w;
+  std::stable_sort(c->order.begin(), c->order.end(),
+                   [&](int a, int b) { return c->wires[a].nk < c->wires[b].nk; });
+  long long om = 0, ov = 0, orr = 0, odd = 0, okr = 0;
+  for (int w : c->order) {
+    WireDev& W = c->wires[w];
     W.off_mat = om;
     W.off_vec = ov;
     W.off_r = orr;
     W.off_dd = odd;
     W.off_kr = okr;
-    W.off_tab = w;
     om += (long long)W.nk * W.nk;
     ov += W.nk;
     orr += W.nr;
     odd += (long long)(2 * W.nk + 1) * W.nk;
     okr += (long long)W.nk * W.nr;
-    c->nk_max = std::max(c->nk_max, W.nk);
-    c->nr_max = std::max(c->nr_max, W.nr);
-    if (d.flags & SBE_F_OFFDIAGDPH) c->any_offdiag = 1;
-    c->wires.push_back(W);
   }
   c->tot_mat = om;
   c->tot_vec = ov;
@@ -696,6 +707,36 @@ int sbe_rk4_step(SbeCtx* c, double* P, double* C, double* D, const double* Ek0, 
   launch_relax_norm(c, p, cc, d, (const double2*)Ek0, dt, s);
   launch_sources(c, p, cc, d, c->ne, c->nh, (double2*)src_out, s);
   return cuda_check(cudaGetLastError(), "sbe_rk4_step");
+}
+
+// ---- local field ---------------------------------------------------------------
+// A field uniform along every wire (the local-field drivers, sbetestprop.py:184-198)
+// in wire k space: Prop2QW of a constant E is E FFTG(window) (qwoptics.py:667-715 with
+// the spline of a constant), so component comp of wire w is e0[w] wk[w] and the
+// other two are 0; dEk likewise from de.  One thread per (r, component, wire).
+__global__ void k_local_field(const WireDev* wires, const double2* wk, const double* e0,
+                              const double* de, int comp, double2* Ek0, double2* dEk) {
+  const WireDev W = wires[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * W.nr) return;
+  const int f = i / W.nr, r = i - f * W.nr;
+  const double2 v = f == comp ? wk[W.off_r + r] : make_double2(0.0, 0.0);
+  const long long o = 3 * W.off_r + i;
+  const double a = e0[blockIdx.y];
+  Ek0[o] = make_double2(a * v.x, a * v.y);
+  if (dEk) {
+    const double b = de[blockIdx.y];
+    dEk[o] = make_double2(b * v.x, b * v.y);
+  }
+}
+
+int sbe_local_field(SbeCtx* c, const double* e0, const double* de, int comp, double* Ek0,
+                    double* dEk, void* stream) {
+  if (!c || !e0 || !Ek0 || (dEk && !de) || comp < 0 || comp > 2)
+    return fail(SBE_ERR_ARG, "sbe_local_field: bad arguments");
+  k_local_field<<<dim3((3 * c->nr_max + 127) / 128, c->nw), 128, 0, as_stream(stream)>>>(
+      c->d_wires, c->wk, e0, de, comp, (double2*)Ek0, (double2*)dEk);
+  return cuda_check(cudaGetLastError(), "sbe_local_field");
 }
 
 // ---- CUDA graph of one step -------------------------------------------------

@@ -9,7 +9,8 @@ struct SbeCtx {
   int nw = 0;
   int nk_max = 0, nr_max = 0;
   std::vector<SbeWireDesc> desc;
-  std::vector<sbe::WireDev> wires;  // host copy of d_wires
+  std::vector<sbe::WireDev> wires;  // host copy of d_wires (the caller's wire order)
+  std::vector<int> order;           // wires in packed-layout order (grouped by Nk)
   sbe::WireDev* d_wires = nullptr;
   long long tot_mat = 0, tot_vec = 0, tot_r = 0, tot_dd = 0, tot_kr = 0;
 

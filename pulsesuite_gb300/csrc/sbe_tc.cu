@@ -10,10 +10,12 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "fp_bits.cuh"
 #include "sbe_ctx.cuh"
 #include "tc_gemm.cuh"
+#include "sbe_mixed.cuh"
 
 namespace sbe {
 
@@ -260,9 +262,13 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-precision workspace of a context (uniform Nk and flags over its wires).
+// Mixed-precision workspace of a context.  The layout groups the wires by Nk, so
+// the wires of one Nk form a bucket whose matrices are one contiguous block of
+// every packed buffer: the per-element kernels run once per bucket (uniform Nk,
+// grid z = the bucket's wires) on pointers offset to the bucket's block, and each
+// GEMM kind runs as one persistent launch over the jobs of all buckets.
 //
-// Commutator planes: 14 matrix slots x 4 planes x Nw x Nk x Nk (FP16):
+// Per bucket, commutator planes: 14 matrix slots x 4 planes x Nw x Nk x Nk (FP16):
 //   0 P, 1 P^T, 2 C, 4 D                            (state, exponent eS)
 //   6 Heh, 7 Heh^T, 8 Hee', 10 Hhh',
 //   12 Hee' + i hbar B, 13 Hhh' + i hbar A          (Hamiltonians, exponent eH)
@@ -270,70 +276,24 @@ void launch_exponents(const double2* X, long long per_batch, long long bstride, 
 // D^T = conj D are taken by conjugating the C and D operands).
 // Exchange: Toeplitz planes T_n (3 x 2 x Nw x Nk x Nk) and sheared state planes
 // S_n (3 x 2 x Nw x 4Nk x Nk).  Sources: E^T planes (4 x Nw x Nr x Nk).
-// Stage values in FP32: kf (dP, dC, dD), accf (RK4 sums), Hf (Heh, Hee', Hhh'),
-// Wf (W, V of the W - W^H form, in the G buffer).
-struct Mixed {
-  int nk = 0, nw = 0, nr = 0;
-  tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
-  float* xsh = nullptr;    // exchange sums, un-sheared: 3 x Nw x Nk x Nk complex (FP32)
-  int* ints = nullptr;     // eS, eH, eT, eE, esc, esx, ess, err  (8 x nw)
-  unsigned* mx = nullptr;  // [0, nw): Hamiltonian maximum; [nw, 2nw): state; [2nw, 3nw): hbar A/B
-  float2* kf = nullptr;    // 3 x tot_mat stage derivatives
-  float2* accf = nullptr;  // 3 x tot_mat RK4 sums k1 + 2 k2 + 2 k3
-  float2* hf = nullptr;    // 3 x tot_mat Heh, Hee', Hhh'
-  float* habf = nullptr;   // 2 x tot_mat hbar A, hbar B
-  float2* ekf = nullptr;   // 3 x tot_r stage field
-  float* vsf = nullptr;    // 3 x nw x nk screened V by |k1 - k2|
-  float2* trf = nullptr;   // 4 x nw x nk traces [2][2nk]
-  float* gamf = nullptr;   // 2 x nw x nk GamE, GamH
-  float2* dgf = nullptr;   // 4 x nw x nk: hi and lo parts of the peeled Hee, Hhh diagonals
-  double2 *dgE = nullptr, *dgH = nullptr;  // the peeled diagonals in FP64
-  // constant FP32 tables (built once): EP, EP^T, HP, HP^T scaled by 2^sP[w];
-  // Expikr; |xe|, |xh|
-  float *epf = nullptr, *eptf = nullptr, *hpf = nullptr, *hptf = nullptr;
-  float2* ekrf = nullptr;
-  float* xef = nullptr;     // 2 x nw x nk
-  int* sP = nullptr;        // nw phonon-table exponents
-  // per-step FP32 tables
-  float* phf = nullptr;     // 2 x nw x nk: Vep(d) 2^-sP, Vhp(d) 2^-sP
-  float* gtab = nullptr;    // 4 x nw x nk: gamma weights per q
-  float2* tpart = nullptr;  // nw x 2 x 32 ceil(2nk/32) x T diagonal partials (T = ceil(nk/32))
-  float* cdf = nullptr;     // 4 x nw x nk: hi / lo parts of Re C_kk and Re D_kk (stage state)
-  double* xdg = nullptr;    // 2 x nw x nk: Re C_kk, Re D_kk of the stage state in FP64
-  int* eS() { return ints; }
-  int* eH() { return ints + nw; }
-  int* eT() { return ints + 2 * nw; }
-  int* eE() { return ints + 3 * nw; }
-  int* esc() { return ints + 4 * nw; }
-  int* esx() { return ints + 5 * nw; }
-  int* ess() { return ints + 6 * nw; }
-  int* err() { return ints + 7 * nw; }
-  int* eO() { return ints + 8 * nw; }   // commutator state operands (diagonals of C, D peeled)
-  unsigned* mxH() { return mx; }
-  unsigned* mxS() { return mx + nw; }
-  unsigned* mxAB() { return mx + 2 * nw; }
-  unsigned* mxO() { return mx + 3 * nw; }  // max over P and the off-diagonal C, D
-};
-
-enum { M_P = 0, M_PT, M_C, M_CT, M_D, M_DT, M_EH, M_EHT, M_EE, M_EET, M_HH, M_HHT, M_EEX, M_HHX };
-
+// Context-wide FP32 stage values (indexed like the packed state): kf (dP, dC, dD),
+// accf (RK4 sums), hf (Heh, Hee', Hhh'), habf (hbar A, hbar B), the phonon tables,
+// the stage field and Expikr.
 void mixed_free(SbeCtx* c) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  if (!m) return;
-  cudaFree(m->pl.ptr);
-  cudaFree(m->tp.ptr);
-  cudaFree(m->sp.ptr);
-  cudaFree(m->ep.ptr);
-  cudaFree(m->xsh);
-  cudaFree(m->ints);
-  cudaFree(m->mx);
-  cudaFree(m->kf);
-  cudaFree(m->dgE);
-  cudaFree(m->epf);
-  cudaFree(m->ekrf);
-  cudaFree(m->tpart);
-  cudaFree(m->xdg);
-  delete m;
+  MixedAll* A = all_of(c);
+  if (!A) return;
+  for (Mixed* m : A->b) {
+    cudaFree(m->pl.ptr);
+    cudaFree(m->tp.ptr);
+    cudaFree(m->sp.ptr);
+    cudaFree(m->ep.ptr);
+    cudaFree(m->xsh);
+    cudaFree(m->block);
+    cudaFree(m->dw);
+    delete m;
+  }
+  cudaFree(A->block);
+  delete A;
   c->mixed = nullptr;
 }
 
@@ -408,117 +368,161 @@ __global__ void k_phon_tables(int nk, const double* EP, const double* HP, const 
   }
 }
 
-__global__ void k_const_f(const WireDev* wires, const double2* expikr, long long tot_kr,
-                          float2* ekrf, const double* xeh, float* xef, int nw) {
+__global__ void k_ekrf(long long n, const double2* expikr, float2* ekrf) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < tot_kr) ekrf[i] = f64_to_f32(expikr[i]);
-  if (i < 2ll * nw * wires[0].nk) {
-    const int nk = wires[0].nk;
-    const int b = (int)(i / (2 * nk)), j = (int)(i % (2 * nk));
-    xef[i] = fabsf(f64_to_f32(xeh[2 * wires[b].off_vec + j]));
+  if (i < n) ekrf[i] = f64_to_f32(expikr[i]);
+}
+
+// |xe|, |xh| of a bucket's wires in FP32: xef[b][j], j < 2 nk
+__global__ void k_xef(const WireDev* wires, int nk, const double* xeh, float* xef) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+  if (j < 2 * nk) xef[(long long)b * 2 * nk + j] = fabsf(f64_to_f32(xeh[2 * wires[b].off_vec + j]));
+}
+
+// carve 256-byte aligned parts out of one allocation
+struct Carver {
+  size_t off = 0;
+  char* base = nullptr;
+  template <typename T>
+  T* take(size_t n) {
+    const size_t o = off;
+    off = (off + sizeof(T) * n + 255) / 256 * 256;
+    return base ? reinterpret_cast<T*>(base + o) : nullptr;
   }
+};
+
+static void carve_bucket(Mixed* m, Carver& k) {
+  const size_t v = (size_t)m->nw * m->nk;
+  const int T = (m->nk + 31) / 32;
+  m->ints = k.take<int>(9 * (size_t)m->nw);
+  m->mx = k.take<unsigned>(4 * (size_t)m->nw);
+  m->mx64 = k.take<unsigned long long>((size_t)m->nw);
+  m->sP = k.take<int>((size_t)m->nw);
+  m->vsf = k.take<float>(3 * v);
+  m->trf = k.take<float2>(4 * v);
+  m->gamf = k.take<float>(2 * v);
+  m->dgf = k.take<float2>(4 * v);
+  m->dgE = k.take<double2>(2 * v);
+  m->dgH = m->dgE ? m->dgE + v : nullptr;
+  m->xef = k.take<float>(2 * v);
+  m->phf = k.take<float>(2 * v);
+  m->gtab = k.take<float>(4 * v);
+  m->tpart = k.take<float2>((size_t)m->nw * 2 * 32 * ((2 * m->nk + 31) / 32) * T);
+  m->cdf = k.take<float>(4 * v);
+  m->xdg = k.take<double>(2 * v);
+}
+
+static void carve_all(MixedAll* A, Carver& k, const SbeCtx* c) {
+  const size_t tm = (size_t)c->tot_mat;
+  A->kf = k.take<float2>(3 * tm);
+  A->accf = k.take<float2>(3 * tm);
+  A->hf = k.take<float2>(3 * tm);
+  A->habf = k.take<float>(2 * tm);
+  A->epf = k.take<float>(tm);
+  A->eptf = k.take<float>(tm);
+  A->hpf = k.take<float>(tm);
+  A->hptf = k.take<float>(tm);
+  A->ekf = k.take<float2>(3 * (size_t)c->tot_r);
+  A->ekrf = k.take<float2>((size_t)c->tot_kr);
+  A->err = k.take<int>(1);
 }
 
 static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
   if (c->mixed) return SBE_OK;
-  const int nk = c->wires[0].nk, nw = c->nw;
-  for (int w = 1; w < nw; ++w)
-    if (c->wires[w].nk != nk || c->wires[w].flags != c->wires[0].flags)
+  const int flags0 = c->wires[0].flags;
+  for (int w = 1; w < c->nw; ++w)
+    if (c->wires[w].flags != flags0)
       return fail(SBE_ERR_UNSUPPORTED,
-                  "mixed path: all wires of a context must share Nk and flags (group by Nk)");
-  if (nk % 8) return fail(SBE_ERR_UNSUPPORTED, "mixed path: Nk must be a multiple of 8");
+                  "mixed path: all wires of a context must share their flags (one context per "
+                  "flag set)");
   // the operand planes take C^T = conj C, D^T = conj D; the reference's DC transport
   // (dcfield.py:1196-1206: the centred Y against the FFT's natural order) leaves C, D
   // non-Hermitian, so DCTrans runs on the FP64 path only
   if (any_dc(c))
     return fail(SBE_ERR_UNSUPPORTED,
                 "mixed path: DCTrans leaves C and D non-Hermitian; use the FP64 path");
-  Mixed* m = new Mixed();
-  m->nk = nk;
-  m->nw = nw;
-  m->nr = 2 * nk + 2;
-  const size_t mm = (size_t)nk * nk, tm = (size_t)nw * mm, tr = (size_t)nw * m->nr;
-  // one block for the FP32 stage buffers
-  const size_t fbytes = sizeof(float2) * (3 * tm + 3 * tm + 3 * tm + 3 * tr + 4 * (size_t)nw * nk +
-                                          4 * (size_t)nw * nk) +
-                        sizeof(float) * (2 * tm + 3 * (size_t)nw * nk + 2 * (size_t)nw * nk);
-  void* fblock = nullptr;
-  m->pl = tc::make_planeset(nullptr, 14, 4, nw, nk, nk);
-  m->tp = tc::make_planeset(nullptr, 3, 2, nw, nk, nk);
-  m->sp = tc::make_planeset(nullptr, 3, 2, nw, 4 * nk, nk);
-  m->ep = tc::make_planeset(nullptr, 1, 4, nw, m->nr, nk);
-  bool ok = cudaMalloc(&m->pl.ptr, tc::planeset_bytes(m->pl)) == cudaSuccess &&
-            cudaMalloc(&m->tp.ptr, tc::planeset_bytes(m->tp)) == cudaSuccess &&
-            cudaMalloc(&m->sp.ptr, tc::planeset_bytes(m->sp)) == cudaSuccess &&
-            cudaMalloc(&m->ep.ptr, tc::planeset_bytes(m->ep)) == cudaSuccess &&
-            cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 2 * mm) == cudaSuccess &&
-            cudaMalloc(&m->ints, sizeof(int) * 9 * nw) == cudaSuccess &&
-            cudaMalloc(&m->mx, sizeof(unsigned) * 4 * nw) == cudaSuccess &&
-            cudaMalloc(&fblock, fbytes) == cudaSuccess &&
-            cudaMalloc(&m->dgE, sizeof(double2) * 2 * nw * nk) == cudaSuccess;
-  m->kf = static_cast<float2*>(fblock);
+  for (const auto& W : c->wires)
+    if (W.nk % 8) return fail(SBE_ERR_UNSUPPORTED, "mixed path: Nk must be a multiple of 8");
+  MixedAll* A = new MixedAll();
+  c->mixed = A;
+  // buckets: runs of equal Nk in the layout order
+  for (int i = 0; i < c->nw;) {
+    const WireDev& W0 = c->wires[c->order[i]];
+    int j = i;
+    while (j < c->nw && c->wires[c->order[j]].nk == W0.nk) ++j;
+    Mixed* m = new Mixed();
+    m->nk = W0.nk;
+    m->nw = j - i;
+    m->nr = 2 * W0.nk + 2;
+    m->first = i;
+    m->bm = W0.off_mat;
+    m->bv = W0.off_vec;
+    m->br = W0.off_r;
+    m->bkr = W0.off_kr;
+    A->b.push_back(m);
+    i = j;
+  }
+  bool ok = true;
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const size_t mm = (size_t)nk * nk;
+    m->pl = tc::make_planeset(nullptr, 14, 4, nw, nk, nk);
+    m->tp = tc::make_planeset(nullptr, 3, 2, nw, nk, nk);
+    m->sp = tc::make_planeset(nullptr, 3, 2, nw, 4 * nk, nk);
+    m->ep = tc::make_planeset(nullptr, 1, 4, nw, m->nr, nk);
+    Carver k;
+    carve_bucket(m, k);
+    const size_t vbytes = k.off;
+    ok = ok && cudaMalloc(&m->pl.ptr, tc::planeset_bytes(m->pl)) == cudaSuccess &&
+         cudaMalloc(&m->tp.ptr, tc::planeset_bytes(m->tp)) == cudaSuccess &&
+         cudaMalloc(&m->sp.ptr, tc::planeset_bytes(m->sp)) == cudaSuccess &&
+         cudaMalloc(&m->ep.ptr, tc::planeset_bytes(m->ep)) == cudaSuccess &&
+         cudaMalloc(&m->xsh, sizeof(float) * 3 * nw * 2 * mm) == cudaSuccess &&
+         cudaMalloc(&m->block, vbytes) == cudaSuccess &&
+         cudaMalloc(&m->dw, sizeof(WireDev) * nw) == cudaSuccess;
+    if (!ok) break;
+    k = Carver{0, static_cast<char*>(m->block)};
+    carve_bucket(m, k);
+    std::vector<WireDev> hw(nw);
+    for (int b = 0; b < nw; ++b) hw[b] = c->wires[c->order[m->first + b]];
+    cudaMemcpyAsync(m->dw, hw.data(), sizeof(WireDev) * nw, cudaMemcpyHostToDevice, s);
+    // the host vector goes out of scope: wait for the copy
+    cudaStreamSynchronize(s);
+  }
+  Carver ka;
+  carve_all(A, ka, c);
+  ok = ok && cudaMalloc(&A->block, ka.off) == cudaSuccess;
   if (!ok) {
-    c->mixed = m;
     mixed_free(c);
     return fail(SBE_ERR_OOM, "mixed path: workspace allocation failed");
   }
-  m->accf = m->kf + 3 * tm;
-  m->hf = m->accf + 3 * tm;
-  m->ekf = m->hf + 3 * tm;
-  m->trf = m->ekf + 3 * tr;
-  m->dgf = m->trf + 4 * (size_t)nw * nk;
-  m->habf = reinterpret_cast<float*>(m->dgf + 4 * (size_t)nw * nk);
-  m->vsf = m->habf + 2 * tm;
-  m->gamf = m->vsf + 3 * (size_t)nw * nk;
-  m->dgH = m->dgE + (size_t)nw * nk;
-  cudaMemsetAsync(m->ints, 0, sizeof(int) * 9 * nw, s);
-  cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 4 * nw, s);
-  // the padding of every plane set stays zero: producers write only inside
-  cudaMemsetAsync(m->pl.ptr, 0, tc::planeset_bytes(m->pl), s);
-  cudaMemsetAsync(m->tp.ptr, 0, tc::planeset_bytes(m->tp), s);
-  cudaMemsetAsync(m->ep.ptr, 0, tc::planeset_bytes(m->ep), s);
-  // constant FP32 tables and per-step FP32 scratch
-  const int T = (nk + 31) / 32;
-  const size_t cbytes = sizeof(float) * (4 * tm + 2 * (size_t)nw * nk + 2 * (size_t)nw * nk +
-                                         4 * (size_t)nw * nk + 4 * (size_t)nw * nk) +
-                        sizeof(int) * (size_t)nw + sizeof(unsigned long long) * (size_t)nw + 64;
-  void* cblock = nullptr;
-  if (cudaMalloc(&cblock, cbytes) != cudaSuccess ||
-      cudaMalloc(&m->ekrf, sizeof(float2) * (size_t)c->tot_kr) != cudaSuccess ||
-      cudaMalloc(&m->tpart, sizeof(float2) * (size_t)nw * 2 * 32 * ((2 * nk + 31) / 32) * T) !=
-          cudaSuccess ||
-      cudaMalloc(&m->xdg, sizeof(double) * 2 * (size_t)nw * nk) != cudaSuccess) {
-    if (cblock) cudaFree(cblock);
-    m->epf = nullptr;
-    c->mixed = m;
-    mixed_free(c);
-    return fail(SBE_ERR_OOM, "mixed path: table allocation failed");
+  ka = Carver{0, static_cast<char*>(A->block)};
+  carve_all(A, ka, c);
+  cudaMemsetAsync(A->block, 0, ka.off, s);
+  k_ekrf<<<(unsigned)((c->tot_kr + 255) / 256), 256, 0, s>>>(c->tot_kr, c->expikr, A->ekrf);
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const long long mm = (long long)nk * nk;
+    const int T = (nk + 31) / 32;
+    cudaMemsetAsync(m->ints, 0, sizeof(int) * 9 * nw, s);
+    cudaMemsetAsync(m->mx, 0, sizeof(unsigned) * 4 * nw, s);
+    // the padding of every plane set stays zero: producers write only inside; the
+    // sheared planes are zeroed once, stages write only the in-band part
+    cudaMemsetAsync(m->pl.ptr, 0, tc::planeset_bytes(m->pl), s);
+    cudaMemsetAsync(m->tp.ptr, 0, tc::planeset_bytes(m->tp), s);
+    cudaMemsetAsync(m->sp.ptr, 0, tc::planeset_bytes(m->sp), s);
+    cudaMemsetAsync(m->ep.ptr, 0, tc::planeset_bytes(m->ep), s);
+    k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(m->dw, c->expikr, m->ep, nw);
+    k_fill_int<<<(nw + 127) / 128, 128, 0, s>>>(m->eE(), nw, 13);
+    cudaMemsetAsync(m->mx64, 0, sizeof(unsigned long long) * nw, s);
+    k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->EP + m->bm, mm, m->mx64);
+    k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->HP + m->bm, mm, m->mx64);
+    k_phon_exp<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mx64, m->sP);
+    k_phon_tables<<<dim3(T, T, nw), dim3(32, 8), 0, s>>>(nk, c->EP + m->bm, c->HP + m->bm, m->sP,
+                                                        A->epf + m->bm, A->eptf + m->bm,
+                                                        A->hpf + m->bm, A->hptf + m->bm);
+    k_xef<<<dim3((2 * nk + 127) / 128, nw), 128, 0, s>>>(m->dw, nk, c->xeh, m->xef);
   }
-  m->epf = static_cast<float*>(cblock);
-  m->eptf = m->epf + tm;
-  m->hpf = m->eptf + tm;
-  m->hptf = m->hpf + tm;
-  m->xef = m->hptf + tm;
-  m->phf = m->xef + 2 * (size_t)nw * nk;
-  m->gtab = m->phf + 2 * (size_t)nw * nk;
-  m->cdf = m->gtab + 4 * (size_t)nw * nk;
-  m->sP = reinterpret_cast<int*>(m->cdf + 4 * (size_t)nw * nk);
-  unsigned long long* mx64 = reinterpret_cast<unsigned long long*>(
-      (reinterpret_cast<uintptr_t>(m->sP + nw) + 7) & ~uintptr_t(7));
-  // sheared planes: zero once; stages write only the in-band part
-  cudaMemsetAsync(m->sp.ptr, 0, tc::planeset_bytes(m->sp), s);
-  k_eplanes<<<dim3((nk + 127) / 128, m->nr, nw), 128, 0, s>>>(c->d_wires, c->expikr, m->ep, nw);
-  k_fill_int<<<(nw + 127) / 128, 128, 0, s>>>(m->eE(), nw, 13);
-  cudaMemsetAsync(mx64, 0, sizeof(unsigned long long) * nw, s);
-  k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->EP, (long long)mm, mx64);
-  k_absmax_r<<<dim3(64, nw), 256, 0, s>>>(c->HP, (long long)mm, mx64);
-  k_phon_exp<<<(nw + 127) / 128, 128, 0, s>>>(nw, mx64, m->sP);
-  k_phon_tables<<<dim3(T, T, nw), dim3(32, 8), 0, s>>>(nk, c->EP, c->HP, m->sP, m->epf, m->eptf,
-                                                      m->hpf, m->hptf);
-  const long long nconst = std::max<long long>(c->tot_kr, 2ll * nw * nk);
-  k_const_f<<<(unsigned)((nconst + 255) / 256), 256, 0, s>>>(c->d_wires, c->expikr, c->tot_kr,
-                                                             m->ekrf, c->xeh, m->xef, nw);
-  c->mixed = m;
   return cuda_check(cudaGetLastError(), "mixed workspace");
 }
 
@@ -943,15 +947,6 @@ __global__ void k_src_reduce_f(const WireDev* wires, const float2* ekrf, const f
   const double f = w / (2.0 * W.L);
   out[3 * nr + r] = make_double2(f32_to_f64(v[2]) * f, f32_to_f64(v[3]) * f);
   out[4 * nr + r] = make_double2(f32_to_f64(v[4]) * f, f32_to_f64(v[5]) * f);
-}
-
-__global__ void k_gam_f(const WireDev* wires, const double* gE, const double* gH, float* gamf,
-                        int nw) {
-  const WireDev W = wires[blockIdx.y];
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= W.nk) return;
-  gamf[(long long)blockIdx.y * W.nk + k] = f64_to_f32(gE[W.off_vec + k]);
-  gamf[((long long)nw + blockIdx.y) * W.nk + k] = f64_to_f32(gH[W.off_vec + k]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1508,6 +1503,97 @@ static tc::GemmJob job(Mixed* m, const tc::PlaneSet& A, const tc::PlaneSet& B, i
   return j;
 }
 
+// Launch a job list (built bucket by bucket, largest Nk first, so that the longest
+// tiles start first): consecutive jobs of one N tile share a persistent launch,
+// tc::MAX_JOBS per launch.
+int launch_jobs(const std::vector<tc::GemmJob>& jobs, cudaStream_t s) {
+  for (size_t i = 0; i < jobs.size();) {
+    size_t j = i + 1;
+    while (j < jobs.size() && j - i < (size_t)tc::MAX_JOBS && jobs[j].d.bn == jobs[i].d.bn) ++j;
+    const int rc = tc_gemm_launch(jobs.data() + i, (int)(j - i), s);
+    if (rc) return rc;
+    i = j;
+  }
+  return SBE_OK;
+}
+
+// The GEMM jobs of one kind for bucket m.  Exchange: T_n S_n (eh, ee, hh), real, the
+// K range limited to the sheared band, un-sheared FP32 output.  Commutators (term
+// lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt, SBEs.py:2309-2327 and
+// 2607-2625, through their W - W^H form): dP, and the hi*lo + lo*hi products of W and
+// V (xonly); their hi*hi products as two K halves with one accumulator per real
+// product (MODE_HH: W - W^H is a small difference of large products near
+// equilibrium).  Sources: [P; C; conj D] E.
+void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
+  MixedAll* A = all_of(c);
+  const long long tm = c->tot_mat, mm = (long long)m->nk * m->nk;
+  const int nk = m->nk;
+  const size_t first = out.size();
+  if (kind == JK_EXCH) {
+    for (int n = 0; n < 3; ++n) {
+      tc::Term t{n, n, 0, 0, 1};
+      tc::EpiArgs e{};
+      e.kind = tc::EPI_F32;
+      e.outf = m->xsh + (long long)n * m->nw * 2 * mm;
+      e.out_bstride = 2 * mm;
+      e.ldo = 2 * nk;
+      e.unshear = nk;
+      e.escale = m->esx();
+      e.err = A->err;
+      out.push_back(job(m, m->tp, m->sp, nk, 4 * nk, nk, 0, 1, &t, 1, e));
+    }
+  } else if (kind == JK_FULL || kind == JK_HH) {
+    const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_D, M_EH, 1, 0, -1},
+                            {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_C, 0, 1, -1}};
+    const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
+    const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
+    // G buffer (FP32 complex, tot_mat each, indexed like the packed state): [W hh
+    // K-half 0, W hh K-half 1, V hh 0, V hh 1, dP sums, W cross terms, V cross terms]
+    float2* wf = reinterpret_cast<float2*>(c->G);   // the buffer holds 12 tot_mat float2
+    auto epi = [&](float2* o) {
+      tc::EpiArgs e{};
+      e.kind = tc::EPI_RAWF;
+      e.outf2 = o + m->bm;
+      e.out_bstride = mm;
+      e.ks_stride = tm;
+      e.escale = m->esc();
+      e.err = A->err;
+      return e;
+    };
+    if (kind == JK_FULL) {
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 4, tP, 0, epi(wf + 4 * tm)));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + 5 * tm), tc::MODE_FULL, 1));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + 6 * tm), tc::MODE_FULL, 1));
+    } else {
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf), tc::MODE_HH, 0, 2));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + 2 * tm), tc::MODE_HH, 0, 2));
+    }
+  } else {
+    float2* gf = reinterpret_cast<float2*>(c->G);
+    for (int j = 0; j < 3; ++j) {
+      tc::Term t{2 * j, 0, j == 2 ? 1 : 0, 0, 1};
+      tc::EpiArgs e{};
+      e.kind = tc::EPI_RAWF;
+      e.outf2 = gf + j * c->tot_kr + m->bkr;
+      e.out_bstride = (long long)nk * m->nr;
+      e.ldo = m->nr;
+      e.escale = m->ess();
+      e.err = A->err;
+      out.push_back(job(m, m->pl, m->ep, nk, m->nr, nk, 1, 1, &t, 0, e));
+    }
+  }
+  if (kind != JK_HH)
+    for (size_t i = first; i < out.size(); ++i) out[i].d.bn = m->bn[kind];
+}
+
+// The jobs of one kind of every bucket, largest Nk first.
+static std::vector<tc::GemmJob> all_jobs(SbeCtx* c, int kind) {
+  MixedAll* A = all_of(c);
+  std::vector<tc::GemmJob> jobs;
+  for (int i = (int)A->b.size() - 1; i >= 0; --i) bucket_jobs(c, A->b[i], kind, jobs);
+  return jobs;
+}
+
 static void exponents_from(Mixed* m, const unsigned* mx, int* e, cudaStream_t s) {
   k_exponents<<<(m->nw + 127) / 128, 128, 0, s>>>(m->nw, mx, e, nullptr, nullptr);
 }
@@ -1515,28 +1601,32 @@ static void exponents_from(Mixed* m, const unsigned* mx, int* e, cudaStream_t s)
 // Per-step set-up of the mixed path: the frozen preparation (screening, rates,
 // dephasing matrices with the FP32 Lorentzian sums) and its FP32 tables.
 static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_t s) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const int nk = m->nk, nw = m->nw;
+  MixedAll* A = all_of(c);
   launch_prep_scalar(c, C, D, s);   // occupations, screening (FP64, O(Nk) per wire)
-  cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
-  k_vs_max<<<nw, 256, 0, s>>>(c->d_wires, c->vs, m->mxH());
-  exponents_from(m, m->mxH(), m->eT(), s);
-  k_toeplitz_planes<<<dim3((nk + 31) / 32, (nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
-      c->d_wires, c->vs, m->eT(), m->tp, nw, m->vsf);
-  k_gamma_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->iq, c->xeh,
-                                                         m->gtab, nw);
-  k_gamma_f<<<dim3((nk + 7) / 8, nw), 256, sizeof(float) * 2 * nk, s>>>(
-      c->d_wires, c->ne, c->nh, c->maps, m->gtab, m->gamf, nw);
-  k_phon_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(c->d_wires, c->vs, c->eps, m->sP, m->phf,
-                                                        nw);
-  cudaMemsetAsync(m->mxAB(), 0, sizeof(unsigned) * nw, s);
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    cudaMemsetAsync(m->mxH(), 0, sizeof(unsigned) * nw, s);
+    k_vs_max<<<nw, 256, 0, s>>>(m->dw, c->vs, m->mxH());
+    exponents_from(m, m->mxH(), m->eT(), s);
+    k_toeplitz_planes<<<dim3((nk + 31) / 32, (nk + 31) / 32, 3 * nw), dim3(32, 8), 0, s>>>(
+        m->dw, c->vs, m->eT(), m->tp, nw, m->vsf);
+    k_gamma_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(m->dw, c->vs, c->iq, c->xeh, m->gtab,
+                                                           nw);
+    k_gamma_f<<<dim3((nk + 7) / 8, nw), 256, sizeof(float) * 2 * nk, s>>>(
+        m->dw, c->ne, c->nh, c->maps, m->gtab, m->gamf, nw);
+    k_phon_tab<<<dim3((nk + 127) / 128, nw), 128, 0, s>>>(m->dw, c->vs, c->eps, m->sP, m->phf,
+                                                          nw);
+    cudaMemsetAsync(m->mxAB(), 0, sizeof(unsigned) * nw, s);
+  }
   if (c->any_offdiag) {
     ProfScope ps(c, 3, s);
     launch_offdiag_D(c, -1, nullptr, true, s);
   }
-  const int T = (nk + 31) / 32;
-  k_hab<<<dim3(T, T, nw), dim3(32, 8), 0, s>>>(c->d_wires, c->De, c->Dh, m->habf, c->tot_mat,
-                                               m->mxAB());
+  for (Mixed* m : A->b) {
+    const int T = (m->nk + 31) / 32;
+    k_hab<<<dim3(T, T, m->nw), dim3(32, 8), 0, s>>>(m->dw, c->De, c->Dh, A->habf, c->tot_mat,
+                                                    m->mxAB());
+  }
   return cuda_check(cudaGetLastError(), "mixed prep");
 }
 
@@ -1544,184 +1634,151 @@ static int mixed_prep(SbeCtx* c, const double2* C, const double2* D, cudaStream_
 // normalisation after the step (SBEs.py:5677-5702), then the state maximum.
 static void mixed_relax(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek,
                         double dt, cudaStream_t s) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const int nk = m->nk, nw = m->nw;
+  MixedAll* A = all_of(c);
   launch_extract_diag(c, C, D, s);
-  k_phonon_rates_f<<<dim3(nk, nw), 128, sizeof(float) * 2 * nk, s>>>(
-      c->d_wires, c->ne, c->nh, m->phf, m->epf, m->eptf, m->hpf, m->hptf, c->wrate, nw);
+  for (Mixed* m : A->b)
+    k_phonon_rates_f<<<dim3(m->nk, m->nw), 128, sizeof(float) * 2 * m->nk, s>>>(
+        m->dw, c->ne, c->nh, m->phf, A->epf, A->eptf, A->hpf, A->hptf, c->wrate, m->nw);
   launch_mbc_rates(c, -1, s, false, true);
   launch_relax_only(c, P, C, D, Ek, dt, s);
-  k_diag_max<<<nw, 256, 0, s>>>(c->d_wires, C, D, m->mxS());
+  for (Mixed* m : A->b) k_diag_max<<<m->nw, 256, 0, s>>>(m->dw, C, D, m->mxS());
 }
 
-// One stage RHS of every wire at state (P, C, D) and wire-k field Ek (FP64);
-// the derivatives go to m->kf (FP32).  When state_max_ready is set, mxS already
-// holds the per-wire maximum of the state (written by the previous stage's
-// update); otherwise it is measured here.
-// Stage-1 state of the mixed path from the FP64 state: FP32 copies in xf, the
-// FP64 diagonals of C and D, and the maxima the stage's exponents need.
+// Stage-1 state of the mixed path from the FP64 state: FP32 copies (the first
+// three tot_mat blocks of the FP32 view of the context's stage buffer), the FP64
+// diagonals of C and D, and the maxima the stage's exponents need.
 static void mixed_state_in(SbeCtx* c, const double2* P, const double2* C, const double2* D,
                            cudaStream_t s) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const int nk = m->nk, nw = m->nw;
-  const long long mm = (long long)nk * nk, tm = c->tot_mat, vn = (long long)nw * nk;
+  MixedAll* A = all_of(c);
+  const long long tm = c->tot_mat;
   float2* xf = reinterpret_cast<float2*>(c->xs);
-  cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-  cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
-  const int blocks = (int)std::min<long long>((mm + 255) / 256, 128);
-  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(P, nk, 0, m->mxS(), m->mxO(), xf, nullptr);
-  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(C, nk, 1, m->mxS(), m->mxO(), xf + tm, m->xdg);
-  k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(D, nk, 1, m->mxS(), m->mxO(), xf + 2 * tm,
-                                              m->xdg + vn);
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const long long mm = (long long)nk * nk, vn = (long long)nw * nk, o = m->bm;
+    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+    cudaMemsetAsync(m->mxO(), 0, sizeof(unsigned) * nw, s);
+    const int blocks = (int)std::min<long long>((mm + 255) / 256, 128);
+    k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(P + o, nk, 0, m->mxS(), m->mxO(), xf + o, nullptr);
+    k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(C + o, nk, 1, m->mxS(), m->mxO(), xf + tm + o,
+                                                m->xdg);
+    k_state_in<<<dim3(blocks, nw), 256, 0, s>>>(D + o, nk, 1, m->mxS(), m->mxO(),
+                                                xf + 2 * tm + o, m->xdg + vn);
+  }
 }
 
-// One RHS evaluation of the mixed path on the FP32 stage state (P, C, D; the
-// FP64 diagonals of C and D in dgC, dgD; the state maxima already in mxS, mxO)
-// with the wire-k field Ek + frac dEk (dEk may be null).  With stage 1-4 the RK4 update of that stage is fused into the element-wise
-// passes (X64: the FP64 states P, C, D; the next stage state goes to the FP32
-// stage buffer and its maxima to mxS, mxO); stage 0 stores the RHS in kf.
-static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2* D,
-                       const double* dgC, const double* dgD, const double2* Ek,
-                       const double2* dEk, double frac, int stage, float dt,
-                       double2* const* X64, cudaStream_t s) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const int nk = m->nk, nw = m->nw;
-  const long long mm = (long long)nk * nk, tm = c->tot_mat;
-  const WireDev& W0 = c->wires[0];
-  // state exponent and planes: P and P^T from one read; C and D need only their
-  // own layout (C^T = conj C and D^T = conj D for the Hermitian C and D)
-  // eS: full state maximum (sheared exchange operands); eO: maximum over P and
-  // the off-diagonal C, D (commutator operands; the diagonals of C and D are
-  // peeled off and applied exactly in the epilogues)
-  k_stage_exponents<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxS(), m->mxO(), m->mxH(), m->eS(),
-                                                     m->eO(), m->eT(), m->esx(), stage > 0);
-  const float2* st[3] = {P, C, D};
-  const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
-  const long long vn = (long long)nw * nk;
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw,
-                                        m->cdf, dgC);
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw,
-                                        m->cdf + 2 * vn, dgD);
-  // stage field and traces in FP32; exchange sums (sheared GEMMs, FP32 output);
-  // then the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled
-  k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, dEk, frac,
-                                                               m->ekf);
+// One RHS evaluation of the mixed path on the FP32 stage state xs (P, C, D at
+// xs, xs + tot_mat, xs + 2 tot_mat; the FP64 diagonals of C and D in each bucket's
+// xdg; the state maxima already in mxS, mxO) with the wire-k field Ek + frac dEk
+// (dEk may be null).  With stage 1-4 the RK4 update of that stage is fused into the
+// element-wise passes (X64: the FP64 states P, C, D; the next stage state goes to
+// the FP32 stage buffer and its maxima to mxS, mxO); stage 0 stores the RHS in kf.
+static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const double2* dEk,
+                       double frac, int stage, float dt, double2* const* X64, cudaStream_t s) {
+  MixedAll* A = all_of(c);
+  const long long tm = c->tot_mat;
+  const int have_x = (c->wires[0].flags & SBE_F_EXCITONS) ? 1 : 0;
+  // stage field in FP32 (all wires)
+  k_field_f<<<(int)((3 * c->tot_r + 255) / 256), 256, 0, s>>>(3 * c->tot_r, Ek, dEk, frac, A->ekf);
+  // state exponents and planes: P and P^T from one read; C and D need only their own
+  // layout (C^T = conj C and D^T = conj D for the Hermitian C and D).  eS: full state
+  // maximum (sheared exchange operands); eO: maximum over P and the off-diagonal C, D
+  // (commutator operands; the diagonals of C and D are peeled off and applied exactly
+  // in the element-wise passes)
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const long long vn = (long long)nw * nk;
+    const float2 *P = xs + m->bm, *C = xs + tm + m->bm, *D = xs + 2 * tm + m->bm;
+    k_stage_exponents<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxS(), m->mxO(), m->mxH(),
+                                                       m->eS(), m->eO(), m->eT(), m->esx(),
+                                                       stage > 0);
+    const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
+    k_planes_nt<float2><<<tg, tb, 0, s>>>(P, nk, m->eO(), m->pl, M_P, M_PT, nw);
+    k_planes_nt<float2><<<tg, tb, 0, s>>>(C, nk, m->eO(), m->pl, M_C, -1, nw, m->cdf, m->xdg);
+    k_planes_nt<float2><<<tg, tb, 0, s>>>(D, nk, m->eO(), m->pl, M_D, -1, nw, m->cdf + 2 * vn,
+                                          m->xdg + vn);
+    if (have_x) {
+      // the traces of C and D (direct terms) come from the shear's diagonal partials
+      const int nbk = (nk + 31) / 32, ndd = 32 * ((2 * nk + 31) / 32);
+      int ny = 0;   // dd blocks of the band per t' block
+      for (int i = 0; i < nbk; ++i) {
+        int cnt = 0;
+        for (int j = shear_first_block(nk, 32 * i); 32 * j < ndd; ++j)
+          if (shear_block_live(nk, 32 * i, 32 * j)) cnt = j - shear_first_block(nk, 32 * i) + 1;
+        ny = std::max(ny, cnt);
+      }
+      k_shear_tiles<<<dim3(nbk, ny, 3 * nw), dim3(32, 8), 0, s>>>(nk, nw, ndd, P, C, D, m->eS(),
+                                                                 m->sp, m->tpart);
+      k_trace_from_shear<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, nbk, ndd,
+                                                                               m->tpart, m->trf);
+    }
+  }
   int rc = SBE_OK;
-  const int have_x = (W0.flags & SBE_F_EXCITONS) ? 1 : 0;
   if (have_x) {
-    // the traces of C and D (direct terms) come from the shear's diagonal partials
-    const int nb = (nk + 31) / 32, ndd = 32 * ((2 * nk + 31) / 32);
-    int ny = 0;   // dd blocks of the band per t' block
-    for (int i = 0; i < nb; ++i) {
-      int cnt = 0;
-      for (int j = shear_first_block(nk, 32 * i); 32 * j < ndd; ++j)
-        if (shear_block_live(nk, 32 * i, 32 * j)) cnt = j - shear_first_block(nk, 32 * i) + 1;
-      ny = std::max(ny, cnt);
-    }
-    k_shear_tiles<<<dim3(nb, ny, 3 * nw), dim3(32, 8), 0, s>>>(nk, nw, ndd, P, C, D, m->eS(),
-                                                              m->sp, m->tpart);
-    k_trace_from_shear<<<dim3((2 * nk - 1 + 127) / 128, 2, nw), 128, 0, s>>>(nk, nb, ndd,
-                                                                             m->tpart, m->trf);
-    // the three exchange products (eh, ee, hh) as one persistent launch
-    tc::GemmJob jobs[3];
-    for (int n = 0; n < 3; ++n) {
-      tc::Term t{n, n, 0, 0, 1};
-      tc::EpiArgs e{};
-      e.kind = tc::EPI_F32;
-      e.outf = m->xsh + (long long)n * nw * 2 * mm;
-      e.out_bstride = 2 * mm;
-      e.ldo = 2 * nk;
-      e.unshear = nk;
-      e.escale = m->esx();
-      e.err = m->err();
-      jobs[n] = job(m, m->tp, m->sp, nk, 4 * nk, nk, 0, 1, &t, 1, e);
-    }
+    // the three exchange products (eh, ee, hh) of every bucket
     ProfScope ps(c, 1, s);
-    rc = tc_gemm_launch(jobs, 3, s);
+    rc = launch_jobs(all_jobs(c, JK_EXCH), s);
     if (rc) return rc;
   }
-  k_h_build<<<dim3((nk + 511) / 512, (nk + HB_ROWS - 1) / HB_ROWS, nw), 128, 0, s>>>(
-      c->d_wires, m->ekf, m->vsf, c->Ee, c->Eh, m->trf, reinterpret_cast<const float2*>(m->xsh),
-      have_x, m->hf, tm, m->dgE, m->dgH,
-      m->dgf, m->mxH());
-  // H exponent: max over the operands and the step's 2 hbar |A|, |B|
-  k_exponents2_sum<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH(), m->eO(),
-                                                    m->esc());
-  k_planes_nt<float2><<<tg, tb, 0, s>>>(m->hf, nk, m->eH(), m->pl, M_EH, M_EHT, nw);
-  k_hplanes<<<dim3((nk + 31) / 32, (nk + 31) / 32, nw), dim3(32, 8), 0, s>>>(
-      m->hf + tm, m->hf + 2 * tm, m->habf, m->habf + tm, nk, m->eH(), m->pl, nw);
-  // commutator GEMMs (term lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt,
-  // SBEs.py:2309-2327 and 2607-2625, through their W - W^H form)
-  const tc::Term tP[4] = {{M_HHX, M_PT, 0, 0, 1}, {M_D, M_EH, 1, 0, -1},
-                          {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_C, 0, 1, -1}};
-  const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
-  const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
-  const tc::Term* tl[3] = {tP, tC, tD};
-  const int nt[3] = {4, 2, 2};
-  // G buffer (FP32 complex, tm each): [W hh K-half 0, W hh K-half 1, V hh 0, V hh 1,
-  // dP sums, W cross terms, V cross terms]; the partials of W and V meet in the
-  // anti-Hermitian pass
-  float2* wf = reinterpret_cast<float2*>(c->G);   // the buffer holds 12 tm float2
+  // the Hamiltonians: Meh + diagonal + direct + exchange, diagonal peeled; their planes
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    k_h_build<<<dim3((nk + 511) / 512, (nk + HB_ROWS - 1) / HB_ROWS, nw), 128, 0, s>>>(
+        m->dw, A->ekf, m->vsf, c->Ee, c->Eh, m->trf, reinterpret_cast<const float2*>(m->xsh),
+        have_x, A->hf, tm, m->dgE, m->dgH, m->dgf, m->mxH());
+    // H exponent: max over the operands and the step's 2 hbar |A|, |B|
+    k_exponents2_sum<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->mxH(), m->mxAB(), m->eH(), m->eO(),
+                                                      m->esc());
+    const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
+    k_planes_nt<float2><<<tg, tb, 0, s>>>(A->hf + m->bm, nk, m->eH(), m->pl, M_EH, M_EHT, nw);
+    k_hplanes<<<tg, tb, 0, s>>>(A->hf + tm + m->bm, A->hf + 2 * tm + m->bm, A->habf + m->bm,
+                                A->habf + tm + m->bm, nk, m->eH(), m->pl, nw);
+  }
+  // commutator GEMMs: dP and the cross terms of W and V, then the hi*hi products of
+  // W and V (the partials of W and V meet in the anti-Hermitian pass)
+  {
+    ProfScope ps(c, 0, s);
+    rc = launch_jobs(all_jobs(c, JK_FULL), s);
+    if (rc) return rc;
+  }
+  {
+    ProfScope ps(c, 0, s);
+    rc = launch_jobs(all_jobs(c, JK_HH), s);
+    if (rc) return rc;
+  }
+  float2* wf = reinterpret_cast<float2*>(c->G);
   float2* gp = wf + 4 * tm;
   float2* wx = wf + 5 * tm;
   float2* vx = wf + 6 * tm;
-  auto epi = [&](float2* out) {
-    tc::EpiArgs e{};
-    e.kind = tc::EPI_RAWF;
-    e.outf2 = out;
-    e.out_bstride = mm;
-    e.ks_stride = tm;
-    e.escale = m->esc();
-    e.err = m->err();
-    return e;
-  };
-  // dP and the hi*lo + lo*hi parts of W and V in one launch; the hi*hi parts of W
-  // and V (their W - W^H is a small difference of large products near
-  // equilibrium) as two K halves each with one accumulator per real product
-  tc::GemmJob full[3] = {job(m, m->pl, m->pl, nk, nk, nk, 1, nt[0], tl[0], 0, epi(gp)),
-                         job(m, m->pl, m->pl, nk, nk, nk, 1, nt[1], tl[1], 0, epi(wx),
-                             tc::MODE_FULL, 1),
-                         job(m, m->pl, m->pl, nk, nk, nk, 1, nt[2], tl[2], 0, epi(vx),
-                             tc::MODE_FULL, 1)};
-  tc::GemmJob hh[2] = {job(m, m->pl, m->pl, nk, nk, nk, 1, nt[1], tl[1], 0, epi(wf),
-                           tc::MODE_HH, 0, 2),
-                       job(m, m->pl, m->pl, nk, nk, nk, 1, nt[2], tl[2], 0, epi(wf + 2 * tm),
-                           tc::MODE_HH, 0, 2)};
-  {
-    ProfScope ps(c, 0, s);
-    rc = tc_gemm_launch(full, 3, s);
-    if (rc) return rc;
-  }
-  {
-    ProfScope ps(c, 0, s);
-    rc = tc_gemm_launch(hh, 2, s);
-    if (rc) return rc;
-  }
-  const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
-  Rk4Ctl rk[3];
-  // stage buffers (FP32, 3 tm each): the step-start state, then the stage states
+  // stage buffers (FP32, 3 tot_mat each): the step-start state, then the stage states
   float2* x0 = reinterpret_cast<float2*>(c->xs);
   float2* xn = x0 + 3 * tm;
-  for (int i = 0; i < 3; ++i) {
-    rk[i] = Rk4Ctl{};
-    rk[i].stage = stage;
-    rk[i].peel = i > 0;
-    rk[i].dt = dt;
-    rk[i].X = X64 ? X64[i] : nullptr;
-    rk[i].x0 = x0 + i * tm;
-    rk[i].acc = m->accf + i * tm;
-    rk[i].xf = xn + i * tm;
-    rk[i].dg = i > 0 ? m->xdg + (i - 1) * vn : nullptr;
-    rk[i].mx = m->mxS();
-    rk[i].mo = m->mxO();
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const long long vn = (long long)nw * nk, o = m->bm;
+    const float2 *P = xs + o, *C = xs + tm + o, *D = xs + 2 * tm + o;
+    Rk4Ctl rk[3];
+    for (int i = 0; i < 3; ++i) {
+      rk[i] = Rk4Ctl{};
+      rk[i].stage = stage;
+      rk[i].peel = i > 0;
+      rk[i].dt = dt;
+      rk[i].X = X64 ? X64[i] + o : nullptr;
+      rk[i].x0 = x0 + i * tm + o;
+      rk[i].acc = A->accf + i * tm + o;
+      rk[i].xf = xn + i * tm + o;
+      rk[i].dg = i > 0 ? m->xdg + (i - 1) * vn : nullptr;
+      rk[i].mx = m->mxS();
+      rk[i].mo = m->mxO();
+    }
+    const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
+    k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp + o, A->hf + o, P, m->dgf, m->gamf, m->cdf, A->kf + o,
+                              rk[0]);
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + o, wf + tm + o, wx + o, A->hf + tm + o, C, m->dgf,
+                                 m->dgf + vn, m->cdf, m->cdf + vn, A->kf + tm + o, rk[1]);
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm + o, wf + 3 * tm + o, vx + o, A->hf + 2 * tm + o,
+                                 D, m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn,
+                                 m->cdf + 3 * vn, A->kf + 2 * tm + o, rk[2]);
   }
-  k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp, m->hf, st[0], m->dgf, m->gamf, m->cdf, m->kf, rk[0]);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf, wf + tm, wx, m->hf + tm, C, m->dgf, m->dgf + vn, m->cdf,
-                               m->cdf + vn, m->kf + tm, rk[1]);
-  k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm, wf + 3 * tm, vx, m->hf + 2 * tm, D,
-                               m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn, m->cdf + 3 * vn,
-                               m->kf + 2 * tm, rk[2]);
   return cuda_check(cudaGetLastError(), "mixed stage");
 }
 
@@ -1730,42 +1787,32 @@ static int mixed_stage(SbeCtx* c, const float2* P, const float2* C, const float2
 // state_max_ready is set.
 static int mixed_sources(SbeCtx* c, const double2* P, const double2* C, const double2* D,
                          double2* src, int state_max_ready, cudaStream_t s) {
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const int nk = m->nk, nw = m->nw;
-  const long long mm = (long long)nk * nk;
-  if (!state_max_ready) {
-    cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
-    absmax_into(P, mm, nw, m->mxS(), s);
-    absmax_into(C, mm, nw, m->mxS(), s);
-    absmax_into(D, mm, nw, m->mxS(), s);
+  MixedAll* A = all_of(c);
+  for (Mixed* m : A->b) {
+    const int nk = m->nk, nw = m->nw;
+    const long long mm = (long long)nk * nk, o = m->bm;
+    if (!state_max_ready) {
+      cudaMemsetAsync(m->mxS(), 0, sizeof(unsigned) * nw, s);
+      absmax_into(P + o, mm, nw, m->mxS(), s);
+      absmax_into(C + o, mm, nw, m->mxS(), s);
+      absmax_into(D + o, mm, nw, m->mxS(), s);
+    }
+    exponents_from(m, m->mxS(), m->eS(), s);
+    const double2* st[3] = {P + o, C + o, D + o};
+    const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
+    for (int i = 0; i < 3; ++i)
+      k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->pl, 2 * i, -1, nw);
+    k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
   }
-  exponents_from(m, m->mxS(), m->eS(), s);
-  const double2* st[3] = {P, C, D};
-  const dim3 tb(32, 8), tg((nk + 31) / 32, (nk + 31) / 32, nw);
-  for (int i = 0; i < 3; ++i)
-    k_planes_nt<double2><<<tg, tb, 0, s>>>(st[i], nk, m->eS(), m->pl, 2 * i, -1, nw);
-  k_add_int<<<(nw + 127) / 128, 128, 0, s>>>(nw, m->eS(), m->eE(), m->ess());
   float2* gf = reinterpret_cast<float2*>(c->G);
-  tc::GemmJob jobs[3];
-  for (int i = 0; i < 3; ++i) {
-    tc::Term t{2 * i, 0, i == 2 ? 1 : 0, 0, 1};
-    tc::EpiArgs e{};
-    e.kind = tc::EPI_RAWF;
-    e.outf2 = gf + i * c->tot_kr;
-    e.out_bstride = (long long)nk * m->nr;
-    e.ldo = m->nr;
-    e.escale = m->ess();
-    e.err = m->err();
-    jobs[i] = job(m, m->pl, m->ep, nk, m->nr, nk, 1, 1, &t, 0, e);
-  }
   {
     ProfScope ps(c, 2, s);
-    int rc = tc_gemm_launch(jobs, 3, s);
+    const int rc = launch_jobs(all_jobs(c, JK_SRC), s);
     if (rc) return rc;
   }
-
-  k_src_reduce_f<<<dim3((m->nr + 31) / 32, nw), dim3(32, 8), 0, s>>>(c->d_wires, m->ekrf, gf,
-                                                                    c->tot_kr, c->window, src);
+  for (Mixed* m : A->b)
+    k_src_reduce_f<<<dim3((m->nr + 31) / 32, m->nw), dim3(32, 8), 0, s>>>(
+        m->dw, A->ekrf, gf, c->tot_kr, c->window, src);
   launch_sources_final(c, c->ne, c->nh, src, s);
   return cuda_check(cudaGetLastError(), "mixed sources");
 }
@@ -1784,17 +1831,16 @@ int rhs_mixed(SbeCtx* c, const double2* P, const double2* C, const double2* D, c
   if (rc) return rc;
   rc = mixed_prep(c, C, D, s);
   if (rc) return rc;
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  const long long n = c->tot_mat, vn = (long long)m->nw * m->nk;
+  MixedAll* A = all_of(c);
+  const long long n = c->tot_mat;
   mixed_state_in(c, P, C, D, s);
-  const float2* xf = reinterpret_cast<const float2*>(c->xs);
-  rc = mixed_stage(c, xf, xf + n, xf + 2 * n, m->xdg, m->xdg + vn, Ek, nullptr, 0.0, 0, 0.f,
-                   nullptr, s);
+  rc = mixed_stage(c, reinterpret_cast<const float2*>(c->xs), Ek, nullptr, 0.0, 0, 0.f, nullptr,
+                   s);
   if (rc) return rc;
   const int g = (int)((n + 255) / 256);
-  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf, dP);
-  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf + n, dC);
-  k_f32_to_f64<<<g, 256, 0, s>>>(n, m->kf + 2 * n, dD);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, A->kf, dP);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, A->kf + n, dC);
+  k_f32_to_f64<<<g, 256, 0, s>>>(n, A->kf + 2 * n, dD);
   return cuda_check(cudaGetLastError(), "rhs_mixed");
 }
 
@@ -1804,21 +1850,17 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   if (rc) return rc;
   rc = mixed_prep(c, C, D, s);
   if (rc) return rc;
-  Mixed* m = static_cast<Mixed*>(c->mixed);
   const long long n = c->tot_mat;
   const double frac[4] = {0.0, 0.5, 0.5, 1.0};
-  const long long vn = (long long)m->nw * m->nk;
-  // FP32 stage buffers in the FP64 stage-state block (6 tm float2): the step-start
-  // state (kept for the RK4 updates), then the stage states of stages 2-4
+  // FP32 stage buffers in the FP64 stage-state block (6 tot_mat float2): the
+  // step-start state (kept for the RK4 updates), then the stage states of stages 2-4
   float2* x0 = reinterpret_cast<float2*>(c->xs);
   mixed_state_in(c, P, C, D, s);
   double2* X64[3] = {P, C, D};
   for (int st = 1; st <= 4; ++st) {
     // the RHS of this stage (stage field Ek0 + frac dEk) and its RK4 update (fused
     // into the element-wise passes)
-    float2* xs = st == 1 ? x0 : x0 + 3 * n;
-    rc = mixed_stage(c, xs, xs + n, xs + 2 * n, m->xdg, m->xdg + vn, Ek0, dEk, frac[st - 1], st,
-                     (float)dt, X64, s);
+    rc = mixed_stage(c, st == 1 ? x0 : x0 + 3 * n, Ek0, dEk, frac[st - 1], st, (float)dt, X64, s);
     if (rc) return rc;
   }
   mixed_relax(c, P, C, D, Ek0, dt, s);   // the new diagonals join the maximum
@@ -1850,22 +1892,20 @@ extern "C" int sbe_convert_selftest(const double* d_in, const float* f_in, long 
   return cuda_check(cudaGetLastError(), "sbe_convert_selftest");
 }
 
-// Device-side error flags of the engine (bounded waits that gave up), read and
+// Device-side error flag of the engine (bounded waits that gave up), read and
 // cleared after the stream has drained.
 extern "C" int sbe_ctx_check(SbeCtx* c, void* stream) {
   if (!c) return fail(SBE_ERR_ARG, "sbe_ctx_check: null context");
   int rc = cuda_check(cudaStreamSynchronize(as_stream(stream)), "sbe_ctx_check");
   if (rc) return rc;
-  Mixed* m = static_cast<Mixed*>(c->mixed);
-  if (!m) return SBE_OK;
-  std::vector<int> h(m->nw);
-  rc = cuda_check(cudaMemcpy(h.data(), m->err(), sizeof(int) * m->nw, cudaMemcpyDeviceToHost),
-                  "sbe_ctx_check: read flags");
+  MixedAll* A = all_of(c);
+  if (!A) return SBE_OK;
+  int h = 0;
+  rc = cuda_check(cudaMemcpy(&h, A->err, sizeof(int), cudaMemcpyDeviceToHost),
+                  "sbe_ctx_check: read flag");
   if (rc) return rc;
-  int any = 0;
-  for (int v : h) any |= v;
-  if (any) {
-    cudaMemset(m->err(), 0, sizeof(int) * m->nw);
+  if (h) {
+    cudaMemset(A->err, 0, sizeof(int));
     return fail(SBE_ERR_TIMEOUT, "a tensor-core pipeline wait timed out (results of the "
                                  "affected calls are invalid)");
   }

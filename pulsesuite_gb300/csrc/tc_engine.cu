@@ -119,8 +119,15 @@ struct TileInfo {
 template <int BNT>
 __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) {
   TileInfo ti;
-  int j = 0;
-  while (j + 1 < L.njobs && t >= L.tile_base[j + 1]) ++j;
+  // job of tile t: the last j with tile_base[j] <= t (binary search)
+  int j = 0, hi = L.njobs - 1;
+  while (j < hi) {
+    const int mid = (j + hi + 1) >> 1;
+    if (L.tile_base[mid] <= t)
+      j = mid;
+    else
+      hi = mid - 1;
+  }
   const GemmDesc& d = L.job[j].d;
   long long r = t - L.tile_base[j];
   const int tn = (d.N + BNT - 1) / BNT, tm = (d.M + BM - 1) / BM;
@@ -302,7 +309,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const int buf = lt % nbuf, use = lt / nbuf;
       if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) break;
       tc_fence_after();
-      const uint32_t acc_re = tmem + buf * 256, acc_im = tmem + 256;
+      // accumulator columns of the tile: [re | im] (BNT each) at buf * 256
+      const uint32_t acc_re = tmem + buf * 256, acc_im = acc_re + BNT;
       bool first = true;
       int s = (int)(g % nstage);
       uint32_t ph = (uint32_t)((g / nstage) & 1);
@@ -425,7 +433,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         } else if (have) {
           tmem_ld16(lane_addr + c * 16, re);
           if (cplx) {
-            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + 256 + c * 16, im);
+            tmem_ld16(lane_addr + BNT + c * 16, im);
           } else {
 #pragma unroll
             for (int j = 0; j < 16; ++j) im[j] = 0.f;
@@ -473,6 +481,8 @@ int tc_gemm_init() {
   if (!attr) {
     if (cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN, tc::MODE_FULL>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(tc::k_tc_gemm<128, tc::MODE_FULL>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
         cudaFuncSetAttribute(tc::k_tc_gemm<tc::BN_HH, tc::MODE_HH>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess)
       return fail(SBE_ERR_CUDA, "tc_gemm: cannot raise the shared-memory limit");
@@ -511,19 +521,22 @@ static bool job_ok(const tc::GemmDesc& d) {
 int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   int rc = tc_gemm_init();
   if (rc) return rc;
-  if (njobs < 1 || njobs > tc::MAX_JOBS) return fail(SBE_ERR_ARG, "tc_gemm: 1 to 4 jobs per launch");
+  if (njobs < 1 || njobs > tc::MAX_JOBS)
+    return fail(SBE_ERR_ARG, "tc_gemm: 1 to " + std::to_string(tc::MAX_JOBS) + " jobs per launch");
   tc::GemmLaunch L{};
   L.njobs = njobs;
   const int mode = jobs[0].d.mode;
   const int cplx = jobs[0].d.complex_mode;
   if (mode != tc::MODE_FULL && mode != tc::MODE_HH) return fail(SBE_ERR_ARG, "tc_gemm: bad mode");
-  const int bnt = mode == tc::MODE_HH ? tc::BN_HH : tc::BN;
+  const int bn = jobs[0].d.bn;
+  if (bn != 0 && bn != 128 && bn != 256) return fail(SBE_ERR_ARG, "tc_gemm: N tile 128 or 256");
+  const int bnt = mode == tc::MODE_HH ? tc::BN_HH : (bn == 128 ? 128 : tc::BN);
   long long nt = 0;
   for (int j = 0; j < njobs; ++j) {
     const tc::GemmDesc& d = jobs[j].d;
     if (!job_ok(d)) return fail(SBE_ERR_ARG, "tc_gemm: operand plane sets do not cover the launch");
-    if (d.mode != mode || d.complex_mode != cplx)
-      return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode");
+    if (d.mode != mode || d.complex_mode != cplx || d.bn != bn)
+      return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode and N tile");
     if ((mode == tc::MODE_HH || d.xonly) && (!d.complex_mode || d.kskip))
       return fail(SBE_ERR_ARG, "tc_gemm: hi*hi and cross-term modes are complex and unskipped only");
     if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
@@ -543,6 +556,8 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   const int grid = (int)std::min<long long>(nt, num_sms());
   if (mode == tc::MODE_HH)
     tc::k_tc_gemm<tc::BN_HH, tc::MODE_HH><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
+  else if (bnt == 128)
+    tc::k_tc_gemm<128, tc::MODE_FULL><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
   else
     tc::k_tc_gemm<tc::BN, tc::MODE_FULL><<<grid, tc::NUM_THREADS, kTcSmem, s>>>(L);
   return cuda_check(cudaGetLastError(), "tc_gemm launch");

@@ -8,7 +8,7 @@
 // textbook formula (conjugation and sign by the MMA's operand-negate bit), all
 // accumulated in FP32 in tensor memory.
 //
-// Tiles: BM = 128 rows, BN = 256 (or 64) columns, BK = 32 (64-byte rows,
+// Tiles: BM = 128 rows, BN = 256 or 128 columns, BK = 32 (64-byte rows,
 // K-major on both operands, 64-byte swizzle).  The planes live in global memory
 // in the tile layout of PlaneSet: every operand tile is one contiguous chunk,
 // moved to shared memory with a single cp.async.bulk.
@@ -36,7 +36,7 @@ constexpr int A_TILE_BYTES = BM * BK * 2;   // 8 KB
 constexpr int B_TILE_BYTES = BN * BK * 2;   // 16 KB
 constexpr int NUM_THREADS = 320;   // producer warp, MMA warp, 8 epilogue warps
 constexpr int MAX_TERMS = 4;
-constexpr int MAX_JOBS = 4;
+constexpr int MAX_JOBS = 32;   // jobs per launch (e.g. three GEMMs for each of ten Nk buckets)
 // bounded waits: an iteration limit after which the kernel flags an error
 constexpr long long WAIT_LIMIT = 1ll << 28;
 
@@ -136,6 +136,10 @@ struct GemmDesc {
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
   // written at out + ks * ks_stride (ksplit 0 counts as 1)
   int ksplit;
+  // N tile of MODE_FULL: 256 (0 = the default) or 128; with 128 a complex tile's
+  // accumulators take 256 TMEM columns, so two tiles are in flight (the epilogue of
+  // one overlaps the MMAs of the next) at twice the operand loads per output
+  int bn;
   PlaneSet A, B;              // operand planes (A: M rows, B: N rows, both K-major)
 };
 
@@ -144,13 +148,15 @@ struct GemmJob {
   EpiArgs e;
 };
 
-// one launch: the concatenated tile lists of njobs jobs (same mode and complex flag)
+// one launch: the concatenated tile lists of njobs jobs (same mode and complex flag),
+// passed as one __grid_constant__ kernel parameter
 struct GemmLaunch {
   GemmJob job[MAX_JOBS];
   long long tile_base[MAX_JOBS + 1];
   int njobs;
   int* sched;                 // tile counter of this launch (zeroed before it)
 };
+static_assert(sizeof(GemmLaunch) <= 32000, "kernel parameter space (32 KB) exceeded");
 
 }  // namespace tc
 

@@ -5,7 +5,9 @@ whose one-time tables (Coulomb V(q), Chi1D, phonon EP/HP, dephasing index maps,
 e^{ikr}, window) live on the GPU.  State tensors are owned by the caller and are
 packed: wire w's Nk x Nk matrix starts at element ``mat_offset[w]`` of a flat
 complex128 tensor; the per-wire field / source vectors (length Nr = 2 Nk + 2)
-start at ``r_offset[w]``.
+start at ``r_offset[w]``.  The layout groups the wires by Nk (ascending; the
+caller's order within one Nk), so use ``pack`` / ``pack_r`` / ``mat`` / ``rvec``
+rather than concatenating per-wire blocks.
 """
 
 import ctypes
@@ -157,8 +159,19 @@ class WireContext:
         return flat[o:o + ncomp * nr].view(ncomp, nr)
 
     def pack(self, mats):
-        flat = [torch.as_tensor(m).reshape(-1).to(self.device, CDTYPE) for m in mats]
-        return torch.cat(flat).contiguous()
+        """Packed state tensor of one Nk x Nk matrix per wire (caller's wire order; each
+        placed at its wire's offset: the layout groups the wires by Nk)."""
+        out = torch.empty(self.total_mat, dtype=CDTYPE, device=self.device)
+        for w, m in enumerate(mats):
+            self.mat(out, w).copy_(torch.as_tensor(m).reshape(self.nk[w], self.nk[w]))
+        return out
+
+    def pack_r(self, vecs, ncomp):
+        """Packed r-vector tensor of one (ncomp, Nr) block per wire (caller's order)."""
+        out = torch.empty(ncomp * self.total_r, dtype=CDTYPE, device=self.device)
+        for w, v in enumerate(vecs):
+            self.rvec(out, w, ncomp).copy_(torch.as_tensor(v).reshape(ncomp, -1))
+        return out
 
     # ---- tables ------------------------------------------------------------
     def table(self, w, name):
@@ -279,6 +292,23 @@ class WireContext:
                                          _lib.ptr(Ek0), _lib.ptr(dEk), float(dt), int(precision),
                                          _lib.ptr(src_out), _lib.stream_handle()), "sbe_rk4_step")
 
+    def local_field(self, e0, de=None, comp=1, Ek0=None, dEk=None):
+        """Field uniform along every wire (sbe_local_field): component ``comp`` of
+        wire w is e0[w] FFTG(window); e0, de: one amplitude per wire (device float64
+        tensors or host sequences).  Fills and returns (Ek0, dEk)."""
+        def dev(v):
+            return torch.as_tensor(v, dtype=torch.float64, device=self.device).contiguous()
+        e0 = dev(e0)
+        de = None if de is None else dev(de)
+        if Ek0 is None:
+            Ek0 = self.zeros_r(3)
+        if dEk is None and de is not None:
+            dEk = self.zeros_r(3)
+        _lib.check(self.lib.sbe_local_field(self.handle, _lib.ptr(e0), _lib.ptr(de), int(comp),
+                                            _lib.ptr(Ek0), _lib.ptr(dEk),
+                                            _lib.stream_handle()), "sbe_local_field")
+        return Ek0, dEk
+
     def rk4_graph(self, P, C, D, Ek0, dEk, dt, src_out, precision=_lib.PREC_FP64):
         """Capture one rk4_step on these buffers into a CUDA graph (RK4Graph)."""
         return RK4Graph(self, P, C, D, Ek0, dEk, dt, src_out, precision)
@@ -293,6 +323,23 @@ class WireContext:
                                               _lib.ptr(De), _lib.ptr(Dh), _lib.stream_handle()),
                    "sbe_deph_selftest")
         return De, Dh
+
+    def autotune(self, cache_json=None):
+        """Choose the mixed path's GEMM tiles per Nk bucket (sbe_autotune): time both
+        N tiles, or load the choice cached in ``cache_json`` for this device and these
+        buckets; returns ``tiles()``."""
+        path = None if cache_json is None else str(cache_json).encode()
+        _lib.check(self.lib.sbe_autotune(self.handle, path), "sbe_autotune")
+        return self.tiles()
+
+    def tiles(self):
+        """Per bucket (Nk, wires, exchange tile, commutator tile, source tile)."""
+        cap = 5 * self.nw
+        out = (ctypes.c_int * cap)()
+        nb = ctypes.c_int()
+        _lib.check(self.lib.sbe_ctx_tiles(self.handle, out, cap, ctypes.byref(nb)),
+                   "sbe_ctx_tiles")
+        return [tuple(out[5 * i:5 * i + 5]) for i in range(nb.value)]
 
     def check(self):
         """Wait for the current stream and raise if a device-side bounded wait gave up."""

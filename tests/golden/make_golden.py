@@ -45,6 +45,11 @@ pstd            Pieces of the field step: ``usefulsubs.dfdx1D`` on FFT-order
                 wavenumbers (``libpulsesuite.helpers.GetKArray``), the grids of
                 ``typespace`` and ``helpers``, and ``rhoPJ.ElongfromRho`` on an
                 (Nx, 1, 1) grid.
+pstd3d          Pieces of the 3-D field step: ``rhoPJ.ElongfromRho`` on a 3-D grid
+                (all ten outputs and the in-place transformed P), the q-space
+                derivatives ``usefulsubs.dfdx1D_q``/``dfdy1D_q``/``dfdx2D_q``/``dfdy2D_q``,
+                ``dfdy2D`` and the axis grids of ``typespace`` and ``helpers`` at
+                256 x 128 x 128 x 20 nm; ``make_golden.py <src> pstd3d`` writes it alone.
 """
 
 import io
@@ -670,6 +675,41 @@ def case_pstd(nx, dx, seed):
                 Exl_PRho=outs[0][:, 0, 0], Exl_P=outs[3][:, 0, 0], Exl_Rho=outs[6][:, 0, 0])
 
 
+def case_pstd3d(seed):
+    from pulsesuite.PSTD3D import rhoPJ, typespace, usefulsubs
+    from pulsesuite.libpulsesuite import helpers
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = 8, 6, 10
+    dx, dy, dz = 20e-9, 25e-9, 15e-9
+    sp = typespace.ss(3, nx, ny, nz, dx, dy, dz, 12.9)
+    qx, qy, qz = typespace.GetKxArray(sp), typespace.GetKyArray(sp), typespace.GetKzArray(sp)
+    rho = cnormal(rng, (nx, ny, nz), 1.0)
+    P = [cnormal(rng, (nx, ny, nz), 1e-9) for _ in range(3)]
+    Pin = [a.copy() for a in P]
+    outs = [np.zeros((nx, ny, nz), complex) for _ in range(10)]
+    rhoPJ.ElongfromRho(sp, rho.copy(), P[0], P[1], P[2], *outs)
+    out = dict(nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, epsr=typespace.GetEpsr(sp), qx=qx,
+               qy=qy, qz=qz, rho=rho, Px=Pin[0], Py=Pin[1], Pz=Pin[2], Pk_x=P[0], Pk_y=P[1],
+               Pk_z=P[2])
+    names = ("ExlfromPRho", "EylfromPRho", "EzlfromPRho", "ExlfromP", "EylfromP", "EzlfromP",
+             "ExlfromRho", "EylfromRho", "EzlfromRho", "RhoBound")
+    for nm, a in zip(names, outs):
+        out[nm] = a
+    # q-space and FFT derivatives
+    f1 = cnormal(rng, (24,), 1.0)
+    f2 = cnormal(rng, (24, 10), 1.0)
+    qa = helpers.GetKArray(24, 24 * 7e-9)
+    qb = helpers.GetKArray(10, 10 * 9e-9)
+    out.update(f1=f1, f2=f2, qa=qa, qb=qb, dfdx1D_q=usefulsubs.dfdx1D_q(f1, qa),
+               dfdy1D_q=usefulsubs.dfdy1D_q(f1, qa), dfdx2D_q=usefulsubs.dfdx2D_q(f2, qa),
+               dfdy2D_q=usefulsubs.dfdy2D_q(f2, qb), dfdy2D=usefulsubs.dfdy2D(f2.copy(), qb))
+    # the axes of the 256 x 128 x 128 x 20 nm grid
+    for ax, n in (("x", 256), ("y", 128), ("z", 128)):
+        out[f"grid_{ax}"] = typespace.GetSpaceArray(n, (n - 1) * 20e-9)
+        out[f"q_{ax}"] = helpers.GetKArray(n, n * 20e-9)
+    return out
+
+
 def main():
     ref_src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PULSESUITE_SRC")
     if not ref_src or not os.path.isdir(ref_src):
@@ -711,8 +751,10 @@ def main():
                 if only in (None, "solver100"):
                     np.savez_compressed(os.path.join(HERE, "solver_100.npz"),
                                         **case_solver100(14.5e-9, 100, 0.1e-15, 2e7, 41))
+                if only in (None, "pstd3d"):
+                    np.savez_compressed(os.path.join(HERE, "pstd3d.npz"), **case_pstd3d(60))
                 if only in ("mbc", "emission", "dc", "backup", "info", "coupling3d",
-                            "solver100"):
+                            "solver100", "pstd3d"):
                     return
                 for nk, seed in ((7, 10), (16, 11), (30, 12)):
                     np.savez_compressed(os.path.join(HERE, f"kernels_nk{nk}.npz"), **case_kernels(nk, seed))

@@ -69,8 +69,8 @@ def field_basis(ctx):
     for w in range(ctx.nw):
         wk = ctx.table(w, "window_k")
         z = torch.zeros_like(wk)
-        parts.append(torch.stack([z, wk, z]).reshape(-1))
-    return torch.cat(parts).contiguous()
+        parts.append(torch.stack([z, wk, z]))
+    return ctx.pack_r(parts, 3)
 
 
 def pulse(t, E0, tau):

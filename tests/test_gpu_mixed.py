@@ -52,7 +52,7 @@ def fields(ctx, amps):
         wk = ctx.table(w, "window_k").cpu().numpy()
         z = np.zeros_like(wk)
         out.append(np.stack([z, a * wk, z]))
-    return torch.as_tensor(np.concatenate([f.reshape(-1) for f in out])).cuda()
+    return ctx.pack_r(out, 3)
 
 
 def rel(a, b):

@@ -271,8 +271,8 @@ def test_batched_rhs_and_rk4_vs_oracle(nk):
     P = c.pack([s[0] for s in states])
     C = c.pack([s[1] for s in states])
     D = c.pack([s[2] for s in states])
-    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
-    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    Ek = c.pack_r([np.stack(f) for f in fields], 3)
+    dEk = c.pack_r([np.stack(f) for f in dfields], 3)
     dP, dC, dD = c.rhs(P, C, D, Ek)
     for w in range(nw):
         rP, rC, rD, _ = wires[w].rhs(*states[w], *fields[w], w + 1)
@@ -331,8 +331,8 @@ def test_rk4_with_carrier_scattering_vs_oracle(lorentz):
     P = c.pack([s[0] for s in states])
     C = c.pack([s[1] for s in states])
     D = c.pack([s[2] for s in states])
-    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
-    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    Ek = c.pack_r([np.stack(f) for f in fields], 3)
+    dEk = c.pack_r([np.stack(f) for f in dfields], 3)
     dt = 0.1e-15
     src = c.zeros_r(5)
     c.rk4_step(P, C, D, Ek, dEk, dt, src)
@@ -374,8 +374,8 @@ def test_rk4_with_recombination_vs_oracle():
     P = c.pack([s[0] for s in states])
     C = c.pack([s[1] for s in states])
     D = c.pack([s[2] for s in states])
-    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
-    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    Ek = c.pack_r([np.stack(f) for f in fields], 3)
+    dEk = c.pack_r([np.stack(f) for f in dfields], 3)
     dt = 0.1e-15
     src = c.zeros_r(5)
     c.rk4_step(P, C, D, Ek, dEk, dt, src)
@@ -414,8 +414,8 @@ def test_rk4_with_dc_transport_vs_oracle(lf):
     P = c.pack([s[0] for s in states])
     C = c.pack([s[1] for s in states])
     D = c.pack([s[2] for s in states])
-    Ek = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in fields]).cuda()
-    dEk = torch.cat([torch.as_tensor(np.stack(f)).reshape(-1) for f in dfields]).cuda()
+    Ek = c.pack_r([np.stack(f) for f in fields], 3)
+    dEk = c.pack_r([np.stack(f) for f in dfields], 3)
     dt = 0.1e-15
     src = c.zeros_r(5)
     c.rk4_step(P, C, D, Ek, dEk, dt, src)

@@ -169,8 +169,8 @@ def test_sample_and_deposit_vs_oracle():
         s = np.stack([(1.0 + 0.3j * c) * np.cos(np.pi * r / (2 * wi.g["L"]) * (c + 1))
                       * rng.standard_normal() for c in range(5)])
         srcs.append(list(s))
-        flat.append(s.reshape(-1))
-    line.view("src").copy_(dev(np.concatenate(flat)))
+        flat.append(s)
+    line.view("src").copy_(ctx.pack_r(flat, 5))
     line.deposit()
     Pg, rho = ol.deposit(srcs)
     assert rel(host(line.view("Pg")), Pg) < 1e-12

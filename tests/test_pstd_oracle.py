@@ -134,3 +134,95 @@ def test_sheet_source_launches_incident_amplitude():
         E, H = p.step(E, H, J, dt)
         peak = max(peak, abs(E[0, 400].real))
     assert 0.97 < peak < 1.03
+
+
+# ---- 3-D grid ---------------------------------------------------------------
+
+def test_elong3d_matches_reference():
+    """rhoPJ.ElongfromRho on a 3-D grid with the reference's own (centred) k tables:
+    all ten outputs and the transformed P it leaves in its inputs."""
+    g = golden("pstd3d")
+    e_prho, e_p, e_rho, rho_b, pk = PO.elong3d(g["rho"], g["Px"], g["Py"], g["Pz"], g["qx"],
+                                               g["qy"], g["qz"], float(g["epsr"]))
+    for c, ax in enumerate("xyz"):
+        assert rel(e_prho[c], g[f"E{ax}lfromPRho"]) < 1e-14
+        assert rel(e_p[c], g[f"E{ax}lfromP"]) < 1e-14
+        assert rel(e_rho[c], g[f"E{ax}lfromRho"]) < 1e-14
+        assert rel(pk[c], g[f"Pk_{ax}"]) < 1e-14
+    assert rel(rho_b, g["RhoBound"]) < 1e-14
+
+
+def test_qspace_derivatives_and_3d_axes_match_reference():
+    """usefulsubs.py:233-380: the q-space derivative is f (i q) along the axis; the
+    FFT derivative of a 2-D array along y; the axes of the 256 x 128 x 128 x 20 nm grid."""
+    g = golden("pstd3d")
+    f1, f2, qa, qb = g["f1"], g["f2"], g["qa"], g["qb"]
+    assert np.array_equal(f1 * (1j * qa), g["dfdx1D_q"])
+    assert np.array_equal(f1 * (1j * qa), g["dfdy1D_q"])
+    assert np.array_equal(f2 * (1j * qa)[:, None], g["dfdx2D_q"])
+    assert np.array_equal(f2 * (1j * qb)[None, :], g["dfdy2D_q"])
+    d = np.stack([PO.deriv(f2[i], qb) for i in range(f2.shape[0])])
+    assert rel(d, g["dfdy2D"]) < 1e-15
+    for ax, n in (("x", 256), ("y", 128), ("z", 128)):
+        x, q = PO.pstd_grid(n, 20e-9)
+        assert np.array_equal(x, g[f"grid_{ax}"])
+        assert np.array_equal(q, g[f"q_{ax}"])
+
+
+def _plane_wave3(p, kvec, pol):
+    """E, H of a plane wave exp(i k.r) with E along pol (pol . k = 0)."""
+    X = np.meshgrid(*p.x, indexing="ij")
+    phase = np.exp(1j * sum(k * xx for k, xx in zip(kvec, X)))
+    E = np.stack([pol[c] * phase for c in range(3)])
+    return E
+
+
+def test_curl3d_of_grid_modes_and_divergence_free():
+    n, d = (16, 12, 10), (7e-9, 9e-9, 11e-9)
+    p = PO.Pstd3D(n, d, 12.9)
+    m = (2, 1, 3)
+    kvec = [2 * np.pi * mm / (nn * dd) for mm, nn, dd in zip(m, n, d)]
+    pol = np.cross(kvec, [0.3, -1.0, 0.7])
+    E = _plane_wave3(p, kvec, pol)
+    want = np.stack([1j * np.cross(kvec, pol)[c] * E[c] / pol[c] for c in range(3)])
+    assert rel(p.curl(E), want) < 1e-12
+    # div curl = 0 in k space
+    rng = np.random.default_rng(0)
+    F = rng.standard_normal((3,) + n) + 1j * rng.standard_normal((3,) + n)
+    ck = [np.fft.fftn(c) for c in p.curl(F)]
+    div = p.Q[0] * ck[0] + p.Q[1] * ck[1] + p.Q[2] * ck[2]
+    qmax = max(np.abs(q).max() for q in p.q)
+    assert np.abs(div).max() < 1e-12 * qmax * max(np.abs(c).max() for c in ck)
+
+
+def test_leapfrog3d_invariant_and_dispersion():
+    n, d, epsr = (16, 16, 8), (10e-9, 10e-9, 10e-9), 12.9
+    p = PO.Pstd3D(n, d, epsr)
+    v = PO.C0 / np.sqrt(epsr)
+    # stable for v dt |q|max / 2 <= 1 with |q|max = sqrt(3) pi / dx
+    dt = 0.3 * d[0] / v
+    rng = np.random.default_rng(1)
+    E = rng.standard_normal((3,) + n) + 1j * rng.standard_normal((3,) + n)
+    H = 1e-3 * (rng.standard_normal((3,) + n) + 1j * rng.standard_normal((3,) + n))
+    Hn = p.update_h(E, H, dt)
+    e0 = p.energy(E, H, Hn)
+    H = Hn
+    for _ in range(50):
+        E = p.update_e(E, H, None, dt)
+        Hn = p.update_h(E, H, dt)
+        e1 = p.energy(E, H, Hn)
+        H = Hn
+    assert abs(e1 - e0) < 1e-10 * abs(e0)
+    # a plane wave along x advances by the discrete phase: sin(w dt / 2) = v q dt / 2
+    kx = 2 * np.pi * 3 / (n[0] * d[0])
+    pol = np.array([0.0, 1.0, 0.0])
+    E = _plane_wave3(p, [kx, 0.0, 0.0], pol)
+    w = 2.0 / dt * np.arcsin(v * kx * dt / 2.0)
+    eta = np.sqrt(PO.MU0 / (PO.EPS0 * epsr))
+    H = np.stack([0 * E[0], 0 * E[0], E[1] / eta * np.exp(1j * w * dt / 2) *
+                  (v * kx * dt / 2) / np.sin(w * dt / 2)])
+    nsteps = 20
+    for _ in range(nsteps):
+        E, H = p.step(E, H, None, dt)
+    want = _plane_wave3(p, [kx, 0.0, 0.0], pol) * np.exp(-1j * w * nsteps * dt)
+    assert rel(E, want) < 1e-9
