@@ -275,6 +275,47 @@ int sbe_pstd_step(SbePstd* p, double* E, double* H, const double* J, double dt, 
 /* Ex from the charge density rho and the polarisation Px (rhoPJ.py:836-866, x only) */
 int sbe_pstd_elong(SbePstd* p, const double* rho, const double* Px, double* Ex, void* stream);
 
+/* ---- 3-D PSTD field grid ----------------------------------------------------------
+ * Six components on nx x ny x nz (C order, z fastest): E = (Ex, Ey, Ez) and
+ * H = (Hx, Hy, Hz), each 3 x c128 N (N = nx ny nz).  The reference has no 3-D
+ * Maxwell stepper (its 3-D driver sets E analytically, sbetestpropnov30.py:709); the
+ * pieces are the q-space derivative f (i q) along each axis (usefulsubs.py:233-380),
+ * the grids (typespace.py:815-849 positions, helpers.py:838-863 FFT-order
+ * wavenumbers per axis), the mask multiply of ApplyABC (usefulsubs.py:584-609) and
+ * ElongfromRho (rhoPJ.py:703-880).  Leapfrog H^{n+1/2} = H^{n-1/2} - dt/mu0 curl E^n,
+ * E^{n+1} = mask (E^n + dt/eps (curl H^{n+1/2} - J)); curl F = IFFT(i q x FFT F).
+ * fp32_work: the transforms between the first and last pass in FP32 (the fields
+ * stay FP64).                                                                      */
+typedef struct {
+  int n[3];            /* nx, ny, nz: powers of two in [8, 1024]               */
+  int n_abc[3];        /* absorbing cells at both ends of each axis            */
+  int fp32_work;       /* 1: FP32 transforms, 0: FP64                          */
+  int pad0;
+  double d[3];         /* cell sizes (m)                                       */
+  double epsr;         /* background relative permittivity                     */
+  double abc_strength; /* mask = prod over axes of exp(-abc_strength s^2)      */
+} SbePstd3Desc;
+typedef struct SbePstd3 SbePstd3;
+int sbe_pstd3_create(const SbePstd3Desc* desc, void* stream, SbePstd3** out);
+int sbe_pstd3_destroy(SbePstd3* p);
+/* device copies of the positions and FFT-order wavenumbers of one axis (NULL skips) */
+int sbe_pstd3_grid(SbePstd3* p, int axis, double* x, double* q, void* stream);
+/* out = curl F (3 x c128 N each)                                                   */
+int sbe_pstd3_curl(SbePstd3* p, const double* F, double* out, void* stream);
+int sbe_pstd3_update_h(SbePstd3* p, const double* E, double* H, double dt, void* stream);
+int sbe_pstd3_update_e(SbePstd3* p, double* E, const double* H, const double* J, double dt,
+                       void* stream);
+/* update_h then update_e (J may be NULL); dt <= 2 / (v |q|max) is checked.          */
+int sbe_pstd3_step(SbePstd3* p, double* E, double* H, const double* J, double dt, void* stream);
+/* rhoPJ.py:703-880 ElongfromRho with the caller's wavenumber tables qx, qy, qz
+ * (device, nx / ny / nz doubles; the reference passes its centred GetKxArray...):
+ * rho (c128 N), P3 (3 x c128 N) -> out10 = 10 x c128 N [E_PRho x, y, z, E_P x, y, z,
+ * E_Rho x, y, z, RhoBound]; P_k (3 x c128 N, may be NULL) receives the transformed P
+ * that the reference leaves in its P arguments.  FP64 transforms.                  */
+int sbe_pstd3_elong(SbePstd3* p, const double* rho, const double* P3, const double* qx,
+                    const double* qy, const double* qz, double* out10, double* P_k,
+                    void* stream);
+
 /* ---- wires on the PSTD grid (coupled step) --------------------------------------
  * Field -> wire: Prop2QW (qwoptics.py:667-715) with the grid spline evaluated at
  * x_w + r; wire -> field: QW2Prop (qwoptics.py:717-805, no plasmonic
@@ -314,6 +355,48 @@ int sbe_couple_step(SbeCouple* cp, double* P, double* C, double* D, double* E, d
 int sbe_couple_graph_create(SbeCouple* cp, double* P, double* C, double* D, double* E, double* H,
                             double* Ex, double dt, int precision, SbeGraph** out,
                             long long* n_kernels);
+
+/* ---- wires along z on the 3-D grid (coupled 3-D step) ------------------------------
+ * The reference's 3-D driver (rhoPJ.py:117-488 QuantumWire) samples the grid field on
+ * each wire's line (EAtXYZ, usefulsubs.py:1996), steps the wires, forms J = dP/dt and
+ * deposits the wire sources with transverse SHO gates exp(-d^2 / (2 a^2))
+ * (rhoPJ.py:383-389, QWPlacement :655-702); its wires all share one line along x and
+ * it never feeds J back into E.  Here wire w lies along the grid's z axis at
+ * (wire_xy[2w], wire_xy[2w + 1]), centred at z = 0, and each wire deposits its own
+ * gated sources: the wire's (x, y, z) components are the grid's (z, x, y).  The
+ * coupled step feeds J back: sample E^n on every wire (bilinear in x, y, Forsythe-
+ * Malcolm-Moler spline along z, window, FFTG as Prop2QW), H update, RK4 of every wire,
+ * deposit, J = (P^{n+1} - P^n)/dt plus the soft source (a current sheet in the plane
+ * x = x[src_index] along component pol with the profile exp(-(y^2 + z^2)/waist^2)
+ * launching E_inc(t) = E0 exp(-((t - tpeak)/tau)^2) cos(w0 (t - tpeak))), E update.  */
+typedef struct {
+  int src_index;     /* x index of the source plane, -1: none                   */
+  int pol;           /* source current component (0 x, 1 y, 2 z)                */
+  int pad0, pad1;
+  double E0, tau, w0, tpeak;
+  double t0;         /* time of step 0                                          */
+  double waist;      /* beam waist in the source plane (m); <= 0: plane wave    */
+  double gate;       /* transverse gate length a of the deposit (m)             */
+} SbeCouple3Desc;
+typedef struct SbeCouple3 SbeCouple3;
+/* wire_xy: HOST array of 2 nw positions (m) inside the grid's x, y range.          */
+int sbe_couple3_create(SbeCtx* ctx, SbePstd3* p, const double* wire_xy, const SbeCouple3Desc* desc,
+                       void* stream, SbeCouple3** out);
+int sbe_couple3_destroy(SbeCouple3* cp);
+/* Device buffers: Ek (per wire 3 x c128 Nr), src (per wire 5 x c128 Nr), J
+ * (3 x c128 N), rho (c128 N).  NULL arguments are skipped.                        */
+int sbe_couple3_buffers(SbeCouple3* cp, double** Ek, double** src, double** J, double** rho);
+/* New run: step 0, previous grid polarisation, J and rho cleared.                   */
+int sbe_couple3_reset(SbeCouple3* cp, void* stream);
+/* E (3 x c128 N) onto every wire (fills Ek; precision selects the FFTG arithmetic).  */
+int sbe_couple3_sample(SbeCouple3* cp, const double* E, int precision, void* stream);
+/* The wire sources in src onto the grid: J (with the source at the current step) and rho. */
+int sbe_couple3_deposit(SbeCouple3* cp, double dt, void* stream);
+int sbe_couple3_step(SbeCouple3* cp, double* P, double* C, double* D, double* E, double* H,
+                     double dt, int precision, void* stream);
+int sbe_couple3_graph_create(SbeCouple3* cp, double* P, double* C, double* D, double* E,
+                             double* H, double dt, int precision, SbeGraph** out,
+                             long long* n_kernels);
 
 /* ---- kernel timing (no counterpart in the reference) ------------------------ */
 /* enable != 0: record CUDA events around the engine launches of category

@@ -289,3 +289,111 @@ class Pstd3D:
         e = EPS0 * self.epsr * np.sum(np.abs(E) ** 2)
         h = MU0 * np.sum(np.real(H_prev * np.conj(H_next)))
         return e + h
+
+
+class CoupledGrid3:
+    """Wires along the z axis of a 3-D grid (one oracle ``Wire`` per wire, its 1-based
+    index and (x, y) position), centred at z = 0: the wire's (x, y, z) components are
+    the grid's (z, x, y).  Field -> wire: bilinear in x, y on every grid z, the spline
+    along z evaluated at the wire's r (Prop2QW, qwoptics.py:667-715); wire -> grid:
+    each source's spline evaluated at the grid z, gated by exp(-d^2 / (2 a^2)) in x and
+    y (the SHO gates of rhoPJ.py:383-389 with QWPlacement, :655-702) around the wire;
+    J = (P^{n+1} - P^n)/dt plus a current sheet in the plane x = x[src_index] along
+    component pol with the profile exp(-(y^2 + z^2)/waist^2)."""
+
+    def __init__(self, pstd, wires, windex, wxy, gate, src_index=-1, pol=1, E0=0.0, tau=1.0,
+                 w0=0.0, tpeak=0.0, t0=0.0, waist=0.0):
+        self.p = pstd
+        self.wires, self.windex = wires, list(windex)
+        self.wxy = np.asarray(wxy, float).reshape(-1, 2)
+        self.gate = gate
+        self.src_index, self.pol, self.E0, self.tau, self.w0 = src_index, pol, E0, tau, w0
+        self.tpeak, self.t0, self.waist = tpeak, t0, waist
+        self.eta = np.sqrt(MU0 / (EPS0 * pstd.epsr))
+        self.Pold = np.zeros((3,) + pstd.n, complex)
+        self.n = 0
+
+    def _cell(self, g, v):
+        i = int(np.searchsorted(g, v, side="right") - 1)
+        i = min(max(i, 0), len(g) - 2)
+        return i, (v - g[i]) / (g[i + 1] - g[i])
+
+    def lines(self, E):
+        """Grid fields on the line of every wire: [w][f][k], f the wire's component."""
+        xg, yg = self.p.x[0], self.p.x[1]
+        out = []
+        for xw, yw in self.wxy:
+            i0, fx = self._cell(xg, xw)
+            j0, fy = self._cell(yg, yw)
+            w00, w10 = (1 - fx) * (1 - fy), fx * (1 - fy)
+            w01, w11 = (1 - fx) * fy, fx * fy
+            fl = []
+            for src in (2, 0, 1):
+                F = E[src]
+                fl.append(w00 * F[i0, j0] + w10 * F[i0 + 1, j0] + w01 * F[i0, j0 + 1] +
+                          w11 * F[i0 + 1, j0 + 1])
+            out.append(fl)
+        return out
+
+    def sample(self, E):
+        zg = self.p.x[2]
+        out = []
+        for wi, fl in zip(self.wires, self.lines(E)):
+            ek = []
+            for f in fl:
+                b, c, d = O.spline_coeffs(zg, f)
+                v = rescale_vec(zg, b, c, d, f, wi.g["r"]) * wi.window
+                ek.append(O.fftg(np.real(v).astype(complex)))
+            out.append(ek)
+        return out
+
+    def deposit(self, srcs):
+        """srcs: per wire real-space (Px, Py, Pz, re, rh).  Returns (Pg (3, ...), rho)."""
+        xg, yg, zg = self.p.x
+        Pg = np.zeros((3,) + self.p.n, complex)
+        rho = np.zeros(self.p.n, complex)
+        a2 = 2.0 * self.gate ** 2
+        for wi, (xw, yw), s in zip(self.wires, self.wxy, srcs):
+            r = wi.g["r"]
+            vals = []
+            for comp in s:
+                b, c, d = O.spline_coeffs(r, comp)
+                vals.append(rescale_vec(r, b, c, d, comp, zg))
+            dl = [vals[1], vals[2], vals[0], vals[4] - vals[3]]
+            g = np.exp(-(xg - xw) ** 2 / a2)[:, None] * np.exp(-(yg - yw) ** 2 / a2)[None, :]
+            for c in range(3):
+                Pg[c] += g[:, :, None] * dl[c][None, None, :]
+            rho += g[:, :, None] * dl[3][None, None, :]
+        return Pg, rho
+
+    def current(self, Pg, dt):
+        J = (Pg - self.Pold) / dt
+        if self.src_index >= 0:
+            th = self.t0 + (self.n + 0.5) * dt
+            a = (th - self.tpeak) / self.tau
+            einc = np.exp(-a * a) * np.cos(self.w0 * (th - self.tpeak))
+            jamp = -2.0 * self.E0 / (self.eta * self.p.d[0])
+            yg, zg = self.p.x[1], self.p.x[2]
+            prof = np.ones((len(yg), len(zg)))
+            if self.waist > 0:
+                prof = np.exp(-(yg[:, None] ** 2 + zg[None, :] ** 2) / self.waist ** 2)
+            J[self.pol, self.src_index] += jamp * einc * prof
+        self.Pold = Pg.copy()
+        return J
+
+    def step(self, states, E, H, dt):
+        """states: per wire [P, C, D] (updated in place).  Returns (E, H, srcs)."""
+        eks = self.sample(E)
+        H = self.p.update_h(E, H, dt)
+        srcs = []
+        z = [np.zeros_like(eks[0][0])] * 3
+        for i, (wi, st) in enumerate(zip(self.wires, states)):
+            P, C, D, Px, Py, Pz, re, rh = wi.rk4_step(st[0], st[1], st[2], eks[i], z, dt,
+                                                     self.windex[i])
+            st[0], st[1], st[2] = P, C, D
+            srcs.append([O.ifftg(a) for a in (Px, Py, Pz, re, rh)])
+        Pg, rho = self.deposit(srcs)
+        J = self.current(Pg, dt)
+        E = self.p.update_e(E, H, J, dt)
+        self.n += 1
+        return E, H, srcs

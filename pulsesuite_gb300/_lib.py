@@ -39,7 +39,11 @@ EXPORTS = (
     "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
     "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info", "sbe_calc_jfx",
     "sbe_qw_placement", "sbe_e_at_xyz", "sbe_autotune", "sbe_ctx_tiles",
-    "sbe_local_field",
+    "sbe_local_field", "sbe_pstd3_create", "sbe_pstd3_destroy", "sbe_pstd3_grid",
+    "sbe_pstd3_curl", "sbe_pstd3_update_h", "sbe_pstd3_update_e", "sbe_pstd3_step",
+    "sbe_pstd3_elong", "sbe_couple3_create", "sbe_couple3_destroy", "sbe_couple3_buffers",
+    "sbe_couple3_reset", "sbe_couple3_sample", "sbe_couple3_deposit", "sbe_couple3_step",
+    "sbe_couple3_graph_create",
 )
 
 
@@ -56,6 +60,19 @@ class SbePstdDesc(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("n_abc", ctypes.c_int), ("pad0", ctypes.c_int),
                 ("pad1", ctypes.c_int), ("dx", ctypes.c_double), ("epsr", ctypes.c_double),
                 ("abc_strength", ctypes.c_double)]
+
+
+class SbePstd3Desc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int * 3), ("n_abc", ctypes.c_int * 3), ("fp32_work", ctypes.c_int),
+                ("pad0", ctypes.c_int), ("d", ctypes.c_double * 3), ("epsr", ctypes.c_double),
+                ("abc_strength", ctypes.c_double)]
+
+
+class SbeCouple3Desc(ctypes.Structure):
+    _fields_ = [("src_index", ctypes.c_int), ("pol", ctypes.c_int), ("pad0", ctypes.c_int),
+                ("pad1", ctypes.c_int), ("E0", ctypes.c_double), ("tau", ctypes.c_double),
+                ("w0", ctypes.c_double), ("tpeak", ctypes.c_double), ("t0", ctypes.c_double),
+                ("waist", ctypes.c_double), ("gate", ctypes.c_double)]
 
 
 class SbeCoupleDesc(ctypes.Structure):
@@ -142,6 +159,22 @@ def load(path=LIB_PATH):
         "sbe_couple_graph_create": [P, P, P, P, P, P, P, Dbl, I, P, P],
         "sbe_autotune": [P, ctypes.c_char_p],
         "sbe_local_field": [P, P, P, I, P, P, P],
+        "sbe_pstd3_create": [P, P, P],
+        "sbe_pstd3_destroy": [P],
+        "sbe_pstd3_grid": [P, I, P, P, P],
+        "sbe_pstd3_curl": [P, P, P, P],
+        "sbe_pstd3_update_h": [P, P, P, Dbl, P],
+        "sbe_pstd3_update_e": [P, P, P, P, Dbl, P],
+        "sbe_pstd3_step": [P, P, P, P, Dbl, P],
+        "sbe_pstd3_elong": [P, P, P, P, P, P, P, P, P],
+        "sbe_couple3_create": [P, P, P, P, P, P],
+        "sbe_couple3_destroy": [P],
+        "sbe_couple3_buffers": [P, P, P, P, P],
+        "sbe_couple3_reset": [P, P],
+        "sbe_couple3_sample": [P, P, I, P],
+        "sbe_couple3_deposit": [P, Dbl, P],
+        "sbe_couple3_step": [P, P, P, P, P, P, Dbl, I, P],
+        "sbe_couple3_graph_create": [P, P, P, P, P, P, Dbl, I, P, P],
         "sbe_ctx_tiles": [P, P, I, P],
     }
     for name, args in sig.items():

@@ -21,6 +21,7 @@
 
 #include "fp_bits.cuh"
 #include "pstd.cuh"
+#include "pstd3d.cuh"
 
 namespace {
 constexpr int kSeg = 16;
@@ -452,6 +453,152 @@ SplBatch wire_batch(SbeCouple* cp) {
   return b;
 }
 
+// ---- wires along z on the 3-D grid --------------------------------------------
+// Wire w lies along the grid's z axis at (x_w, y_w), centred at z = 0; its own axis
+// is the reference wire's x, so the wire's field components (x, y, z) are the grid's
+// (Ez, Ex, Ey) and its sources (Px, Py, Pz) go to the grid's (Pz, Px, Py).
+
+// The three grid fields on the line of each wire (bilinear in x, y at every grid z):
+// lines[w][f][k], f the wire's component.
+__global__ void k_c3_lines(int nx, int ny, int nz, const double* xg, const double* yg,
+                           const double* wxy, const double2* E, double2* lines) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, w = blockIdx.y;
+  if (k >= nz) return;
+  const double xw = wxy[2 * w], yw = wxy[2 * w + 1];
+  const int i0 = min(max(locate_sorted(xg, nx, xw), 0), nx - 2);
+  const int j0 = min(max(locate_sorted(yg, ny, yw), 0), ny - 2);
+  const double fx = (xw - xg[i0]) / (xg[i0 + 1] - xg[i0]);
+  const double fy = (yw - yg[j0]) / (yg[j0 + 1] - yg[j0]);
+  const long long N = (long long)nx * ny * nz;
+  const int src[3] = {2, 0, 1};   // wire x, y, z <- grid Ez, Ex, Ey
+  for (int f = 0; f < 3; ++f) {
+    const double2* F = E + src[f] * N;
+    auto at = [&](int i, int j) { return F[((long long)i * ny + j) * nz + k]; };
+    const double2 a = at(i0, j0), b = at(i0 + 1, j0), c = at(i0, j0 + 1), d = at(i0 + 1, j0 + 1);
+    const double w00 = (1 - fx) * (1 - fy), w10 = fx * (1 - fy), w01 = (1 - fx) * fy, w11 = fx * fy;
+    lines[((long long)w * 3 + f) * nz + k] =
+        make_double2(w00 * a.x + w10 * b.x + w01 * c.x + w11 * d.x,
+                     w00 * a.y + w10 * b.y + w01 * c.y + w11 * d.y);
+  }
+}
+
+// Line splines -> wire grids: spline at z = r_j, window, real part.
+__global__ void k_c3_eval(const WireDev* wires, int nz, const double* zg, const double2* lines,
+                          const double2* lcoef, const double* r, const double* window, double2* wv,
+                          float* wvf) {
+  const int w = blockIdx.y;
+  const WireDev W = wires[w];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= W.nr) return;
+  const double u = r[W.off_r + j];
+  const double win = window[W.off_r + j];
+  double v[3] = {0.0, 0.0, 0.0};
+  if (u >= zg[0] && u <= zg[nz - 1]) {
+    const int i = locate_sorted(zg, nz, u);
+    const double dz = u - zg[i];
+    for (int f = 0; f < 3; ++f) {
+      const long long pb = (long long)w * 3 + f;
+      v[f] = spl_eval(lines + pb * nz, lcoef + 3 * pb * nz, nz, i, dz).x;
+    }
+  }
+  for (int f = 0; f < 3; ++f) {
+    const double a = v[f] * win;
+    wv[3 * W.off_r + (long long)f * W.nr + j] = make_double2(a, 0.0);
+    wvf[3 * W.off_r + (long long)f * W.nr + j] = f64_to_f32(a);
+  }
+}
+
+// Wire sources on the grid z of their line: dl[w][c][k] for the grid components
+// c = 0, 1, 2 (Px, Py, Pz of the grid) and 3 (rho = rh - re).
+__global__ void k_c3_wire_lines(const WireDev* wires, int nz, const double* zg, const double* r,
+                                const double2* src, const double2* wcoef, double2* dl) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, w = blockIdx.y;
+  if (k >= nz) return;
+  const WireDev W = wires[w];
+  const double* rw = r + W.off_r;
+  const double u = zg[k];
+  double2 v[5];
+  for (int c = 0; c < 5; ++c) v[c] = make_double2(0.0, 0.0);
+  if (u >= rw[0] && u <= rw[W.nr - 1]) {
+    const int i = locate_sorted(rw, W.nr, u);
+    const double dx = u - rw[i];
+    const double2* y = src + 5 * W.off_r;
+    const double2* cf = wcoef + 15 * W.off_r;
+    for (int c = 0; c < 5; ++c)
+      v[c] = spl_eval(y + (long long)c * W.nr, cf + 3LL * c * W.nr, W.nr, i, dx);
+  }
+  double2* o = dl + (long long)w * 4 * nz;
+  o[k] = v[1];            // grid Px <- wire Py
+  o[nz + k] = v[2];       // grid Py <- wire Pz
+  o[2 * nz + k] = v[0];   // grid Pz <- wire Px (along the wire)
+  o[3 * nz + k] = csub(v[4], v[3]);
+}
+
+// Grid polarisation of the wires' gated lines, the current J = (P^{n+1} - P^n)/dt
+// (P^n <- P^{n+1}), rho, and the soft source: a current sheet in the plane
+// x = x[src_index] along component pol with the profile exp(-(y^2 + z^2)/waist^2).
+// One block per (x, y) column, threads along z; the column's wires and gate weights
+// come from a list built at creation.
+struct C3Dep {
+  int nx, ny, nz;
+  const int* col_start;   // nx ny + 1
+  const int* col_wire;
+  const double* col_gate;
+  const double2* dl;      // [w][4][nz]
+  double2* Pold;          // 3 N
+  double2* J;             // 3 N
+  double2* rho;           // N
+  double dt;
+  // source
+  const long long* step;
+  double t0, jamp, tau, w0, tpeak, waist;
+  int src_index, pol;
+  const double* yg;
+  const double* zg;
+};
+
+__global__ void k_c3_deposit(C3Dep a) {
+  const int col = blockIdx.x;
+  const int i = col / a.ny, j = col % a.ny;
+  const long long N = (long long)a.nx * a.ny * a.nz;
+  const int b = a.col_start[col], e = a.col_start[col + 1];
+  double src_amp = 0.0;
+  if (i == a.src_index) {
+    const double th = a.t0 + ((double)(*a.step) + 0.5) * a.dt;
+    const double u = (th - a.tpeak) / a.tau;
+    src_amp = a.jamp * exp(-u * u) * cos(a.w0 * (th - a.tpeak));
+  }
+  for (int k = threadIdx.x; k < a.nz; k += blockDim.x) {
+    double2 P[4] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0),
+                    make_double2(0, 0)};
+    for (int q = b; q < e; ++q) {
+      const double g = a.col_gate[q];
+      const double2* l = a.dl + (long long)a.col_wire[q] * 4 * a.nz;
+      for (int c = 0; c < 4; ++c) {
+        const double2 v = l[(long long)c * a.nz + k];
+        P[c].x += g * v.x;
+        P[c].y += g * v.y;
+      }
+    }
+    const long long g0 = (long long)col * a.nz + k;
+    for (int c = 0; c < 3; ++c) {
+      const double2 po = a.Pold[c * N + g0];
+      double2 jj = make_double2((P[c].x - po.x) / a.dt, (P[c].y - po.y) / a.dt);
+      if (c == a.pol && src_amp != 0.0) {
+        double prof = 1.0;
+        if (a.waist > 0.0) {
+          const double y = a.yg[j], z = a.zg[k];
+          prof = exp(-(y * y + z * z) / (a.waist * a.waist));
+        }
+        jj.x += src_amp * prof;
+      }
+      a.J[c * N + g0] = jj;
+      a.Pold[c * N + g0] = P[c];
+    }
+    a.rho[g0] = P[3];
+  }
+}
+
 }  // namespace
 
 int couple_sample(SbeCouple* cp, const double2* Ex, const double2* E, int precision,
@@ -693,6 +840,331 @@ int sbe_couple_graph_create(SbeCouple* cp, double* P, double* C, double* D, doub
   return capture_graph(
       cp->ctx, precision,
       [&](cudaStream_t cs) { return sbe_couple_step(cp, P, C, D, E, H, Ex, dt, precision, (void*)cs); },
+      out, n_kernels);
+}
+
+}  // extern "C"
+
+// ---- wires along z on the 3-D grid ---------------------------------------------
+struct SbeCouple3 {
+  SbeCtx* ctx = nullptr;
+  SbePstd3* p = nullptr;
+  int nw = 0;
+  SbeCouple3Desc desc{};
+  double eta = 0.0;
+  void* arena = nullptr;
+  double* wxy = nullptr;        // 2 nw wire positions (x, y)
+  int *col_start = nullptr, *col_wire = nullptr;
+  double* col_gate = nullptr;
+  int *probn = nullptr, *wfn = nullptr;
+  long long *probl = nullptr, *wfl = nullptr;
+  double *z_b = nullptr, *z_t = nullptr;   // spline factors of the grid z knots
+  double *w_b = nullptr, *w_t = nullptr;   // of the wire knots
+  double2 *lines = nullptr, *l_c1 = nullptr, *l_c2 = nullptr, *l_coef = nullptr;   // 3 nw nz
+  double2 *w_c1 = nullptr, *w_c2 = nullptr, *w_coef = nullptr;
+  double2* twr = nullptr;
+  float2* twrf = nullptr;
+  double2* wv = nullptr;
+  float* wvf = nullptr;
+  double2 *Ek = nullptr, *dEk = nullptr, *src = nullptr;
+  double2* dl = nullptr;        // 4 nw nz: wire sources on their lines
+  double2 *Pold = nullptr, *J = nullptr, *rho = nullptr;   // 3 N, 3 N, N
+  long long* step = nullptr;
+};
+
+namespace {
+
+SplBatch line_batch(SbeCouple3* cp) {
+  SplBatch b{};
+  b.X = cp->p->x[2];
+  b.B = cp->z_b;
+  b.T = cp->z_t;
+  b.Y = cp->lines;
+  b.C1 = cp->l_c1;
+  b.C2 = cp->l_c2;
+  b.coef = cp->l_coef;
+  b.n0 = cp->p->n[2];
+  return b;
+}
+
+SplBatch wire_batch3(SbeCouple3* cp) {
+  SplBatch b{};
+  b.X = cp->ctx->r;
+  b.B = cp->w_b;
+  b.T = cp->w_t;
+  b.Y = cp->src;
+  b.C1 = cp->w_c1;
+  b.C2 = cp->w_c2;
+  b.coef = cp->w_coef;
+  b.n = cp->probn;
+  b.off = cp->probl;
+  return b;
+}
+
+int check_cp3(SbeCouple3* cp, const char* who) {
+  if (!cp || !cp->ctx || !cp->p) return fail(SBE_ERR_ARG, std::string(who) + ": null coupling");
+  return SBE_OK;
+}
+
+int c3_sample(SbeCouple3* cp, const double2* E, int precision, cudaStream_t s) {
+  SbeCtx* c = cp->ctx;
+  SbePstd3* p = cp->p;
+  const int nz = p->n[2];
+  k_c3_lines<<<dim3((nz + 127) / 128, c->nw), 128, 0, s>>>(p->n[0], p->n[1], nz, p->x[0],
+                                                           p->x[1], cp->wxy, E, cp->lines);
+  run_splines(line_batch(cp), 3 * c->nw, nz, s);
+  k_c3_eval<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(
+      c->d_wires, nz, p->x[2], cp->lines, cp->l_coef, c->r, c->window, cp->wv, cp->wvf);
+  if (precision == SBE_PREC_MIXED)
+    k_couple_fftg_f<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
+                                                                     cp->wvf, cp->Ek);
+  else
+    k_couple_fftg<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twr, cp->wv,
+                                                                   cp->Ek);
+  return cuda_check(cudaGetLastError(), "couple3 sample");
+}
+
+int c3_deposit(SbeCouple3* cp, double dt, cudaStream_t s) {
+  SbeCtx* c = cp->ctx;
+  SbePstd3* p = cp->p;
+  const int nz = p->n[2];
+  run_splines(wire_batch3(cp), 5 * c->nw, c->nr_max, s);
+  k_c3_wire_lines<<<dim3((nz + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, nz, p->x[2], c->r,
+                                                                cp->src, cp->w_coef, cp->dl);
+  C3Dep a{};
+  a.nx = p->n[0];
+  a.ny = p->n[1];
+  a.nz = nz;
+  a.col_start = cp->col_start;
+  a.col_wire = cp->col_wire;
+  a.col_gate = cp->col_gate;
+  a.dl = cp->dl;
+  a.Pold = cp->Pold;
+  a.J = cp->J;
+  a.rho = cp->rho;
+  a.dt = dt;
+  const SbeCouple3Desc& d = cp->desc;
+  a.step = cp->step;
+  a.t0 = d.t0;
+  a.jamp = d.src_index >= 0 ? -2.0 * d.E0 / (cp->eta * p->d[0]) : 0.0;
+  a.tau = d.tau;
+  a.w0 = d.w0;
+  a.tpeak = d.tpeak;
+  a.waist = d.waist;
+  a.src_index = d.src_index;
+  a.pol = d.pol;
+  a.yg = p->x[1];
+  a.zg = p->x[2];
+  k_c3_deposit<<<p->n[0] * p->n[1], 128, 0, s>>>(a);
+  return cuda_check(cudaGetLastError(), "couple3 deposit");
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbe_couple3_create(SbeCtx* c, SbePstd3* p, const double* wire_xy, const SbeCouple3Desc* d,
+                       void* stream, SbeCouple3** out) {
+  if (!c || !p || !wire_xy || !d || !out) return fail(SBE_ERR_ARG, "sbe_couple3_create: null");
+  *out = nullptr;
+  if (d->src_index >= p->n[0] || d->pol < 0 || d->pol > 2)
+    return fail(SBE_ERR_ARG, "sbe_couple3_create: source plane or polarisation");
+  if (d->src_index >= 0 && !(d->tau > 0.0)) return fail(SBE_ERR_ARG, "sbe_couple3_create: tau");
+  if (!(d->gate > 0.0)) return fail(SBE_ERR_ARG, "sbe_couple3_create: gate length");
+  const int nx = p->n[0], ny = p->n[1], nz = p->n[2];
+  std::vector<double> xg(nx), yg(ny);
+  cudaStream_t s = as_stream(stream);
+  // the wires' gated columns: gate exp(-(x - x_w)^2 / (2 a^2)) exp(-(y - y_w)^2 / (2 a^2))
+  // (the reference's SHO gates, rhoPJ.py:383-389), every column where it is nonzero
+  int rc = cuda_check(cudaMemcpy(xg.data(), p->x[0], sizeof(double) * nx, cudaMemcpyDeviceToHost),
+                      "sbe_couple3_create: grid");
+  if (!rc) rc = cuda_check(cudaMemcpy(yg.data(), p->x[1], sizeof(double) * ny,
+                                      cudaMemcpyDeviceToHost), "sbe_couple3_create: grid");
+  if (rc) return rc;
+  for (int w = 0; w < c->nw; ++w)
+    if (!(wire_xy[2 * w] >= xg[0] && wire_xy[2 * w] <= xg[nx - 1] &&
+          wire_xy[2 * w + 1] >= yg[0] && wire_xy[2 * w + 1] <= yg[ny - 1]))
+      return fail(SBE_ERR_ARG, "sbe_couple3_create: wire outside the grid");
+  const double a2 = 2.0 * d->gate * d->gate;
+  std::vector<int> cstart(nx * ny + 1, 0), cwire;
+  std::vector<double> cgate;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      cstart[i * ny + j] = (int)cwire.size();
+      for (int w = 0; w < c->nw; ++w) {
+        const double dx = xg[i] - wire_xy[2 * w], dy = yg[j] - wire_xy[2 * w + 1];
+        const double g = std::exp(-dx * dx / a2) * std::exp(-dy * dy / a2);
+        if (g > 0.0) {
+          cwire.push_back(w);
+          cgate.push_back(g);
+        }
+      }
+    }
+  cstart[nx * ny] = (int)cwire.size();
+  SbeCouple3* cp = new SbeCouple3();
+  cp->ctx = c;
+  cp->p = p;
+  cp->nw = c->nw;
+  cp->desc = *d;
+  cp->eta = std::sqrt(kMu0c / (kEps0 * p->epsr));
+  const long long R = c->tot_r, N = p->N, L = 3LL * c->nw * nz;
+  const int np = 5 * c->nw;
+  std::vector<std::pair<void**, size_t>> parts = {
+      {(void**)&cp->wxy, sizeof(double) * 2 * c->nw},
+      {(void**)&cp->col_start, sizeof(int) * cstart.size()},
+      {(void**)&cp->col_wire, sizeof(int) * std::max<size_t>(cwire.size(), 1)},
+      {(void**)&cp->col_gate, sizeof(double) * std::max<size_t>(cgate.size(), 1)},
+      {(void**)&cp->probn, sizeof(int) * np},
+      {(void**)&cp->probl, sizeof(long long) * 2 * np},
+      {(void**)&cp->wfn, sizeof(int) * c->nw},
+      {(void**)&cp->wfl, sizeof(long long) * 2 * c->nw},
+      {(void**)&cp->z_b, sizeof(double) * nz},
+      {(void**)&cp->z_t, sizeof(double) * nz},
+      {(void**)&cp->w_b, sizeof(double) * R},
+      {(void**)&cp->w_t, sizeof(double) * R},
+      {(void**)&cp->lines, sizeof(double2) * L},
+      {(void**)&cp->l_c1, sizeof(double2) * L},
+      {(void**)&cp->l_c2, sizeof(double2) * L},
+      {(void**)&cp->l_coef, sizeof(double2) * 3 * L},
+      {(void**)&cp->w_c1, sizeof(double2) * 5 * R},
+      {(void**)&cp->w_c2, sizeof(double2) * 5 * R},
+      {(void**)&cp->w_coef, sizeof(double2) * 15 * R},
+      {(void**)&cp->twr, sizeof(double2) * R},
+      {(void**)&cp->twrf, sizeof(float2) * R},
+      {(void**)&cp->wv, sizeof(double2) * 3 * R},
+      {(void**)&cp->wvf, sizeof(float) * 3 * R},
+      {(void**)&cp->Ek, sizeof(double2) * 3 * R},
+      {(void**)&cp->dEk, sizeof(double2) * 3 * R},
+      {(void**)&cp->src, sizeof(double2) * 5 * R},
+      {(void**)&cp->dl, sizeof(double2) * 4 * (size_t)c->nw * nz},
+      {(void**)&cp->Pold, sizeof(double2) * 3 * N},
+      {(void**)&cp->J, sizeof(double2) * 3 * N},
+      {(void**)&cp->rho, sizeof(double2) * N},
+      {(void**)&cp->step, sizeof(long long)},
+  };
+  size_t total = 0;
+  for (auto& pr : parts) total += (pr.second + 255) / 256 * 256;
+  if (cudaMalloc(&cp->arena, total) != cudaSuccess) {
+    delete cp;
+    return fail(SBE_ERR_OOM, "sbe_couple3_create: device allocation");
+  }
+  size_t o = 0;
+  for (auto& pr : parts) {
+    *pr.first = static_cast<char*>(cp->arena) + o;
+    o += (pr.second + 255) / 256 * 256;
+  }
+  cudaMemsetAsync(cp->arena, 0, total, s);
+  std::vector<int> pn(np);
+  std::vector<long long> pl(2 * np), wl(2 * c->nw);
+  std::vector<int> wn(c->nw);
+  for (int w = 0; w < c->nw; ++w) {
+    const WireDev& W = c->wires[w];
+    wl[2 * w] = W.off_r;
+    wl[2 * w + 1] = 0;
+    wn[w] = W.nr;
+    for (int k = 0; k < 5; ++k) {
+      pn[5 * w + k] = W.nr;
+      pl[2 * (5 * w + k)] = W.off_r;
+      pl[2 * (5 * w + k) + 1] = 5 * W.off_r + (long long)k * W.nr;
+    }
+  }
+  cudaMemcpyAsync(cp->wxy, wire_xy, sizeof(double) * 2 * c->nw, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(cp->col_start, cstart.data(), sizeof(int) * cstart.size(),
+                  cudaMemcpyHostToDevice, s);
+  if (!cwire.empty()) {
+    cudaMemcpyAsync(cp->col_wire, cwire.data(), sizeof(int) * cwire.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(cp->col_gate, cgate.data(), sizeof(double) * cgate.size(),
+                    cudaMemcpyHostToDevice, s);
+  }
+  cudaMemcpyAsync(cp->probn, pn.data(), sizeof(int) * pn.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(cp->probl, pl.data(), sizeof(long long) * pl.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(cp->wfn, wn.data(), sizeof(int) * wn.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(cp->wfl, wl.data(), sizeof(long long) * wl.size(), cudaMemcpyHostToDevice, s);
+  k_spl_factors<<<1, 32, 0, s>>>(1, p->x[2], nullptr, nullptr, nz, cp->z_b, cp->z_t);
+  k_spl_factors<<<(c->nw + 31) / 32, 32, 0, s>>>(c->nw, c->r, cp->wfn, cp->wfl, 0, cp->w_b,
+                                                 cp->w_t);
+  k_twr<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(c->d_wires, cp->twr, cp->twrf);
+  rc = cuda_check(cudaGetLastError(), "sbe_couple3_create");
+  if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "sbe_couple3_create: tables");
+  if (rc) {
+    cudaFree(cp->arena);
+    delete cp;
+    return rc;
+  }
+  *out = cp;
+  return SBE_OK;
+}
+
+int sbe_couple3_destroy(SbeCouple3* cp) {
+  if (!cp) return SBE_OK;
+  cudaFree(cp->arena);
+  delete cp;
+  return SBE_OK;
+}
+
+int sbe_couple3_buffers(SbeCouple3* cp, double** Ek, double** src, double** J, double** rho) {
+  int rc = check_cp3(cp, "sbe_couple3_buffers");
+  if (rc) return rc;
+  if (Ek) *Ek = reinterpret_cast<double*>(cp->Ek);
+  if (src) *src = reinterpret_cast<double*>(cp->src);
+  if (J) *J = reinterpret_cast<double*>(cp->J);
+  if (rho) *rho = reinterpret_cast<double*>(cp->rho);
+  return SBE_OK;
+}
+
+int sbe_couple3_reset(SbeCouple3* cp, void* stream) {
+  int rc = check_cp3(cp, "sbe_couple3_reset");
+  if (rc) return rc;
+  cudaStream_t s = as_stream(stream);
+  const size_t N = cp->p->N;
+  cudaMemsetAsync(cp->Pold, 0, sizeof(double2) * 3 * N, s);
+  cudaMemsetAsync(cp->J, 0, sizeof(double2) * 3 * N, s);
+  cudaMemsetAsync(cp->rho, 0, sizeof(double2) * N, s);
+  cudaMemsetAsync(cp->step, 0, sizeof(long long), s);
+  return cuda_check(cudaGetLastError(), "sbe_couple3_reset");
+}
+
+int sbe_couple3_sample(SbeCouple3* cp, const double* E, int precision, void* stream) {
+  int rc = check_cp3(cp, "sbe_couple3_sample");
+  if (rc) return rc;
+  if (!E) return fail(SBE_ERR_ARG, "sbe_couple3_sample: null field");
+  return c3_sample(cp, reinterpret_cast<const double2*>(E), precision, as_stream(stream));
+}
+
+int sbe_couple3_deposit(SbeCouple3* cp, double dt, void* stream) {
+  int rc = check_cp3(cp, "sbe_couple3_deposit");
+  if (rc) return rc;
+  return c3_deposit(cp, dt, as_stream(stream));
+}
+
+int sbe_couple3_step(SbeCouple3* cp, double* P, double* C, double* D, double* E, double* H,
+                     double dt, int precision, void* stream) {
+  int rc = check_cp3(cp, "sbe_couple3_step");
+  if (rc) return rc;
+  if (!P || !C || !D || !E || !H) return fail(SBE_ERR_ARG, "sbe_couple3_step: null");
+  cudaStream_t s = as_stream(stream);
+  if ((rc = c3_sample(cp, reinterpret_cast<const double2*>(E), precision, s))) return rc;
+  if ((rc = sbe_pstd3_update_h(cp->p, E, H, dt, stream))) return rc;
+  if ((rc = sbe_rk4_step(cp->ctx, P, C, D, reinterpret_cast<double*>(cp->Ek),
+                         reinterpret_cast<double*>(cp->dEk), dt, precision,
+                         reinterpret_cast<double*>(cp->src), stream)))
+    return rc;
+  if ((rc = c3_deposit(cp, dt, s))) return rc;
+  if ((rc = sbe_pstd3_update_e(cp->p, E, H, reinterpret_cast<double*>(cp->J), dt, stream)))
+    return rc;
+  k_tick<<<1, 1, 0, s>>>(cp->step);
+  return cuda_check(cudaGetLastError(), "sbe_couple3_step");
+}
+
+int sbe_couple3_graph_create(SbeCouple3* cp, double* P, double* C, double* D, double* E,
+                             double* H, double dt, int precision, SbeGraph** out,
+                             long long* n_kernels) {
+  int rc = check_cp3(cp, "sbe_couple3_graph_create");
+  if (rc) return rc;
+  if (!out) return fail(SBE_ERR_ARG, "sbe_couple3_graph_create: null");
+  return capture_graph(
+      cp->ctx, precision,
+      [&](cudaStream_t cs) { return sbe_couple3_step(cp, P, C, D, E, H, dt, precision, (void*)cs); },
       out, n_kernels);
 }
 

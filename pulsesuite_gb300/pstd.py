@@ -86,6 +86,84 @@ class Pstd1D:
         return out
 
 
+class Pstd3D:
+    """3-D grid of n = (nx, ny, nz) points (powers of two in [8, 1024]), cells
+    d = (dx, dy, dz), background epsr, absorbing layers of n_abc cells per axis; fields
+    are caller-owned complex128 tensors of shape (3, nx, ny, nz): E = (Ex, Ey, Ez),
+    H = (Hx, Hy, Hz).  ``fp32_work``: transforms between the first and last pass in
+    FP32 (the fields stay FP64)."""
+
+    def __init__(self, n, d, epsr, n_abc=(0, 0, 0), abc_strength=0.0, fp32_work=False,
+                 device=None):
+        if not torch.cuda.is_available():
+            raise _lib.SbeError("a CUDA device is required (no CPU fallback)")
+        self.lib = _lib.load()
+        self.n = tuple(int(v) for v in n)
+        self.d = tuple(float(v) for v in d)
+        self.epsr = float(epsr)
+        self.device = torch.device(device or "cuda")
+        desc = _lib.SbePstd3Desc((ctypes.c_int * 3)(*self.n),
+                                 (ctypes.c_int * 3)(*[int(v) for v in n_abc]),
+                                 int(bool(fp32_work)), 0, (ctypes.c_double * 3)(*self.d),
+                                 self.epsr, float(abc_strength))
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.sbe_pstd3_create(ctypes.byref(desc), _lib.stream_handle(),
+                                                 ctypes.byref(h)), "sbe_pstd3_create")
+        self.handle = h
+        self.x, self.q = [], []
+        for a in range(3):
+            x = torch.empty(self.n[a], dtype=torch.float64, device=self.device)
+            q = torch.empty_like(x)
+            _lib.check(self.lib.sbe_pstd3_grid(h, a, _lib.ptr(x), _lib.ptr(q),
+                                               _lib.stream_handle()), "sbe_pstd3_grid")
+            self.x.append(x)
+            self.q.append(q)
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.sbe_pstd3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def zeros(self):
+        return torch.zeros((3,) + self.n, dtype=CDTYPE, device=self.device)
+
+    def max_dt(self):
+        """Largest stable leapfrog step: v dt |q|max / 2 <= 1."""
+        qm = sum((3.141592653589793 / d) ** 2 for d in self.d) ** 0.5
+        return 2.0 * self.epsr ** 0.5 / (C0 * qm)
+
+    def curl(self, F):
+        out = torch.empty_like(F)
+        _lib.check(self.lib.sbe_pstd3_curl(self.handle, _lib.ptr(F.contiguous()), _lib.ptr(out),
+                                           _lib.stream_handle()), "sbe_pstd3_curl")
+        return out
+
+    def step(self, E, H, J, dt):
+        _lib.check(self.lib.sbe_pstd3_step(self.handle, _lib.ptr(E), _lib.ptr(H), _lib.ptr(J),
+                                           float(dt), _lib.stream_handle()), "sbe_pstd3_step")
+
+    def elong(self, rho, P, qx=None, qy=None, qz=None):
+        """ElongfromRho (rhoPJ.py:703-880): returns (out10 (10, nx, ny, nz), P_k (3, ...))
+        with out10 = [E_PRho x, y, z, E_P x, y, z, E_Rho x, y, z, RhoBound]; the
+        wavenumber tables default to the grid's FFT-order ones."""
+        q = [qq if qq is not None else self.q[a] for a, qq in enumerate((qx, qy, qz))]
+        q = [torch.as_tensor(v, dtype=torch.float64, device=self.device).contiguous() for v in q]
+        out = torch.empty((10,) + self.n, dtype=CDTYPE, device=self.device)
+        pk = torch.empty((3,) + self.n, dtype=CDTYPE, device=self.device)
+        _lib.check(self.lib.sbe_pstd3_elong(self.handle, _lib.ptr(rho.contiguous()),
+                                            _lib.ptr(P.contiguous()), *[_lib.ptr(v) for v in q],
+                                            _lib.ptr(out), _lib.ptr(pk), _lib.stream_handle()),
+                   "sbe_pstd3_elong")
+        return out, pk
+
+
 @dataclass
 class SheetSource:
     """Soft source: a current sheet at grid cell ``index`` launching
@@ -200,3 +278,78 @@ class CoupledLine:
                                                     ctypes.byref(h), ctypes.byref(n)),
                    "sbe_couple_graph_create")
         return _Graph(self.lib, h, n.value, (P, C, D, E, H, Ex))
+
+
+class CoupledGrid3:
+    """Wires of ``ctx`` along the z axis of the 3-D grid ``pstd`` at positions
+    ``wire_xy`` ((x, y) per wire, m), centred at z = 0 (sbe_couple3_*): the wire's
+    (x, y, z) components are the grid's (z, x, y).  ``gate``: the transverse SHO gate
+    length of the deposit (the reference's 5 nm); ``source``: a current sheet in the
+    plane x = x[index] (a :class:`SheetSource`) along component ``pol`` with a
+    Gaussian profile of waist ``waist`` (<= 0: uniform)."""
+
+    def __init__(self, ctx, pstd, wire_xy, source=None, pol=1, waist=0.0, gate=5e-9, t0=0.0):
+        self.ctx, self.pstd, self.lib = ctx, pstd, pstd.lib
+        xy = [float(v) for p in wire_xy for v in p]
+        wxy = (ctypes.c_double * len(xy))(*xy)
+        if source is None:
+            d = _lib.SbeCouple3Desc(-1, int(pol), 0, 0, 0.0, 1.0, 0.0, 0.0, float(t0),
+                                    float(waist), float(gate))
+        else:
+            d = _lib.SbeCouple3Desc(int(source.index), int(pol), 0, 0, float(source.E0),
+                                    float(source.tau), float(source.w0), float(source.tpeak),
+                                    float(t0), float(waist), float(gate))
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.sbe_couple3_create(ctx.handle, pstd.handle, wxy, ctypes.byref(d),
+                                               _lib.stream_handle(), ctypes.byref(h)),
+                   "sbe_couple3_create")
+        self.handle = h
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        _lib.check(self.lib.sbe_couple3_buffers(h, *[ctypes.byref(p) for p in ptrs]),
+                   "sbe_couple3_buffers")
+        self._ptr = dict(zip(("Ek", "src", "J", "rho"), [p.value for p in ptrs]))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.sbe_couple3_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def view(self, name):
+        """Zero-copy view of Ek (3 total_r), src (5 total_r), J (3, nx, ny, nz), rho."""
+        tr, n = self.ctx.total_r, self.pstd.n
+        shape = dict(Ek=(3 * tr,), src=(5 * tr,), J=(3,) + n, rho=n)[name]
+        raw = torch.as_tensor(_DeviceArray(self._ptr[name], shape + (2,)), device=self.pstd.device)
+        return torch.view_as_complex(raw)
+
+    def reset(self):
+        _lib.check(self.lib.sbe_couple3_reset(self.handle, _lib.stream_handle()),
+                   "sbe_couple3_reset")
+
+    def sample(self, E, precision=_lib.PREC_FP64):
+        _lib.check(self.lib.sbe_couple3_sample(self.handle, _lib.ptr(E), int(precision),
+                                               _lib.stream_handle()), "sbe_couple3_sample")
+
+    def deposit(self, dt):
+        _lib.check(self.lib.sbe_couple3_deposit(self.handle, float(dt), _lib.stream_handle()),
+                   "sbe_couple3_deposit")
+
+    def step(self, P, C, D, E, H, dt, precision=_lib.PREC_FP64):
+        _lib.check(self.lib.sbe_couple3_step(self.handle, _lib.ptr(P), _lib.ptr(C), _lib.ptr(D),
+                                             _lib.ptr(E), _lib.ptr(H), float(dt), int(precision),
+                                             _lib.stream_handle()), "sbe_couple3_step")
+
+    def graph(self, P, C, D, E, H, dt, precision=_lib.PREC_FP64):
+        h = ctypes.c_void_p()
+        n = ctypes.c_longlong()
+        _lib.check(self.lib.sbe_couple3_graph_create(self.handle, _lib.ptr(P), _lib.ptr(C),
+                                                     _lib.ptr(D), _lib.ptr(E), _lib.ptr(H),
+                                                     float(dt), int(precision), ctypes.byref(h),
+                                                     ctypes.byref(n)),
+                   "sbe_couple3_graph_create")
+        return _Graph(self.lib, h, n.value, (P, C, D, E, H))
