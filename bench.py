@@ -66,6 +66,16 @@ WORKLOADS = {
 # RK4 dt = 0.1 fs; each wire's pulse peaks at t = 2 tau from t = 0.
 SWEEP = dict(nw=512, nks=(64, 96, 128, 192, 256, 384, 512), kmax=3e9, dt=0.1e-15, seed=3)
 
+# Wires along z on a 3-D grid: 256 x 128 x 128 cells of 20 nm, 64 wires of Nk = 1024
+# at (x, y) drawn with numpy default_rng(4) in the central 60 % of the x-y
+# cross-section, a Gaussian beam (waist 1 um, polarised along y) E0 = 2e7 V/m, tau =
+# 80 fs, hbar w0 = Eg + 30 meV launched along x by a current sheet next to the left
+# absorbing layer and already in flight at step 0 (its peak at x = 0), RK4 and field
+# step dt = 0.02 fs, T = 77 K.
+GRID3 = dict(n=(256, 128, 128), d=20e-9, n_abc=(16, 8, 8), abc=0.05, nw=64, nk=1024, kmax=3e9,
+             E0=2e7, tau=80e-15, det=30e-3, dt=0.02e-15, waist=1e-6, temp=77.0, seed=4,
+             src_cell=24)
+
 MAT = dict(me=0.067 * ME0, mh=0.45 * ME0, gap=1.52 * E0C, HO=100e-3 * E0C, Delta0=6e-9,
            gam_e=1e12, gam_h=1e12, gam_eh=1e12, epsr=12.9, Oph=36e-3 * E0C / HBAR,
            Gph=3e-3 * E0C / HBAR)
@@ -720,6 +730,213 @@ def sweep_arm(args):
         dist.destroy_process_group()
 
 
+def grid3_config():
+    g = GRID3
+    return {"workload": f"{g['nw']} GaAs-like wires of Nk={g['nk']} along z at seeded (x, y) in the "
+                        f"central 60% of a {g['n'][0]}x{g['n'][1]}x{g['n'][2]} 3-D PSTD grid of "
+                        f"{g['d']*1e9:.0f} nm, Gaussian beam E0={g['E0']:.0e} V/m "
+                        f"tau={g['tau']*1e15:.0f} fs hbar w0=Eg+{g['det']*1e3:.0f} meV, "
+                        f"T={g['temp']:.0f} K, RK4 dt={g['dt']*1e15:.2f} fs",
+            "wires": g["nw"], "nk": g["nk"], "grid": list(g["n"]),
+            "flags": " ".join(k for k, v in FLAGS.items() if v),
+            "field": "3-D PSTD, six c128 components, FP32 transforms, FP64 fields",
+            "l2": "inputs larger than L2 (FP64 wire state 3.2 GB, fields 403 MB)"}
+
+
+def grid3_arm(args):
+    """Config 4: 64 wires of Nk = 1024 coupled to the 3-D grid; value = wire-steps/s of
+    the coupled step (mixed path); the field step alone is timed for its HBM roofline."""
+    import torch
+    import __graft_entry__ as ge
+    rank, world, local = env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    ge.build()
+    from pulsesuite_gb300 import _lib
+    from pulsesuite_gb300.pstd import CoupledGrid3, Pstd3D, SheetSource
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    g3 = GRID3
+    n, d, nw, nk, dt = g3["n"], g3["d"], g3["nw"], g3["nk"], g3["dt"]
+    rng = np.random.default_rng(g3["seed"])
+    Lx, Ly = (n[0] - 1) * d, (n[1] - 1) * d
+    wxy = np.stack([rng.uniform(-0.3 * Lx, 0.3 * Lx, nw), rng.uniform(-0.3 * Ly, 0.3 * Ly, nw)], 1)
+    L = wire_L(nk, g3["kmax"])
+    specs = [WireSpec(nk=nk, L=L, temp=g3["temp"], wire_index=w + 1, flags=dict(FLAGS), **MAT)
+             for w in range(nw)]
+    t_ctx = time.perf_counter()
+    ctx = WireContext(specs)
+    t_ctx = time.perf_counter() - t_ctx
+    prec = _lib.PREC_MIXED if args.precision == "mixed" else _lib.PREC_FP64
+    grid = Pstd3D(n, (d, d, d), MAT["epsr"], n_abc=g3["n_abc"], abc_strength=g3["abc"],
+                  fp32_work=prec == _lib.PREC_MIXED)
+    x = grid.x[0].cpu().numpy()
+    y = grid.x[1].cpu().numpy()
+    z = grid.x[2].cpu().numpy()
+    i_src = g3["n_abc"][0] + g3["src_cell"]
+    x_src = float(x[i_src])
+    v = C0 / np.sqrt(MAT["epsr"])
+    w0 = (MAT["gap"] + g3["det"] * E0C) / HBAR
+    t_start = (0.0 - x_src) / v
+    line = CoupledGrid3(ctx, grid, wxy,
+                        source=SheetSource(index=i_src, E0=g3["E0"], tau=g3["tau"], w0=w0, tpeak=0.0),
+                        pol=1, waist=g3["waist"], gate=5e-9, t0=t_start)
+    cache = args.tile_cache or os.path.join(tempfile.gettempdir(), "sbe_tiles.json")
+    tiles = ctx.autotune(cache) if prec == _lib.PREC_MIXED else []
+    # the beam in flight: Ey = E_inc(t - |x - x_src|/v) exp(-(y^2 + z^2)/waist^2),
+    # Hz = sign(x - x_src) Ey(t - dt/2) / eta
+    eta = np.sqrt(1.25663706127e-06 / (8.8541878188e-12 * MAT["epsr"]))
+    prof = np.exp(-(y[:, None] ** 2 + z[None, :] ** 2) / g3["waist"] ** 2)
+
+    def einc(t):
+        return g3["E0"] * np.exp(-(t / g3["tau"]) ** 2) * np.cos(w0 * t)
+
+    dist_x = np.abs(x - x_src)
+    ex = einc(t_start - dist_x / v)
+    hx = np.sign(x - x_src) * einc(t_start - dt / 2 - dist_x / v) / eta
+    fe = 1.0 / (np.exp(np.minimum((ctx.table(0, "Ee").cpu().numpy() + MAT["gap"] / 2.0) /
+                                  (1.380649e-23 * g3["temp"]), 700.0)) + 1.0)
+
+    def fresh():
+        E = torch.zeros((3,) + n, dtype=torch.complex128, device="cuda")
+        H = torch.zeros_like(E)
+        pr = torch.as_tensor(prof, device="cuda")
+        E[1] = torch.as_tensor(ex, device="cuda")[:, None, None] * pr[None]
+        H[2] = torch.as_tensor(hx, device="cuda")[:, None, None] * pr[None]
+        dg = np.diag(fe).astype(complex)
+        return ctx.zeros_state(), ctx.pack([dg] * nw), ctx.pack([dg] * nw), E, H
+
+    st = fresh()
+    line.reset()
+    line.step(*st, dt, prec)
+    graph = line.graph(*st, dt, prec)
+    for _ in range(max(0, args.warmup - 1)):
+        graph.launch()
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    for cat in range(4):
+        ctx.profile_read(cat)
+    clk_dir = os.environ.get("SBE_CLOCKS_DIR", tempfile.gettempdir())
+    clocks = ClockSampler(local, os.path.join(clk_dir, f"clocks_grid3_{rank}.csv"))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        graph.launch()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    prof_k = {cat: ctx.profile_read(cat) for cat in range(4)}
+    ctx.profile(False)
+    ctx.check()
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * nw * args.steps / (ms / 1e3)
+    n_kernels = graph.kernels
+    graph.close()
+
+    # end to end: the grid field E in from pinned host memory and the grid current J
+    # back to pinned host memory every step (the wires' effect on the field)
+    h_E = st[3].cpu().pin_memory()
+    h_J = torch.empty((3,) + n, dtype=torch.complex128).pin_memory()
+    Jv = line.view("J")
+    torch.cuda.synchronize()
+    e0e = torch.cuda.Event(enable_timing=True)
+    e1e = torch.cuda.Event(enable_timing=True)
+    e0e.record()
+    for _ in range(args.steps):
+        st[3].copy_(h_E, non_blocking=True)
+        line.step(*st, dt, prec)
+        h_J.copy_(Jv, non_blocking=True)
+    e1e.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0e.elapsed_time(e1e)
+
+    # the field step alone (H and E updates with the wires' current), its HBM roofline
+    Et, Ht = st[3].clone(), st[4].clone()
+    Jt = line.view("J").clone()
+    for _ in range(3):
+        grid.step(Et, Ht, Jt, dt)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for _ in range(20):
+        grid.step(Et, Ht, Jt, dt)
+    p1.record()
+    torch.cuda.synchronize()
+    field_ms = p0.elapsed_time(p1) / 20
+    del Et, Ht, Jt
+
+    # RHS error against FP64 at the current state and field on the wires
+    P, C, D = st[0], st[1], st[2]
+    Ek = line.view("Ek").clone()
+    r64 = ctx.rhs(P, C, D, Ek, _lib.PREC_FP64)
+    rmx = ctx.rhs(P, C, D, Ek, _lib.PREC_MIXED)
+    rhs_err = max(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) for a, b in zip(rmx, r64))
+    del r64, rmx
+
+    fp64_ms = fp64_val = None
+    if not args.no_fp64:
+        st64 = tuple(t.clone() for t in st)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record()
+        line.step(*st64, dt, _lib.PREC_FP64)
+        f1.record()
+        torch.cuda.synchronize()
+        fp64_ms = f0.elapsed_time(f1)
+        fp64_val = world * nw / (fp64_ms / 1e3)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, pk_kind = measured_peaks()
+    N = n[0] * n[1] * n[2]
+    field_bytes = N * (4 * 3 * 16 + 3 * 16)     # E, H read + write, J read (c128)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved_gbs = field_bytes / (field_ms / 1e3) / 1e9
+    comm_ms, comm_n = prof_k[0]
+    per_eval_s = comm_ms / (4 * args.steps) / 1e3
+    bf = peaks.get("bf16_tflops_sustained", 1700.0)
+    line_out = {"metric": METRIC, "value": value, "unit": "wire-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
+                "data": "synthetic", "config": grid3_config(), "precision": args.precision,
+                "clocks": clk,
+                "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
+                        "h2d_bytes_per_step": int(3 * N * 16), "d2h_bytes_per_step": int(3 * N * 16)},
+                "gpu_launches": int(n_kernels * args.steps), "gpu_launches_per_step": int(n_kernels),
+                "roofline": {"bound": "hbm", "kernel": "3-D PSTD field step (FFT passes + curl + update)",
+                             "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved_gbs / hbm, "peak_kind": f"{pk_kind} HBM copy",
+                             "traffic": None, "ms_per_field_step": field_ms,
+                             "bytes_model": "E and H read and written, J read once: 240 B per grid "
+                                            "point (c128), over the CUDA-event time of one step"},
+                "commutator_gemm": {"achieved_tflops": 96.0 * nk ** 3 * nw / per_eval_s / 1e12,
+                                    "frac": 96.0 * nk ** 3 * nw / per_eval_s / 1e12 / bf,
+                                    "ms_per_rhs_eval": per_eval_s * 1e3, "launches": comm_n},
+                "step_tflops": 496.0 * nk ** 3 * nw * (args.steps / (ms / 1e3)) / 1e12,
+                "tiles": tiles, "ctx_create_s": t_ctx,
+                "fp64_gpu": {"value": fp64_val, "unit": "wire-steps/s", "ms_per_step": fp64_ms,
+                             "steps": 1},
+                "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
+                "rhs_rel_err_vs_fp64": rhs_err,
+                "cpu_baseline": None}
+    print(json.dumps(line_out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -727,7 +944,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS) + ["sweep"])
+    ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS) + ["sweep", "grid3d"])
     ap.add_argument("--tile-cache", default=None,
                     help="JSON tile cache of the autotuner (default: in the temp directory)")
     ap.add_argument("--fp64-steps", type=int, default=3)
@@ -742,6 +959,8 @@ def main():
     wl = WORKLOADS.get(args.workload)
     if args.impl == "reference":
         reference_arm(args, wl)
+    elif args.workload == "grid3d":
+        grid3_arm(args)
     elif wl is None:
         sweep_arm(args)
     else:

@@ -138,11 +138,20 @@ _LEVELS = ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3")
 
 
 class SBESolver:
-    """SBEs.py:4619 SBESolver on the GPU: one device context per wire."""
+    """SBEs.py:4619 SBESolver on the GPU.
+
+    By default every wire has a device context of its own and QWCalculator(w) steps
+    wire w, as the reference does.  With ``batch=True`` all wires share one context:
+    QWCalculator(w) for w < Nw stages wire w's field and keeps its output arrays, and
+    the call for w = Nw steps every wire in one batched leapfrog step and fills the
+    output arrays of all of them (the drivers call the wires of a time step in order
+    and read the outputs after the last one, sbetestprop.py:181-234,
+    rhoPJ.py:306-343)."""
 
     def __init__(self, q, rr, r0, Emaxxx, lam, Nw, QW, backend="gb300", params=None, flags=None,
-                 nk=None, temp=77.0):
+                 nk=None, temp=77.0, batch=False):
         self.Nw = Nw
+        self.batch = bool(batch)
         self.QW = QW
         self.xxx = 1
         self.jjj = 1
@@ -168,14 +177,15 @@ class SBESolver:
         self.Nk = nk
         self.Nr = 2 * nk + 2
         cflags = {k: bool(f.get(k, False)) for k in _lib.FLAG_BITS}
-        self.contexts = []
-        for w in range(1, Nw + 1):
-            spec = WireSpec(nk=nk, L=self.L, Delta0=self.Delta0, gap=self.gap, me=self.me,
-                            mh=self.mh, HO=self.HO, gam_e=self.gam_e, gam_h=self.gam_h,
-                            gam_eh=self.gam_eh, epsr=self.epsr, Oph=self.Oph, Gph=self.Gph,
-                            temp=temp, Edc=float(getattr(self, "Edc", 0.0)), wire_index=w,
-                            flags=cflags)
-            self.contexts.append(WireContext([spec]))
+        specs = [WireSpec(nk=nk, L=self.L, Delta0=self.Delta0, gap=self.gap, me=self.me,
+                          mh=self.mh, HO=self.HO, gam_e=self.gam_e, gam_h=self.gam_h,
+                          gam_eh=self.gam_eh, epsr=self.epsr, Oph=self.Oph, Gph=self.Gph,
+                          temp=temp, Edc=float(getattr(self, "Edc", 0.0)), wire_index=w,
+                          flags=cflags) for w in range(1, Nw + 1)]
+        if self.batch:
+            self.contexts = [WireContext(specs)]
+        else:
+            self.contexts = [WireContext([sp]) for sp in specs]
         c0 = self.contexts[0]
         self.kr = c0.table(0, "kr").cpu().numpy()
         self.r = c0.table(0, "r").cpu().numpy()
@@ -191,13 +201,20 @@ class SBESolver:
         with np.errstate(over="ignore"):
             fe = 1.0 / (np.exp((self.Ee + self.gap / 2.0) / KB / temp) + 1.0)
         dev = torch.device("cuda")
-        self._st = []
+        d = torch.as_tensor(fe, dtype=CDTYPE, device=dev)
+        if self.batch:
+            # nine packed levels of all wires; _st[w][i] are views of wire w's blocks
+            self._lev = [c0.zeros_state() for _ in range(9)]
+            self._st = [[c0.mat(self._lev[i], w) for i in range(9)] for w in range(Nw)]
+            self._ek = c0.zeros_r(3)
+            self._src = c0.zeros_r(5)
+            self._outs = [None] * Nw
+        else:
+            self._st = [[torch.zeros((nk, nk), dtype=CDTYPE, device=dev) for _ in range(9)]
+                        for _ in range(Nw)]
         for w in range(Nw):
-            lv = [torch.zeros((nk, nk), dtype=CDTYPE, device=dev) for _ in range(9)]
-            d = torch.as_tensor(fe, dtype=CDTYPE, device=dev)
             for i in (3, 4, 5, 6, 7, 8):
-                lv[i].diagonal().copy_(d)
-            self._st.append(lv)
+                self._st[w][i].diagonal().copy_(d)
         self.rr_offset = np.asarray(rr) - r0
         self._rr_dev = None
 
@@ -224,8 +241,8 @@ class SBESolver:
         self.Optics = False
         self.flags["Optics"] = False
         for ctx in self.contexts:
-            spec = ctx.specs[0]
-            spec.flags = dict(spec.flags, Optics=False)
+            for spec in ctx.specs:
+                spec.flags = dict(spec.flags, Optics=False)
         self.contexts = [WireContext(ctx.specs) for ctx in self.contexts]
 
     def QWCalculator(self, Exx, Eyy, Ezz, Vrr, rr, q, dt, w, Pxx, Pyy, Pzz, Rho, DoQWP, DoQWDl):
@@ -246,10 +263,13 @@ class SBESolver:
         self.wireoff = False
         DoQWP[0] = self.Optics
         DoQWDl[0] = self.LF
-        ctx = self.contexts[w - 1]
         RR = torch.as_tensor(np.asarray(rr, dtype=np.float64), device="cuda")
         f4 = torch.as_tensor(np.stack([np.asarray(a, dtype=complex) for a in (Exx, Eyy, Ezz, Vrr)]),
                              dtype=CDTYPE, device="cuda").contiguous()
+        if self.batch:
+            self._batched(w, RR, f4, dt, (Pxx, Pyy, Pzz, Rho))
+            return
+        ctx = self.contexts[w - 1]
         Ek = ctx.prop2qw(0, RR, f4)                       # (4, Nr): Ex, Ey, Ez, Vr in wire k space
         src = torch.empty((5, self.Nr), dtype=CDTYPE, device="cuda")
         Ek3 = Ek[:3].contiguous()
@@ -267,12 +287,41 @@ class SBESolver:
             Pzz[:] = 0.0
             Rho[:] = 0.0
 
+    def _batched(self, w, RR, f4, dt, outs):
+        """Stage wire w's field; on the last wire step them all and fill every wire's
+        outputs (Pxx, Pyy, Pzz, Rho = RhoH - RhoE, SBEs.py:5917)."""
+        ctx = self.contexts[0]
+        Ek = ctx.prop2qw(w - 1, RR, f4)
+        ctx.rvec(self._ek, w - 1, 3).copy_(Ek[:3])
+        self._outs[w - 1] = outs
+        if w != self.Nw:
+            return
+        ctx.leapfrog_step(self._lev, self._ek, dt, self._src)
+        for wi in range(self.Nw):
+            o = self._outs[wi]
+            if o is None:
+                continue
+            src = ctx.rvec(self._src, wi, 5).contiguous()
+            out = ctx.qw2prop(wi, RR, src, self.LF).cpu().numpy()
+            if self.write_info:
+                self._write_info(ctx, wi + 1, dt, None, None)
+            ign = getattr(self, "ignorewire", False)
+            o[0][:] = 0.0 if ign else out[0]
+            o[1][:] = 0.0 if ign else out[1]
+            o[2][:] = 0.0 if ign else out[2]
+            o[3][:] = 0.0 if ign else out[4] - out[3]
+        self._outs = [None] * self.Nw
+
     def _write_info(self, ctx, w, dt, src, Ek3):
         """SBEs.py:5769-5809: append this step's line to dataQW/info.WW.t.dat and to
         dataQW/EP.WW.t.dat (statistics reduced on the device by sbe_wire_info; the
         CalcI0n columns print as complex numbers, as the reference's do)."""
         st = self._st[w - 1]
-        v = ctx.wire_info(0, st[4], st[7], src, Ek3)
+        if self.batch:
+            # the statistics kernel reads wire w's blocks of the packed buffers
+            v = ctx.wire_info(w - 1, self._lev[4], self._lev[7], self._src, self._ek)
+        else:
+            v = ctx.wire_info(0, st[4], st[7], src, Ek3)
         t = self.xxx * dt
         info = [t] + [float(x) for x in v[:15]] + [complex(v[15], 0.0), complex(v[16], 0.0)]
         os.makedirs("dataQW", exist_ok=True)

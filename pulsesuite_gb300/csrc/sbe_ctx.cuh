@@ -142,6 +142,7 @@ struct GemmBatch {
   const double* gamH;
   const double2* offp;  // optional explicit OffP (single-wire API)
   int w_only = -1;      // >= 0: only this wire of the context
+  int flag_mask = 0;    // != 0: only the wires whose flags hold every bit of it (batched)
 };
 void launch_gemm64(const WireDev* d_wires, int nw, int nk_max, const GemmBatch& b,
                    bool batched, int nk_single, cudaStream_t s);

@@ -104,7 +104,8 @@ void launch_dc_transport(SbeCtx* c, double2* P, double2* C, double2* D, const do
   double2* X[3] = {C, D, P};
   if (lf) {
     // S into dA (the dephasing contraction matrices are not used after the RHS), the
-    // product S X into dP (the RHS outputs are consumed by then), then X = (S X) S^T
+    // product S X into dP (the RHS outputs are consumed by then), then X = (S X) S^T;
+    // only the wires with DCTrans and LF take part (the others keep X untouched)
     double2* S = c->dA;
     double2* T = c->dP;
     k_dc_smat<<<dim3((nk + 127) / 128, nk, c->nw), 128, 0, s>>>(c->d_wires, c->dcs, S);
@@ -113,11 +114,13 @@ void launch_dc_transport(SbeCtx* c, double2* P, double2* C, double2* D, const do
       b.nterms = 1;
       b.t[0] = Term{S, X[i], OP_N, OP_N, 0, make_double2(1.0, 0.0)};
       b.out = T;
+      b.flag_mask = SBE_F_DCTRANS | SBE_F_LF;
       launch_gemm64(c->d_wires, c->nw, nk, b, true, 0, s);
       GemmBatch b2{};
       b2.nterms = 1;
       b2.t[0] = Term{T, S, OP_N, OP_T, 0, make_double2(1.0, 0.0)};
       b2.out = X[i];
+      b2.flag_mask = SBE_F_DCTRANS | SBE_F_LF;
       launch_gemm64(c->d_wires, c->nw, nk, b2, true, 0, s);
     }
   }

@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256) k_gemm64(const WireDev* wires, GemmArgs g
   long long off_mat = 0, off_kr = 0, off_vec = 0;
   if (g.batched) {
     const WireDev& W = wires[g.b.w_only >= 0 ? g.b.w_only : blockIdx.z];
+    if (g.b.flag_mask && (W.flags & g.b.flag_mask) != g.b.flag_mask) return;
     nk = W.nk;
     nr = W.nr;
     off_mat = W.off_mat;

@@ -208,6 +208,38 @@ def test_solver_leapfrog_vs_golden(tmp_path, monkeypatch):
     s.close()
 
 
+def test_batched_solver_leapfrog_vs_golden(tmp_path, monkeypatch):
+    """SBESolver(batch=True): both wires in one context, stepped together on the call
+    for wire 2, outputs of wire 1 filled then; the reference driver's call order gives
+    the reference's three steps."""
+    from pulsesuite_gb300 import SBEs
+    monkeypatch.chdir(tmp_path)
+    g = golden("solver_step")
+    prm = dict(L=float(g["L"]), Delta0=6e-9, gap=1.52 * O.E0, me=0.067 * O.ME0,
+               mh=0.45 * O.ME0, HO=100e-3 * O.E0, gam_e=1e12, gam_h=1e12, gam_eh=1e12,
+               epsr=12.9, Oph=36e-3 * O.E0 / O.HBAR, Gph=3e-3 * O.E0 / O.HBAR, Edc=0.0,
+               jmax=100000, ntmax=100000)
+    rr = g["rr"]
+    s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
+                       flags=SOLVER_FLAGS, batch=True)
+    assert len(s.contexts) == 1
+    for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+        setattr(s, nm, g["init_" + nm])
+    dt = float(g["dt"])
+    for n in range(3):
+        outs = {}
+        for w in (1, 2):
+            outs[w] = [np.zeros(len(rr), complex) for _ in range(4)]
+            s.QWCalculator(g[f"s{n}_Exx"], g[f"s{n}_Eyy"], g[f"s{n}_Ezz"],
+                           np.zeros(len(rr), complex), rr, None, dt, w, *outs[w], [False], [False])
+        for w in (1, 2):
+            for a, nm in zip(outs[w], ("Pxx", "Pyy", "Pzz", "Rho")):
+                assert rel(a, g[f"s{n}_w{w}_{nm}"]) < SCREEN, (n, w, nm)
+        for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
+            assert rel(getattr(s, nm), g[f"s{n}_{nm}"]) < SCREEN, (n, nm)
+    s.close()
+
+
 def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch):
     """100 reference QWCalculator steps on two wires (SBESolver drop-in, FP64 path):
     the sources of every tenth step and the nine state levels at the end <= 1e-10."""
@@ -480,6 +512,34 @@ def test_solver_leapfrog_dc_vs_oracle(tmp_path, monkeypatch):
             assert rel(getattr(s, nm), getattr(ref, nm)) < SCREEN, (n, nm)
     assert rel(ref.CC3, g["s2_CC3"]) > 1e-6   # the transport changed the state
     s.close()
+
+
+def test_dc_transport_leaves_other_wires_untouched():
+    """A context of one wire with DCTrans + LF and one without: the second wire's RK4
+    step (FP64 path) is bit for bit the step of that wire in a context of its own (the
+    transport's circulant products run on the DCTrans wires only)."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    dc = dict(ALL, DCTrans=True)
+    both = WireContext([WireSpec(nk=nk, L=L, temp=77.0, wire_index=1, flags=dc, Edc=5e7, **MAT),
+                        WireSpec(nk=nk, L=L, temp=77.0, wire_index=2, flags=dict(ALL), **MAT)])
+    alone = WireContext([WireSpec(nk=nk, L=L, temp=77.0, wire_index=2, flags=dict(ALL), **MAT)])
+    rng = np.random.default_rng(17)
+    st = [_seeded_state(rng, nk) for _ in range(2)]
+    wire = O.Wire(nk, L, MAT, ALL)
+    fld = [_uniform_field_k(wire, 2e7), _uniform_field_k(wire, 1e7)]
+    dfld = [_uniform_field_k(wire, -1e5), _uniform_field_k(wire, 3e5)]
+    P2, C2, D2 = (both.pack([s[i] for s in st]) for i in range(3))
+    P1, C1, D1 = (alone.pack([st[1][i]]) for i in range(3))
+    both.rk4_step(P2, C2, D2, both.pack_r([np.stack(f) for f in fld], 3),
+                  both.pack_r([np.stack(f) for f in dfld], 3), 0.1e-15, both.zeros_r(5))
+    alone.rk4_step(P1, C1, D1, alone.pack_r([np.stack(fld[1])], 3),
+                   alone.pack_r([np.stack(dfld[1])], 3), 0.1e-15, alone.zeros_r(5))
+    torch.cuda.synchronize()
+    for a, b in ((P2, P1), (C2, C1), (D2, D1)):
+        assert torch.equal(both.mat(a, 1), alone.mat(b, 0))
+    assert not torch.equal(both.mat(C2, 0), both.pack([st[0][1]])[:nk * nk].view(nk, nk))
 
 
 def test_solver_backup_files_round_trip(tmp_path, monkeypatch):
