@@ -8,7 +8,8 @@
 // File format (one entry per line, so that entries can be replaced line by line):
 //   {"sbe_autotune": 1, "entries": [
 //   {"key": "<device>|sm<cc>|<SMs>|f<flags>|<nk>x<nw>;...", "buckets": [{"nk": N,
-//    "nw": W, "exchange_bn": B, "commutator_bn": B, "sources_bn": B, "ms": {...}}, ...]},
+//    "nw": W, "exchange_bn": B, "commutator_bn": B, "sources_bn": B, "hh_split": S,
+//    "ms": {...}}, ...]},
 //   ...
 //   ]}
 #include <cstdio>
@@ -70,7 +71,7 @@ bool load(const char* path, const std::string& key, MixedAll* A) {
     if (key_in(line) != key) continue;
     std::vector<int> v;
     size_t pos = 0;
-    const std::string tag = "{\"nk\": ";
+    const std::string tag = "{\"nk\": ", htag = "\"hh_split\": ";
     while ((pos = line.find(tag, pos)) != std::string::npos) {
       int nk, nw, e, f, s;
       if (std::sscanf(line.c_str() + pos,
@@ -78,22 +79,30 @@ bool load(const char* path, const std::string& key, MixedAll* A) {
                       "\"sources_bn\": %d",
                       &nk, &nw, &e, &f, &s) != 5)
         return false;
-      v.insert(v.end(), {nk, nw, e, f, s});
+      // optional hi*hi split of this bucket (before the next bucket's entry)
+      const size_t next = line.find(tag, pos + tag.size());
+      const size_t hp = line.find(htag, pos);
+      int hs = 2;
+      if (hp != std::string::npos && (next == std::string::npos || hp < next) &&
+          std::sscanf(line.c_str() + hp + htag.size(), "%d", &hs) != 1)
+        return false;
+      v.insert(v.end(), {nk, nw, e, f, s, hs});
       pos += tag.size();
     }
-    if (v.size() != 5 * A->b.size()) return false;
+    if (v.size() != 6 * A->b.size()) return false;
     for (size_t i = 0; i < A->b.size(); ++i) {
       Mixed* m = A->b[i];
-      const int* r = &v[5 * i];
-      if (r[0] != m->nk || r[1] != m->nw) return false;
+      const int* r = &v[6 * i];
+      if (r[0] != m->nk || r[1] != m->nw || r[5] < 1 || r[5] > 4) return false;
       for (int j = 2; j < 5; ++j)
         if (r[j] != 128 && r[j] != 256) return false;
     }
     for (size_t i = 0; i < A->b.size(); ++i) {
       Mixed* m = A->b[i];
-      m->bn[JK_EXCH] = v[5 * i + 2];
-      m->bn[JK_FULL] = v[5 * i + 3];
-      m->bn[JK_SRC] = v[5 * i + 4];
+      m->bn[JK_EXCH] = v[6 * i + 2];
+      m->bn[JK_FULL] = v[6 * i + 3];
+      m->bn[JK_SRC] = v[6 * i + 4];
+      m->hs = v[6 * i + 5];
     }
     return true;
   }
@@ -178,9 +187,9 @@ extern "C" int sbe_autotune(SbeCtx* c, const char* cache_json) {
     char buf[512];
     std::snprintf(buf, sizeof(buf),
                   "%s{\"nk\": %d, \"nw\": %d, \"exchange_bn\": %d, \"commutator_bn\": %d, "
-                  "\"sources_bn\": %d, \"ms\": {\"%s\": [%.5f, %.5f], \"%s\": [%.5f, %.5f], "
-                  "\"%s\": [%.5f, %.5f]}}",
-                  i ? ", " : "", m->nk, m->nw, m->bn[JK_EXCH], m->bn[JK_FULL], m->bn[JK_SRC],
+                  "\"sources_bn\": %d, \"hh_split\": %d, \"ms\": {\"%s\": [%.5f, %.5f], "
+                  "\"%s\": [%.5f, %.5f], \"%s\": [%.5f, %.5f]}}",
+                  i ? ", " : "", m->nk, m->nw, m->bn[JK_EXCH], m->bn[JK_FULL], m->bn[JK_SRC], m->hs,
                   kNames[0], ms[0][0], ms[0][1], kNames[1], ms[1][0], ms[1][1], kNames[2],
                   ms[2][0], ms[2][1]);
     entry << buf;
@@ -199,11 +208,12 @@ extern "C" int sbe_ctx_tiles(const SbeCtx* cc, int* out, int cap, int* nbuckets)
   if (!c || !nbuckets || (cap > 0 && !out)) return fail(SBE_ERR_ARG, "sbe_ctx_tiles: bad arguments");
   MixedAll* A = all_of(c);
   *nbuckets = A ? (int)A->b.size() : 0;
-  for (int i = 0; A && i < (int)A->b.size() && 5 * i + 4 < cap; ++i) {
+  for (int i = 0; A && i < (int)A->b.size() && 6 * i + 5 < cap; ++i) {
     Mixed* m = A->b[i];
-    const int v[5] = {m->nk, m->nw, m->bn[JK_EXCH] ? m->bn[JK_EXCH] : 256,
-                      m->bn[JK_FULL] ? m->bn[JK_FULL] : 256, m->bn[JK_SRC] ? m->bn[JK_SRC] : 256};
-    for (int j = 0; j < 5; ++j) out[5 * i + j] = v[j];
+    const int v[6] = {m->nk, m->nw, m->bn[JK_EXCH] ? m->bn[JK_EXCH] : 256,
+                      m->bn[JK_FULL] ? m->bn[JK_FULL] : 256, m->bn[JK_SRC] ? m->bn[JK_SRC] : 256,
+                      m->hs};
+    for (int j = 0; j < 6; ++j) out[6 * i + j] = v[j];
   }
   return SBE_OK;
 }

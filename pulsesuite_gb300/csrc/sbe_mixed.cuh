@@ -17,6 +17,9 @@ struct Mixed {
   // the engine's default of 256; the hi*hi mode has its own fixed tile), chosen by
   // sbe_autotune
   int bn[4] = {0, 0, 0, 0};
+  // K parts of the hi*hi products of W and V (split-K: shorter truncating FP32
+  // chains; the parts meet in the anti-Hermitian pass); 1 to 4
+  int hs = 2;
   tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
   float* xsh = nullptr;    // exchange sums, un-sheared: 3 x Nw x Nk x Nk complex (FP32)
   void* block = nullptr;   // one allocation for the per-wire vectors below

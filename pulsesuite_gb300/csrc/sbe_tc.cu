@@ -1194,6 +1194,18 @@ __global__ void k_hplanes(const float2* hee, const float2* hhh, const float* hA,
   }
 }
 
+// s + e = a + b exactly (Knuth's two-sum in round-to-nearest FP32).  The peeled
+// diagonal energies enter as products with the state every stage; a rounded FP32
+// energy sum would be the same rounding every step, i.e. a frequency bias whose phase
+// error grows with the number of oscillation periods, so the sum is kept exact as an
+// unevaluated pair and the products round independently.
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+  return make_float2(s, e);
+}
+
 // RK4 stage update fused into the element-wise RHS passes (k_rhs_p, k_antiherm):
 // the stage derivative k of an element is used where it is formed.  The
 // arithmetic is that of the RK4 of the mixed path: FP32 k and sums k1 + 2 k2 +
@@ -1275,7 +1287,7 @@ __device__ __forceinline__ void rk4_block_max(const Rk4Ctl& r, int b, unsigned m
 // halves and the hi*lo + lo*hi products); g[j] - g[i] comes from the hi / lo FP32
 // parts of g.
 __global__ void __launch_bounds__(256) k_antiherm(
-    int nk, const float2* __restrict__ W, const float2* __restrict__ W2,
+    int nk, const float2* __restrict__ W, int nparts, long long pstride,
     const float2* __restrict__ W3, const float2* __restrict__ Hp, const float2* X,
     const float2* __restrict__ ghi, const float2* __restrict__ glo, const float* __restrict__ chi,
     const float* __restrict__ clo, float2* out, Rk4Ctl rk) {
@@ -1297,24 +1309,29 @@ __global__ void __launch_bounds__(256) k_antiherm(
     cv[ty][0][tx] = chi[v];
     cv[ty][1][tx] = clo[v];
   }
-  // the mirror tile: four rows per thread, loads issued together
+  // the mirror tile: four rows per thread, loads issued together; W is the sum of the
+  // hi*hi K parts (in order) and the cross terms
   {
-    float2 w[4][3], h[4];
+    float2 w[4], h[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int ib = j0 + ty + 8 * q, jb = i0 + tx;
       const bool ok = ib < nk && jb < nk;
       const long long ob = mb + (long long)(ok ? ib : 0) * nk + (ok ? jb : 0);
-      w[q][0] = W[ob];
-      w[q][1] = W2[ob];
-      w[q][2] = W3[ob];
+      w[q] = W[ob];
+      for (int p = 1; p < nparts; ++p) {
+        const float2 v = W[p * pstride + ob];
+        w[q].x += v.x;
+        w[q].y += v.y;
+      }
+      const float2 x3 = W3[ob];
+      w[q] = make_float2(w[q].x + x3.x, w[q].y + x3.y);
       h[q] = Hp[ob];
-      if (!ok) w[q][0] = w[q][1] = w[q][2] = h[q] = make_float2(0.f, 0.f);
+      if (!ok) w[q] = h[q] = make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      tb[ty + 8 * q][tx] = make_float2((w[q][0].x + w[q][1].x) + w[q][2].x,
-                                       (w[q][0].y + w[q][1].y) + w[q][2].y);
+      tb[ty + 8 * q][tx] = w[q];
       hb[ty + 8 * q][tx] = h[q];
     }
   }
@@ -1323,15 +1340,20 @@ __global__ void __launch_bounds__(256) k_antiherm(
   unsigned mxv = 0, mov = 0;
   // the tile (i0.., j0..): i <= j wherever it is written
   {
-    float2 w[4][3], x[4];
+    float2 w[4], x[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int i = i0 + ty + 8 * q, j = j0 + tx;
       const bool ok = i < nk && j < nk;
       const long long oa = mb + (long long)(ok ? i : 0) * nk + (ok ? j : 0);
-      w[q][0] = W[oa];
-      w[q][1] = W2[oa];
-      w[q][2] = W3[oa];
+      w[q] = W[oa];
+      for (int p = 1; p < nparts; ++p) {
+        const float2 v = W[p * pstride + oa];
+        w[q].x += v.x;
+        w[q].y += v.y;
+      }
+      const float2 x3 = W3[oa];
+      w[q] = make_float2(w[q].x + x3.x, w[q].y + x3.y);
       x[q] = X[oa];
     }
     const float2 gjh = gv[1][0][tx], gjl = gv[1][1][tx];
@@ -1340,16 +1362,18 @@ __global__ void __launch_bounds__(256) k_antiherm(
     for (int q = 0; q < 4; ++q) {
       const int r = ty + 8 * q;
       const int i = i0 + r, j = j0 + tx;
-      const float2 a = make_float2((w[q][0].x + w[q][1].x) + w[q][2].x,
-                                   (w[q][0].y + w[q][1].y) + w[q][2].y);   // W[i][j]
+      const float2 a = w[q];                         // W[i][j]
       const float2 bt = tb[tx][r];                   // W[j][i]
       const float2 hji = hb[tx][r];                  // H'[j][i]
       const float2 gih = gv[0][0][r], gil = gv[0][1][r];
-      const float dr = (gjh.x - gih.x) + (gjl.x - gil.x);
+      const float2 dh = two_sum(gjh.x, -gih.x);            // exact difference of the hi parts
+      const float drl = dh.y + (gjl.x - gil.x);
       const float di = (gjh.y - gih.y) + (gjl.y - gil.y);
       const float dc = (cv[0][0][r] - cjh) + (cv[0][1][r] - cjl);
-      const float re = (a.x - bt.x) + dc * hji.x + (dr * x[q].x - di * x[q].y);
-      const float im = (a.y + bt.y) + dc * hji.y + (dr * x[q].y + di * x[q].x);
+      const float re = (a.x - bt.x) + dc * hji.x +
+                       ((dh.x * x[q].x - di * x[q].y) + drl * x[q].x);
+      const float im = (a.y + bt.y) + dc * hji.y +
+                       ((dh.x * x[q].y + di * x[q].x) + drl * x[q].y);
       const float2 v = make_float2(im * ih, -re * ih);
       vt[r][tx] = v;
       if (i < nk && j < nk && (bi < bj || j >= i)) {
@@ -1452,9 +1476,10 @@ __global__ void __launch_bounds__(256) k_rhs_p(
     const float pb = ((1.f - chi) - rv[1][r]) - (clo + rv[2][r]);
     const float ax = g[q].x + pb * h0.x, ay = g[q].y + pb * h0.y;
     const float2 gh = rg[0][r], gl = rg[1][r];
-    const float der = (gh.x + eh.x) + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
-    const float ar = ax + (der * x[q].x - dei * x[q].y);
-    const float ai = ay + (der * x[q].y + dei * x[q].x);
+    const float2 sh = two_sum(gh.x, eh.x);                 // exact sum of the hi parts
+    const float derl = sh.y + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
+    const float ar = ax + ((sh.x * x[q].x - dei * x[q].y) + derl * x[q].x);
+    const float ai = ay + ((sh.x * x[q].y + dei * x[q].x) + derl * x[q].y);
     const float gam = gamE + rv[0][r];
     const float2 kv = make_float2(ai * ih - gam * x[q].x, -ar * ih - gam * x[q].y);
     const long long o = mb + (long long)m * nk + n;
@@ -1548,8 +1573,9 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
     const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
     const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
     // G buffer (FP32 complex, tot_mat each, indexed like the packed state): [W hh
-    // K-half 0, W hh K-half 1, V hh 0, V hh 1, dP sums, W cross terms, V cross terms]
+    // K-parts 0 .. hs-1, V hh parts, dP sums, W cross terms, V cross terms]
     float2* wf = reinterpret_cast<float2*>(c->G);   // the buffer holds 12 tot_mat float2
+    const int hs = m->hs;
     auto epi = [&](float2* o) {
       tc::EpiArgs e{};
       e.kind = tc::EPI_RAWF;
@@ -1561,12 +1587,15 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
       return e;
     };
     if (kind == JK_FULL) {
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 4, tP, 0, epi(wf + 4 * tm)));
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + 5 * tm), tc::MODE_FULL, 1));
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + 6 * tm), tc::MODE_FULL, 1));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 4, tP, 0, epi(wf + 2 * hs * tm)));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + (2 * hs + 1) * tm),
+                        tc::MODE_FULL, 1));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + (2 * hs + 2) * tm),
+                        tc::MODE_FULL, 1));
     } else {
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf), tc::MODE_HH, 0, 2));
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + 2 * tm), tc::MODE_HH, 0, 2));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf), tc::MODE_HH, 0, hs));
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + hs * tm), tc::MODE_HH, 0,
+                        hs));
     }
   } else {
     float2* gf = reinterpret_cast<float2*>(c->G);
@@ -1746,16 +1775,17 @@ static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const dou
     if (rc) return rc;
   }
   float2* wf = reinterpret_cast<float2*>(c->G);
-  float2* gp = wf + 4 * tm;
-  float2* wx = wf + 5 * tm;
-  float2* vx = wf + 6 * tm;
   // stage buffers (FP32, 3 tot_mat each): the step-start state, then the stage states
   float2* x0 = reinterpret_cast<float2*>(c->xs);
   float2* xn = x0 + 3 * tm;
   for (Mixed* m : A->b) {
-    const int nk = m->nk, nw = m->nw;
+    const int nk = m->nk, nw = m->nw, hs = m->hs;
     const long long vn = (long long)nw * nk, o = m->bm;
     const float2 *P = xs + o, *C = xs + tm + o, *D = xs + 2 * tm + o;
+    // this bucket's slices of the G buffer (see bucket_jobs)
+    const float2* gp = wf + 2 * hs * tm;
+    const float2* wx = wf + (2 * hs + 1) * tm;
+    const float2* vx = wf + (2 * hs + 2) * tm;
     Rk4Ctl rk[3];
     for (int i = 0; i < 3; ++i) {
       rk[i] = Rk4Ctl{};
@@ -1773,10 +1803,10 @@ static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const dou
     const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
     k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp + o, A->hf + o, P, m->dgf, m->gamf, m->cdf, A->kf + o,
                               rk[0]);
-    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + o, wf + tm + o, wx + o, A->hf + tm + o, C, m->dgf,
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + o, hs, tm, wx + o, A->hf + tm + o, C, m->dgf,
                                  m->dgf + vn, m->cdf, m->cdf + vn, A->kf + tm + o, rk[1]);
-    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + 2 * tm + o, wf + 3 * tm + o, vx + o, A->hf + 2 * tm + o,
-                                 D, m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn,
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + hs * tm + o, hs, tm, vx + o, A->hf + 2 * tm + o, D,
+                                 m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn,
                                  m->cdf + 3 * vn, A->kf + 2 * tm + o, rk[2]);
   }
   return cuda_check(cudaGetLastError(), "mixed stage");

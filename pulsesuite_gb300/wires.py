@@ -333,13 +333,14 @@ class WireContext:
         return self.tiles()
 
     def tiles(self):
-        """Per bucket (Nk, wires, exchange tile, commutator tile, source tile)."""
-        cap = 5 * self.nw
+        """Per bucket (Nk, wires, exchange tile, commutator tile, source tile,
+        hi*hi split)."""
+        cap = 6 * self.nw
         out = (ctypes.c_int * cap)()
         nb = ctypes.c_int()
         _lib.check(self.lib.sbe_ctx_tiles(self.handle, out, cap, ctypes.byref(nb)),
                    "sbe_ctx_tiles")
-        return [tuple(out[5 * i:5 * i + 5]) for i in range(nb.value)]
+        return [tuple(out[6 * i:6 * i + 6]) for i in range(nb.value)]
 
     def check(self):
         """Wait for the current stream and raise if a device-side bounded wait gave up."""

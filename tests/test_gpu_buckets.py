@@ -199,7 +199,7 @@ def test_autotune_writes_loads_and_both_tiles_agree(tmp_path):
     entry = data["entries"][0]
     assert [(b["nk"], b["nw"]) for b in entry["buckets"]] == [t[:2] for t in tiles]
     for b, t in zip(entry["buckets"], tiles):
-        assert (b["exchange_bn"], b["commutator_bn"], b["sources_bn"]) == t[2:]
+        assert (b["exchange_bn"], b["commutator_bn"], b["sources_bn"], b["hh_split"]) == t[2:]
         assert all(v > 0 for k in ("exchange", "commutator", "sources") for v in b["ms"][k])
     _, (P, C, D) = _states(ctx, 4)
     Ek = fields(ctx, [2e7] * len(NKS))
@@ -209,7 +209,7 @@ def test_autotune_writes_loads_and_both_tiles_agree(tmp_path):
     for tile in (128, 256):
         _forced_cache(cache, ctx, tile)
         c2 = make_ctx()
-        assert all(t[2:] == (tile, tile, tile) for t in c2.autotune(cache))   # loaded, not timed
+        assert all(t[2:5] == (tile, tile, tile) for t in c2.autotune(cache))   # loaded, not timed
         rmx = c2.rhs(P, C, D, Ek, _lib.PREC_MIXED)
         c2.check()
         for a, b in zip(rmx, r64):
