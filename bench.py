@@ -212,6 +212,19 @@ def cpu_sweep_rate():
     return SWEEP["nw"] / total, per_nk
 
 
+def reference_timing():
+    """The reference's own pure-Python step (SBESolver + QWCalculator, Nk = 64 local
+    field) as timed by oracle/time_reference.py where the reference source is available
+    (it is not on the GPU host): the recorded figures with the host they come from."""
+    p = os.path.join(ROOT, "oracle", "reference_timing.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    d["note"] = "measured by oracle/time_reference.py on the host named here, not in this run"
+    return d
+
+
 def reference_arm(args, wl):
     rank, world, local = env()
     if rank != 0:
@@ -524,7 +537,8 @@ def gpu_arm(args, wl):
         cpu = {"value": 1.0 / ct[0], "unit": "wire-steps/s", "cores": os.cpu_count(),
                "kind": "port",
                "sample": f"one RK4 wire-step of one wire (Nk={nk}) of this workload, NumPy FP64 "
-                         "restatement (BLAS matmuls multi-threaded, O(Nk^3) sums single-threaded)"}
+                         "restatement (BLAS matmuls multi-threaded, O(Nk^3) sums single-threaded)",
+               "reference_python": reference_timing()}
 
     line_out = {"metric": METRIC, "value": value, "unit": "wire-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
