@@ -609,12 +609,12 @@ def sweep_arm(args):
     P, C, D = fresh()
     Ek0, dEk = ctx.zeros_r(3), ctx.zeros_r(3)
     src = ctx.zeros_r(5)
-    ctx.rk4_step(P.clone(), C.clone(), D.clone(), Ek0, dEk, dt, src.clone(), prec)
-    graph = ctx.rk4_graph(P, C, D, Ek0, dEk, dt, src, prec)
     for n in range(args.warmup):
         ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
-        graph.launch()
+        ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
     torch.cuda.synchronize()
+    # timed region: one step of all wires per step (direct calls, engine launches timed
+    # with events); the same step as a CUDA graph is timed after it
     ctx.profile(True)
     for cat in range(4):
         ctx.profile_read(cat)
@@ -628,7 +628,7 @@ def sweep_arm(args):
     ev0.record()
     for n in range(args.warmup, nsteps):
         ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
-        graph.launch()
+        ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -636,6 +636,17 @@ def sweep_arm(args):
     prof = {cat: ctx.profile_read(cat) for cat in range(4)}
     ctx.profile(False)
     ctx.check()
+    graph = ctx.rk4_graph(P, C, D, Ek0, dEk, dt, src, prec)
+    n_kernels = graph.kernels
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for n in range(args.warmup, nsteps):
+        ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
+        graph.launch()
+    g1.record()
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / args.steps
     if dist:
         tt = torch.tensor([ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -720,7 +731,9 @@ def sweep_arm(args):
                 "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
                         "h2d_bytes_per_step": int(2 * 8 * nw),
                         "d2h_bytes_per_step": int(src.numel() * 16)},
-                "gpu_launches_per_step": None,
+                "gpu_launches": int((n_kernels + 1) * args.steps),
+                "gpu_launches_per_step": int(n_kernels + 1),
+                "graph_replay_ms_per_step": graph_ms,
                 "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)",
                              "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                              "frac": achieved / peak,
@@ -757,11 +770,52 @@ def grid3_config():
             "l2": "inputs larger than L2 (FP64 wire state 3.2 GB, fields 403 MB)"}
 
 
+def grid3_field_arm(args):
+    """The 3-D field step alone on the 256 x 128 x 128 grid (FP32 transforms, a fixed
+    current): steps/s and achieved HBM GB/s (the case the FFT-pass profiles use)."""
+    import torch
+    import __graft_entry__ as ge
+    torch.cuda.set_device(env()[2])
+    ge.build()
+    from pulsesuite_gb300.pstd import Pstd3D
+    g3 = GRID3
+    n, d = g3["n"], g3["d"]
+    grid = Pstd3D(n, (d, d, d), MAT["epsr"], n_abc=g3["n_abc"], abc_strength=g3["abc"],
+                  fp32_work=args.precision == "mixed")
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    E = torch.randn((3,) + n, dtype=torch.complex128, device="cuda", generator=gen) * 1e6
+    H = torch.randn((3,) + n, dtype=torch.complex128, device="cuda", generator=gen) * 1e3
+    J = torch.randn((3,) + n, dtype=torch.complex128, device="cuda", generator=gen) * 1e9
+    dt = g3["dt"]
+    for _ in range(args.warmup):
+        grid.step(E, H, J, dt)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        grid.step(E, H, J, dt)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    peaks, pk_kind = measured_peaks()
+    N = n[0] * n[1] * n[2]
+    gbs = N * 240 / (ms / 1e3) / 1e9
+    print(json.dumps({"workload": "3-D field step alone, 256x128x128 x 20 nm, six c128 components",
+                      "precision": args.precision, "steps": args.steps, "ms_per_step": ms,
+                      "achieved_gbs": gbs, "peak_gbs": peaks.get("hbm_gbs"), "peak_kind": pk_kind,
+                      "frac": gbs / peaks.get("hbm_gbs", 6800.0),
+                      "bytes_model": "E, H read and written, J read: 240 B per point"}), flush=True)
+
+
 def grid3_arm(args):
     """Config 4: 64 wires of Nk = 1024 coupled to the 3-D grid; value = wire-steps/s of
     the coupled step (mixed path); the field step alone is timed for its HBM roofline."""
     import torch
     import __graft_entry__ as ge
+    if args.field_only:
+        grid3_field_arm(args)
+        return
     rank, world, local = env()
     dist = None
     if world > 1:
@@ -824,10 +878,8 @@ def grid3_arm(args):
 
     st = fresh()
     line.reset()
-    line.step(*st, dt, prec)
-    graph = line.graph(*st, dt, prec)
-    for _ in range(max(0, args.warmup - 1)):
-        graph.launch()
+    for _ in range(args.warmup):
+        line.step(*st, dt, prec)
     torch.cuda.synchronize()
     ctx.profile(True)
     for cat in range(4):
@@ -841,7 +893,7 @@ def grid3_arm(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
     for _ in range(args.steps):
-        graph.launch()
+        line.step(*st, dt, prec)
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -854,7 +906,16 @@ def grid3_arm(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     value = world * nw * args.steps / (ms / 1e3)
+    graph = line.graph(*st, dt, prec)
     n_kernels = graph.kernels
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(args.steps):
+        graph.launch()
+    g1.record()
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / args.steps
     graph.close()
 
     # end to end: the grid field E in from pinned host memory and the grid current J
@@ -930,6 +991,7 @@ def grid3_arm(args):
                 "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
                         "h2d_bytes_per_step": int(3 * N * 16), "d2h_bytes_per_step": int(3 * N * 16)},
                 "gpu_launches": int(n_kernels * args.steps), "gpu_launches_per_step": int(n_kernels),
+                "graph_replay_ms_per_step": graph_ms,
                 "roofline": {"bound": "hbm", "kernel": "3-D PSTD field step (FFT passes + curl + update)",
                              "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                              "frac": achieved_gbs / hbm, "peak_kind": f"{pk_kind} HBM copy",
@@ -959,6 +1021,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="multiwire", choices=sorted(WORKLOADS) + ["sweep", "grid3d"])
+    ap.add_argument("--field-only", action="store_true",
+                    help="grid3d: time the 3-D field step alone")
     ap.add_argument("--tile-cache", default=None,
                     help="JSON tile cache of the autotuner (default: in the temp directory)")
     ap.add_argument("--fp64-steps", type=int, default=3)

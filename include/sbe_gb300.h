@@ -290,7 +290,7 @@ int sbe_pstd_elong(SbePstd* p, const double* rho, const double* Px, double* Ex, 
  * fp32_work: the transforms between the first and last pass in FP32 (the fields
  * stay FP64).                                                                      */
 typedef struct {
-  int n[3];            /* nx, ny, nz: powers of two in [8, 1024]               */
+  int n[3];            /* nx, ny, nz: powers of two in [2, 1024]               */
   int n_abc[3];        /* absorbing cells at both ends of each axis            */
   int fp32_work;       /* 1: FP32 transforms, 0: FP64                          */
   int pad0;

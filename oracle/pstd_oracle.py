@@ -386,8 +386,8 @@ class CoupledGrid3:
         eks = self.sample(E)
         H = self.p.update_h(E, H, dt)
         srcs = []
-        z = [np.zeros_like(eks[0][0])] * 3
         for i, (wi, st) in enumerate(zip(self.wires, states)):
+            z = [np.zeros_like(eks[i][0])] * 3
             P, C, D, Px, Py, Pz, re, rh = wi.rk4_step(st[0], st[1], st[2], eks[i], z, dt,
                                                      self.windex[i])
             st[0], st[1], st[2] = P, C, D

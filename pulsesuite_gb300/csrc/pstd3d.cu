@@ -305,10 +305,12 @@ __global__ void k_tables3(int n, double d, double* x, double* q, double2* tw, fl
                           double* mask, int n_abc, double strength) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  // GetSpaceArray: numpy linspace(-L/2, L/2, n) with L = (n - 1) d (typespace.py:815-849)
+  // GetSpaceArray: numpy linspace(-L/2, L/2, n) with L = (n - 1) d (typespace.py:815-849):
+  // j * step + start, rounded as numpy does (no fused multiply-add), the last point = stop
   const double L = (n - 1) * d;
-  const double step = L / (n - 1);
-  x[j] = (j == n - 1) ? L / 2 : -L / 2 + j * step;
+  const double start = -L / 2, stop = L / 2;
+  const double step = (stop - start) / (double)(n - 1);
+  x[j] = (j == n - 1) ? stop : __dadd_rn(__dmul_rn((double)j, step), start);
   const double dq = 2.0 * kPi / (n * d);
   q[j] = (j <= n / 2 ? j : j - n) * dq;
   double s, c;
@@ -324,7 +326,7 @@ __global__ void k_tables3(int n, double d, double* x, double* q, double2* tw, fl
   mask[j] = m;
 }
 
-bool pow2(int v) { return v >= 8 && v <= 1024 && (v & (v - 1)) == 0; }
+bool pow2(int v) { return v >= 2 && v <= 1024 && (v & (v - 1)) == 0; }
 
 // tl lines per block within the shared-memory budget (two ping-pong buffers of nf
 // fields x n x tl elements), tl <= 8 and dividing inner
@@ -429,7 +431,7 @@ int sbe_pstd3_create(const SbePstd3Desc* d, void* stream, SbePstd3** out) {
   for (int a = 0; a < 3; ++a) {
     if (!pow2(d->n[a]))
       return fail(SBE_ERR_UNSUPPORTED, "sbe_pstd3_create: every axis must be a power of two in "
-                                       "[8, 1024]");
+                                       "[2, 1024]");
     if (!(d->d[a] > 0) || d->n_abc[a] < 0 || 2 * d->n_abc[a] > d->n[a])
       return fail(SBE_ERR_ARG, "sbe_pstd3_create: bad spacing or absorbing width");
   }

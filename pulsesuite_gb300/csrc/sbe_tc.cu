@@ -1213,9 +1213,13 @@ __device__ __forceinline__ float2 two_sum(float a, float b) {
 // for C and D, its real diagonal in FP64; stage 4 adds to the FP64 state.  The
 // maxima of the written state (all elements in mx, off-diagonal ones in mo when
 // peel) feed the next stage's exponents.  stage 0: no update (the RHS is stored).
+// The step's scale (dt / 2 or dt for the stage states, dt / 6 for the final sum)
+// enters as an unevaluated FP32 pair fh + fl: an FP32-rounded dt would be the same
+// relative error every step, i.e. a slightly different time step whose phase error
+// grows with the number of oscillation periods of the state.
 struct Rk4Ctl {
   int stage, peel;
-  float dt;
+  float fh, fl;
   double2* X;      // FP64 state of this matrix, all wires
   const float2* x0;  // FP32 copy of the step-start state (stages 1-3)
   float2* acc;     // RK4 sums
@@ -1228,7 +1232,6 @@ struct Rk4Ctl {
 __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, float2 kv, bool diag,
                                                long long dgi) {
   if (r.stage < 4) {
-    const float f = (r.stage == 1 || r.stage == 2) ? 0.5f * r.dt : r.dt;
     if (r.stage == 1) {
       r.acc[i] = kv;
     } else {
@@ -1236,16 +1239,17 @@ __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, flo
       r.acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
     }
     const float2 xs = r.x0[i];   // fp32 of the FP64 state, converted once per step
-    const float2 v = make_float2(xs.x + f * kv.x, xs.y + f * kv.y);
+    const float2 fk = make_float2(fmaf(r.fl, kv.x, r.fh * kv.x), fmaf(r.fl, kv.y, r.fh * kv.y));
+    const float2 v = make_float2(xs.x + fk.x, xs.y + fk.y);
     r.xf[i] = v;
-    if (diag && r.dg) r.dg[dgi] = r.X[i].x + f32_to_f64(f * kv.x);
+    if (diag && r.dg) r.dg[dgi] = r.X[i].x + f32_to_f64(fk.x);
     return max(__float_as_uint(v.x) & 0x7FFFFFFFu, __float_as_uint(v.y) & 0x7FFFFFFFu);
   }
   const double2 x = r.X[i];
   const float2 a = r.acc[i];
-  const float sc = r.dt / 6.f;
-  const double2 v = make_double2(x.x + f32_to_f64(sc * (a.x + kv.x)),
-                                 x.y + f32_to_f64(sc * (a.y + kv.y)));
+  const float sx = a.x + kv.x, sy = a.y + kv.y;
+  const double2 v = make_double2(x.x + f32_to_f64(fmaf(r.fl, sx, r.fh * sx)),
+                                 x.y + f32_to_f64(fmaf(r.fl, sy, r.fh * sy)));
   r.X[i] = v;
   return bits_to_fmax(max(absbits(v.x), absbits(v.y)));
 }
@@ -1588,10 +1592,12 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
     };
     if (kind == JK_FULL) {
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 4, tP, 0, epi(wf + 2 * hs * tm)));
+      // the cross terms of W and V with their lo*lo products
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + (2 * hs + 1) * tm),
                         tc::MODE_FULL, 1));
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + (2 * hs + 2) * tm),
                         tc::MODE_FULL, 1));
+      out[out.size() - 1].d.lolo = out[out.size() - 2].d.lolo = 1;
     } else {
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf), tc::MODE_HH, 0, hs));
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + hs * tm), tc::MODE_HH, 0,
@@ -1702,7 +1708,7 @@ static void mixed_state_in(SbeCtx* c, const double2* P, const double2* C, const 
 // element-wise passes (X64: the FP64 states P, C, D; the next stage state goes to
 // the FP32 stage buffer and its maxima to mxS, mxO); stage 0 stores the RHS in kf.
 static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const double2* dEk,
-                       double frac, int stage, float dt, double2* const* X64, cudaStream_t s) {
+                       double frac, int stage, double dt, double2* const* X64, cudaStream_t s) {
   MixedAll* A = all_of(c);
   const long long tm = c->tot_mat;
   const int have_x = (c->wires[0].flags & SBE_F_EXCITONS) ? 1 : 0;
@@ -1791,7 +1797,10 @@ static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const dou
       rk[i] = Rk4Ctl{};
       rk[i].stage = stage;
       rk[i].peel = i > 0;
-      rk[i].dt = dt;
+      // the stage scale as an exact FP32 pair (see Rk4Ctl)
+      const double f = stage == 4 ? dt / 6.0 : (stage == 3 ? dt : 0.5 * dt);
+      rk[i].fh = (float)f;
+      rk[i].fl = (float)(f - (double)rk[i].fh);
       rk[i].X = X64 ? X64[i] + o : nullptr;
       rk[i].x0 = x0 + i * tm + o;
       rk[i].acc = A->accf + i * tm + o;
@@ -1890,7 +1899,7 @@ int rk4_mixed(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek0,
   for (int st = 1; st <= 4; ++st) {
     // the RHS of this stage (stage field Ek0 + frac dEk) and its RK4 update (fused
     // into the element-wise passes)
-    rc = mixed_stage(c, st == 1 ? x0 : x0 + 3 * n, Ek0, dEk, frac[st - 1], st, (float)dt, X64, s);
+    rc = mixed_stage(c, st == 1 ? x0 : x0 + 3 * n, Ek0, dEk, frac[st - 1], st, dt, X64, s);
     if (rc) return rc;
   }
   mixed_relax(c, P, C, D, Ek0, dt, s);   // the new diagonals join the maximum

@@ -301,6 +301,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const bool hh = !d.xonly;
+      const bool lolo = d.lolo != 0;
       // a last N tile narrower than BNT (MODE_FULL): MMAs of N rounded up to 16
       const int nrem = d.N - ti.n0;
       const bool narrow = !HH && nrem < BNT;
@@ -367,6 +368,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               umma_f16(acc_im, A(1), B(2), iri, 1u);
               umma_f16(acc_im, A(2), B(1), iir, 1u);
               umma_f16(acc_im, A(3), B(0), iir, 1u);
+              if (lolo) {
+                umma_f16(acc_re, A(1), B(1), irr, 1u);
+                umma_f16(acc_re, A(3), B(3), iii, 1u);
+                umma_f16(acc_im, A(1), B(3), iri, 1u);
+                umma_f16(acc_im, A(3), B(1), iir, 1u);
+              }
             }
             first = false;
           }
@@ -537,7 +544,7 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
     if (!job_ok(d)) return fail(SBE_ERR_ARG, "tc_gemm: operand plane sets do not cover the launch");
     if (d.mode != mode || d.complex_mode != cplx || d.bn != bn)
       return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode and N tile");
-    if ((mode == tc::MODE_HH || d.xonly) && (!d.complex_mode || d.kskip))
+    if ((mode == tc::MODE_HH || d.xonly || d.lolo) && (!d.complex_mode || d.kskip))
       return fail(SBE_ERR_ARG, "tc_gemm: hi*hi and cross-term modes are complex and unskipped only");
     if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
     if (mode == tc::MODE_HH)

@@ -133,6 +133,10 @@ struct GemmDesc {
   // through xonly.
   int mode;
   int xonly;
+  // complex MODE_FULL: also the lo*lo products (hi*lo + lo*hi + lo*lo with xonly).  The
+  // lo*lo terms are 2^-22 of the product; W - W^H of dC, dD cancels most of W, so what
+  // W leaves out there shows in the result
+  int lolo;
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
   // written at out + ks * ks_stride (ksplit 0 counts as 1)
   int ksplit;

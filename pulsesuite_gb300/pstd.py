@@ -87,7 +87,7 @@ class Pstd1D:
 
 
 class Pstd3D:
-    """3-D grid of n = (nx, ny, nz) points (powers of two in [8, 1024]), cells
+    """3-D grid of n = (nx, ny, nz) points (powers of two in [2, 1024]), cells
     d = (dx, dy, dz), background epsr, absorbing layers of n_abc cells per axis; fields
     are caller-owned complex128 tensors of shape (3, nx, ny, nz): E = (Ex, Ey, Ez),
     H = (Hx, Hy, Hz).  ``fp32_work``: transforms between the first and last pass in

@@ -679,7 +679,7 @@ def case_pstd3d(seed):
     from pulsesuite.PSTD3D import rhoPJ, typespace, usefulsubs
     from pulsesuite.libpulsesuite import helpers
     rng = np.random.default_rng(seed)
-    nx, ny, nz = 8, 6, 10
+    nx, ny, nz = 8, 4, 16
     dx, dy, dz = 20e-9, 25e-9, 15e-9
     sp = typespace.ss(3, nx, ny, nz, dx, dy, dz, 12.9)
     qx, qy, qz = typespace.GetKxArray(sp), typespace.GetKyArray(sp), typespace.GetKzArray(sp)
