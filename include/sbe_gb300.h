@@ -158,11 +158,13 @@ int sbe_sources(SbeCtx* ctx, int w, const double* P, const double* C, const doub
                 double* re, double* rh, void* stream);
 /* qwoptics.py:667 Prop2QW: spline from the propagation grid RR (n_rr) to the wire
  * grid, window, real part, FFTG.  fields_in: 4 x c128 n_rr (Exx, Eyy, Ezz, Vrr);
- * out: 4 x c128 Nr.                                                           */
+ * out: 4 x c128 Nr.  The spline scratch (12 x c128 n_rr) is the context's: the
+ * first call and a call with a larger grid than any before allocate it (cudaMalloc;
+ * growing it waits for the device), other calls allocate nothing.              */
 int sbe_prop2qw(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* fields_in,
                 double* out, void* stream);
 /* qwoptics.py:717 QW2Prop (real-space sources in): 5 x c128 Nr (Px, Py, Pz, re, rh)
- * -> 5 x c128 n_rr (Pxx, Pyy, Pzz, RhoE, RhoH).                               */
+ * -> 5 x c128 n_rr (Pxx, Pyy, Pzz, RhoE, RhoH).  Scratch from the context's arena. */
 int sbe_qw2prop(SbeCtx* ctx, int w, const double* RR, int n_rr, const double* src_in,
                 double* out, int plasmonics, void* stream);
 

@@ -209,6 +209,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   }
   add((void**)&c->emis, D8 * std::max<size_t>(emis_host.size(), 1));
   add((void**)&c->G, C16 * 3 * okr);
+  add((void**)&c->qscr, C16 * (20 * (size_t)c->nr_max + 1));
   add((void**)&c->kacc, C16 * 3 * om);
   add((void**)&c->xs, C16 * 3 * om);
   add((void**)&c->scal, D8 * 16 * n_wires);
@@ -290,6 +291,7 @@ int sbe_ctx_destroy(SbeCtx* c) {
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->d_wires && cudaFree(c->d_wires) != cudaSuccess) rc = SBE_ERR_CUDA;
   if (c->arena && cudaFree(c->arena) != cudaSuccess) rc = SBE_ERR_CUDA;
+  if (c->p2q_coef && cudaFree(c->p2q_coef) != cudaSuccess) rc = SBE_ERR_CUDA;
   sbe::mixed_free(c);
   delete c;
   if (rc != SBE_OK) set_error("sbe_ctx_destroy: cudaFree failed");

@@ -47,6 +47,9 @@ struct SbeCtx {
   double2* dcs = nullptr;                // tot_vec DC transport shift kernel s(m) per wire
   double* emis = nullptr;                // emission tables (per wire emis_nw values)
   double2* G = nullptr;                  // 3*tot_kr source GEMM outputs
+  double2* qscr = nullptr;               // 20*nr_max + 1: Prop2QW / QW2Prop wire-grid scratch
+  double2* p2q_coef = nullptr;           // Prop2QW spline coefficients of the caller's grid
+  long long p2q_cap = 0;                 // (12 per grid point; grown on a larger grid)
   double2* kacc = nullptr;               // 3*tot_mat RK4 accumulator
   double2* xs = nullptr;                 // 3*tot_mat RK4 stage state
   double* scal = nullptr;                // 16*nw per-wire scalars

@@ -5,8 +5,9 @@
 // pool and must not allocate behind it (its allocations would fail or fragment the
 // pool), and real-time loops that must not call cudaMallocAsync / cudaFreeAsync
 // because those calls take the driver's allocator lock and may synchronise with
-// other streams of the process.  sbe_prop2qw allocates 12 n_rr + 4 Nr complex
-// values per call; this variant uses one fixed array instead.
+// other streams of the process.  sbe_prop2qw keeps 12 n_rr complex values of
+// spline scratch in its context, allocated (cudaMalloc) on its first call and again
+// whenever a larger grid comes; this variant uses one fixed array instead.
 //
 // Limits: n_rr <= SBE_NOALLOC_MAX_GRID (8192 propagation-grid points) and
 // Nr <= SBE_NOALLOC_MAX_NR (2050 wire points, Nk <= 1024).  Larger calls are

@@ -544,22 +544,24 @@ __global__ void k_fftg(int n, int nf, const double2* in, double2* out) {
   if (threadIdx.x == 0) out[(long long)f * n + q] = make_double2(-rr[0] / n, -ri[0] / n);
 }
 
+// Prop2QW on the context's scratch: the wire-grid part lives in the context's arena;
+// the spline coefficients of the caller's grid (12 per point) in a context buffer that
+// is allocated on the first call and grown only when a larger grid comes (cudaFree and
+// cudaMalloc then wait for the device's pending work); calls of one context are
+// ordered on its stream, so they share the scratch.
 int launch_prop2qw(SbeCtx* c, int w, const double* RR, int n_rr, const double2* fin,
                    double2* out, cudaStream_t s) {
-  const WireDev& W = c->wires[w];
-  double2* coef = nullptr;
-  double2* tmp = nullptr;
-  if (cudaMallocAsync(&coef, sizeof(double2) * 12 * (size_t)n_rr, s) != cudaSuccess ||
-      cudaMallocAsync(&tmp, sizeof(double2) * 4 * (size_t)W.nr, s) != cudaSuccess)
-    return fail(SBE_ERR_OOM, "prop2qw scratch");
-  k_spline_coef<<<1, 32, 0, s>>>(n_rr, RR, fin, 4, coef);
-  k_spline_eval<<<dim3((W.nr + 127) / 128, 4), 128, 0, s>>>(n_rr, RR, fin, coef, W.nr,
-                                                           c->r + W.off_r, 4,
-                                                           c->window + W.off_r, 1, tmp);
-  k_fftg<<<dim3(W.nr, 4), 128, 0, s>>>(W.nr, 4, tmp, out);
-  cudaFreeAsync(coef, s);
-  cudaFreeAsync(tmp, s);
-  return cuda_check(cudaGetLastError(), "prop2qw");
+  const long long need = 12LL * n_rr;
+  if (need > c->p2q_cap) {
+    if (c->p2q_coef && cudaFree(c->p2q_coef) != cudaSuccess)
+      return cuda_check(cudaGetLastError(), "prop2qw: release the smaller scratch");
+    c->p2q_coef = nullptr;
+    c->p2q_cap = 0;
+    if (cudaMalloc(&c->p2q_coef, sizeof(double2) * need) != cudaSuccess)
+      return fail(SBE_ERR_OOM, "prop2qw scratch");
+    c->p2q_cap = need;
+  }
+  return launch_prop2qw_scratch(c, w, RR, n_rr, fin, out, c->p2q_coef, c->qscr, s);
 }
 
 // The same three launches as launch_prop2qw on scratch the caller provides:
@@ -616,14 +618,11 @@ __global__ void k_plasmonics(int n, const double* grid, double2* a, double2* b, 
 
 int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* src,
                    double2* out, int plasmonics, cudaStream_t s) {
+  // scratch in the context's arena (15 + 5 wire-grid columns and the total)
   const WireDev& W = c->wires[w];
-  double2* coef = nullptr;
-  double2* tmp = nullptr;
-  double* total = nullptr;
-  if (cudaMallocAsync(&coef, sizeof(double2) * 15 * (size_t)W.nr, s) != cudaSuccess ||
-      cudaMallocAsync(&tmp, sizeof(double2) * 5 * (size_t)W.nr, s) != cudaSuccess ||
-      cudaMallocAsync(&total, sizeof(double), s) != cudaSuccess)
-    return fail(SBE_ERR_OOM, "qw2prop scratch");
+  double2* coef = c->qscr;
+  double2* tmp = coef + 15 * (size_t)c->nr_max;
+  double* total = reinterpret_cast<double*>(tmp + 5 * (size_t)c->nr_max);
   cudaMemcpyAsync(tmp, src, sizeof(double2) * 5 * (size_t)W.nr, cudaMemcpyDeviceToDevice, s);
   const double* rw = c->r + W.off_r;
   if (plasmonics)
@@ -634,9 +633,6 @@ int launch_qw2prop(SbeCtx* c, int w, const double* RR, int n_rr, const double2* 
   if (plasmonics)
     k_plasmonics<<<1, 256, 0, s>>>(n_rr, RR, out + 3 * (size_t)n_rr, out + 4 * (size_t)n_rr,
                                    total, 1);
-  cudaFreeAsync(coef, s);
-  cudaFreeAsync(tmp, s);
-  cudaFreeAsync(total, s);
   return cuda_check(cudaGetLastError(), "qw2prop");
 }
 

@@ -89,6 +89,14 @@ class _DefaultPool:
         assert self.cu.cuMemPoolGetAttribute(self.pool, attr, ctypes.byref(v)) == 0
         return v.value
 
+    def probe_allocation(self, nbytes=1 << 20):
+        """One stream-ordered allocation from the default pool and its release (what
+        the check must be able to see)."""
+        ptr = ctypes.c_uint64()
+        assert self.cu.cuMemAllocAsync(ctypes.byref(ptr), ctypes.c_size_t(nbytes), None) == 0
+        assert self.cu.cuMemFreeAsync(ptr, None) == 0
+        assert self.cu.cuStreamSynchronize(None) == 0
+
     def reset_high(self):
         zero = ctypes.c_uint64(0)
         assert self.cu.cuMemPoolSetAttribute(self.pool, self.USED_MEM_HIGH,
@@ -99,8 +107,8 @@ class _DefaultPool:
 def test_noalloc_allocates_nothing_and_covers_its_largest_wire():
     """Nk = 1024 (Nr = 2050, the scratch limit) on the largest grid: equal to
     sbe_prop2qw, while the default pool's high-water mark and the free device memory
-    stay where they were; the allocating entry point moves the mark (so the check can
-    see an allocation)."""
+    stay where they were; a stream-ordered allocation moves the mark (so the check can
+    see one)."""
     torch = pytest.importorskip("torch")
     from pulsesuite_gb300.wires import WireContext, WireSpec
     spec = WireSpec(nk=1024, L=np.pi / (3e9 / 511.5), wire_index=1)
@@ -122,9 +130,10 @@ def test_noalloc_allocates_nothing_and_covers_its_largest_wire():
     torch.cuda.synchronize()
     assert pool.get(_DefaultPool.USED_MEM_HIGH) <= used0
     assert torch.cuda.mem_get_info()[0] == free0
+    pool.probe_allocation()
+    assert pool.get(_DefaultPool.USED_MEM_HIGH) > used0
     _call(lib, "sbe_prop2qw", ctx, 0, RR, f4, ref)
     torch.cuda.synchronize()
-    assert pool.get(_DefaultPool.USED_MEM_HIGH) > used0
     r = ref.cpu().numpy()
     assert np.abs(r).max() > 0
     for out in outs:
