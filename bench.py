@@ -416,6 +416,8 @@ def gpu_arm(args, wl):
     prof = {cat: ctx.profile_read(cat) for cat in range(4)}
     ctx.profile(False)
     ctx.check()
+    # the FP64 conservation check of the last timed step (read after the timed region)
+    charge_imb = ctx.charge_imbalance()
     value = world * nw * args.steps / (ms / 1e3)
 
     # CUDA graph of the same coupled step (launch count, replay time)
@@ -557,6 +559,9 @@ def gpu_arm(args, wl):
                              "steps": n64},
                 "speedup_vs_fp64_gpu": (value / fp64_val) if fp64_val else None,
                 "rhs_rel_err_vs_fp64": rhs_err,
+                "charge_imbalance": {"value": charge_imb,
+                                     "what": "max over wires of |N_e - N_h| / mean found by the "
+                                             "FP64 charge normalisation of the last timed step"},
                 "wire_field_peak_k": field_peak,
                 "cpu_baseline": cpu}
     print(json.dumps(line_out), flush=True)

@@ -238,9 +238,10 @@ int sbe_graph_destroy(SbeGraph* g);
  * the JSON file cache_json (NULL: no cache) under a key of the device and the
  * context's (Nk, wires) buckets: a later call with a matching entry loads it and
  * times nothing.  Without a call every GEMM uses the 256 tile.  Synchronises the
- * device; not capturable.  A cache entry may also set "hh_split" (1-4, default 2):
- * the K parts of the hi*hi products of the anti-Hermitian W, V (shorter truncating
- * FP32 chains: accuracy, not speed, so the tuner records it but does not time it).
+ * device; not capturable.  A cache entry may also set "hh_split" (1-4; default 2
+ * below Nk = 512, else 4): the K parts of the hi*hi products of the anti-Hermitian
+ * W, V (shorter truncating FP32 chains: accuracy, not speed, so the tuner records
+ * it but does not time it).
  * sbe_ctx_tiles: per bucket (ascending Nk) 6 ints (Nk, wires, exchange tile,
  * commutator tile, source tile, hi*hi split) into out (cap ints); *nbuckets = 0
  * before the mixed workspace exists.                                            */
@@ -410,6 +411,15 @@ int sbe_couple3_graph_create(SbeCouple3* cp, double* P, double* C, double* D, do
  * category and clears it.                                                      */
 int sbe_ctx_profile(SbeCtx* ctx, int enable);
 int sbe_ctx_profile_read(SbeCtx* ctx, int category, double* total_ms, long long* launches);
+
+/* ---- carrier-number balance (the FP64 conservation check) ------------------- */
+/* The charge normalisation of every step (SBEs.py:5692-5702: ne, nh scaled to
+ * their common mean) records, per wire, the carrier numbers it found:
+ * out[2w] = sum_k |C_kk|, out[2w + 1] = sum_k |D_kk| after the relaxation and
+ * before the normalisation of the last step (FP64; zeros before the first step).
+ * |out[2w] - out[2w+1]| / mean is the electron-hole imbalance that step produced.
+ * out: host or device memory, 2 * n_wires doubles; waits for the stream.       */
+int sbe_ctx_charge(SbeCtx* ctx, double* out, void* stream);
 
 /* ---- device-side error flags (no counterpart in the reference) ------------- */
 /* Waits for the stream, then reports whether a bounded wait of the tensor-core

@@ -1320,6 +1320,8 @@ class Wire:
                        for X in (C, D, P)]
         ne3 = np.abs(np.diag(C)).astype(complex)
         nh3 = np.abs(np.diag(D)).astype(complex)
+        # carrier numbers before the normalisation (the library's charge record)
+        self.last_charge = (float(np.sum(np.abs(ne3))), float(np.sum(np.abs(nh3))))
         total = (np.sum(np.abs(ne3)) + np.sum(np.abs(nh3))) / 2.0
         ne3 = ne3 * total / (np.sum(np.abs(ne3)) + SMALL)
         nh3 = nh3 * total / (np.sum(np.abs(nh3)) + SMALL)

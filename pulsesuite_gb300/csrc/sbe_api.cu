@@ -213,6 +213,7 @@ int sbe_ctx_create(const SbeWireDesc* wires, int n_wires, void* stream, SbeCtx**
   add((void**)&c->kacc, C16 * 3 * om);
   add((void**)&c->xs, C16 * 3 * om);
   add((void**)&c->scal, D8 * 16 * n_wires);
+  add((void**)&c->charge, D8 * 2 * n_wires);
   add((void**)&c->ekst, C16 * 3 * orr);
   add((void**)&c->occf, 4 * 2 * ov);
   add((void**)&c->dconst, 4 * 16 * (size_t)n_wires);
@@ -844,6 +845,17 @@ int sbe_ctx_profile_read(SbeCtx* c, int category, double* total_ms, long long* l
   if (launches) *launches = (long long)c->prof_ev[category].size();
   c->prof_ev[category].clear();
   return SBE_OK;
+}
+
+// ---- charge balance ---------------------------------------------------------
+int sbe_ctx_charge(SbeCtx* c, double* out, void* stream) {
+  if (!c || !out) return fail(SBE_ERR_ARG, "sbe_ctx_charge: null argument");
+  cudaStream_t s = as_stream(stream);
+  int rc = cuda_check(cudaMemcpyAsync(out, c->charge, sizeof(double) * 2 * c->nw,
+                                      cudaMemcpyDefault, s),
+                      "sbe_ctx_charge: copy");
+  if (rc) return rc;
+  return cuda_check(cudaStreamSynchronize(s), "sbe_ctx_charge");
 }
 
 }  // extern "C"

@@ -53,6 +53,7 @@ struct SbeCtx {
   double2* kacc = nullptr;               // 3*tot_mat RK4 accumulator
   double2* xs = nullptr;                 // 3*tot_mat RK4 stage state
   double* scal = nullptr;                // 16*nw per-wire scalars
+  double* charge = nullptr;              // 2*nw sum |C_kk|, sum |D_kk| before the last normalisation
   double2* ekst = nullptr;               // 3*tot_r stage field
   float* occf = nullptr;                 // 2*tot_vec |ne|, |nh| in FP32
   float* dconst = nullptr;               // 16*nw FP32 dephasing constants

@@ -105,7 +105,7 @@ __device__ __forceinline__ double2 cexp_d(double2 z) {
 // diagonals back into C3, D3); 2: normalisation only.
 __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, const double* wrate,
                              const double* rsp, double dt, double2* ne_out, double2* nh_out,
-                             int mode) {
+                             double* charge, int mode) {
   const WireDev W = wires[blockIdx.x];
   const int nk = W.nk;
   const bool relax = mode != 2 && (W.flags & (SBE_F_PHONON | SBE_F_EHS)) != 0;
@@ -159,6 +159,12 @@ __global__ void k_relax_norm(const WireDev* wires, double2* C3, double2* D3, con
     __syncthreads();
   }
   double sum_e = red[0][0], sum_h = red[1][0];
+  if (threadIdx.x == 0) {
+    // the carrier numbers before the normalisation: their difference is what this
+    // step's relaxation and rounding left of the electron-hole balance
+    charge[2 * blockIdx.x] = sum_e;
+    charge[2 * blockIdx.x + 1] = sum_h;
+  }
   double total = (sum_e + sum_h) / 2.0;
   double fe = total / (sum_e + kSmall), fh = total / (sum_h + kSmall);
   for (int k = threadIdx.x; k < nk; k += blockDim.x) {
@@ -186,12 +192,14 @@ void launch_relax_only(SbeCtx* c, double2* P3, double2* C3, double2* D3, const d
                        double dt, cudaStream_t s) {
   if (!any_dc(c)) {
     k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh,
-                                       0);
+                                       c->charge, 0);
     return;
   }
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh, 1);
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh,
+                                     c->charge, 1);
   launch_dc_transport(c, P3, C3, D3, Ek, dt, s);
-  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh, 2);
+  k_relax_norm<<<c->nw, 256, 0, s>>>(c->d_wires, C3, D3, c->wrate, c->rsp, dt, c->ne, c->nh,
+                                     c->charge, 2);
 }
 
 void launch_phonon_rates_one(SbeCtx* c, int w, cudaStream_t s) {

@@ -459,6 +459,9 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
     m->bv = W0.off_vec;
     m->br = W0.off_r;
     m->bkr = W0.off_kr;
+    // four K parts from Nk = 512 on: the hi*hi chains of 512 and more long K ranges
+    // set the truncation error of W - W^H (the autotuner's cache may override)
+    m->hs = W0.nk >= 512 ? 4 : 2;
     A->b.push_back(m);
     i = j;
   }
@@ -1340,7 +1343,9 @@ __global__ void __launch_bounds__(256) k_antiherm(
     }
   }
   __syncthreads();
-  const float ih = (float)(1.0 / kHbar);
+  // 1 / hbar as an FP32 pair: one FP32 constant is 1e-8 off, a fixed relative error
+  // of every rotation frequency that adds up over a pulse
+  const float ihh = (float)(1.0 / kHbar), ihl = (float)(1.0 / kHbar - (double)ihh);
   unsigned mxv = 0, mov = 0;
   // the tile (i0.., j0..): i <= j wherever it is written
   {
@@ -1378,7 +1383,7 @@ __global__ void __launch_bounds__(256) k_antiherm(
                        ((dh.x * x[q].x - di * x[q].y) + drl * x[q].x);
       const float im = (a.y + bt.y) + dc * hji.y +
                        ((dh.x * x[q].y + di * x[q].x) + drl * x[q].y);
-      const float2 v = make_float2(im * ih, -re * ih);
+      const float2 v = make_float2(fmaf(im, ihl, im * ihh), -fmaf(re, ihl, re * ihh));
       vt[r][tx] = v;
       if (i < nk && j < nk && (bi < bj || j >= i)) {
         const long long o = mb + (long long)i * nk + j;
@@ -1457,7 +1462,8 @@ __global__ void __launch_bounds__(256) k_rhs_p(
   __syncthreads();
   const int n = n0 + tx;
   const bool on = n < nk;
-  const float ih = (float)(1.0 / kHbar);
+  // 1 / hbar as an FP32 pair (the rotation frequency of P to FP32 precision)
+  const float ihh = (float)(1.0 / kHbar), ihl = (float)(1.0 / kHbar - (double)ihh);
   unsigned mxv = 0, mov = 0;
   const long long vnn = vb + (on ? n : 0);
   const float2 eh = dgf[vnn], el = dgf[vn + vnn];
@@ -1485,7 +1491,8 @@ __global__ void __launch_bounds__(256) k_rhs_p(
     const float ar = ax + ((sh.x * x[q].x - dei * x[q].y) + derl * x[q].x);
     const float ai = ay + ((sh.x * x[q].y + dei * x[q].x) + derl * x[q].y);
     const float gam = gamE + rv[0][r];
-    const float2 kv = make_float2(ai * ih - gam * x[q].x, -ar * ih - gam * x[q].y);
+    const float2 kv = make_float2(fmaf(ai, ihl, ai * ihh) - gam * x[q].x,
+                                  -fmaf(ar, ihl, ar * ihh) - gam * x[q].y);
     const long long o = mb + (long long)m * nk + n;
     if (rk.stage == 0) {
       out[o] = kv;

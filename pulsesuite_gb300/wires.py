@@ -346,6 +346,22 @@ class WireContext:
         """Wait for the current stream and raise if a device-side bounded wait gave up."""
         _lib.check(self.lib.sbe_ctx_check(self.handle, _lib.stream_handle()), "sbe_ctx_check")
 
+    def charge(self):
+        """(n_wires, 2) carrier numbers sum |C_kk|, sum |D_kk| that the charge
+        normalisation of the last step found (FP64, before it rescaled them)."""
+        out = torch.zeros(len(self.specs), 2, dtype=torch.float64)
+        _lib.check(self.lib.sbe_ctx_charge(self.handle, ctypes.c_void_p(out.data_ptr()),
+                                           _lib.stream_handle()), "sbe_ctx_charge")
+        return out
+
+    def charge_imbalance(self):
+        """max over wires of |N_e - N_h| / ((N_e + N_h) / 2) before the last step's
+        normalisation (0 for wires without carriers)."""
+        q = self.charge()
+        mean = 0.5 * (q[:, 0] + q[:, 1])
+        r = (q[:, 0] - q[:, 1]).abs() / torch.where(mean > 0, mean, torch.ones_like(mean))
+        return float(r.max()) if len(r) else 0.0
+
     def profile(self, enable=True):
         _lib.check(self.lib.sbe_ctx_profile(self.handle, int(bool(enable))), "sbe_ctx_profile")
 

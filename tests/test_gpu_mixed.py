@@ -158,10 +158,12 @@ def test_mixed_rk4_pulse_vs_fp64(nk, ehs):
             Ek0 = fields(ctx, [e0, 0.5 * e0])
             dEk = fields(ctx, [e1 - e0, 0.5 * (e1 - e0)])
             ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
-        states[prec] = (P, C, D, src)
+        states[prec] = (P, C, D, src, ctx.charge())
     ctx.check()
-    P64, C64, D64, s64 = states[_lib.PREC_FP64]
-    Pm, Cm, Dm, sm = states[_lib.PREC_MIXED]
+    P64, C64, D64, s64, q64 = states[_lib.PREC_FP64]
+    Pm, Cm, Dm, sm, qm = states[_lib.PREC_MIXED]
+    # the FP64 conservation check of the last step sees the same carrier numbers
+    assert rel(qm, q64) < 1e-5
     for w in range(nw):
         ne64 = ctx.mat(C64, w).diagonal()
         nem = ctx.mat(Cm, w).diagonal()

@@ -314,11 +314,17 @@ def test_batched_rhs_and_rk4_vs_oracle(nk):
     dt = 0.1e-15
     src = c.zeros_r(5)
     c.rk4_step(P, C, D, Ek, dEk, dt, src)
+    charge = c.charge().numpy()
     for w in range(nw):
         ref = wires[w].rk4_step(*states[w], fields[w], dfields[w], dt, w + 1)
         assert rel(host(c.mat(P, w)), ref[0]) < SCREEN
         assert rel(host(c.mat(C, w)), ref[1]) < SCREEN
         assert rel(host(c.mat(D, w)), ref[2]) < SCREEN
+        # the conservation record: carrier numbers before the normalisation, and the
+        # normalised diagonals summing to their mean
+        assert rel(charge[w], np.array(wires[w].last_charge)) < SCREEN
+        ne = np.abs(np.diag(host(c.mat(C, w)))).sum()
+        assert abs(ne - charge[w].mean()) <= 1e-12 * ne
         s5 = host(c.rvec(src, w, 5))
         for i in range(5):
             assert rel(O.fftg(s5[i]), ref[3 + i]) < SCREEN, (w, i)

@@ -160,7 +160,7 @@ def _grid3_setup(nks, wxy, fp32=False):
     Ls = [np.pi / (3e9 / (nk / 2 - 0.5)) for nk in nks]
     ctx = WireContext([WireSpec(nk=nk, L=L, temp=300.0, wire_index=w + 1, flags=dict(ALL), **MAT)
                        for w, (nk, L) in enumerate(zip(nks, Ls))])
-    ows = [O.Wire(nk, L, MAT, ALL) for nk, L in zip(nks, Ls)]
+    ows = [O.Wire(nk, L, MAT, ALL, temp=300.0) for nk, L in zip(nks, Ls)]
     g = Pstd3D(n, d, epsr, n_abc=(3, 3, 4), abc_strength=0.05, fp32_work=fp32)
     o = PO.Pstd3D(n, d, epsr, n_abc=(3, 3, 4), strength=0.05)
     w0 = (1.52 + 0.02) * O.E0 / O.HBAR
