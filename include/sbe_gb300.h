@@ -143,6 +143,18 @@ int sbe_spont_emission(SbeCtx* ctx, int w, const double* ne, const double* nh, c
  * and Re Px, Py, Pz [Nr/2].                                                     */
 int sbe_wire_info(SbeCtx* ctx, int w, const double* C2, const double* D2, const double* src,
                   const double* Ek, const double* VC, double* out23, void* stream);
+/* SBEs.py:5924-5978 PdotE.w.dat, the wire-grid term of the reference's EPEnergyW:
+ * *out (device) = sum_{c = x,y,z} sum_r (Re P_c(r) - P0_c(r)) Re E_c(r) with P_c the
+ * packed real-space sources src (5 x c128 Nr per wire), E_c = iFFTG of the packed
+ * wire-k field Ek (3 x c128 Nr per wire; usefulsubs.py:2271, the QW2Prop
+ * transform of qwoptics.py:775) and P0 (f64 3 x Nr, the caller's history of Re P;
+ * NULL: zeros).  The caller applies 0.5 dr area and accumulates.              */
+int sbe_wire_pdote(SbeCtx* ctx, int w, const double* Ek, const double* src, const double* P0,
+                   double* out, void* stream);
+/* dephasing.py:731-740 (MaxOffDiag.e.dat / .h.dat): out4 (device) = max Re De,
+ * min Re De, max Re Dh, min Re Dh of wire w's off-diagonal dephasing matrices
+ * ([2Nk+1][Nk]) of the last preparation (either path).                        */
+int sbe_deph_extrema(SbeCtx* ctx, int w, double* out4, void* stream);
 /* coulomb.py:1298/1313 MBCE/MBCH (carrier-carrier scattering, EHs; tables of
  * CalcMBArrays, coulomb.py:367, evaluated on the fly, Lorentzian broadening with
  * SBE_F_LORENTZ in the wire's flags, else Gaussian): Win/Wout accumulated in place.

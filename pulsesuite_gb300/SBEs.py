@@ -14,8 +14,11 @@ The names, arguments and in-place/return conventions follow the reference
 
 Arrays may be NumPy (host; results come back as NumPy) or CUDA torch tensors
 (results stay on the device).  All arithmetic runs in libsbe_gb300 on the GPU;
-there is no CPU path.  Text diagnostics the reference appends every step
-(dataQW/info.*.t.dat, EP.*.t.dat, output/PdotE.*.dat) are not written.
+there is no CPU path.  With ``write_info`` (on, as in the reference) the solver
+appends the reference's per-step text diagnostics: dataQW/info.WW.t.dat and
+EP.WW.t.dat (SBEs.py:5769-5809), output/PdotE.p.dat and PdotE.w.dat
+(SBEs.py:5924-5975) and dataQW/Wire/info/MaxOffDiag.e.dat and .h.dat
+(dephasing.py:538-539, 731-740); the statistics are reduced on the device.
 """
 
 import os
@@ -217,6 +220,15 @@ class SBESolver:
                 self._st[w][i].diagonal().copy_(d)
         self.rr_offset = np.asarray(rr) - r0
         self._rr_dev = None
+        # PdotE bookkeeping (SBEs.py:5924-5975): one history of the last two calls'
+        # Re P on both grids, shared by all wires as in the reference
+        self._pde = None
+        self._fld = [None] * Nw
+        if self.OffDiagDph and self.write_info:
+            # InitializeDephasing opens (truncates) both files (dephasing.py:537-539)
+            os.makedirs("dataQW/Wire/info", exist_ok=True)
+            for sp in ("e", "h"):
+                open(f"dataQW/Wire/info/MaxOffDiag.{sp}.dat", "w", encoding="utf-8").close()
 
     # reference-shaped state views (Nk, Nk, Nw), copied from/to the GPU
     def _get_level(self, i):
@@ -277,10 +289,13 @@ class SBESolver:
         out = ctx.qw2prop(0, RR, src, self.LF).cpu().numpy()
         if self.write_info:
             self._write_info(ctx, w, dt, src, Ek3)
+            self._write_maxoffdiag(ctx, 0)
         Pxx[:] = out[0]
         Pyy[:] = out[1]
         Pzz[:] = out[2]
         Rho[:] = out[4] - out[3]
+        if self.write_info:
+            self._pdote(ctx, 0, (Exx, Eyy, Ezz), (Pxx, Pyy, Pzz), rr, Ek3, src)
         if getattr(self, "ignorewire", False):
             Pxx[:] = 0.0
             Pyy[:] = 0.0
@@ -294,6 +309,8 @@ class SBESolver:
         Ek = ctx.prop2qw(w - 1, RR, f4)
         ctx.rvec(self._ek, w - 1, 3).copy_(Ek[:3])
         self._outs[w - 1] = outs
+        self._fld[w - 1] = (f4[0].real.cpu().numpy(), f4[1].real.cpu().numpy(),
+                            f4[2].real.cpu().numpy(), RR.cpu().numpy())
         if w != self.Nw:
             return
         ctx.leapfrog_step(self._lev, self._ek, dt, self._src)
@@ -305,6 +322,10 @@ class SBESolver:
             out = ctx.qw2prop(wi, RR, src, self.LF).cpu().numpy()
             if self.write_info:
                 self._write_info(ctx, wi + 1, dt, None, None)
+                self._write_maxoffdiag(ctx, wi)
+                ex, ey, ez, rr = self._fld[wi]
+                self._pdote(ctx, wi, (ex, ey, ez), (out[0], out[1], out[2]), rr, self._ek,
+                            self._src)
             ign = getattr(self, "ignorewire", False)
             o[0][:] = 0.0 if ign else out[0]
             o[1][:] = 0.0 if ign else out[1]
@@ -329,6 +350,44 @@ class SBESolver:
             f.write("".join(f"{x:18.6e} " for x in info[:-1]) + f"{info[-1]:18.6e}\n")
         with open(f"dataQW/EP.{w:02d}.t.dat", "a", encoding="utf-8") as f:
             f.write(" ".join(f"{x:18.6e}" for x in [t] + [float(x) for x in v[17:23]]) + "\n")
+
+    def _write_maxoffdiag(self, ctx, wc):
+        """dephasing.py:731-740: one line per preparation, t and the extrema of Re De
+        (MaxOffDiag.e.dat) and Re Dh (MaxOffDiag.h.dat) of the wire just stepped."""
+        if not self.OffDiagDph:
+            return
+        v = ctx.deph_extrema(wc)
+        for sp, mx, mn in (("e", v[0], v[1]), ("h", v[2], v[3])):
+            with open(f"dataQW/Wire/info/MaxOffDiag.{sp}.dat", "a", encoding="utf-8") as f:
+                f.write(f"{float(self.t)!r} {float(mx)!r} {float(mn)!r}\n")
+
+    def _pdote(self, ctx, wc, E3, P3, rr, Ek, src):
+        """SBEs.py:5924-5975: accumulate P.E on the propagation grid (host arrays of
+        this call) and on the wire grid (sbe_wire_pdote on the device), shift the
+        two-call history, append t and the energies / e0 to output/PdotE.{p,w}.dat."""
+        nrr, nr = len(P3[0]), self.Nr
+        if self._pde is None:
+            os.makedirs("output", exist_ok=True)
+            for sp in ("p", "w"):
+                open(f"output/PdotE.{sp}.dat", "w", encoding="utf-8").close()
+            z = np.zeros((3, nrr))
+            self._pde = dict(p0=z.copy(), p1=z.copy(), ep=0.0, epw=0.0,
+                             w0=torch.zeros((3, nr), dtype=torch.float64, device="cuda"),
+                             w1=torch.zeros((3, nr), dtype=torch.float64, device="cuda"))
+        h = self._pde
+        rr = np.asarray(rr)
+        drr = rr[1] - rr[0] if len(rr) > 1 else 1.0
+        inc = 0.0
+        for c in range(3):
+            inc = inc + np.sum((np.real(P3[c]) - h["p0"][c]) * np.real(E3[c]) * 0.5) * drr * self.area
+        h["ep"] += inc
+        h["epw"] += ctx.wire_pdote(wc, Ek, src, h["w0"]) * 0.5 * self.dr * self.area
+        h["p0"], h["p1"] = h["p1"], np.stack([np.real(np.asarray(p)) for p in P3])
+        h["w0"], h["w1"] = h["w1"], ctx.rvec(src.reshape(-1), wc, 5)[:3].real.contiguous()
+        with open("output/PdotE.p.dat", "a", encoding="utf-8") as f:
+            f.write(f"{float(self.t)!r} {float(h['ep'] / E0)!r}\n")
+        with open("output/PdotE.w.dat", "a", encoding="utf-8") as f:
+            f.write(f"{float(self.t)!r} {float(h['epw'] / E0)!r}\n")
 
     def write_sbes_data(self, n):
         """SBEs.py:5524-5546: dataQW/backup/{CC,DD,YY}{1,2,3}.n.dat, 're im' per line

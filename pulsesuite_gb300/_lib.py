@@ -38,7 +38,8 @@ EXPORTS = (
     "sbe_couple_destroy", "sbe_couple_buffers", "sbe_couple_set_step", "sbe_couple_reset",
     "sbe_couple_sample",
     "sbe_couple_deposit", "sbe_couple_step", "sbe_couple_graph_create",
-    "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info", "sbe_calc_jfx",
+    "sbe_backup_format", "sbe_backup_parse", "sbe_wire_info", "sbe_wire_pdote",
+    "sbe_deph_extrema", "sbe_calc_jfx",
     "sbe_qw_placement", "sbe_e_at_xyz", "sbe_autotune", "sbe_ctx_tiles",
     "sbe_local_field", "sbe_pstd3_create", "sbe_pstd3_destroy", "sbe_pstd3_grid",
     "sbe_pstd3_curl", "sbe_pstd3_update_h", "sbe_pstd3_update_e", "sbe_pstd3_step",
@@ -122,6 +123,8 @@ def load(path=LIB_PATH):
         "sbe_carrier_rates": [P, I, P, P, P, P, P, P, P, I, P],
         "sbe_spont_emission": [P, I, P, P, P, P, P],
         "sbe_wire_info": [P, I, P, P, P, P, P, P, P],
+        "sbe_wire_pdote": [P, I, P, P, P, P, P],
+        "sbe_deph_extrema": [P, I, P, P],
         "sbe_calc_jfx": [ctypes.c_longlong, P, P, Dbl, Dbl, P, P],
         "sbe_qw_placement": [I, I, I, P, P, P, P, P, P],
         "sbe_e_at_xyz": [P, P, I, P, I, P, I, P, I, P, P],

@@ -1144,13 +1144,18 @@ int sbe_couple3_step(SbeCouple3* cp, double* P, double* C, double* D, double* E,
   if (!P || !C || !D || !E || !H) return fail(SBE_ERR_ARG, "sbe_couple3_step: null");
   cudaStream_t s = as_stream(stream);
   if ((rc = c3_sample(cp, reinterpret_cast<const double2*>(E), precision, s))) return rc;
-  if ((rc = sbe_pstd3_update_h(cp->p, E, H, dt, stream))) return rc;
+  // the H half-step leaves the transform of the new H for the E half-step (the wire
+  // step and the deposit in between do not touch the field grid's work array)
+  if ((rc = pstd3_update_h_fwd(cp->p, reinterpret_cast<const double2*>(E),
+                               reinterpret_cast<double2*>(H), dt, s)))
+    return rc;
   if ((rc = sbe_rk4_step(cp->ctx, P, C, D, reinterpret_cast<double*>(cp->Ek),
                          reinterpret_cast<double*>(cp->dEk), dt, precision,
                          reinterpret_cast<double*>(cp->src), stream)))
     return rc;
   if ((rc = c3_deposit(cp, dt, s))) return rc;
-  if ((rc = sbe_pstd3_update_e(cp->p, E, H, reinterpret_cast<double*>(cp->J), dt, stream)))
+  if ((rc = pstd3_update_e_from_work(cp->p, reinterpret_cast<double2*>(E),
+                                     reinterpret_cast<const double2*>(H), cp->J, dt, s)))
     return rc;
   k_tick<<<1, 1, 0, s>>>(cp->step);
   return cuda_check(cudaGetLastError(), "sbe_couple3_step");

@@ -326,6 +326,253 @@ __global__ void k_tables3(int n, double d, double* x, double* q, double2* tw, fl
   mask[j] = m;
 }
 
+// ---- FP32 work with (y, z) planes in shared memory: three passes per curl ------
+// When a (y, z) plane of FP32 complex values fits in one block's shared memory
+// (ny nz <= kPlaneMax) a curl is three passes instead of five:
+//   A  per (x, component) plane: FP64 field -> FP32, forward transforms along z and y
+//   B  x lines of tl (y, z) columns of all three components: forward along x, the curl
+//      i q x F, inverse along x
+//   C  per plane: inverse along y and z, out (+)= a curl / N (- ja J), mask; in the
+//      field step C of the H update continues with pass A of the E update on the new
+//      H it has just written (the plane is still in shared memory)
+// The transforms run in place: radix-2 decimation in frequency (natural order in,
+// bit-reversed order out, exp(-i ...)) and its exact inverse, decimation in time
+// (bit-reversed in, natural out, unnormalised), two radix-2 stages fused per sweep
+// over shared memory.  The spectrum is never reordered: the curl is pointwise in k
+// space and reads the wavenumber of position p as q[bitrev(p)].
+constexpr int kPlaneMax = 16384;   // FP32 complex elements of one plane (128 KB)
+constexpr int kPlaneThreads = 1024;
+constexpr int kXThreads = 512;
+constexpr int kXSmem = 96 * 1024;  // shared memory of one x-pass block's lines
+
+__device__ __forceinline__ float2 c_mul(float2 a, float2 w) {
+  return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+__device__ __forceinline__ float2 c_mulc(float2 a, float2 w) {   // a conj(w)
+  return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ int brev(int p, int lg) { return lg ? (int)(__brev((unsigned)p) >> (32 - lg)) : 0; }
+
+// nl lines of n = 2^lg elements in shared memory, element p of line l at
+// a[l * ls + p * es]; tw[j] = exp(-2 pi i j / n), j < n / 2.  line_fast: consecutive
+// threads take consecutive lines (lines adjacent in memory), else consecutive
+// positions of one line.  Ends with __syncthreads.
+template <bool INV>
+__device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line_fast,
+                            const float2* tw) {
+  const int n = 1 << lg, npair = lg >> 1, q4 = n >> 2;
+  if (lg & 1) {
+    // the radix-2 stage of span 1 (twiddle 1): last for DIF, first for DIT
+    if (INV) {
+      for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
+        const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
+        float2* x = a + (long long)l * ls + 2 * b * es;
+        const float2 x0 = x[0], x1 = x[es];
+        x[0] = c_add(x0, x1);
+        x[es] = c_sub(x0, x1);
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = 0; t < npair; ++t) {
+    const int pi = INV ? npair - 1 - t : t;
+    const int m = n >> (2 * pi + 2), lgm = lg - 2 * pi - 2;
+    const int tws = q4 / m;     // n / (4 m): w_{4m}^j = tw[j tws]
+    for (int u = threadIdx.x; u < nl * q4; u += blockDim.x) {
+      const int l = line_fast ? u % nl : u / q4, r = line_fast ? u / nl : u % q4;
+      const int j = r & (m - 1), p0 = ((r >> lgm) << (lgm + 2)) + j;
+      float2* x = a + (long long)l * ls + (long long)p0 * es;
+      const int sm = m * es;
+      const float2 x0 = x[0], x1 = x[sm], x2 = x[2 * sm], x3 = x[3 * sm];
+      const float2 w1a = tw[j * tws], w1b = tw[(j + m) * tws], w2 = tw[2 * j * tws];
+      float2 y0, y1, y2, y3;
+      if (!INV) {
+        const float2 a0 = c_add(x0, x2), a2 = c_mul(c_sub(x0, x2), w1a);
+        const float2 a1 = c_add(x1, x3), a3 = c_mul(c_sub(x1, x3), w1b);
+        y0 = c_add(a0, a1);
+        y1 = c_mul(c_sub(a0, a1), w2);
+        y2 = c_add(a2, a3);
+        y3 = c_mul(c_sub(a2, a3), w2);
+      } else {
+        const float2 t1 = c_mulc(x1, w2), t3 = c_mulc(x3, w2);
+        const float2 a0 = c_add(x0, t1), a1 = c_sub(x0, t1);
+        const float2 a2 = c_add(x2, t3), a3 = c_sub(x2, t3);
+        const float2 t2 = c_mulc(a2, w1a), t4 = c_mulc(a3, w1b);
+        y0 = c_add(a0, t2);
+        y2 = c_sub(a0, t2);
+        y1 = c_add(a1, t4);
+        y3 = c_sub(a1, t4);
+      }
+      x[0] = y0;
+      x[sm] = y1;
+      x[2 * sm] = y2;
+      x[3 * sm] = y3;
+    }
+    __syncthreads();
+  }
+  if ((lg & 1) && !INV) {
+    for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
+      const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
+      float2* x = a + (long long)l * ls + 2 * b * es;
+      const float2 x0 = x[0], x1 = x[es];
+      x[0] = c_add(x0, x1);
+      x[es] = c_sub(x0, x1);
+    }
+    __syncthreads();
+  }
+}
+
+struct PlaneArgs {
+  int lgy, lgz, ny, nz, nx;
+  long long N, P;                 // grid points, points per (y, z) plane
+  const float2* twy;              // exp(-2 pi i j / ny), j < ny (global)
+  const float2* twz;
+};
+
+// shared memory of a plane block: the plane, then the y and z twiddles (half each)
+__device__ __forceinline__ void plane_tables(const PlaneArgs& A, float2* sty, float2* stz) {
+  for (int j = threadIdx.x; j < (A.ny >> 1); j += blockDim.x) sty[j] = A.twy[j];
+  for (int j = threadIdx.x; j < (A.nz >> 1); j += blockDim.x) stz[j] = A.twz[j];
+}
+
+// forward along z (rows of the plane) then y (columns)
+__device__ __forceinline__ void plane_forward(const PlaneArgs& A, float2* a, const float2* sty,
+                                              const float2* stz) {
+  fft_inplace<false>(a, A.lgz, A.ny, A.nz, 1, false, stz);
+  fft_inplace<false>(a, A.lgy, A.nz, 1, A.nz, true, sty);
+}
+
+// pass A: plane (x = blockIdx.x, component blockIdx.y) of the FP64 field F -> W
+__global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, const double2* F,
+                                                                float2* W) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* a = reinterpret_cast<float2*>(smraw);
+  float2* sty = a + A.P;
+  float2* stz = sty + (A.ny >> 1);
+  const long long base = blockIdx.y * A.N + blockIdx.x * A.P;
+  plane_tables(A, sty, stz);
+  // all loads of a thread before the stores to shared memory (4 per round)
+  for (int i0 = threadIdx.x; i0 < A.P; i0 += 4 * kPlaneThreads) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kPlaneThreads;
+      v[u] = i < A.P ? F[base + i] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kPlaneThreads;
+      if (i < A.P) a[i] = make_float2((float)v[u].x, (float)v[u].y);
+    }
+  }
+  __syncthreads();
+  plane_forward(A, a, sty, stz);
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[i];
+}
+
+// pass B: the x lines of tl consecutive (y, z) columns of all three components;
+// shared memory [x][component][column]
+__global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W, int lgx, int tl,
+                                                         const float2* twx, const double* qx,
+                                                         const double* qy, const double* qz) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = 1 << lgx, w3 = 3 * tl;
+  float2* a = reinterpret_cast<float2*>(smraw);
+  float2* stx = a + (size_t)nx * w3;
+  for (int j = threadIdx.x; j < (nx >> 1); j += blockDim.x) stx[j] = twx[j];
+  const long long b0 = (long long)blockIdx.x * tl;
+  const int total = nx * w3;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
+    a[idx] = W[f * A.N + px * A.P + b0 + c];
+  }
+  __syncthreads();
+  fft_inplace<false>(a, lgx, w3, 1, w3, true, stx);
+  for (int idx = threadIdx.x; idx < nx * tl; idx += blockDim.x) {
+    const int px = idx / tl, c = idx - px * tl;
+    const long long col = b0 + c;
+    const int py = (int)(col >> A.lgz), pz = (int)(col & (A.nz - 1));
+    const double kx = qx[brev(px, lgx)], ky = qy[brev(py, A.lgy)], kz = qz[brev(pz, A.lgz)];
+    float2* e = a + (size_t)px * w3 + c;
+    const float2 fx = e[0], fy = e[tl], fz = e[2 * tl];
+    // i (k x F)
+    const double cxr = ky * fz.x - kz * fy.x, cxi = ky * fz.y - kz * fy.y;
+    const double cyr = kz * fx.x - kx * fz.x, cyi = kz * fx.y - kx * fz.y;
+    const double czr = kx * fy.x - ky * fx.x, czi = kx * fy.y - ky * fx.y;
+    e[0] = make_float2((float)-cxi, (float)cxr);
+    e[tl] = make_float2((float)-cyi, (float)cyr);
+    e[2 * tl] = make_float2((float)-czi, (float)czr);
+  }
+  __syncthreads();
+  fft_inplace<true>(a, lgx, w3, 1, w3, true, stx);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
+    W[f * A.N + px * A.P + b0 + c] = a[idx];
+  }
+}
+
+// pass C: inverse along y and z of plane (x, component), then out (+)= ...: the
+// update of Upd (the masks per axis); with fwd_next the plane of the updated FP64
+// field continues as pass A of the next curl (W overwritten with its transform: the
+// block owns its plane of W)
+__global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, float2* W, Upd U,
+                                                                int fwd_next) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* a = reinterpret_cast<float2*>(smraw);
+  float2* sty = a + A.P;
+  float2* stz = sty + (A.ny >> 1);
+  const int x = blockIdx.x;
+  const long long base = blockIdx.y * A.N + x * A.P;
+  plane_tables(A, sty, stz);
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) a[i] = W[base + i];
+  __syncthreads();
+  fft_inplace<true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
+  fft_inplace<true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
+  const double invN = 1.0 / (double)A.N;
+  const double mx = U.m0 ? U.m0[x] : 1.0;
+  for (int i0 = threadIdx.x; i0 < A.P; i0 += 2 * kPlaneThreads) {
+    // both elements' FP64 loads before their updates
+    double2 o[2], jv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int i = i0 + u * kPlaneThreads;
+      const bool in = i < A.P;
+      o[u] = (in && !U.store) ? U.out[base + i] : make_double2(0.0, 0.0);
+      jv[u] = (in && U.J) ? U.J[base + i] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int i = i0 + u * kPlaneThreads;
+      if (i >= A.P) continue;
+      const float2 v = a[i];
+      const double vx = (double)v.x * invN, vy = (double)v.y * invN;
+      double2 r;
+      if (U.store) {
+        r = make_double2(vx, vy);
+      } else {
+        r = make_double2(o[u].x + U.a * vx, o[u].y + U.a * vy);
+        if (U.J) {
+          r.x -= U.ja * jv[u].x;
+          r.y -= U.ja * jv[u].y;
+        }
+      }
+      if (U.m0) {
+        const double m = mx * U.m1[i >> A.lgz] * U.m2[i & (A.nz - 1)];
+        r.x *= m;
+        r.y *= m;
+      }
+      U.out[base + i] = r;
+      if (fwd_next) a[i] = make_float2((float)r.x, (float)r.y);
+    }
+  }
+  if (!fwd_next) return;   // block-uniform
+  __syncthreads();
+  plane_forward(A, a, sty, stz);
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[i];
+}
+
 bool pow2(int v) { return v >= 2 && v <= 1024 && (v & (v - 1)) == 0; }
 
 // tl lines per block within the shared-memory budget (two ping-pong buffers of nf
@@ -418,7 +665,110 @@ int curl_any(SbePstd3* p, const double2* F, double2* out, double a, const double
 
 bool is_masked(const SbePstd3* p) { return p->n_abc[0] > 0 || p->n_abc[1] > 0 || p->n_abc[2] > 0; }
 
+// ---- the three-pass curl (FP32 work, planes in shared memory) -----------------
+bool planes_fit(const SbePstd3* p) { return p->fp32 && (long long)p->n[1] * p->n[2] <= kPlaneMax; }
+
+PlaneArgs plane_args(const SbePstd3* p) {
+  PlaneArgs A{};
+  A.nx = p->n[0];
+  A.ny = p->n[1];
+  A.nz = p->n[2];
+  A.lgy = ilog2i(A.ny);
+  A.lgz = ilog2i(A.nz);
+  A.N = p->N;
+  A.P = (long long)A.ny * A.nz;
+  A.twy = p->twf[1];
+  A.twz = p->twf[2];
+  return A;
+}
+
+size_t plane_smem(const PlaneArgs& A) {
+  return sizeof(float2) * ((size_t)A.P + (A.ny >> 1) + (A.nz >> 1));
+}
+
+// x-pass columns per block: the three components' x lines of tl columns within
+// kXSmem, tl <= 16 and dividing the plane
+int x_lines(const SbePstd3* p) {
+  const long long P = (long long)p->n[1] * p->n[2];
+  int tl = 16;
+  while (tl > 1 && ((size_t)3 * p->n[0] * tl * sizeof(float2) > (size_t)kXSmem || P % tl)) tl >>= 1;
+  return tl;
+}
+
+int plane_pass_a(SbePstd3* p, const double2* F, cudaStream_t s) {
+  const PlaneArgs A = plane_args(p);
+  k_plane_fwd<<<dim3(A.nx, 3), kPlaneThreads, plane_smem(A), s>>>(A, F,
+                                                                  static_cast<float2*>(p->work));
+  return cuda_check(cudaGetLastError(), "pstd3 plane pass");
+}
+
+int plane_pass_b(SbePstd3* p, cudaStream_t s) {
+  const PlaneArgs A = plane_args(p);
+  const int tl = x_lines(p), nx = p->n[0];
+  const size_t smem = sizeof(float2) * ((size_t)3 * nx * tl + (nx >> 1));
+  k_x_curl_ip<<<(unsigned)(A.P / tl), kXThreads, smem, s>>>(
+      A, static_cast<float2*>(p->work), ilog2i(nx), tl, p->twf[0], p->q[0], p->q[1], p->q[2]);
+  return cuda_check(cudaGetLastError(), "pstd3 x pass");
+}
+
+int plane_pass_c(SbePstd3* p, const Upd& U, int fwd_next, cudaStream_t s) {
+  const PlaneArgs A = plane_args(p);
+  k_plane_inv<<<dim3(A.nx, 3), kPlaneThreads, plane_smem(A), s>>>(
+      A, static_cast<float2*>(p->work), U, fwd_next);
+  return cuda_check(cudaGetLastError(), "pstd3 plane pass");
+}
+
+Upd upd_for(SbePstd3* p, double2* out, double a, const double2* J, double ja, bool masked,
+            int store) {
+  Upd U = upd_store(p);
+  U.out = out;
+  U.a = a;
+  U.J = J;
+  U.ja = ja;
+  U.store = store;
+  if (masked) {
+    U.m0 = p->mask[0];
+    U.m1 = p->mask[1];
+    U.m2 = p->mask[2];
+  }
+  return U;
+}
+
+// out (+)= a curl F ...: the three-pass form when the planes fit, else five passes
+int curl_best(SbePstd3* p, const double2* F, double2* out, double a, const double2* J, double ja,
+              bool masked, int store, cudaStream_t s) {
+  if (!planes_fit(p)) return curl_any(p, F, out, a, J, ja, masked, store, s);
+  int rc = plane_pass_a(p, F, s);
+  if (!rc) rc = plane_pass_b(p, s);
+  if (!rc) rc = plane_pass_c(p, upd_for(p, out, a, J, ja, masked, store), 0, s);
+  return rc;
+}
+
 }  // namespace
+
+// The H half-step of a field step, leaving the work array ready for the E half-step
+// of the same step: with planes in shared memory the H update's last pass continues
+// with the first pass of curl H on the new H.
+int pstd3_update_h_fwd(SbePstd3* p, const double2* E, double2* H, double dt, cudaStream_t s) {
+  if (!planes_fit(p))
+    return curl_any(p, E, H, -dt / kMu0, nullptr, 0.0, is_masked(p), 0, s);
+  int rc = plane_pass_a(p, E, s);
+  if (!rc) rc = plane_pass_b(p, s);
+  if (!rc) rc = plane_pass_c(p, upd_for(p, H, -dt / kMu0, nullptr, 0.0, is_masked(p), 0), 1, s);
+  return rc;
+}
+
+// The E half-step after pstd3_update_h_fwd on the same H, with nothing else using the
+// work array in between.
+int pstd3_update_e_from_work(SbePstd3* p, double2* E, const double2* H, const double2* J,
+                             double dt, cudaStream_t s) {
+  const double ie = dt / (kEps0 * p->epsr);
+  if (!planes_fit(p)) return curl_any(p, H, E, ie, J, ie, is_masked(p), 0, s);
+  int rc = plane_pass_b(p, s);
+  if (!rc) rc = plane_pass_c(p, upd_for(p, E, ie, J, ie, is_masked(p), 0), 0, s);
+  return rc;
+}
+
 }  // namespace sbe
 
 using namespace sbe;
@@ -479,6 +829,9 @@ int sbe_pstd3_create(const SbePstd3Desc* d, void* stream, SbePstd3** out) {
     cudaFuncSetAttribute(k_line_pass<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_line_pass<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_x_curl<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_plane_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_plane_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_x_curl_ip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     rc = cuda_check(cudaFuncSetAttribute(k_x_curl<float2>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                     "sbe_pstd3_create: shared memory");
@@ -511,22 +864,22 @@ int sbe_pstd3_grid(SbePstd3* p, int axis, double* x, double* q, void* stream) {
 
 int sbe_pstd3_curl(SbePstd3* p, const double* F, double* out, void* stream) {
   if (!p || !F || !out) return fail(SBE_ERR_ARG, "sbe_pstd3_curl: null");
-  return curl_any(p, (const double2*)F, (double2*)out, 1.0, nullptr, 0.0, false, 1,
-                  as_stream(stream));
+  return curl_best(p, (const double2*)F, (double2*)out, 1.0, nullptr, 0.0, false, 1,
+                   as_stream(stream));
 }
 
 int sbe_pstd3_update_h(SbePstd3* p, const double* E, double* H, double dt, void* stream) {
   if (!p || !E || !H) return fail(SBE_ERR_ARG, "sbe_pstd3_update_h: null");
-  return curl_any(p, (const double2*)E, (double2*)H, -dt / kMu0, nullptr, 0.0, is_masked(p), 0,
-                  as_stream(stream));
+  return curl_best(p, (const double2*)E, (double2*)H, -dt / kMu0, nullptr, 0.0, is_masked(p), 0,
+                   as_stream(stream));
 }
 
 int sbe_pstd3_update_e(SbePstd3* p, double* E, const double* H, const double* J, double dt,
                        void* stream) {
   if (!p || !E || !H) return fail(SBE_ERR_ARG, "sbe_pstd3_update_e: null");
   const double ie = dt / (kEps0 * p->epsr);
-  return curl_any(p, (const double2*)H, (double2*)E, ie, (const double2*)J, ie, is_masked(p), 0,
-                  as_stream(stream));
+  return curl_best(p, (const double2*)H, (double2*)E, ie, (const double2*)J, ie, is_masked(p), 0,
+                   as_stream(stream));
 }
 
 int sbe_pstd3_step(SbePstd3* p, double* E, double* H, const double* J, double dt, void* stream) {
@@ -537,9 +890,11 @@ int sbe_pstd3_step(SbePstd3* p, double* E, double* H, const double* J, double dt
   for (int a = 0; a < 3; ++a) qm += (kPi / p->d[a]) * (kPi / p->d[a]);
   if (v * dt * std::sqrt(qm) / 2.0 > 1.0)
     return fail(SBE_ERR_ARG, "sbe_pstd3_step: dt above the stability limit 2 / (v |q|max)");
-  int rc = sbe_pstd3_update_h(p, E, H, dt, stream);
+  if (!E || !H) return fail(SBE_ERR_ARG, "sbe_pstd3_step: null");
+  cudaStream_t s = as_stream(stream);
+  int rc = pstd3_update_h_fwd(p, (const double2*)E, (double2*)H, dt, s);
   if (rc) return rc;
-  return sbe_pstd3_update_e(p, E, H, J, dt, stream);
+  return pstd3_update_e_from_work(p, (double2*)E, (const double2*)H, (const double2*)J, dt, s);
 }
 
 // rhoPJ.py:703-880 ElongfromRho with the caller's wavenumber tables (the reference

@@ -21,3 +21,12 @@ struct SbePstd3 {
   void* work = nullptr;         // up to 10 fields of N complex (FP64) work
 };
 
+namespace sbe {
+// Field half-steps of one leapfrog step (pstd3d.cu): the H update leaves the work
+// array holding the forward transform of the new H when the transform planes fit in
+// shared memory, and the E update that follows starts from it; nothing else may use
+// the work array in between.
+int pstd3_update_h_fwd(SbePstd3* p, const double2* E, double2* H, double dt, cudaStream_t s);
+int pstd3_update_e_from_work(SbePstd3* p, double2* E, const double2* H, const double2* J,
+                             double dt, cudaStream_t s);
+}  // namespace sbe

@@ -565,6 +565,22 @@ int sbe_wire_info(SbeCtx* c, int w, const double* C2, const double* D2, const do
                           (const double2*)Ek, out23, s);
 }
 
+int sbe_wire_pdote(SbeCtx* c, int w, const double* Ek, const double* src, const double* P0,
+                   double* out, void* stream) {
+  int rc = check_w(c, w, "sbe_wire_pdote");
+  if (rc) return rc;
+  if (!Ek || !src || !out) return fail(SBE_ERR_ARG, "sbe_wire_pdote: null pointer");
+  return launch_wire_pdote(c, w, (const double2*)Ek, (const double2*)src, P0, out,
+                           as_stream(stream));
+}
+
+int sbe_deph_extrema(SbeCtx* c, int w, double* out4, void* stream) {
+  int rc = check_w(c, w, "sbe_deph_extrema");
+  if (rc) return rc;
+  if (!out4) return fail(SBE_ERR_ARG, "sbe_deph_extrema: null pointer");
+  return launch_deph_extrema(c, w, out4, as_stream(stream));
+}
+
 int sbe_carrier_rates(SbeCtx* c, int w, const double* ne, const double* nh, const double* VC,
                       double* WinE, double* WoutE, double* WinH, double* WoutH, int precision,
                       void* stream) {

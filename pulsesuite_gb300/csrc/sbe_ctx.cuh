@@ -189,6 +189,11 @@ void launch_relax_only(SbeCtx* c, double2* P3, double2* C3, double2* D3, const d
 // sbe_info.cu: per-step statistics of wire w (info / EP columns) into out (23 doubles)
 int launch_wire_info(SbeCtx* c, int w, const double2* C2, const double2* D2, const double2* src,
                      const double2* Ek, double* out, cudaStream_t s);
+// sbe_info.cu: wire-grid P.E increment (PdotE.w.dat) and the De / Dh extrema
+// (MaxOffDiag.{e,h}.dat) of wire w
+int launch_wire_pdote(SbeCtx* c, int w, const double2* Ek, const double2* src, const double* P0,
+                      double* out, cudaStream_t s);
+int launch_deph_extrema(SbeCtx* c, int w, double* out4, cudaStream_t s);
 // sbe_dc.cu: DC transport (dcfield.py:1154-1236 Transport) of P, C, D
 bool any_dc(const SbeCtx* c);
 void launch_dc_transport(SbeCtx* c, double2* P, double2* C, double2* D, const double2* Ek,

@@ -185,7 +185,80 @@ __global__ void __launch_bounds__(kInfoThreads) k_wire_info(const WireDev* wires
   }
 }
 
+// Re iFFTG(E_c)(r) of the wire-k field (usefulsubs.py:2271-2294: iFFTG(F) = -N
+// ifft(F) = -sum_q F[q] e^{+2 pi i q r / N}): one block per (r, component)
+__global__ void k_wire_field_r(const WireDev* wires, int w, const double2* Ek, double* er) {
+  const WireDev W = wires[w];
+  const int nr = W.nr, r = blockIdx.x, c = blockIdx.y;
+  const double2* e = Ek + 3LL * W.off_r + (long long)c * nr;
+  double acc = 0.0;
+  for (int q = threadIdx.x; q < nr; q += blockDim.x) {
+    const long long qr = ((long long)q * r) % nr;
+    double sn, cs;
+    sincospi(2.0 * (double)qr / (double)nr, &sn, &cs);
+    acc += e[q].x * cs - e[q].y * sn;
+  }
+  __shared__ double red[33];
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) er[(long long)c * nr + r] = -t;
+}
+
+// sum_c sum_r (Re P_c(r) - P0_c(r)) Re E_c(r): the wire-grid increment of the
+// reference's EPEnergyW (SBEs.py:5950-5958) before its 0.5 dr area factor
+__global__ void k_wire_pdote(const WireDev* wires, int w, const double2* src, const double* P0,
+                             const double* er, double* out) {
+  const WireDev W = wires[w];
+  const int nr = W.nr;
+  double acc = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    const double2* pc = src + 5LL * W.off_r + (long long)c * nr;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+      const double p0 = P0 ? P0[(long long)c * nr + r] : 0.0;
+      acc += (pc[r].x - p0) * er[(long long)c * nr + r];
+    }
+  }
+  __shared__ double red[33];
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) *out = t;
+}
+
+// max and min of Re De and Re Dh of wire w (dephasing.py:731-740), [2Nk+1][Nk] each
+__global__ void k_deph_extrema(const WireDev* wires, int w, const double* De, const double* Dh,
+                               double* out4) {
+  const WireDev W = wires[w];
+  const long long n = (long long)(2 * W.nk + 1) * W.nk;
+  const double* a[2] = {De + W.off_dd, Dh + W.off_dd};
+  __shared__ double red[33];
+  for (int i = 0; i < 2; ++i) {
+    double mx = -INFINITY, mn = INFINITY;
+    for (long long j = threadIdx.x; j < n; j += blockDim.x) {
+      mx = fmax(mx, a[i][j]);
+      mn = fmin(mn, a[i][j]);
+    }
+    mx = block_max(mx, red);
+    mn = -block_max(-mn, red);
+    if (threadIdx.x == 0) {
+      out4[2 * i] = mx;
+      out4[2 * i + 1] = mn;
+    }
+  }
+}
+
 }  // namespace
+
+int launch_wire_pdote(SbeCtx* c, int w, const double2* Ek, const double2* src, const double* P0,
+                      double* out, cudaStream_t s) {
+  const int nr = c->wires[w].nr;
+  double* er = reinterpret_cast<double*>(c->qscr);   // 3 nr doubles of the scratch
+  k_wire_field_r<<<dim3(nr, 3), kInfoThreads, 0, s>>>(c->d_wires, w, Ek, er);
+  k_wire_pdote<<<1, kInfoThreads, 0, s>>>(c->d_wires, w, src, P0, er, out);
+  return cuda_check(cudaGetLastError(), "sbe_wire_pdote");
+}
+
+int launch_deph_extrema(SbeCtx* c, int w, double* out4, cudaStream_t s) {
+  k_deph_extrema<<<1, kInfoThreads, 0, s>>>(c->d_wires, w, c->De, c->Dh, out4);
+  return cuda_check(cudaGetLastError(), "sbe_deph_extrema");
+}
 
 int launch_wire_info(SbeCtx* c, int w, const double2* C2, const double2* D2, const double2* src,
                      const double2* Ek, double* out, cudaStream_t s) {

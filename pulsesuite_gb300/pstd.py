@@ -149,6 +149,17 @@ class Pstd3D:
         _lib.check(self.lib.sbe_pstd3_step(self.handle, _lib.ptr(E), _lib.ptr(H), _lib.ptr(J),
                                            float(dt), _lib.stream_handle()), "sbe_pstd3_step")
 
+    def update_h(self, E, H, dt):
+        """H -= dt/mu0 curl E (masked), the first half of ``step``."""
+        _lib.check(self.lib.sbe_pstd3_update_h(self.handle, _lib.ptr(E), _lib.ptr(H), float(dt),
+                                               _lib.stream_handle()), "sbe_pstd3_update_h")
+
+    def update_e(self, E, H, J, dt):
+        """E += dt/eps (curl H - J) (masked), the second half of ``step``."""
+        _lib.check(self.lib.sbe_pstd3_update_e(self.handle, _lib.ptr(E), _lib.ptr(H), _lib.ptr(J),
+                                               float(dt), _lib.stream_handle()),
+                   "sbe_pstd3_update_e")
+
     def elong(self, rho, P, qx=None, qy=None, qz=None):
         """ElongfromRho (rhoPJ.py:703-880): returns (out10 (10, nx, ny, nz), P_k (3, ...))
         with out10 = [E_PRho x, y, z, E_P x, y, z, E_Rho x, y, z, RhoBound]; the

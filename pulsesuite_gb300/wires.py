@@ -255,6 +255,24 @@ class WireContext:
                                           _lib.stream_handle()), "sbe_wire_info")
         return out.cpu().numpy()
 
+    def wire_pdote(self, w, Ek, src, P0=None):
+        """sum_c sum_r (Re P_c - P0_c) Re iFFTG(E_c) of wire w (see sbe_wire_pdote):
+        Ek, src the packed wire-k field and real-space sources, P0 (3, Nr) float64 or
+        None."""
+        out = torch.empty(1, dtype=torch.float64, device=self.device)
+        p0 = None if P0 is None else P0.contiguous()
+        _lib.check(self.lib.sbe_wire_pdote(self.handle, w, _lib.ptr(Ek), _lib.ptr(src),
+                                           _lib.ptr(p0), _lib.ptr(out), _lib.stream_handle()),
+                   "sbe_wire_pdote")
+        return float(out.item())
+
+    def deph_extrema(self, w):
+        """(max Re De, min Re De, max Re Dh, min Re Dh) of wire w's last preparation."""
+        out = torch.empty(4, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.sbe_deph_extrema(self.handle, w, _lib.ptr(out), _lib.stream_handle()),
+                   "sbe_deph_extrema")
+        return out.cpu().numpy()
+
     def sources(self, w, P, C, D, ne, nh):
         nr = 2 * self.nk[w] + 2
         out = [torch.empty(nr, dtype=CDTYPE, device=self.device) for _ in range(5)]

@@ -650,6 +650,13 @@ def case_solver100(L, nsteps, dt, E0, seed):
     for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
         out[f"end_{nm}"] = getattr(s, nm).copy()
     s.close()
+    # the text diagnostics the reference appended on the way (SBEs.py:5940-5975,
+    # dephasing.py:538-539 and 731-740)
+    for key, path in (("pdote_p", "output/PdotE.p.dat"), ("pdote_w", "output/PdotE.w.dat"),
+                      ("maxoff_e", "dataQW/Wire/info/MaxOffDiag.e.dat"),
+                      ("maxoff_h", "dataQW/Wire/info/MaxOffDiag.h.dat")):
+        with open(path, "rb") as f:
+            out["txt_" + key] = np.frombuffer(f.read(), dtype=np.uint8)
     return out
 
 

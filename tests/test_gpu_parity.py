@@ -240,9 +240,28 @@ def test_batched_solver_leapfrog_vs_golden(tmp_path, monkeypatch):
     s.close()
 
 
-def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch):
+def _diagnostic_files_match(g):
+    """The text diagnostics of the run against the reference's files: the same lines,
+    the times equal, the values within 1e-8 of their column's largest magnitude."""
+    for key, path in (("pdote_p", "output/PdotE.p.dat"), ("pdote_w", "output/PdotE.w.dat"),
+                      ("maxoff_e", "dataQW/Wire/info/MaxOffDiag.e.dat"),
+                      ("maxoff_h", "dataQW/Wire/info/MaxOffDiag.h.dat")):
+        want = np.array([[float(v) for v in ln.split()]
+                         for ln in bytes(g["txt_" + key]).decode().splitlines()])
+        with open(path, encoding="utf-8") as fh:
+            got = np.array([[float(v) for v in ln.split()] for ln in fh.read().splitlines()])
+        assert got.shape == want.shape, (key, got.shape, want.shape)
+        assert np.array_equal(got[:, 0], want[:, 0]), key
+        for c in range(1, want.shape[1]):
+            scale = np.abs(want[:, c]).max()
+            assert np.abs(got[:, c] - want[:, c]).max() <= 1e-8 * scale, (key, c)
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch, batch):
     """100 reference QWCalculator steps on two wires (SBESolver drop-in, FP64 path):
-    the sources of every tenth step and the nine state levels at the end <= 1e-10."""
+    the sources of every tenth step and the nine state levels at the end <= 1e-10,
+    and the PdotE and MaxOffDiag files the reference wrote on the way."""
     from pulsesuite_gb300 import SBEs
     monkeypatch.chdir(tmp_path)
     g = golden("solver_100")
@@ -252,7 +271,7 @@ def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch):
                jmax=100000, ntmax=100000)
     rr, f = g["rr"], g["fields"]
     s = SBEs.SBESolver(np.zeros(len(rr)), rr, 0.0, float(g["E0"]), 800e-9, 2, True, params=prm,
-                       flags=SOLVER_FLAGS)
+                       flags=SOLVER_FLAGS, batch=batch)
     assert s.Nk == int(g["nk"])
     for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
         setattr(s, nm, g["init_" + nm])
@@ -268,6 +287,7 @@ def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch):
     for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
         assert rel(getattr(s, nm), g[f"end_{nm}"]) < SCREEN, nm
     s.close()
+    _diagnostic_files_match(g)
 
 
 def _seeded_state(rng, nk):
@@ -606,3 +626,37 @@ def test_wire_info_vs_oracle():
     for i, (a, b) in enumerate(zip(v, want)):
         assert abs(a - b) <= 1e-12 * abs(b) + 1e-300, (i, a, b)
     assert np.imag(info[15]) == 0.0 and np.imag(info[16]) == 0.0
+
+
+def test_wire_pdote_and_deph_extrema_vs_oracle():
+    """sbe_wire_pdote against sum (Re P - P0) Re iFFTG(E) of the oracle, and
+    sbe_deph_extrema against the De, Dh the library's preparation produced."""
+    from pulsesuite_gb300.wires import WireContext, WireSpec
+    nk = 16
+    L = np.pi / (3e9 / (nk / 2 - 0.5))
+    c = WireContext([WireSpec(nk=nk, L=L, temp=77.0, wire_index=w + 1, flags=dict(ALL), **MAT)
+                     for w in range(2)])
+    rng = np.random.default_rng(33)
+    nr = 2 * nk + 2
+    src = [(rng.standard_normal((5, nr)) + 1j * rng.standard_normal((5, nr))) * 1e-3
+           for _ in range(2)]
+    Ek = [(rng.standard_normal((3, nr)) + 1j * rng.standard_normal((3, nr))) * 1e6
+          for _ in range(2)]
+    P0 = rng.standard_normal((3, nr)) * 1e-3
+    for w in range(2):
+        got = c.wire_pdote(w, c.pack_r(Ek, 3), c.pack_r(src, 5), dev(P0))
+        want = sum(np.sum((src[w][i].real - P0[i]) * O.ifftg(Ek[w][i]).real) for i in range(3))
+        assert abs(got - want) <= 1e-12 * np.abs(src[w][:3].real * O.ifftg(Ek[w][0]).real).sum()
+        got0 = c.wire_pdote(w, c.pack_r(Ek, 3), c.pack_r(src, 5), None)
+        want0 = sum(np.sum(src[w][i].real * O.ifftg(Ek[w][i]).real) for i in range(3))
+        assert abs(got0 - want0) <= 1e-12 * abs(want0) + 1e-300
+    states = [_seeded_state(rng, nk) for _ in range(2)]
+    De, Dh = c.deph(c.pack([s[1] for s in states]), c.pack([s[2] for s in states]), fp32=False)
+    off = 0
+    for w in range(2):
+        n = (2 * nk + 1) * nk
+        e, h = De[off:off + n], Dh[off:off + n]
+        v = c.deph_extrema(w)
+        assert list(v) == [float(e.max()), float(e.min()), float(h.max()), float(h.min())]
+        off += n
+    c.close()
