@@ -292,10 +292,20 @@ class ClockSampler:
                  "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+        # nvidia-smi takes a while to start: wait (up to 5 s) for its first sample so
+        # that the samples cover the timed region that follows
+        t0 = time.time()
+        while self.p is not None and time.time() - t0 < 5.0:
+            try:
+                if os.path.getsize(path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.02)
 
     def stop(self):
         if self.p is None:
@@ -506,9 +516,10 @@ def gpu_arm(args, wl):
     # algorithmic work of a1-a3 per RHS evaluation: dP, dC, dD as 12 complex Nk^3
     # products = 96 Nk^3 flop per wire
     useful = 96.0 * nk ** 3 * nw
-    # executed: 8 complex products (W - W^H form) x 4 real products x 3 hi/lo terms x
-    # 2 Nk^3 = 192 Nk^3 per wire
-    executed = 192.0 * nk ** 3 * nw
+    # executed per wire, in 2 Nk^3 real-product MMA chains: dP 4 complex terms x 4 real
+    # products x 3 hi/lo terms = 48; W, V 2 complex terms each x 4 x (hi*lo, lo*hi,
+    # lo*lo) = 48; their hi*hi products 16: 112 x 2 Nk^3 = 224 Nk^3
+    executed = 224.0 * nk ** 3 * nw
     achieved = useful / per_eval_s / 1e12
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     roof = {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)", "achieved": achieved,
@@ -525,10 +536,14 @@ def gpu_arm(args, wl):
                             "scaled by wires; a constant of this file, refreshed with the profile",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
                            "12 complex Nk^3 products) over the summed CUDA-event time of the "
-                           "evaluation's two commutator launches (dP with the hi*lo + lo*hi "
-                           "products of W and V; the hi*hi products of W and V as two K halves "
-                           "with one accumulator per real product); executed 192*Nk^3 (8 complex "
-                           "products x 4 real products x 3 hi/lo terms)"}
+                           "evaluation's two commutator launches (dP with the hi*lo + lo*hi + "
+                           "lo*lo products of W and V; the hi*hi products of W and V in K parts "
+                           "with one accumulator per real product); executed 224*Nk^3 (dP 96, "
+                           "W and V cross terms 96, their hi*hi products 32); step: 496*Nk^3 "
+                           "algorithmic flop per wire-step (4 evaluations of a1-a3 and the "
+                           "exchange and source products) over the step time",
+            "step_tflops": 496.0 * nk ** 3 * value / 1e12,
+            "step_frac": 496.0 * nk ** 3 * value / 1e12 / peak}
     other = {name: {"ms_per_step": prof[c][0] / args.steps, "launches": prof[c][1]}
              for c, name in ((1, "exchange_gemm"), (2, "source_gemm"), (3, "dephasing_fp32"))}
     other["pstd_field_step"] = {"ms_per_step": pstd_ms, "launches": 6}

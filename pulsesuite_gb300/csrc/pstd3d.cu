@@ -25,6 +25,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fp_bits.cuh"
 #include "pstd3d.cuh"
 
 namespace sbe {
@@ -138,6 +139,7 @@ struct Upd {
   const double* m2;
   int nx, ny, nz;
   int store;               // 1: out = result / N (no update)
+  float af[2], jf[2];      // the plane path's a / N and ja as FP32 pairs (hi, lo)
 };
 
 template <typename T>
@@ -302,9 +304,19 @@ __global__ void k_elong3(long long N, int ny, int nz, const double2* S, double2*
 }
 
 __global__ void k_tables3(int n, double d, double* x, double* q, double2* tw, float2* twf,
-                          double* mask, int n_abc, double strength) {
+                          float2* qb, double* mask, int n_abc, double strength) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
+  {
+    // the wavenumber of bit-reversed position j as an FP32 pair (the plane path's
+    // spectrum order)
+    int lg = 0;
+    while ((1 << lg) < n) ++lg;
+    const int jb = (int)(__brev((unsigned)j) >> (32 - lg));
+    const double qv = (jb <= n / 2 ? jb : jb - n) * (2.0 * kPi / (n * d));
+    const float hi = (float)qv;
+    qb[j] = make_float2(hi, (float)(qv - (double)hi));
+  }
   // GetSpaceArray: numpy linspace(-L/2, L/2, n) with L = (n - 1) d (typespace.py:815-849):
   // j * step + start, rounded as numpy does (no fused multiply-add), the last point = stop
   const double L = (n - 1) * d;
@@ -356,25 +368,30 @@ __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2
 __device__ __forceinline__ int brev(int p, int lg) { return lg ? (int)(__brev((unsigned)p) >> (32 - lg)) : 0; }
 
 // nl lines of n = 2^lg elements in shared memory, element p of line l at
-// a[l * ls + p * es]; tw[j] = exp(-2 pi i j / n), j < n / 2.  line_fast: consecutive
-// threads take consecutive lines (lines adjacent in memory), else consecutive
-// positions of one line.  Ends with __syncthreads.
-template <bool INV>
+// a[l * ls + p * es] (PAD: at a[i + i / 16] for that index i, one padding slot per 16
+// elements, so that the short spans of the last stages along a contiguous line do not
+// pile onto a few banks); tw[j] = exp(-2 pi i j / n), j < n / 2.  line_fast:
+// consecutive threads take consecutive lines (lines adjacent in memory), else
+// consecutive positions of one line.  Ends with __syncthreads.
+template <bool PAD>
+__device__ __forceinline__ int smi(int i) {
+  return PAD ? i + (i >> 4) : i;
+}
+
+template <bool INV, bool PAD>
 __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line_fast,
                             const float2* tw) {
   const int n = 1 << lg, npair = lg >> 1, q4 = n >> 2;
-  if (lg & 1) {
-    // the radix-2 stage of span 1 (twiddle 1): last for DIF, first for DIT
-    if (INV) {
-      for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
-        const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
-        float2* x = a + (long long)l * ls + 2 * b * es;
-        const float2 x0 = x[0], x1 = x[es];
-        x[0] = c_add(x0, x1);
-        x[es] = c_sub(x0, x1);
-      }
-      __syncthreads();
+  if ((lg & 1) && INV) {
+    // the radix-2 stage of span 1 (twiddle 1): first for DIT, last for DIF
+    for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
+      const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
+      const int i0 = l * ls + 2 * b * es;
+      const float2 x0 = a[smi<PAD>(i0)], x1 = a[smi<PAD>(i0 + es)];
+      a[smi<PAD>(i0)] = c_add(x0, x1);
+      a[smi<PAD>(i0 + es)] = c_sub(x0, x1);
     }
+    __syncthreads();
   }
   for (int t = 0; t < npair; ++t) {
     const int pi = INV ? npair - 1 - t : t;
@@ -383,9 +400,10 @@ __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line
     for (int u = threadIdx.x; u < nl * q4; u += blockDim.x) {
       const int l = line_fast ? u % nl : u / q4, r = line_fast ? u / nl : u % q4;
       const int j = r & (m - 1), p0 = ((r >> lgm) << (lgm + 2)) + j;
-      float2* x = a + (long long)l * ls + (long long)p0 * es;
-      const int sm = m * es;
-      const float2 x0 = x[0], x1 = x[sm], x2 = x[2 * sm], x3 = x[3 * sm];
+      const int sm = m * es, i0 = l * ls + p0 * es;
+      const int k0 = smi<PAD>(i0), k1 = smi<PAD>(i0 + sm), k2 = smi<PAD>(i0 + 2 * sm),
+                k3 = smi<PAD>(i0 + 3 * sm);
+      const float2 x0 = a[k0], x1 = a[k1], x2 = a[k2], x3 = a[k3];
       const float2 w1a = tw[j * tws], w1b = tw[(j + m) * tws], w2 = tw[2 * j * tws];
       float2 y0, y1, y2, y3;
       if (!INV) {
@@ -405,20 +423,20 @@ __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line
         y1 = c_add(a1, t4);
         y3 = c_sub(a1, t4);
       }
-      x[0] = y0;
-      x[sm] = y1;
-      x[2 * sm] = y2;
-      x[3 * sm] = y3;
+      a[k0] = y0;
+      a[k1] = y1;
+      a[k2] = y2;
+      a[k3] = y3;
     }
     __syncthreads();
   }
   if ((lg & 1) && !INV) {
     for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
       const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
-      float2* x = a + (long long)l * ls + 2 * b * es;
-      const float2 x0 = x[0], x1 = x[es];
-      x[0] = c_add(x0, x1);
-      x[es] = c_sub(x0, x1);
+      const int i0 = l * ls + 2 * b * es;
+      const float2 x0 = a[smi<PAD>(i0)], x1 = a[smi<PAD>(i0 + es)];
+      a[smi<PAD>(i0)] = c_add(x0, x1);
+      a[smi<PAD>(i0 + es)] = c_sub(x0, x1);
     }
     __syncthreads();
   }
@@ -431,7 +449,10 @@ struct PlaneArgs {
   const float2* twz;
 };
 
-// shared memory of a plane block: the plane, then the y and z twiddles (half each)
+// padded plane of P elements in shared memory
+__host__ __device__ inline long long plane_slots(long long P) { return P + (P >> 4); }
+
+// shared memory of a plane block: the padded plane, then the y and z twiddles (half each)
 __device__ __forceinline__ void plane_tables(const PlaneArgs& A, float2* sty, float2* stz) {
   for (int j = threadIdx.x; j < (A.ny >> 1); j += blockDim.x) sty[j] = A.twy[j];
   for (int j = threadIdx.x; j < (A.nz >> 1); j += blockDim.x) stz[j] = A.twz[j];
@@ -440,16 +461,17 @@ __device__ __forceinline__ void plane_tables(const PlaneArgs& A, float2* sty, fl
 // forward along z (rows of the plane) then y (columns)
 __device__ __forceinline__ void plane_forward(const PlaneArgs& A, float2* a, const float2* sty,
                                               const float2* stz) {
-  fft_inplace<false>(a, A.lgz, A.ny, A.nz, 1, false, stz);
-  fft_inplace<false>(a, A.lgy, A.nz, 1, A.nz, true, sty);
+  fft_inplace<false, true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
+  fft_inplace<false, true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
 }
 
 // pass A: plane (x = blockIdx.x, component blockIdx.y) of the FP64 field F -> W
+// (FP64 -> FP32 on the integer pipe: the FP64 pipe is ~1/64 of the FP32 rate here)
 __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, const double2* F,
                                                                 float2* W) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2* a = reinterpret_cast<float2*>(smraw);
-  float2* sty = a + A.P;
+  float2* sty = a + plane_slots(A.P);
   float2* stz = sty + (A.ny >> 1);
   const long long base = blockIdx.y * A.N + blockIdx.x * A.P;
   plane_tables(A, sty, stz);
@@ -464,19 +486,22 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, con
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = i0 + u * kPlaneThreads;
-      if (i < A.P) a[i] = make_float2((float)v[u].x, (float)v[u].y);
+      if (i < A.P) a[smi<true>(i)] = f64_to_f32(v[u]);
     }
   }
   __syncthreads();
   plane_forward(A, a, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[i];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi<true>(i)];
 }
 
 // pass B: the x lines of tl consecutive (y, z) columns of all three components;
-// shared memory [x][component][column]
+// shared memory [x][component][column].  qb*: the wavenumbers of the bit-reversed
+// positions as FP32 pairs (hi, lo): k f = fmaf(lo, f, hi f), one rounding per
+// product (an FP32 wavenumber alone is up to 6e-8 off, a fixed phase-velocity error
+// of its mode)
 __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W, int lgx, int tl,
-                                                         const float2* twx, const double* qx,
-                                                         const double* qy, const double* qz) {
+                                                         const float2* twx, const float2* qbx,
+                                                         const float2* qby, const float2* qbz) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = 1 << lgx, w3 = 3 * tl;
   float2* a = reinterpret_cast<float2*>(smraw);
@@ -489,24 +514,25 @@ __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W,
     a[idx] = W[f * A.N + px * A.P + b0 + c];
   }
   __syncthreads();
-  fft_inplace<false>(a, lgx, w3, 1, w3, true, stx);
+  fft_inplace<false, false>(a, lgx, w3, 1, w3, true, stx);
   for (int idx = threadIdx.x; idx < nx * tl; idx += blockDim.x) {
     const int px = idx / tl, c = idx - px * tl;
     const long long col = b0 + c;
     const int py = (int)(col >> A.lgz), pz = (int)(col & (A.nz - 1));
-    const double kx = qx[brev(px, lgx)], ky = qy[brev(py, A.lgy)], kz = qz[brev(pz, A.lgz)];
+    const float2 kx = qbx[px], ky = qby[py], kz = qbz[pz];
     float2* e = a + (size_t)px * w3 + c;
     const float2 fx = e[0], fy = e[tl], fz = e[2 * tl];
+    auto km = [](float2 k, float f) { return fmaf(k.y, f, k.x * f); };
     // i (k x F)
-    const double cxr = ky * fz.x - kz * fy.x, cxi = ky * fz.y - kz * fy.y;
-    const double cyr = kz * fx.x - kx * fz.x, cyi = kz * fx.y - kx * fz.y;
-    const double czr = kx * fy.x - ky * fx.x, czi = kx * fy.y - ky * fx.y;
-    e[0] = make_float2((float)-cxi, (float)cxr);
-    e[tl] = make_float2((float)-cyi, (float)cyr);
-    e[2 * tl] = make_float2((float)-czi, (float)czr);
+    const float cxr = km(ky, fz.x) - km(kz, fy.x), cxi = km(ky, fz.y) - km(kz, fy.y);
+    const float cyr = km(kz, fx.x) - km(kx, fz.x), cyi = km(kz, fx.y) - km(kx, fz.y);
+    const float czr = km(kx, fy.x) - km(ky, fx.x), czi = km(kx, fy.y) - km(ky, fx.y);
+    e[0] = make_float2(-cxi, cxr);
+    e[tl] = make_float2(-cyi, cyr);
+    e[2 * tl] = make_float2(-czi, czr);
   }
   __syncthreads();
-  fft_inplace<true>(a, lgx, w3, 1, w3, true, stx);
+  fft_inplace<true, false>(a, lgx, w3, 1, w3, true, stx);
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
     W[f * A.N + px * A.P + b0 + c] = a[idx];
@@ -516,21 +542,23 @@ __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W,
 // pass C: inverse along y and z of plane (x, component), then out (+)= ...: the
 // update of Upd (the masks per axis); with fwd_next the plane of the updated FP64
 // field continues as pass A of the next curl (W overwritten with its transform: the
-// block owns its plane of W)
+// block owns its plane of W).  The increment a v / N - ja J is formed in FP32 (v is
+// the FP32 transform; a / N and ja as FP32 pairs, J rounded to FP32 on the integer
+// pipe) and added to the FP64 field: one FP64 add per component; the mask multiplies
+// only where it is not 1.
 __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, float2* W, Upd U,
                                                                 int fwd_next) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2* a = reinterpret_cast<float2*>(smraw);
-  float2* sty = a + A.P;
+  float2* sty = a + plane_slots(A.P);
   float2* stz = sty + (A.ny >> 1);
   const int x = blockIdx.x;
   const long long base = blockIdx.y * A.N + x * A.P;
   plane_tables(A, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) a[i] = W[base + i];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) a[smi<true>(i)] = W[base + i];
   __syncthreads();
-  fft_inplace<true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
-  fft_inplace<true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
-  const double invN = 1.0 / (double)A.N;
+  fft_inplace<true, true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
+  fft_inplace<true, true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
   const double mx = U.m0 ? U.m0[x] : 1.0;
   for (int i0 = threadIdx.x; i0 < A.P; i0 += 2 * kPlaneThreads) {
     // both elements' FP64 loads before their updates
@@ -546,31 +574,29 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, flo
     for (int u = 0; u < 2; ++u) {
       const int i = i0 + u * kPlaneThreads;
       if (i >= A.P) continue;
-      const float2 v = a[i];
-      const double vx = (double)v.x * invN, vy = (double)v.y * invN;
-      double2 r;
-      if (U.store) {
-        r = make_double2(vx, vy);
-      } else {
-        r = make_double2(o[u].x + U.a * vx, o[u].y + U.a * vy);
-        if (U.J) {
-          r.x -= U.ja * jv[u].x;
-          r.y -= U.ja * jv[u].y;
-        }
+      const float2 v = a[smi<true>(i)];
+      float ix = fmaf(v.x, U.af[1], v.x * U.af[0]), iy = fmaf(v.y, U.af[1], v.y * U.af[0]);
+      if (U.J) {
+        const float2 jf = f64_to_f32(jv[u]);
+        ix -= fmaf(jf.x, U.jf[1], jf.x * U.jf[0]);
+        iy -= fmaf(jf.y, U.jf[1], jf.y * U.jf[0]);
       }
+      double2 r = make_double2(o[u].x + f32_to_f64(ix), o[u].y + f32_to_f64(iy));
       if (U.m0) {
         const double m = mx * U.m1[i >> A.lgz] * U.m2[i & (A.nz - 1)];
-        r.x *= m;
-        r.y *= m;
+        if (m != 1.0) {
+          r.x *= m;
+          r.y *= m;
+        }
       }
       U.out[base + i] = r;
-      if (fwd_next) a[i] = make_float2((float)r.x, (float)r.y);
+      if (fwd_next) a[smi<true>(i)] = f64_to_f32(r);
     }
   }
   if (!fwd_next) return;   // block-uniform
   __syncthreads();
   plane_forward(A, a, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[i];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi<true>(i)];
 }
 
 bool pow2(int v) { return v >= 2 && v <= 1024 && (v & (v - 1)) == 0; }
@@ -683,7 +709,7 @@ PlaneArgs plane_args(const SbePstd3* p) {
 }
 
 size_t plane_smem(const PlaneArgs& A) {
-  return sizeof(float2) * ((size_t)A.P + (A.ny >> 1) + (A.nz >> 1));
+  return sizeof(float2) * ((size_t)plane_slots(A.P) + (A.ny >> 1) + (A.nz >> 1));
 }
 
 // x-pass columns per block: the three components' x lines of tl columns within
@@ -707,7 +733,7 @@ int plane_pass_b(SbePstd3* p, cudaStream_t s) {
   const int tl = x_lines(p), nx = p->n[0];
   const size_t smem = sizeof(float2) * ((size_t)3 * nx * tl + (nx >> 1));
   k_x_curl_ip<<<(unsigned)(A.P / tl), kXThreads, smem, s>>>(
-      A, static_cast<float2*>(p->work), ilog2i(nx), tl, p->twf[0], p->q[0], p->q[1], p->q[2]);
+      A, static_cast<float2*>(p->work), ilog2i(nx), tl, p->twf[0], p->qb[0], p->qb[1], p->qb[2]);
   return cuda_check(cudaGetLastError(), "pstd3 x pass");
 }
 
@@ -731,6 +757,12 @@ Upd upd_for(SbePstd3* p, double2* out, double a, const double2* J, double ja, bo
     U.m1 = p->mask[1];
     U.m2 = p->mask[2];
   }
+  // FP32 pairs of the plane path: the curl arrives as N curl (N a power of two)
+  const double an = (store ? 1.0 : a) / (double)p->N;
+  U.af[0] = (float)an;
+  U.af[1] = (float)(an - (double)U.af[0]);
+  U.jf[0] = (float)ja;
+  U.jf[1] = (float)(ja - (double)U.jf[0]);
   return U;
 }
 
@@ -798,7 +830,7 @@ int sbe_pstd3_create(const SbePstd3Desc* d, void* stream, SbePstd3** out) {
   p->N = (long long)p->n[0] * p->n[1] * p->n[2];
   size_t tab = 0;
   for (int a = 0; a < 3; ++a)
-    tab += ((3 * sizeof(double) + sizeof(double2) + sizeof(float2)) * p->n[a] + 1024);
+    tab += ((3 * sizeof(double) + sizeof(double2) + 2 * sizeof(float2)) * p->n[a] + 1536);
   // work: ten FP64 complex fields (the longitudinal-field spectra; the curl uses three)
   const size_t work = sizeof(double2) * 10 * (size_t)p->N;
   if (cudaMalloc(&p->arena, tab + work) != cudaSuccess) {
@@ -819,8 +851,9 @@ int sbe_pstd3_create(const SbePstd3Desc* d, void* stream, SbePstd3** out) {
     p->mask[a] = reinterpret_cast<double*>(take(sizeof(double) * n));
     p->tw[a] = reinterpret_cast<double2*>(take(sizeof(double2) * n));
     p->twf[a] = reinterpret_cast<float2*>(take(sizeof(float2) * n));
+    p->qb[a] = reinterpret_cast<float2*>(take(sizeof(float2) * n));
     k_tables3<<<(n + 127) / 128, 128, 0, s>>>(n, p->d[a], p->x[a], p->q[a], p->tw[a], p->twf[a],
-                                             p->mask[a], p->n_abc[a], p->abc);
+                                             p->qb[a], p->mask[a], p->n_abc[a], p->abc);
   }
   p->work = take(work);
   int rc = cuda_check(cudaGetLastError(), "sbe_pstd3_create");

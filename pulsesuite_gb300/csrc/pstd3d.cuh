@@ -18,6 +18,7 @@ struct SbePstd3 {
   double* mask[3] = {nullptr, nullptr, nullptr};  // absorbing mask per axis
   double2* tw[3] = {nullptr, nullptr, nullptr};   // exp(-2 pi i j / n), j < n
   float2* twf[3] = {nullptr, nullptr, nullptr};
+  float2* qb[3] = {nullptr, nullptr, nullptr};    // q of bit-reversed positions, FP32 pairs
   void* work = nullptr;         // up to 10 fields of N complex (FP64) work
 };
 

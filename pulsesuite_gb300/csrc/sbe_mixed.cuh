@@ -74,6 +74,11 @@ static inline MixedAll* all_of(SbeCtx* c) { return static_cast<MixedAll*>(c->mix
 
 // GEMM kinds of a stage: exchange products (real), commutators (dP with the cross
 // terms of W and V), hi*hi products of W and V, sources
+// Slots of the context's G buffer (tot_mat FP32 complex each, indexed like the
+// packed state) that one stage's commutator GEMMs write: the hi*hi products of W and
+// V, the dP sums, the cross terms of W and V
+enum GSlot : int { G_W = 0, G_V = 1, G_DP = 2, G_WX = 3, G_VX = 4 };
+
 enum JobKind { JK_EXCH = 0, JK_FULL = 1, JK_HH = 2, JK_SRC = 3 };
 
 // The GEMM jobs of one kind for bucket m (its tile choice included).

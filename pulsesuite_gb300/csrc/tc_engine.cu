@@ -47,7 +47,7 @@ __device__ __forceinline__ EpiTile epi_tile(const GemmDesc& d, const EpiArgs& e,
 // accesses through generic pointers would otherwise serialise on the
 // shared-memory latency).
 __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int n0, float* re,
-                                               float* im, float2* scr) {
+                                               float* im, float2* scr, bool accumulate) {
   const int lane = threadIdx.x & 31;
   const int es = t.es;
   // ---- row pass
@@ -77,9 +77,20 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
   const long long rs = 2 * (long long)t.ld;
   if (t.kind == EPI_RAWF) {
     float2* o = t.of2 + base;
+    if (accumulate) {
+      // a later K part of a kseq tile: add to the running sum this thread stored
+      float2 pv[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i)
-      if (2 * i + rh < rmax) o[i * rs] = v[i];
+      for (int i = 0; i < 16; ++i)
+        if (2 * i + rh < rmax) pv[i] = o[i * rs];
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (2 * i + rh < rmax) o[i * rs] = make_float2(pv[i].x + v[i].x, pv[i].y + v[i].y);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (2 * i + rh < rmax) o[i * rs] = v[i];
+    }
   } else if (t.kind == EPI_F32 && t.unshear) {
     // row r = mrow0 + rh + 2i, diagonal n >> 1: complex column k2 = r + (n >> 1) -
     // (unshear - 1); consecutive lanes store consecutive floats of one row
@@ -113,8 +124,15 @@ __device__ __forceinline__ void epilogue_chunk(const EpiTile& t, int mrow0, int 
 // One output tile of the launch's tile list.
 struct TileInfo {
   int job, b, m0, n0, ks, kb_begin, nkb, n_iters;
+  int nparts;  // K parts run in sequence in this tile (kseq), else 1
   bool dead;   // exchange tile whose outputs all lie outside the un-sheared matrix
 };
+
+// K blocks [begin, end) of part p of nparts over all K blocks
+__device__ __forceinline__ void part_range(int nkb_all, int p, int nparts, int* b, int* e) {
+  *b = p * nkb_all / nparts;
+  *e = (p + 1) * nkb_all / nparts;
+}
 
 template <int BNT>
 __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) {
@@ -138,8 +156,10 @@ __device__ __forceinline__ TileInfo tile_info(const GemmLaunch& L, long long t) 
   r /= tm;
   ti.b = (int)(r % d.batch);
   ti.ks = (int)(r / d.batch);
-  // K blocks of this part
-  const int nkb_all = (d.K + BK - 1) / BK, ksplit = d.ksplit > 1 ? d.ksplit : 1;
+  // K blocks of this part (kseq: of the whole K range; the parts are cut in the loops)
+  const int nkb_all = (d.K + BK - 1) / BK;
+  const int ksplit = (d.ksplit > 1 && !d.kseq) ? d.ksplit : 1;
+  ti.nparts = (d.ksplit > 1 && d.kseq) ? d.ksplit : 1;
   int kb_begin = ti.ks * nkb_all / ksplit, kb_end = (ti.ks + 1) * nkb_all / ksplit;
   if (d.kskip) {
     // the sheared exchange operand is zero outside the band of this N tile
@@ -252,14 +272,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const uint32_t tx_bytes = (uint32_t)(npl * (A_TILE_BYTES + bbytes));
       int s = (int)(g % nstage);
       uint32_t ph = (uint32_t)((g / nstage) & 1);
-      for (int term = 0; ok && term < d.nterms && ti.nkb > 0; ++term) {
+      for (int part = 0; ok && part < ti.nparts; ++part) {
+      int kb0 = ti.kb_begin, nkb = ti.nkb;
+      if (ti.nparts > 1) {
+        int e_;
+        part_range(ti.nkb, part, ti.nparts, &kb0, &e_);
+        nkb = e_ - kb0;
+        kb0 += ti.kb_begin;
+      }
+      for (int term = 0; ok && term < d.nterms && nkb > 0; ++term) {
         const Term T = d.t[term];
         const __half* ga0 = d.A.ptr + ((long long)T.a_mat * d.A.nplanes * d.A.batch + ti.b) * sA +
-                            ((long long)ti.kb_begin * d.A.rows_pad + ti.m0) * BK;
+                            ((long long)kb0 * d.A.rows_pad + ti.m0) * BK;
         const __half* gb0 = d.B.ptr + ((long long)T.b_mat * d.B.nplanes * d.B.batch + ti.b) * sB +
-                            ((long long)ti.kb_begin * d.B.rows_pad + ti.n0) * BK;
+                            ((long long)kb0 * d.B.rows_pad + ti.n0) * BK;
         const long long pA = (long long)pstep * d.A.batch * sA, pB = (long long)pstep * d.B.batch * sB;
-        for (int kk = 0; kk < ti.nkb; ++kk, ++g) {
+        for (int kk = 0; kk < nkb; ++kk, ++g) {
           if (!mbar_wait(&empty[s], ph ^ 1u, err, abort_flag)) {
             ok = false;
             break;
@@ -279,6 +307,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
         }
       }
+      }
     }
     // no copy may still be landing in shared memory when the CTA exits: wait
     // (bounded) for the last stages issued
@@ -292,6 +321,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const uint32_t id_pos_full = idesc_f16(BM, MMA_N, 0), id_neg_full = idesc_f16(BM, MMA_N, 1);
     long long g = 0;
     bool ok = true;
+    int st = 0;   // accumulator sub-tiles issued (one per K part of a kseq tile)
     for (int lt = 0; ok; ++lt) {
       const int qs = lt & 3;
       if (!mbar_wait(&qfull[qs], (uint32_t)((lt >> 2) & 1), err, abort_flag)) break;
@@ -307,22 +337,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const bool narrow = !HH && nrem < BNT;
       const uint32_t id_pos = narrow ? idesc_f16(BM, (nrem + 15) & ~15, 0) : id_pos_full;
       const uint32_t id_neg = narrow ? idesc_f16(BM, (nrem + 15) & ~15, 1) : id_neg_full;
-      const int buf = lt % nbuf, use = lt / nbuf;
-      if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) break;
+      int s = (int)(g % nstage);
+      uint32_t ph = (uint32_t)((g / nstage) & 1);
+#pragma unroll 1
+      for (int part = 0; ok && part < ti.nparts; ++part, ++st) {
+      int nkb = ti.nkb;
+      if (ti.nparts > 1) {
+        int b_, e_;
+        part_range(ti.nkb, part, ti.nparts, &b_, &e_);
+        nkb = e_ - b_;
+      }
+      const int buf = st % nbuf, use = st / nbuf;
+      if (use > 0 && !mbar_wait(&tempty[buf], (uint32_t)((use - 1) & 1), err, abort_flag)) {
+        ok = false;
+        break;
+      }
       tc_fence_after();
       // accumulator columns of the tile: [re | im] (BNT each) at buf * 256
       const uint32_t acc_re = tmem + buf * 256, acc_im = acc_re + BNT;
       bool first = true;
-      int s = (int)(g % nstage);
-      uint32_t ph = (uint32_t)((g / nstage) & 1);
-      for (int term = 0; ok && term < d.nterms && ti.nkb > 0; ++term) {
+      for (int term = 0; ok && term < d.nterms && nkb > 0; ++term) {
         const Term T = d.t[term];
         const int sa_ = T.a_conj ? -1 : 1, sb_ = T.b_conj ? -1 : 1;
         const int s_rr = T.sign, s_ii = -T.sign * sa_ * sb_;
         const int s_ri = T.sign * sb_, s_ir = T.sign * sa_;
         const uint32_t irr = s_rr < 0 ? id_neg : id_pos, iii = s_ii < 0 ? id_neg : id_pos;
         const uint32_t iri = s_ri < 0 ? id_neg : id_pos, iir = s_ir < 0 ? id_neg : id_pos;
-        for (int kk = 0; kk < ti.nkb; ++kk, ++g) {
+        for (int kk = 0; kk < nkb; ++kk, ++g) {
           if (!mbar_wait(&full[s], ph, err, abort_flag)) {
             ok = false;
             break;
@@ -384,19 +425,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
         }
       }
-      // accumulators of this tile complete (a tile without K blocks leaves tensor
+      if (!ok) break;
+      // accumulators of this (sub-)tile complete (one without K blocks leaves tensor
       // memory untouched and its epilogue stores zeros)
-      if (ti.n_iters > 0)
+      if (nkb > 0 && d.nterms > 0)
         umma_commit(&tfull[buf]);
       else
         mbar_arrive(&tfull[buf]);
+      }
     }
   } else if (warp >= 2) {
     // ---------------- epilogue ----------------
     const int q = warp & 3;                 // TMEM lane quarter of this warp
     float2* scr = scr_all + (warp - 2) * (32 * 16);
     const int half = (warp - 2) >> 2;         // column half of the tile
-    for (int lt = 0;; ++lt) {
+    int st = 0;   // accumulator sub-tiles drained (one per K part of a kseq tile)
+    bool stop = false;
+    for (int lt = 0; !stop; ++lt) {
       const int qs = lt & 3;
       if (!mbar_wait(&qfull[qs], (uint32_t)((lt >> 2) & 1), err, abort_flag)) break;
       const int t = tq[qs];
@@ -406,13 +451,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const EpiArgs& e = L.job[ti.job].e;
-      const int buf = lt % nbuf, use = lt / nbuf;
       const int mrow0 = ti.m0 + 32 * q;
       const EpiTile et = epi_tile(d, e, ti.b, ti.ks);   // before the wait
-      if (!mbar_wait(&tfull[buf], (uint32_t)(use & 1), err, abort_flag)) break;
+#pragma unroll 1
+      for (int part = 0; part < ti.nparts; ++part, ++st) {
+      int nkb = ti.nkb;
+      if (ti.nparts > 1) {
+        int b_, e_;
+        part_range(ti.nkb, part, ti.nparts, &b_, &e_);
+        nkb = e_ - b_;
+      }
+      const int buf = st % nbuf, use = st / nbuf;
+      if (!mbar_wait(&tfull[buf], (uint32_t)(use & 1), err, abort_flag)) {
+        stop = true;
+        break;
+      }
       tc_fence_after();
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16) + buf * 256;
-      const bool have = ti.n_iters > 0;
+      const bool have = nkb > 0 && d.nterms > 0;
       constexpr int NCH = BNT / 32;   // 16-column chunks per column half
       for (int cc = 0; cc < NCH; ++cc) {
         const int c = half * NCH + cc;   // chunk of the tile
@@ -455,7 +511,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        epilogue_chunk(et, mrow0, ti.n0 + c * 16, re, im, scr);
+        epilogue_chunk(et, mrow0, ti.n0 + c * 16, re, im, scr, part > 0);
+      }
       }
     }
   }
@@ -552,8 +609,10 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
         if (d.t[i].b_conj) return fail(SBE_ERR_ARG, "tc_gemm: hi*hi mode takes B unconjugated");
     L.job[j] = jobs[j];
     L.tile_base[j] = nt;
+    if (d.kseq && (d.ksplit < 2 || jobs[j].e.kind != tc::EPI_RAWF))
+      return fail(SBE_ERR_ARG, "tc_gemm: K parts in sequence need split-K and FP32 complex output");
     nt += (long long)((d.N + bnt - 1) / bnt) * ((d.M + tc::BM - 1) / tc::BM) * d.batch *
-          (d.ksplit > 1 ? d.ksplit : 1);
+          (d.ksplit > 1 && !d.kseq ? d.ksplit : 1);
   }
   L.tile_base[njobs] = nt;
   if (nt == 0) return SBE_OK;

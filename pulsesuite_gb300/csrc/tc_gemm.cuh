@@ -124,9 +124,9 @@ struct GemmDesc {
   int nk_shear;               // exchange: Nk of the shear
   // Product modes.  MODE_FULL: hi*hi + hi*lo + lo*hi (N tile 256); with xonly set
   // (complex only) the hi*hi products are left out.  MODE_HH (complex only, B never
-  // conjugated): the hi*hi products alone, N tile 64, one FP32 accumulator per real
-  // product (rr, ri, ir, ii: one MMA of N = 128 per A plane over B's re and im
-  // tiles), summed in the epilogue; 256 TMEM columns, so two tiles in flight.  The tensor core's accumulation
+  // conjugated): the hi*hi products alone, N tile 128, one FP32 accumulator per real
+  // product (rr, ri, ir, ii: one MMA of N = 256 per A plane over B's re and im
+  // tiles), summed in the epilogue; 512 TMEM columns, one tile in flight.  The tensor core's accumulation
   // truncates at every MMA, so a product whose result is a small difference of
   // large sums (the W - W^H form of dC, dD) takes its hi*hi part in MODE_HH with
   // split-K (short truncating chains) and its hi*lo + lo*hi part, 2^-11 smaller,
@@ -140,6 +140,11 @@ struct GemmDesc {
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
   // written at out + ks * ks_stride (ksplit 0 counts as 1)
   int ksplit;
+  // with ksplit > 1 (EPI_RAWF only): the parts of an output tile run in sequence in
+  // one CTA, each its own accumulation chain, and the epilogue sums them in part
+  // order into one output, ((p0 + p1) + p2) + ..., in FP32 (the first part stores,
+  // each later part reads back what the same thread stored and adds to it)
+  int kseq;
   // N tile of MODE_FULL: 256 (0 = the default) or 128; with 128 a complex tile's
   // accumulators take 256 TMEM columns, so two tiles are in flight (the epilogue of
   // one overlaps the MMAs of the next) at twice the operand loads per output

@@ -277,12 +277,16 @@ def test_solver_leapfrog_100_steps_vs_golden(tmp_path, monkeypatch, batch):
         setattr(s, nm, g["init_" + nm])
     dt = float(g["dt"])
     for n in range(int(g["nsteps"])):
+        step_outs = {}
         for w in (1, 2):
             outs = [np.zeros(len(rr), complex) for _ in range(4)]
             s.QWCalculator(f[n, 0] + 0j, f[n, 1] + 0j, f[n, 2] + 0j, np.zeros(len(rr), complex),
                            rr, None, dt, w, *outs, [False], [False])
+            step_outs[w] = outs
+        # (batched: every wire's outputs are filled on the call for the last wire)
+        for w in (1, 2):
             if f"s{n}_w{w}_Pxx" in g:
-                for a, nm in zip(outs, ("Pxx", "Pyy", "Pzz", "Rho")):
+                for a, nm in zip(step_outs[w], ("Pxx", "Pyy", "Pzz", "Rho")):
                     assert rel(a, g[f"s{n}_w{w}_{nm}"]) < SCREEN, (n, w, nm)
     for nm in ("YY1", "YY2", "YY3", "CC1", "CC2", "CC3", "DD1", "DD2", "DD3"):
         assert rel(getattr(s, nm), g[f"end_{nm}"]) < SCREEN, nm
