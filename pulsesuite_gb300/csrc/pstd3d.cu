@@ -140,6 +140,7 @@ struct Upd {
   int nx, ny, nz;
   int store;               // 1: out = result / N (no update)
   float af[2], jf[2];      // the plane path's a / N and ja as FP32 pairs (hi, lo)
+  int nabc[3];             // absorbing widths: the mask is exactly 1 further inside
 };
 
 template <typename T>
@@ -367,29 +368,26 @@ __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2
 __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ int brev(int p, int lg) { return lg ? (int)(__brev((unsigned)p) >> (32 - lg)) : 0; }
 
-// nl lines of n = 2^lg elements in shared memory, element p of line l at
-// a[l * ls + p * es] (PAD: at a[i + i / 16] for that index i, one padding slot per 16
-// elements, so that the short spans of the last stages along a contiguous line do not
-// pile onto a few banks); tw[j] = exp(-2 pi i j / n), j < n / 2.  line_fast:
-// consecutive threads take consecutive lines (lines adjacent in memory), else
-// consecutive positions of one line.  Ends with __syncthreads.
-template <bool PAD>
-__device__ __forceinline__ int smi(int i) {
-  return PAD ? i + (i >> 4) : i;
-}
+// nl lines of n = 2^lg elements in shared memory, element p of line l at logical
+// index i = l * ls + p * es, stored at a[i + (i >> psh)] (psh > 0: one padding slot
+// after every 2^psh elements; the planes pad each row of nz, so that rows start on
+// successive banks); tw[j] = exp(-2 pi i j / n), j < n / 2.  line_fast: consecutive
+// threads take consecutive lines, else consecutive positions of one line.  Ends with
+// __syncthreads.
+__device__ __forceinline__ int smi(int i, int psh) { return psh ? i + (i >> psh) : i; }
 
-template <bool INV, bool PAD>
+template <bool INV>
 __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line_fast,
-                            const float2* tw) {
+                            const float2* tw, int psh) {
   const int n = 1 << lg, npair = lg >> 1, q4 = n >> 2;
   if ((lg & 1) && INV) {
     // the radix-2 stage of span 1 (twiddle 1): first for DIT, last for DIF
     for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
       const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
       const int i0 = l * ls + 2 * b * es;
-      const float2 x0 = a[smi<PAD>(i0)], x1 = a[smi<PAD>(i0 + es)];
-      a[smi<PAD>(i0)] = c_add(x0, x1);
-      a[smi<PAD>(i0 + es)] = c_sub(x0, x1);
+      const float2 x0 = a[smi(i0, psh)], x1 = a[smi(i0 + es, psh)];
+      a[smi(i0, psh)] = c_add(x0, x1);
+      a[smi(i0 + es, psh)] = c_sub(x0, x1);
     }
     __syncthreads();
   }
@@ -401,8 +399,8 @@ __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line
       const int l = line_fast ? u % nl : u / q4, r = line_fast ? u / nl : u % q4;
       const int j = r & (m - 1), p0 = ((r >> lgm) << (lgm + 2)) + j;
       const int sm = m * es, i0 = l * ls + p0 * es;
-      const int k0 = smi<PAD>(i0), k1 = smi<PAD>(i0 + sm), k2 = smi<PAD>(i0 + 2 * sm),
-                k3 = smi<PAD>(i0 + 3 * sm);
+      const int k0 = smi(i0, psh), k1 = smi(i0 + sm, psh), k2 = smi(i0 + 2 * sm, psh),
+                k3 = smi(i0 + 3 * sm, psh);
       const float2 x0 = a[k0], x1 = a[k1], x2 = a[k2], x3 = a[k3];
       const float2 w1a = tw[j * tws], w1b = tw[(j + m) * tws], w2 = tw[2 * j * tws];
       float2 y0, y1, y2, y3;
@@ -434,9 +432,9 @@ __device__ void fft_inplace(float2* a, int lg, int nl, int ls, int es, bool line
     for (int u = threadIdx.x; u < nl * (n >> 1); u += blockDim.x) {
       const int l = line_fast ? u % nl : u / (n >> 1), b = line_fast ? u / nl : u % (n >> 1);
       const int i0 = l * ls + 2 * b * es;
-      const float2 x0 = a[smi<PAD>(i0)], x1 = a[smi<PAD>(i0 + es)];
-      a[smi<PAD>(i0)] = c_add(x0, x1);
-      a[smi<PAD>(i0 + es)] = c_sub(x0, x1);
+      const float2 x0 = a[smi(i0, psh)], x1 = a[smi(i0 + es, psh)];
+      a[smi(i0, psh)] = c_add(x0, x1);
+      a[smi(i0 + es, psh)] = c_sub(x0, x1);
     }
     __syncthreads();
   }
@@ -450,7 +448,7 @@ struct PlaneArgs {
 };
 
 // padded plane of P elements in shared memory
-__host__ __device__ inline long long plane_slots(long long P) { return P + (P >> 4); }
+__host__ __device__ inline long long plane_slots(long long P, int lgz) { return P + (P >> lgz); }
 
 // shared memory of a plane block: the padded plane, then the y and z twiddles (half each)
 __device__ __forceinline__ void plane_tables(const PlaneArgs& A, float2* sty, float2* stz) {
@@ -461,8 +459,10 @@ __device__ __forceinline__ void plane_tables(const PlaneArgs& A, float2* sty, fl
 // forward along z (rows of the plane) then y (columns)
 __device__ __forceinline__ void plane_forward(const PlaneArgs& A, float2* a, const float2* sty,
                                               const float2* stz) {
-  fft_inplace<false, true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
-  fft_inplace<false, true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
+  // both directions with consecutive threads on consecutive lines: along z the lines
+  // are the padded rows (successive banks), along y the adjacent columns
+  fft_inplace<false>(a, A.lgz, A.ny, A.nz, 1, true, stz, A.lgz);
+  fft_inplace<false>(a, A.lgy, A.nz, 1, A.nz, true, sty, A.lgz);
 }
 
 // pass A: plane (x = blockIdx.x, component blockIdx.y) of the FP64 field F -> W
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, con
                                                                 float2* W) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2* a = reinterpret_cast<float2*>(smraw);
-  float2* sty = a + plane_slots(A.P);
+  float2* sty = a + plane_slots(A.P, A.lgz);
   float2* stz = sty + (A.ny >> 1);
   const long long base = blockIdx.y * A.N + blockIdx.x * A.P;
   plane_tables(A, sty, stz);
@@ -486,12 +486,12 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, con
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = i0 + u * kPlaneThreads;
-      if (i < A.P) a[smi<true>(i)] = f64_to_f32(v[u]);
+      if (i < A.P) a[smi(i, A.lgz)] = f64_to_f32(v[u]);
     }
   }
   __syncthreads();
   plane_forward(A, a, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi<true>(i)];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi(i, A.lgz)];
 }
 
 // pass B: the x lines of tl consecutive (y, z) columns of all three components;
@@ -509,12 +509,23 @@ __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W,
   for (int j = threadIdx.x; j < (nx >> 1); j += blockDim.x) stx[j] = twx[j];
   const long long b0 = (long long)blockIdx.x * tl;
   const int total = nx * w3;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
-    a[idx] = W[f * A.N + px * A.P + b0 + c];
+  // four loads of a thread in flight before their stores to shared memory
+  for (int i0 = threadIdx.x; i0 < total; i0 += 4 * kXThreads) {
+    float2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = i0 + u * kXThreads;
+      if (idx < total) {
+        const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
+        v[u] = W[f * A.N + px * A.P + b0 + c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u * kXThreads < total) a[i0 + u * kXThreads] = v[u];
   }
   __syncthreads();
-  fft_inplace<false, false>(a, lgx, w3, 1, w3, true, stx);
+  fft_inplace<false>(a, lgx, w3, 1, w3, true, stx, 0);
   for (int idx = threadIdx.x; idx < nx * tl; idx += blockDim.x) {
     const int px = idx / tl, c = idx - px * tl;
     const long long col = b0 + c;
@@ -532,7 +543,7 @@ __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W,
     e[2 * tl] = make_float2(-czi, czr);
   }
   __syncthreads();
-  fft_inplace<true, false>(a, lgx, w3, 1, w3, true, stx);
+  fft_inplace<true>(a, lgx, w3, 1, w3, true, stx, 0);
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     const int px = idx / w3, r = idx - px * w3, f = r / tl, c = r - f * tl;
     W[f * A.N + px * A.P + b0 + c] = a[idx];
@@ -550,16 +561,17 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, flo
                                                                 int fwd_next) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2* a = reinterpret_cast<float2*>(smraw);
-  float2* sty = a + plane_slots(A.P);
+  float2* sty = a + plane_slots(A.P, A.lgz);
   float2* stz = sty + (A.ny >> 1);
   const int x = blockIdx.x;
   const long long base = blockIdx.y * A.N + x * A.P;
   plane_tables(A, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) a[smi<true>(i)] = W[base + i];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) a[smi(i, A.lgz)] = W[base + i];
   __syncthreads();
-  fft_inplace<true, true>(a, A.lgy, A.nz, 1, A.nz, true, sty);
-  fft_inplace<true, true>(a, A.lgz, A.ny, A.nz, 1, false, stz);
+  fft_inplace<true>(a, A.lgy, A.nz, 1, A.nz, true, sty, A.lgz);
+  fft_inplace<true>(a, A.lgz, A.ny, A.nz, 1, true, stz, A.lgz);
   const double mx = U.m0 ? U.m0[x] : 1.0;
+  const bool xin = min(x, A.nx - 1 - x) >= U.nabc[0];
   for (int i0 = threadIdx.x; i0 < A.P; i0 += 2 * kPlaneThreads) {
     // both elements' FP64 loads before their updates
     double2 o[2], jv[2];
@@ -574,7 +586,7 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, flo
     for (int u = 0; u < 2; ++u) {
       const int i = i0 + u * kPlaneThreads;
       if (i >= A.P) continue;
-      const float2 v = a[smi<true>(i)];
+      const float2 v = a[smi(i, A.lgz)];
       float ix = fmaf(v.x, U.af[1], v.x * U.af[0]), iy = fmaf(v.y, U.af[1], v.y * U.af[0]);
       if (U.J) {
         const float2 jf = f64_to_f32(jv[u]);
@@ -583,20 +595,22 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, flo
       }
       double2 r = make_double2(o[u].x + f32_to_f64(ix), o[u].y + f32_to_f64(iy));
       if (U.m0) {
-        const double m = mx * U.m1[i >> A.lgz] * U.m2[i & (A.nz - 1)];
-        if (m != 1.0) {
+        // FP64 only inside the absorbing layers (integer test of the position)
+        const int y = i >> A.lgz, z = i & (A.nz - 1);
+        if (!xin || min(y, A.ny - 1 - y) < U.nabc[1] || min(z, A.nz - 1 - z) < U.nabc[2]) {
+          const double m = mx * U.m1[y] * U.m2[z];
           r.x *= m;
           r.y *= m;
         }
       }
       U.out[base + i] = r;
-      if (fwd_next) a[smi<true>(i)] = f64_to_f32(r);
+      if (fwd_next) a[smi(i, A.lgz)] = f64_to_f32(r);
     }
   }
   if (!fwd_next) return;   // block-uniform
   __syncthreads();
   plane_forward(A, a, sty, stz);
-  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi<true>(i)];
+  for (int i = threadIdx.x; i < A.P; i += kPlaneThreads) W[base + i] = a[smi(i, A.lgz)];
 }
 
 bool pow2(int v) { return v >= 2 && v <= 1024 && (v & (v - 1)) == 0; }
@@ -709,7 +723,7 @@ PlaneArgs plane_args(const SbePstd3* p) {
 }
 
 size_t plane_smem(const PlaneArgs& A) {
-  return sizeof(float2) * ((size_t)plane_slots(A.P) + (A.ny >> 1) + (A.nz >> 1));
+  return sizeof(float2) * ((size_t)plane_slots(A.P, A.lgz) + (A.ny >> 1) + (A.nz >> 1));
 }
 
 // x-pass columns per block: the three components' x lines of tl columns within
@@ -757,6 +771,7 @@ Upd upd_for(SbePstd3* p, double2* out, double a, const double2* J, double ja, bo
     U.m1 = p->mask[1];
     U.m2 = p->mask[2];
   }
+  for (int ax = 0; ax < 3; ++ax) U.nabc[ax] = p->n_abc[ax];
   // FP32 pairs of the plane path: the curl arrives as N curl (N a power of two)
   const double an = (store ? 1.0 : a) / (double)p->N;
   U.af[0] = (float)an;
