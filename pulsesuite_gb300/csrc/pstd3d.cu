@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_fwd(PlaneArgs A, con
 
 // pass B: the x lines of tl consecutive (y, z) columns of all three components;
 // shared memory [x][component][column].  qb*: the wavenumbers of the bit-reversed
-// positions as FP32 pairs (hi, lo): k f = fmaf(lo, f, hi f), one rounding per
+// positions as FP32 pairs (hi, lo): k f = fmaf(hi, f, lo f), one rounding per
 // product (an FP32 wavenumber alone is up to 6e-8 off, a fixed phase-velocity error
 // of its mode)
 __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W, int lgx, int tl,
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(kXThreads) k_x_curl_ip(PlaneArgs A, float2* W,
     const float2 kx = qbx[px], ky = qby[py], kz = qbz[pz];
     float2* e = a + (size_t)px * w3 + c;
     const float2 fx = e[0], fy = e[tl], fz = e[2 * tl];
-    auto km = [](float2 k, float f) { return fmaf(k.y, f, k.x * f); };
+    auto km = [](float2 k, float f) { return fmaf(k.x, f, k.y * f); };
     // i (k x F)
     const float cxr = km(ky, fz.x) - km(kz, fy.x), cxi = km(ky, fz.y) - km(kz, fy.y);
     const float cyr = km(kz, fx.x) - km(kx, fz.x), cyi = km(kz, fx.y) - km(kx, fz.y);
@@ -587,11 +587,11 @@ __global__ void __launch_bounds__(kPlaneThreads, 1) k_plane_inv(PlaneArgs A, flo
       const int i = i0 + u * kPlaneThreads;
       if (i >= A.P) continue;
       const float2 v = a[smi(i, A.lgz)];
-      float ix = fmaf(v.x, U.af[1], v.x * U.af[0]), iy = fmaf(v.y, U.af[1], v.y * U.af[0]);
+      float ix = fmaf(v.x, U.af[0], v.x * U.af[1]), iy = fmaf(v.y, U.af[0], v.y * U.af[1]);
       if (U.J) {
         const float2 jf = f64_to_f32(jv[u]);
-        ix -= fmaf(jf.x, U.jf[1], jf.x * U.jf[0]);
-        iy -= fmaf(jf.y, U.jf[1], jf.y * U.jf[0]);
+        ix -= fmaf(jf.x, U.jf[0], jf.x * U.jf[1]);
+        iy -= fmaf(jf.y, U.jf[0], jf.y * U.jf[1]);
       }
       double2 r = make_double2(o[u].x + f32_to_f64(ix), o[u].y + f32_to_f64(iy));
       if (U.m0) {

@@ -1219,7 +1219,10 @@ __device__ __forceinline__ float2 two_sum(float a, float b) {
 // The step's scale (dt / 2 or dt for the stage states, dt / 6 for the final sum)
 // enters as an unevaluated FP32 pair fh + fl: an FP32-rounded dt would be the same
 // relative error every step, i.e. a slightly different time step whose phase error
-// grows with the number of oscillation periods of the state.
+// grows with the number of oscillation periods of the state.  A pair product is
+// fmaf(hi, x, lo x): the small term first, then one rounding of x hi + lo x (rounding
+// x hi first would lose the correction in most cases and leave the constant's error
+// as a bias).
 struct Rk4Ctl {
   int stage, peel;
   float fh, fl;
@@ -1242,7 +1245,7 @@ __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, flo
       r.acc[i] = make_float2(a.x + 2.f * kv.x, a.y + 2.f * kv.y);
     }
     const float2 xs = r.x0[i];   // fp32 of the FP64 state, converted once per step
-    const float2 fk = make_float2(fmaf(r.fl, kv.x, r.fh * kv.x), fmaf(r.fl, kv.y, r.fh * kv.y));
+    const float2 fk = make_float2(fmaf(r.fh, kv.x, r.fl * kv.x), fmaf(r.fh, kv.y, r.fl * kv.y));
     const float2 v = make_float2(xs.x + fk.x, xs.y + fk.y);
     r.xf[i] = v;
     if (diag && r.dg) r.dg[dgi] = r.X[i].x + f32_to_f64(fk.x);
@@ -1251,8 +1254,8 @@ __device__ __forceinline__ unsigned rk4_update(const Rk4Ctl& r, long long i, flo
   const double2 x = r.X[i];
   const float2 a = r.acc[i];
   const float sx = a.x + kv.x, sy = a.y + kv.y;
-  const double2 v = make_double2(x.x + f32_to_f64(fmaf(r.fl, sx, r.fh * sx)),
-                                 x.y + f32_to_f64(fmaf(r.fl, sy, r.fh * sy)));
+  const double2 v = make_double2(x.x + f32_to_f64(fmaf(r.fh, sx, r.fl * sx)),
+                                 x.y + f32_to_f64(fmaf(r.fh, sy, r.fl * sy)));
   r.X[i] = v;
   return bits_to_fmax(max(absbits(v.x), absbits(v.y)));
 }
@@ -1369,10 +1372,10 @@ __global__ void __launch_bounds__(256) k_antiherm(
       const float di = (gjh.y - gih.y) + (gjl.y - gil.y);
       const float dc = (cv[0][0][r] - cjh) + (cv[0][1][r] - cjl);
       const float re = (a.x - bt.x) + dc * hji.x +
-                       ((dh.x * x[q].x - di * x[q].y) + drl * x[q].x);
+                       fmaf(dh.x, x[q].x, fmaf(drl, x[q].x, -di * x[q].y));
       const float im = (a.y + bt.y) + dc * hji.y +
-                       ((dh.x * x[q].y + di * x[q].x) + drl * x[q].y);
-      const float2 v = make_float2(fmaf(im, ihl, im * ihh), -fmaf(re, ihl, re * ihh));
+                       fmaf(dh.x, x[q].y, fmaf(drl, x[q].y, di * x[q].x));
+      const float2 v = make_float2(fmaf(im, ihh, im * ihl), -fmaf(re, ihh, re * ihl));
       vt[r][tx] = v;
       if (i < nk && j < nk && (bi < bj || j >= i)) {
         const long long o = mb + (long long)i * nk + j;
@@ -1477,11 +1480,11 @@ __global__ void __launch_bounds__(256) k_rhs_p(
     const float2 gh = rg[0][r], gl = rg[1][r];
     const float2 sh = two_sum(gh.x, eh.x);                 // exact sum of the hi parts
     const float derl = sh.y + (gl.x + el.x), dei = (gh.y + eh.y) + (gl.y + el.y);
-    const float ar = ax + ((sh.x * x[q].x - dei * x[q].y) + derl * x[q].x);
-    const float ai = ay + ((sh.x * x[q].y + dei * x[q].x) + derl * x[q].y);
+    const float ar = ax + fmaf(sh.x, x[q].x, fmaf(derl, x[q].x, -dei * x[q].y));
+    const float ai = ay + fmaf(sh.x, x[q].y, fmaf(derl, x[q].y, dei * x[q].x));
     const float gam = gamE + rv[0][r];
-    const float2 kv = make_float2(fmaf(ai, ihl, ai * ihh) - gam * x[q].x,
-                                  -fmaf(ar, ihl, ar * ihh) - gam * x[q].y);
+    const float2 kv = make_float2(fmaf(ai, ihh, ai * ihl) - gam * x[q].x,
+                                  -fmaf(ar, ihh, ar * ihl) - gam * x[q].y);
     const long long o = mb + (long long)m * nk + n;
     if (rk.stage == 0) {
       out[o] = kv;
