@@ -518,9 +518,9 @@ def gpu_arm(args, wl):
     # products = 96 Nk^3 flop per wire
     useful = 96.0 * nk ** 3 * nw
     # executed per wire, in 2 Nk^3 real-product MMA chains: dP 4 complex terms x 4 real
-    # products x 3 hi/lo terms = 48; W, V 2 complex terms each x 4 x (hi*lo, lo*hi,
-    # lo*lo) = 48; their hi*hi products 16: 112 x 2 Nk^3 = 224 Nk^3
-    executed = 224.0 * nk ** 3 * nw
+    # products x 3 hi/lo terms = 48; W, V 2 complex terms each x 4 x (hi*lo, lo*hi) =
+    # 32; their hi*hi products 16: 96 x 2 Nk^3 = 192 Nk^3
+    executed = 192.0 * nk ** 3 * nw
     achieved = useful / per_eval_s / 1e12
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     roof = {"bound": "tensor", "kernel": "k_tc_gemm (commutator dP/dC/dD)", "achieved": achieved,
@@ -537,10 +537,11 @@ def gpu_arm(args, wl):
                             "scaled by wires; a constant of this file, refreshed with the profile",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
                            "12 complex Nk^3 products) over the summed CUDA-event time of the "
-                           "evaluation's two commutator launches (dP with the hi*lo + lo*hi + "
-                           "lo*lo products of W and V; the hi*hi products of W and V in K parts "
-                           "with one accumulator per real product); executed 224*Nk^3 (dP 96, "
-                           "W and V cross terms 96, their hi*hi products 32); step: 496*Nk^3 "
+                           "evaluation's two commutator launches (dP with the hi*lo + lo*hi "
+                           "products of W and V; the hi*hi products of W and V in K parts with "
+                           "one accumulator per real product, added to them in order); executed "
+                           "192*Nk^3 (dP 96, W and V cross terms 64, their hi*hi products 32); "
+                           "step: 496*Nk^3 "
                            "algorithmic flop per wire-step (4 evaluations of a1-a3 and the "
                            "exchange and source products) over the step time",
             "step_tflops": 496.0 * nk ** 3 * value / 1e12,

@@ -251,7 +251,7 @@ int sbe_graph_destroy(SbeGraph* g);
  * context's (Nk, wires) buckets: a later call with a matching entry loads it and
  * times nothing.  Without a call every GEMM uses the 256 tile.  Synchronises the
  * device; not capturable.  A cache entry may also set "hh_split" (1-4; default 2
- * below Nk = 512, else 4): the K parts of the hi*hi products of the anti-Hermitian
+ * below Nk = 256, else 4): the K parts of the hi*hi products of the anti-Hermitian
  * W, V (shorter truncating FP32 chains: accuracy, not speed, so the tuner records
  * it but does not time it).
  * sbe_ctx_tiles: per bucket (ascending Nk) 6 ints (Nk, wires, exchange tile,

@@ -82,7 +82,7 @@ bool load(const char* path, const std::string& key, MixedAll* A) {
       // optional hi*hi split of this bucket (before the next bucket's entry)
       const size_t next = line.find(tag, pos + tag.size());
       const size_t hp = line.find(htag, pos);
-      int hs = nk >= 512 ? 4 : 2;   // the default of mixed_ensure
+      int hs = nk >= 256 ? 4 : 2;   // the default of mixed_ensure
       if (hp != std::string::npos && (next == std::string::npos || hp < next) &&
           std::sscanf(line.c_str() + hp + htag.size(), "%d", &hs) != 1)
         return false;

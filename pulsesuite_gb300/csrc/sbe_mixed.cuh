@@ -18,8 +18,8 @@ struct Mixed {
   // sbe_autotune
   int bn[4] = {0, 0, 0, 0};
   // K parts of the hi*hi products of W and V (split-K: shorter truncating FP32
-  // chains; the parts meet in the anti-Hermitian pass); 1 to 4, by default 2 below
-  // Nk = 512 and 4 from there on
+  // chains; the parts are summed in order by the GEMM epilogue); 1 to 4, by default 2
+  // below Nk = 256 and 4 from there on
   int hs = 2;
   tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
   float* xsh = nullptr;    // exchange sums, un-sheared: 3 x Nw x Nk x Nk complex (FP32)
@@ -75,9 +75,9 @@ static inline MixedAll* all_of(SbeCtx* c) { return static_cast<MixedAll*>(c->mix
 // GEMM kinds of a stage: exchange products (real), commutators (dP with the cross
 // terms of W and V), hi*hi products of W and V, sources
 // Slots of the context's G buffer (tot_mat FP32 complex each, indexed like the
-// packed state) that one stage's commutator GEMMs write: the hi*hi products of W and
-// V, the dP sums, the cross terms of W and V
-enum GSlot : int { G_W = 0, G_V = 1, G_DP = 2, G_WX = 3, G_VX = 4 };
+// packed state) that one stage's commutator GEMMs write: W, V (cross terms from the dP
+// launch, hi*hi parts added by the hi*hi launch) and the dP sums
+enum GSlot : int { G_W = 0, G_V = 1, G_DP = 2 };
 
 enum JobKind { JK_EXCH = 0, JK_FULL = 1, JK_HH = 2, JK_SRC = 3 };
 

@@ -459,9 +459,9 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
     m->bv = W0.off_vec;
     m->br = W0.off_r;
     m->bkr = W0.off_kr;
-    // four K parts from Nk = 512 on: the hi*hi chains of 512 and more long K ranges
-    // set the truncation error of W - W^H (the autotuner's cache may override)
-    m->hs = W0.nk >= 512 ? 4 : 2;
+    // four K parts from Nk = 256 on: the hi*hi chains of long K ranges set the
+    // truncation error of W - W^H (the autotuner's cache may override)
+    m->hs = W0.nk >= 256 ? 4 : 2;
     A->b.push_back(m);
     i = j;
   }
@@ -1293,11 +1293,11 @@ __device__ __forceinline__ void rk4_block_max(const Rk4Ctl& r, int b, unsigned m
 // occupations differ exactly), so it does not carry the GEMM's rounding.  The
 // result is exactly anti-Hermitian, which keeps C and D Hermitian.  A block owns
 // the tile pair (bi, bj), (bj, bi) with bi <= bj and reads each W and H' element
-// once.  W arrives as two FP32 partials (the hi*hi products, their K parts summed in
-// order by the GEMM's epilogue, and the hi*lo + lo*hi + lo*lo products); g[j] - g[i]
-// comes from the hi / lo FP32 parts of g.
+// once.  W arrives in FP32 from the GEMMs (the hi*lo + lo*hi products, to
+// which the hi*hi launch adds its K parts in order); g[j] - g[i] comes from the hi /
+// lo FP32 parts of g.
 __global__ void __launch_bounds__(256) k_antiherm(
-    int nk, const float2* __restrict__ W, const float2* __restrict__ W3, const float2* __restrict__ Hp, const float2* X,
+    int nk, const float2* __restrict__ W, const float2* __restrict__ Hp, const float2* X,
     const float2* __restrict__ ghi, const float2* __restrict__ glo, const float* __restrict__ chi,
     const float* __restrict__ clo, float2* out, Rk4Ctl rk) {
   // tb / hb: W and H' of the mirror tile (rows j0.., columns i0..); vt: results;
@@ -1318,8 +1318,7 @@ __global__ void __launch_bounds__(256) k_antiherm(
     cv[ty][0][tx] = chi[v];
     cv[ty][1][tx] = clo[v];
   }
-  // the mirror tile: four rows per thread, loads issued together; W is the sum of the
-  // hi*hi products and the cross terms
+  // the mirror tile: four rows per thread, loads issued together
   {
     float2 w[4], h[4];
 #pragma unroll
@@ -1328,8 +1327,6 @@ __global__ void __launch_bounds__(256) k_antiherm(
       const bool ok = ib < nk && jb < nk;
       const long long ob = mb + (long long)(ok ? ib : 0) * nk + (ok ? jb : 0);
       w[q] = W[ob];
-      const float2 x3 = W3[ob];
-      w[q] = make_float2(w[q].x + x3.x, w[q].y + x3.y);
       h[q] = Hp[ob];
       if (!ok) w[q] = h[q] = make_float2(0.f, 0.f);
     }
@@ -1353,8 +1350,6 @@ __global__ void __launch_bounds__(256) k_antiherm(
       const bool ok = i < nk && j < nk;
       const long long oa = mb + (long long)(ok ? i : 0) * nk + (ok ? j : 0);
       w[q] = W[oa];
-      const float2 x3 = W3[oa];
-      w[q] = make_float2(w[q].x + x3.x, w[q].y + x3.y);
       x[q] = X[oa];
     }
     const float2 gjh = gv[1][0][tx], gjl = gv[1][1][tx];
@@ -1575,9 +1570,9 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
                             {M_P, M_EEX, 0, 0, 1}, {M_EHT, M_C, 0, 1, -1}};
     const tc::Term tC[2] = {{M_C, M_EE, 0, 0, 1}, {M_PT, M_EH, 1, 0, 1}};
     const tc::Term tD[2] = {{M_D, M_HH, 0, 0, 1}, {M_P, M_EHT, 1, 0, 1}};
-    // G buffer (FP32 complex, tot_mat each, indexed like the packed state): [W hh
-    // (its K parts summed in the engine's epilogue), V hh, dP sums, W cross terms, V
-    // cross terms]
+    // G buffer (FP32 complex, tot_mat each, indexed like the packed state): [W, V, dP
+    // sums]: the dP launch writes the cross terms of W and V, the hi*hi launch that
+    // follows adds its K parts to them in order
     float2* wf = reinterpret_cast<float2*>(c->G);   // the buffer holds 12 tot_mat float2
     const int hs = m->hs;
     auto epi = [&](float2* o) {
@@ -1592,12 +1587,11 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
     };
     if (kind == JK_FULL) {
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 4, tP, 0, epi(wf + G_DP * tm)));
-      // the cross terms of W and V with their lo*lo products
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + G_WX * tm),
+      // the hi*lo + lo*hi products of W and V
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + G_W * tm),
                         tc::MODE_FULL, 1));
-      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + G_VX * tm),
+      out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + G_V * tm),
                         tc::MODE_FULL, 1));
-      out[out.size() - 1].d.lolo = out[out.size() - 2].d.lolo = 1;
     } else {
       // the K parts of a tile in sequence in one CTA, summed by its epilogue
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tC, 0, epi(wf + G_W * tm), tc::MODE_HH,
@@ -1605,6 +1599,7 @@ void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
       out.push_back(job(m, m->pl, m->pl, nk, nk, nk, 1, 2, tD, 0, epi(wf + G_V * tm), tc::MODE_HH,
                         0, hs));
       out[out.size() - 1].d.kseq = out[out.size() - 2].d.kseq = hs > 1 ? 1 : 0;
+      out[out.size() - 1].d.kacc = out[out.size() - 2].d.kacc = 1;
     }
   } else {
     float2* gf = reinterpret_cast<float2*>(c->G);
@@ -1793,8 +1788,6 @@ static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const dou
     const float2 *P = xs + o, *C = xs + tm + o, *D = xs + 2 * tm + o;
     // this bucket's slices of the G buffer (see bucket_jobs)
     const float2* gp = wf + G_DP * tm;
-    const float2* wx = wf + G_WX * tm;
-    const float2* vx = wf + G_VX * tm;
     Rk4Ctl rk[3];
     for (int i = 0; i < 3; ++i) {
       rk[i] = Rk4Ctl{};
@@ -1815,9 +1808,9 @@ static int mixed_stage(SbeCtx* c, const float2* xs, const double2* Ek, const dou
     const dim3 ag((nk + 31) / 32, (nk + 31) / 32, nw), ab(32, 8);
     k_rhs_p<<<ag, ab, 0, s>>>(nk, nw, gp + o, A->hf + o, P, m->dgf, m->gamf, m->cdf, A->kf + o,
                               rk[0]);
-    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + G_W * tm + o, wx + o, A->hf + tm + o, C, m->dgf,
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + G_W * tm + o, A->hf + tm + o, C, m->dgf,
                                  m->dgf + vn, m->cdf, m->cdf + vn, A->kf + tm + o, rk[1]);
-    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + G_V * tm + o, vx + o, A->hf + 2 * tm + o, D,
+    k_antiherm<<<ag, ab, 0, s>>>(nk, wf + G_V * tm + o, A->hf + 2 * tm + o, D,
                                  m->dgf + 2 * vn, m->dgf + 3 * vn, m->cdf + 2 * vn,
                                  m->cdf + 3 * vn, A->kf + 2 * tm + o, rk[2]);
   }

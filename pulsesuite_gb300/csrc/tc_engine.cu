@@ -331,7 +331,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const TileInfo ti = tile_info<BNT>(L, t);
       const GemmDesc& d = L.job[ti.job].d;
       const bool hh = !d.xonly;
-      const bool lolo = d.lolo != 0;
       // a last N tile narrower than BNT (MODE_FULL): MMAs of N rounded up to 16
       const int nrem = d.N - ti.n0;
       const bool narrow = !HH && nrem < BNT;
@@ -409,12 +408,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               umma_f16(acc_im, A(1), B(2), iri, 1u);
               umma_f16(acc_im, A(2), B(1), iir, 1u);
               umma_f16(acc_im, A(3), B(0), iir, 1u);
-              if (lolo) {
-                umma_f16(acc_re, A(1), B(1), irr, 1u);
-                umma_f16(acc_re, A(3), B(3), iii, 1u);
-                umma_f16(acc_im, A(1), B(3), iri, 1u);
-                umma_f16(acc_im, A(3), B(1), iir, 1u);
-              }
             }
             first = false;
           }
@@ -511,7 +504,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        epilogue_chunk(et, mrow0, ti.n0 + c * 16, re, im, scr, part > 0);
+        epilogue_chunk(et, mrow0, ti.n0 + c * 16, re, im, scr, part > 0 || d.kacc);
       }
       }
     }
@@ -601,7 +594,7 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
     if (!job_ok(d)) return fail(SBE_ERR_ARG, "tc_gemm: operand plane sets do not cover the launch");
     if (d.mode != mode || d.complex_mode != cplx || d.bn != bn)
       return fail(SBE_ERR_ARG, "tc_gemm: the jobs of a launch share one mode and N tile");
-    if ((mode == tc::MODE_HH || d.xonly || d.lolo) && (!d.complex_mode || d.kskip))
+    if ((mode == tc::MODE_HH || d.xonly) && (!d.complex_mode || d.kskip))
       return fail(SBE_ERR_ARG, "tc_gemm: hi*hi and cross-term modes are complex and unskipped only");
     if (d.kskip && d.ksplit > 1) return fail(SBE_ERR_ARG, "tc_gemm: band skip and split-K exclude");
     if (mode == tc::MODE_HH)
@@ -611,6 +604,9 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
     L.tile_base[j] = nt;
     if (d.kseq && (d.ksplit < 2 || jobs[j].e.kind != tc::EPI_RAWF))
       return fail(SBE_ERR_ARG, "tc_gemm: K parts in sequence need split-K and FP32 complex output");
+    if (d.kacc && (jobs[j].e.kind != tc::EPI_RAWF || (d.ksplit > 1 && !d.kseq)))
+      return fail(SBE_ERR_ARG, "tc_gemm: accumulating output needs FP32 complex output and one "
+                               "tile per output");
     nt += (long long)((d.N + bnt - 1) / bnt) * ((d.M + tc::BM - 1) / tc::BM) * d.batch *
           (d.ksplit > 1 && !d.kseq ? d.ksplit : 1);
   }

@@ -133,10 +133,6 @@ struct GemmDesc {
   // through xonly.
   int mode;
   int xonly;
-  // complex MODE_FULL: also the lo*lo products (hi*lo + lo*hi + lo*lo with xonly).  The
-  // lo*lo terms are 2^-22 of the product; W - W^H of dC, dD cancels most of W, so what
-  // W leaves out there shows in the result
-  int lolo;
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
   // written at out + ks * ks_stride (ksplit 0 counts as 1)
   int ksplit;
@@ -145,6 +141,9 @@ struct GemmDesc {
   // order into one output, ((p0 + p1) + p2) + ..., in FP32 (the first part stores,
   // each later part reads back what the same thread stored and adds to it)
   int kseq;
+  // EPI_RAWF: add every part (the first one too) to what the output already holds,
+  // e.g. the cross terms another launch wrote there before
+  int kacc;
   // N tile of MODE_FULL: 256 (0 = the default) or 128; with 128 a complex tile's
   // accumulators take 256 TMEM columns, so two tiles are in flight (the epilogue of
   // one overlaps the MMAs of the next) at twice the operand loads per output
