@@ -83,10 +83,10 @@ FLAGS = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, 
              LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel err"
 # dram__bytes_read.sum + dram__bytes_write.sum of the commutator launches of one RHS
-# evaluation (dP with the hi*lo + lo*hi + lo*lo products of W and V: 202.96 + 21.53 MB;
-# the hi*hi products of W and V in four K parts: 67.49 + 1.30 MB), 8 wires x Nk = 512
-# (ncu), per wire
-TRAFFIC_PER_EVAL_WIRE = (202.96e6 + 21.53e6 + 67.49e6 + 1.30e6) / 8
+# evaluation (dP with the hi*lo + lo*hi products of W and V: 200.64 + 22.40 MB; the
+# hi*hi products of W and V in four K parts added to those: 100.97 + 1.15 MB),
+# 8 wires x Nk = 512 (ncu), per wire
+TRAFFIC_PER_EVAL_WIRE = (200.64e6 + 22.40e6 + 100.97e6 + 1.15e6) / 8
 
 
 def wire_L(nk, kmax):
