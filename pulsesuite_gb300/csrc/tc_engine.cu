@@ -476,16 +476,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         float re[16], im[16];
         if (have && HH) {
-          // buffer columns [rr | ri | ir | -ii] (BNT each): re = rr + ii, im = ri + ir
-          float t0[16];
-          tmem_ld16(lane_addr + 0 * BNT + c * 16, re);
-          tmem_ld16(lane_addr + 3 * BNT + c * 16, t0);
+          // buffer columns [rr | ri | ir | -ii] (BNT each): re = rr + ii, im = ri + ir;
+          // the four loads under one wait
+          uint32_t a0[16], a1[16], a2[16], a3[16];
+          tmem_ld16_nw(lane_addr + 0 * BNT + c * 16, a0);
+          tmem_ld16_nw(lane_addr + 3 * BNT + c * 16, a3);
+          tmem_ld16_nw(lane_addr + 1 * BNT + c * 16, a1);
+          tmem_ld16_nw(lane_addr + 2 * BNT + c * 16, a2);
+          tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 16; ++j) re[j] -= t0[j];
-          tmem_ld16(lane_addr + 1 * BNT + c * 16, im);
-          tmem_ld16(lane_addr + 2 * BNT + c * 16, t0);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) im[j] += t0[j];
+          for (int j = 0; j < 16; ++j) {
+            re[j] = __uint_as_float(a0[j]) - __uint_as_float(a3[j]);
+            im[j] = __uint_as_float(a1[j]) + __uint_as_float(a2[j]);
+          }
         } else if (have) {
           tmem_ld16(lane_addr + c * 16, re);
           if (cplx) {
