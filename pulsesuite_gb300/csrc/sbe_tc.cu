@@ -1544,8 +1544,9 @@ int launch_jobs(const std::vector<tc::GemmJob>& jobs, cudaStream_t s) {
 // K range limited to the sheared band, un-sheared FP32 output.  Commutators (term
 // lists follow dpdt, SBEs.py:1942-1965; dCdt and dDdt, SBEs.py:2309-2327 and
 // 2607-2625, through their W - W^H form): dP, and the hi*lo + lo*hi products of W and
-// V (xonly); their hi*hi products as two K halves with one accumulator per real
-// product (MODE_HH: W - W^H is a small difference of large products near
+// V (xonly); their hi*hi products in K parts (hs) run in sequence per tile, with one
+// accumulator per real product, which the epilogue adds in order to the cross terms
+// (MODE_HH, kseq, kacc: W - W^H is a small difference of large products near
 // equilibrium).  Sources: [P; C; conj D] E.
 void bucket_jobs(SbeCtx* c, Mixed* m, int kind, std::vector<tc::GemmJob>& out) {
   MixedAll* A = all_of(c);

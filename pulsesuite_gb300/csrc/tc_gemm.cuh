@@ -126,11 +126,11 @@ struct GemmDesc {
   // (complex only) the hi*hi products are left out.  MODE_HH (complex only, B never
   // conjugated): the hi*hi products alone, N tile 128, one FP32 accumulator per real
   // product (rr, ri, ir, ii: one MMA of N = 256 per A plane over B's re and im
-  // tiles), summed in the epilogue; 512 TMEM columns, one tile in flight.  The tensor core's accumulation
-  // truncates at every MMA, so a product whose result is a small difference of
-  // large sums (the W - W^H form of dC, dD) takes its hi*hi part in MODE_HH with
-  // split-K (short truncating chains) and its hi*lo + lo*hi part, 2^-11 smaller,
-  // through xonly.
+  // tiles), combined in the epilogue; 512 TMEM columns, one tile in flight.  The
+  // tensor core's accumulation truncates at every MMA, so a product whose result is a
+  // small difference of large sums (the W - W^H form of dC, dD) takes its hi*hi part
+  // in MODE_HH with split-K (short truncating chains, kseq) and its hi*lo + lo*hi
+  // part, 2^-11 smaller, through xonly.
   int mode;
   int xonly;
   // split-K: the K blocks are cut into ksplit parts, each a separate output tile
