@@ -250,8 +250,8 @@ int sbe_graph_destroy(SbeGraph* g);
  * the JSON file cache_json (NULL: no cache) under a key of the device and the
  * context's (Nk, wires) buckets: a later call with a matching entry loads it and
  * times nothing.  Without a call every GEMM uses the 256 tile.  Synchronises the
- * device; not capturable.  A cache entry may also set "hh_split" (1-4; default 2
- * below Nk = 256, else 4): the K parts of the hi*hi products of the anti-Hermitian
+ * device; not capturable.  A cache entry may also set "hh_split" (1-8; default 2
+ * below Nk = 256, 4 below Nk = 1024, else 8): the K parts of the hi*hi products of the anti-Hermitian
  * W, V (shorter truncating FP32 chains: accuracy, not speed, so the tuner records
  * it but does not time it).
  * sbe_ctx_tiles: per bucket (ascending Nk) 6 ints (Nk, wires, exchange tile,

@@ -82,7 +82,7 @@ bool load(const char* path, const std::string& key, MixedAll* A) {
       // optional hi*hi split of this bucket (before the next bucket's entry)
       const size_t next = line.find(tag, pos + tag.size());
       const size_t hp = line.find(htag, pos);
-      int hs = nk >= 256 ? 4 : 2;   // the default of mixed_ensure
+      int hs = nk >= 1024 ? 8 : (nk >= 256 ? 4 : 2);   // the default of mixed_ensure
       if (hp != std::string::npos && (next == std::string::npos || hp < next) &&
           std::sscanf(line.c_str() + hp + htag.size(), "%d", &hs) != 1)
         return false;
@@ -93,7 +93,7 @@ bool load(const char* path, const std::string& key, MixedAll* A) {
     for (size_t i = 0; i < A->b.size(); ++i) {
       Mixed* m = A->b[i];
       const int* r = &v[6 * i];
-      if (r[0] != m->nk || r[1] != m->nw || r[5] < 1 || r[5] > 4) return false;
+      if (r[0] != m->nk || r[1] != m->nw || r[5] < 1 || r[5] > 8) return false;
       for (int j = 2; j < 5; ++j)
         if (r[j] != 128 && r[j] != 256) return false;
     }

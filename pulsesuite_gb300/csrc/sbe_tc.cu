@@ -459,9 +459,10 @@ static int mixed_ensure(SbeCtx* c, cudaStream_t s) {
     m->bv = W0.off_vec;
     m->br = W0.off_r;
     m->bkr = W0.off_kr;
-    // four K parts from Nk = 256 on: the hi*hi chains of long K ranges set the
-    // truncation error of W - W^H (the autotuner's cache may override)
-    m->hs = W0.nk >= 256 ? 4 : 2;
+    // K parts of 128 or fewer from Nk = 256 on (four, eight from Nk = 1024): the
+    // hi*hi chains of long K ranges set the truncation error of W - W^H (the
+    // autotuner's cache may override)
+    m->hs = W0.nk >= 1024 ? 8 : (W0.nk >= 256 ? 4 : 2);
     A->b.push_back(m);
     i = j;
   }
