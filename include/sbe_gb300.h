@@ -103,7 +103,10 @@ int sbe_dCdt(int nk, const double* C, const double* D, const double* P, const do
 /* SBEs.py:2502 dDdt.                                                           */
 int sbe_dDdt(int nk, const double* C, const double* D, const double* P, const double* Heh,
              const double* Hee, const double* Hhh, double* out, void* stream);
-/* SBEs.py:658 CalcH (VC is Nk*Nk*3 real, [k1][k2][n]; only VC[q][0][n] is read). */
+/* SBEs.py:658 CalcH (VC is Nk*Nk*3 real, [k1][k2][n]; only VC[q][0][n] is read).
+ * Having no context, it takes its scratch (3 Nk doubles, 4 Nk complex) from the
+ * device's stream-ordered pool (cudaMallocAsync / cudaFreeAsync on stream: no host
+ * synchronisation); the batched context path builds H with no allocation.      */
 int sbe_calch(int nk, const double* Meh, const double* Wee, const double* Whh, const double* C,
               const double* D, const double* P, const double* VC, const double* Ee,
               const double* Eh, double gap, int excitons, int lf, int freepot, double* Heh,
