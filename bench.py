@@ -83,10 +83,10 @@ FLAGS = dict(Optics=True, Excitons=True, EHs=False, Screened=True, Phonon=True, 
              LF=True, FreePot=False, DiagDph=True, OffDiagDph=True, Recomb=False)
 METRIC = "SBE wire-steps/s: batched mixed-prec vs plain FP64 GPU at ≤1e-6 rel err"
 # dram__bytes_read.sum + dram__bytes_write.sum of the commutator launches of one RHS
-# evaluation (dP with the hi*lo + lo*hi products of W and V: 200.64 + 22.40 MB; the
-# hi*hi products of W and V in four K parts added to those: 100.97 + 1.15 MB),
-# 8 wires x Nk = 512 (ncu), per wire
-TRAFFIC_PER_EVAL_WIRE = (200.64e6 + 22.40e6 + 100.97e6 + 1.15e6) / 8
+# evaluation (dP with the hi*lo + lo*hi products of W and V: 1070.4 + 171.8 MB; the
+# hi*hi products of W and V in four K parts added to those: 404.6 + 100.0 MB),
+# 32 wires x Nk = 512 (ncu, one timed coupled step), per wire
+TRAFFIC_PER_EVAL_WIRE = (1070.4e6 + 171.8e6 + 404.6e6 + 100.0e6) / 32
 
 
 def wire_L(nk, kmax):
@@ -413,8 +413,10 @@ def gpu_arm(args, wl):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
+    torch.cuda.nvtx.range_push("timed_steps")   # ncu --nvtx-include timed_steps/
     for _ in range(args.steps):
         line.step(*st, dt, prec)
+    torch.cuda.nvtx.range_pop()
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -533,8 +535,9 @@ def gpu_arm(args, wl):
             "traffic": TRAFFIC_PER_EVAL_WIRE * nw,
             "traffic_note": "DRAM read+write bytes of the commutator launches of one RHS "
                             "evaluation: dram__bytes_read.sum + dram__bytes_write.sum of an ncu "
-                            "capture of the 8-wire case (profiles/k_tc_gemm_multiwire_nk512.md), "
-                            "scaled by wires; a constant of this file, refreshed with the profile",
+                            "capture of one timed step of the 32-wire case "
+                            "(profiles/coupled_step_dram_multiwire_nk512.md), scaled by wires; "
+                            "a constant of this file, refreshed with the profile",
             "flops_model": "algorithmic 96*Nk^3 per wire per RHS evaluation (dpdt/dCdt/dDdt as "
                            "12 complex Nk^3 products) over the summed CUDA-event time of the "
                            "evaluation's two commutator launches (dP with the hi*lo + lo*hi "
@@ -648,9 +651,11 @@ def sweep_arm(args):
         dist.barrier()
     torch.cuda.synchronize()
     ev0.record()
+    torch.cuda.nvtx.range_push("timed_steps")   # ncu --nvtx-include timed_steps/
     for n in range(args.warmup, nsteps):
         ctx.local_field(e0_dev[n], de_dev[n], 1, Ek0, dEk)
         ctx.rk4_step(P, C, D, Ek0, dEk, dt, src, prec)
+    torch.cuda.nvtx.range_pop()
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -914,8 +919,10 @@ def grid3_arm(args):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
+    torch.cuda.nvtx.range_push("timed_steps")   # ncu --nvtx-include timed_steps/
     for _ in range(args.steps):
         line.step(*st, dt, prec)
+    torch.cuda.nvtx.range_pop()
     ev1.record()
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
