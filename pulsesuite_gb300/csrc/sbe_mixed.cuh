@@ -18,8 +18,8 @@ struct Mixed {
   // sbe_autotune
   int bn[4] = {0, 0, 0, 0};
   // K parts of the hi*hi products of W and V (split-K: shorter truncating FP32
-  // chains; the parts are summed in order by the GEMM epilogue); 1 to 4, by default 2
-  // below Nk = 256 and 4 from there on
+  // chains; the parts are summed in order by the GEMM epilogue); 1 to 8, by default 2
+  // below Nk = 256, 4 below Nk = 1024 and 8 from there on
   int hs = 2;
   tc::PlaneSet pl{}, tp{}, sp{}, ep{};   // commutator, Toeplitz, sheared, E^T planes
   float* xsh = nullptr;    // exchange sums, un-sheared: 3 x Nw x Nk x Nk complex (FP32)
