@@ -267,14 +267,16 @@ __global__ void k_couple_eval(const WireDev* wires, int nx, const double* xg, co
 }
 
 // FFTG as k_couple_fftg in FP32 with compensated (Kahan) sums, for the
-// mixed-precision step (its field operands are FP32 values).
+// mixed-precision step (its field operands are FP32 values).  The sampled fields are
+// real, so Ek[Nr - q] = conj(Ek[q]): the warps sum q = 0 .. Nr / 2 (Nr = 2 Nk + 2 is
+// even) and store both.
 __global__ void __launch_bounds__(256) k_couple_fftg_f(const WireDev* wires, const float2* twr,
                                                        const float* wv, double2* Ek) {
   const int w = blockIdx.y;
   const WireDev W = wires[w];
   const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (q >= W.nr) return;
+  if (2 * q > W.nr) return;
   const int nr = W.nr;
   const float2* tw = twr + W.off_r;
   const float* v0 = wv + 3 * W.off_r;
@@ -302,9 +304,12 @@ __global__ void __launch_bounds__(256) k_couple_fftg_f(const WireDev* wires, con
     for (int o = 16; o > 0; o >>= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
   }
   if (lane == 0)
-    for (int f = 0; f < 3; ++f)
-      Ek[3 * W.off_r + (long long)f * nr + q] =
-          make_double2(-f32_to_f64(s[2 * f]) / nr, -f32_to_f64(s[2 * f + 1]) / nr);
+    for (int f = 0; f < 3; ++f) {
+      const double re = -f32_to_f64(s[2 * f]) / nr, im = -f32_to_f64(s[2 * f + 1]) / nr;
+      double2* e = Ek + 3 * W.off_r + (long long)f * nr;
+      e[q] = make_double2(re, im);
+      if (q > 0 && 2 * q < nr) e[nr - q] = make_double2(re, -im);
+    }
 }
 
 // FFTG of the three sampled fields of every wire: Ek[q] = -(1/Nr) sum_j v_j e^{-2 pi i q j/Nr}.
@@ -345,29 +350,54 @@ __global__ void __launch_bounds__(256) k_couple_fftg(const WireDev* wires, const
 
 // Wire sources -> grid: spline of each wire's (Px, Py, Pz, re, rh) at x_j - x_w,
 // summed over the wires; rho = sum_w (rh_w - re_w).
-__global__ void k_couple_deposit(const WireDev* wires, int nw, int nx, const double* xg,
-                                 const double* wx, const double* r, const double2* src,
-                                 const double2* wcoef, double2* Pg, double2* rho) {
+// The wires' positions and grid ends are staged in shared memory DEP_CHUNK wires at a
+// time, so that the test of a wire against the grid point costs no global load; the
+// wires are added in index order as before.
+constexpr int DEP_CHUNK = 256;
+
+__global__ void __launch_bounds__(64) k_couple_deposit(const WireDev* wires, int nw, int nx,
+                                                       const double* xg, const double* wx,
+                                                       const double* r, const double2* src,
+                                                       const double2* wcoef, double2* Pg,
+                                                       double2* rho) {
+  __shared__ double s_wx[DEP_CHUNK], s_r0[DEP_CHUNK], s_r1[DEP_CHUNK];
+  __shared__ long long s_off[DEP_CHUNK];
+  __shared__ int s_nr[DEP_CHUNK];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nx) return;
+  const bool in = j < nx;
   double2 P[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
   double2 rh = make_double2(0, 0);
-  const double xj = xg[j];
-  for (int w = 0; w < nw; ++w) {
-    const WireDev& W = wires[w];
-    const double* rw = r + W.off_r;
-    const double u = xj - wx[w];
-    if (!(u >= rw[0] && u <= rw[W.nr - 1])) continue;
-    const int i = locate_sorted(rw, W.nr, u);
-    const double dx = u - rw[i];
-    const double2* y = src + 5 * W.off_r;
-    const double2* cf = wcoef + 15 * W.off_r;
-    double2 v[5];
-    for (int c = 0; c < 5; ++c)
-      v[c] = spl_eval(y + (long long)c * W.nr, cf + 3LL * c * W.nr, W.nr, i, dx);
-    for (int c = 0; c < 3; ++c) P[c] = cadd(P[c], v[c]);
-    rh = cadd(rh, csub(v[4], v[3]));
+  const double xj = in ? xg[j] : 0.0;
+  for (int w0 = 0; w0 < nw; w0 += DEP_CHUNK) {
+    const int nc = min(DEP_CHUNK, nw - w0);
+    __syncthreads();   // the previous chunk is no longer read
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      const WireDev& W = wires[w0 + i];
+      s_wx[i] = wx[w0 + i];
+      s_r0[i] = r[W.off_r];
+      s_r1[i] = r[W.off_r + W.nr - 1];
+      s_off[i] = W.off_r;
+      s_nr[i] = W.nr;
+    }
+    __syncthreads();
+    if (!in) continue;
+    for (int k = 0; k < nc; ++k) {
+      const double u = xj - s_wx[k];
+      if (!(u >= s_r0[k] && u <= s_r1[k])) continue;
+      const long long off = s_off[k];
+      const int nr = s_nr[k];
+      const double* rw = r + off;
+      const int i = locate_sorted(rw, nr, u);
+      const double dx = u - rw[i];
+      const double2* y = src + 5 * off;
+      const double2* cf = wcoef + 15 * off;
+      double2 v[5];
+      for (int c = 0; c < 5; ++c) v[c] = spl_eval(y + (long long)c * nr, cf + 3LL * c * nr, nr, i, dx);
+      for (int c = 0; c < 3; ++c) P[c] = cadd(P[c], v[c]);
+      rh = cadd(rh, csub(v[4], v[3]));
+    }
   }
+  if (!in) return;
   for (int c = 0; c < 3; ++c) Pg[(long long)c * nx + j] = P[c];
   rho[j] = rh;
 }
@@ -610,8 +640,8 @@ int couple_sample(SbeCouple* cp, const double2* Ex, const double2* E, int precis
   k_couple_eval<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(
       c->d_wires, nx, cp->p->x, cp->g_y, cp->g_coef, cp->wx, c->r, c->window, cp->wv, cp->wvf);
   if (precision == SBE_PREC_MIXED)
-    k_couple_fftg_f<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
-                                                                     cp->wvf, cp->Ek);
+    k_couple_fftg_f<<<dim3((c->nr_max / 2 + 8) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
+                                                                         cp->wvf, cp->Ek);
   else
     k_couple_fftg<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twr, cp->wv,
                                                                    cp->Ek);
@@ -622,8 +652,8 @@ int couple_deposit(SbeCouple* cp, cudaStream_t s) {
   SbeCtx* c = cp->ctx;
   const int nx = cp->p->nx;
   run_splines(wire_batch(cp), cp->nprob_w, c->nr_max, s);
-  k_couple_deposit<<<(nx + 127) / 128, 128, 0, s>>>(c->d_wires, c->nw, nx, cp->p->x, cp->wx,
-                                                     c->r, cp->src, cp->w_coef, cp->Pg, cp->rho);
+  k_couple_deposit<<<(nx + 63) / 64, 64, 0, s>>>(c->d_wires, c->nw, nx, cp->p->x, cp->wx, c->r,
+                                                   cp->src, cp->w_coef, cp->Pg, cp->rho);
   return cuda_check(cudaGetLastError(), "couple deposit");
 }
 
@@ -916,8 +946,8 @@ int c3_sample(SbeCouple3* cp, const double2* E, int precision, cudaStream_t s) {
   k_c3_eval<<<dim3((c->nr_max + 127) / 128, c->nw), 128, 0, s>>>(
       c->d_wires, nz, p->x[2], cp->lines, cp->l_coef, c->r, c->window, cp->wv, cp->wvf);
   if (precision == SBE_PREC_MIXED)
-    k_couple_fftg_f<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
-                                                                     cp->wvf, cp->Ek);
+    k_couple_fftg_f<<<dim3((c->nr_max / 2 + 8) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twrf,
+                                                                         cp->wvf, cp->Ek);
   else
     k_couple_fftg<<<dim3((c->nr_max + 7) / 8, c->nw), 256, 0, s>>>(c->d_wires, cp->twr, cp->wv,
                                                                    cp->Ek);
