@@ -126,6 +126,37 @@ def env():
     return rank, world, local
 
 
+def dist_init(world, backend=None):
+    """Process group of a torchrun launch (one rank per GPU, each stepping its own
+    replica of the wire batch): NCCL where the ranks have GPUs, gloo where they have
+    none or where backend says so (the CPU test of this logic).  None for a single
+    process."""
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group(backend or ("nccl" if torch.cuda.is_available() else "gloo"))
+    return dist
+
+
+def max_over_ranks(dist, ms):
+    """The job's time: the largest of the ranks' times, returned on every rank."""
+    if dist is None:
+        return ms
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, nw, steps, ms):
+    """Whole-job wire-steps/s: each of the world ranks steps nw wires (weak scaling)
+    steps times in ms milliseconds (the slowest rank's time)."""
+    return world * nw * steps / (ms / 1e3)
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (the oracle restatement) -------------------------------------------
 
@@ -348,10 +379,7 @@ def gpu_arm(args, wl):
     import torch
     import __graft_entry__ as ge
     rank, world, local = env()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = dist_init(world)
     torch.cuda.set_device(local)
     ge.build()
     from pulsesuite_gb300 import _lib
@@ -422,16 +450,14 @@ def gpu_arm(args, wl):
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(dist, ms)
         dist.barrier()
     prof = {cat: ctx.profile_read(cat) for cat in range(4)}
     ctx.profile(False)
     ctx.check()
     # the FP64 conservation check of the last timed step (read after the timed region)
     charge_imb = ctx.charge_imbalance()
-    value = world * nw * args.steps / (ms / 1e3)
+    value = job_rate(world, nw, args.steps, ms)
 
     # CUDA graph of the same coupled step (launch count, replay time)
     graph = line.graph(*st, dt, prec)
@@ -479,8 +505,8 @@ def gpu_arm(args, wl):
         h_out[3].copy_(rho, non_blocking=True)
     e1.record()
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    e2e_val = world * nw * args.steps / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(dist, e0.elapsed_time(e1))
+    e2e_val = job_rate(world, nw, args.steps, e2e_ms)
 
     # RHS error of the mixed path against the FP64 path at the current state
     P, C, D = st[0], st[1], st[2]
@@ -504,8 +530,8 @@ def gpu_arm(args, wl):
             line.step(*st64, dt, _lib.PREC_FP64)
         f1e.record()
         torch.cuda.synchronize()
-        fp64_ms = f0e.elapsed_time(f1e) / n64
-        fp64_val = world * nw / (fp64_ms / 1e3)
+        fp64_ms = max_over_ranks(dist, f0e.elapsed_time(f1e) / n64)
+        fp64_val = job_rate(world, nw, 1, fp64_ms)
 
     if rank != 0:
         if dist:
@@ -596,10 +622,7 @@ def sweep_arm(args):
     import torch
     import __graft_entry__ as ge
     rank, world, local = env()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = dist_init(world)
     torch.cuda.set_device(local)
     ge.build()
     from pulsesuite_gb300 import _lib
@@ -675,10 +698,8 @@ def sweep_arm(args):
     torch.cuda.synchronize()
     graph_ms = g0.elapsed_time(g1) / args.steps
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * nw * args.steps / (ms / 1e3)
+        ms = max_over_ranks(dist, ms)
+    value = job_rate(world, nw, args.steps, ms)
 
     # end to end: the step's field amplitudes from pinned host memory, the wires'
     # real-space sources (Px, Py, Pz, re, rh) back to pinned host memory every step
@@ -699,7 +720,7 @@ def sweep_arm(args):
         h_src.copy_(src, non_blocking=True)
     e1e.record()
     torch.cuda.synchronize()
-    e2e_ms = e0e.elapsed_time(e1e)
+    e2e_ms = max_over_ranks(dist, e0e.elapsed_time(e1e))
     graph.close()
 
     # RHS error against FP64 at the current state (every wire)
@@ -730,8 +751,8 @@ def sweep_arm(args):
             ctx.rk4_step(*st64, Ek0, dEk, dt, s64, _lib.PREC_FP64)
         f1.record()
         torch.cuda.synchronize()
-        fp64_ms = f0.elapsed_time(f1) / n64
-        fp64_val = world * nw / (fp64_ms / 1e3)
+        fp64_ms = max_over_ranks(dist, f0.elapsed_time(f1) / n64)
+        fp64_val = job_rate(world, nw, 1, fp64_ms)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -755,7 +776,7 @@ def sweep_arm(args):
                 "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
                 "data": "synthetic", "config": sweep_config(), "precision": args.precision,
                 "clocks": clk,
-                "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
+                "e2e": {"value": job_rate(world, nw, args.steps, e2e_ms), "unit": "wire-steps/s",
                         "h2d_bytes_per_step": int(2 * 8 * nw),
                         "d2h_bytes_per_step": int(src.numel() * 16)},
                 "gpu_launches": int((n_kernels + 1) * args.steps),
@@ -844,10 +865,7 @@ def grid3_arm(args):
         grid3_field_arm(args)
         return
     rank, world, local = env()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = dist_init(world)
     torch.cuda.set_device(local)
     ge.build()
     from pulsesuite_gb300 import _lib
@@ -931,10 +949,8 @@ def grid3_arm(args):
     ctx.profile(False)
     ctx.check()
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * nw * args.steps / (ms / 1e3)
+        ms = max_over_ranks(dist, ms)
+    value = job_rate(world, nw, args.steps, ms)
     graph = line.graph(*st, dt, prec)
     n_kernels = graph.kernels
     g0 = torch.cuda.Event(enable_timing=True)
@@ -962,7 +978,7 @@ def grid3_arm(args):
         h_J.copy_(Jv, non_blocking=True)
     e1e.record()
     torch.cuda.synchronize()
-    e2e_ms = e0e.elapsed_time(e1e)
+    e2e_ms = max_over_ranks(dist, e0e.elapsed_time(e1e))
 
     # the field step alone (H and E updates with the wires' current), its HBM roofline
     Et, Ht = st[3].clone(), st[4].clone()
@@ -997,8 +1013,8 @@ def grid3_arm(args):
         line.step(*st64, dt, _lib.PREC_FP64)
         f1.record()
         torch.cuda.synchronize()
-        fp64_ms = f0.elapsed_time(f1)
-        fp64_val = world * nw / (fp64_ms / 1e3)
+        fp64_ms = max_over_ranks(dist, f0.elapsed_time(f1))
+        fp64_val = job_rate(world, nw, 1, fp64_ms)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -1017,7 +1033,7 @@ def grid3_arm(args):
                 "dtype": "fp16x3-f32acc/f64" if prec == _lib.PREC_MIXED else "f64",
                 "data": "synthetic", "config": grid3_config(), "precision": args.precision,
                 "clocks": clk,
-                "e2e": {"value": world * nw * args.steps / (e2e_ms / 1e3), "unit": "wire-steps/s",
+                "e2e": {"value": job_rate(world, nw, args.steps, e2e_ms), "unit": "wire-steps/s",
                         "h2d_bytes_per_step": int(3 * N * 16), "d2h_bytes_per_step": int(3 * N * 16)},
                 "gpu_launches": int(n_kernels * args.steps), "gpu_launches_per_step": int(n_kernels),
                 "graph_replay_ms_per_step": graph_ms,
