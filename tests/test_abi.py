@@ -64,3 +64,47 @@ def test_new_entry_points_check_arguments_without_gpu(lib_path):
     n = ctypes.c_longlong(-1)
     assert lib.sbe_backup_format(None, 0, None, 0, ctypes.byref(n), 0) == 0 and n.value == 0
     assert lib.sbe_backup_parse(None, 0, None, 0, 0) == 0
+
+
+def _declared_params():
+    """name -> parameter kinds of every declaration in the header ('ptr', 'double',
+    'i64', 'int'), comments removed; a (void) list is empty."""
+    with open(os.path.join(ROOT, "include", "sbe_gb300.h")) as f:
+        src = re.sub(r"/\*.*?\*/", " ", f.read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*(?:const char\*|int)\s+(sbe_\w+)\s*\(([^;]*?)\)\s*;", src, re.M | re.S):
+        params = [p.strip() for p in m.group(2).split(",")]
+        if params == ["void"] or params == [""]:
+            params = []
+        kinds = []
+        for p in params:
+            if "*" in p:
+                kinds.append("ptr")
+            elif "double" in p:
+                kinds.append("double")
+            elif "long long" in p:
+                kinds.append("i64")
+            elif "int" in p:
+                kinds.append("int")
+            else:
+                raise AssertionError(f"unclassified parameter {p!r} of {m.group(1)}")
+        out[m.group(1)] = kinds
+    return out
+
+
+def test_binding_signatures_match_header(lib_path):
+    """Every ctypes signature in the binding has the header's parameter count and kinds
+    (pointer, double, 64-bit or 32-bit integer): a drift between the two would pass
+    arguments in the wrong registers."""
+    from pulsesuite_gb300 import _lib
+    lib = _lib.load(lib_path)
+    kind = {ctypes.c_void_p: "ptr", ctypes.c_char_p: "ptr", ctypes.c_double: "double",
+            ctypes.c_longlong: "i64", ctypes.c_int: "int"}
+    decl = _declared_params()
+    assert sorted(decl) == _declared()
+    for name, params in decl.items():
+        f = getattr(lib, name)
+        if f.argtypes is None:
+            assert params == [], f"{name}: no binding signature for {len(params)} parameters"
+            continue
+        assert [kind[t] for t in f.argtypes] == params, name
