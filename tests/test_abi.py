@@ -108,3 +108,39 @@ def test_binding_signatures_match_header(lib_path):
             assert params == [], f"{name}: no binding signature for {len(params)} parameters"
             continue
         assert [kind[t] for t in f.argtypes] == params, name
+
+
+def test_descriptor_structs_match_the_header(tmp_path):
+    """The ctypes descriptor structures have the C structs' size and field offsets
+    (gcc compiles offsetof() of every field against the header)."""
+    import shutil
+    import subprocess
+    from pulsesuite_gb300 import _lib
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    structs = [_lib.SbeWireDesc, _lib.SbePstdDesc, _lib.SbePstd3Desc, _lib.SbeCoupleDesc,
+               _lib.SbeCouple3Desc]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "sbe_gb300.h"',
+             'int main(void) {']
+    for st in structs:
+        n = st.__name__
+        lines.append(f'  printf("{n} size %zu\\n", sizeof({n}));')
+        for fname, _ in st._fields_:
+            lines.append(f'  printf("{n} {fname} %zu\\n", offsetof({n}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n"):
+        if ln.strip():
+            a, b, c = ln.split()
+            got[(a, b)] = int(c)
+    for st in structs:
+        n = st.__name__
+        assert got[(n, "size")] == ctypes.sizeof(st), n
+        for fname, _ in st._fields_:
+            assert got[(n, fname)] == getattr(st, fname).offset, f"{n}.{fname}"
