@@ -348,22 +348,31 @@ class ClockSampler:
         except Exception:
             self.p.kill()
         self.f.close()
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in open(self.path):
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax = float(parts[2])
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        with open(self.path) as f:
+            return clock_summary(f)
+
+
+def clock_summary(lines):
+    """Median SM clock, maximum clock and the throttle reasons seen in nvidia-smi samples
+    (csv, noheader, nounits: index, clocks.sm, clocks.max.sm, power.draw, active mask,
+    then hw_slowdown, hw_thermal_slowdown, sw_thermal_slowdown, sw_power_cap as
+    "Active" / "Not Active"); lines that are not samples are skipped."""
+    sm, smax, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        parts = [x.strip() for x in ln.split(",")]
+        if len(parts) < 9:
+            continue
+        try:
+            sm.append(float(parts[1]))
+            smax = float(parts[2])
+        except ValueError:
+            continue
+        for nm, v in zip(names, parts[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(nm)
+    return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+            "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def measured_peaks():
