@@ -440,6 +440,11 @@ int sbe_ctx_charge(SbeCtx* ctx, double* out, void* stream);
 /* Waits for the stream, then reports whether a bounded wait of the tensor-core
  * engine gave up since the last check (SBE_ERR_TIMEOUT; the flags are cleared). */
 int sbe_ctx_check(SbeCtx* ctx, void* stream);
+/* Self-test of that path: one launch waits, with the engine's bounded wait, on a
+ * barrier nothing completes; the wait gives up after ~2 s and raises the flag that
+ * the next sbe_ctx_check reports.  *gave_up = 1 when it did.  Needs the context's
+ * mixed-precision workspace (any mixed call creates it); waits for the stream.  */
+int sbe_wait_selftest(SbeCtx* ctx, int* gave_up, void* stream);
 
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Diagnostic entry, no counterpart in the reference: out[b] = op(A[b]) op(B[b])

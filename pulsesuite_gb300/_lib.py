@@ -31,7 +31,7 @@ EXPORTS = (
     "sbe_prop2qw", "sbe_qw2prop", "sbe_leapfrog_step", "sbe_rk4_step", "sbe_rhs",
     "sbe_tc_selftest", "sbe_rk4_graph_create", "sbe_graph_launch", "sbe_graph_destroy",
     "sbe_ctx_profile", "sbe_ctx_profile_read", "sbe_prop2qw_noalloc", "sbe_ctx_check",
-    "sbe_ctx_charge",
+    "sbe_ctx_charge", "sbe_wait_selftest",
     "sbe_convert_selftest", "sbe_deph_selftest",
     "sbe_pstd_create", "sbe_pstd_destroy", "sbe_pstd_grid", "sbe_pstd_deriv", "sbe_pstd_update_h",
     "sbe_pstd_update_e", "sbe_pstd_step", "sbe_pstd_elong", "sbe_couple_create",
@@ -142,6 +142,7 @@ def load(path=LIB_PATH):
         "sbe_ctx_profile": [P, I],
         "sbe_ctx_profile_read": [P, I, P, P],
         "sbe_ctx_check": [P, P],
+        "sbe_wait_selftest": [P, P, P],
         "sbe_ctx_charge": [P, P, P],
         "sbe_convert_selftest": [P, P, ctypes.c_longlong, P, P, P],
         "sbe_deph_selftest": [P, P, P, I, P, P, P],

@@ -1949,6 +1949,27 @@ extern "C" int sbe_ctx_check(SbeCtx* c, void* stream) {
   return SBE_OK;
 }
 
+extern "C" int sbe_wait_selftest(SbeCtx* c, int* gave_up, void* stream) {
+  if (!c || !gave_up) return fail(SBE_ERR_ARG, "sbe_wait_selftest: null argument");
+  MixedAll* A = all_of(c);
+  if (!A)
+    return fail(SBE_ERR_ARG, "sbe_wait_selftest: no mixed-precision workspace yet (make a "
+                             "mixed-precision call first)");
+  cudaStream_t s = as_stream(stream);
+  int* d = nullptr;
+  if (cudaMallocAsync(&d, sizeof(int), s) != cudaSuccess)
+    return fail(SBE_ERR_OOM, "sbe_wait_selftest: scratch allocation failed");
+  int rc = tc_wait_selftest(A->err, d, s);
+  int h = 0;
+  if (!rc)
+    rc = cuda_check(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s),
+                    "sbe_wait_selftest: read result");
+  cudaFreeAsync(d, s);
+  if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "sbe_wait_selftest");
+  *gave_up = h;
+  return rc;
+}
+
 extern "C" int sbe_tc_selftest(int nk, int nbatch, const double* A, const double* B, int opA,
                                int opB, int complex_mode, double* out, void* stream) {
   if (nk < 8 || nk % 8 || nbatch < 1 || !A || !B || !out || opA < 0 || opA > 3 || opB < 0 ||

@@ -628,6 +628,29 @@ int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s) {
   return cuda_check(cudaGetLastError(), "tc_gemm launch");
 }
 
+namespace tc {
+// Self-test of the bounded wait: thread 0 waits, through mbar_wait, for phase 0 of a
+// fresh barrier that nothing arrives on.  The wait gives up after its cycle limit
+// (~2 s), sets *err and returns false; *gave_up records that.
+__global__ void k_wait_selftest(int* err, int* gave_up) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    *gave_up = mbar_wait(&bar, 0u, err, reinterpret_cast<volatile int*>(&abort_flag)) ? 0 : 1;
+}
+}  // namespace tc
+
+int tc_wait_selftest(int* err, int* gave_up, cudaStream_t s) {
+  tc::k_wait_selftest<<<1, 32, 0, s>>>(err, gave_up);
+  return cuda_check(cudaGetLastError(), "tc_wait_selftest launch");
+}
+
 int tc_gemm_launch(const tc::GemmDesc& d, const tc::EpiArgs& e, cudaStream_t s) {
   tc::GemmJob j{d, e};
   return tc_gemm_launch(&j, 1, s);

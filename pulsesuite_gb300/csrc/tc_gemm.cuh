@@ -171,6 +171,8 @@ static_assert(sizeof(GemmLaunch) <= 32000, "kernel parameter space (32 KB) excee
 // Host API of the engine.
 int tc_gemm_launch(const tc::GemmJob* jobs, int njobs, cudaStream_t s);
 int tc_gemm_launch(const tc::GemmDesc& d, const tc::EpiArgs& e, cudaStream_t s);
+// One launch whose bounded wait gives up (~2 s): raises *err, *gave_up = 1.
+int tc_wait_selftest(int* err, int* gave_up, cudaStream_t s);
 int tc_gemm_init();
 
 }  // namespace sbe

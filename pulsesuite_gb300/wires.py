@@ -364,6 +364,14 @@ class WireContext:
         """Wait for the current stream and raise if a device-side bounded wait gave up."""
         _lib.check(self.lib.sbe_ctx_check(self.handle, _lib.stream_handle()), "sbe_ctx_check")
 
+    def wait_selftest(self):
+        """Make one bounded wait give up (~2 s) on a barrier nothing completes; True if
+        it did.  The next check() then raises; the context stays usable."""
+        g = ctypes.c_int(0)
+        _lib.check(self.lib.sbe_wait_selftest(self.handle, ctypes.byref(g), _lib.stream_handle()),
+                   "sbe_wait_selftest")
+        return g.value == 1
+
     def charge(self):
         """(n_wires, 2) carrier numbers sum |C_kk|, sum |D_kk| that the charge
         normalisation of the last step found (FP64, before it rescaled them)."""

@@ -81,6 +81,34 @@ def test_mixed_rhs_vs_fp64(nk):
             assert e < 1e-6, (nk, n, w, e)
 
 
+# Written without a GPU run to validate it: off unless SBE_WAIT_SELFTEST=1 is set.
+@pytest.mark.skipif(__import__("os").environ.get("SBE_WAIT_SELFTEST") != "1",
+                    reason="bounded-wait self-test: run with SBE_WAIT_SELFTEST=1 (about 2 s)")
+def test_bounded_wait_gives_up_and_context_stays_usable():
+    """A bounded device wait that nothing satisfies gives up (no hang, no fault), the
+    next check reports SBE_ERR_TIMEOUT once, and the context then computes as before."""
+    from pulsesuite_gb300 import _lib
+    nk, nw = 64, 2
+    ctx, _ = make_ctx(nk, nw)
+    rng = np.random.default_rng(5)
+    st = [seeded(rng, nk) for _ in range(nw)]
+    P = ctx.pack([s[0] for s in st])
+    C = ctx.pack([s[1] for s in st])
+    D = ctx.pack([s[2] for s in st])
+    Ek = fields(ctx, [1e7, 2e7])
+    before = ctx.rhs(P, C, D, Ek, _lib.PREC_MIXED)
+    ctx.check()
+    assert ctx.wait_selftest()
+    with pytest.raises(_lib.SbeError) as e:
+        ctx.check()
+    assert "(code 5)" in str(e.value)   # SBE_ERR_TIMEOUT
+    ctx.check()                # the flag was cleared
+    after = ctx.rhs(P, C, D, Ek, _lib.PREC_MIXED)
+    ctx.check()
+    for a, b in zip(after, before):
+        assert torch.equal(a, b)
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_graph_replay_matches_direct_step(prec):
     """A captured RK4 step replays to the same state as the direct call."""
